@@ -1,0 +1,269 @@
+"""ctypes front end of the oracle -- TEST INFRASTRUCTURE ONLY.
+
+Loads ``oracle/liborc.so`` (the CPU restatement in mgx_oracle.cpp) and, when
+present, ``oracle/_ref/libmgref.so`` (the reference MGmol's own hot-path
+translation units compiled against single-task shims by build_ref.sh).
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use it.
+
+All arrays are numpy, orbital-major (nfunc, nx*ny*nz), points x-slowest /
+z-fastest, which is the ghost-free BlockVector layout of src/BlockVector.h.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+_ORC = None
+_REF = None
+
+_dp = ctypes.POINTER(ctypes.c_double)
+_fp = ctypes.POINTER(ctypes.c_float)
+_ip = ctypes.POINTER(ctypes.c_int)
+
+
+def build():
+    """Compile liborc.so (quick, plain make)."""
+    subprocess.run(["make", "-s", "-C", HERE], check=True)
+
+
+def lib():
+    global _ORC
+    if _ORC is None:
+        path = os.path.join(HERE, "liborc.so")
+        if not os.path.exists(path):
+            build()
+        _ORC = ctypes.CDLL(path)
+        _ORC.orc_set_gamma.restype = ctypes.c_double
+        _ORC.orc_jacobi_factor.restype = ctypes.c_double
+        _ORC.orc_trace_prod.restype = ctypes.c_double
+    return _ORC
+
+
+def ref_lib():
+    """The reference's own code (None when it was not built here)."""
+    global _REF
+    if _REF is None:
+        path = os.path.join(HERE, "_ref", "libmgref.so")
+        if not os.path.exists(path):
+            return None
+        _REF = ctypes.CDLL(path)
+    return _REF
+
+
+def _p(a):
+    a = np.ascontiguousarray(a)
+    if a.dtype == np.float64:
+        return a.ctypes.data_as(_dp)
+    if a.dtype == np.float32:
+        return a.ctypes.data_as(_fp)
+    if a.dtype == np.int32:
+        return a.ctypes.data_as(_ip)
+    raise TypeError(a.dtype)
+
+
+def _grid(n, ll):
+    return (ctypes.c_int * 3)(*n), (ctypes.c_double * 3)(*ll)
+
+
+def _sfx(a):
+    return "d" if a.dtype == np.float64 else "f"
+
+
+def _call(L, name, *args):
+    rc = getattr(L, name)(*args)
+    if rc != 0:
+        raise RuntimeError(f"{name} returned {rc}")
+
+
+# The reference's batched FDkernelDel2_6th / FDkernelDel2_8th initialise the
+# x offset once outside the function loop (src/pb/FDkernels.cc:298,341 and
+# :391,442), so for nfunc > 1 every function after the first is addressed
+# dim0 planes too far.  The reference is therefore called one function at a
+# time for lap types 3 and 4; the oracle implements the per-function operator.
+_PER_FUNCTION = (3, 4)
+
+
+def fd_apply(n, ll, lap_type, u, ref=False):
+    if ref and lap_type in _PER_FUNCTION and np.asarray(u).shape[0] > 1:
+        return np.concatenate([fd_apply(n, ll, lap_type, u[i:i + 1], ref=True)
+                               for i in range(u.shape[0])])
+    L = ref_lib() if ref else lib()
+    pre = "ref" if ref else "orc"
+    u = np.ascontiguousarray(u)
+    out = np.zeros_like(u)
+    gn, gl = _grid(n, ll)
+    _call(L, f"{pre}_fd_apply_{_sfx(u)}", gn, gl, lap_type, u.shape[0], _p(u), _p(out))
+    return out
+
+
+def rhs_mehr(n, ll, u, ref=False):
+    L = ref_lib() if ref else lib()
+    pre = "ref" if ref else "orc"
+    u = np.ascontiguousarray(u)
+    out = np.zeros_like(u)
+    gn, gl = _grid(n, ll)
+    _call(L, f"{pre}_rhs_mehr_{_sfx(u)}", gn, gl, u.shape[0], _p(u), _p(out))
+    return out
+
+
+def hpsi(n, ll, lap_type, psi, V, apply_B=1, ref=False):
+    psi = np.ascontiguousarray(psi)
+    V = np.ascontiguousarray(V, dtype=np.float64)
+    out = np.zeros_like(psi)
+    gn, gl = _grid(n, ll)
+    if ref:
+        assert lap_type == 0 and apply_B == 1
+        _call(ref_lib(), f"ref_hpsi_mehr_{_sfx(psi)}", gn, gl, psi.shape[0], _p(psi), _p(V), _p(out))
+    else:
+        _call(lib(), f"orc_hpsi_{_sfx(psi)}", gn, gl, lap_type, apply_B, psi.shape[0], _p(psi), _p(V), _p(out))
+    return out
+
+
+def restrict(n, ll, u, ref=False):
+    L = ref_lib() if ref else lib()
+    pre = "ref" if ref else "orc"
+    u = np.ascontiguousarray(u)
+    out = np.zeros((u.shape[0], (n[0] // 2) * (n[1] // 2) * (n[2] // 2)), dtype=u.dtype)
+    gn, gl = _grid(n, ll)
+    _call(L, f"{pre}_restrict_{_sfx(u)}", gn, gl, u.shape[0], _p(u), _p(out))
+    return out
+
+
+def extend(n, ll, c, ref=False):
+    """n is the FINE grid."""
+    L = ref_lib() if ref else lib()
+    pre = "ref" if ref else "orc"
+    c = np.ascontiguousarray(c)
+    out = np.zeros((c.shape[0], n[0] * n[1] * n[2]), dtype=c.dtype)
+    gn, gl = _grid(n, ll)
+    _call(L, f"{pre}_extend_{_sfx(c)}", gn, gl, c.shape[0], _p(c), _p(out))
+    return out
+
+
+def mask_build(n, ll, ng, nlevels, centers, radii, func=0, ref=False, dtype=np.float64):
+    """Masks of every orbital at levels 0..nlevels-1 (func 0 gaussianDecay,
+    1 one).  Returns (state[nlevels, nfunc], values list per level
+    [nfunc, level_points])."""
+    centers = np.ascontiguousarray(centers, dtype=np.float64)
+    radii = np.ascontiguousarray(radii, dtype=np.float64)
+    nf = radii.shape[0]
+    sizes = [(n[0] >> l) * (n[1] >> l) * (n[2] >> l) for l in range(nlevels)]
+    state = np.zeros(nlevels * nf, dtype=np.int32)
+    gn, gl = _grid(n, ll)
+    if ref:
+        vals = np.zeros(sum(sizes) * nf, dtype=np.float64)
+        _call(ref_lib(), "ref_mask_build", gn, gl, ng, nlevels, nf, _p(centers), _p(radii), func,
+              _p(state), _p(vals))
+        vals = vals.astype(dtype)
+    else:
+        vals = np.zeros(sum(sizes) * nf, dtype=dtype)
+        _call(lib(), f"orc_mask_build_{_sfx(vals)}", gn, gl, ng, nlevels, nf, _p(centers), _p(radii),
+              func, _p(state), _p(vals))
+    out, off = [], 0
+    for s in sizes:
+        out.append(vals[off:off + nf * s].reshape(nf, s))
+        off += nf * s
+    return state.reshape(nlevels, nf), out
+
+
+def mask_apply(n, level, state, values, u, kind=0):
+    """Apply level masks (from mask_build) to ghost-free data u (copy)."""
+    u = np.array(u, copy=True)
+    nl = state.shape[0]
+    flat = np.ascontiguousarray(np.concatenate([v.reshape(-1) for v in values]).astype(u.dtype))
+    st = np.ascontiguousarray(state.reshape(-1), dtype=np.int32)
+    gn = (ctypes.c_int * 3)(*n)
+    _call(lib(), f"orc_mask_apply_{_sfx(u)}", gn, level, nl, u.shape[0], kind, _p(st), _p(flat), _p(u))
+    return u
+
+
+def precond(n, ll, lap_type, maxlevels, gamma, res, masks=None, kind=0, ref=False):
+    """OrbitalsPreconditioning::precond_mg on a residual block.  masks: for the
+    oracle, (state, values) from mask_build; for the reference, (centers,
+    radii) (it builds its own GridMask objects)."""
+    res = np.ascontiguousarray(res)
+    out = np.zeros_like(res)
+    gn, gl = _grid(n, ll)
+    nf = res.shape[0]
+    if ref and lap_type in _PER_FUNCTION and nf > 1:
+        parts = []
+        for i in range(nf):
+            m = None if masks is None else (np.asarray(masks[0])[i:i + 1], np.asarray(masks[1])[i:i + 1])
+            parts.append(precond(n, ll, lap_type, maxlevels, gamma, res[i:i + 1], m, kind, ref=True))
+        return np.concatenate(parts)
+    if ref:
+        if masks is None:
+            c = np.zeros(3)
+            r = np.zeros(1)
+            nm = 0
+        else:
+            c, r = (np.ascontiguousarray(m, dtype=np.float64) for m in masks)
+            nm = nf
+        _call(ref_lib(), f"ref_precond_{_sfx(res)}", gn, gl, lap_type, maxlevels, ctypes.c_double(gamma),
+              nf, _p(res), _p(out), nm, _p(c), _p(r), kind)
+        return out
+    if masks is None:
+        _call(lib(), f"orc_precond_{_sfx(res)}", gn, gl, lap_type, maxlevels, ctypes.c_double(gamma),
+              nf, _p(res), _p(out), kind, None, None)
+    else:
+        state, values = masks
+        flat = np.ascontiguousarray(np.concatenate([v.reshape(-1) for v in values]).astype(res.dtype))
+        st = np.ascontiguousarray(state.reshape(-1), dtype=np.int32)
+        _call(lib(), f"orc_precond_{_sfx(res)}", gn, gl, lap_type, maxlevels, ctypes.c_double(gamma),
+              nf, _p(res), _p(out), kind, _p(st), _p(flat))
+    return out
+
+
+def set_gamma(inv_diag, mg_levels, vmax, small_eig):
+    return lib().orc_set_gamma(ctypes.c_double(inv_diag), mg_levels, ctypes.c_double(vmax),
+                               ctypes.c_double(small_eig))
+
+
+def jacobi_factor(n, ll, lap_type):
+    gn, gl = _grid(n, ll)
+    return lib().orc_jacobi_factor(gn, gl, lap_type)
+
+
+def gram(psi, vel):
+    psi = np.ascontiguousarray(psi)
+    nf, npt = psi.shape
+    S = np.zeros((nf, nf))
+    _call(lib(), f"orc_gram_{_sfx(psi)}", _p(psi), ctypes.c_long(npt), nf, ctypes.c_long(npt),
+          ctypes.c_double(vel), _p(S))
+    return S
+
+
+def hmat(psi, hpsi_, vel):
+    psi = np.ascontiguousarray(psi)
+    hpsi_ = np.ascontiguousarray(hpsi_, dtype=psi.dtype)
+    nf, npt = psi.shape
+    H = np.zeros((nf, nf))
+    _call(lib(), f"orc_hmat_{_sfx(psi)}", _p(psi), _p(hpsi_), ctypes.c_long(npt), nf,
+          ctypes.c_long(npt), ctypes.c_double(vel), _p(H))
+    # H is column-major (j*n+i) = H(i,j); return H[i, j]
+    return H.T.copy()
+
+
+def potrf(S):
+    """Lower Cholesky factor of S (column-major inside; numpy in/out)."""
+    n = S.shape[0]
+    A = np.ascontiguousarray(np.asarray(S, dtype=np.float64).T.copy())
+    info = lib().orc_potrf(n, _p(A))
+    return info, A.T.copy()
+
+
+def inverse_from_chol(L):
+    n = L.shape[0]
+    Lc = np.ascontiguousarray(L.T)
+    out = np.zeros((n, n))
+    _call(lib(), "orc_inverse_from_chol", n, _p(Lc), _p(out))
+    return out.T.copy()
+
+
+def trace_prod(H, Sinv):
+    n = H.shape[0]
+    Hc = np.ascontiguousarray(np.asarray(H, dtype=np.float64).T)
+    Sc = np.ascontiguousarray(np.asarray(Sinv, dtype=np.float64).T)
+    return lib().orc_trace_prod(n, _p(Hc), _p(Sc))
