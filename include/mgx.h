@@ -1,0 +1,242 @@
+/*
+ * mgx.h -- C ABI of the GB300 (sm_103a) implementation of MGmol's orbital
+ * hot path: the local Hamiltonian on a block of orbitals, the block
+ * multigrid V-cycle used as orbital preconditioner, localization masks, and
+ * the Gram / H-matrix contractions with FP64 Cholesky, inverse and trace.
+ *
+ * Conventions
+ *  - Every call returns an mgx_status; mgx_last_error_string() gives the
+ *    text of the last failure on the calling host thread.
+ *  - All data pointers are DEVICE pointers owned by the caller, unless a
+ *    parameter says "host".  Nothing here copies between host and device
+ *    except where stated.  Calls are ordered on the cudaStream_t passed as
+ *    `stream` (NULL = the legacy default stream).
+ *  - Orbital blocks without ghosts use MGmol's BlockVector layout
+ *    (src/BlockVector.h:22-67): function-major, nfunc columns of
+ *    n[0]*n[1]*n[2] points with leading dimension `ld` (elements), points
+ *    x-slowest, z-fastest.  Ghosted blocks use pb::GridFuncVector's layout
+ *    (src/pb/GridFuncVector.cc:21-43): nfunc blocks of
+ *    (n[0]+2g)(n[1]+2g)(n[2]+2g) values, inc_x = (n[1]+2g)(n[2]+2g),
+ *    inc_y = n[2]+2g.
+ *  - Operators work in MGmol's Rydberg convention: the "del2" kernels
+ *    return -Laplacian (a positive operator), and the Mehrstellen local
+ *    Hamiltonian is H psi = -Lap_M psi + B (V psi)
+ *    (src/Hamiltonian.cc:106-132).  Hartree = Rydberg / 2.
+ *  - Boundary conditions: periodic in all three directions (the only
+ *    case the implementation accepts; anything else is MGX_UNSUPPORTED).
+ *  - N x N matrices (S, H, S^-1, L) are FP64, column-major, leading
+ *    dimension n, on the device.
+ */
+#ifndef MGX_H
+#define MGX_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum mgx_status
+{
+    MGX_OK          = 0,
+    MGX_BAD_ARG     = 1, /* wrong shape, pointer, alignment or option */
+    MGX_NOT_SPD     = 2, /* Cholesky met a non-positive pivot */
+    MGX_NONFINITE   = 3, /* NaN or Inf detected where checked */
+    MGX_TIMEOUT     = 4, /* a bounded device wait gave up */
+    MGX_CUDA_ERROR  = 5, /* a CUDA runtime call failed */
+    MGX_UNSUPPORTED = 6, /* valid request outside what is implemented */
+    MGX_NO_MEMORY   = 7  /* device workspace allocation failed */
+} mgx_status;
+
+typedef enum mgx_dtype
+{
+    MGX_F64 = 0,
+    MGX_F32 = 1
+} mgx_dtype;
+
+/* lap_type values of MGmol (src/LapFactory.h:26-53) */
+typedef enum mgx_lap_type
+{
+    MGX_LAP_MEHR4 = 0, /* Mehrstellen 4th order, pb::Laph4M */
+    MGX_LAP_2ND   = 1, /* pb::Laph2 */
+    MGX_LAP_4TH   = 2, /* pb::Laph4 */
+    MGX_LAP_6TH   = 3, /* pb::Laph6 */
+    MGX_LAP_8TH   = 4  /* pb::Laph8 */
+} mgx_lap_type;
+
+/* Arithmetic of the Gram / H contractions. */
+typedef enum mgx_gemm_mode
+{
+    MGX_GEMM_FP64   = 0, /* FP64 data, FP64 FMA (plain path) */
+    MGX_GEMM_FP32   = 1, /* FP32 data, FP32 FMA on CUDA cores */
+    MGX_GEMM_TF32   = 2, /* FP32 data, tcgen05 kind::tf32, FP32 accumulate */
+    MGX_GEMM_BF16X3 = 3  /* FP32 data split hi+lo bf16, 3 tcgen05 products */
+} mgx_gemm_mode;
+
+typedef struct mgx_grid
+{
+    int n[3];     /* interior points per direction */
+    double ll[3]; /* domain lengths (bohr); h = ll / n, as pb::Grid */
+    int bc[3];    /* 1 = periodic (required) */
+} mgx_grid;
+
+typedef struct mgx_ctx mgx_ctx;
+typedef struct mgx_masks mgx_masks;
+
+/* ---------------------------------------------------------------- */
+/* Context: grid geometry plus device workspaces owned by the context  */
+/* (V-cycle levels, GEMM partials).  One context per stream.           */
+/* ---------------------------------------------------------------- */
+int mgx_create(const mgx_grid* grid, mgx_ctx** ctx);
+int mgx_destroy(mgx_ctx* ctx);
+const char* mgx_last_error_string(void);
+/* Number of kernels this library launched since process start (all
+ * contexts); a counter for benchmarks and tests. */
+unsigned long long mgx_kernel_launch_count(void);
+
+/* ---------------------------------------------------------------- */
+/* Drop-in kernels on ghosted GridFuncVector blocks (ghosts already     */
+/* filled), the MemorySpace::Device overloads of src/pb/FDkernels.h:   */
+/* 38-75 and src/pb/MGkernels.h:10-16.  `ghosts` is the ghost width of   */
+/* the block; it must be at least the operator radius.                  */
+/* ---------------------------------------------------------------- */
+
+/* pb::FDkernelDel2_{4th_Mehr,2nd,4th,6th,8th}<T>(grid, v, b, nfunc,
+ * MemorySpace::Device), src/pb/FDkernels.h:38-75: b = -Lap v on interior
+ * points; ghost values of b untouched. */
+int mgx_fdkernel_del2(const mgx_grid* grid, int ghosts, int lap_type,
+    mgx_dtype dtype, const void* v, void* b, size_t nfunc, void* stream);
+
+/* pb::FDkernelRHS_4th_Mehr1<T>(grid, v, rhs, rhs_ghosts, nfunc),
+ * src/pb/FDkernels.cc:522-584: rhs = B v (Mehrstellen right-hand side);
+ * rhs has rhs_ghosts ghost layers (0 = ghost-free). */
+int mgx_fdkernel_rhs_mehr1(const mgx_grid* grid, int ghosts, mgx_dtype dtype,
+    const void* v, void* rhs, int rhs_ghosts, size_t nfunc, void* stream);
+
+/* pb::MGkernelRestrict3D<T>(fine, fine_grid, coarse, coarse_grid, nfunc),
+ * src/pb/MGkernels.cc:203-283.  `grid` is the fine grid; the coarse grid
+ * has n/2 points and the same ghost width. */
+int mgx_mgkernel_restrict3d(const mgx_grid* grid, int ghosts, mgx_dtype dtype,
+    const void* fine, void* coarse, size_t nfunc, void* stream);
+
+/* pb::MGkernelExtend3D<T>(coarse, coarse_grid, fine, fine_grid, nfunc),
+ * src/pb/MGkernels.cc:28-201 (coarse ghosts must be filled).  `grid` is the
+ * fine grid. */
+int mgx_mgkernel_extend3d(const mgx_grid* grid, int ghosts, mgx_dtype dtype,
+    const void* coarse, void* fine, size_t nfunc, void* stream);
+
+/* GridFuncVector::trade_boundaries on one task, periodic
+ * (src/pb/GridFuncVector.cc:1543-1621): fills all ghost layers. */
+int mgx_trade_boundaries(const mgx_grid* grid, int ghosts, mgx_dtype dtype,
+    void* u, size_t nfunc, void* stream);
+
+/* ---------------------------------------------------------------- */
+/* Fused path on ghost-free blocks (periodic halo handled in the tile    */
+/* loaders).                                                            */
+/* ---------------------------------------------------------------- */
+
+/* out = -Lap u for nfunc functions (lap_type 0..4). */
+int mgx_fd_apply(mgx_ctx* ctx, int lap_type, mgx_dtype dtype, const void* u,
+    size_t ld, void* out, int nfunc, void* stream);
+
+/* out = B u, the Mehrstellen right-hand-side operator. */
+int mgx_rhs_mehr(mgx_ctx* ctx, mgx_dtype dtype, const void* u, size_t ld,
+    void* out, int nfunc, void* stream);
+
+/* Hamiltonian<T>::applyLocal (src/Hamiltonian.cc:85-159), Rydberg units.
+ * lap_type 0 and apply_B_to_V 1: hpsi = -Lap_M psi + B(V psi);
+ * lap_type 0 and apply_B_to_V 0: hpsi = -Lap_M psi + V psi;
+ * lap_type 1..4: hpsi = -Lap psi + V psi.
+ * V has n[0]*n[1]*n[2] points of type v_dtype (FP64 like MGmol's POTDTYPE,
+ * or FP32). */
+int mgx_hpsi(mgx_ctx* ctx, int lap_type, mgx_dtype dtype, const void* psi,
+    size_t ld, const void* V, mgx_dtype v_dtype, void* hpsi, int nfunc,
+    int apply_B_to_V, void* stream);
+
+/* Full-weighting restriction and trilinear prolongation between level
+ * `level` (0 = the context grid) and level+1, ghost-free, periodic
+ * (src/pb/MGkernels.cc:28-283). */
+int mgx_mg_restrict(mgx_ctx* ctx, int level, mgx_dtype dtype, const void* fine,
+    void* coarse, int nfunc, void* stream);
+int mgx_mg_prolong(mgx_ctx* ctx, int level, mgx_dtype dtype, const void* coarse,
+    void* fine, int nfunc, void* stream);
+
+/* OrbitalsPreconditioning<T>::precond_mg (src/OrbitalsPreconditioning.cc:
+ * 86-117) with Preconditioning<T>::mg (src/Preconditioning.cc:155-216):
+ * out = V-cycle(res) started from gamma * res, `maxlevels` coarse levels,
+ * 2 pre / 2 post Jacobi sweeps, 4 sweeps on the coarsest level, fine-level
+ * Jacobi factor of lap_type, Laph2 on coarse levels.  masks may be NULL.
+ * res and out may not alias.  The V-cycle workspace is owned by ctx and
+ * processes at most `chunk` functions at a time (0 = all at once). */
+typedef struct mgx_precond_params
+{
+    int lap_type;
+    int maxlevels;
+    double gamma;
+    int chunk;
+} mgx_precond_params;
+int mgx_precond_mg(mgx_ctx* ctx, const mgx_precond_params* p, mgx_dtype dtype,
+    const void* res, size_t ld, void* out, int nfunc, const mgx_masks* masks,
+    void* stream);
+
+/* OrbitalsPreconditioning<T>::setGamma (src/OrbitalsPreconditioning.cc:
+ * 119-145); host computation, returned in *gamma. */
+int mgx_precond_gamma(const mgx_grid* grid, int lap_type, int mg_levels,
+    double vmax, double small_eig, double* gamma);
+
+/* ---------------------------------------------------------------- */
+/* Localization masks (GridMask / GridMaskMax / GridMaskMult,           */
+/* src/GridMask.cc:120-264, src/MasksSet.cc:16-48,110-123).             */
+/* ---------------------------------------------------------------- */
+
+/* Builds, on the device, the masks of nfunc orbitals for levels
+ * 0..nlevels-1.  centers (nfunc x 3) and radii (nfunc) are HOST arrays.
+ * func: 0 gaussianDecay, 1 one.  kind: 0 GridMaskMax (clamp), 1
+ * GridMaskMult (multiply).  mesh_ghosts: ghost width of the mesh grid
+ * (enters the overlap margin, src/GridMask.cc:42-45).  dtype: storage
+ * type of the mask values (MGmol's lmasktype = orbital type). */
+int mgx_masks_create(mgx_ctx* ctx, int nlevels, int nfunc,
+    const double* centers, const double* radii, int func, int kind,
+    int mesh_ghosts, mgx_dtype dtype, mgx_masks** masks, void* stream);
+int mgx_masks_destroy(mgx_masks* masks);
+/* Applies level `level` masks to nfunc ghost-free functions in place
+ * (GridFuncVector::app_mask, src/pb/GridFuncVector.cc:2427-2438). */
+int mgx_masks_apply(mgx_ctx* ctx, const mgx_masks* masks, int level,
+    void* u, size_t ld, int nfunc, void* stream);
+/* Writes the dense mask values of one level (nfunc x level points, dtype
+ * of the masks) and the states (host int array, nfunc) -- for checking. */
+int mgx_masks_expand(const mgx_masks* masks, int level, void* dense,
+    int* host_state, void* stream);
+
+/* ---------------------------------------------------------------- */
+/* Gram and H matrices (LocGridOrbitals::getLocalOverlap /              */
+/* computeLocalProduct, src/LocGridOrbitals.cc:1504-1604, then the      */
+/* |x| > 1e-14 filter of src/LocalMatrices2DistMatrix.cc:16,60).        */
+/* ---------------------------------------------------------------- */
+
+/* S = Psi^T Psi * vel, full symmetric, FP64 n x n. */
+int mgx_gram(mgx_ctx* ctx, int mode, const void* psi, size_t ld, int nfunc,
+    double* S, void* stream);
+/* H = Psi^T (H Psi) * vel, FP64 n x n (H(i,j) = <psi_i, hpsi_j>). */
+int mgx_hmat(mgx_ctx* ctx, int mode, const void* psi, const void* hpsi,
+    size_t ld, int nfunc, double* H, void* stream);
+
+/* GramMatrix::updateLS (src/GramMatrix.cc:180-191): A (n x n, FP64) is
+ * overwritten by its lower Cholesky factor (upper part zeroed).  *info
+ * (host) receives 0 or the 1-based index of the first non-positive pivot;
+ * the call then returns MGX_NOT_SPD instead of aborting. Synchronous. */
+int mgx_cholesky(mgx_ctx* ctx, int n, double* A, int* info, void* stream);
+/* GramMatrix::computeInverse (src/GramMatrix.cc:75-91): Sinv = (L L^T)^-1
+ * from the factor L. */
+int mgx_inverse_from_cholesky(mgx_ctx* ctx, int n, const double* L,
+    double* Sinv, void* stream);
+/* ProjectedMatrices::getEigSum (src/ProjectedMatrices.cc:550-566):
+ * *trace (device) = tr(H Sinv), H taken symmetric from its lower part. */
+int mgx_trace_prod(mgx_ctx* ctx, int n, const double* H, const double* Sinv,
+    double* trace, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,360 @@
+"""ctypes binding of the mgx C ABI (include/mgx.h) with torch device tensors.
+
+This is the Python face of the library used by the tests and the benchmark;
+C++ callers use include/mgx.h directly or the MGmol-shaped adaptor classes in
+mgmol_gb300/cpp/.  The shared library is the in-tree mgmol_gb300/libmgx.so
+built for sm_103a; there is no other implementation behind these calls, and
+importing fails loudly when the library cannot be loaded.
+
+Orbital blocks are torch tensors of shape (nfunc, nx*ny*nz) (or (nx*ny*nz,)
+for one function), float64 or float32, on the CUDA device, points x-slowest
+and z-fastest.  Matrices are (n, n) float64 tensors, column-major as in the
+C ABI (use .T to read them row-major; S and S^-1 are symmetric).
+"""
+import ctypes
+import os
+
+import torch
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libmgx.so")
+
+MGX_OK, MGX_BAD_ARG, MGX_NOT_SPD, MGX_NONFINITE, MGX_TIMEOUT, MGX_CUDA_ERROR, \
+    MGX_UNSUPPORTED, MGX_NO_MEMORY = range(8)
+F64, F32 = 0, 1
+GEMM_FP64, GEMM_FP32, GEMM_TF32, GEMM_BF16X3 = 0, 1, 2, 3
+LAP_MEHR4, LAP_2ND, LAP_4TH, LAP_6TH, LAP_8TH = 0, 1, 2, 3, 4
+
+_STATUS = {0: "MGX_OK", 1: "MGX_BAD_ARG", 2: "MGX_NOT_SPD", 3: "MGX_NONFINITE", 4: "MGX_TIMEOUT",
+           5: "MGX_CUDA_ERROR", 6: "MGX_UNSUPPORTED", 7: "MGX_NO_MEMORY"}
+
+
+class MgxError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"{_STATUS.get(status, status)}: {msg}")
+        self.status = status
+
+
+class Grid(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_int * 3), ("ll", ctypes.c_double * 3), ("bc", ctypes.c_int * 3)]
+
+    @staticmethod
+    def make(n, ll, bc=(1, 1, 1)):
+        g = Grid()
+        for i in range(3):
+            g.n[i] = int(n[i])
+            g.ll[i] = float(ll[i])
+            g.bc[i] = int(bc[i])
+        return g
+
+
+class PrecondParams(ctypes.Structure):
+    _fields_ = [("lap_type", ctypes.c_int), ("maxlevels", ctypes.c_int), ("gamma", ctypes.c_double),
+                ("chunk", ctypes.c_int)]
+
+
+_LIB = None
+_vp = ctypes.c_void_p
+_i = ctypes.c_int
+_sz = ctypes.c_size_t
+_d = ctypes.c_double
+_dp = ctypes.POINTER(ctypes.c_double)
+_ip = ctypes.POINTER(ctypes.c_int)
+
+_SIGS = {
+    "mgx_create": [ctypes.POINTER(Grid), ctypes.POINTER(_vp)],
+    "mgx_destroy": [_vp],
+    "mgx_fdkernel_del2": [ctypes.POINTER(Grid), _i, _i, _i, _vp, _vp, _sz, _vp],
+    "mgx_fdkernel_rhs_mehr1": [ctypes.POINTER(Grid), _i, _i, _vp, _vp, _i, _sz, _vp],
+    "mgx_mgkernel_restrict3d": [ctypes.POINTER(Grid), _i, _i, _vp, _vp, _sz, _vp],
+    "mgx_mgkernel_extend3d": [ctypes.POINTER(Grid), _i, _i, _vp, _vp, _sz, _vp],
+    "mgx_trade_boundaries": [ctypes.POINTER(Grid), _i, _i, _vp, _sz, _vp],
+    "mgx_fd_apply": [_vp, _i, _i, _vp, _sz, _vp, _i, _vp],
+    "mgx_rhs_mehr": [_vp, _i, _vp, _sz, _vp, _i, _vp],
+    "mgx_hpsi": [_vp, _i, _i, _vp, _sz, _vp, _i, _vp, _i, _i, _vp],
+    "mgx_mg_restrict": [_vp, _i, _i, _vp, _vp, _i, _vp],
+    "mgx_mg_prolong": [_vp, _i, _i, _vp, _vp, _i, _vp],
+    "mgx_precond_mg": [_vp, ctypes.POINTER(PrecondParams), _i, _vp, _sz, _vp, _i, _vp, _vp],
+    "mgx_precond_gamma": [ctypes.POINTER(Grid), _i, _i, _d, _d, _dp],
+    "mgx_masks_create": [_vp, _i, _i, _dp, _dp, _i, _i, _i, _i, ctypes.POINTER(_vp), _vp],
+    "mgx_masks_destroy": [_vp],
+    "mgx_masks_apply": [_vp, _vp, _i, _vp, _sz, _i, _vp],
+    "mgx_masks_expand": [_vp, _i, _vp, _ip, _vp],
+    "mgx_gram": [_vp, _i, _vp, _sz, _i, _vp, _vp],
+    "mgx_hmat": [_vp, _i, _vp, _vp, _sz, _i, _vp, _vp],
+    "mgx_cholesky": [_vp, _i, _vp, _ip, _vp],
+    "mgx_inverse_from_cholesky": [_vp, _i, _vp, _vp, _vp],
+    "mgx_trace_prod": [_vp, _i, _vp, _vp, _vp, _vp],
+}
+
+# every entry point declared in include/mgx.h
+EXPORTS = sorted(list(_SIGS) + ["mgx_last_error_string", "mgx_kernel_launch_count"])
+
+
+def load(path=LIB_PATH):
+    """Loads libmgx.so (building it first when nvcc is available)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    if not os.path.exists(path):
+        from . import build as _b
+        _b.build()
+    if not os.path.exists(path):
+        raise ImportError(f"mgx library not found at {path}")
+    L = ctypes.CDLL(path)
+    for name, args in _SIGS.items():
+        fn = getattr(L, name)
+        fn.argtypes = args
+        fn.restype = ctypes.c_int
+    L.mgx_last_error_string.restype = ctypes.c_char_p
+    L.mgx_last_error_string.argtypes = []
+    L.mgx_kernel_launch_count.restype = ctypes.c_ulonglong
+    L.mgx_kernel_launch_count.argtypes = []
+    _LIB = L
+    return L
+
+
+def _check(status):
+    if status != MGX_OK:
+        raise MgxError(status, load().mgx_last_error_string().decode())
+
+
+def launches():
+    return int(load().mgx_kernel_launch_count())
+
+
+def _stream(stream=None):
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return ctypes.c_void_p(s.cuda_stream)
+
+
+def _dtype(t):
+    if t.dtype == torch.float64:
+        return F64
+    if t.dtype == torch.float32:
+        return F32
+    raise TypeError(f"unsupported dtype {t.dtype}")
+
+
+def _block(t, npts):
+    """(pointer, ld, nfunc) of an orbital block tensor."""
+    if not t.is_cuda:
+        raise ValueError("orbital block must be a CUDA tensor")
+    if t.dim() == 1:
+        if t.numel() != npts or t.stride(0) != 1:
+            raise ValueError("bad single-function block")
+        return ctypes.c_void_p(t.data_ptr()), npts, 1
+    if t.dim() != 2 or t.shape[1] != npts or t.stride(1) != 1:
+        raise ValueError(f"block must be (nfunc, {npts}) with unit point stride")
+    return ctypes.c_void_p(t.data_ptr()), t.stride(0), t.shape[0]
+
+
+def _ptr(t):
+    return ctypes.c_void_p(t.data_ptr()) if t is not None else None
+
+
+class Context:
+    """An mgx context: grid geometry plus device workspaces."""
+
+    def __init__(self, n, ll):
+        self.n = tuple(int(x) for x in n)
+        self.ll = tuple(float(x) for x in ll)
+        self.grid = Grid.make(self.n, self.ll)
+        self.npts = self.n[0] * self.n[1] * self.n[2]
+        h = ctypes.c_void_p()
+        _check(load().mgx_create(ctypes.byref(self.grid), ctypes.byref(h)))
+        self.handle = h
+
+    def close(self):
+        if getattr(self, "handle", None):
+            load().mgx_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def h(self):
+        return tuple(self.ll[i] / self.n[i] for i in range(3))
+
+    @property
+    def vel(self):
+        h = self.h
+        return h[0] * h[1] * h[2]
+
+    def level_points(self, level):
+        return (self.n[0] >> level) * (self.n[1] >> level) * (self.n[2] >> level)
+
+    # ------------------------------------------------------------ stencils
+    def fd_apply(self, u, lap_type, out=None, stream=None):
+        p, ld, nf = _block(u, self.npts)
+        out = torch.empty_like(u) if out is None else out
+        po, ldo, _ = _block(out, self.npts)
+        assert ldo == ld
+        _check(load().mgx_fd_apply(self.handle, lap_type, _dtype(u), p, ld, po, nf, _stream(stream)))
+        return out
+
+    def rhs_mehr(self, u, out=None, stream=None):
+        p, ld, nf = _block(u, self.npts)
+        out = torch.empty_like(u) if out is None else out
+        _check(load().mgx_rhs_mehr(self.handle, _dtype(u), p, ld, _ptr(out), nf, _stream(stream)))
+        return out
+
+    def hpsi(self, psi, V, lap_type=LAP_MEHR4, apply_B=True, out=None, stream=None):
+        p, ld, nf = _block(psi, self.npts)
+        out = torch.empty_like(psi) if out is None else out
+        if V.numel() != self.npts or not V.is_contiguous():
+            raise ValueError("V must be contiguous with one value per grid point")
+        _check(load().mgx_hpsi(self.handle, lap_type, _dtype(psi), p, ld, _ptr(V), _dtype(V),
+                               _ptr(out), nf, 1 if apply_B else 0, _stream(stream)))
+        return out
+
+    def restrict(self, fine, level=0, stream=None):
+        nf = 1 if fine.dim() == 1 else fine.shape[0]
+        out = torch.empty((nf, self.level_points(level + 1)), dtype=fine.dtype, device=fine.device)
+        _check(load().mgx_mg_restrict(self.handle, level, _dtype(fine), _ptr(fine), _ptr(out), nf,
+                                      _stream(stream)))
+        return out
+
+    def prolong(self, coarse, level=0, stream=None):
+        nf = 1 if coarse.dim() == 1 else coarse.shape[0]
+        out = torch.empty((nf, self.level_points(level)), dtype=coarse.dtype, device=coarse.device)
+        _check(load().mgx_mg_prolong(self.handle, level, _dtype(coarse), _ptr(coarse), _ptr(out), nf,
+                                     _stream(stream)))
+        return out
+
+    # ------------------------------------------------------------ preconditioner
+    def precond_mg(self, res, lap_type, maxlevels, gamma, masks=None, chunk=0, out=None,
+                   stream=None):
+        p, ld, nf = _block(res, self.npts)
+        out = torch.empty_like(res) if out is None else out
+        prm = PrecondParams(lap_type, maxlevels, float(gamma), int(chunk))
+        _check(load().mgx_precond_mg(self.handle, ctypes.byref(prm), _dtype(res), p, ld, _ptr(out), nf,
+                                     masks.handle if masks is not None else None, _stream(stream)))
+        return out
+
+    def gamma(self, lap_type, mg_levels, vmax, small_eig):
+        g = ctypes.c_double()
+        _check(load().mgx_precond_gamma(ctypes.byref(self.grid), lap_type, mg_levels, vmax, small_eig,
+                                        ctypes.byref(g)))
+        return g.value
+
+    # ------------------------------------------------------------ Gram / H
+    def gram(self, psi, mode=GEMM_FP64, out=None, stream=None):
+        p, ld, nf = _block(psi, self.npts)
+        S = torch.empty((nf, nf), dtype=torch.float64, device=psi.device) if out is None else out
+        _check(load().mgx_gram(self.handle, mode, p, ld, nf, _ptr(S), _stream(stream)))
+        return S
+
+    def hmat(self, psi, hpsi, mode=GEMM_FP64, out=None, stream=None):
+        p, ld, nf = _block(psi, self.npts)
+        ph, ldh, _ = _block(hpsi, self.npts)
+        assert ldh == ld
+        H = torch.empty((nf, nf), dtype=torch.float64, device=psi.device) if out is None else out
+        _check(load().mgx_hmat(self.handle, mode, p, ph, ld, nf, _ptr(H), _stream(stream)))
+        # column-major H(i,j) = <psi_i, hpsi_j>; return the row-major view
+        return H.T
+
+    def cholesky(self, S, stream=None):
+        """Lower factor L (returned as a row-major tensor) of symmetric S."""
+        n = S.shape[0]
+        A = S.T.contiguous().clone()
+        info = ctypes.c_int(0)
+        st = load().mgx_cholesky(self.handle, n, _ptr(A), ctypes.byref(info), _stream(stream))
+        if st != MGX_OK:
+            raise MgxError(st, load().mgx_last_error_string().decode() + f" (info={info.value})")
+        return A.T
+
+    def inverse_from_cholesky(self, L, stream=None):
+        n = L.shape[0]
+        Lc = L.T.contiguous()
+        out = torch.empty((n, n), dtype=torch.float64, device=L.device)
+        _check(load().mgx_inverse_from_cholesky(self.handle, n, _ptr(Lc), _ptr(out), _stream(stream)))
+        return out.T
+
+    def trace_prod(self, H, Sinv, stream=None):
+        n = H.shape[0]
+        Hc = H.T.contiguous()
+        Sc = Sinv.T.contiguous()
+        out = torch.empty(1, dtype=torch.float64, device=H.device)
+        _check(load().mgx_trace_prod(self.handle, n, _ptr(Hc), _ptr(Sc), _ptr(out), _stream(stream)))
+        return out
+
+
+class Masks:
+    """Localization masks (GridMaskMax / GridMaskMult) of nfunc orbitals."""
+
+    def __init__(self, ctx, nlevels, centers, radii, func=0, kind=0, mesh_ghosts=1,
+                 dtype=torch.float64, stream=None):
+        import numpy as np
+        c = np.ascontiguousarray(np.asarray(centers, dtype=np.float64).reshape(-1))
+        r = np.ascontiguousarray(np.asarray(radii, dtype=np.float64).reshape(-1))
+        self.nfunc = r.shape[0]
+        self.nlevels = nlevels
+        self.ctx = ctx
+        self.dtype = dtype
+        h = ctypes.c_void_p()
+        _check(load().mgx_masks_create(ctx.handle, nlevels, self.nfunc, c.ctypes.data_as(_dp),
+                                       r.ctypes.data_as(_dp), func, kind, mesh_ghosts,
+                                       F64 if dtype == torch.float64 else F32, ctypes.byref(h),
+                                       _stream(stream)))
+        self.handle = h
+
+    def apply(self, u, level, stream=None):
+        p, ld, nf = _block(u, self.ctx.level_points(level))
+        _check(load().mgx_masks_apply(self.ctx.handle, self.handle, level, p, ld, nf, _stream(stream)))
+        return u
+
+    def expand(self, level, stream=None):
+        """(state int array, dense values tensor (nfunc, level points))."""
+        import numpy as np
+        dense = torch.empty((self.nfunc, self.ctx.level_points(level)), dtype=self.dtype, device="cuda")
+        st = np.zeros(self.nfunc, dtype=np.int32)
+        _check(load().mgx_masks_expand(self.handle, level, _ptr(dense), st.ctypes.data_as(_ip),
+                                       _stream(stream)))
+        return st, dense
+
+    def close(self):
+        if getattr(self, "handle", None):
+            load().mgx_masks_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+# ---------------------------------------------------------------- drop-in (ghosted)
+def fdkernel_del2(n, ll, ghosts, lap_type, v, b, nfunc, stream=None):
+    g = Grid.make(n, ll)
+    _check(load().mgx_fdkernel_del2(ctypes.byref(g), ghosts, lap_type, _dtype(v), _ptr(v), _ptr(b),
+                                    nfunc, _stream(stream)))
+
+
+def fdkernel_rhs_mehr1(n, ll, ghosts, v, rhs, rhs_ghosts, nfunc, stream=None):
+    g = Grid.make(n, ll)
+    _check(load().mgx_fdkernel_rhs_mehr1(ctypes.byref(g), ghosts, _dtype(v), _ptr(v), _ptr(rhs),
+                                         rhs_ghosts, nfunc, _stream(stream)))
+
+
+def trade_boundaries(n, ll, ghosts, u, nfunc, stream=None):
+    g = Grid.make(n, ll)
+    _check(load().mgx_trade_boundaries(ctypes.byref(g), ghosts, _dtype(u), _ptr(u), nfunc,
+                                       _stream(stream)))
+
+
+def mgkernel_restrict3d(n, ll, ghosts, fine, coarse, nfunc, stream=None):
+    g = Grid.make(n, ll)
+    _check(load().mgx_mgkernel_restrict3d(ctypes.byref(g), ghosts, _dtype(fine), _ptr(fine),
+                                          _ptr(coarse), nfunc, _stream(stream)))
+
+
+def mgkernel_extend3d(n, ll, ghosts, coarse, fine, nfunc, stream=None):
+    g = Grid.make(n, ll)
+    _check(load().mgx_mgkernel_extend3d(ctypes.byref(g), ghosts, _dtype(coarse), _ptr(coarse),
+                                        _ptr(fine), nfunc, _stream(stream)))

@@ -1,0 +1,504 @@
+// C ABI of the mgx library (include/mgx.h): argument checks, contexts,
+// error reporting, and dispatch to the sm_103a kernels.
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <algorithm>
+#include <cmath>
+
+#include "mgx_internal.cuh"
+#include "mgx_stencil.cuh"
+
+namespace mgx
+{
+static thread_local char g_err[512] = "";
+static std::atomic<unsigned long long> g_launches{ 0 };
+
+void set_error(const char* fmt, ...)
+{
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof(g_err), fmt, ap);
+    va_end(ap);
+}
+
+int fail(int status, const char* fmt, ...)
+{
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof(g_err), fmt, ap);
+    va_end(ap);
+    return status;
+}
+
+int cuda_check(cudaError_t e, const char* what)
+{
+    if (e == cudaSuccess) return MGX_OK;
+    set_error("%s: %s", what, cudaGetErrorString(e));
+    return e == cudaErrorMemoryAllocation ? MGX_NO_MEMORY : MGX_CUDA_ERROR;
+}
+
+void count_launch(unsigned n) { g_launches += n; }
+
+int DeviceBuffer::ensure(size_t b)
+{
+    if (b <= bytes) return MGX_OK;
+    release();
+    cudaError_t e = cudaMalloc(&ptr, b);
+    if (e != cudaSuccess)
+    {
+        ptr = nullptr;
+        cudaGetLastError();
+        return cuda_check(e, "workspace cudaMalloc");
+    }
+    bytes = b;
+    return MGX_OK;
+}
+
+void DeviceBuffer::release()
+{
+    if (ptr) cudaFree(ptr);
+    ptr   = nullptr;
+    bytes = 0;
+}
+
+// defined in the other translation units
+int precond_mg(mgx_ctx*, const mgx_precond_params*, int, const void*, size_t,
+    void*, int, const mgx_masks*, cudaStream_t);
+int restrict_launch(int, const Level&, const void*, size_t, void*, size_t, int,
+    const MaskDev&, cudaStream_t);
+int prolong_launch(int, int, const Level&, const void*, size_t, void*, size_t,
+    int, const MaskDev&, cudaStream_t);
+int masks_create(mgx_ctx*, int, int, const double*, const double*, int, int,
+    int, int, mgx_masks**, cudaStream_t);
+int masks_apply(mgx_ctx*, const mgx_masks*, int, void*, size_t, int, cudaStream_t);
+int masks_expand(const mgx_masks*, int, void*, int*, cudaStream_t);
+int gram_cuda_cores(mgx_ctx*, int, const void*, const void*, size_t, size_t,
+    int, double, int, double*, cudaStream_t);
+int gram_tcgen05(mgx_ctx*, int, const void*, const void*, size_t, size_t, int,
+    double, int, double*, cudaStream_t);
+int cholesky(mgx_ctx*, int, double*, int*, cudaStream_t);
+int inverse_from_cholesky(mgx_ctx*, int, const double*, double*, cudaStream_t);
+int trace_prod(int, const double*, const double*, double*, cudaStream_t);
+
+static int check_grid(const mgx_grid* g)
+{
+    if (!g) return fail(MGX_BAD_ARG, "grid is NULL");
+    for (int i = 0; i < 3; i++)
+    {
+        if (g->n[i] < 1 || g->n[i] > 8192)
+            return fail(MGX_BAD_ARG, "grid dimension %d = %d out of range", i, g->n[i]);
+        if (!(g->ll[i] > 0.))
+            return fail(MGX_BAD_ARG, "domain length %d not positive", i);
+        if (g->bc[i] != 1)
+            return fail(MGX_UNSUPPORTED, "only periodic boundary conditions are implemented");
+    }
+    return MGX_OK;
+}
+
+static int check_dtype(int d)
+{
+    if (d != MGX_F64 && d != MGX_F32) return fail(MGX_BAD_ARG, "dtype %d invalid", d);
+    return MGX_OK;
+}
+
+static int check_block(const mgx_grid& g, const void* p, size_t ld, int nfunc,
+    const char* name)
+{
+    if (nfunc < 0) return fail(MGX_BAD_ARG, "%s: nfunc < 0", name);
+    if (nfunc > 0 && !p) return fail(MGX_BAD_ARG, "%s is NULL", name);
+    const size_t np = (size_t)g.n[0] * g.n[1] * g.n[2];
+    if (nfunc > 1 && ld < np) return fail(MGX_BAD_ARG, "%s: ld %zu < %zu points", name, ld, np);
+    return MGX_OK;
+}
+
+static PlaneParams plane(const mgx_grid& g)
+{
+    PlaneParams p;
+    for (int i = 0; i < 3; i++)
+        p.n[i] = g.n[i];
+    return p;
+}
+// ghosted restriction / extension: strip ghosts of the fine (resp. coarse)
+// block, run the ghost-free kernel, write back inside the ghosted target.
+template <typename T>
+__global__ void strip_kernel(const T* g, int gw, int nx, int ny, int nz, T* out,
+    size_t nfunc, int to_ghosted)
+{
+    const size_t np = (size_t)nx * ny * nz;
+    const int ey = ny + 2 * gw, ez = nz + 2 * gw;
+    const size_t sg = (size_t)(nx + 2 * gw) * ey * ez;
+    for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < np * nfunc;
+         t += (size_t)gridDim.x * blockDim.x)
+    {
+        const size_t f = t / np, i = t - f * np;
+        const int z = (int)(i % nz), y = (int)((i / nz) % ny), x = (int)(i / ((size_t)nz * ny));
+        const size_t gi = f * sg + ((size_t)(x + gw) * ey + (y + gw)) * ez + z + gw;
+        if (to_ghosted)
+            const_cast<T*>(g)[gi] = out[t];
+        else
+            out[t] = g[gi];
+    }
+}
+
+int strip(int dtype, const void* g, int gw, const int n[3], void* out,
+    size_t nfunc, int to_ghosted, cudaStream_t s)
+{
+    const size_t np = (size_t)n[0] * n[1] * n[2] * nfunc;
+    const int nb    = (int)std::min<size_t>((np + 255) / 256, 1u << 20);
+    if (dtype == MGX_F64)
+        strip_kernel<double><<<nb, 256, 0, s>>>((const double*)g, gw, n[0], n[1], n[2],
+            (double*)out, nfunc, to_ghosted);
+    else
+        strip_kernel<float><<<nb, 256, 0, s>>>((const float*)g, gw, n[0], n[1], n[2],
+            (float*)out, nfunc, to_ghosted);
+    MGX_LAUNCH_CHECK("strip_kernel");
+    return MGX_OK;
+}
+
+} // namespace mgx
+
+using namespace mgx;
+
+extern "C" {
+
+const char* mgx_last_error_string(void) { return g_err; }
+
+unsigned long long mgx_kernel_launch_count(void) { return g_launches.load(); }
+
+int mgx_create(const mgx_grid* grid, mgx_ctx** ctx)
+{
+    MGX_TRY(check_grid(grid));
+    if (!ctx) return fail(MGX_BAD_ARG, "ctx is NULL");
+    int dev = 0;
+    MGX_TRY(cuda_check(cudaGetDevice(&dev), "cudaGetDevice"));
+    mgx_ctx* c = new mgx_ctx;
+    c->grid    = *grid;
+    int sms = 0, smem = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaDeviceGetAttribute(&smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    c->sm_count   = sms > 0 ? sms : 152;
+    c->smem_optin = (size_t)smem;
+    *ctx          = c;
+    return MGX_OK;
+}
+
+int mgx_destroy(mgx_ctx* ctx)
+{
+    delete ctx;
+    return MGX_OK;
+}
+
+int mgx_fdkernel_del2(const mgx_grid* grid, int ghosts, int lap_type,
+    mgx_dtype dtype, const void* v, void* b, size_t nfunc, void* stream)
+{
+    MGX_TRY(check_grid(grid));
+    MGX_TRY(check_dtype(dtype));
+    if (nfunc && (!v || !b)) return fail(MGX_BAD_ARG, "NULL block");
+    return ghosted_del2(*grid, ghosts, lap_type, dtype, v, b, nfunc, (cudaStream_t)stream);
+}
+
+int mgx_fdkernel_rhs_mehr1(const mgx_grid* grid, int ghosts, mgx_dtype dtype,
+    const void* v, void* rhs, int rhs_ghosts, size_t nfunc, void* stream)
+{
+    MGX_TRY(check_grid(grid));
+    MGX_TRY(check_dtype(dtype));
+    if (nfunc && (!v || !rhs)) return fail(MGX_BAD_ARG, "NULL block");
+    return ghosted_rhs(*grid, ghosts, dtype, v, rhs, rhs_ghosts, nfunc, (cudaStream_t)stream);
+}
+
+int mgx_trade_boundaries(const mgx_grid* grid, int ghosts, mgx_dtype dtype,
+    void* u, size_t nfunc, void* stream)
+{
+    MGX_TRY(check_grid(grid));
+    MGX_TRY(check_dtype(dtype));
+    if (nfunc && !u) return fail(MGX_BAD_ARG, "NULL block");
+    return ghosted_trade(*grid, ghosts, dtype, u, nfunc, (cudaStream_t)stream);
+}
+
+int mgx_mgkernel_restrict3d(const mgx_grid* grid, int ghosts, mgx_dtype dtype,
+    const void* fine, void* coarse, size_t nfunc, void* stream)
+{
+    MGX_TRY(check_grid(grid));
+    MGX_TRY(check_dtype(dtype));
+    if (ghosts < 1) return fail(MGX_BAD_ARG, "ghost width must be >= 1");
+    if (nfunc == 0) return MGX_OK;
+    if (!fine || !coarse) return fail(MGX_BAD_ARG, "NULL block");
+    for (int i = 0; i < 3; i++)
+        if (grid->n[i] % 2) return fail(MGX_BAD_ARG, "odd fine dimension");
+    cudaStream_t s = (cudaStream_t)stream;
+    const Level F  = make_level(*grid, 0), C = make_level(*grid, 1);
+    DeviceBuffer a, b;
+    const size_t es = dtype_size(dtype);
+    MGX_TRY(a.ensure(F.npts() * nfunc * es));
+    MGX_TRY(b.ensure(C.npts() * nfunc * es));
+    // the fine ghosts are not needed: the ghost-free kernel wraps periodically
+    MGX_TRY(strip(dtype, fine, ghosts, F.n, a.ptr, nfunc, 0, s));
+    MGX_TRY(restrict_launch(dtype, F, a.ptr, F.npts(), b.ptr, C.npts(), (int)nfunc, MaskDev(), s));
+    MGX_TRY(strip(dtype, coarse, ghosts, C.n, b.ptr, nfunc, 1, s));
+    return cuda_check(cudaStreamSynchronize(s), "restrict3d sync");
+}
+
+int mgx_mgkernel_extend3d(const mgx_grid* grid, int ghosts, mgx_dtype dtype,
+    const void* coarse, void* fine, size_t nfunc, void* stream)
+{
+    MGX_TRY(check_grid(grid));
+    MGX_TRY(check_dtype(dtype));
+    if (ghosts < 1) return fail(MGX_BAD_ARG, "ghost width must be >= 1");
+    if (nfunc == 0) return MGX_OK;
+    if (!fine || !coarse) return fail(MGX_BAD_ARG, "NULL block");
+    for (int i = 0; i < 3; i++)
+        if (grid->n[i] % 2) return fail(MGX_BAD_ARG, "odd fine dimension");
+    cudaStream_t s = (cudaStream_t)stream;
+    const Level F  = make_level(*grid, 0), C = make_level(*grid, 1);
+    DeviceBuffer a, b;
+    const size_t es = dtype_size(dtype);
+    MGX_TRY(a.ensure(F.npts() * nfunc * es));
+    MGX_TRY(b.ensure(C.npts() * nfunc * es));
+    MGX_TRY(strip(dtype, coarse, ghosts, C.n, b.ptr, nfunc, 0, s));
+    MGX_TRY(prolong_launch(dtype, 0, F, b.ptr, C.npts(), a.ptr, F.npts(), (int)nfunc, MaskDev(), s));
+    MGX_TRY(strip(dtype, fine, ghosts, F.n, a.ptr, nfunc, 1, s));
+    // the reference also injects the first high-side ghost layer; refresh
+    // the fine ghosts so that they hold the periodic images
+    MGX_TRY(ghosted_trade(*grid, ghosts, dtype, fine, nfunc, s));
+    return cuda_check(cudaStreamSynchronize(s), "extend3d sync");
+}
+
+int mgx_fd_apply(mgx_ctx* ctx, int lap_type, mgx_dtype dtype, const void* u,
+    size_t ld, void* out, int nfunc, void* stream)
+{
+    if (!ctx) return fail(MGX_BAD_ARG, "ctx is NULL");
+    MGX_TRY(check_dtype(dtype));
+    MGX_TRY(check_block(ctx->grid, u, ld, nfunc, "u"));
+    MGX_TRY(check_block(ctx->grid, out, ld, nfunc, "out"));
+    if (lap_radius(lap_type) < 0) return fail(MGX_BAD_ARG, "lap_type %d", lap_type);
+    PlaneParams p = plane(ctx->grid);
+    p.u   = u;
+    p.ldu = ld;
+    p.out = out;
+    p.ldo = ld;
+    return stencil_launch(OP_LAP, lap_type, dtype, dtype, p, make_level(ctx->grid, 0),
+        0., nfunc, (cudaStream_t)stream);
+}
+
+int mgx_rhs_mehr(mgx_ctx* ctx, mgx_dtype dtype, const void* u, size_t ld,
+    void* out, int nfunc, void* stream)
+{
+    if (!ctx) return fail(MGX_BAD_ARG, "ctx is NULL");
+    MGX_TRY(check_dtype(dtype));
+    MGX_TRY(check_block(ctx->grid, u, ld, nfunc, "u"));
+    MGX_TRY(check_block(ctx->grid, out, ld, nfunc, "out"));
+    PlaneParams p = plane(ctx->grid);
+    p.u   = u;
+    p.ldu = ld;
+    p.out = out;
+    p.ldo = ld;
+    return stencil_launch(OP_RHS, 0, dtype, dtype, p, make_level(ctx->grid, 0), 0.,
+        nfunc, (cudaStream_t)stream);
+}
+
+int mgx_hpsi(mgx_ctx* ctx, int lap_type, mgx_dtype dtype, const void* psi,
+    size_t ld, const void* V, mgx_dtype v_dtype, void* hpsi, int nfunc,
+    int apply_B_to_V, void* stream)
+{
+    if (!ctx) return fail(MGX_BAD_ARG, "ctx is NULL");
+    MGX_TRY(check_dtype(dtype));
+    MGX_TRY(check_dtype(v_dtype));
+    MGX_TRY(check_block(ctx->grid, psi, ld, nfunc, "psi"));
+    MGX_TRY(check_block(ctx->grid, hpsi, ld, nfunc, "hpsi"));
+    if (nfunc && !V) return fail(MGX_BAD_ARG, "V is NULL");
+    if (lap_radius(lap_type) < 0) return fail(MGX_BAD_ARG, "lap_type %d", lap_type);
+    if (psi == hpsi) return fail(MGX_BAD_ARG, "psi and hpsi alias");
+    PlaneParams p = plane(ctx->grid);
+    p.u   = psi;
+    p.ldu = ld;
+    p.V   = V;
+    p.out = hpsi;
+    p.ldo = ld;
+    const int op = (lap_type == 0 && apply_B_to_V) ? OP_HPSI_B : OP_HPSI_V;
+    return stencil_launch(op, lap_type, dtype, v_dtype, p, make_level(ctx->grid, 0),
+        0., nfunc, (cudaStream_t)stream);
+}
+
+int mgx_mg_restrict(mgx_ctx* ctx, int level, mgx_dtype dtype, const void* fine,
+    void* coarse, int nfunc, void* stream)
+{
+    if (!ctx) return fail(MGX_BAD_ARG, "ctx is NULL");
+    MGX_TRY(check_dtype(dtype));
+    if (level < 0) return fail(MGX_BAD_ARG, "level < 0");
+    const Level F = make_level(ctx->grid, level);
+    for (int i = 0; i < 3; i++)
+        if (F.n[i] < 2 || F.n[i] % 2) return fail(MGX_BAD_ARG, "level %d not coarsenable", level);
+    if (nfunc && (!fine || !coarse)) return fail(MGX_BAD_ARG, "NULL block");
+    if (nfunc == 0) return MGX_OK;
+    return restrict_launch(dtype, F, fine, F.npts(), coarse, F.npts() / 8, nfunc,
+        MaskDev(), (cudaStream_t)stream);
+}
+
+int mgx_mg_prolong(mgx_ctx* ctx, int level, mgx_dtype dtype, const void* coarse,
+    void* fine, int nfunc, void* stream)
+{
+    if (!ctx) return fail(MGX_BAD_ARG, "ctx is NULL");
+    MGX_TRY(check_dtype(dtype));
+    if (level < 0) return fail(MGX_BAD_ARG, "level < 0");
+    const Level F = make_level(ctx->grid, level);
+    for (int i = 0; i < 3; i++)
+        if (F.n[i] < 2 || F.n[i] % 2) return fail(MGX_BAD_ARG, "level %d not coarsenable", level);
+    if (nfunc && (!fine || !coarse)) return fail(MGX_BAD_ARG, "NULL block");
+    if (nfunc == 0) return MGX_OK;
+    return prolong_launch(dtype, 0, F, coarse, F.npts() / 8, fine, F.npts(), nfunc,
+        MaskDev(), (cudaStream_t)stream);
+}
+
+int mgx_precond_mg(mgx_ctx* ctx, const mgx_precond_params* p, mgx_dtype dtype,
+    const void* res, size_t ld, void* out, int nfunc, const mgx_masks* masks,
+    void* stream)
+{
+    if (!ctx) return fail(MGX_BAD_ARG, "ctx is NULL");
+    MGX_TRY(check_dtype(dtype));
+    MGX_TRY(check_block(ctx->grid, res, ld, nfunc, "res"));
+    MGX_TRY(check_block(ctx->grid, out, ld, nfunc, "out"));
+    if (masks && masks->dtype != dtype)
+        return fail(MGX_BAD_ARG, "mask value type differs from the orbital type");
+    const size_t np = (size_t)ctx->grid.n[0] * ctx->grid.n[1] * ctx->grid.n[2];
+    const size_t ldv = nfunc > 1 ? ld : (ld ? ld : np);
+    int st = precond_mg(ctx, p, dtype, res, ldv, out, nfunc, masks, (cudaStream_t)stream);
+    if (st != MGX_OK) return st;
+    return MGX_OK;
+}
+
+int mgx_precond_gamma(const mgx_grid* grid, int lap_type, int mg_levels,
+    double vmax, double small_eig, double* gamma)
+{
+    MGX_TRY(check_grid(grid));
+    if (!gamma) return fail(MGX_BAD_ARG, "gamma is NULL");
+    if (lap_radius(lap_type) < 0) return fail(MGX_BAD_ARG, "lap_type %d", lap_type);
+    const Level L = make_level(*grid, 0);
+    // invDiagEl() of the operator (src/pb/Laph*.h); Laph4M: 1 / ((4/3) sum)
+    const double s = 1. / (L.h[0] * L.h[0]) + 1. / (L.h[1] * L.h[1])
+                     + 1. / (L.h[2] * L.h[2]);
+    double diag = 0.;
+    switch (lap_type)
+    {
+        case 0: diag = (4. / 3.) * s; break;
+        case 1: diag = 2. * s; break;
+        case 2: diag = 2.5 * s; break;
+        case 3: diag = (49. / 18.) * s; break;
+        case 4: diag = (1435. / 504.) * s; break;
+    }
+    double g = 1. / diag;
+    for (int ln = 0; ln <= mg_levels; ln++)
+        g *= 4.;
+    *gamma = 1.0 / (2.0 / g + fabs(vmax - small_eig));
+    return MGX_OK;
+}
+
+int mgx_masks_create(mgx_ctx* ctx, int nlevels, int nfunc, const double* centers,
+    const double* radii, int func, int kind, int mesh_ghosts, mgx_dtype dtype,
+    mgx_masks** masks, void* stream)
+{
+    if (!ctx) return fail(MGX_BAD_ARG, "ctx is NULL");
+    MGX_TRY(check_dtype(dtype));
+    if (mesh_ghosts < 1) return fail(MGX_BAD_ARG, "mesh ghost width < 1");
+    return masks_create(ctx, nlevels, nfunc, centers, radii, func, kind, mesh_ghosts,
+        dtype, masks, (cudaStream_t)stream);
+}
+
+int mgx_masks_destroy(mgx_masks* masks)
+{
+    delete masks;
+    return MGX_OK;
+}
+
+int mgx_masks_apply(mgx_ctx* ctx, const mgx_masks* masks, int level, void* u,
+    size_t ld, int nfunc, void* stream)
+{
+    if (!ctx || !masks) return fail(MGX_BAD_ARG, "NULL ctx or masks");
+    if (nfunc < 0) return fail(MGX_BAD_ARG, "nfunc < 0");
+    if (level < 0) return fail(MGX_BAD_ARG, "level < 0");
+    if (nfunc && !u) return fail(MGX_BAD_ARG, "u is NULL");
+    const Level L = make_level(ctx->grid, level);
+    if (nfunc > 1 && ld < L.npts()) return fail(MGX_BAD_ARG, "ld below level size");
+    return masks_apply(ctx, masks, level, u, ld ? ld : L.npts(), nfunc, (cudaStream_t)stream);
+}
+
+int mgx_masks_expand(const mgx_masks* masks, int level, void* dense,
+    int* host_state, void* stream)
+{
+    if (!masks || !dense) return fail(MGX_BAD_ARG, "NULL masks or output");
+    return masks_expand(masks, level, dense, host_state, (cudaStream_t)stream);
+}
+
+int mgx_gram(mgx_ctx* ctx, int mode, const void* psi, size_t ld, int nfunc,
+    double* S, void* stream)
+{
+    if (!ctx) return fail(MGX_BAD_ARG, "ctx is NULL");
+    MGX_TRY(check_block(ctx->grid, psi, ld, nfunc, "psi"));
+    if (nfunc == 0) return MGX_OK;
+    if (!S) return fail(MGX_BAD_ARG, "S is NULL");
+    const Level L    = make_level(ctx->grid, 0);
+    const double vel = L.h[0] * L.h[1] * L.h[2];
+    const size_t ldv = nfunc > 1 ? ld : L.npts();
+    cudaStream_t s   = (cudaStream_t)stream;
+    switch (mode)
+    {
+        case MGX_GEMM_FP64:
+            return gram_cuda_cores(ctx, MGX_F64, psi, psi, ldv, L.npts(), nfunc, vel, 1, S, s);
+        case MGX_GEMM_FP32:
+            return gram_cuda_cores(ctx, MGX_F32, psi, psi, ldv, L.npts(), nfunc, vel, 1, S, s);
+        case MGX_GEMM_TF32:
+        case MGX_GEMM_BF16X3:
+            return gram_tcgen05(ctx, mode, psi, psi, ldv, L.npts(), nfunc, vel, 1, S, s);
+    }
+    return fail(MGX_BAD_ARG, "gemm mode %d", mode);
+}
+
+int mgx_hmat(mgx_ctx* ctx, int mode, const void* psi, const void* hpsi, size_t ld,
+    int nfunc, double* H, void* stream)
+{
+    if (!ctx) return fail(MGX_BAD_ARG, "ctx is NULL");
+    MGX_TRY(check_block(ctx->grid, psi, ld, nfunc, "psi"));
+    MGX_TRY(check_block(ctx->grid, hpsi, ld, nfunc, "hpsi"));
+    if (nfunc == 0) return MGX_OK;
+    if (!H) return fail(MGX_BAD_ARG, "H is NULL");
+    const Level L    = make_level(ctx->grid, 0);
+    const double vel = L.h[0] * L.h[1] * L.h[2];
+    const size_t ldv = nfunc > 1 ? ld : L.npts();
+    cudaStream_t s   = (cudaStream_t)stream;
+    switch (mode)
+    {
+        case MGX_GEMM_FP64:
+            return gram_cuda_cores(ctx, MGX_F64, psi, hpsi, ldv, L.npts(), nfunc, vel, 0, H, s);
+        case MGX_GEMM_FP32:
+            return gram_cuda_cores(ctx, MGX_F32, psi, hpsi, ldv, L.npts(), nfunc, vel, 0, H, s);
+        case MGX_GEMM_TF32:
+        case MGX_GEMM_BF16X3:
+            return gram_tcgen05(ctx, mode, psi, hpsi, ldv, L.npts(), nfunc, vel, 0, H, s);
+    }
+    return fail(MGX_BAD_ARG, "gemm mode %d", mode);
+}
+
+int mgx_cholesky(mgx_ctx* ctx, int n, double* A, int* info, void* stream)
+{
+    if (!ctx) return fail(MGX_BAD_ARG, "ctx is NULL");
+    return cholesky(ctx, n, A, info, (cudaStream_t)stream);
+}
+
+int mgx_inverse_from_cholesky(mgx_ctx* ctx, int n, const double* L, double* Sinv,
+    void* stream)
+{
+    if (!ctx) return fail(MGX_BAD_ARG, "ctx is NULL");
+    return inverse_from_cholesky(ctx, n, L, Sinv, (cudaStream_t)stream);
+}
+
+int mgx_trace_prod(mgx_ctx* ctx, int n, const double* H, const double* Sinv,
+    double* trace, void* stream)
+{
+    if (!ctx) return fail(MGX_BAD_ARG, "ctx is NULL");
+    return trace_prod(n, H, Sinv, trace, (cudaStream_t)stream);
+}
+
+} // extern "C"

@@ -1,0 +1,482 @@
+// Gram / H-matrix contractions and the small dense FP64 algebra of the
+// orbital hot path on sm_103a:
+//  - S = Psi^T Psi * vel and H = Psi^T (H Psi) * vel as split-K tall-skinny
+//    products on CUDA cores (FP64 data with FP64 FMA, or FP32 data with FP32
+//    FMA per K-slice), FP64 atomics across slices, then the finishing pass
+//    (scale by vel, the |x| > 1e-14 filter of
+//    src/LocalMatrices2DistMatrix.cc:16,60, symmetric fill of S);
+//  - GramMatrix::updateLS / computeInverse (src/GramMatrix.cc:75-191):
+//    blocked right-looking Cholesky with inverted diagonal blocks, the
+//    inverse factor, and S^-1 = L^-T L^-1, all FP64;
+//  - ProjectedMatrices::getEigSum (src/ProjectedMatrices.cc:550-566):
+//    tr(H S^-1) as a device reduction.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "mgx_internal.cuh"
+
+namespace mgx
+{
+
+/* ------------------------------------------------------------------ */
+/* split-K Gram kernel: C[i][j] += sum_p A[i][p] B[j][p]                 */
+/* A, B orbital-major (row i at A + i*ld), 64x64 output tiles.            */
+/* ------------------------------------------------------------------ */
+constexpr int GT  = 64; // output tile
+constexpr int GKC = 32; // k chunk
+
+template <typename T>
+__global__ void __launch_bounds__(256) gram_splitk_kernel(const T* __restrict__ A,
+    const T* __restrict__ B, size_t ld, int n, size_t K, size_t kslice,
+    const int2* __restrict__ tiles, double* __restrict__ C)
+{
+    __shared__ T As[GKC][GT + 1];
+    __shared__ T Bs[GKC][GT + 1];
+    const int2 tile = tiles[blockIdx.x];
+    const int i0 = tile.x * GT, j0 = tile.y * GT;
+    const size_t k0 = (size_t)blockIdx.y * kslice;
+    const size_t k1 = min(K, k0 + kslice);
+    const int tid   = threadIdx.x;
+    const int tx = tid % 16, ty = tid / 16; // 16 x 16 threads, 4x4 outputs each
+    T acc[4][4];
+#pragma unroll
+    for (int a = 0; a < 4; a++)
+#pragma unroll
+        for (int b = 0; b < 4; b++)
+            acc[a][b] = (T)0;
+    for (size_t kc = k0; kc < k1; kc += GKC)
+    {
+        // 64 rows x 32 k for each operand: 2048 elements, 8 per thread
+#pragma unroll
+        for (int r = 0; r < 8; r++)
+        {
+            const int e   = tid + r * 256;
+            const int row = e / GKC;
+            const int kk  = e % GKC;
+            const size_t k = kc + kk;
+            T av = (T)0, bv = (T)0;
+            if (k < k1)
+            {
+                if (i0 + row < n) av = A[(size_t)(i0 + row) * ld + k];
+                if (j0 + row < n) bv = B[(size_t)(j0 + row) * ld + k];
+            }
+            As[kk][row] = av;
+            Bs[kk][row] = bv;
+        }
+        __syncthreads();
+#pragma unroll 8
+        for (int kk = 0; kk < GKC; kk++)
+        {
+            T a[4], b[4];
+#pragma unroll
+            for (int q = 0; q < 4; q++)
+            {
+                a[q] = As[kk][ty + 16 * q];
+                b[q] = Bs[kk][tx + 16 * q];
+            }
+#pragma unroll
+            for (int p = 0; p < 4; p++)
+#pragma unroll
+                for (int q = 0; q < 4; q++)
+                    acc[p][q] += a[p] * b[q];
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int p = 0; p < 4; p++)
+#pragma unroll
+        for (int q = 0; q < 4; q++)
+        {
+            const int i = i0 + ty + 16 * p, j = j0 + tx + 16 * q;
+            if (i < n && j < n) atomicAdd(&C[(size_t)j * n + i], (double)acc[p][q]);
+        }
+}
+
+/* S or H finishing: scale, filter, (S) mirror the lower triangle */
+__global__ void gram_finish_kernel(double* C, int n, double vel, int symmetric)
+{
+    const size_t nn = (size_t)n * n;
+    for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < nn;
+         t += (size_t)gridDim.x * blockDim.x)
+    {
+        const int i = (int)(t % n), j = (int)(t / n);
+        if (symmetric && i < j) continue;
+        double x = C[t] * vel;
+        if (!(fabs(x) > 1.e-14)) x = 0.;
+        C[t] = x;
+        if (symmetric && i != j) C[(size_t)i * n + j] = x;
+    }
+}
+
+int gram_cuda_cores(mgx_ctx* ctx, int dtype, const void* A, const void* B,
+    size_t ld, size_t K, int n, double vel, int symmetric, double* C,
+    cudaStream_t s)
+{
+    const int nt = (n + GT - 1) / GT;
+    std::vector<int2> tiles;
+    for (int j = 0; j < nt; j++)
+        for (int i = 0; i < nt; i++)
+            if (!symmetric || i >= j) tiles.push_back(make_int2(i, j));
+    const int ntiles = (int)tiles.size();
+    int ksplit       = std::max(1, (8 * ctx->sm_count + ntiles - 1) / ntiles);
+    size_t kslice    = (K + ksplit - 1) / ksplit;
+    kslice           = ((kslice + GKC - 1) / GKC) * GKC;
+    ksplit           = (int)((K + kslice - 1) / kslice);
+    if (ksplit > 65535) return fail(MGX_UNSUPPORTED, "K too large for split");
+    MGX_TRY(ctx->gemm_ws.ensure(tiles.size() * sizeof(int2)));
+    MGX_TRY(cuda_check(cudaMemcpyAsync(ctx->gemm_ws.ptr, tiles.data(),
+                           tiles.size() * sizeof(int2), cudaMemcpyHostToDevice, s),
+        "gram tiles upload"));
+    MGX_TRY(cuda_check(cudaMemsetAsync(C, 0, (size_t)n * n * sizeof(double), s),
+        "gram zero"));
+    dim3 grid(ntiles, ksplit);
+    if (dtype == MGX_F64)
+        gram_splitk_kernel<double><<<grid, 256, 0, s>>>((const double*)A,
+            (const double*)B, ld, n, K, kslice, (const int2*)ctx->gemm_ws.ptr, C);
+    else
+        gram_splitk_kernel<float><<<grid, 256, 0, s>>>((const float*)A,
+            (const float*)B, ld, n, K, kslice, (const int2*)ctx->gemm_ws.ptr, C);
+    MGX_LAUNCH_CHECK("gram_splitk_kernel");
+    // the tile list must stay alive until the kernel has read it
+    MGX_TRY(cuda_check(cudaStreamSynchronize(s), "gram sync"));
+    const int nb = (int)std::min<size_t>(((size_t)n * n + 255) / 256, 4096);
+    gram_finish_kernel<<<nb, 256, 0, s>>>(C, n, vel, symmetric);
+    MGX_LAUNCH_CHECK("gram_finish_kernel");
+    return MGX_OK;
+}
+
+/* ------------------------------------------------------------------ */
+/* generic FP64 GEMM, column-major: C = alpha op(A) op(B) + beta C        */
+/* ------------------------------------------------------------------ */
+template <bool TA, bool TB>
+__global__ void __launch_bounds__(256) dgemm_kernel(int m, int n, int k,
+    double alpha, const double* __restrict__ A, int lda,
+    const double* __restrict__ B, int ldb, double beta, double* C, int ldc,
+    int lower_only)
+{
+    __shared__ double As[16][65];
+    __shared__ double Bs[16][65];
+    const int i0 = blockIdx.x * 64, j0 = blockIdx.y * 64;
+    if (lower_only && i0 + 63 < j0) return;
+    const int tid = threadIdx.x, tx = tid % 16, ty = tid / 16;
+    double acc[4][4] = {};
+    for (int kc = 0; kc < k; kc += 16)
+    {
+#pragma unroll
+        for (int r = 0; r < 4; r++)
+        {
+            const int e  = tid + r * 256;
+            const int mm = e % 64, kk = e / 64;
+            const int i = i0 + mm, j = j0 + mm, kq = kc + kk;
+            double av = 0., bv = 0.;
+            if (i < m && kq < k) av = TA ? A[(size_t)i * lda + kq] : A[(size_t)kq * lda + i];
+            if (j < n && kq < k) bv = TB ? B[(size_t)kq * ldb + j] : B[(size_t)j * ldb + kq];
+            As[kk][mm] = av;
+            Bs[kk][mm] = bv;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int kk = 0; kk < 16; kk++)
+        {
+            double a[4], b[4];
+#pragma unroll
+            for (int q = 0; q < 4; q++)
+            {
+                a[q] = As[kk][ty + 16 * q];
+                b[q] = Bs[kk][tx + 16 * q];
+            }
+#pragma unroll
+            for (int p = 0; p < 4; p++)
+#pragma unroll
+                for (int q = 0; q < 4; q++)
+                    acc[p][q] = fma(a[p], b[q], acc[p][q]);
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int p = 0; p < 4; p++)
+#pragma unroll
+        for (int q = 0; q < 4; q++)
+        {
+            const int i = i0 + ty + 16 * p, j = j0 + tx + 16 * q;
+            if (i < m && j < n && (!lower_only || i >= j))
+            {
+                double* c = C + (size_t)j * ldc + i;
+                *c        = alpha * acc[p][q] + (beta == 0. ? 0. : beta * *c);
+            }
+        }
+}
+
+static int dgemm(bool ta, bool tb, int m, int n, int k, double alpha,
+    const double* A, int lda, const double* B, int ldb, double beta, double* C,
+    int ldc, int lower_only, cudaStream_t s)
+{
+    if (m <= 0 || n <= 0) return MGX_OK;
+    dim3 grid((m + 63) / 64, (n + 63) / 64);
+    if (!ta && !tb)
+        dgemm_kernel<false, false><<<grid, 256, 0, s>>>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, lower_only);
+    else if (!ta && tb)
+        dgemm_kernel<false, true><<<grid, 256, 0, s>>>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, lower_only);
+    else if (ta && !tb)
+        dgemm_kernel<true, false><<<grid, 256, 0, s>>>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, lower_only);
+    else
+        dgemm_kernel<true, true><<<grid, 256, 0, s>>>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, lower_only);
+    MGX_LAUNCH_CHECK("dgemm_kernel");
+    return MGX_OK;
+}
+
+/* ------------------------------------------------------------------ */
+/* Cholesky                                                             */
+/* ------------------------------------------------------------------ */
+constexpr int NB        = 64;
+constexpr int DIAG_SMEM = 2 * NB * (NB + 1) * sizeof(double);
+
+/* Factor the diagonal block A[k0:k0+nb, k0:k0+nb] (lower), write L_kk in
+ * place (upper part zeroed) and its inverse W (nb x nb, column-major, ld
+ * NB) to `winv`.  Sets *info to the 1-based global pivot index on failure. */
+__global__ void __launch_bounds__(256) potrf_diag_kernel(double* A, int n, int k0,
+    int nb, double* winv, int* info)
+{
+    extern __shared__ double dsm[];
+    double(*L)[NB + 1] = reinterpret_cast<double(*)[NB + 1]>(dsm);
+    double(*W)[NB + 1] = reinterpret_cast<double(*)[NB + 1]>(dsm + NB * (NB + 1));
+    __shared__ int bad;
+    if (*info != 0) return;
+    const int tid = threadIdx.x;
+    for (int e = tid; e < nb * nb; e += blockDim.x)
+    {
+        const int i = e % nb, j = e / nb;
+        L[i][j]     = (i >= j) ? A[(size_t)(k0 + j) * n + k0 + i] : 0.;
+    }
+    if (tid == 0) bad = 0;
+    __syncthreads();
+    for (int j = 0; j < nb; j++)
+    {
+        if (tid == 0)
+        {
+            const double d = L[j][j];
+            if (!(d > 0.) || !isfinite(d))
+                bad = k0 + j + 1;
+            else
+                L[j][j] = sqrt(d);
+        }
+        __syncthreads();
+        if (bad) break;
+        const double djj = L[j][j];
+        for (int i = j + 1 + tid; i < nb; i += blockDim.x)
+            L[i][j] /= djj;
+        __syncthreads();
+        // trailing update of the block (lower part)
+        for (int e = tid; e < nb * nb; e += blockDim.x)
+        {
+            const int i = e % nb, c = e / nb;
+            if (c > j && i >= c) L[i][c] -= L[i][j] * L[c][j];
+        }
+        __syncthreads();
+    }
+    if (bad)
+    {
+        if (tid == 0) atomicCAS(info, 0, bad);
+        return;
+    }
+    // inverse of the lower-triangular block, column by column
+    for (int e = tid; e < nb * nb; e += blockDim.x)
+        W[e % nb][e / nb] = 0.;
+    __syncthreads();
+    for (int c = tid; c < nb; c += blockDim.x)
+    {
+        W[c][c] = 1. / L[c][c];
+        for (int i = c + 1; i < nb; i++)
+        {
+            double s = 0.;
+            for (int q = c; q < i; q++)
+                s -= L[i][q] * W[q][c];
+            W[i][c] = s / L[i][i];
+        }
+    }
+    __syncthreads();
+    for (int e = tid; e < nb * nb; e += blockDim.x)
+    {
+        const int i = e % nb, j = e / nb;
+        A[(size_t)(k0 + j) * n + k0 + i] = (i >= j) ? L[i][j] : 0.;
+        winv[(size_t)j * NB + i]         = W[i][j];
+    }
+}
+
+__global__ void copy_panel_kernel(const double* src, int lds, double* dst,
+    int ldd, int m, int nb)
+{
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < m * nb;
+         e += gridDim.x * blockDim.x)
+    {
+        const int i = e % m, j = e / m;
+        dst[(size_t)j * ldd + i] = src[(size_t)j * lds + i];
+    }
+}
+
+__global__ void zero_upper_kernel(double* A, int n)
+{
+    const size_t nn = (size_t)n * n;
+    for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < nn;
+         t += (size_t)gridDim.x * blockDim.x)
+    {
+        const int i = (int)(t % n), j = (int)(t / n);
+        if (i < j) A[t] = 0.;
+    }
+}
+
+/* workspace: diagonal inverses (nblocks x NB x NB) + panel (n x NB) + X */
+static int dense_ws(mgx_ctx* ctx, int n, double** winv, double** panel,
+    double** X, int** info)
+{
+    const int nbk = (n + NB - 1) / NB;
+    const size_t b_w = (size_t)nbk * NB * NB * 8, b_p = (size_t)n * NB * 8,
+                 b_x = (size_t)n * n * 8;
+    MGX_TRY(ctx->dense_ws.ensure(b_w + b_p + b_x + 256));
+    char* base = (char*)ctx->dense_ws.ptr;
+    *winv      = (double*)base;
+    *panel     = (double*)(base + b_w);
+    *X         = (double*)(base + b_w + b_p);
+    *info      = (int*)(base + b_w + b_p + b_x);
+    return MGX_OK;
+}
+
+int cholesky(mgx_ctx* ctx, int n, double* A, int* info_host, cudaStream_t s)
+{
+    if (n <= 0 || !A || !info_host) return fail(MGX_BAD_ARG, "cholesky: bad arguments");
+    double *winv, *panel, *X;
+    int* dinfo;
+    MGX_TRY(dense_ws(ctx, n, &winv, &panel, &X, &dinfo));
+    MGX_TRY(cuda_check(cudaMemsetAsync(dinfo, 0, sizeof(int), s), "info reset"));
+    MGX_TRY(cuda_check(cudaFuncSetAttribute(potrf_diag_kernel,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize, DIAG_SMEM),
+        "potrf smem attribute"));
+    const int nbk = (n + NB - 1) / NB;
+    for (int kb = 0; kb < nbk; kb++)
+    {
+        const int k0 = kb * NB, nb = std::min(NB, n - k0);
+        potrf_diag_kernel<<<1, 256, DIAG_SMEM, s>>>(A, n, k0, nb, winv + (size_t)kb * NB * NB, dinfo);
+        MGX_LAUNCH_CHECK("potrf_diag_kernel");
+        const int m = n - k0 - nb; // rows below the block
+        if (m <= 0) continue;
+        double* Ap = A + (size_t)k0 * n + k0 + nb; // panel A[k0+nb:, k0:k0+nb]
+        // panel <- A_panel * W^T   (L_ik = A_ik L_kk^-T)
+        MGX_TRY(dgemm(false, true, m, nb, nb, 1., Ap, n, winv + (size_t)kb * NB * NB,
+            NB, 0., panel, n, 0, s));
+        copy_panel_kernel<<<std::min(1024, (m * nb + 255) / 256), 256, 0, s>>>(panel, n, Ap, n, m, nb);
+        MGX_LAUNCH_CHECK("copy_panel_kernel");
+        // trailing update A22 -= P P^T (lower)
+        double* A22 = A + (size_t)(k0 + nb) * n + k0 + nb;
+        MGX_TRY(dgemm(false, true, m, m, nb, -1., panel, n, panel, n, 1., A22, n, 1, s));
+    }
+    zero_upper_kernel<<<std::min<size_t>(((size_t)n * n + 255) / 256, 4096), 256, 0, s>>>(A, n);
+    MGX_LAUNCH_CHECK("zero_upper_kernel");
+    int hinfo = 0;
+    MGX_TRY(cuda_check(cudaMemcpyAsync(&hinfo, dinfo, sizeof(int), cudaMemcpyDeviceToHost, s),
+        "info download"));
+    MGX_TRY(cuda_check(cudaStreamSynchronize(s), "cholesky sync"));
+    *info_host = hinfo;
+    if (hinfo != 0) return fail(MGX_NOT_SPD, "Cholesky: leading minor %d not positive", hinfo);
+    return MGX_OK;
+}
+
+/* inverse of a lower-triangular factor, blocked by rows:
+ * X_ii = L_ii^-1 ; X_i,0:i = -X_ii (L_i,0:i X_0:i,0:i) */
+__global__ void __launch_bounds__(256) trinv_diag_kernel(const double* L, int n,
+    double* X)
+{
+    extern __shared__ double dsm[];
+    double(*T)[NB + 1] = reinterpret_cast<double(*)[NB + 1]>(dsm);
+    double(*W)[NB + 1] = reinterpret_cast<double(*)[NB + 1]>(dsm + NB * (NB + 1));
+    const int kb = blockIdx.x, k0 = kb * NB, nb = min(NB, n - k0);
+    const int tid = threadIdx.x;
+    for (int e = tid; e < nb * nb; e += blockDim.x)
+    {
+        const int i = e % nb, j = e / nb;
+        T[i][j]     = (i >= j) ? L[(size_t)(k0 + j) * n + k0 + i] : 0.;
+        W[i][j]     = 0.;
+    }
+    __syncthreads();
+    for (int c = tid; c < nb; c += blockDim.x)
+    {
+        W[c][c] = 1. / T[c][c];
+        for (int i = c + 1; i < nb; i++)
+        {
+            double s = 0.;
+            for (int q = c; q < i; q++)
+                s -= T[i][q] * W[q][c];
+            W[i][c] = s / T[i][i];
+        }
+    }
+    __syncthreads();
+    for (int e = tid; e < nb * nb; e += blockDim.x)
+    {
+        const int i = e % nb, j = e / nb;
+        X[(size_t)(k0 + j) * n + k0 + i] = W[i][j];
+    }
+}
+
+int inverse_from_cholesky(mgx_ctx* ctx, int n, const double* L, double* Sinv,
+    cudaStream_t s)
+{
+    if (n <= 0 || !L || !Sinv) return fail(MGX_BAD_ARG, "inverse: bad arguments");
+    double *winv, *panel, *X;
+    int* dinfo;
+    MGX_TRY(dense_ws(ctx, n, &winv, &panel, &X, &dinfo));
+    MGX_TRY(cuda_check(cudaMemsetAsync(X, 0, (size_t)n * n * 8, s), "X zero"));
+    const int nbk = (n + NB - 1) / NB;
+    MGX_TRY(cuda_check(cudaFuncSetAttribute(trinv_diag_kernel,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize, DIAG_SMEM),
+        "trinv smem attribute"));
+    trinv_diag_kernel<<<nbk, 256, DIAG_SMEM, s>>>(L, n, X);
+    MGX_LAUNCH_CHECK("trinv_diag_kernel");
+    for (int kb = 1; kb < nbk; kb++)
+    {
+        const int k0 = kb * NB, nb = std::min(NB, n - k0);
+        // panel(nb x k0) = L[k0:k0+nb, 0:k0] * X[0:k0, 0:k0]
+        MGX_TRY(dgemm(false, false, nb, k0, k0, 1., L + k0, n, X, n, 0., panel, nb, 0, s));
+        // X[k0:k0+nb, 0:k0] = -X_kk * panel
+        MGX_TRY(dgemm(false, false, nb, k0, nb, -1., X + (size_t)k0 * n + k0, n, panel,
+            nb, 0., X + k0, n, 0, s));
+    }
+    // S^-1 = X^T X
+    MGX_TRY(dgemm(true, false, n, n, n, 1., X, n, X, n, 0., Sinv, n, 0, s));
+    return MGX_OK;
+}
+
+__global__ void trace_prod_kernel(const double* H, const double* Sinv, int n,
+    double* out)
+{
+    __shared__ double red[256];
+    double acc      = 0.;
+    const size_t nn = (size_t)n * n;
+    for (size_t t = threadIdx.x; t < nn; t += blockDim.x)
+    {
+        const int i = (int)(t % n), k = (int)(t / n);
+        // H used as symmetric from its lower triangle; Sinv(k, i)
+        const double h = (i >= k) ? H[(size_t)k * n + i] : H[(size_t)i * n + k];
+        acc += h * Sinv[(size_t)i * n + k];
+    }
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1)
+    {
+        if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *out = red[0];
+}
+
+int trace_prod(int n, const double* H, const double* Sinv, double* out,
+    cudaStream_t s)
+{
+    if (n <= 0 || !H || !Sinv || !out) return fail(MGX_BAD_ARG, "trace: bad arguments");
+    trace_prod_kernel<<<1, 256, 0, s>>>(H, Sinv, n, out);
+    MGX_LAUNCH_CHECK("trace_prod_kernel");
+    return MGX_OK;
+}
+
+} // namespace mgx

@@ -1,0 +1,808 @@
+// Multigrid transfers, localization masks and the block V-cycle of the
+// orbital preconditioner on sm_103a.
+//
+//  - restriction: full weighting (8,4,2,1)/64 around fine point 2i
+//    (pb::MGkernelRestrict3D, src/pb/MGkernels.cc:203-283), with the
+//    coarse-level mask in the epilogue;
+//  - prolongation: injection at even points and 1-D / 2-D / 3-D averages at
+//    odd points (pb::MGkernelExtend3D, src/pb/MGkernels.cc:28-201), fused
+//    with the fine-level mask and the correction v -= P e;
+//  - masks: GridMask::init (src/GridMask.cc:120-264) evaluated on the device
+//    over a periodic bounding box per orbital and level, with the per-axis
+//    point coordinates formed on the host by the reference's repeated
+//    addition so that membership tests are bit-identical;
+//  - Preconditioning<T>::mg (src/Preconditioning.cc:155-216) driven from the
+//    host: Jacobi sweeps (stencil engine, OP_JACOBI), restriction,
+//    recursion with Laph2 on coarse grids, prolongation-correction.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "mgx_internal.cuh"
+#include "mgx_stencil.cuh"
+
+namespace mgx
+{
+
+/* ------------------------------------------------------------------ */
+/* transfers                                                            */
+/* ------------------------------------------------------------------ */
+__device__ __forceinline__ int wrp(int i, int n)
+{
+    return i < 0 ? i + n : (i >= n ? i - n : i);
+}
+
+template <typename T>
+__device__ __forceinline__ T mask_point(const MaskDev& m, int f, int x, int y,
+    int z, T v)
+{
+    if (m.state == nullptr) return v;
+    const int st = m.state[f];
+    if (st == 1) return v;
+    if (st <= 0) return (T)0;
+    const int* b = m.box + 6 * f;
+    int dx = x - b[0];
+    if (dx < 0) dx += m.n[0];
+    int dy = y - b[1];
+    if (dy < 0) dy += m.n[1];
+    int dz = z - b[2];
+    if (dz < 0) dz += m.n[2];
+    T mv = (T)0;
+    if (dx < b[3] && dy < b[4] && dz < b[5])
+        mv = reinterpret_cast<const T*>(m.values)[m.offset[f]
+                                                  + ((size_t)dx * b[4] + dy) * b[5]
+                                                  + dz];
+    if (m.kind == 0)
+    {
+        if (v > mv) return mv;
+        if (v < -mv) return -mv;
+        return v;
+    }
+    return v * mv;
+}
+
+/* restriction of nfunc functions; accumulation type A (double for the FP64
+ * path, as the reference; float for the FP32 path) */
+template <typename T, typename A>
+__global__ void restrict_kernel(const T* fine, size_t ldf, T* coarse, size_t ldc,
+    int fx, int fy, int fz, MaskDev mask)
+{
+    const int cx = fx >> 1, cy = fy >> 1, cz = fz >> 1;
+    const size_t cn = (size_t)cx * cy * cz;
+    const int f     = blockIdx.y;
+    const T* u      = fine + (size_t)f * ldf;
+    for (size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x; idx < cn;
+         idx += (size_t)gridDim.x * blockDim.x)
+    {
+        const int k = (int)(idx % cz);
+        const int j = (int)((idx / cz) % cy);
+        const int i = (int)(idx / ((size_t)cz * cy));
+        const int x = 2 * i, y = 2 * j, z = 2 * k;
+        const int xm = wrp(x - 1, fx), xp = wrp(x + 1, fx);
+        const int ym = wrp(y - 1, fy), yp = wrp(y + 1, fy);
+        const int zm = wrp(z - 1, fz), zp = wrp(z + 1, fz);
+        auto U = [&](int a, int b, int c) -> A {
+            return (A)u[((size_t)a * fy + b) * fz + c];
+        };
+        const A face = U(xp, y, z) + U(xm, y, z) + U(x, yp, z) + U(x, ym, z)
+                       + U(x, y, zm) + U(x, y, zp);
+        const A corner = U(xp, yp, zm) + U(xp, yp, zp) + U(xp, ym, zm)
+                         + U(xp, ym, zp) + U(xm, yp, zm) + U(xm, yp, zp)
+                         + U(xm, ym, zm) + U(xm, ym, zp);
+        const A edge = U(x, yp, zm) + U(x, yp, zp) + U(x, ym, zm) + U(x, ym, zp)
+                       + U(xp, y, zm) + U(xp, y, zp) + U(xm, y, zm)
+                       + U(xm, y, zp) + U(xm, ym, z) + U(xp, ym, z)
+                       + U(xm, yp, z) + U(xp, yp, z);
+        const A r = (A)(1. / 64.)
+                    * ((A)8. * U(x, y, z) + (A)4. * face + (A)2. * edge + corner);
+        coarse[(size_t)f * ldc + idx] = mask_point<T>(mask, f, i, j, k, (T)r);
+    }
+}
+
+/* trilinear prolongation; MODE 0: out = P e; MODE 1: out -= mask(P e) */
+template <typename T, int MODE>
+__global__ void prolong_kernel(const T* coarse, size_t ldc, T* out, size_t ldo,
+    int fx, int fy, int fz, MaskDev mask)
+{
+    const int cx = fx >> 1, cy = fy >> 1, cz = fz >> 1;
+    const size_t fn = (size_t)fx * fy * fz;
+    const int f     = blockIdx.y;
+    const T* e      = coarse + (size_t)f * ldc;
+    for (size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x; idx < fn;
+         idx += (size_t)gridDim.x * blockDim.x)
+    {
+        const int z = (int)(idx % fz);
+        const int y = (int)((idx / fz) % fy);
+        const int x = (int)(idx / ((size_t)fz * fy));
+        const int i = x >> 1, j = y >> 1, k = z >> 1;
+        const int a = x & 1, b = y & 1, c = z & 1;
+        const int i1 = wrp(i + 1, cx), j1 = wrp(j + 1, cy), k1 = wrp(k + 1, cz);
+        auto C = [&](int p, int q, int r) -> T {
+            return e[((size_t)p * cy + q) * cz + r];
+        };
+        T v;
+        // operation order of src/pb/MGkernels.cc:84-197
+        if (!a && !b && !c)
+            v = C(i, j, k);
+        else if (!a && !b && c)
+            v = (T)0.5 * (C(i, j, k) + C(i, j, k1));
+        else if (!a && b && !c)
+            v = (T)0.5 * (C(i, j1, k) + C(i, j, k));
+        else if (!a && b && c)
+            v = (T)0.25 * (C(i, j1, k1) + C(i, j, k1) + C(i, j1, k) + C(i, j, k));
+        else if (a && !b && c)
+            v = (T)0.25 * (C(i1, j, k1) + C(i1, j, k) + C(i, j, k1) + C(i, j, k));
+        else if (a && !b && !c)
+            v = (T)0.5 * (C(i1, j, k) + C(i, j, k));
+        else if (a && b && c)
+            v = (T)0.125
+                * (C(i1, j1, k1) + C(i1, j1, k) + C(i1, j, k1) + C(i1, j, k)
+                    + C(i, j1, k1) + C(i, j1, k) + C(i, j, k1) + C(i, j, k));
+        else
+            v = (T)0.25 * (C(i1, j1, k) + C(i1, j, k) + C(i, j1, k) + C(i, j, k));
+        T* o = out + (size_t)f * ldo + idx;
+        if (MODE == 0)
+            *o = v;
+        else
+            *o = *o - mask_point<T>(mask, f, x, y, z, v);
+    }
+}
+
+template <typename T>
+__global__ void scale_kernel(const T* in, size_t ldi, T* out, size_t ldo,
+    size_t npts, T alpha)
+{
+    const int f = blockIdx.y;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < npts;
+         i += (size_t)gridDim.x * blockDim.x)
+        out[(size_t)f * ldo + i] = alpha * in[(size_t)f * ldi + i];
+}
+
+template <typename T>
+__global__ void mask_apply_kernel(T* u, size_t ld, int nx, int ny, int nz,
+    MaskDev mask)
+{
+    const int f       = blockIdx.y;
+    const size_t npts = (size_t)nx * ny * nz;
+    for (size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x; idx < npts;
+         idx += (size_t)gridDim.x * blockDim.x)
+    {
+        const int z = (int)(idx % nz);
+        const int y = (int)((idx / nz) % ny);
+        const int x = (int)(idx / ((size_t)nz * ny));
+        T* p        = u + (size_t)f * ld + idx;
+        *p          = mask_point<T>(mask, f, x, y, z, *p);
+    }
+}
+
+static dim3 grid_for(size_t npts, int nfunc)
+{
+    const int bx = (int)std::min<size_t>((npts + 255) / 256, 2048);
+    return dim3(bx, nfunc);
+}
+
+int restrict_launch(int dtype, const Level& fine, const void* f, size_t ldf,
+    void* c, size_t ldc, int nfunc, const MaskDev& mask, cudaStream_t s)
+{
+    const size_t cn = fine.npts() / 8;
+    const dim3 g    = grid_for(cn, nfunc);
+    if (dtype == MGX_F64)
+        restrict_kernel<double, double><<<g, 256, 0, s>>>((const double*)f, ldf,
+            (double*)c, ldc, fine.n[0], fine.n[1], fine.n[2], mask);
+    else
+        restrict_kernel<float, float><<<g, 256, 0, s>>>((const float*)f, ldf,
+            (float*)c, ldc, fine.n[0], fine.n[1], fine.n[2], mask);
+    MGX_LAUNCH_CHECK("restrict_kernel");
+    return MGX_OK;
+}
+
+int prolong_launch(int dtype, int mode, const Level& fine, const void* c,
+    size_t ldc, void* out, size_t ldo, int nfunc, const MaskDev& mask,
+    cudaStream_t s)
+{
+    const dim3 g = grid_for(fine.npts(), nfunc);
+    if (dtype == MGX_F64)
+    {
+        if (mode == 0)
+            prolong_kernel<double, 0><<<g, 256, 0, s>>>((const double*)c, ldc,
+                (double*)out, ldo, fine.n[0], fine.n[1], fine.n[2], mask);
+        else
+            prolong_kernel<double, 1><<<g, 256, 0, s>>>((const double*)c, ldc,
+                (double*)out, ldo, fine.n[0], fine.n[1], fine.n[2], mask);
+    }
+    else
+    {
+        if (mode == 0)
+            prolong_kernel<float, 0><<<g, 256, 0, s>>>((const float*)c, ldc,
+                (float*)out, ldo, fine.n[0], fine.n[1], fine.n[2], mask);
+        else
+            prolong_kernel<float, 1><<<g, 256, 0, s>>>((const float*)c, ldc,
+                (float*)out, ldo, fine.n[0], fine.n[1], fine.n[2], mask);
+    }
+    MGX_LAUNCH_CHECK("prolong_kernel");
+    return MGX_OK;
+}
+
+int scale_launch(int dtype, const void* in, size_t ldi, void* out, size_t ldo,
+    size_t npts, int nfunc, double alpha, cudaStream_t s)
+{
+    const dim3 g = grid_for(npts, nfunc);
+    if (dtype == MGX_F64)
+        scale_kernel<double><<<g, 256, 0, s>>>((const double*)in, ldi,
+            (double*)out, ldo, npts, alpha);
+    else
+        scale_kernel<float><<<g, 256, 0, s>>>((const float*)in, ldi,
+            (float*)out, ldo, npts, (float)alpha);
+    MGX_LAUNCH_CHECK("scale_kernel");
+    return MGX_OK;
+}
+
+/* ------------------------------------------------------------------ */
+/* masks                                                                */
+/* ------------------------------------------------------------------ */
+struct MaskJob
+{
+    double center[3];
+    double rcut;
+    double rc_inv;
+    double overlap_radius;
+    int box[6];
+    size_t offset;
+    int func;
+};
+
+/* GridMask::init over the box of one (orbital, level) job; grid-stride
+ * over the box points of all jobs of the level. */
+template <typename M>
+__global__ void mask_values_kernel(const MaskJob* jobs, int njobs,
+    const double* cx, const double* cy, const double* cz, int nx, int ny,
+    int nz, double llx, double lly, double llz, double exp2_rc,
+    double exp2_coeff, M* values, unsigned long long* counts)
+{
+    const int j = blockIdx.y;
+    if (j >= njobs) return;
+    const MaskJob& J = jobs[j];
+    const size_t nb  = (size_t)J.box[3] * J.box[4] * J.box[5];
+    unsigned long long ni = 0, nc = 0;
+    for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < nb;
+         t += (size_t)gridDim.x * blockDim.x)
+    {
+        const int dz = (int)(t % J.box[5]);
+        const int dy = (int)((t / J.box[5]) % J.box[4]);
+        const int dx = (int)(t / ((size_t)J.box[5] * J.box[4]));
+        int x = J.box[0] + dx;
+        if (x >= nx) x -= nx;
+        int y = J.box[1] + dy;
+        if (y >= ny) y -= ny;
+        int z = J.box[2] + dz;
+        if (z >= nz) z -= nz;
+        // Vector3D::minimage (src/tools/Vector3D.cc:13-30), no contraction
+        const double d0 = remainder(__dsub_rn(cx[x], J.center[0]), llx);
+        const double d1 = remainder(__dsub_rn(cy[y], J.center[1]), lly);
+        const double d2 = remainder(__dsub_rn(cz[z], J.center[2]), llz);
+        const double r
+            = sqrt(__dadd_rn(__dadd_rn(__dmul_rn(d0, d0), __dmul_rn(d1, d1)),
+                __dmul_rn(d2, d2)));
+        M val = (M)0;
+        if (r < J.overlap_radius)
+        {
+            ni++;
+            if (r <= J.rcut)
+            {
+                nc++;
+                const double rr = __dmul_rn(r, J.rc_inv);
+                if (J.func == 0)
+                {
+                    // gaussianDecay, src/MasksSet.cc:37-48
+                    float fv = 1.f;
+                    if (rr > 0.75)
+                    {
+                        const double t1 = __dsub_rn(rr, 0.75);
+                        const double ex = exp(__dmul_rn(__dmul_rn(-32., t1), t1));
+                        fv              = (float)__dmul_rn(__dsub_rn(ex, exp2_rc),
+                            exp2_coeff);
+                    }
+                    val = (M)fv;
+                }
+                else
+                {
+                    // one, src/MasksSet.cc:26-35
+                    if (rr < 0.99999)
+                        val = (M)1.;
+                    else
+                        val = (M)__dmul_rn(__dsub_rn(1., rr), 1. / (1. - 0.99999));
+                }
+            }
+        }
+        values[J.offset + t] = val;
+    }
+    // warp reduction of the counts
+    for (int o = 16; o > 0; o >>= 1)
+    {
+        ni += __shfl_down_sync(0xffffffffu, ni, o);
+        nc += __shfl_down_sync(0xffffffffu, nc, o);
+    }
+    if ((threadIdx.x & 31) == 0)
+    {
+        atomicAdd(counts + 2 * j, ni);
+        atomicAdd(counts + 2 * j + 1, nc);
+    }
+}
+
+/* SubCell::spherePossibleOverlap for the single subdomain of a level
+ * (src/SubCell.cc:14-95) */
+static bool sphere_overlap(const double center[3], double radius,
+    const double ll[3], const int dims[3], const double hs[3])
+{
+    double vd[3];
+    for (int i = 0; i < 3; i++)
+    {
+        const double subdim = (dims[i] - 1) * hs[i];
+        const double cc     = 0. + 0.5 * subdim;
+        const double d      = cc - center[i];
+        double r            = fmod(d, ll[i]);
+        const double ax2    = 0.5 * ll[i];
+        if (r > ax2)
+            r -= ll[i];
+        else if (r < -ax2)
+            r += ll[i];
+        const double vc = r < 0. ? std::max(-0.5 * subdim, r) : std::min(0.5 * subdim, r);
+        vd[i]           = r - vc;
+    }
+    const double dc = sqrt(vd[0] * vd[0] + vd[1] * vd[1] + vd[2] * vd[2]);
+    return dc <= radius;
+}
+
+int masks_create(mgx_ctx* ctx, int nlevels, int nfunc, const double* centers,
+    const double* radii, int func, int kind, int mesh_ghosts, int dtype,
+    mgx_masks** out, cudaStream_t s)
+{
+    if (nlevels < 1 || nlevels > 8 || nfunc < 1 || !centers || !radii || !out)
+        return fail(MGX_BAD_ARG, "masks_create: bad arguments");
+    if (func != 0 && func != 1) return fail(MGX_BAD_ARG, "mask func %d", func);
+    if (kind != 0 && kind != 1) return fail(MGX_BAD_ARG, "mask kind %d", kind);
+    const mgx_grid& g = ctx->grid;
+    mgx_masks* M      = new mgx_masks;
+    M->nlevels = nlevels;
+    M->nfunc   = nfunc;
+    M->kind    = kind;
+    M->dtype   = dtype;
+    for (int i = 0; i < 3; i++)
+        M->n[i] = g.n[i];
+    M->state.resize(nlevels);
+    M->box.resize(nlevels);
+    M->offset.resize(nlevels);
+    M->values.resize(nlevels);
+    M->h_state.resize(nlevels);
+    M->h_box.resize(nlevels);
+    M->dev.resize(nlevels);
+
+    const double h[3] = { g.ll[0] / g.n[0], g.ll[1] / g.n[1], g.ll[2] / g.n[2] };
+    const double exp2_rc    = exp(-32. * (1. - 0.75) * (1. - 0.75));
+    const double exp2_coeff = 1. / (1. - exp2_rc);
+    const size_t esz        = dtype_size(dtype);
+    DeviceBuffer d_coords, d_jobs, d_counts;
+
+    for (int l = 0; l < nlevels; l++)
+    {
+        const int nl[3] = { g.n[0] >> l, g.n[1] >> l, g.n[2] >> l };
+        double delta = sqrt(h[0] * h[0] + h[1] * h[1] + h[2] * h[2]) + 1.e-8;
+        delta *= (double)mesh_ghosts;
+        for (int k = 0; k < l; k++)
+            delta *= 2.;
+        double hs[3] = { h[0], h[1], h[2] };
+        for (int k = 0; k < l; k++)
+            for (int i = 0; i < 3; i++)
+                hs[i] *= 2.;
+        const double hl[3] = { h[0] * (1 << l), h[1] * (1 << l), h[2] * (1 << l) };
+        // per-axis coordinates by repeated addition (src/GridMask.cc:190-234)
+        std::vector<double> coords(nl[0] + nl[1] + nl[2]);
+        {
+            size_t o = 0;
+            for (int i = 0; i < 3; i++)
+            {
+                double xc = 0.;
+                for (int k = 0; k < nl[i]; k++)
+                {
+                    coords[o++] = xc;
+                    xc += hl[i];
+                }
+            }
+        }
+        std::vector<int>& st = M->h_state[l];
+        std::vector<int>& bx = M->h_box[l];
+        st.assign(nfunc, 0);
+        bx.assign(6 * (size_t)nfunc, 0);
+        std::vector<size_t> offs(nfunc, 0);
+        std::vector<MaskJob> jobs;
+        size_t total = 0;
+        for (int f = 0; f < nfunc; f++)
+        {
+            const double* c  = centers + 3 * f;
+            const double rc  = radii[f];
+            const double ovr = rc + delta;
+            if (!(rc > 0.001))
+            {
+                delete M;
+                return fail(MGX_BAD_ARG, "mask radius %g too small", rc);
+            }
+            if (!sphere_overlap(c, ovr, g.ll, nl, hs))
+            {
+                st[f] = -1;
+                continue;
+            }
+            if (100. < rc)
+            {
+                st[f] = 1;
+                continue;
+            }
+            MaskJob J;
+            for (int i = 0; i < 3; i++)
+                J.center[i] = c[i];
+            J.rcut           = rc;
+            J.rc_inv         = 1. / rc;
+            J.overlap_radius = ovr;
+            J.func           = func;
+            for (int i = 0; i < 3; i++)
+            {
+                const int k   = (int)ceil(ovr / hl[i]) + 2;
+                const int ext = 2 * k + 1;
+                if (ext >= nl[i])
+                {
+                    J.box[i]     = 0;
+                    J.box[3 + i] = nl[i];
+                }
+                else
+                {
+                    int ci = (int)floor(c[i] / hl[i]);
+                    int b0 = ci - k;
+                    b0 %= nl[i];
+                    if (b0 < 0) b0 += nl[i];
+                    J.box[i]     = b0;
+                    J.box[3 + i] = ext;
+                }
+            }
+            J.offset = total;
+            offs[f]  = total;
+            total += (size_t)J.box[3] * J.box[4] * J.box[5];
+            for (int i = 0; i < 6; i++)
+                bx[6 * f + i] = J.box[i];
+            st[f] = 2; // provisional, fixed from the counts below
+            jobs.push_back(J);
+        }
+        MGX_TRY(M->values[l].ensure(std::max<size_t>(total, 1) * esz));
+        if (!jobs.empty())
+        {
+            MGX_TRY(d_coords.ensure(coords.size() * sizeof(double)));
+            MGX_TRY(d_jobs.ensure(jobs.size() * sizeof(MaskJob)));
+            MGX_TRY(d_counts.ensure(jobs.size() * 2 * sizeof(unsigned long long)));
+            MGX_TRY(cuda_check(cudaMemcpyAsync(d_coords.ptr, coords.data(),
+                                   coords.size() * sizeof(double),
+                                   cudaMemcpyHostToDevice, s),
+                "mask coords upload"));
+            MGX_TRY(cuda_check(cudaMemcpyAsync(d_jobs.ptr, jobs.data(),
+                                   jobs.size() * sizeof(MaskJob),
+                                   cudaMemcpyHostToDevice, s),
+                "mask jobs upload"));
+            MGX_TRY(cuda_check(cudaMemsetAsync(d_counts.ptr, 0,
+                                   jobs.size() * 2 * sizeof(unsigned long long), s),
+                "mask counts"));
+            const double* dc = (const double*)d_coords.ptr;
+            size_t maxbox    = 0;
+            for (auto& J : jobs)
+                maxbox = std::max(maxbox, (size_t)J.box[3] * J.box[4] * J.box[5]);
+            // one grid row per job (jobs are processed in slices of 65535)
+            for (size_t j0 = 0; j0 < jobs.size(); j0 += 65535)
+            {
+                const int nj = (int)std::min<size_t>(65535, jobs.size() - j0);
+                dim3 grid((unsigned)std::min<size_t>((maxbox + 255) / 256, 256), nj);
+                const MaskJob* dj = (const MaskJob*)d_jobs.ptr + j0;
+                unsigned long long* cnt = (unsigned long long*)d_counts.ptr + 2 * j0;
+                if (dtype == MGX_F64)
+                    mask_values_kernel<double><<<grid, 256, 0, s>>>(dj, nj, dc,
+                        dc + nl[0], dc + nl[0] + nl[1], nl[0], nl[1], nl[2], g.ll[0],
+                        g.ll[1], g.ll[2], exp2_rc, exp2_coeff,
+                        (double*)M->values[l].ptr, cnt);
+                else
+                    mask_values_kernel<float><<<grid, 256, 0, s>>>(dj, nj, dc,
+                        dc + nl[0], dc + nl[0] + nl[1], nl[0], nl[1], nl[2], g.ll[0],
+                        g.ll[1], g.ll[2], exp2_rc, exp2_coeff,
+                        (float*)M->values[l].ptr, cnt);
+                MGX_LAUNCH_CHECK("mask_values_kernel");
+            }
+            std::vector<unsigned long long> counts(jobs.size() * 2);
+            MGX_TRY(cuda_check(cudaMemcpyAsync(counts.data(), d_counts.ptr,
+                                   counts.size() * sizeof(unsigned long long),
+                                   cudaMemcpyDeviceToHost, s),
+                "mask counts download"));
+            MGX_TRY(cuda_check(cudaStreamSynchronize(s), "mask build sync"));
+            // GridMask::assign (src/GridMask.cc:311-339) from the counts
+            size_t jj = 0;
+            for (int f = 0; f < nfunc; f++)
+            {
+                if (st[f] != 2) continue;
+                unsigned long long icount = counts[2 * jj], ncount = counts[2 * jj + 1];
+                jj++;
+                if (l == 0 && icount < 1) icount = 1;
+                if (ncount == 0 && icount == 0)
+                    st[f] = -1;
+                else if (ncount == 0)
+                    st[f] = 0;
+                else
+                    st[f] = 2;
+            }
+        }
+        MGX_TRY(M->state[l].ensure(nfunc * sizeof(int)));
+        MGX_TRY(M->box[l].ensure(6 * (size_t)nfunc * sizeof(int)));
+        MGX_TRY(M->offset[l].ensure(nfunc * sizeof(size_t)));
+        MGX_TRY(cuda_check(cudaMemcpyAsync(M->state[l].ptr, st.data(),
+                               nfunc * sizeof(int), cudaMemcpyHostToDevice, s),
+            "mask state upload"));
+        MGX_TRY(cuda_check(cudaMemcpyAsync(M->box[l].ptr, bx.data(),
+                               bx.size() * sizeof(int), cudaMemcpyHostToDevice, s),
+            "mask box upload"));
+        MGX_TRY(cuda_check(cudaMemcpyAsync(M->offset[l].ptr, offs.data(),
+                               nfunc * sizeof(size_t), cudaMemcpyHostToDevice, s),
+            "mask offset upload"));
+        MGX_TRY(cuda_check(cudaStreamSynchronize(s), "mask upload sync"));
+        MaskDev& D = M->dev[l];
+        D.state    = (const int*)M->state[l].ptr;
+        D.box      = (const int*)M->box[l].ptr;
+        D.offset   = (const size_t*)M->offset[l].ptr;
+        D.values   = M->values[l].ptr;
+        for (int i = 0; i < 3; i++)
+            D.n[i] = nl[i];
+        D.kind = kind;
+    }
+    *out = M;
+    return MGX_OK;
+}
+
+/* masks of functions [f0, f0 + nf) at level l, as seen by a launch whose
+ * blockIdx.y runs over those functions */
+MaskDev mask_slice(const mgx_masks* M, int level, int f0)
+{
+    MaskDev D;
+    if (M == nullptr || level >= M->nlevels) return D;
+    D = M->dev[level];
+    D.state += f0;
+    D.box += 6 * (size_t)f0;
+    D.offset += f0;
+    return D;
+}
+
+int masks_apply(mgx_ctx* ctx, const mgx_masks* M, int level, void* u, size_t ld,
+    int nfunc, cudaStream_t s)
+{
+    if (!M || level < 0 || level >= M->nlevels || nfunc > M->nfunc)
+        return fail(MGX_BAD_ARG, "masks_apply: bad level or nfunc");
+    const Level L = make_level(ctx->grid, level);
+    const MaskDev D = mask_slice(M, level, 0);
+    const dim3 g    = grid_for(L.npts(), nfunc);
+    if (M->dtype == MGX_F64)
+        mask_apply_kernel<double><<<g, 256, 0, s>>>((double*)u, ld, L.n[0], L.n[1], L.n[2], D);
+    else
+        mask_apply_kernel<float><<<g, 256, 0, s>>>((float*)u, ld, L.n[0], L.n[1], L.n[2], D);
+    MGX_LAUNCH_CHECK("mask_apply_kernel");
+    return MGX_OK;
+}
+
+template <typename T>
+__global__ void mask_expand_kernel(T* dense, int nx, int ny, int nz, MaskDev m)
+{
+    const int f       = blockIdx.y;
+    const size_t npts = (size_t)nx * ny * nz;
+    for (size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x; idx < npts;
+         idx += (size_t)gridDim.x * blockDim.x)
+    {
+        const int z = (int)(idx % nz);
+        const int y = (int)((idx / nz) % ny);
+        const int x = (int)(idx / ((size_t)nz * ny));
+        const int st = m.state[f];
+        T v          = (T)0;
+        if (st == 1)
+            v = (T)1;
+        else if (st == 2)
+        {
+            const int* b = m.box + 6 * f;
+            int dx = x - b[0], dy = y - b[1], dz = z - b[2];
+            if (dx < 0) dx += nx;
+            if (dy < 0) dy += ny;
+            if (dz < 0) dz += nz;
+            if (dx < b[3] && dy < b[4] && dz < b[5])
+                v = reinterpret_cast<const T*>(m.values)[m.offset[f]
+                                                         + ((size_t)dx * b[4] + dy) * b[5]
+                                                         + dz];
+        }
+        dense[(size_t)f * npts + idx] = v;
+    }
+}
+
+int masks_expand(const mgx_masks* M, int level, void* dense, int* host_state,
+    cudaStream_t s)
+{
+    if (!M || level < 0 || level >= M->nlevels)
+        return fail(MGX_BAD_ARG, "masks_expand: bad level");
+    const MaskDev D = M->dev[level];
+    const size_t np = (size_t)D.n[0] * D.n[1] * D.n[2];
+    const dim3 g    = grid_for(np, M->nfunc);
+    if (M->dtype == MGX_F64)
+        mask_expand_kernel<double><<<g, 256, 0, s>>>((double*)dense, D.n[0], D.n[1], D.n[2], D);
+    else
+        mask_expand_kernel<float><<<g, 256, 0, s>>>((float*)dense, D.n[0], D.n[1], D.n[2], D);
+    MGX_LAUNCH_CHECK("mask_expand_kernel");
+    if (host_state)
+        std::memcpy(host_state, M->h_state[level].data(), M->nfunc * sizeof(int));
+    return MGX_OK;
+}
+
+/* ------------------------------------------------------------------ */
+/* the V-cycle                                                          */
+/* ------------------------------------------------------------------ */
+struct VCycle
+{
+    mgx_ctx* ctx;
+    int dtype;
+    int lap_type;
+    int L; // maxlevels
+    int nf;
+    int f0;
+    const mgx_masks* masks;
+    cudaStream_t s;
+    std::vector<Level> lev;
+    std::vector<double> jf;
+    // per level: v[2], w, f  (level 0: v[0] = caller out, f = caller res)
+    std::vector<void*> v0, v1, w, f;
+    std::vector<size_t> ld;
+    int* err;
+
+    int jacobi(int l, int cur, bool write_w)
+    {
+        PlaneParams p;
+        p.u   = cur ? v1[l] : v0[l];
+        p.ldu = ld[l];
+        p.f   = f[l];
+        p.ldf = ld[l];
+        p.out = cur ? v0[l] : v1[l];
+        p.ldo = ld[l];
+        p.w   = write_w ? w[l] : nullptr;
+        p.ldw = ld[l];
+        for (int i = 0; i < 3; i++)
+            p.n[i] = lev[l].n[i];
+        p.mask = mask_slice(masks, l, f0);
+        p.err  = err;
+        return stencil_launch(OP_JACOBI, l == 0 ? lap_type : 1, dtype, dtype, p,
+            lev[l], jf[l], nf, s);
+    }
+
+    // returns the buffer index holding the result at level l
+    int mg(int l)
+    {
+        int cur         = 0;
+        const int ncycl = (l == L) ? 4 : 2;
+        for (int it = 0; it < ncycl; it++)
+        {
+            const int st = jacobi(l, cur, (it == ncycl - 1) && (l < L));
+            if (st != MGX_OK) return -st - 1;
+            cur ^= 1;
+        }
+        if (l == L) return cur;
+        int st = restrict_launch(dtype, lev[l], w[l], ld[l], f[l + 1], ld[l + 1],
+            nf, mask_slice(masks, l + 1, f0), s);
+        if (st != MGX_OK) return -st - 1;
+        st = cuda_check(cudaMemsetAsync(v0[l + 1], 0,
+                            ld[l + 1] * nf * dtype_size(dtype), s),
+            "coarse zero");
+        if (st != MGX_OK) return -st - 1;
+        const int c1 = mg(l + 1);
+        if (c1 < 0) return c1;
+        st = prolong_launch(dtype, 1, lev[l], c1 ? v1[l + 1] : v0[l + 1],
+            ld[l + 1], cur ? v1[l] : v0[l], ld[l], nf, mask_slice(masks, l, f0), s);
+        if (st != MGX_OK) return -st - 1;
+        for (int it = 0; it < 2; it++)
+        {
+            st = jacobi(l, cur, false);
+            if (st != MGX_OK) return -st - 1;
+            cur ^= 1;
+        }
+        return cur;
+    }
+};
+
+int precond_mg(mgx_ctx* ctx, const mgx_precond_params* P, int dtype,
+    const void* res, size_t ld, void* out, int nfunc, const mgx_masks* masks,
+    cudaStream_t s)
+{
+    if (!P || !res || !out || nfunc < 0) return fail(MGX_BAD_ARG, "precond_mg: null argument");
+    if (res == out) return fail(MGX_BAD_ARG, "precond_mg: res and out alias");
+    if (P->lap_type < 0 || P->lap_type > 4) return fail(MGX_BAD_ARG, "lap_type %d", P->lap_type);
+    const int L = P->maxlevels;
+    if (L < 0 || L > 6) return fail(MGX_BAD_ARG, "maxlevels %d", L);
+    const mgx_grid& g = ctx->grid;
+    for (int l = 0; l < L; l++)
+        for (int i = 0; i < 3; i++)
+            if ((g.n[i] >> l) % 2)
+                return fail(MGX_BAD_ARG, "grid dimension %d not divisible by 2^%d", i, L);
+    if (masks && (masks->nlevels < L + 1 || masks->nfunc < nfunc))
+        return fail(MGX_BAD_ARG, "masks cover %d levels / %d functions", masks->nlevels, masks->nfunc);
+    if (nfunc == 0) return MGX_OK;
+    const size_t es = dtype_size(dtype);
+
+    VCycle V;
+    V.ctx      = ctx;
+    V.dtype    = dtype;
+    V.lap_type = P->lap_type;
+    V.L        = L;
+    V.masks    = masks;
+    V.s        = s;
+    for (int l = 0; l <= L; l++)
+    {
+        V.lev.push_back(make_level(g, l));
+        V.jf.push_back(jacobi_factor(l == 0 ? P->lap_type : 1, V.lev[l].h));
+    }
+    // workspace per function: level 0: v1 + w ; level l>0: v0, v1, w, f
+    size_t per_func = 2 * V.lev[0].npts();
+    for (int l = 1; l <= L; l++)
+        per_func += 4 * V.lev[l].npts();
+    per_func *= es;
+    int chunk = P->chunk > 0 ? P->chunk : nfunc;
+    if (P->chunk <= 0)
+    {
+        size_t fr = 0, tot = 0;
+        cudaMemGetInfo(&fr, &tot);
+        const size_t cap = (size_t)(0.4 * (double)(fr + ctx->vc.bytes));
+        if (per_func * (size_t)chunk > cap)
+            chunk = (int)std::max<size_t>(1, cap / per_func);
+    }
+    chunk = std::min(chunk, 65535);
+    chunk = std::min(chunk, nfunc);
+    MGX_TRY(ctx->vc.ensure(per_func * chunk + 256));
+    MGX_TRY(ctx->flag.ensure(256));
+    V.err = (int*)ctx->flag.ptr;
+    MGX_TRY(cuda_check(cudaMemsetAsync(V.err, 0, sizeof(int), s), "flag reset"));
+
+    for (int f0 = 0; f0 < nfunc; f0 += chunk)
+    {
+        const int nf = std::min(chunk, nfunc - f0);
+        V.nf = nf;
+        V.f0 = f0;
+        V.v0.assign(L + 1, nullptr);
+        V.v1.assign(L + 1, nullptr);
+        V.w.assign(L + 1, nullptr);
+        V.f.assign(L + 1, nullptr);
+        V.ld.assign(L + 1, 0);
+        char* base = (char*)ctx->vc.ptr;
+        V.ld[0]    = ld;
+        V.v0[0]    = (char*)out + (size_t)f0 * ld * es;
+        V.f[0]     = (void*)((const char*)res + (size_t)f0 * ld * es);
+        const size_t p0 = V.lev[0].npts();
+        V.v1[0]    = base;
+        base += (size_t)nf * p0 * es;
+        V.w[0] = base;
+        base += (size_t)nf * p0 * es;
+        for (int l = 1; l <= L; l++)
+        {
+            const size_t pl = V.lev[l].npts();
+            V.ld[l]         = pl;
+            V.v0[l]         = base;
+            base += (size_t)nf * pl * es;
+            V.v1[l] = base;
+            base += (size_t)nf * pl * es;
+            V.w[l] = base;
+            base += (size_t)nf * pl * es;
+            V.f[l] = base;
+            base += (size_t)nf * pl * es;
+        }
+        // v = gamma * res (src/OrbitalsPreconditioning.cc:102-107)
+        MGX_TRY(scale_launch(dtype, V.f[0], ld, V.v0[0], ld, p0, nf, P->gamma, s));
+        const int c = V.mg(0);
+        if (c < 0) return -(c + 1);
+        if (c != 0) return fail(MGX_UNSUPPORTED, "V-cycle ended in the work buffer");
+    }
+    return MGX_OK;
+}
+
+} // namespace mgx

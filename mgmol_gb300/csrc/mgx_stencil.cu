@@ -1,0 +1,787 @@
+// Finite-difference stencils of MGmol's orbital hot path on sm_103a.
+//
+// Fused path (ghost-free blocks, periodic): a plane-marching engine.  Each
+// CTA owns one function, a band of TY y-rows and a chunk of x-planes.  The
+// tile of every plane (TY + 2R rows, whole z lines, the periodic y wrap
+// split into at most two contiguous runs) is fetched with 1-D bulk copies
+// (cp.async.bulk) into a ring of S shared-memory stages completed on
+// mbarriers, so that S - 2R - 1 planes are in flight while one is computed.
+// z neighbours wrap inside the staged line; x neighbours come from the other
+// stages.  One template serves -Lap, the Hamiltonian (with B(V psi) or
+// V psi), the Mehrstellen B operator and the Jacobi sweep of the V-cycle
+// (residual, update, localization mask in the epilogue).
+//
+// Coefficients follow src/pb/FDkernels.cc (del2 2nd/4th/6th/8th and
+// Mehrstellen) and src/pb/Laph*.h (diagonals and Jacobi factors).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+
+#include "mgx_internal.cuh"
+#include "mgx_stencil.cuh"
+
+namespace mgx
+{
+
+int lap_radius(int lap_type)
+{
+    switch (lap_type)
+    {
+        case 0: return 1;
+        case 1: return 1;
+        case 2: return 2;
+        case 3: return 3;
+        case 4: return 4;
+    }
+    return -1;
+}
+
+StencilCoeffs stencil_coeffs(int lap_type, const double h[3])
+{
+    StencilCoeffs c = {};
+    const double ih[3] = { 1. / (h[0] * h[0]), 1. / (h[1] * h[1]),
+        1. / (h[2] * h[2]) };
+    const double inv12 = 1. / 12.;
+    c.radius           = lap_radius(lap_type);
+    switch (lap_type)
+    {
+        case 0: // FDkernelDel2_4th_Mehr, src/pb/FDkernels.cc:453-463
+        {
+            c.c0    = 16. * inv12 * (ih[0] + ih[1] + ih[2]);
+            c.cx[0] = -10. * inv12 * ih[0] + 0.125 * c.c0;
+            c.cy[0] = -10. * inv12 * ih[1] + 0.125 * c.c0;
+            c.cz[0] = -10. * inv12 * ih[2] + 0.125 * c.c0;
+            c.cxy   = -inv12 * (ih[0] + ih[1]);
+            c.cyz   = -inv12 * (ih[2] + ih[1]);
+            c.cxz   = -inv12 * (ih[0] + ih[2]);
+            break;
+        }
+        case 1: // FDkernelDel2_2nd, src/pb/FDkernels.cc:28-42
+            c.cx[0] = -ih[0];
+            c.cy[0] = -ih[1];
+            c.cz[0] = -ih[2];
+            c.c0    = -2. * (c.cx[0] + c.cy[0] + c.cz[0]);
+            break;
+        case 2: // FDkernelDel2_4th, src/pb/FDkernels.cc:86-104
+        {
+            const double w[2] = { -16., 1. };
+            double s = 0.;
+            for (int k = 0; k < 2; k++)
+            {
+                c.cx[k] = w[k] * (inv12 * ih[0]);
+                c.cy[k] = w[k] * (inv12 * ih[1]);
+                c.cz[k] = w[k] * (inv12 * ih[2]);
+            }
+            s    = c.cx[0] + c.cx[1] + c.cy[0] + c.cy[1] + c.cz[0] + c.cz[1];
+            c.c0 = -2. * s;
+            break;
+        }
+        case 3: // FDkernelDel2_6th, src/pb/FDkernels.cc:261-281
+        {
+            const double w[3] = { -270., 27., -2. };
+            for (int k = 0; k < 3; k++)
+            {
+                c.cx[k] = w[k] * ((1. / 180.) * ih[0]);
+                c.cy[k] = w[k] * ((1. / 180.) * ih[1]);
+                c.cz[k] = w[k] * ((1. / 180.) * ih[2]);
+            }
+            c.c0 = -2.
+                   * (c.cx[0] + c.cx[1] + c.cx[2] + c.cy[0] + c.cy[1] + c.cy[2]
+                       + c.cz[0] + c.cz[1] + c.cz[2]);
+            break;
+        }
+        case 4: // FDkernelDel2_8th, src/pb/FDkernels.cc:350-374
+        {
+            const double w[4] = { -8064., 1008., -128., 9. };
+            for (int k = 0; k < 4; k++)
+            {
+                c.cx[k] = w[k] * ((1. / 5040.) * ih[0]);
+                c.cy[k] = w[k] * ((1. / 5040.) * ih[1]);
+                c.cz[k] = w[k] * ((1. / 5040.) * ih[2]);
+            }
+            c.c0 = -2.
+                   * (c.cx[0] + c.cx[1] + c.cx[2] + c.cx[3] + c.cy[0] + c.cy[1]
+                       + c.cy[2] + c.cy[3] + c.cz[0] + c.cz[1] + c.cz[2]
+                       + c.cz[3]);
+            break;
+        }
+    }
+    return c;
+}
+
+double jacobi_factor(int lap_type, const double h[3])
+{
+    const double s = 1. / (h[0] * h[0]) + 1. / (h[1] * h[1]) + 1. / (h[2] * h[2]);
+    switch (lap_type)
+    {
+        case 0: return 1. / ((4. / 3.) * s);                   // Laph4M.h:29-31,80
+        case 1: return 6. * (1. / (2. * s)) / 7.;              // Laph2.h:32-34,95
+        case 2: return (1. / (2.5 * s)) / 1.5;                 // Laph4.h:35,106
+        case 3: return (1. / ((49. / 18.) * s)) / 1.5;         // Laph6.h:40,101
+        case 4: return (1. / ((1435. / 504.) * s)) / 1.5;      // Laph8.h:40-42,100
+    }
+    return 0.;
+}
+
+/* ------------------------------------------------------------------ */
+/* device helpers                                                       */
+/* ------------------------------------------------------------------ */
+template <typename T>
+struct DevCoef
+{
+    T c0;
+    T cx[4], cy[4], cz[4];
+    T cxy, cyz, cxz;
+    T jf;
+};
+
+template <typename T>
+DevCoef<T> to_dev(const StencilCoeffs& c, double jf)
+{
+    DevCoef<T> d;
+    d.c0 = (T)c.c0;
+    for (int k = 0; k < 4; k++)
+    {
+        d.cx[k] = (T)c.cx[k];
+        d.cy[k] = (T)c.cy[k];
+        d.cz[k] = (T)c.cz[k];
+    }
+    d.cxy = (T)c.cxy;
+    d.cyz = (T)c.cyz;
+    d.cxz = (T)c.cxz;
+    d.jf  = (T)jf;
+    return d;
+}
+
+__device__ __forceinline__ int wrap(int i, int n)
+{
+    return i < 0 ? i + n : (i >= n ? i - n : i);
+}
+
+/* localization mask of one function at one level (box representation) */
+template <typename T>
+__device__ __forceinline__ T apply_mask(const MaskDev& m, int f, int x, int y,
+    int z, T v)
+{
+    const int st = m.state[f];
+    if (st == 1) return v;
+    if (st <= 0) return (T)0;
+    const int* b = m.box + 6 * f;
+    int dx = x - b[0];
+    if (dx < 0) dx += m.n[0];
+    int dy = y - b[1];
+    if (dy < 0) dy += m.n[1];
+    int dz = z - b[2];
+    if (dz < 0) dz += m.n[2];
+    T mv = (T)0;
+    if (dx < b[3] && dy < b[4] && dz < b[5])
+        mv = reinterpret_cast<const T*>(m.values)[m.offset[f]
+                                                  + ((size_t)dx * b[4] + dy) * b[5]
+                                                  + dz];
+    if (m.kind == 0)
+    {
+        if (v > mv) return mv;
+        if (v < -mv) return -mv;
+        return v;
+    }
+    return v * mv;
+}
+
+/* Per-point operator evaluation shared by the staged and direct kernels.
+ * `at(dx, dy, dz)` returns u at the offset; `vat` returns V. */
+template <typename T, int LAP, int R, typename UA>
+__device__ __forceinline__ T eval_lap(const DevCoef<T>& c, UA at)
+{
+    if (LAP == 0)
+    {
+        const T u0 = at(0, 0, 0);
+        T r        = c.c0 * u0;
+        r += c.cz[0] * (at(0, 0, -1) + at(0, 0, 1));
+        r += c.cy[0] * (at(0, -1, 0) + at(0, 1, 0));
+        r += c.cx[0] * (at(-1, 0, 0) + at(1, 0, 0));
+        r += c.cxz * (at(-1, 0, -1) + at(-1, 0, 1) + at(1, 0, -1) + at(1, 0, 1));
+        r += c.cyz * (at(0, -1, -1) + at(0, -1, 1) + at(0, 1, -1) + at(0, 1, 1));
+        r += c.cxy * (at(-1, -1, 0) + at(1, -1, 0) + at(-1, 1, 0) + at(1, 1, 0));
+        return r;
+    }
+    T r = c.c0 * at(0, 0, 0);
+#pragma unroll
+    for (int k = 1; k <= R; k++)
+    {
+        r += c.cx[k - 1] * (at(-k, 0, 0) + at(k, 0, 0));
+        r += c.cy[k - 1] * (at(0, -k, 0) + at(0, k, 0));
+        r += c.cz[k - 1] * (at(0, 0, -k) + at(0, 0, k));
+    }
+    return r;
+}
+
+/* B w = 1/2 w + 1/12 (sum of the 6 face neighbours), FDkernelRHS_4th_Mehr1 */
+template <typename T, typename WA>
+__device__ __forceinline__ T eval_rhs(WA w)
+{
+    const T c0 = (T)0.5, c1 = (T)(1. / 12.);
+    return c0 * w(0, 0, 0)
+           + c1 * (w(-1, 0, 0) + w(1, 0, 0) + w(0, -1, 0) + w(0, 1, 0)
+                   + w(0, 0, -1) + w(0, 0, 1));
+}
+
+template <typename T, typename TV, int LAP, int OP, int R>
+struct PointOp
+{
+    /* returns the value written to `out`; writes *wres for OP_JACOBI */
+    template <typename UA, typename VA>
+    __device__ __forceinline__ static T apply(const PlaneParams& p,
+        const DevCoef<T>& c, UA at, VA vat, int f, size_t idx, T* wres)
+    {
+        if (OP == OP_RHS)
+        {
+            return eval_rhs<T>(at);
+        }
+        const T lap = eval_lap<T, LAP, R>(c, at);
+        if (OP == OP_LAP) return lap;
+        if (OP == OP_HPSI_B)
+        {
+            auto w = [&](int dx, int dy, int dz) -> T {
+                return (T)((TV)at(dx, dy, dz) * vat(dx, dy, dz));
+            };
+            // reference order: B(V psi) first, then += -Lap psi
+            return eval_rhs<T>(w) + lap;
+        }
+        if (OP == OP_HPSI_V)
+        {
+            return lap + (T)((TV)at(0, 0, 0) * vat(0, 0, 0));
+        }
+        // OP_JACOBI: w = A v - f ; v -= jf w
+        const T fv = reinterpret_cast<const T*>(p.f)[(size_t)f * p.ldf + idx];
+        const T w  = lap - fv;
+        *wres      = w;
+        return at(0, 0, 0) - c.jf * w;
+    }
+};
+
+/* ------------------------------------------------------------------ */
+/* staged (bulk-copy) plane kernel                                       */
+/* ------------------------------------------------------------------ */
+template <typename T, typename TV, int LAP, int OP, int R, int S>
+__global__ void __launch_bounds__(256) plane_kernel(PlaneParams p, DevCoef<T> c)
+{
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    constexpr bool STAGE_V = (OP == OP_HPSI_B);
+    const int nx = p.n[0], ny = p.n[1], nz = p.n[2];
+    const int TY     = p.ty;
+    const int rows   = TY + 2 * R;
+    const int tile_y = blockIdx.x % p.ntile_y;
+    const int tile_x = blockIdx.x / p.ntile_y;
+    const int f      = blockIdx.y;
+    const int y0     = tile_y * TY;
+    const int x0     = tile_x * p.xc;
+    const int xcount = min(p.xc, nx - x0);
+    const int nplanes = xcount + 2 * R;
+
+    const size_t stage_elems = (size_t)rows * nz;
+    T* stages                = reinterpret_cast<T*>(smem_raw);
+    TV* vstages = reinterpret_cast<TV*>(smem_raw + S * stage_elems * sizeof(T));
+    uint64_t* bars = reinterpret_cast<uint64_t*>(
+        smem_raw + S * stage_elems * (sizeof(T) + (STAGE_V ? sizeof(TV) : 0)));
+
+    const T* ubase  = reinterpret_cast<const T*>(p.u) + (size_t)f * p.ldu;
+    const TV* vbase = reinterpret_cast<const TV*>(p.V);
+
+    // rows y0-R .. y0+TY+R-1 (mod ny): run A then (if wrapped) run B
+    int ya = y0 - R;
+    int na, yb, nb;
+    if (ya < 0)
+    {
+        // rows [ny+ya, ny) then [0, y0+TY+R)
+        yb = 0;
+        nb = y0 + TY + R;
+        na = -ya;
+        ya = ny + ya;
+    }
+    else if (y0 + TY + R > ny)
+    {
+        na = ny - ya;
+        yb = 0;
+        nb = y0 + TY + R - ny;
+    }
+    else
+    {
+        na = rows;
+        yb = 0;
+        nb = 0;
+    }
+    const uint32_t bytes_u = (uint32_t)(stage_elems * sizeof(T));
+    const uint32_t bytes_v = STAGE_V ? (uint32_t)(stage_elems * sizeof(TV)) : 0u;
+
+    auto issue = [&](int plane_idx) {
+        const int slot = plane_idx % S;
+        const int x    = wrap(x0 - R + plane_idx, nx);
+        uint64_t* bar  = bars + slot;
+        mbar_arrive_expect_tx(bar, bytes_u + bytes_v);
+        T* dst         = stages + slot * stage_elems;
+        const T* src   = ubase + ((size_t)x * ny) * nz;
+        bulk_g2s(dst, src + (size_t)ya * nz, (uint32_t)(na * nz * sizeof(T)), bar);
+        if (nb > 0)
+            bulk_g2s(dst + (size_t)na * nz, src + (size_t)yb * nz,
+                (uint32_t)(nb * nz * sizeof(T)), bar);
+        if (STAGE_V)
+        {
+            TV* vdst       = vstages + slot * stage_elems;
+            const TV* vsrc = vbase + ((size_t)x * ny) * nz;
+            bulk_g2s(vdst, vsrc + (size_t)ya * nz,
+                (uint32_t)(na * nz * sizeof(TV)), bar);
+            if (nb > 0)
+                bulk_g2s(vdst + (size_t)na * nz, vsrc + (size_t)yb * nz,
+                    (uint32_t)(nb * nz * sizeof(TV)), bar);
+        }
+    };
+
+    if (threadIdx.x == 0)
+    {
+        for (int s = 0; s < S; s++)
+            mbar_init(bars + s, 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0)
+    {
+        const int pre = min(S, nplanes);
+        for (int i = 0; i < pre; i++)
+            issue(i);
+    }
+
+    const int npts = TY * nz;
+    bool ok        = true;
+    int waited     = -1; // planes 0..waited have completed
+    int issued     = min(S, nplanes) - 1;
+    for (int io = 0; io < xcount; io++)
+    {
+        // planes io .. io+2R must be resident; the newest is io+2R
+        {
+            const int need = io + 2 * R;
+            for (int i = waited + 1; i <= need && ok; i++)
+            {
+                ok = mbar_wait(bars + (i % S), (uint32_t)((i / S) & 1));
+                if (ok) waited = i;
+            }
+        }
+        const int x = x0 + io;
+        for (int pt = threadIdx.x; pt < npts; pt += blockDim.x)
+        {
+            const int yy = pt / nz;
+            const int z  = pt - yy * nz;
+            auto at      = [&](int dx, int dy, int dz) -> T {
+                const T* st = stages + ((io + R + dx) % S) * stage_elems;
+                return st[(size_t)(yy + R + dy) * nz + wrap(z + dz, nz)];
+            };
+            auto vat = [&](int dx, int dy, int dz) -> TV {
+                if (STAGE_V)
+                {
+                    const TV* st = vstages + ((io + R + dx) % S) * stage_elems;
+                    return st[(size_t)(yy + R + dy) * nz + wrap(z + dz, nz)];
+                }
+                const int y = y0 + yy;
+                return vbase[((size_t)x * ny + y) * nz + z];
+            };
+            const int y      = y0 + yy;
+            const size_t idx = ((size_t)x * ny + y) * nz + z;
+            T wres           = (T)0;
+            T r = PointOp<T, TV, LAP, OP, R>::apply(p, c, at, vat, f, idx, &wres);
+            if (OP == OP_JACOBI)
+            {
+                if (p.mask.state != nullptr)
+                {
+                    r = apply_mask<T>(p.mask, f, x, y, z, r);
+                    if (p.w != nullptr)
+                        wres = apply_mask<T>(p.mask, f, x, y, z, wres);
+                }
+                if (p.w != nullptr)
+                    reinterpret_cast<T*>(p.w)[(size_t)f * p.ldw + idx] = wres;
+            }
+            reinterpret_cast<T*>(p.out)[(size_t)f * p.ldo + idx] = r;
+        }
+        __syncthreads();
+        if (io + S < nplanes)
+        {
+            if (threadIdx.x == 0)
+            {
+                fence_proxy_async_smem();
+                issue(io + S);
+            }
+            issued = io + S;
+        }
+    }
+    if (!ok && threadIdx.x == 0)
+    {
+        // a wait gave up: record it, then let the copies still in flight land
+        // (bounded) before the block releases its shared memory
+        if (p.err != nullptr) atomicExch(p.err, MGX_TIMEOUT);
+        for (int i = waited + 1; i <= issued; i++)
+            mbar_wait(bars + (i % S), (uint32_t)((i / S) & 1));
+    }
+}
+
+/* ------------------------------------------------------------------ */
+/* direct kernel (global loads with wrap), for small / unaligned cases  */
+/* ------------------------------------------------------------------ */
+template <typename T, typename TV, int LAP, int OP, int R>
+__global__ void __launch_bounds__(256) direct_kernel(PlaneParams p, DevCoef<T> c)
+{
+    const int nx = p.n[0], ny = p.n[1], nz = p.n[2];
+    const size_t npts = (size_t)nx * ny * nz;
+    const int f       = blockIdx.y;
+    const T* ub       = reinterpret_cast<const T*>(p.u) + (size_t)f * p.ldu;
+    const TV* vb      = reinterpret_cast<const TV*>(p.V);
+    for (size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x; idx < npts;
+         idx += (size_t)gridDim.x * blockDim.x)
+    {
+        const int z = (int)(idx % nz);
+        const int y = (int)((idx / nz) % ny);
+        const int x = (int)(idx / ((size_t)nz * ny));
+        auto at     = [&](int dx, int dy, int dz) -> T {
+            return ub[((size_t)wrap(x + dx, nx) * ny + wrap(y + dy, ny)) * nz
+                      + wrap(z + dz, nz)];
+        };
+        auto vat = [&](int dx, int dy, int dz) -> TV {
+            return vb[((size_t)wrap(x + dx, nx) * ny + wrap(y + dy, ny)) * nz
+                      + wrap(z + dz, nz)];
+        };
+        T wres = (T)0;
+        T r    = PointOp<T, TV, LAP, OP, R>::apply(p, c, at, vat, f, idx, &wres);
+        if (OP == OP_JACOBI)
+        {
+            if (p.mask.state != nullptr)
+            {
+                r = apply_mask<T>(p.mask, f, x, y, z, r);
+                if (p.w != nullptr) wres = apply_mask<T>(p.mask, f, x, y, z, wres);
+            }
+            if (p.w != nullptr)
+                reinterpret_cast<T*>(p.w)[(size_t)f * p.ldw + idx] = wres;
+        }
+        reinterpret_cast<T*>(p.out)[(size_t)f * p.ldo + idx] = r;
+    }
+}
+
+/* ------------------------------------------------------------------ */
+/* launcher                                                             */
+/* ------------------------------------------------------------------ */
+template <int R>
+constexpr int stages_for()
+{
+    return R == 1 ? 6 : (R == 2 ? 7 : (R == 3 ? 9 : 10));
+}
+
+template <typename T, typename TV, int LAP, int OP, int R>
+static int launch_t(const PlaneParams& p0, const DevCoef<T>& c, int nfunc,
+    cudaStream_t stream, int force_direct)
+{
+    PlaneParams p = p0;
+    constexpr int S = stages_for<R>();
+    constexpr bool STAGE_V = (OP == OP_HPSI_B);
+    const int nx = p.n[0], ny = p.n[1], nz = p.n[2];
+    const size_t esz = sizeof(T) + (STAGE_V ? sizeof(TV) : 0);
+
+    bool staged = !force_direct;
+    // bulk copies need 16-byte aligned rows and bases
+    if ((nz * sizeof(T)) % 16 || (p.ldu * sizeof(T)) % 16
+        || ((uintptr_t)p.u % 16))
+        staged = false;
+    if (STAGE_V && ((nz * sizeof(TV)) % 16 || ((uintptr_t)p.V % 16)))
+        staged = false;
+    // rows per tile: divides ny, leaves room for the halo, fits shared memory
+    int ty = 0;
+    if (staged)
+    {
+        const size_t smem_cap = 110 * 1024;
+        for (int cand = 32; cand >= 1; cand /= 2)
+        {
+            if (ny % cand) continue;
+            if (cand + 2 * R > ny) continue;
+            const size_t sm = (size_t)S * (cand + 2 * R) * nz * esz + S * 8;
+            if (sm > smem_cap) continue;
+            if (cand * nz < 256 && cand < ny - 2 * R && cand < 32)
+            {
+                // prefer bigger tiles when the plane is narrow
+            }
+            ty = cand;
+            break;
+        }
+        if (ty == 0 || nz > 4096) staged = false;
+    }
+    if (staged)
+    {
+        p.ty      = ty;
+        p.ntile_y = ny / ty;
+        // x chunk: enough CTAs to fill the GPU, little halo re-read
+        int xc = 32;
+        while (xc > 4 && (size_t)p.ntile_y * ((nx + xc - 1) / xc) * nfunc < 4 * 152)
+            xc /= 2;
+        if (xc > nx) xc = nx;
+        p.xc       = xc;
+        p.ntile_x  = (nx + xc - 1) / xc;
+        const size_t smem = (size_t)S * (ty + 2 * R) * nz * esz + S * 8;
+        auto kern         = plane_kernel<T, TV, LAP, OP, R, S>;
+        cudaError_t e     = cudaFuncSetAttribute(
+            kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return cuda_check(e, "plane_kernel smem attribute");
+        dim3 grid(p.ntile_y * p.ntile_x, nfunc);
+        kern<<<grid, 256, smem, stream>>>(p, c);
+        MGX_LAUNCH_CHECK("plane_kernel");
+        return MGX_OK;
+    }
+    const size_t npts = (size_t)nx * ny * nz;
+    int bx            = (int)std::min<size_t>((npts + 255) / 256, 4096);
+    dim3 grid(bx, nfunc);
+    direct_kernel<T, TV, LAP, OP, R><<<grid, 256, 0, stream>>>(p, c);
+    MGX_LAUNCH_CHECK("direct_kernel");
+    return MGX_OK;
+}
+
+template <typename T, typename TV, int OP>
+static int dispatch_lap(int lap_type, const PlaneParams& p, const DevCoef<T>& c,
+    int nfunc, cudaStream_t s, int force_direct)
+{
+    switch (lap_type)
+    {
+        case 0: return launch_t<T, TV, 0, OP, 1>(p, c, nfunc, s, force_direct);
+        case 1: return launch_t<T, TV, 1, OP, 1>(p, c, nfunc, s, force_direct);
+        case 2: return launch_t<T, TV, 2, OP, 2>(p, c, nfunc, s, force_direct);
+        case 3: return launch_t<T, TV, 3, OP, 3>(p, c, nfunc, s, force_direct);
+        case 4: return launch_t<T, TV, 4, OP, 4>(p, c, nfunc, s, force_direct);
+    }
+    return fail(MGX_BAD_ARG, "lap_type %d invalid", lap_type);
+}
+
+int stencil_launch(int op, int lap_type, int dtype, int v_dtype,
+    const PlaneParams& p, const Level& L, double jf, int nfunc,
+    cudaStream_t stream, int force_direct)
+{
+    if (nfunc <= 0) return MGX_OK;
+    if (nfunc > 65535) return fail(MGX_BAD_ARG, "nfunc %d > 65535 per launch", nfunc);
+    {
+        const int R = (op == OP_RHS) ? 1 : lap_radius(lap_type);
+        for (int i = 0; i < 3; i++)
+            if (p.n[i] < R)
+                return fail(MGX_BAD_ARG, "grid dimension %d = %d below stencil radius %d",
+                    i, p.n[i], R);
+    }
+    const StencilCoeffs sc = stencil_coeffs(op == OP_RHS ? 1 : lap_type, L.h);
+    if (op == OP_RHS)
+    {
+        if (dtype == MGX_F64)
+            return launch_t<double, double, 0, OP_RHS, 1>(
+                p, to_dev<double>(sc, jf), nfunc, stream, force_direct);
+        return launch_t<float, float, 0, OP_RHS, 1>(
+            p, to_dev<float>(sc, jf), nfunc, stream, force_direct);
+    }
+    if (dtype == MGX_F64)
+    {
+        const DevCoef<double> c = to_dev<double>(sc, jf);
+        switch (op)
+        {
+            case OP_LAP:
+                return dispatch_lap<double, double, OP_LAP>(lap_type, p, c, nfunc, stream, force_direct);
+            case OP_JACOBI:
+                return dispatch_lap<double, double, OP_JACOBI>(lap_type, p, c, nfunc, stream, force_direct);
+            case OP_HPSI_B:
+                if (v_dtype == MGX_F64)
+                    return launch_t<double, double, 0, OP_HPSI_B, 1>(p, c, nfunc, stream, force_direct);
+                return launch_t<double, float, 0, OP_HPSI_B, 1>(p, c, nfunc, stream, force_direct);
+            case OP_HPSI_V:
+                if (v_dtype == MGX_F64)
+                    return dispatch_lap<double, double, OP_HPSI_V>(lap_type, p, c, nfunc, stream, force_direct);
+                return dispatch_lap<double, float, OP_HPSI_V>(lap_type, p, c, nfunc, stream, force_direct);
+        }
+    }
+    else
+    {
+        const DevCoef<float> c = to_dev<float>(sc, jf);
+        switch (op)
+        {
+            case OP_LAP:
+                return dispatch_lap<float, float, OP_LAP>(lap_type, p, c, nfunc, stream, force_direct);
+            case OP_JACOBI:
+                return dispatch_lap<float, float, OP_JACOBI>(lap_type, p, c, nfunc, stream, force_direct);
+            case OP_HPSI_B:
+                if (v_dtype == MGX_F64)
+                    return launch_t<float, double, 0, OP_HPSI_B, 1>(p, c, nfunc, stream, force_direct);
+                return launch_t<float, float, 0, OP_HPSI_B, 1>(p, c, nfunc, stream, force_direct);
+            case OP_HPSI_V:
+                if (v_dtype == MGX_F64)
+                    return dispatch_lap<float, double, OP_HPSI_V>(lap_type, p, c, nfunc, stream, force_direct);
+                return dispatch_lap<float, float, OP_HPSI_V>(lap_type, p, c, nfunc, stream, force_direct);
+        }
+    }
+    return fail(MGX_BAD_ARG, "stencil op %d invalid", op);
+}
+
+/* ------------------------------------------------------------------ */
+/* ghosted drop-in kernels (src/pb/FDkernels.cc, src/pb/MGkernels.cc)   */
+/* ------------------------------------------------------------------ */
+struct GhostGeom
+{
+    int n[3];
+    int g;
+    int incx, incy;
+    size_t sizeg;
+};
+
+inline GhostGeom ghost_geom(const int n[3], int g)
+{
+    GhostGeom G;
+    for (int i = 0; i < 3; i++)
+        G.n[i] = n[i];
+    G.g     = g;
+    G.incy  = n[2] + 2 * g;
+    G.incx  = (n[1] + 2 * g) * G.incy;
+    G.sizeg = (size_t)(n[0] + 2 * g) * G.incx;
+    return G;
+}
+
+template <typename T, int LAP, int R>
+__global__ void ghosted_del2_kernel(GhostGeom G, DevCoef<T> c, const T* v, T* b,
+    size_t nfunc)
+{
+    const size_t npts  = (size_t)G.n[0] * G.n[1] * G.n[2];
+    const size_t total = npts * nfunc;
+    for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+         t += (size_t)gridDim.x * blockDim.x)
+    {
+        const size_t f   = t / npts;
+        const size_t idx = t - f * npts;
+        const int z      = (int)(idx % G.n[2]);
+        const int y      = (int)((idx / G.n[2]) % G.n[1]);
+        const int x      = (int)(idx / ((size_t)G.n[2] * G.n[1]));
+        const size_t i0  = f * G.sizeg + (size_t)(x + G.g) * G.incx
+                          + (size_t)(y + G.g) * G.incy + z + G.g;
+        auto at = [&](int dx, int dy, int dz) -> T {
+            return v[i0 + (ptrdiff_t)dx * G.incx + (ptrdiff_t)dy * G.incy + dz];
+        };
+        b[i0] = eval_lap<T, LAP, R>(c, at);
+    }
+}
+
+template <typename T>
+__global__ void ghosted_rhs_kernel(GhostGeom G, GhostGeom O, const T* v, T* rhs,
+    size_t nfunc)
+{
+    const size_t npts  = (size_t)G.n[0] * G.n[1] * G.n[2];
+    const size_t total = npts * nfunc;
+    for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+         t += (size_t)gridDim.x * blockDim.x)
+    {
+        const size_t f   = t / npts;
+        const size_t idx = t - f * npts;
+        const int z      = (int)(idx % G.n[2]);
+        const int y      = (int)((idx / G.n[2]) % G.n[1]);
+        const int x      = (int)(idx / ((size_t)G.n[2] * G.n[1]));
+        const size_t i0  = f * G.sizeg + (size_t)(x + G.g) * G.incx
+                          + (size_t)(y + G.g) * G.incy + z + G.g;
+        auto at = [&](int dx, int dy, int dz) -> T {
+            return v[i0 + (ptrdiff_t)dx * G.incx + (ptrdiff_t)dy * G.incy + dz];
+        };
+        const size_t o0 = f * O.sizeg + (size_t)(x + O.g) * O.incx
+                          + (size_t)(y + O.g) * O.incy + z + O.g;
+        rhs[o0] = eval_rhs<T>(at);
+    }
+}
+
+/* periodic ghost fill: every ghost point takes its periodic image */
+template <typename T>
+__global__ void trade_kernel(GhostGeom G, T* u, size_t nfunc)
+{
+    const int ex = G.n[0] + 2 * G.g, ey = G.n[1] + 2 * G.g, ez = G.n[2] + 2 * G.g;
+    const size_t total = G.sizeg * nfunc;
+    for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+         t += (size_t)gridDim.x * blockDim.x)
+    {
+        const size_t f   = t / G.sizeg;
+        const size_t idx = t - f * G.sizeg;
+        const int z      = (int)(idx % ez);
+        const int y      = (int)((idx / ez) % ey);
+        const int x      = (int)(idx / ((size_t)ez * ey));
+        const int ix = x - G.g, iy = y - G.g, iz = z - G.g;
+        if (ix >= 0 && ix < G.n[0] && iy >= 0 && iy < G.n[1] && iz >= 0
+            && iz < G.n[2])
+            continue;
+        const int sx = (ix % G.n[0] + G.n[0]) % G.n[0] + G.g;
+        const int sy = (iy % G.n[1] + G.n[1]) % G.n[1] + G.g;
+        const int sz = (iz % G.n[2] + G.n[2]) % G.n[2] + G.g;
+        u[f * G.sizeg + idx]
+            = u[f * G.sizeg + (size_t)sx * G.incx + (size_t)sy * G.incy + sz];
+    }
+}
+
+static int grid_blocks(size_t total)
+{
+    return (int)std::min<size_t>((total + 255) / 256, 1u << 20);
+}
+
+template <typename T>
+static int ghosted_del2_t(const GhostGeom& G, const StencilCoeffs& sc, int lap,
+    const void* v, void* b, size_t nfunc, cudaStream_t s)
+{
+    const DevCoef<T> c = to_dev<T>(sc, 0.);
+    const int nb = grid_blocks((size_t)G.n[0] * G.n[1] * G.n[2] * nfunc);
+    const T* vv  = (const T*)v;
+    T* bb        = (T*)b;
+    switch (lap)
+    {
+        case 0: ghosted_del2_kernel<T, 0, 1><<<nb, 256, 0, s>>>(G, c, vv, bb, nfunc); break;
+        case 1: ghosted_del2_kernel<T, 1, 1><<<nb, 256, 0, s>>>(G, c, vv, bb, nfunc); break;
+        case 2: ghosted_del2_kernel<T, 2, 2><<<nb, 256, 0, s>>>(G, c, vv, bb, nfunc); break;
+        case 3: ghosted_del2_kernel<T, 3, 3><<<nb, 256, 0, s>>>(G, c, vv, bb, nfunc); break;
+        case 4: ghosted_del2_kernel<T, 4, 4><<<nb, 256, 0, s>>>(G, c, vv, bb, nfunc); break;
+    }
+    MGX_LAUNCH_CHECK("ghosted_del2_kernel");
+    return MGX_OK;
+}
+
+int ghosted_del2(const mgx_grid& g, int ghosts, int lap_type, int dtype,
+    const void* v, void* b, size_t nfunc, cudaStream_t s)
+{
+    const int R = lap_radius(lap_type);
+    if (R < 0) return fail(MGX_BAD_ARG, "lap_type %d invalid", lap_type);
+    if (ghosts < R)
+        return fail(MGX_BAD_ARG, "ghost width %d below operator radius %d", ghosts, R);
+    const Level L = make_level(g, 0);
+    const StencilCoeffs sc = stencil_coeffs(lap_type, L.h);
+    const GhostGeom G = ghost_geom(g.n, ghosts);
+    if (dtype == MGX_F64) return ghosted_del2_t<double>(G, sc, lap_type, v, b, nfunc, s);
+    return ghosted_del2_t<float>(G, sc, lap_type, v, b, nfunc, s);
+}
+
+int ghosted_rhs(const mgx_grid& g, int ghosts, int dtype, const void* v, void* rhs,
+    int rhs_ghosts, size_t nfunc, cudaStream_t s)
+{
+    if (ghosts < 1) return fail(MGX_BAD_ARG, "ghost width must be >= 1");
+    if (rhs_ghosts < 0) return fail(MGX_BAD_ARG, "rhs_ghosts < 0");
+    const GhostGeom G = ghost_geom(g.n, ghosts), O = ghost_geom(g.n, rhs_ghosts);
+    const int nb = grid_blocks((size_t)g.n[0] * g.n[1] * g.n[2] * nfunc);
+    if (dtype == MGX_F64)
+        ghosted_rhs_kernel<double><<<nb, 256, 0, s>>>(G, O, (const double*)v, (double*)rhs, nfunc);
+    else
+        ghosted_rhs_kernel<float><<<nb, 256, 0, s>>>(G, O, (const float*)v, (float*)rhs, nfunc);
+    MGX_LAUNCH_CHECK("ghosted_rhs_kernel");
+    return MGX_OK;
+}
+
+int ghosted_trade(const mgx_grid& g, int ghosts, int dtype, void* u, size_t nfunc,
+    cudaStream_t s)
+{
+    if (ghosts < 1) return MGX_OK;
+    for (int i = 0; i < 3; i++)
+        if (g.n[i] < ghosts)
+            return fail(MGX_BAD_ARG, "dimension %d smaller than ghost width", i);
+    const GhostGeom G = ghost_geom(g.n, ghosts);
+    const int nb      = grid_blocks(G.sizeg * nfunc);
+    if (dtype == MGX_F64)
+        trade_kernel<double><<<nb, 256, 0, s>>>(G, (double*)u, nfunc);
+    else
+        trade_kernel<float><<<nb, 256, 0, s>>>(G, (float*)u, nfunc);
+    MGX_LAUNCH_CHECK("trade_kernel");
+    return MGX_OK;
+}
+
+} // namespace mgx

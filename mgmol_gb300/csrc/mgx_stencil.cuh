@@ -1,0 +1,76 @@
+// Shared declarations of the stencil engine (mgx_stencil.cu) and its users.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <vector>
+
+#include "mgx_internal.cuh"
+
+namespace mgx
+{
+
+enum StencilOp
+{
+    OP_LAP    = 0, // out = -Lap u
+    OP_HPSI_B = 1, // out = -Lap_M u + B(V u)          (Mehrstellen only)
+    OP_HPSI_V = 2, // out = -Lap u + V u
+    OP_JACOBI = 3, // w = -Lap u - f ; out = mask(u - jf w) ; w_out = mask(w)
+    OP_RHS    = 4  // out = B u
+};
+
+/* Localization masks of one level in box form: for function f, values of
+ * the box starting at (box[6f], box[6f+1], box[6f+2]) (periodic) with
+ * extents (box[6f+3..5]); points outside the box have mask value 0.
+ * state[f] follows src/GridMask.h:47-52 (-1, 0: zero; 1: identity; 2:
+ * values).  kind 0 clamps (GridMaskMax), 1 multiplies (GridMaskMult). */
+struct MaskDev
+{
+    const int* state = nullptr;
+    const int* box   = nullptr;
+    const size_t* offset = nullptr;
+    const void* values   = nullptr;
+    int n[3]             = { 0, 0, 0 };
+    int kind             = 0;
+};
+
+struct PlaneParams
+{
+    const void* u = nullptr;
+    size_t ldu    = 0;
+    const void* V = nullptr;
+    const void* f = nullptr;
+    size_t ldf    = 0;
+    void* out     = nullptr;
+    size_t ldo    = 0;
+    void* w       = nullptr;
+    size_t ldw    = 0;
+    int n[3]      = { 0, 0, 0 };
+    int ty = 0, xc = 0, ntile_y = 0, ntile_x = 0;
+    MaskDev mask;
+    int* err = nullptr;
+};
+
+int stencil_launch(int op, int lap_type, int dtype, int v_dtype,
+    const PlaneParams& p, const Level& L, double jf, int nfunc,
+    cudaStream_t stream, int force_direct = 0);
+
+int ghosted_del2(const mgx_grid& g, int ghosts, int lap_type, int dtype,
+    const void* v, void* b, size_t nfunc, cudaStream_t s);
+int ghosted_rhs(const mgx_grid& g, int ghosts, int dtype, const void* v,
+    void* rhs, int rhs_ghosts, size_t nfunc, cudaStream_t s);
+int ghosted_trade(const mgx_grid& g, int ghosts, int dtype, void* u,
+    size_t nfunc, cudaStream_t s);
+
+} // namespace mgx
+
+/* the opaque mask set of the C ABI: per level, device arrays in box form */
+struct mgx_masks
+{
+    int nlevels = 0, nfunc = 0, kind = 0, dtype = 0;
+    int n[3]    = { 0, 0, 0 };
+    std::vector<mgx::DeviceBuffer> state, box, offset, values;
+    std::vector<std::vector<int>> h_state, h_box;
+    std::vector<mgx::MaskDev> dev;
+};

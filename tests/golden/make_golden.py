@@ -1,0 +1,75 @@
+"""Records golden vectors from the reference MGmol's own hot-path code.
+
+Runs the reference translation units compiled unmodified against single-task
+shims (oracle/build_ref.sh -> oracle/_ref/libmgref.so, built from the MGmol
+source tree in this container) on small seeded inputs, and stores inputs and
+outputs in tests/golden/ref_vectors.npz.  tests/test_oracle.py checks the
+oracle restatement against these vectors; the GPU tests check the CUDA
+kernels against the oracle.  Re-run after changing the generator:
+
+    oracle/build_ref.sh && python tests/golden/make_golden.py
+"""
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+import oracle as O  # noqa: E402
+from mgmol_gb300 import synth  # noqa: E402
+
+
+def main():
+    if O.ref_lib() is None:
+        raise SystemExit("oracle/_ref/libmgref.so missing: run oracle/build_ref.sh first")
+    out = {}
+    # ragged grid, all operators, both precisions
+    n = (16, 12, 20)
+    ll = (16 * 0.35, 12 * 0.35, 20 * 0.35)
+    psi, centers, _ = synth.gaussian_orbitals(n, ll, 3, 1001)
+    V = synth.gaussian_wells(n, ll, 8, 1001)
+    out["stencil_n"] = np.array(n)
+    out["stencil_ll"] = np.array(ll)
+    out["stencil_psi"] = psi
+    out["stencil_V"] = V
+    for tag, dt in (("d", np.float64), ("f", np.float32)):
+        p = psi.astype(dt)
+        for t in range(5):
+            out[f"fd{t}_{tag}"] = O.fd_apply(n, ll, t, p, ref=True)
+        out[f"rhs_{tag}"] = O.rhs_mehr(n, ll, p, ref=True)
+        out[f"hpsi_{tag}"] = O.hpsi(n, ll, 0, p, V, ref=True)
+        out[f"restrict_{tag}"] = O.restrict(n, ll, p, ref=True)
+        out[f"extend_{tag}"] = O.extend(n, ll, out[f"restrict_{tag}"], ref=True)
+    # V-cycle preconditioner, 3 grids (16^3 coarsest 4^3), three operators
+    n = (16, 16, 16)
+    ll = (16 * 0.35,) * 3
+    res, centers, _ = synth.gaussian_orbitals(n, ll, 3, 1002)
+    out["pc_n"] = np.array(n)
+    out["pc_ll"] = np.array(ll)
+    out["pc_res"] = res
+    out["pc_gamma"] = np.array(0.3)
+    for tag, dt in (("d", np.float64), ("f", np.float32)):
+        for t in (0, 2, 4):
+            out[f"pc{t}_{tag}"] = O.precond(n, ll, t, 2, 0.3, res.astype(dt), ref=True)
+    # masks (GridMaskMax, gaussianDecay) at 3 levels, and the masked V-cycle
+    radii = synth.mask_radii(3, 1003, 1.5, 3.0)
+    out["mask_centers"] = centers
+    out["mask_radii"] = radii
+    st, vals = O.mask_build(n, ll, 1, 3, centers, radii, func=0, ref=True)
+    out["mask_state"] = st
+    for l, v in enumerate(vals):
+        out[f"mask_values_{l}"] = v
+    st1, vals1 = O.mask_build(n, ll, 1, 1, centers, radii, func=1, ref=True)
+    out["mask1_state"] = st1
+    out["mask1_values_0"] = vals1[0]
+    out["pc0_masked_d"] = O.precond(n, ll, 0, 2, 0.3, res, masks=(centers, radii), ref=True)
+    np.savez_compressed(os.path.join(HERE, "ref_vectors.npz"), **out)
+    print("wrote", os.path.join(HERE, "ref_vectors.npz"), len(out), "arrays")
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,65 @@
+"""C-ABI checks that need no GPU: the library loads, exports exactly the
+entry points include/mgx.h declares, and its host-only logic behaves."""
+import ctypes
+import os
+import re
+import subprocess
+
+import pytest
+
+from mgmol_gb300 import capi
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _declared():
+    names = set()
+    for h in os.listdir(os.path.join(ROOT, "include")):
+        if h.endswith(".h"):
+            txt = open(os.path.join(ROOT, "include", h)).read()
+            names |= set(re.findall(r"^(?:int|const char\*|unsigned long long)\s+(mgx_\w+)\(", txt, re.M))
+    return names
+
+
+def test_library_exports_every_declared_symbol():
+    capi.load()
+    out = subprocess.run(["nm", "-D", "--defined-only", capi.LIB_PATH], capture_output=True,
+                         text=True, check=True).stdout
+    exported = {l.split()[-1] for l in out.splitlines() if re.search(r"\sT\smgx_", l)}
+    declared = _declared()
+    assert declared, "no declarations parsed"
+    assert declared == exported, (declared ^ exported)
+    assert declared == set(capi.EXPORTS)
+
+
+def test_library_is_built_for_sm103a():
+    out = subprocess.run(["cuobjdump", "--list-elf", capi.LIB_PATH], capture_output=True, text=True)
+    if out.returncode != 0:
+        pytest.skip("cuobjdump unavailable")
+    assert "sm_103a" in out.stdout
+
+
+def test_precond_gamma_host_logic():
+    """mgx_precond_gamma is host arithmetic: setGamma with Laph4M invDiag."""
+    import oracle as O
+    g = capi.Grid.make((64, 64, 64), (22.4, 22.4, 22.4))
+    out = ctypes.c_double()
+    st = capi.load().mgx_precond_gamma(ctypes.byref(g), 0, 2, -0.5, -1.7, ctypes.byref(out))
+    assert st == capi.MGX_OK
+    h = 22.4 / 64
+    inv_diag = 1.0 / ((4.0 / 3.0) * 3.0 / (h * h))
+    assert abs(out.value - O.set_gamma(inv_diag, 2, -0.5, -1.7)) < 1e-15 * out.value
+
+
+def test_bad_arguments_are_reported_not_aborted():
+    L = capi.load()
+    g = capi.Grid.make((16, 16, 16), (4.0, 4.0, 4.0), bc=(1, 0, 1))
+    h = ctypes.c_void_p()
+    assert L.mgx_create(ctypes.byref(g), ctypes.byref(h)) == capi.MGX_UNSUPPORTED
+    assert b"periodic" in L.mgx_last_error_string()
+    g2 = capi.Grid.make((0, 16, 16), (4.0, 4.0, 4.0))
+    assert L.mgx_create(ctypes.byref(g2), ctypes.byref(h)) == capi.MGX_BAD_ARG
+    assert L.mgx_fd_apply(None, 0, 0, None, 0, None, 1, None) == capi.MGX_BAD_ARG
+    out = ctypes.c_double()
+    assert L.mgx_precond_gamma(ctypes.byref(capi.Grid.make((8, 8, 8), (1, 1, 1))), 9, 1, 0.0, 0.0,
+                               ctypes.byref(out)) == capi.MGX_BAD_ARG
