@@ -1,0 +1,337 @@
+"""Orbital-sweep benchmark of the GB300 implementation of MGmol's hot path.
+
+One step = one orbital sweep over all N orbitals (H psi with the Mehrstellen
+operator and B(V psi), S and H matrices, FP64 Cholesky / inverse / trace,
+one V-cycle preconditioner application), on seeded synthetic orbitals.
+
+Default workload: 2048 orbitals on a 192^3 periodic grid (h = 0.25 bohr,
+FP32 orbitals, 64 Gaussian wells) -- the configuration the metric is quoted
+on.  Inputs (58 GB of orbitals) are far larger than the 126 MB L2, so no L2
+flush is needed between steps.
+
+Output: one JSON line (see the keys below).  --impl reference times the
+CPU implementation of the same sweep (the oracle port of the reference's
+algorithm, all host cores) on a bounded sample and extrapolates to the
+workload; under torchrun only rank 0 runs it.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+CONFIGS = {
+    # name: grid, h, nfunc, wells, lap_type, seed
+    "c5": dict(n=(192, 192, 192), h=0.25, nfunc=2048, wells=64, seed=1005,
+               workload="full sweep at scale: 2048 orbitals, 192^3, h=0.25, Mehrstellen, FP32 orbitals"),
+    "c1": dict(n=(64, 64, 64), h=0.35, nfunc=64, wells=8, seed=1001,
+               workload="plain FP64 case: 64 orbitals, 64^3, h=0.35, Mehrstellen"),
+    "small": dict(n=(64, 64, 64), h=0.25, nfunc=256, wells=16, seed=7,
+                  workload="small sweep: 256 orbitals, 64^3, Mehrstellen, FP32"),
+}
+METRIC = "orbital sweeps/s (Hpsi+precond+Gram)"
+
+
+def _env_int(k, d):
+    try:
+        return int(os.environ.get(k, d))
+    except ValueError:
+        return d
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.samples = []
+        self.proc = None
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 7:
+                self.samples.append(parts)
+
+    def stop(self):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+        if self.thread is not None:
+            self.thread.join(timeout=2)
+
+    def summary(self):
+        import statistics
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if s[3 + i] == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(self.samples)}
+
+
+def _peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return d.get("hbm_gbs", 6800.0), d.get("bf16_tflops", 1900.0), d.get(
+            "bf16_tflops_sustained", 1700.0), "measured"
+    return 6800.0, 1900.0, 1700.0, "fallback"
+
+
+# --------------------------------------------------------------------- CPU leg
+def cpu_sweep_estimate(cfg, sample_funcs=4):
+    """Times the oracle port (all host threads) of one sweep on
+    `sample_funcs` orbitals of the workload grid and extrapolates to N:
+    H psi and the V-cycle scale with N, S and H with N^2."""
+    import numpy as np
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    from mgmol_gb300 import synth
+
+    n = cfg["n"]
+    ll = tuple(x * cfg["h"] for x in n)
+    N = cfg["nfunc"]
+    psi, _, _ = synth.gaussian_orbitals(n, ll, sample_funcs, cfg["seed"], dtype=np.float32)
+    V = synth.gaussian_wells(n, ll, cfg["wells"], cfg["seed"])
+    vel = (cfg["h"]) ** 3
+    t0 = time.perf_counter()
+    hp = O.hpsi(n, ll, 0, psi, V)
+    t1 = time.perf_counter()
+    O.precond(n, ll, 0, 2, 0.2, hp)
+    t2 = time.perf_counter()
+    # S and H on a 64-orbital x 2^17-point slab: time per (pair, point)
+    ns, ks = 64, min(1 << 17, n[0] * n[1] * n[2])
+    rng = np.random.default_rng(0)
+    slab = rng.standard_normal((ns, ks)).astype(np.float32)
+    t3 = time.perf_counter()
+    O.gram(slab, vel)
+    O.hmat(slab, slab, vel)
+    t4 = time.perf_counter()
+    P = n[0] * n[1] * n[2]
+    pairs_s = ns * (ns + 1) / 2 + ns * ns
+    per_pair_point = (t4 - t3) / (pairs_s * ks)
+    lin = (t2 - t0) * (N / sample_funcs)
+    quad = per_pair_point * (N * (N + 1) / 2 + N * N) * P
+    per_sweep = lin + quad
+    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    return {
+        "value": 1.0 / per_sweep, "unit": "sweeps/s", "cores": cores, "kind": "port",
+        "sample": (f"oracle port of the reference loops (FP32 data, FP64 accumulation as the "
+                   f"USE_MP build), {cores} threads: H psi + V-cycle on {sample_funcs} of {N} "
+                   f"orbitals ({n[0]}^3), scaled by N; S and H timed on a 64-orbital x {ks}-point "
+                   f"slab, scaled by pairs x points; sample took {t4 - t0:.1f} s"),
+        "seconds_per_sweep": per_sweep,
+    }
+
+
+def run_reference(args, cfg):
+    rank = _env_int("RANK", 0)
+    if rank != 0:
+        return 0
+    os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count() or 1))
+    vals = []
+    for _ in range(max(1, args.warmup and 0) + args.steps):
+        vals.append(cpu_sweep_estimate(cfg, sample_funcs=args.cpu_sample))
+    best = vals[-1]
+    line = {
+        "impl": "reference", "metric": METRIC, "value": best["value"], "unit": "sweeps/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * best["seconds_per_sweep"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": cfg["workload"], "grid": list(cfg["n"]), "h": cfg["h"],
+                   "orbitals": cfg["nfunc"]},
+        "cpu_baseline": {k: best[k] for k in ("value", "unit", "cores", "kind", "sample")},
+        "e2e": {"value": best["value"], "unit": "sweeps/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# --------------------------------------------------------------------- GPU leg
+def run_gpu(args, cfg):
+    import torch
+    import torch.distributed as dist
+    from mgmol_gb300 import capi, synth
+    from mgmol_gb300.sweep import OrbitalSweep
+
+    world = _env_int("WORLD_SIZE", 1)
+    rank = _env_int("RANK", 0)
+    local = _env_int("LOCAL_RANK", 0)
+    if world > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    capi.load()
+
+    n = cfg["n"]
+    ll = tuple(x * cfg["h"] for x in n)
+    N = cfg["nfunc"]
+    mode = args.mode
+    dt = torch.float64 if mode == "plain" else torch.float32
+    gemm = {"fp64": capi.GEMM_FP64, "fp32": capi.GEMM_FP32, "tf32": capi.GEMM_TF32,
+            "bf16x3": capi.GEMM_BF16X3}[args.gemm if mode == "mixed" else "fp64"]
+    ctx = capi.Context(n, ll)
+    # replicas only: every rank runs the same workload on its own GPU
+    psi, _, _ = synth.gaussian_orbitals_device(n, ll, N, cfg["seed"] + rank, dt)
+    V = synth.gaussian_wells_device(n, ll, cfg["wells"], cfg["seed"])
+    sw = OrbitalSweep(ctx, V, N, mode=mode, gemm=gemm, precond_chunk=args.chunk)
+    torch.cuda.synchronize()
+
+    for _ in range(args.warmup):
+        sw.run(psi)
+    torch.cuda.synchronize()
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    l0 = capi.launches()
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    start.record()
+    for _ in range(args.steps):
+        e = sw.run(psi, timed=True)
+    stop.record()
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    launches = capi.launches() - l0
+    ms = start.elapsed_time(stop) / args.steps
+    clocks.stop()
+    phases = sw.phase_ms()
+    energy = float(e.cpu()[0])
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t[0])
+
+    # end to end through the C ABI with host buffers: pinned host orbitals
+    # copied in each step, energy and S read back
+    e2e = None
+    if args.e2e:
+        host = torch.empty(psi.shape, dtype=dt, pin_memory=True)
+        host.copy_(psi)
+        dev = psi  # the device block is overwritten by the upload each step
+        s_host = torch.empty((N, N), dtype=torch.float64, pin_memory=True)
+        e_host = torch.empty(1, dtype=torch.float64, pin_memory=True)
+        torch.cuda.synchronize()
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        t0.record()
+        ksteps = max(1, min(args.steps, 3))
+        for _ in range(ksteps):
+            dev.copy_(host, non_blocking=True)
+            ee = sw.run(dev)
+            e_host.copy_(ee, non_blocking=True)
+            s_host.copy_(sw.S, non_blocking=True)
+        t1.record()
+        torch.cuda.synchronize()
+        ms_e2e = t0.elapsed_time(t1) / ksteps
+        e2e = {"value": 1e3 / ms_e2e, "unit": "sweeps/s",
+               "h2d_bytes_per_step": int(host.numel() * host.element_size()),
+               "d2h_bytes_per_step": int(8 + N * N * 8), "steps": ksteps}
+
+    if rank != 0:
+        return 0
+    hbm, bf16, bf16s, peak_kind = _peaks()
+    npts = n[0] * n[1] * n[2]
+    s = 4 if dt == torch.float32 else 8
+    # algorithmic work per sweep phase
+    hpsi_bytes = N * npts * 2 * s + npts * s
+    gram_flops = N * (N + 1) * npts + 2.0 * N * N * npts
+    shares = {k: v / sum(phases.values()) for k, v in phases.items()}
+    dominant = max(phases, key=phases.get)
+    if dominant == "gram":
+        achieved = gram_flops / (phases["gram"] * 1e-3) / 1e12
+        roof = {"kernel": "gram+hmat", "bound": "tensor", "achieved": achieved, "peak": bf16,
+                "unit": "TFLOP/s", "frac": achieved / bf16, "traffic": None,
+                "algorithmic": f"{gram_flops:.3e} flop per sweep (S lower incl. diagonal + H)"}
+    elif dominant == "hpsi":
+        achieved = hpsi_bytes / (phases["hpsi"] * 1e-3) / 1e9
+        roof = {"kernel": "hpsi", "bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                "frac": achieved / hbm, "traffic": None,
+                "algorithmic": f"{hpsi_bytes:.3e} B per sweep"}
+    else:
+        # V-cycle: fine-level passes dominate; count read u,f + write v per
+        # Jacobi sweep (5 fine sweeps incl. residual write), restriction and
+        # prolongation-correction
+        fine = N * npts * s
+        pc_bytes = fine * (5 * 3 + 1 + 1.125 + 3 + 2)
+        achieved = pc_bytes / (phases["precond"] * 1e-3) / 1e9
+        roof = {"kernel": "precond_mg", "bound": "hbm", "achieved": achieved, "peak": hbm,
+                "unit": "GB/s", "frac": achieved / hbm, "traffic": None,
+                "algorithmic": f"{pc_bytes:.3e} B per sweep"}
+    roof["peak_kind"] = peak_kind
+    line = {
+        "metric": METRIC, "value": world * 1e3 / ms, "unit": "sweeps/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32" if dt == torch.float32 else "f64",
+        "data": "synthetic (seeded Gaussian orbitals and wells generated on the device)",
+        "config": {"workload": cfg["workload"], "grid": list(n), "h": cfg["h"], "orbitals": N,
+                   "mode": mode, "gemm": args.gemm if mode == "mixed" else "fp64",
+                   "lap_type": "mehrstellen", "precond": "V-cycle 2 coarse levels",
+                   "l2": "inputs larger than L2 (no flush)", "parallelism": f"replicas x{world}"},
+        "phases_ms": phases, "phase_share": shares, "energy_trace_ry": energy,
+        "roofline": roof, "gpu_launches": launches, "clocks": clocks.summary(),
+    }
+    if e2e:
+        line["e2e"] = e2e
+    if not args.no_cpu:
+        line["cpu_baseline"] = {k: v for k, v in cpu_sweep_estimate(cfg, args.cpu_sample).items()
+                                if k != "seconds_per_sweep"}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--config", default="c5", choices=sorted(CONFIGS))
+    ap.add_argument("--mode", default="mixed", choices=["mixed", "plain"])
+    ap.add_argument("--gemm", default="bf16x3", choices=["fp32", "tf32", "bf16x3"])
+    ap.add_argument("--chunk", type=int, default=0, help="V-cycle orbital chunk (0 = auto)")
+    ap.add_argument("--cpu-sample", type=int, default=4)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-e2e", dest="e2e", action="store_false")
+    args = ap.parse_args()
+    cfg = CONFIGS[args.config]
+    if args.impl == "reference":
+        return run_reference(args, cfg)
+    return run_gpu(args, cfg)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

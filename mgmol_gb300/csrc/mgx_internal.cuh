@@ -97,6 +97,8 @@ struct mgx_ctx
     mgx::DeviceBuffer gemm_ws;
     mgx::DeviceBuffer dense_ws;
     mgx::DeviceBuffer flag;
+    // tensor-core GEMM: bf16 hi/lo planes, tile list, status word
+    mgx::DeviceBuffer tc_split, tc_tiles, tc_err;
 };
 
 /* ---------------- PTX helpers: mbarrier + 1-D bulk copies ---------------- */

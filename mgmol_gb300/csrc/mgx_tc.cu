@@ -1,12 +1,475 @@
-// Tensor-core (tcgen05) Gram / H-matrix products: placeholder until the
-// tcgen05 kernels land.
+// Tensor-core (tcgen05) Gram / H-matrix products on sm_103a.
+//
+// C[i][j] += sum_k A[i][k] B[j][k] over the orbital block (K = grid points),
+// the "TN" product of two K-major operands.  One CTA owns a 128 x BN output
+// tile and a contiguous range of K blocks:
+//   warp 0      TMA producer: 2-D tiled bulk tensor copies (SWIZZLE_128B)
+//               of the A and B K-slices into an S-stage shared-memory ring;
+//   warp 1      allocates the TMEM accumulator (128 lanes x BN FP32
+//               columns) and issues tcgen05.mma from one thread, committing
+//               each stage back to its "empty" mbarrier;
+//   warps 2-5   epilogue: tcgen05.ld of the accumulator, FP64 atomic
+//               accumulation of the partial tile into C.
+// Modes:
+//   TF32   -- the FP32 orbitals feed kind::tf32 directly;
+//   BF16X3 -- each operand is split once into bf16 hi + lo planes
+//             (x = hi + lo to ~2^-17 relative), and every K step issues
+//             hi*hi + hi*lo + lo*hi into the same FP32 accumulator.
+// The K range of a CTA is bounded (at most 512 K blocks) so that the FP32
+// accumulation error stays small; partial tiles meet in FP64.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <vector>
+
 #include "mgx_internal.cuh"
 
 namespace mgx
 {
-int gram_tcgen05(mgx_ctx*, int mode, const void*, const void*, size_t, size_t,
-    int, double, int, double*, cudaStream_t)
+int gram_cuda_cores(mgx_ctx*, int, const void*, const void*, size_t, size_t,
+    int, double, int, double*, cudaStream_t);
+
+namespace tc
 {
-    return fail(MGX_UNSUPPORTED, "gemm mode %d not built yet", mode);
+constexpr int BM      = 128;
+constexpr int ROWB    = 128; // bytes of one K slice row (one 128B swizzle atom)
+constexpr int THREADS = 192;
+
+__device__ __forceinline__ uint64_t desc_sw128(uint32_t saddr)
+{
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);
+    d |= (uint64_t)1 << 16;            // leading byte offset (unused, K-major swizzled)
+    d |= (uint64_t)(1024 >> 4) << 32;  // stride byte offset: 8 rows x 128 B
+    d |= (uint64_t)1 << 46;            // descriptor version for tcgen05
+    d |= (uint64_t)2 << 61;            // SWIZZLE_128B
+    return d;
+}
+
+// kind::tf32 (format 2) or kind::f16 with bf16 operands (format 1), FP32 D,
+// both operands K-major
+template <int KIND>
+__host__ __device__ constexpr uint32_t instr_desc(int M, int N)
+{
+    return (1u << 4) | ((KIND == 0 ? 2u : 1u) << 7) | ((KIND == 0 ? 2u : 1u) << 10)
+           | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map,
+    int c0, int c1, uint64_t* bar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes "
+        "[%0], [%1, {%2, %3}], [%4];" ::"r"(smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(smem_u32(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ void prefetch_map(const CUtensorMap* map)
+{
+    asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(map))
+                 : "memory");
+}
+
+template <int KIND>
+__device__ __forceinline__ void mma(uint32_t tmem, uint64_t ad, uint64_t bd,
+    uint32_t idesc, uint32_t acc)
+{
+    if (KIND == 0)
+        asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                     "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem),
+            "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
+            : "memory");
+    else
+        asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                     "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem),
+            "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
+            : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint64_t* bar)
+{
+    asm volatile(
+        "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+            smem_u32(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ void fence_after_sync()
+{
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void fence_before_sync()
+{
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32])
+{
+    uint32_t r[32];
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+                 "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+                 "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]),
+                 "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]),
+                 "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
+                 "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]),
+                 "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]),
+                 "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+                 : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 32; i++)
+        v[i] = __uint_as_float(r[i]);
+}
+
+struct Params
+{
+    const int2* tiles;
+    int kblocks;    // total K blocks
+    int kb_per_cta; // K blocks per CTA
+    int n;          // matrix order
+    int symmetric;  // only i >= j entries of C are produced
+    double* C;      // column-major n x n, FP64, accumulated atomically
+    int* err;
+};
+
+// KIND 0: tf32 (NPROD 1); KIND 1: bf16 (NPROD 1 plain, 3 for hi/lo split)
+template <int KIND, int NPROD, int BN, int STAGES>
+__global__ void __launch_bounds__(THREADS, 1) gram_kernel(
+    const __grid_constant__ CUtensorMap mA0, const __grid_constant__ CUtensorMap mA1,
+    const __grid_constant__ CUtensorMap mB0, const __grid_constant__ CUtensorMap mB1,
+    Params p)
+{
+    constexpr int NOP     = (NPROD == 3) ? 2 : 1;       // planes per operand
+    constexpr int A_BYTES = BM * ROWB;                  // 16 KB
+    constexpr int B_BYTES = BN * ROWB;
+    constexpr int STAGE   = NOP * (A_BYTES + B_BYTES);
+    constexpr int KSTEP   = 32;                          // bytes of K per MMA
+    constexpr int NK      = ROWB / KSTEP;                // MMAs per plane pair
+    constexpr int ELEM    = (KIND == 0) ? 4 : 2;
+    constexpr int BK      = ROWB / ELEM;                 // K elements per block
+    constexpr uint32_t TMEM_COLS = BN;                   // power of two >= 32
+
+    extern __shared__ unsigned char smem_raw[];
+    unsigned char* smem = reinterpret_cast<unsigned char*>(
+        (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    uint64_t* full  = reinterpret_cast<uint64_t*>(smem + STAGES * STAGE);
+    uint64_t* empty = full + STAGES;
+    uint64_t* accf  = empty + STAGES;
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(accf + 1);
+
+    const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+    const int2 tile = p.tiles[blockIdx.x];
+    const int i0 = tile.x * BM, j0 = tile.y * BN;
+    const int kb0 = blockIdx.y * p.kb_per_cta;
+    const int kb1 = min(p.kblocks, kb0 + p.kb_per_cta);
+    const int nkb = kb1 - kb0;
+
+    if (threadIdx.x == 0)
+    {
+        for (int s = 0; s < STAGES; s++)
+        {
+            mbar_init(full + s, 1);
+            mbar_init(empty + s, 1);
+        }
+        mbar_init(accf, 1);
+        fence_mbar_init();
+    }
+    if (warp == 1)
+    {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                         smem_u32(tslot)),
+            "r"(TMEM_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    fence_before_sync();
+    __syncthreads();
+    fence_after_sync();
+    const uint32_t tmem = *tslot;
+    bool ok = true;
+
+    if (warp == 0 && lane == 0)
+    {
+        prefetch_map(&mA0);
+        prefetch_map(&mB0);
+        if (NPROD == 3)
+        {
+            prefetch_map(&mA1);
+            prefetch_map(&mB1);
+        }
+        for (int it = 0; it < nkb && ok; it++)
+        {
+            const int s = it % STAGES;
+            const uint32_t ph = (uint32_t)((it / STAGES) & 1);
+            ok = mbar_wait(empty + s, ph ^ 1u);
+            if (!ok) break;
+            unsigned char* st = smem + s * STAGE;
+            mbar_arrive_expect_tx(full + s, STAGE);
+            const int kc = (kb0 + it) * BK;
+            tma_load_2d(st, &mA0, kc, i0, full + s);
+            tma_load_2d(st + NOP * A_BYTES, &mB0, kc, j0, full + s);
+            if (NPROD == 3)
+            {
+                tma_load_2d(st + A_BYTES, &mA1, kc, i0, full + s);
+                tma_load_2d(st + NOP * A_BYTES + B_BYTES, &mB1, kc, j0, full + s);
+            }
+        }
+    }
+    else if (warp == 1 && lane == 0)
+    {
+        constexpr uint32_t idesc = instr_desc<KIND>(BM, BN);
+        int it = 0;
+        for (; it < nkb && ok; it++)
+        {
+            const int s = it % STAGES;
+            const uint32_t ph = (uint32_t)((it / STAGES) & 1);
+            ok = mbar_wait(full + s, ph);
+            if (!ok) break;
+            fence_after_sync();
+            const uint32_t a0 = smem_u32(smem + s * STAGE);
+            const uint32_t b0 = a0 + NOP * A_BYTES;
+#pragma unroll
+            for (int kk = 0; kk < NK; kk++)
+            {
+                const uint64_t ad = desc_sw128(a0 + kk * KSTEP);
+                const uint64_t bd = desc_sw128(b0 + kk * KSTEP);
+                mma<KIND>(tmem, ad, bd, idesc, (it > 0 || kk > 0) ? 1u : 0u);
+                if (NPROD == 3)
+                {
+                    const uint64_t bl = desc_sw128(b0 + B_BYTES + kk * KSTEP);
+                    const uint64_t al = desc_sw128(a0 + A_BYTES + kk * KSTEP);
+                    mma<KIND>(tmem, ad, bl, idesc, 1u);
+                    mma<KIND>(tmem, al, bd, idesc, 1u);
+                }
+            }
+            mma_commit(empty + s);
+        }
+        // the accumulator is final once every MMA issued above completes
+        mma_commit(accf);
+        if (!ok && p.err) atomicExch(p.err, MGX_TIMEOUT);
+    }
+    else if (warp >= 2)
+    {
+        const bool got = mbar_wait(accf, 0);
+        fence_after_sync();
+        const int q   = warp & 3; // TMEM lane quarter this warp may access
+        const int row = q * 32 + lane;
+        const int i   = i0 + row;
+        if (got && nkb > 0)
+        {
+#pragma unroll 1
+            for (int c0 = 0; c0 < BN; c0 += 32)
+            {
+                float v[32];
+                tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)c0, v);
+                if (i < p.n)
+                {
+#pragma unroll
+                    for (int t = 0; t < 32; t++)
+                    {
+                        const int j = j0 + c0 + t;
+                        if (j < p.n && (!p.symmetric || i >= j))
+                            atomicAdd(p.C + (size_t)j * p.n + i, (double)v[t]);
+                    }
+                }
+            }
+        }
+        else if (!got && p.err && lane == 0)
+            atomicExch(p.err, MGX_TIMEOUT);
+    }
+    fence_before_sync();
+    __syncthreads();
+    fence_after_sync();
+    if (warp == 1)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+            "r"(TMEM_COLS)
+                     : "memory");
+}
+
+// fp32 -> bf16 hi + lo planes (x = hi + lo + O(2^-17 |x|)); rows of K
+// values with leading dimension ld (source) and ldo (planes)
+__global__ void split_kernel(const float* __restrict__ x, size_t ld, int rows,
+    size_t K, __nv_bfloat16* __restrict__ hi, __nv_bfloat16* __restrict__ lo,
+    size_t ldo)
+{
+    const size_t per_row = (ldo + 1) / 2; // pairs per output row
+    const size_t total   = per_row * rows;
+    for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+         t += (size_t)gridDim.x * blockDim.x)
+    {
+        const size_t r = t / per_row, k = 2 * (t - r * per_row);
+        float a = 0.f, b = 0.f;
+        if (k < K) a = x[r * ld + k];
+        if (k + 1 < K) b = x[r * ld + k + 1];
+        const __nv_bfloat16 ha = __float2bfloat16_rn(a), hb = __float2bfloat16_rn(b);
+        const __nv_bfloat16 la = __float2bfloat16_rn(a - __bfloat162float(ha));
+        const __nv_bfloat16 lb = __float2bfloat16_rn(b - __bfloat162float(hb));
+        __nv_bfloat162 h2, l2;
+        h2.x = ha;
+        h2.y = hb;
+        l2.x = la;
+        l2.y = lb;
+        if (k + 1 < ldo)
+        {
+            *reinterpret_cast<__nv_bfloat162*>(hi + r * ldo + k) = h2;
+            *reinterpret_cast<__nv_bfloat162*>(lo + r * ldo + k) = l2;
+        }
+    }
+}
+
+static PFN_cuTensorMapEncodeTiled_v12000 encoder()
+{
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    if (!fn)
+    {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000,
+                cudaEnableDefault, &q)
+                == cudaSuccess
+            && q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    }
+    return fn;
+}
+
+// 2-D map over a row-major (rows x K) array with leading dimension ld
+// (elements); box = 128-byte K slice x box_rows rows, SWIZZLE_128B.
+static int make_map(CUtensorMap* m, const void* base, bool bf16, size_t K,
+    size_t rows, size_t ld, int box_rows)
+{
+    auto enc = encoder();
+    if (!enc) return fail(MGX_CUDA_ERROR, "cuTensorMapEncodeTiled unavailable");
+    const int esz = bf16 ? 2 : 4;
+    if (((uintptr_t)base % 16) || ((ld * esz) % 16))
+        return fail(MGX_BAD_ARG, "tensor-core operands need 16-byte aligned rows");
+    cuuint64_t dims[2]    = { (cuuint64_t)K, (cuuint64_t)rows };
+    cuuint64_t strides[1] = { (cuuint64_t)(ld * esz) };
+    cuuint32_t box[2]     = { (cuuint32_t)(ROWB / esz), (cuuint32_t)box_rows };
+    cuuint32_t estr[2]    = { 1, 1 };
+    CUresult r = enc(m, bf16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32,
+        2, const_cast<void*>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+        CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return fail(MGX_CUDA_ERROR, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+    return MGX_OK;
+}
+
+template <int KIND, int NPROD, int BN, int STAGES>
+static int launch(const CUtensorMap& a0, const CUtensorMap& a1, const CUtensorMap& b0,
+    const CUtensorMap& b1, const Params& p, int ntiles, int ksplit, cudaStream_t s)
+{
+    constexpr int NOP   = (NPROD == 3) ? 2 : 1;
+    constexpr int STAGE = NOP * (BM * ROWB + BN * ROWB);
+    const size_t smem   = (size_t)STAGES * STAGE + (2 * STAGES + 1) * 8 + 16 + 1024;
+    auto kern           = gram_kernel<KIND, NPROD, BN, STAGES>;
+    MGX_TRY(cuda_check(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)smem),
+        "gram_kernel smem attribute"));
+    dim3 grid(ntiles, ksplit);
+    kern<<<grid, THREADS, smem, s>>>(a0, a1, b0, b1, p);
+    MGX_LAUNCH_CHECK("tc gram_kernel");
+    return MGX_OK;
+}
+
+__global__ void finish_kernel(double* C, int n, double vel, int symmetric)
+{
+    const size_t nn = (size_t)n * n;
+    for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < nn;
+         t += (size_t)gridDim.x * blockDim.x)
+    {
+        const int i = (int)(t % n), j = (int)(t / n);
+        if (symmetric && i < j) continue;
+        double x = C[t] * vel;
+        if (!(fabs(x) > 1.e-14)) x = 0.;
+        C[t] = x;
+        if (symmetric && i != j) C[(size_t)i * n + j] = x;
+    }
+}
+} // namespace tc
+
+int gram_tcgen05(mgx_ctx* ctx, int mode, const void* A, const void* B, size_t ld,
+    size_t K, int n, double vel, int symmetric, double* C, cudaStream_t s)
+{
+    using namespace tc;
+    const bool same = (A == B);
+    const bool split = (mode == MGX_GEMM_BF16X3);
+    const int BN    = 128;
+    const int nti = (n + BM - 1) / BM, ntj = (n + BN - 1) / BN;
+    std::vector<int2> tiles;
+    for (int j = 0; j < ntj; j++)
+        for (int i = 0; i < nti; i++)
+            if (!symmetric || (i * BM + BM - 1) >= j * BN) tiles.push_back(make_int2(i, j));
+    const int ntiles = (int)tiles.size();
+    const int bk     = split ? 64 : 32;
+    const int kblocks = (int)((K + bk - 1) / bk);
+    int ksplit = std::max((4 * ctx->sm_count + ntiles - 1) / ntiles, (kblocks + 511) / 512);
+    ksplit     = std::min(ksplit, kblocks);
+    const int kb_per = (kblocks + ksplit - 1) / ksplit;
+    ksplit           = (kblocks + kb_per - 1) / kb_per;
+    if (ksplit > 65535) return fail(MGX_UNSUPPORTED, "K too large");
+
+    MGX_TRY(ctx->tc_tiles.ensure(tiles.size() * sizeof(int2)));
+    MGX_TRY(ctx->tc_err.ensure(16));
+    MGX_TRY(cuda_check(cudaMemcpyAsync(ctx->tc_tiles.ptr, tiles.data(),
+                           tiles.size() * sizeof(int2), cudaMemcpyHostToDevice, s),
+        "tile list upload"));
+    MGX_TRY(cuda_check(cudaMemsetAsync(ctx->tc_err.ptr, 0, 16, s), "err reset"));
+    MGX_TRY(cuda_check(cudaMemsetAsync(C, 0, (size_t)n * n * sizeof(double), s), "C zero"));
+
+    Params p;
+    p.tiles      = (const int2*)ctx->tc_tiles.ptr;
+    p.kblocks    = kblocks;
+    p.kb_per_cta = kb_per;
+    p.n          = n;
+    p.symmetric  = symmetric;
+    p.C          = C;
+    p.err        = (int*)ctx->tc_err.ptr;
+
+    CUtensorMap a0, a1, b0, b1;
+    if (!split)
+    {
+        MGX_TRY(make_map(&a0, A, false, K, n, ld, BM));
+        MGX_TRY(make_map(&b0, B, false, K, n, ld, BN));
+        MGX_TRY((launch<0, 1, 128, 6>(a0, a0, b0, b0, p, ntiles, ksplit, s)));
+    }
+    else
+    {
+        const size_t ldo  = ((K + 63) / 64) * 64;
+        const size_t plane = ldo * (size_t)n * sizeof(__nv_bfloat16);
+        MGX_TRY(ctx->tc_split.ensure((same ? 2 : 4) * plane));
+        char* base = (char*)ctx->tc_split.ptr;
+        auto* ahi  = (__nv_bfloat16*)base;
+        auto* alo  = (__nv_bfloat16*)(base + plane);
+        auto* bhi  = same ? ahi : (__nv_bfloat16*)(base + 2 * plane);
+        auto* blo  = same ? alo : (__nv_bfloat16*)(base + 3 * plane);
+        const int nb = (int)std::min<size_t>((ldo / 2 * n + 255) / 256, 1 << 20);
+        split_kernel<<<nb, 256, 0, s>>>((const float*)A, ld, n, K, ahi, alo, ldo);
+        MGX_LAUNCH_CHECK("split_kernel");
+        if (!same)
+        {
+            split_kernel<<<nb, 256, 0, s>>>((const float*)B, ld, n, K, bhi, blo, ldo);
+            MGX_LAUNCH_CHECK("split_kernel");
+        }
+        MGX_TRY(make_map(&a0, ahi, true, K, n, ldo, BM));
+        MGX_TRY(make_map(&a1, alo, true, K, n, ldo, BM));
+        MGX_TRY(make_map(&b0, bhi, true, K, n, ldo, BN));
+        MGX_TRY(make_map(&b1, blo, true, K, n, ldo, BN));
+        MGX_TRY((launch<1, 3, 128, 3>(a0, a1, b0, b1, p, ntiles, ksplit, s)));
+    }
+    const int nbf = (int)std::min<size_t>(((size_t)n * n + 255) / 256, 4096);
+    finish_kernel<<<nbf, 256, 0, s>>>(C, n, vel, symmetric);
+    MGX_LAUNCH_CHECK("finish_kernel");
+    int herr = 0;
+    MGX_TRY(cuda_check(cudaMemcpyAsync(&herr, ctx->tc_err.ptr, sizeof(int), cudaMemcpyDeviceToHost, s),
+        "err download"));
+    MGX_TRY(cuda_check(cudaStreamSynchronize(s), "tc gram sync"));
+    if (herr) return fail(MGX_TIMEOUT, "tensor-core pipeline wait gave up");
+    return MGX_OK;
 }
 } // namespace mgx

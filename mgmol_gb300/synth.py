@@ -65,3 +65,58 @@ def mask_radii(nfunc, seed, lo=4.0, hi=8.0):
     """Seeded localization radii U[lo, hi] bohr."""
     rng = np.random.Generator(np.random.Philox(key=seed + 70000))
     return rng.uniform(lo, hi, size=nfunc)
+
+
+def gaussian_orbitals_device(n, ll, nfunc, seed, dtype, device="cuda", noise=0.05,
+                             sigma=(1.0, 2.0), chunk=32):
+    """The same distributions as gaussian_orbitals, generated on the GPU with
+    torch's seeded device generator (used for the large benchmark blocks,
+    where host generation and upload would dominate).  Returns the block
+    (nfunc, nx*ny*nz) on `device`."""
+    import torch
+
+    g = torch.Generator(device=device)
+    g.manual_seed(int(seed))
+    L = torch.tensor(ll, dtype=torch.float64, device=device)
+    centers = torch.rand((nfunc, 3), generator=g, dtype=torch.float64, device=device) * L
+    sig = sigma[0] + (sigma[1] - sigma[0]) * torch.rand(nfunc, generator=g, dtype=torch.float64,
+                                                        device=device)
+    xs = [torch.arange(n[i], dtype=torch.float64, device=device) * (ll[i] / n[i]) for i in range(3)]
+    out = torch.empty((nfunc, n[0] * n[1] * n[2]), dtype=dtype, device=device)
+    for f0 in range(0, nfunc, chunk):
+        f1 = min(nfunc, f0 + chunk)
+        c = centers[f0:f1]
+        d2 = []
+        for i in range(3):
+            d = xs[i][None, :] - c[:, i:i + 1]
+            d = d - L[i] * torch.round(d / L[i])
+            d2.append(d * d)
+        r2 = (d2[0][:, :, None, None] + d2[1][:, None, :, None] + d2[2][:, None, None, :])
+        s = sig[f0:f1][:, None, None, None]
+        gv = torch.exp(-r2 / (2.0 * s * s))
+        gv *= 1.0 + noise * torch.randn(gv.shape, generator=g, dtype=torch.float64, device=device)
+        out[f0:f1] = gv.reshape(f1 - f0, -1).to(dtype)
+    return out, centers, sig
+
+
+def gaussian_wells_device(n, ll, nwells, seed, device="cuda", width=1.5, depth=(-2.0, -0.5)):
+    """Sum of Gaussian wells on the GPU (float64, flattened)."""
+    import torch
+
+    g = torch.Generator(device=device)
+    g.manual_seed(int(seed) + 50000)
+    L = torch.tensor(ll, dtype=torch.float64, device=device)
+    R = torch.rand((nwells, 3), generator=g, dtype=torch.float64, device=device) * L
+    dep = depth[0] + (depth[1] - depth[0]) * torch.rand(nwells, generator=g, dtype=torch.float64,
+                                                        device=device)
+    xs = [torch.arange(n[i], dtype=torch.float64, device=device) * (ll[i] / n[i]) for i in range(3)]
+    V = torch.zeros((n[0], n[1], n[2]), dtype=torch.float64, device=device)
+    for k in range(nwells):
+        d2 = []
+        for i in range(3):
+            d = xs[i] - R[k, i]
+            d = d - L[i] * torch.round(d / L[i])
+            d2.append(d * d)
+        r2 = d2[0][:, None, None] + d2[1][None, :, None] + d2[2][None, None, :]
+        V += dep[k] * torch.exp(-r2 / (2.0 * width * width))
+    return V.reshape(-1)
