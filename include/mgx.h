@@ -221,6 +221,11 @@ int mgx_gram(mgx_ctx* ctx, int mode, const void* psi, size_t ld, int nfunc,
 int mgx_hmat(mgx_ctx* ctx, int mode, const void* psi, const void* hpsi,
     size_t ld, int nfunc, double* H, void* stream);
 
+/* S and H in one call (the tensor-core modes convert Psi once for both);
+ * same conventions as mgx_gram and mgx_hmat. */
+int mgx_gram_hmat(mgx_ctx* ctx, int mode, const void* psi, const void* hpsi,
+    size_t ld, int nfunc, double* S, double* H, void* stream);
+
 /* GramMatrix::updateLS (src/GramMatrix.cc:180-191): A (n x n, FP64) is
  * overwritten by its lower Cholesky factor (upper part zeroed).  *info
  * (host) receives 0 or the 1-based index of the first non-positive pivot;

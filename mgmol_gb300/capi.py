@@ -82,6 +82,7 @@ _SIGS = {
     "mgx_masks_expand": [_vp, _i, _vp, _ip, _vp],
     "mgx_gram": [_vp, _i, _vp, _sz, _i, _vp, _vp],
     "mgx_hmat": [_vp, _i, _vp, _vp, _sz, _i, _vp, _vp],
+    "mgx_gram_hmat": [_vp, _i, _vp, _vp, _sz, _i, _vp, _vp, _vp],
     "mgx_cholesky": [_vp, _i, _vp, _ip, _vp],
     "mgx_inverse_from_cholesky": [_vp, _i, _vp, _vp, _vp],
     "mgx_trace_prod": [_vp, _i, _vp, _vp, _vp, _vp],
@@ -257,6 +258,16 @@ class Context:
         _check(load().mgx_hmat(self.handle, mode, p, ph, ld, nf, _ptr(H), _stream(stream)))
         # column-major H(i,j) = <psi_i, hpsi_j>; return the row-major view
         return H.T
+
+    def gram_hmat(self, psi, hpsi, mode=GEMM_FP64, S=None, H=None, stream=None):
+        """(S, H) with H returned as the row-major view (H[i, j] = <psi_i, hpsi_j>)."""
+        p, ld, nf = _block(psi, self.npts)
+        ph, ldh, _ = _block(hpsi, self.npts)
+        assert ldh == ld
+        S = torch.empty((nf, nf), dtype=torch.float64, device=psi.device) if S is None else S
+        H = torch.empty((nf, nf), dtype=torch.float64, device=psi.device) if H is None else H
+        _check(load().mgx_gram_hmat(self.handle, mode, p, ph, ld, nf, _ptr(S), _ptr(H), _stream(stream)))
+        return S, H.T
 
     def cholesky(self, S, stream=None):
         """Lower factor L (returned as a row-major tensor) of symmetric S."""

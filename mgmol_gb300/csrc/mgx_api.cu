@@ -80,6 +80,8 @@ int gram_cuda_cores(mgx_ctx*, int, const void*, const void*, size_t, size_t,
     int, double, int, double*, cudaStream_t);
 int gram_tcgen05(mgx_ctx*, int, const void*, const void*, size_t, size_t, int,
     double, int, double*, cudaStream_t);
+int gram_hmat_tcgen05(mgx_ctx*, int, const void*, const void*, size_t, size_t, int,
+    double, double*, double*, cudaStream_t);
 int cholesky(mgx_ctx*, int, double*, int*, cudaStream_t);
 int inverse_from_cholesky(mgx_ctx*, int, const double*, double*, cudaStream_t);
 int trace_prod(int, const double*, const double*, double*, cudaStream_t);
@@ -479,6 +481,26 @@ int mgx_hmat(mgx_ctx* ctx, int mode, const void* psi, const void* hpsi, size_t l
             return gram_tcgen05(ctx, mode, psi, hpsi, ldv, L.npts(), nfunc, vel, 0, H, s);
     }
     return fail(MGX_BAD_ARG, "gemm mode %d", mode);
+}
+
+int mgx_gram_hmat(mgx_ctx* ctx, int mode, const void* psi, const void* hpsi,
+    size_t ld, int nfunc, double* S, double* H, void* stream)
+{
+    if (!ctx) return fail(MGX_BAD_ARG, "ctx is NULL");
+    MGX_TRY(check_block(ctx->grid, psi, ld, nfunc, "psi"));
+    MGX_TRY(check_block(ctx->grid, hpsi, ld, nfunc, "hpsi"));
+    if (nfunc == 0) return MGX_OK;
+    if (!S || !H) return fail(MGX_BAD_ARG, "S or H is NULL");
+    if (mode == MGX_GEMM_TF32 || mode == MGX_GEMM_BF16X3)
+    {
+        const Level L    = make_level(ctx->grid, 0);
+        const double vel = L.h[0] * L.h[1] * L.h[2];
+        const size_t ldv = nfunc > 1 ? ld : L.npts();
+        return gram_hmat_tcgen05(ctx, mode, psi, hpsi, ldv, L.npts(), nfunc, vel, S, H,
+            (cudaStream_t)stream);
+    }
+    MGX_TRY(mgx_gram(ctx, mode, psi, ld, nfunc, S, stream));
+    return mgx_hmat(ctx, mode, psi, hpsi, ld, nfunc, H, stream);
 }
 
 int mgx_cholesky(mgx_ctx* ctx, int n, double* A, int* info, void* stream)

@@ -65,89 +65,87 @@ __device__ __forceinline__ T mask_point(const MaskDev& m, int f, int x, int y,
 }
 
 /* restriction of nfunc functions; accumulation type A (double for the FP64
- * path, as the reference; float for the FP32 path) */
+ * path, as the reference; float for the FP32 path).  One block per coarse
+ * (i, j) line, threads along coarse z; blockIdx.y = function. */
 template <typename T, typename A>
-__global__ void restrict_kernel(const T* fine, size_t ldf, T* coarse, size_t ldc,
-    int fx, int fy, int fz, MaskDev mask)
+__global__ void restrict_kernel(const T* __restrict__ fine, size_t ldf,
+    T* __restrict__ coarse, size_t ldc, int fx, int fy, int fz, MaskDev mask)
 {
-    const int cx = fx >> 1, cy = fy >> 1, cz = fz >> 1;
-    const size_t cn = (size_t)cx * cy * cz;
-    const int f     = blockIdx.y;
-    const T* u      = fine + (size_t)f * ldf;
-    for (size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x; idx < cn;
-         idx += (size_t)gridDim.x * blockDim.x)
+    const int cy = fy >> 1, cz = fz >> 1;
+    const int f  = blockIdx.y;
+    const int i  = blockIdx.x / cy, j = blockIdx.x - (blockIdx.x / cy) * cy;
+    const T* u   = fine + (size_t)f * ldf;
+    const int x = 2 * i, y = 2 * j;
+    const int xm = wrp(x - 1, fx), xp = wrp(x + 1, fx);
+    const int ym = wrp(y - 1, fy), yp = wrp(y + 1, fy);
+    const T* r00 = u + ((size_t)x * fy + y) * fz;
+    const T* rp0 = u + ((size_t)xp * fy + y) * fz;
+    const T* rm0 = u + ((size_t)xm * fy + y) * fz;
+    const T* r0p = u + ((size_t)x * fy + yp) * fz;
+    const T* r0m = u + ((size_t)x * fy + ym) * fz;
+    const T* rpp = u + ((size_t)xp * fy + yp) * fz;
+    const T* rpm = u + ((size_t)xp * fy + ym) * fz;
+    const T* rmp = u + ((size_t)xm * fy + yp) * fz;
+    const T* rmm = u + ((size_t)xm * fy + ym) * fz;
+    for (int k = threadIdx.x; k < cz; k += blockDim.x)
     {
-        const int k = (int)(idx % cz);
-        const int j = (int)((idx / cz) % cy);
-        const int i = (int)(idx / ((size_t)cz * cy));
-        const int x = 2 * i, y = 2 * j, z = 2 * k;
-        const int xm = wrp(x - 1, fx), xp = wrp(x + 1, fx);
-        const int ym = wrp(y - 1, fy), yp = wrp(y + 1, fy);
-        const int zm = wrp(z - 1, fz), zp = wrp(z + 1, fz);
-        auto U = [&](int a, int b, int c) -> A {
-            return (A)u[((size_t)a * fy + b) * fz + c];
-        };
-        const A face = U(xp, y, z) + U(xm, y, z) + U(x, yp, z) + U(x, ym, z)
-                       + U(x, y, zm) + U(x, y, zp);
-        const A corner = U(xp, yp, zm) + U(xp, yp, zp) + U(xp, ym, zm)
-                         + U(xp, ym, zp) + U(xm, yp, zm) + U(xm, yp, zp)
-                         + U(xm, ym, zm) + U(xm, ym, zp);
-        const A edge = U(x, yp, zm) + U(x, yp, zp) + U(x, ym, zm) + U(x, ym, zp)
-                       + U(xp, y, zm) + U(xp, y, zp) + U(xm, y, zm)
-                       + U(xm, y, zp) + U(xm, ym, z) + U(xp, ym, z)
-                       + U(xm, yp, z) + U(xp, yp, z);
-        const A r = (A)(1. / 64.)
-                    * ((A)8. * U(x, y, z) + (A)4. * face + (A)2. * edge + corner);
-        coarse[(size_t)f * ldc + idx] = mask_point<T>(mask, f, i, j, k, (T)r);
+        const int z = 2 * k, zm = wrp(z - 1, fz), zp = wrp(z + 1, fz);
+        // grouping and order of src/pb/MGkernels.cc:249-270
+        const A face = (A)rp0[z] + (A)rm0[z] + (A)r0p[z] + (A)r0m[z] + (A)r00[zm] + (A)r00[zp];
+        const A corner = (A)rpp[zm] + (A)rpp[zp] + (A)rpm[zm] + (A)rpm[zp] + (A)rmp[zm]
+                         + (A)rmp[zp] + (A)rmm[zm] + (A)rmm[zp];
+        const A edge = (A)r0p[zm] + (A)r0p[zp] + (A)r0m[zm] + (A)r0m[zp] + (A)rp0[zm]
+                       + (A)rp0[zp] + (A)rm0[zm] + (A)rm0[zp] + (A)rmm[z] + (A)rpm[z]
+                       + (A)rmp[z] + (A)rpp[z];
+        const A r = (A)(1. / 64.) * ((A)8. * (A)r00[z] + (A)4. * face + (A)2. * edge + corner);
+        coarse[(size_t)f * ldc + ((size_t)i * cy + j) * cz + k]
+            = mask_point<T>(mask, f, i, j, k, (T)r);
     }
 }
 
-/* trilinear prolongation; MODE 0: out = P e; MODE 1: out -= mask(P e) */
+/* trilinear prolongation; MODE 0: out = P e; MODE 1: out -= mask(P e).
+ * One block per fine (x, y) line, threads along fine z. */
 template <typename T, int MODE>
-__global__ void prolong_kernel(const T* coarse, size_t ldc, T* out, size_t ldo,
-    int fx, int fy, int fz, MaskDev mask)
+__global__ void prolong_kernel(const T* __restrict__ coarse, size_t ldc,
+    T* __restrict__ out, size_t ldo, int fx, int fy, int fz, MaskDev mask)
 {
     const int cx = fx >> 1, cy = fy >> 1, cz = fz >> 1;
-    const size_t fn = (size_t)fx * fy * fz;
-    const int f     = blockIdx.y;
-    const T* e      = coarse + (size_t)f * ldc;
-    for (size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x; idx < fn;
-         idx += (size_t)gridDim.x * blockDim.x)
+    const int f  = blockIdx.y;
+    const int x  = blockIdx.x / fy, y = blockIdx.x - (blockIdx.x / fy) * fy;
+    const T* e   = coarse + (size_t)f * ldc;
+    const int i = x >> 1, j = y >> 1, a = x & 1, b = y & 1;
+    const int i1 = wrp(i + 1, cx), j1 = wrp(j + 1, cy);
+    const T* c00 = e + ((size_t)i * cy + j) * cz;
+    const T* c01 = e + ((size_t)i * cy + j1) * cz;
+    const T* c10 = e + ((size_t)i1 * cy + j) * cz;
+    const T* c11 = e + ((size_t)i1 * cy + j1) * cz;
+    T* o         = out + (size_t)f * ldo + ((size_t)x * fy + y) * fz;
+    for (int z = threadIdx.x; z < fz; z += blockDim.x)
     {
-        const int z = (int)(idx % fz);
-        const int y = (int)((idx / fz) % fy);
-        const int x = (int)(idx / ((size_t)fz * fy));
-        const int i = x >> 1, j = y >> 1, k = z >> 1;
-        const int a = x & 1, b = y & 1, c = z & 1;
-        const int i1 = wrp(i + 1, cx), j1 = wrp(j + 1, cy), k1 = wrp(k + 1, cz);
-        auto C = [&](int p, int q, int r) -> T {
-            return e[((size_t)p * cy + q) * cz + r];
-        };
+        const int k = z >> 1, c = z & 1, k1 = wrp(k + 1, cz);
         T v;
         // operation order of src/pb/MGkernels.cc:84-197
         if (!a && !b && !c)
-            v = C(i, j, k);
+            v = c00[k];
         else if (!a && !b && c)
-            v = (T)0.5 * (C(i, j, k) + C(i, j, k1));
+            v = (T)0.5 * (c00[k] + c00[k1]);
         else if (!a && b && !c)
-            v = (T)0.5 * (C(i, j1, k) + C(i, j, k));
+            v = (T)0.5 * (c01[k] + c00[k]);
         else if (!a && b && c)
-            v = (T)0.25 * (C(i, j1, k1) + C(i, j, k1) + C(i, j1, k) + C(i, j, k));
+            v = (T)0.25 * (c01[k1] + c00[k1] + c01[k] + c00[k]);
         else if (a && !b && c)
-            v = (T)0.25 * (C(i1, j, k1) + C(i1, j, k) + C(i, j, k1) + C(i, j, k));
+            v = (T)0.25 * (c10[k1] + c10[k] + c00[k1] + c00[k]);
         else if (a && !b && !c)
-            v = (T)0.5 * (C(i1, j, k) + C(i, j, k));
+            v = (T)0.5 * (c10[k] + c00[k]);
         else if (a && b && c)
             v = (T)0.125
-                * (C(i1, j1, k1) + C(i1, j1, k) + C(i1, j, k1) + C(i1, j, k)
-                    + C(i, j1, k1) + C(i, j1, k) + C(i, j, k1) + C(i, j, k));
+                * (c11[k1] + c11[k] + c10[k1] + c10[k] + c01[k1] + c01[k] + c00[k1] + c00[k]);
         else
-            v = (T)0.25 * (C(i1, j1, k) + C(i1, j, k) + C(i, j1, k) + C(i, j, k));
-        T* o = out + (size_t)f * ldo + idx;
+            v = (T)0.25 * (c11[k] + c10[k] + c01[k] + c00[k]);
         if (MODE == 0)
-            *o = v;
+            o[z] = v;
         else
-            *o = *o - mask_point<T>(mask, f, x, y, z, v);
+            o[z] = o[z] - mask_point<T>(mask, f, x, y, z, v);
     }
 }
 
@@ -187,13 +185,13 @@ static dim3 grid_for(size_t npts, int nfunc)
 int restrict_launch(int dtype, const Level& fine, const void* f, size_t ldf,
     void* c, size_t ldc, int nfunc, const MaskDev& mask, cudaStream_t s)
 {
-    const size_t cn = fine.npts() / 8;
-    const dim3 g    = grid_for(cn, nfunc);
+    const dim3 g((fine.n[0] / 2) * (fine.n[1] / 2), nfunc);
+    const int nt = std::min(256, std::max(32, ((fine.n[2] / 2 + 31) / 32) * 32));
     if (dtype == MGX_F64)
-        restrict_kernel<double, double><<<g, 256, 0, s>>>((const double*)f, ldf,
+        restrict_kernel<double, double><<<g, nt, 0, s>>>((const double*)f, ldf,
             (double*)c, ldc, fine.n[0], fine.n[1], fine.n[2], mask);
     else
-        restrict_kernel<float, float><<<g, 256, 0, s>>>((const float*)f, ldf,
+        restrict_kernel<float, float><<<g, nt, 0, s>>>((const float*)f, ldf,
             (float*)c, ldc, fine.n[0], fine.n[1], fine.n[2], mask);
     MGX_LAUNCH_CHECK("restrict_kernel");
     return MGX_OK;
@@ -203,23 +201,24 @@ int prolong_launch(int dtype, int mode, const Level& fine, const void* c,
     size_t ldc, void* out, size_t ldo, int nfunc, const MaskDev& mask,
     cudaStream_t s)
 {
-    const dim3 g = grid_for(fine.npts(), nfunc);
+    const dim3 g(fine.n[0] * fine.n[1], nfunc);
+    const int nt = std::min(256, std::max(32, ((fine.n[2] + 31) / 32) * 32));
     if (dtype == MGX_F64)
     {
         if (mode == 0)
-            prolong_kernel<double, 0><<<g, 256, 0, s>>>((const double*)c, ldc,
+            prolong_kernel<double, 0><<<g, nt, 0, s>>>((const double*)c, ldc,
                 (double*)out, ldo, fine.n[0], fine.n[1], fine.n[2], mask);
         else
-            prolong_kernel<double, 1><<<g, 256, 0, s>>>((const double*)c, ldc,
+            prolong_kernel<double, 1><<<g, nt, 0, s>>>((const double*)c, ldc,
                 (double*)out, ldo, fine.n[0], fine.n[1], fine.n[2], mask);
     }
     else
     {
         if (mode == 0)
-            prolong_kernel<float, 0><<<g, 256, 0, s>>>((const float*)c, ldc,
+            prolong_kernel<float, 0><<<g, nt, 0, s>>>((const float*)c, ldc,
                 (float*)out, ldo, fine.n[0], fine.n[1], fine.n[2], mask);
         else
-            prolong_kernel<float, 1><<<g, 256, 0, s>>>((const float*)c, ldc,
+            prolong_kernel<float, 1><<<g, nt, 0, s>>>((const float*)c, ldc,
                 (float*)out, ldo, fine.n[0], fine.n[1], fine.n[2], mask);
     }
     MGX_LAUNCH_CHECK("prolong_kernel");

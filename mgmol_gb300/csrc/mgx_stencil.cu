@@ -261,22 +261,38 @@ struct PointOp
 };
 
 /* ------------------------------------------------------------------ */
-/* staged (bulk-copy) plane kernel                                       */
+/* staged, register-pipelined plane kernel                              */
 /* ------------------------------------------------------------------ */
-template <typename T, typename TV, int LAP, int OP, int R, int S>
+// Each thread owns up to NP points (y, z) of the CTA's y-band and marches
+// with them through the x-planes of its chunk.  Planes arrive in a ring of
+// S shared-memory stages (1-D bulk copies of TY + 2RR whole z lines).
+//  - Radius-1 "Mehrstellen-like" operators (LAP 0 and the B operator)
+//    fold plane p, as soon as it lands, into a(p) (the part of the output at
+//    p that lives in plane p) and b(p) (what plane p adds to its two x
+//    neighbours): out(x) = a(x) + b(x-1) + b(x+1).  One plane is read per
+//    point and step (9 values, plus 5 of V for B(V psi)).
+//  - Axis stencils of radius R keep the centre column u(x-R..x+R) in a
+//    register queue and read the y/z neighbours of plane x from the stage
+//    still resident when plane x+R lands (4R + 1 values per point).
+template <typename T, typename TV, int LAP, int OP, int R, int S, int NP>
 __global__ void __launch_bounds__(256) plane_kernel(PlaneParams p, DevCoef<T> c)
 {
+    constexpr bool MEHRLIKE = (LAP == 0) || (OP == OP_RHS);
+    constexpr int RR        = MEHRLIKE ? 1 : R; // halo rows staged
+    constexpr int HOLD      = MEHRLIKE ? 0 : R; // stages kept behind the newest
+    constexpr bool STAGE_V  = (OP == OP_HPSI_B);
+    constexpr int QL        = MEHRLIKE ? 1 : 2 * R + 1;
     extern __shared__ __align__(128) unsigned char smem_raw[];
-    constexpr bool STAGE_V = (OP == OP_HPSI_B);
+
     const int nx = p.n[0], ny = p.n[1], nz = p.n[2];
-    const int TY     = p.ty;
-    const int rows   = TY + 2 * R;
-    const int tile_y = blockIdx.x % p.ntile_y;
-    const int tile_x = blockIdx.x / p.ntile_y;
-    const int f      = blockIdx.y;
-    const int y0     = tile_y * TY;
-    const int x0     = tile_x * p.xc;
-    const int xcount = min(p.xc, nx - x0);
+    const int TY      = p.ty;
+    const int rows    = TY + 2 * RR;
+    const int tile_y  = blockIdx.x % p.ntile_y;
+    const int tile_x  = blockIdx.x / p.ntile_y;
+    const int f       = blockIdx.y;
+    const int y0      = tile_y * TY;
+    const int x0      = tile_x * p.xc;
+    const int xcount  = min(p.xc, nx - x0);
     const int nplanes = xcount + 2 * R;
 
     const size_t stage_elems = (size_t)rows * nz;
@@ -288,52 +304,44 @@ __global__ void __launch_bounds__(256) plane_kernel(PlaneParams p, DevCoef<T> c)
     const T* ubase  = reinterpret_cast<const T*>(p.u) + (size_t)f * p.ldu;
     const TV* vbase = reinterpret_cast<const TV*>(p.V);
 
-    // rows y0-R .. y0+TY+R-1 (mod ny): run A then (if wrapped) run B
-    int ya = y0 - R;
-    int na, yb, nb;
+    // staged rows y0-RR .. y0+TY+RR-1 (mod ny) as at most two runs
+    int ya = y0 - RR, na, nb;
     if (ya < 0)
     {
-        // rows [ny+ya, ny) then [0, y0+TY+R)
-        yb = 0;
-        nb = y0 + TY + R;
         na = -ya;
-        ya = ny + ya;
+        ya += ny;
+        nb = rows - na;
     }
-    else if (y0 + TY + R > ny)
+    else if (ya + rows > ny)
     {
         na = ny - ya;
-        yb = 0;
-        nb = y0 + TY + R - ny;
+        nb = rows - na;
     }
     else
     {
         na = rows;
-        yb = 0;
         nb = 0;
     }
     const uint32_t bytes_u = (uint32_t)(stage_elems * sizeof(T));
     const uint32_t bytes_v = STAGE_V ? (uint32_t)(stage_elems * sizeof(TV)) : 0u;
 
-    auto issue = [&](int plane_idx) {
-        const int slot = plane_idx % S;
-        const int x    = wrap(x0 - R + plane_idx, nx);
+    auto issue = [&](int i) {
+        const int slot = i % S;
+        const int x    = wrap(x0 - R + i, nx);
         uint64_t* bar  = bars + slot;
         mbar_arrive_expect_tx(bar, bytes_u + bytes_v);
-        T* dst         = stages + slot * stage_elems;
-        const T* src   = ubase + ((size_t)x * ny) * nz;
+        T* dst       = stages + slot * stage_elems;
+        const T* src = ubase + (size_t)x * ny * nz;
         bulk_g2s(dst, src + (size_t)ya * nz, (uint32_t)(na * nz * sizeof(T)), bar);
         if (nb > 0)
-            bulk_g2s(dst + (size_t)na * nz, src + (size_t)yb * nz,
-                (uint32_t)(nb * nz * sizeof(T)), bar);
+            bulk_g2s(dst + (size_t)na * nz, src, (uint32_t)(nb * nz * sizeof(T)), bar);
         if (STAGE_V)
         {
             TV* vdst       = vstages + slot * stage_elems;
-            const TV* vsrc = vbase + ((size_t)x * ny) * nz;
-            bulk_g2s(vdst, vsrc + (size_t)ya * nz,
-                (uint32_t)(na * nz * sizeof(TV)), bar);
+            const TV* vsrc = vbase + (size_t)x * ny * nz;
+            bulk_g2s(vdst, vsrc + (size_t)ya * nz, (uint32_t)(na * nz * sizeof(TV)), bar);
             if (nb > 0)
-                bulk_g2s(vdst + (size_t)na * nz, vsrc + (size_t)yb * nz,
-                    (uint32_t)(nb * nz * sizeof(TV)), bar);
+                bulk_g2s(vdst + (size_t)na * nz, vsrc, (uint32_t)(nb * nz * sizeof(TV)), bar);
         }
     };
 
@@ -344,78 +352,173 @@ __global__ void __launch_bounds__(256) plane_kernel(PlaneParams p, DevCoef<T> c)
         fence_mbar_init();
     }
     __syncthreads();
+    int issued = min(S, nplanes) - 1;
     if (threadIdx.x == 0)
-    {
-        const int pre = min(S, nplanes);
-        for (int i = 0; i < pre; i++)
+        for (int i = 0; i <= issued; i++)
             issue(i);
+
+    // per-point geometry, fixed for the whole march
+    const int npts = TY * nz;
+    int oc[NP], ozm[NP], ozp[NP], zz[NP], yy[NP];
+    bool val[NP];
+#pragma unroll
+    for (int k = 0; k < NP; k++)
+    {
+        const int pt = threadIdx.x + k * 256;
+        const int y  = pt / nz;
+        const int z  = pt - y * nz;
+        val[k]       = (pt < npts) && (y0 + y < ny);
+        yy[k]        = y;
+        zz[k]        = z;
+        oc[k]        = (y + RR) * nz + z;
+        ozm[k]       = oc[k] + (z > 0 ? -1 : nz - 1);
+        ozp[k]       = oc[k] + (z < nz - 1 ? 1 : 1 - nz);
+    }
+    T A1[NP], B1[NP], B2[NP], U1[NP];
+    T q[NP][QL];
+#pragma unroll
+    for (int k = 0; k < NP; k++)
+    {
+        A1[k] = B1[k] = B2[k] = U1[k] = (T)0;
+#pragma unroll
+        for (int j = 0; j < QL; j++)
+            q[k][j] = (T)0;
     }
 
-    const int npts = TY * nz;
-    bool ok        = true;
-    int waited     = -1; // planes 0..waited have completed
-    int issued     = min(S, nplanes) - 1;
-    for (int io = 0; io < xcount; io++)
-    {
-        // planes io .. io+2R must be resident; the newest is io+2R
+    T* __restrict__ outp     = reinterpret_cast<T*>(p.out) + (size_t)f * p.ldo;
+    T* __restrict__ wp       = p.w ? reinterpret_cast<T*>(p.w) + (size_t)f * p.ldw : nullptr;
+    const T* __restrict__ fp = p.f ? reinterpret_cast<const T*>(p.f) + (size_t)f * p.ldf : nullptr;
+    constexpr bool POINTWISE = (OP == OP_JACOBI) || (OP == OP_HPSI_V);
+
+    // pv: the pointwise operand at the emitted point (f for Jacobi, V for
+    // V psi), loaded before the plane wait so that its latency overlaps it
+    auto finish = [&](int k, int x, T lap, T ucen, T pv) {
+        const int y      = y0 + yy[k];
+        const int z      = zz[k];
+        const size_t idx = ((size_t)x * ny + y) * nz + z;
+        T r              = lap;
+        if (OP == OP_HPSI_V) r = lap + (T)((TV)ucen * (TV)pv);
+        if (OP == OP_JACOBI)
         {
-            const int need = io + 2 * R;
-            for (int i = waited + 1; i <= need && ok; i++)
+            T w = lap - pv;
+            r   = ucen - c.jf * w;
+            if (p.mask.state != nullptr)
             {
-                ok = mbar_wait(bars + (i % S), (uint32_t)((i / S) & 1));
-                if (ok) waited = i;
+                r = apply_mask<T>(p.mask, f, x, y, z, r);
+                if (wp != nullptr) w = apply_mask<T>(p.mask, f, x, y, z, w);
+            }
+            if (wp != nullptr) wp[idx] = w;
+        }
+        outp[idx] = r;
+    };
+
+    bool ok    = true;
+    int waited = -1;
+    for (int i = 0; i < nplanes; i++)
+    {
+        T pv[NP];
+        if (POINTWISE)
+        {
+            const int xe = MEHRLIKE ? x0 + i - 2 : x0 + i - 2 * R;
+            if (xe >= x0)
+            {
+#pragma unroll
+                for (int k = 0; k < NP; k++)
+                {
+                    const size_t idx = ((size_t)xe * ny + y0 + yy[k]) * nz + zz[k];
+                    pv[k]            = (T)0;
+                    if (val[k]) pv[k] = (OP == OP_JACOBI) ? fp[idx] : (T)vbase[idx];
+                }
             }
         }
-        const int x = x0 + io;
-        for (int pt = threadIdx.x; pt < npts; pt += blockDim.x)
+        ok = ok && mbar_wait(bars + (i % S), (uint32_t)((i / S) & 1));
+        if (ok) waited = i;
+        const T* st = stages + (i % S) * stage_elems;
+        if (MEHRLIKE)
         {
-            const int yy = pt / nz;
-            const int z  = pt - yy * nz;
-            auto at      = [&](int dx, int dy, int dz) -> T {
-                const T* st = stages + ((io + R + dx) % S) * stage_elems;
-                return st[(size_t)(yy + R + dy) * nz + wrap(z + dz, nz)];
-            };
-            auto vat = [&](int dx, int dy, int dz) -> TV {
-                if (STAGE_V)
-                {
-                    const TV* st = vstages + ((io + R + dx) % S) * stage_elems;
-                    return st[(size_t)(yy + R + dy) * nz + wrap(z + dz, nz)];
-                }
-                const int y = y0 + yy;
-                return vbase[((size_t)x * ny + y) * nz + z];
-            };
-            const int y      = y0 + yy;
-            const size_t idx = ((size_t)x * ny + y) * nz + z;
-            T wres           = (T)0;
-            T r = PointOp<T, TV, LAP, OP, R>::apply(p, c, at, vat, f, idx, &wres);
-            if (OP == OP_JACOBI)
+            const TV* vs = vstages + (i % S) * stage_elems;
+            const bool emit = (i >= 2);
+            const int x     = x0 + i - 2;
+#pragma unroll
+            for (int k = 0; k < NP; k++)
             {
-                if (p.mask.state != nullptr)
+                if (!val[k]) continue;
+                const T u = st[oc[k]], uzm = st[ozm[k]], uzp = st[ozp[k]];
+                const T uym = st[oc[k] - nz], uyp = st[oc[k] + nz];
+                T a, b;
+                if (OP == OP_RHS)
                 {
-                    r = apply_mask<T>(p.mask, f, x, y, z, r);
-                    if (p.w != nullptr)
-                        wres = apply_mask<T>(p.mask, f, x, y, z, wres);
+                    a = (T)0.5 * u + (T)(1. / 12.) * (uym + uyp + uzm + uzp);
+                    b = (T)(1. / 12.) * u;
                 }
-                if (p.w != nullptr)
-                    reinterpret_cast<T*>(p.w)[(size_t)f * p.ldw + idx] = wres;
+                else
+                {
+                    const T sz = uzm + uzp, sy = uym + uyp;
+                    const T corners = st[ozm[k] - nz] + st[ozp[k] - nz] + st[ozm[k] + nz]
+                                      + st[ozp[k] + nz];
+                    a = c.c0 * u + c.cz[0] * sz + c.cy[0] * sy + c.cyz * corners;
+                    b = c.cx[0] * u + c.cxz * sz + c.cxy * sy;
+                    if (STAGE_V)
+                    {
+                        const T wc = (T)((TV)u * vs[oc[k]]);
+                        const T wf = (T)((TV)uzm * vs[ozm[k]]) + (T)((TV)uzp * vs[ozp[k]])
+                                     + (T)((TV)uym * vs[oc[k] - nz])
+                                     + (T)((TV)uyp * vs[oc[k] + nz]);
+                        a += (T)0.5 * wc + (T)(1. / 12.) * wf;
+                        b += (T)(1. / 12.) * wc;
+                    }
+                }
+                if (emit) finish(k, x, A1[k] + B2[k] + b, U1[k], POINTWISE ? pv[k] : (T)0);
+                B2[k] = B1[k];
+                B1[k] = b;
+                A1[k] = a;
+                U1[k] = u;
             }
-            reinterpret_cast<T*>(p.out)[(size_t)f * p.ldo + idx] = r;
+        }
+        else
+        {
+            const bool emit = (i >= 2 * R);
+            const int x     = x0 + i - 2 * R;
+            const T* sc     = stages + ((i - R + S) % S) * stage_elems; // plane x
+#pragma unroll
+            for (int k = 0; k < NP; k++)
+            {
+                if (!val[k]) continue;
+#pragma unroll
+                for (int j = 0; j < QL - 1; j++)
+                    q[k][j] = q[k][j + 1];
+                q[k][QL - 1] = st[oc[k]];
+                if (emit)
+                {
+                    const int z = zz[k];
+                    T r         = c.c0 * q[k][R];
+#pragma unroll
+                    for (int d = 1; d <= R; d++)
+                    {
+                        const int zp = (z + d < nz) ? d : d - nz;
+                        const int zm = (z - d >= 0) ? -d : nz - d;
+                        r += c.cx[d - 1] * (q[k][R - d] + q[k][R + d]);
+                        r += c.cy[d - 1] * (sc[oc[k] - d * nz] + sc[oc[k] + d * nz]);
+                        r += c.cz[d - 1] * (sc[oc[k] + zm] + sc[oc[k] + zp]);
+                    }
+                    finish(k, x, r, q[k][R], POINTWISE ? pv[k] : (T)0);
+                }
+            }
         }
         __syncthreads();
-        if (io + S < nplanes)
+        const int nxt = i - HOLD + S;
+        if (nxt < nplanes && nxt > issued)
         {
             if (threadIdx.x == 0)
             {
                 fence_proxy_async_smem();
-                issue(io + S);
+                issue(nxt);
             }
-            issued = io + S;
+            issued = nxt;
         }
     }
     if (!ok && threadIdx.x == 0)
     {
-        // a wait gave up: record it, then let the copies still in flight land
-        // (bounded) before the block releases its shared memory
         if (p.err != nullptr) atomicExch(p.err, MGX_TIMEOUT);
         for (int i = waited + 1; i <= issued; i++)
             mbar_wait(bars + (i % S), (uint32_t)((i / S) & 1));
@@ -466,10 +569,13 @@ __global__ void __launch_bounds__(256) direct_kernel(PlaneParams p, DevCoef<T> c
 /* ------------------------------------------------------------------ */
 /* launcher                                                             */
 /* ------------------------------------------------------------------ */
-template <int R>
+constexpr int PLANE_NP = 8; // points per thread (TY * nz <= 2048)
+
+template <int LAP, int OP, int R>
 constexpr int stages_for()
 {
-    return R == 1 ? 6 : (R == 2 ? 7 : (R == 3 ? 9 : 10));
+    // ring depth: planes held behind the newest + 3 in flight
+    return ((LAP == 0) || (OP == OP_RHS)) ? 4 : R + 4;
 }
 
 template <typename T, typename TV, int LAP, int OP, int R>
@@ -477,7 +583,8 @@ static int launch_t(const PlaneParams& p0, const DevCoef<T>& c, int nfunc,
     cudaStream_t stream, int force_direct)
 {
     PlaneParams p = p0;
-    constexpr int S = stages_for<R>();
+    constexpr int S  = stages_for<LAP, OP, R>();
+    constexpr int RR = ((LAP == 0) || (OP == OP_RHS)) ? 1 : R;
     constexpr bool STAGE_V = (OP == OP_HPSI_B);
     const int nx = p.n[0], ny = p.n[1], nz = p.n[2];
     const size_t esz = sizeof(T) + (STAGE_V ? sizeof(TV) : 0);
@@ -489,30 +596,27 @@ static int launch_t(const PlaneParams& p0, const DevCoef<T>& c, int nfunc,
         staged = false;
     if (STAGE_V && ((nz * sizeof(TV)) % 16 || ((uintptr_t)p.V % 16)))
         staged = false;
-    // rows per tile: divides ny, leaves room for the halo, fits shared memory
+    if (nz < 2 * RR + 1 || nx < R) staged = false;
+    // rows per tile: as many as the per-thread point budget allows, room for
+    // the halo (one wrap at most), shared memory within ~110 KB
     int ty = 0;
     if (staged)
     {
         const size_t smem_cap = 110 * 1024;
-        for (int cand = 32; cand >= 1; cand /= 2)
+        int cand = std::min(32, (256 * PLANE_NP) / nz);
+        cand     = std::min(cand, ny - 2 * RR);
+        for (; cand >= 1; cand--)
         {
-            if (ny % cand) continue;
-            if (cand + 2 * R > ny) continue;
-            const size_t sm = (size_t)S * (cand + 2 * R) * nz * esz + S * 8;
-            if (sm > smem_cap) continue;
-            if (cand * nz < 256 && cand < ny - 2 * R && cand < 32)
-            {
-                // prefer bigger tiles when the plane is narrow
-            }
-            ty = cand;
-            break;
+            const size_t sm = (size_t)S * (cand + 2 * RR) * nz * esz + S * 8;
+            if (sm <= smem_cap) break;
         }
-        if (ty == 0 || nz > 4096) staged = false;
+        ty = cand;
+        if (ty < 1 || nz > 256 * PLANE_NP) staged = false;
     }
     if (staged)
     {
         p.ty      = ty;
-        p.ntile_y = ny / ty;
+        p.ntile_y = (ny + ty - 1) / ty;
         // x chunk: enough CTAs to fill the GPU, little halo re-read
         int xc = 32;
         while (xc > 4 && (size_t)p.ntile_y * ((nx + xc - 1) / xc) * nfunc < 4 * 152)
@@ -520,8 +624,8 @@ static int launch_t(const PlaneParams& p0, const DevCoef<T>& c, int nfunc,
         if (xc > nx) xc = nx;
         p.xc       = xc;
         p.ntile_x  = (nx + xc - 1) / xc;
-        const size_t smem = (size_t)S * (ty + 2 * R) * nz * esz + S * 8;
-        auto kern         = plane_kernel<T, TV, LAP, OP, R, S>;
+        const size_t smem = (size_t)S * (ty + 2 * RR) * nz * esz + S * 8;
+        auto kern         = plane_kernel<T, TV, LAP, OP, R, S, PLANE_NP>;
         cudaError_t e     = cudaFuncSetAttribute(
             kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return cuda_check(e, "plane_kernel smem attribute");

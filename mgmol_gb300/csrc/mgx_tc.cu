@@ -131,9 +131,10 @@ struct Params
     const int2* tiles;
     int kblocks;    // total K blocks
     int kb_per_cta; // K blocks per CTA
-    int n;          // matrix order
+    int n;          // rows of C (and its leading dimension)
+    int ncols;      // columns of C produced by this launch
     int symmetric;  // only i >= j entries of C are produced
-    double* C;      // column-major n x n, FP64, accumulated atomically
+    double* C;      // column-major, leading dimension n, FP64, accumulated atomically
     int* err;
 };
 
@@ -273,7 +274,7 @@ __global__ void __launch_bounds__(THREADS, 1) gram_kernel(
                     for (int t = 0; t < 32; t++)
                     {
                         const int j = j0 + c0 + t;
-                        if (j < p.n && (!p.symmetric || i >= j))
+                        if (j < p.ncols && (!p.symmetric || i >= j))
                             atomicAdd(p.C + (size_t)j * p.n + i, (double)v[t]);
                     }
                 }
@@ -393,83 +394,230 @@ __global__ void finish_kernel(double* C, int n, double vel, int symmetric)
 }
 } // namespace tc
 
-int gram_tcgen05(mgx_ctx* ctx, int mode, const void* A, const void* B, size_t ld,
-    size_t K, int n, double vel, int symmetric, double* C, cudaStream_t s)
+namespace
+{
+struct Operand
+{
+    CUtensorMap m0, m1;
+    const void* base0 = nullptr;
+    const void* base1 = nullptr;
+    bool bf16         = false;
+    size_t K = 0, ld = 0;
+    int rows = 0;
+};
+
+/* re-encodes the maps of an operand with another box height */
+int rebox(Operand& op, int box_rows)
+{
+    MGX_TRY(tc::make_map(&op.m0, op.base0, op.bf16, op.K, op.rows, op.ld, box_rows));
+    if (op.base1)
+        MGX_TRY(tc::make_map(&op.m1, op.base1, op.bf16, op.K, op.rows, op.ld, box_rows));
+    else
+        op.m1 = op.m0;
+    return MGX_OK;
+}
+
+/* Prepares the tensor maps of one operand (rows x K, leading dimension ld):
+ * TF32 reads the FP32 data in place (or a 16-byte aligned copy in `ws`);
+ * BF16X3 writes the hi / lo planes into `ws`.  Returns the workspace bytes
+ * used in *used. */
+int prepare(int mode, const void* X, size_t ld, size_t K, int rows, int box_rows,
+    char* ws, size_t* used, Operand& op, cudaStream_t s)
 {
     using namespace tc;
-    const bool same = (A == B);
-    const bool split = (mode == MGX_GEMM_BF16X3);
-    const int BN    = 128;
-    const int nti = (n + BM - 1) / BM, ntj = (n + BN - 1) / BN;
+    *used = 0;
+    if (mode == MGX_GEMM_TF32)
+    {
+        if (((uintptr_t)X % 16) || ((ld * 4) % 16))
+        {
+            const size_t ldp = ((K + 31) / 32) * 32;
+            MGX_TRY(cuda_check(cudaMemcpy2DAsync(ws, ldp * 4, X, ld * 4, K * 4, rows,
+                                   cudaMemcpyDeviceToDevice, s),
+                "tf32 pad copy"));
+            X     = ws;
+            ld    = ldp;
+            *used = ldp * (size_t)rows * 4;
+        }
+        MGX_TRY(make_map(&op.m0, X, false, K, rows, ld, box_rows));
+        op.m1    = op.m0;
+        op.base0 = X;
+        op.base1 = nullptr;
+        op.bf16  = false;
+        op.K     = K;
+        op.ld    = ld;
+        op.rows  = rows;
+        return MGX_OK;
+    }
+    const size_t ldo   = ((K + 63) / 64) * 64;
+    const size_t plane = ldo * (size_t)rows * sizeof(__nv_bfloat16);
+    auto* hi           = (__nv_bfloat16*)ws;
+    auto* lo           = (__nv_bfloat16*)(ws + plane);
+    const int nb       = (int)std::min<size_t>((ldo / 2 * rows + 255) / 256, 1 << 20);
+    split_kernel<<<nb, 256, 0, s>>>((const float*)X, ld, rows, K, hi, lo, ldo);
+    MGX_LAUNCH_CHECK("split_kernel");
+    MGX_TRY(make_map(&op.m0, hi, true, K, rows, ldo, box_rows));
+    MGX_TRY(make_map(&op.m1, lo, true, K, rows, ldo, box_rows));
+    op.base0 = hi;
+    op.base1 = lo;
+    op.bf16  = true;
+    op.K     = K;
+    op.ld    = ldo;
+    op.rows  = rows;
+    *used    = 2 * plane;
+    return MGX_OK;
+}
+
+size_t operand_bytes(int mode, size_t K, int rows)
+{
+    if (mode == MGX_GEMM_TF32) return ((K + 31) / 32) * 32 * (size_t)rows * 4;
+    return 2 * ((K + 63) / 64) * 64 * (size_t)rows * sizeof(__nv_bfloat16);
+}
+
+/* C[0:nrows, 0:ncols] (leading dimension ldc) += A B^T over K.  Output
+ * tiles are 128 x 256 (128 x 128 when ncols <= 128); the B operand map must
+ * have been built with the matching box height. */
+int run(mgx_ctx* ctx, int mode, const Operand& a, const Operand& b, int nrows, int ncols,
+    int symmetric, double* C, int ldc, size_t K, int tile_slot, int BN, cudaStream_t s)
+{
+    using namespace tc;
+    const int nti = (nrows + BM - 1) / BM, ntj = (ncols + BN - 1) / BN;
     std::vector<int2> tiles;
     for (int j = 0; j < ntj; j++)
         for (int i = 0; i < nti; i++)
             if (!symmetric || (i * BM + BM - 1) >= j * BN) tiles.push_back(make_int2(i, j));
-    const int ntiles = (int)tiles.size();
-    const int bk     = split ? 64 : 32;
+    const int ntiles  = (int)tiles.size();
+    const int bk      = (mode == MGX_GEMM_BF16X3) ? 64 : 32;
     const int kblocks = (int)((K + bk - 1) / bk);
     int ksplit = std::max((4 * ctx->sm_count + ntiles - 1) / ntiles, (kblocks + 511) / 512);
     ksplit     = std::min(ksplit, kblocks);
     const int kb_per = (kblocks + ksplit - 1) / ksplit;
     ksplit           = (kblocks + kb_per - 1) / kb_per;
     if (ksplit > 65535) return fail(MGX_UNSUPPORTED, "K too large");
-
-    MGX_TRY(ctx->tc_tiles.ensure(tiles.size() * sizeof(int2)));
-    MGX_TRY(ctx->tc_err.ensure(16));
-    MGX_TRY(cuda_check(cudaMemcpyAsync(ctx->tc_tiles.ptr, tiles.data(),
-                           tiles.size() * sizeof(int2), cudaMemcpyHostToDevice, s),
+    const size_t slot_bytes = 64 * 1024 * sizeof(int2);
+    if (tiles.size() > 64 * 1024) return fail(MGX_UNSUPPORTED, "too many output tiles");
+    int2* dtiles = (int2*)((char*)ctx->tc_tiles.ptr + tile_slot * slot_bytes);
+    MGX_TRY(cuda_check(cudaMemcpyAsync(dtiles, tiles.data(), tiles.size() * sizeof(int2),
+                           cudaMemcpyHostToDevice, s),
         "tile list upload"));
-    MGX_TRY(cuda_check(cudaMemsetAsync(ctx->tc_err.ptr, 0, 16, s), "err reset"));
-    MGX_TRY(cuda_check(cudaMemsetAsync(C, 0, (size_t)n * n * sizeof(double), s), "C zero"));
-
     Params p;
-    p.tiles      = (const int2*)ctx->tc_tiles.ptr;
+    p.tiles      = dtiles;
     p.kblocks    = kblocks;
     p.kb_per_cta = kb_per;
-    p.n          = n;
+    p.n          = ldc;
+    p.ncols      = ncols;
     p.symmetric  = symmetric;
     p.C          = C;
     p.err        = (int*)ctx->tc_err.ptr;
+    (void)nrows;
+    if (BN == 256)
+    {
+        if (mode == MGX_GEMM_TF32)
+            return launch<0, 1, 256, 4>(a.m0, a.m0, b.m0, b.m0, p, ntiles, ksplit, s);
+        return launch<1, 3, 256, 2>(a.m0, a.m1, b.m0, b.m1, p, ntiles, ksplit, s);
+    }
+    if (mode == MGX_GEMM_TF32)
+        return launch<0, 1, 128, 6>(a.m0, a.m0, b.m0, b.m0, p, ntiles, ksplit, s);
+    return launch<1, 3, 128, 3>(a.m0, a.m1, b.m0, b.m1, p, ntiles, ksplit, s);
+}
 
-    CUtensorMap a0, a1, b0, b1;
-    if (!split)
-    {
-        MGX_TRY(make_map(&a0, A, false, K, n, ld, BM));
-        MGX_TRY(make_map(&b0, B, false, K, n, ld, BN));
-        MGX_TRY((launch<0, 1, 128, 6>(a0, a0, b0, b0, p, ntiles, ksplit, s)));
-    }
-    else
-    {
-        const size_t ldo  = ((K + 63) / 64) * 64;
-        const size_t plane = ldo * (size_t)n * sizeof(__nv_bfloat16);
-        MGX_TRY(ctx->tc_split.ensure((same ? 2 : 4) * plane));
-        char* base = (char*)ctx->tc_split.ptr;
-        auto* ahi  = (__nv_bfloat16*)base;
-        auto* alo  = (__nv_bfloat16*)(base + plane);
-        auto* bhi  = same ? ahi : (__nv_bfloat16*)(base + 2 * plane);
-        auto* blo  = same ? alo : (__nv_bfloat16*)(base + 3 * plane);
-        const int nb = (int)std::min<size_t>((ldo / 2 * n + 255) / 256, 1 << 20);
-        split_kernel<<<nb, 256, 0, s>>>((const float*)A, ld, n, K, ahi, alo, ldo);
-        MGX_LAUNCH_CHECK("split_kernel");
-        if (!same)
-        {
-            split_kernel<<<nb, 256, 0, s>>>((const float*)B, ld, n, K, bhi, blo, ldo);
-            MGX_LAUNCH_CHECK("split_kernel");
-        }
-        MGX_TRY(make_map(&a0, ahi, true, K, n, ldo, BM));
-        MGX_TRY(make_map(&a1, alo, true, K, n, ldo, BM));
-        MGX_TRY(make_map(&b0, bhi, true, K, n, ldo, BN));
-        MGX_TRY(make_map(&b1, blo, true, K, n, ldo, BN));
-        MGX_TRY((launch<1, 3, 128, 3>(a0, a1, b0, b1, p, ntiles, ksplit, s)));
-    }
-    const int nbf = (int)std::min<size_t>(((size_t)n * n + 255) / 256, 4096);
-    finish_kernel<<<nbf, 256, 0, s>>>(C, n, vel, symmetric);
-    MGX_LAUNCH_CHECK("finish_kernel");
+int tile_n(int ncols) { return ncols > 128 ? 256 : 128; }
+
+/* lower triangle of A A^T: the A maps (box 128 rows) are rebuilt with the
+ * 256-row box for the B side when the wide tile is used */
+int run_sym(mgx_ctx* ctx, int mode, const Operand& a, int n, double* C, size_t K,
+    int tile_slot, cudaStream_t s)
+{
+    const int BN = tile_n(n);
+    if (BN == 128) return run(ctx, mode, a, a, n, n, 1, C, n, K, tile_slot, 128, s);
+    Operand b = a;
+    MGX_TRY(rebox(b, BN));
+    return run(ctx, mode, a, b, n, n, 1, C, n, K, tile_slot, BN, s);
+}
+
+int begin(mgx_ctx* ctx, cudaStream_t s)
+{
+    MGX_TRY(ctx->tc_tiles.ensure(2 * 64 * 1024 * sizeof(int2)));
+    MGX_TRY(ctx->tc_err.ensure(16));
+    return cuda_check(cudaMemsetAsync(ctx->tc_err.ptr, 0, 16, s), "err reset");
+}
+
+int end(mgx_ctx* ctx, cudaStream_t s)
+{
     int herr = 0;
-    MGX_TRY(cuda_check(cudaMemcpyAsync(&herr, ctx->tc_err.ptr, sizeof(int), cudaMemcpyDeviceToHost, s),
+    MGX_TRY(cuda_check(cudaMemcpyAsync(&herr, ctx->tc_err.ptr, sizeof(int),
+                           cudaMemcpyDeviceToHost, s),
         "err download"));
     MGX_TRY(cuda_check(cudaStreamSynchronize(s), "tc gram sync"));
     if (herr) return fail(MGX_TIMEOUT, "tensor-core pipeline wait gave up");
     return MGX_OK;
+}
+
+int finish(double* C, int n, double vel, int symmetric, cudaStream_t s)
+{
+    const int nbf = (int)std::min<size_t>(((size_t)n * n + 255) / 256, 4096);
+    tc::finish_kernel<<<nbf, 256, 0, s>>>(C, n, vel, symmetric);
+    MGX_LAUNCH_CHECK("finish_kernel");
+    return MGX_OK;
+}
+
+// columns of the second operand converted per pass (bounds the workspace)
+constexpr int CHUNK = 512;
+
+/* C = A B^T over K with B processed CHUNK rows at a time; A prepared once */
+int product(mgx_ctx* ctx, int mode, const Operand& a, size_t a_used, const void* B,
+    size_t ld, size_t K, int n, double* C, int tile_slot, cudaStream_t s)
+{
+    for (int j0 = 0; j0 < n; j0 += CHUNK)
+    {
+        const int nc = std::min(CHUNK, n - j0);
+        Operand b;
+        size_t used = 0;
+        const void* Bj = (const char*)B + (size_t)j0 * ld * 4;
+        const int BN = tile_n(nc);
+        MGX_TRY(prepare(mode, Bj, ld, K, nc, BN, (char*)ctx->tc_split.ptr + a_used, &used, b, s));
+        MGX_TRY(run(ctx, mode, a, b, n, nc, 0, C + (size_t)j0 * n, n, K, tile_slot, BN, s));
+    }
+    return MGX_OK;
+}
+} // namespace
+
+int gram_tcgen05(mgx_ctx* ctx, int mode, const void* A, const void* B, size_t ld,
+    size_t K, int n, double vel, int symmetric, double* C, cudaStream_t s)
+{
+    const bool same = (A == B) && symmetric;
+    const size_t a_bytes = operand_bytes(mode, K, n);
+    const size_t b_bytes = same ? 0 : operand_bytes(mode, K, std::min(n, CHUNK));
+    MGX_TRY(ctx->tc_split.ensure(a_bytes + b_bytes + 256));
+    MGX_TRY(begin(ctx, s));
+    MGX_TRY(cuda_check(cudaMemsetAsync(C, 0, (size_t)n * n * sizeof(double), s), "C zero"));
+    Operand a;
+    size_t used = 0;
+    MGX_TRY(prepare(mode, A, ld, K, n, tc::BM, (char*)ctx->tc_split.ptr, &used, a, s));
+    if (same)
+        MGX_TRY(run_sym(ctx, mode, a, n, C, K, 0, s));
+    else
+        MGX_TRY(product(ctx, mode, a, ((used + 255) / 256) * 256, B, ld, K, n, C, 0, s));
+    MGX_TRY(finish(C, n, vel, same ? 1 : 0, s));
+    return end(ctx, s);
+}
+
+/* S = Psi^T Psi * vel and H = Psi^T (H Psi) * vel with one conversion of Psi */
+int gram_hmat_tcgen05(mgx_ctx* ctx, int mode, const void* psi, const void* hpsi,
+    size_t ld, size_t K, int n, double vel, double* S, double* H, cudaStream_t s)
+{
+    const size_t a_bytes = operand_bytes(mode, K, n);
+    const size_t b_bytes = operand_bytes(mode, K, std::min(n, CHUNK));
+    MGX_TRY(ctx->tc_split.ensure(a_bytes + b_bytes + 512));
+    MGX_TRY(begin(ctx, s));
+    MGX_TRY(cuda_check(cudaMemsetAsync(S, 0, (size_t)n * n * sizeof(double), s), "S zero"));
+    MGX_TRY(cuda_check(cudaMemsetAsync(H, 0, (size_t)n * n * sizeof(double), s), "H zero"));
+    Operand a;
+    size_t used = 0;
+    MGX_TRY(prepare(mode, psi, ld, K, n, tc::BM, (char*)ctx->tc_split.ptr, &used, a, s));
+    MGX_TRY(run_sym(ctx, mode, a, n, S, K, 0, s));
+    MGX_TRY(product(ctx, mode, a, ((used + 255) / 256) * 256, hpsi, ld, K, n, H, 1, s));
+    MGX_TRY(finish(S, n, vel, 1, s));
+    MGX_TRY(finish(H, n, vel, 0, s));
+    return end(ctx, s);
 }
 } // namespace mgx

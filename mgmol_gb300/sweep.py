@@ -60,8 +60,7 @@ class OrbitalSweep:
         ctx.hpsi(psi, self.V, self.lap_type, True, out=self.hpsi)
         if timed:
             self._ev("gram0")
-        ctx.gram(psi, self.gemm, out=self.S)
-        ctx.hmat(psi, self.hpsi, self.gemm, out=self.Hm)
+        ctx.gram_hmat(psi, self.hpsi, self.gemm, S=self.S, H=self.Hm)
         if timed:
             self._ev("dense0")
         L = ctx.cholesky(self.S)

@@ -63,3 +63,26 @@ def test_bf16x3_beats_tf32():
     e_tf = rel_err(ctx.gram(_dev(p32), mode=capi.GEMM_TF32).cpu().numpy(), ref)
     e_b3 = rel_err(ctx.gram(_dev(p32), mode=capi.GEMM_BF16X3).cpu().numpy(), ref)
     assert e_b3 < e_tf / 10
+
+
+@pytest.mark.parametrize("mode", [capi.GEMM_TF32, capi.GEMM_BF16X3, capi.GEMM_FP32, capi.GEMM_FP64])
+def test_fused_gram_hmat_equals_separate(mode):
+    """mgx_gram_hmat (one conversion of Psi, H in column chunks of 512)
+    agrees with the separate calls; n > 512 exercises the chunking."""
+    grid = (16, 16, 12)
+    ll = tuple(x * 0.35 for x in grid)
+    nf = 600
+    psi, _, _ = synth.gaussian_orbitals(grid, ll, nf, 41)
+    V = synth.gaussian_wells(grid, ll, 6, 41)
+    ctx = capi.Context(grid, ll)
+    dt = np.float64 if mode == capi.GEMM_FP64 else np.float32
+    p = psi.astype(dt)
+    hp = O.hpsi(grid, ll, 0, p, V)
+    S, H = ctx.gram_hmat(_dev(p, dt), _dev(hp, dt), mode=mode)
+    S2 = ctx.gram(_dev(p, dt), mode=mode)
+    H2 = ctx.hmat(_dev(p, dt), _dev(hp, dt), mode=mode)
+    tol = {capi.GEMM_TF32: 2e-3, capi.GEMM_BF16X3: 2e-5, capi.GEMM_FP32: 1e-5, capi.GEMM_FP64: 1e-12}[mode]
+    assert rel_err(S.cpu().numpy(), S2.cpu().numpy()) < tol
+    assert rel_err(H.cpu().numpy(), H2.cpu().numpy()) < tol
+    assert rel_err(H.cpu().numpy(), O.hmat(p, hp, ctx.vel)) < tol
+    assert rel_err(S.cpu().numpy(), O.gram(p, ctx.vel)) < tol
