@@ -33,6 +33,8 @@ CONFIGS = {
                workload="plain FP64 case: 64 orbitals, 64^3, h=0.35, Mehrstellen"),
     "c5_256": dict(n=(192, 192, 192), h=0.25, nfunc=256, wells=64, seed=1005,
                    workload="profiling slice: 256 orbitals on the 192^3 grid, h=0.25, Mehrstellen, FP32"),
+    "c5_32": dict(n=(192, 192, 192), h=0.25, nfunc=32, wells=64, seed=1005,
+                  workload="profiling slice: 32 orbitals on the 192^3 grid, h=0.25, Mehrstellen, FP32"),
     "small": dict(n=(64, 64, 64), h=0.25, nfunc=256, wells=16, seed=7,
                   workload="small sweep: 256 orbitals, 64^3, Mehrstellen, FP32"),
 }

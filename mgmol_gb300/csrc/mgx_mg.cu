@@ -658,9 +658,41 @@ struct VCycle
     std::vector<size_t> ld;
     int* err;
 
+    double gamma = 0.;
+    bool pending_scale = false; // level-0 iterate still to be set to gamma*f
+
     int jacobi(int l, int cur, bool write_w)
     {
         PlaneParams p;
+        if (l == 0 && pending_scale)
+        {
+            // first sweep straight from f with u = gamma f
+            p.gamma_in = gamma;
+            p.u        = f[0];
+            p.ldu      = ld[0];
+            p.f        = f[0];
+            p.ldf      = ld[0];
+            p.out      = cur ? v0[0] : v1[0];
+            p.ldo      = ld[0];
+            p.w        = write_w ? w[0] : nullptr;
+            p.ldw      = ld[0];
+            for (int i = 0; i < 3; i++)
+                p.n[i] = lev[0].n[i];
+            p.mask = mask_slice(masks, 0, f0);
+            p.err  = err;
+            int st = stencil_launch(OP_JACOBI, lap_type, dtype, dtype, p, lev[0], jf[0], nf, s);
+            if (st == MGX_UNSUPPORTED)
+            {
+                // v = gamma * res (src/OrbitalsPreconditioning.cc:102-107), then a plain sweep
+                st = scale_launch(dtype, f[0], ld[0], cur ? v1[0] : v0[0], ld[0],
+                    lev[0].npts(), nf, gamma, s);
+                if (st != MGX_OK) return st;
+                pending_scale = false;
+                return jacobi(l, cur, write_w);
+            }
+            pending_scale = false;
+            return st;
+        }
         p.u   = cur ? v1[l] : v0[l];
         p.ldu = ld[l];
         p.f   = f[l];
@@ -796,7 +828,8 @@ int precond_mg(mgx_ctx* ctx, const mgx_precond_params* P, int dtype,
             base += (size_t)nf * pl * es;
         }
         // v = gamma * res (src/OrbitalsPreconditioning.cc:102-107)
-        MGX_TRY(scale_launch(dtype, V.f[0], ld, V.v0[0], ld, p0, nf, P->gamma, s));
+        V.gamma         = P->gamma;
+        V.pending_scale = true;
         const int c = V.mg(0);
         if (c < 0) return -(c + 1);
         if (c != 0) return fail(MGX_UNSUPPORTED, "V-cycle ended in the work buffer");

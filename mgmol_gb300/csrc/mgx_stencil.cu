@@ -526,6 +526,312 @@ __global__ void __launch_bounds__(256) plane_kernel(PlaneParams p, DevCoef<T> c)
 }
 
 /* ------------------------------------------------------------------ */
+/* vectorised radius-1 plane kernel                                     */
+/* ------------------------------------------------------------------ */
+// The radius-1 operators (Mehrstellen -Lap_M with or without B(V psi), the
+// B operator, and the 2nd-order operator of the coarse levels) on groups of
+// VEC = 16 / sizeof(T) consecutive z points: every shared-memory row access
+// is one 16-byte vector plus the two z neighbours at the group ends, and the
+// outputs leave as 16-byte stores.  The plane recurrence is the one of
+// plane_kernel: out(x) = a(x) + b(x-1) + b(x+1).
+template <typename T>
+struct Vec16;
+template <>
+struct Vec16<float>
+{
+    using type = float4;
+    static constexpr int N = 4;
+    __device__ static float get(const float4& v, int i)
+    {
+        return i == 0 ? v.x : (i == 1 ? v.y : (i == 2 ? v.z : v.w));
+    }
+    __device__ static void set(float4& v, int i, float x)
+    {
+        if (i == 0) v.x = x;
+        else if (i == 1) v.y = x;
+        else if (i == 2) v.z = x;
+        else v.w = x;
+    }
+};
+template <>
+struct Vec16<double>
+{
+    using type = double2;
+    static constexpr int N = 2;
+    __device__ static double get(const double2& v, int i) { return i == 0 ? v.x : v.y; }
+    __device__ static void set(double2& v, int i, double x)
+    {
+        if (i == 0) v.x = x;
+        else v.y = x;
+    }
+};
+
+template <typename T, int LAP, int OP, int S, int NG>
+__global__ void __launch_bounds__(256) plane_vec_kernel(PlaneParams p, DevCoef<T> c)
+{
+    using V4          = typename Vec16<T>::type;
+    using VH          = Vec16<T>;
+    constexpr int VEC = VH::N;
+    constexpr bool EDGES   = (LAP == 0) && (OP != OP_RHS);
+    constexpr bool STAGE_V = (OP == OP_HPSI_B);
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+
+    const int nx = p.n[0], ny = p.n[1], nz = p.n[2];
+    const int TY      = p.ty;
+    const int rows    = TY + 2;
+    const int tile_y  = blockIdx.x % p.ntile_y;
+    const int tile_x  = blockIdx.x / p.ntile_y;
+    const int f       = blockIdx.y;
+    const int y0      = tile_y * TY;
+    const int x0      = tile_x * p.xc;
+    const int xcount  = min(p.xc, nx - x0);
+    const int nplanes = xcount + 2;
+    const bool scaled = (OP == OP_JACOBI) && (p.gamma_in != 0.);
+    const T gam       = (T)p.gamma_in;
+
+    const size_t stage_elems = (size_t)rows * nz;
+    T* stages                = reinterpret_cast<T*>(smem_raw);
+    T* vstages = reinterpret_cast<T*>(smem_raw + S * stage_elems * sizeof(T));
+    uint64_t* bars = reinterpret_cast<uint64_t*>(
+        smem_raw + S * stage_elems * sizeof(T) * (STAGE_V ? 2 : 1));
+
+    const T* ubase = reinterpret_cast<const T*>(scaled ? p.f : p.u)
+                     + (size_t)f * (scaled ? p.ldf : p.ldu);
+    const T* vbase = reinterpret_cast<const T*>(p.V);
+
+    int ya = y0 - 1, na, nb;
+    if (ya < 0)
+    {
+        na = 1;
+        ya += ny;
+        nb = rows - 1;
+    }
+    else if (ya + rows > ny)
+    {
+        na = ny - ya;
+        nb = rows - na;
+    }
+    else
+    {
+        na = rows;
+        nb = 0;
+    }
+    const uint32_t bytes = (uint32_t)(stage_elems * sizeof(T)) * (STAGE_V ? 2u : 1u);
+
+    auto issue = [&](int i) {
+        const int slot = i % S;
+        const int x    = wrap(x0 - 1 + i, nx);
+        uint64_t* bar  = bars + slot;
+        mbar_arrive_expect_tx(bar, bytes);
+        T* dst       = stages + slot * stage_elems;
+        const T* src = ubase + (size_t)x * ny * nz;
+        bulk_g2s(dst, src + (size_t)ya * nz, (uint32_t)(na * nz * sizeof(T)), bar);
+        if (nb > 0) bulk_g2s(dst + (size_t)na * nz, src, (uint32_t)(nb * nz * sizeof(T)), bar);
+        if (STAGE_V)
+        {
+            T* vdst       = vstages + slot * stage_elems;
+            const T* vsrc = vbase + (size_t)x * ny * nz;
+            bulk_g2s(vdst, vsrc + (size_t)ya * nz, (uint32_t)(na * nz * sizeof(T)), bar);
+            if (nb > 0)
+                bulk_g2s(vdst + (size_t)na * nz, vsrc, (uint32_t)(nb * nz * sizeof(T)), bar);
+        }
+    };
+
+    if (threadIdx.x == 0)
+    {
+        for (int s = 0; s < S; s++)
+            mbar_init(bars + s, 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    int issued = min(S, nplanes) - 1;
+    if (threadIdx.x == 0)
+        for (int i = 0; i <= issued; i++)
+            issue(i);
+
+    // group geometry
+    const int gpr  = nz / VEC; // groups per row
+    const int ngrp = TY * gpr;
+    int oc[NG], om[NG], op[NG], goff[NG], gy[NG], gz[NG];
+    bool val[NG];
+#pragma unroll
+    for (int k = 0; k < NG; k++)
+    {
+        const int g  = threadIdx.x + k * 256;
+        const int y  = g / gpr;
+        const int z0 = (g - y * gpr) * VEC;
+        val[k]       = (g < ngrp) && (y0 + y < ny);
+        gy[k]        = y;
+        gz[k]        = z0;
+        oc[k]        = (y + 1) * nz + z0;
+        om[k]        = (y + 1) * nz + (z0 > 0 ? z0 - 1 : nz - 1);
+        op[k]        = (y + 1) * nz + (z0 + VEC < nz ? z0 + VEC : 0);
+        goff[k]      = (y0 + y) * nz + z0; // point offset within an x-plane
+    }
+    T A1[NG][VEC], B1[NG][VEC], B2[NG][VEC], U1[NG][VEC];
+#pragma unroll
+    for (int k = 0; k < NG; k++)
+#pragma unroll
+        for (int v = 0; v < VEC; v++)
+            A1[k][v] = B1[k][v] = B2[k][v] = U1[k][v] = (T)0;
+
+    T* __restrict__ outp     = reinterpret_cast<T*>(p.out) + (size_t)f * p.ldo;
+    T* __restrict__ wp       = p.w ? reinterpret_cast<T*>(p.w) + (size_t)f * p.ldw : nullptr;
+    const T* __restrict__ fp = p.f ? reinterpret_cast<const T*>(p.f) + (size_t)f * p.ldf : nullptr;
+    constexpr bool POINTWISE = (OP == OP_JACOBI) || (OP == OP_HPSI_V);
+    const T c12 = (T)(1. / 12.), c05 = (T)0.5;
+
+    bool ok    = true;
+    int waited = -1;
+    for (int i = 0; i < nplanes; i++)
+    {
+        const int xe    = x0 + i - 2;
+        const bool emit = (i >= 2);
+        const size_t xoff = (size_t)(emit ? xe : 0) * ny * nz;
+        V4 pv[NG];
+        if (POINTWISE && emit && !scaled)
+        {
+#pragma unroll
+            for (int k = 0; k < NG; k++)
+                if (val[k])
+                    pv[k] = *reinterpret_cast<const V4*>(
+                        (OP == OP_JACOBI ? fp : vbase) + xoff + goff[k]);
+        }
+        ok = ok && mbar_wait(bars + (i % S), (uint32_t)((i / S) & 1));
+        if (ok) waited = i;
+        const T* st = stages + (i % S) * stage_elems;
+        const T* vs = vstages + (i % S) * stage_elems;
+#pragma unroll
+        for (int k = 0; k < NG; k++)
+        {
+            if (!val[k]) continue;
+            const V4 c0v = *reinterpret_cast<const V4*>(st + oc[k]);
+            const V4 cmv = *reinterpret_cast<const V4*>(st + oc[k] - nz);
+            const V4 cpv = *reinterpret_cast<const V4*>(st + oc[k] + nz);
+            const T zl = st[om[k]], zr = st[op[k]];
+            T ml = 0, mr = 0, pl = 0, pr = 0;
+            if (EDGES)
+            {
+                ml = st[om[k] - nz];
+                mr = st[op[k] - nz];
+                pl = st[om[k] + nz];
+                pr = st[op[k] + nz];
+            }
+            V4 vcv, vmv, vpv;
+            T vzl = 0, vzr = 0;
+            if (STAGE_V)
+            {
+                vcv = *reinterpret_cast<const V4*>(vs + oc[k]);
+                vmv = *reinterpret_cast<const V4*>(vs + oc[k] - nz);
+                vpv = *reinterpret_cast<const V4*>(vs + oc[k] + nz);
+                vzl = vs[om[k]];
+                vzr = vs[op[k]];
+            }
+            V4 res;
+            V4 wres;
+#pragma unroll
+            for (int v = 0; v < VEC; v++)
+            {
+                T u         = VH::get(c0v, v);
+                T uzm       = v == 0 ? zl : VH::get(c0v, v - 1);
+                T uzp       = v == VEC - 1 ? zr : VH::get(c0v, v + 1);
+                T uym       = VH::get(cmv, v);
+                T uyp       = VH::get(cpv, v);
+                T a, b;
+                if (OP == OP_RHS)
+                {
+                    a = c05 * u + c12 * (uym + uyp + uzm + uzp);
+                    b = c12 * u;
+                }
+                else
+                {
+                    const T sz = uzm + uzp, sy = uym + uyp;
+                    a          = c.c0 * u + c.cz[0] * sz + c.cy[0] * sy;
+                    b          = c.cx[0] * u;
+                    if (EDGES)
+                    {
+                        const T yml = v == 0 ? ml : VH::get(cmv, v - 1);
+                        const T ymr = v == VEC - 1 ? mr : VH::get(cmv, v + 1);
+                        const T ypl = v == 0 ? pl : VH::get(cpv, v - 1);
+                        const T ypr = v == VEC - 1 ? pr : VH::get(cpv, v + 1);
+                        a += c.cyz * (yml + ymr + ypl + ypr);
+                        b += c.cxz * sz + c.cxy * sy;
+                    }
+                    if (STAGE_V)
+                    {
+                        const T vc  = VH::get(vcv, v);
+                        const T vzm = v == 0 ? vzl : VH::get(vcv, v - 1);
+                        const T vzp = v == VEC - 1 ? vzr : VH::get(vcv, v + 1);
+                        const T wc  = u * vc;
+                        const T wf  = uzm * vzm + uzp * vzp + uym * VH::get(vmv, v)
+                                     + uyp * VH::get(vpv, v);
+                        a += c05 * wc + c12 * wf;
+                        b += c12 * wc;
+                    }
+                }
+                if (emit)
+                {
+                    T lap = A1[k][v] + B2[k][v] + b;
+                    T ucen = U1[k][v];
+                    T r    = lap;
+                    if (OP == OP_HPSI_V) r = lap + ucen * VH::get(pv[k], v);
+                    if (OP == OP_JACOBI)
+                    {
+                        T fv;
+                        if (scaled)
+                        {
+                            // staged f: u = gamma f, -Lap u = gamma (-Lap f)
+                            fv   = ucen;
+                            lap  = gam * lap;
+                            ucen = gam * ucen;
+                        }
+                        else
+                            fv = VH::get(pv[k], v);
+                        T w = lap - fv;
+                        r   = ucen - c.jf * w;
+                        if (p.mask.state != nullptr)
+                        {
+                            const int y = y0 + gy[k], z = gz[k] + v;
+                            r           = apply_mask<T>(p.mask, f, xe, y, z, r);
+                            w           = apply_mask<T>(p.mask, f, xe, y, z, w);
+                        }
+                        VH::set(wres, v, w);
+                    }
+                    VH::set(res, v, r);
+                }
+                B2[k][v] = B1[k][v];
+                B1[k][v] = b;
+                A1[k][v] = a;
+                U1[k][v] = u;
+            }
+            if (emit)
+            {
+                *reinterpret_cast<V4*>(outp + xoff + goff[k]) = res;
+                if (OP == OP_JACOBI && wp != nullptr)
+                    *reinterpret_cast<V4*>(wp + xoff + goff[k]) = wres;
+            }
+        }
+        __syncthreads();
+        const int nxt = i + S;
+        if (nxt < nplanes && nxt > issued)
+        {
+            if (threadIdx.x == 0)
+            {
+                fence_proxy_async_smem();
+                issue(nxt);
+            }
+            issued = nxt;
+        }
+    }
+    if (!ok && threadIdx.x == 0)
+    {
+        if (p.err != nullptr) atomicExch(p.err, MGX_TIMEOUT);
+        for (int i = waited + 1; i <= issued; i++)
+            mbar_wait(bars + (i % S), (uint32_t)((i / S) & 1));
+    }
+}
+
+/* ------------------------------------------------------------------ */
 /* direct kernel (global loads with wrap), for small / unaligned cases  */
 /* ------------------------------------------------------------------ */
 template <typename T, typename TV, int LAP, int OP, int R>
@@ -578,10 +884,70 @@ constexpr int stages_for()
     return ((LAP == 0) || (OP == OP_RHS)) ? 4 : R + 4;
 }
 
+/* Can the vectorised radius-1 kernel run this launch?  It needs the
+ * operator to be radius 1 with a uniform element type, and every block it
+ * touches 16-byte aligned with rows of whole vectors. */
+template <typename T, typename TV, int LAP, int OP, int R>
+static bool vec_ok(const PlaneParams& p, int force_direct)
+{
+    if (force_direct || R != 1) return false;
+    if (!(LAP == 0 || LAP == 1 || OP == OP_RHS)) return false;
+    if ((OP == OP_HPSI_B || OP == OP_HPSI_V) && sizeof(T) != sizeof(TV)) return false;
+    const int nx = p.n[0], ny = p.n[1], nz = p.n[2];
+    auto al = [](const void* q, size_t ld) {
+        return q == nullptr || (((uintptr_t)q % 16) == 0 && (ld * sizeof(T)) % 16 == 0);
+    };
+    if ((nz * sizeof(T)) % 16) return false;
+    if (!al(p.u, p.ldu) || !al(p.out, p.ldo) || !al(p.w, p.ldw) || !al(p.f, p.ldf)) return false;
+    if (p.V && ((uintptr_t)p.V % 16)) return false;
+    if (ny < 3 || nx < 1 || nz > 256 * 2 * (16 / (int)sizeof(T))) return false;
+    return true;
+}
+
+template <typename T, typename TV, int LAP, int OP, int R>
+static int launch_vec(const PlaneParams& p0, const DevCoef<T>& c, int nfunc,
+    cudaStream_t stream)
+{
+    constexpr int S   = 4;
+    constexpr int NG  = 2;
+    constexpr int VEC = 16 / sizeof(T);
+    constexpr bool STAGE_V = (OP == OP_HPSI_B);
+    PlaneParams p = p0;
+    const int nx = p.n[0], ny = p.n[1], nz = p.n[2];
+    const size_t esz = sizeof(T) * (STAGE_V ? 2 : 1);
+    const size_t smem_cap = 110 * 1024;
+    int ty = std::min(32, (256 * NG * VEC) / nz);
+    ty     = std::min(ty, ny - 2);
+    for (; ty >= 1; ty--)
+        if ((size_t)S * (ty + 2) * nz * esz + S * 8 <= smem_cap) break;
+    if (ty < 1) return fail(MGX_UNSUPPORTED, "plane too large for the vector kernel");
+    p.ty      = ty;
+    p.ntile_y = (ny + ty - 1) / ty;
+    int xc = 32;
+    while (xc > 4 && (size_t)p.ntile_y * ((nx + xc - 1) / xc) * nfunc < 4 * 152)
+        xc /= 2;
+    if (xc > nx) xc = nx;
+    p.xc       = xc;
+    p.ntile_x  = (nx + xc - 1) / xc;
+    const size_t smem = (size_t)S * (ty + 2) * nz * esz + S * 8;
+    auto kern         = plane_vec_kernel<T, LAP == 1 ? 1 : 0, OP, S, NG>;
+    cudaError_t e     = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        (int)smem);
+    if (e != cudaSuccess) return cuda_check(e, "plane_vec_kernel smem attribute");
+    dim3 grid(p.ntile_y * p.ntile_x, nfunc);
+    kern<<<grid, 256, smem, stream>>>(p, c);
+    MGX_LAUNCH_CHECK("plane_vec_kernel");
+    return MGX_OK;
+}
+
 template <typename T, typename TV, int LAP, int OP, int R>
 static int launch_t(const PlaneParams& p0, const DevCoef<T>& c, int nfunc,
     cudaStream_t stream, int force_direct)
 {
+    if (vec_ok<T, TV, LAP, OP, R>(p0, force_direct))
+        return launch_vec<T, TV, LAP, OP, R>(p0, c, nfunc, stream);
+    if (p0.gamma_in != 0.)
+        return fail(MGX_UNSUPPORTED, "scaled first sweep needs the vector kernel");
     PlaneParams p = p0;
     constexpr int S  = stages_for<LAP, OP, R>();
     constexpr int RR = ((LAP == 0) || (OP == OP_RHS)) ? 1 : R;

@@ -50,6 +50,10 @@ struct PlaneParams
     int ty = 0, xc = 0, ntile_y = 0, ntile_x = 0;
     MaskDev mask;
     int* err = nullptr;
+    // OP_JACOBI only: when nonzero the staged input is f itself and the
+    // iterate is u = gamma_in * f (the first sweep of the V-cycle started
+    // from gamma * res, src/OrbitalsPreconditioning.cc:102-107)
+    double gamma_in = 0.;
 };
 
 int stencil_launch(int op, int lap_type, int dtype, int v_dtype,
