@@ -104,25 +104,32 @@ __global__ void restrict_kernel(const T* __restrict__ fine, size_t ldf,
 }
 
 /* trilinear prolongation; MODE 0: out = P e; MODE 1: out -= mask(P e).
- * One block per fine (x, y) line, threads along fine z. */
+ * One block per fine x plane and band of PROLONG_ROWS y lines; threads run
+ * along z (coalesced), the rows of the band in turn. */
+constexpr int PROLONG_ROWS = 8;
+
 template <typename T, int MODE>
-__global__ void prolong_kernel(const T* __restrict__ coarse, size_t ldc,
-    T* __restrict__ out, size_t ldo, int fx, int fy, int fz, MaskDev mask)
+__global__ void __launch_bounds__(256) prolong_kernel(const T* __restrict__ coarse,
+    size_t ldc, T* __restrict__ out, size_t ldo, int fx, int fy, int fz, MaskDev mask)
 {
     const int cx = fx >> 1, cy = fy >> 1, cz = fz >> 1;
-    const int f  = blockIdx.y;
-    const int x  = blockIdx.x / fy, y = blockIdx.x - (blockIdx.x / fy) * fy;
-    const T* e   = coarse + (size_t)f * ldc;
-    const int i = x >> 1, j = y >> 1, a = x & 1, b = y & 1;
-    const int i1 = wrp(i + 1, cx), j1 = wrp(j + 1, cy);
-    const T* c00 = e + ((size_t)i * cy + j) * cz;
-    const T* c01 = e + ((size_t)i * cy + j1) * cz;
-    const T* c10 = e + ((size_t)i1 * cy + j) * cz;
-    const T* c11 = e + ((size_t)i1 * cy + j1) * cz;
-    T* o         = out + (size_t)f * ldo + ((size_t)x * fy + y) * fz;
-    for (int z = threadIdx.x; z < fz; z += blockDim.x)
+    const int f      = blockIdx.y;
+    const int bands  = (fy + PROLONG_ROWS - 1) / PROLONG_ROWS;
+    const int x      = blockIdx.x / bands;
+    const int yb     = (blockIdx.x - x * bands) * PROLONG_ROWS;
+    const T* e       = coarse + (size_t)f * ldc;
+    const int i = x >> 1, a = x & 1, i1 = wrp(i + 1, cx);
+    for (int t = threadIdx.x; t < PROLONG_ROWS * fz; t += blockDim.x)
     {
+        const int r = t / fz, z = t - (t / fz) * fz;
+        const int y = yb + r;
+        if (y >= fy) break;
+        const int j = y >> 1, b = y & 1, j1 = wrp(j + 1, cy);
         const int k = z >> 1, c = z & 1, k1 = wrp(k + 1, cz);
+        const T* c00 = e + ((size_t)i * cy + j) * cz;
+        const T* c01 = e + ((size_t)i * cy + j1) * cz;
+        const T* c10 = e + ((size_t)i1 * cy + j) * cz;
+        const T* c11 = e + ((size_t)i1 * cy + j1) * cz;
         T v;
         // operation order of src/pb/MGkernels.cc:84-197
         if (!a && !b && !c)
@@ -142,10 +149,11 @@ __global__ void prolong_kernel(const T* __restrict__ coarse, size_t ldc,
                 * (c11[k1] + c11[k] + c10[k1] + c10[k] + c01[k1] + c01[k] + c00[k1] + c00[k]);
         else
             v = (T)0.25 * (c11[k] + c10[k] + c01[k] + c00[k]);
+        T* o = out + (size_t)f * ldo + ((size_t)x * fy + y) * fz + z;
         if (MODE == 0)
-            o[z] = v;
+            *o = v;
         else
-            o[z] = o[z] - mask_point<T>(mask, f, x, y, z, v);
+            *o = *o - mask_point<T>(mask, f, x, y, z, v);
     }
 }
 
@@ -201,8 +209,9 @@ int prolong_launch(int dtype, int mode, const Level& fine, const void* c,
     size_t ldc, void* out, size_t ldo, int nfunc, const MaskDev& mask,
     cudaStream_t s)
 {
-    const dim3 g(fine.n[0] * fine.n[1], nfunc);
-    const int nt = std::min(256, std::max(32, ((fine.n[2] + 31) / 32) * 32));
+    const int bands = (fine.n[1] + PROLONG_ROWS - 1) / PROLONG_ROWS;
+    const dim3 g(fine.n[0] * bands, nfunc);
+    const int nt = 256;
     if (dtype == MGX_F64)
     {
         if (mode == 0)

@@ -23,6 +23,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdlib>
 #include <vector>
 
 #include "mgx_internal.cuh"
@@ -520,7 +521,19 @@ int run(mgx_ctx* ctx, int mode, const Operand& a, const Operand& b, int nrows, i
     return launch<1, 3, 128, 3>(a.m0, a.m1, b.m0, b.m1, p, ntiles, ksplit, s);
 }
 
-int tile_n(int ncols) { return ncols > 128 ? 256 : 128; }
+/* output tile width: 256 when the product is wide enough; MGX_TC_TILE_N
+ * (128 or 256) overrides the choice for tuning */
+int tile_n(int ncols)
+{
+    static int forced = -1;
+    if (forced < 0)
+    {
+        const char* e = getenv("MGX_TC_TILE_N");
+        forced        = (e && (atoi(e) == 128 || atoi(e) == 256)) ? atoi(e) : 0;
+    }
+    if (forced) return ncols > 128 ? forced : 128;
+    return ncols > 128 ? 256 : 128;
+}
 
 /* lower triangle of A A^T: the A maps (box 128 rows) are rebuilt with the
  * 256-row box for the B side when the wide tile is used */
