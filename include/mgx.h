@@ -130,6 +130,12 @@ int mgx_mgkernel_extend3d(const mgx_grid* grid, int ghosts, mgx_dtype dtype,
 int mgx_trade_boundaries(const mgx_grid* grid, int ghosts, mgx_dtype dtype,
     void* u, size_t nfunc, void* stream);
 
+/* GridFuncVector::axpy / operator-= (src/pb/GridFuncVector.cc:1643-1668,
+ * LinearAlgebraUtils::MPaxpy, src/linear_algebra/mputils.cc:222-244):
+ * y += alpha * x over n elements of dtype. */
+int mgx_axpy(size_t n, double alpha, mgx_dtype dtype, const void* x, void* y,
+    void* stream);
+
 /* ---------------------------------------------------------------- */
 /* Fused path on ghost-free blocks (periodic halo handled in the tile    */
 /* loaders).                                                            */

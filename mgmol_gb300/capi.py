@@ -69,6 +69,7 @@ _SIGS = {
     "mgx_mgkernel_restrict3d": [ctypes.POINTER(Grid), _i, _i, _vp, _vp, _sz, _vp],
     "mgx_mgkernel_extend3d": [ctypes.POINTER(Grid), _i, _i, _vp, _vp, _sz, _vp],
     "mgx_trade_boundaries": [ctypes.POINTER(Grid), _i, _i, _vp, _sz, _vp],
+    "mgx_axpy": [_sz, _d, _i, _vp, _vp, _vp],
     "mgx_fd_apply": [_vp, _i, _i, _vp, _sz, _vp, _i, _vp],
     "mgx_rhs_mehr": [_vp, _i, _vp, _sz, _vp, _i, _vp],
     "mgx_hpsi": [_vp, _i, _i, _vp, _sz, _vp, _i, _vp, _i, _i, _vp],

@@ -161,6 +161,13 @@ int strip(int dtype, const void* g, int gw, const int n[3], void* out,
     return MGX_OK;
 }
 
+template <typename T>
+__global__ void axpy_kernel(size_t n, T alpha, const T* __restrict__ x, T* __restrict__ y)
+{
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (size_t)gridDim.x * blockDim.x)
+        y[i] += alpha * x[i];
+}
 } // namespace mgx
 
 using namespace mgx;
@@ -219,6 +226,22 @@ int mgx_trade_boundaries(const mgx_grid* grid, int ghosts, mgx_dtype dtype,
     MGX_TRY(check_dtype(dtype));
     if (nfunc && !u) return fail(MGX_BAD_ARG, "NULL block");
     return ghosted_trade(*grid, ghosts, dtype, u, nfunc, (cudaStream_t)stream);
+}
+
+int mgx_axpy(size_t n, double alpha, mgx_dtype dtype, const void* x, void* y, void* stream)
+{
+    MGX_TRY(check_dtype(dtype));
+    if (n == 0) return MGX_OK;
+    if (!x || !y) return fail(MGX_BAD_ARG, "NULL vector");
+    const int nb = (int)std::min<size_t>((n + 255) / 256, 8192);
+    if (dtype == MGX_F64)
+        axpy_kernel<double><<<nb, 256, 0, (cudaStream_t)stream>>>(n, alpha, (const double*)x,
+            (double*)y);
+    else
+        axpy_kernel<float><<<nb, 256, 0, (cudaStream_t)stream>>>(n, (float)alpha,
+            (const float*)x, (float*)y);
+    MGX_LAUNCH_CHECK("axpy_kernel");
+    return MGX_OK;
 }
 
 int mgx_mgkernel_restrict3d(const mgx_grid* grid, int ghosts, mgx_dtype dtype,

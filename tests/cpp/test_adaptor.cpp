@@ -1,0 +1,237 @@
+// The reference's unit tests of the orbital hot path, written against the
+// MGmol-shaped C++ surface of mgmol_adaptor.h and run on the GPU:
+//   testLaph4 / testBatchLaph4 (tests/testLaph4.cc:7-86, testBatchLaph4.cc:7-110)
+//   testMGkernels (tests/testMGkernels.cc:8-85)
+//   testGramMatrix, single task (tests/testGramMatrix.cc:21-120)
+// plus checks of Hamiltonian::applyLocal and OrbitalsPreconditioning.
+// Prints one line per check and exits non-zero on the first failure.
+#include "mgmol_adaptor.h"
+
+#include <cmath>
+#include <cstdio>
+#include <random>
+#include <vector>
+
+static int failures = 0;
+#define CHECK(cond, ...)                                                       \
+    do                                                                         \
+    {                                                                          \
+        if (!(cond))                                                           \
+        {                                                                      \
+            std::printf("FAIL %s:%d ", __FILE__, __LINE__);                    \
+            std::printf(__VA_ARGS__);                                          \
+            std::printf("\n");                                                 \
+            failures++;                                                        \
+        }                                                                      \
+    } while (0)
+
+using namespace mgx;
+
+static void sine_field(const pb::Grid& g, std::vector<double>& u, std::vector<double>& lap)
+{
+    const double k[3] = { 2 * M_PI / g.ll(0), 2 * M_PI / g.ll(1), 2 * M_PI / g.ll(2) };
+    u.assign(g.size(), 0.);
+    lap.assign(g.size(), 0.);
+    for (unsigned x = 0; x < g.dim(0); x++)
+        for (unsigned y = 0; y < g.dim(1); y++)
+            for (unsigned z = 0; z < g.dim(2); z++)
+            {
+                const size_t i = ((size_t)x * g.dim(1) + y) * g.dim(2) + z;
+                const double X = x * g.hgrid(0), Y = y * g.hgrid(1), Z = z * g.hgrid(2);
+                u[i] = std::sin(k[0] * X) + std::sin(k[1] * Y) + std::sin(k[2] * Z);
+                lap[i] = k[0] * k[0] * std::sin(k[0] * X) + k[1] * k[1] * std::sin(k[1] * Y)
+                         + k[2] * k[2] * std::sin(k[2] * Z);
+            }
+}
+
+static void test_laph4(int nfunc)
+{
+    const double origin[3] = { 0., 0., 0. }, ll[3] = { 2., 2., 2. };
+    const unsigned n[3] = { 32, 24, 20 };
+    pb::Grid grid(origin, ll, n, 2);
+    pb::Laph4<double> lap(grid);
+    pb::GridFuncVector<double> gu(grid, nfunc), gv(grid, nfunc);
+    std::vector<double> u, ex, out(grid.size());
+    sine_field(grid, u, ex);
+    for (int f = 0; f < nfunc; f++)
+    {
+        std::vector<double> uf(u);
+        for (auto& x : uf) x *= (f + 1);
+        gu.assign(f, uf.data());
+    }
+    lap.apply(gu, gv);
+    for (int f = 0; f < nfunc; f++)
+    {
+        gv.getValues(f, out.data());
+        double err = 0., mx = 0.;
+        for (size_t i = 0; i < out.size(); i++)
+        {
+            err = std::max(err, std::fabs(out[i] - (f + 1) * ex[i]));
+            mx  = std::max(mx, std::fabs((f + 1) * ex[i]));
+        }
+        CHECK(err < 2e-3 * mx, "Laph4 function %d: err %g", f, err / mx);
+    }
+    std::printf("ok   testLaph4 (nfunc = %d)\n", nfunc);
+}
+
+static void test_mgkernels()
+{
+    const double origin[3] = { 0., 0., 0. }, ll[3] = { 3.2, 2.4, 2.0 };
+    const unsigned n[3] = { 32, 24, 20 };
+    pb::Grid fine(origin, ll, n, 1);
+    pb::Grid coarse = fine.coarse_grid();
+    pb::GridFuncVector<double> gf(fine, 5), gc(coarse, 5);
+    for (int f = 0; f < 5; f++)
+    {
+        std::vector<double> c(fine.size(), f * 1.11);
+        gf.assign(f, c.data());
+    }
+    gf.trade_boundaries();
+    gf.restrict3D(gc);
+    std::vector<double> vc(coarse.size()), vf(fine.size());
+    for (int f = 0; f < 5; f++)
+    {
+        gc.getValues(f, vc.data());
+        for (double v : vc) CHECK(std::fabs(v - f * 1.11) < 1e-8, "restrict %d: %g", f, v);
+    }
+    gc.set_updated_boundaries(false);
+    gf.extend3D(gc);
+    for (int f = 0; f < 5; f++)
+    {
+        gf.getValues(f, vf.data());
+        for (double v : vf) CHECK(std::fabs(v - f * 1.11) < 1e-8, "extend %d: %g", f, v);
+    }
+    std::printf("ok   testMGkernels\n");
+}
+
+static void test_gram_matrix()
+{
+    const int n = 213;
+    std::mt19937 gen(213);
+    std::normal_distribution<double> N01;
+    std::vector<double> A((size_t)n * n), S((size_t)n * n, 0.);
+    for (auto& a : A) a = N01(gen);
+    for (int i = 0; i < n; i++)
+        for (int j = 0; j < n; j++)
+        {
+            double s = 0.;
+            for (int k = 0; k < n; k++) s += A[(size_t)i * n + k] * A[(size_t)j * n + k];
+            S[(size_t)j * n + i] = s / n + (i == j ? 1. : 0.);
+        }
+    const double origin[3] = { 0, 0, 0 }, ll[3] = { 1, 1, 1 };
+    const unsigned g8[3] = { 8, 8, 8 };
+    pb::Grid grid(origin, ll, g8, 1);
+    OrbitalBlock<double> dummy(grid, 1);
+    GramMatrix gm(dummy.ctx(), n);
+    DeviceArray<double> dS((size_t)n * n);
+    dS.upload(S.data(), S.size());
+    gm.setMatrix(dS);
+    std::vector<double> L((size_t)n * n), Si((size_t)n * n);
+    gm.getCholeskyL().download(L.data(), L.size());
+    gm.getInverse().download(Si.data(), Si.size());
+    double e1 = 0., e2 = 0., mx = 0.;
+    for (int i = 0; i < n; i++)
+        for (int j = 0; j < n; j++)
+        {
+            double llt = 0., sis = 0.;
+            for (int k = 0; k < n; k++)
+            {
+                llt += L[(size_t)k * n + i] * L[(size_t)k * n + j];
+                sis += Si[(size_t)k * n + i] * S[(size_t)j * n + k];
+            }
+            e1 = std::max(e1, std::fabs(llt - S[(size_t)j * n + i]));
+            e2 = std::max(e2, std::fabs(sis - (i == j ? 1. : 0.)));
+            mx = std::max(mx, std::fabs(S[(size_t)j * n + i]));
+        }
+    CHECK(e1 <= 1e-14 * mx * n, "L L^T - S = %g", e1);
+    CHECK(e2 < 1e-12, "S^-1 S - I = %g", e2);
+    // a non-SPD matrix throws the status instead of aborting
+    S[5 * n + 5] = -1.;
+    dS.upload(S.data(), S.size());
+    bool threw = false;
+    try
+    {
+        gm.setMatrix(dS);
+    }
+    catch (const Error& e)
+    {
+        threw = (e.status == MGX_NOT_SPD);
+    }
+    CHECK(threw, "non-SPD matrix not reported");
+    std::printf("ok   testGramMatrix (one task)\n");
+}
+
+static void test_hamiltonian_and_precond()
+{
+    const double origin[3] = { 0., 0., 0. }, ll[3] = { 6.4, 6.4, 6.4 };
+    const unsigned n[3] = { 32, 32, 32 };
+    pb::Grid grid(origin, ll, n, 1);
+    const int nf = 3;
+    OrbitalBlock<double> phi(grid, nf), hphi(grid, nf);
+    std::vector<double> u, ex, all;
+    sine_field(grid, u, ex);
+    for (int f = 0; f < nf; f++) all.insert(all.end(), u.begin(), u.end());
+    phi.set(all.data());
+    DeviceArray<double> V(grid.size()); // zero potential: H phi = -Lap_M phi
+    Hamiltonian<double> H(0);
+    H.applyLocal(phi, V, hphi);
+    std::vector<double> out(all.size());
+    hphi.get(out.data());
+    double err = 0., mx = 0.;
+    for (size_t i = 0; i < u.size(); i++)
+    {
+        err = std::max(err, std::fabs(out[i] - ex[i]));
+        mx  = std::max(mx, std::fabs(ex[i]));
+    }
+    // -Lap_M u approximates B(-Lap u); B differs from 1 by O(h^2 k^2)
+    CHECK(err < 5e-2 * mx, "Mehrstellen H phi vs -Lap phi: %g", err / mx);
+    // the preconditioner is linear: P(2 r) = 2 P(r)
+    OrbitalsPreconditioning<double> P;
+    P.setup(2, 0);
+    P.setGamma(grid, 0.0, -1.0);
+    OrbitalBlock<double> r1(grid, nf), r2(grid, nf);
+    std::vector<double> two(all);
+    for (auto& x : two) x *= 2.;
+    r1.set(all.data());
+    r2.set(two.data());
+    P.precond_mg(r1);
+    P.precond_mg(r2);
+    std::vector<double> a(all.size()), b(all.size());
+    r1.get(a.data());
+    r2.get(b.data());
+    double lin = 0., am = 0.;
+    for (size_t i = 0; i < a.size(); i++)
+    {
+        lin = std::max(lin, std::fabs(b[i] - 2. * a[i]));
+        am  = std::max(am, std::fabs(a[i]));
+    }
+    CHECK(am > 0. && lin < 1e-12 * am, "precond linearity %g", lin / am);
+    // S of identical orbitals: every entry equals the squared norm
+    DeviceArray<double> S((size_t)nf * nf);
+    phi.computeGram(S);
+    std::vector<double> hs((size_t)nf * nf);
+    S.download(hs.data(), hs.size());
+    double nrm = 0.;
+    for (double x : u) nrm += x * x;
+    nrm *= grid.vel();
+    for (double s : hs) CHECK(std::fabs(s - nrm) < 1e-12 * nrm, "Gram entry %g vs %g", s, nrm);
+    std::printf("ok   Hamiltonian::applyLocal, OrbitalsPreconditioning, computeGram\n");
+}
+
+int main()
+{
+    try
+    {
+        test_laph4(1);
+        test_laph4(10);
+        test_mgkernels();
+        test_gram_matrix();
+        test_hamiltonian_and_precond();
+    }
+    catch (const std::exception& e)
+    {
+        std::printf("FAIL exception: %s\n", e.what());
+        return 2;
+    }
+    return failures ? 1 : 0;
+}
