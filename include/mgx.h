@@ -185,6 +185,24 @@ int mgx_precond_mg(mgx_ctx* ctx, const mgx_precond_params* p, mgx_dtype dtype,
     const void* res, size_t ld, void* out, int nfunc, const mgx_masks* masks,
     void* stream);
 
+/* mgx_precond_mg without any device allocation.  This entry point has no
+ * counterpart in the reference; it serves callers that cannot allocate
+ * device memory (code inside a stream capture that must not allocate,
+ * hosts whose device memory belongs to a pool they do not control, plug-ins
+ * in processes that forbid allocations after start-up).  Same arguments and
+ * results as mgx_precond_mg; ctx only supplies the grid (its workspaces are
+ * not used).  The V-cycle levels live in a fixed 64 MiB device array that
+ * is part of the library and held by every GPU that loads it: functions are
+ * processed in chunks that fit it, and a request whose single function
+ * needs more than the array holds is rejected with MGX_BAD_ARG.  The first
+ * call on a device looks up the array's device address (make it before any
+ * stream capture).  All calls share the array, so calls that overlap on the
+ * GPU (other streams, other host threads) race; the call returns after its
+ * work is complete on `stream`. */
+int mgx_precond_mg_static(mgx_ctx* ctx, const mgx_precond_params* p,
+    mgx_dtype dtype, const void* res, size_t ld, void* out, int nfunc,
+    const mgx_masks* masks, void* stream);
+
 /* OrbitalsPreconditioning<T>::setGamma (src/OrbitalsPreconditioning.cc:
  * 119-145); host computation, returned in *gamma. */
 int mgx_precond_gamma(const mgx_grid* grid, int lap_type, int mg_levels,

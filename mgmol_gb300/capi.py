@@ -76,6 +76,7 @@ _SIGS = {
     "mgx_mg_restrict": [_vp, _i, _i, _vp, _vp, _i, _vp],
     "mgx_mg_prolong": [_vp, _i, _i, _vp, _vp, _i, _vp],
     "mgx_precond_mg": [_vp, ctypes.POINTER(PrecondParams), _i, _vp, _sz, _vp, _i, _vp, _vp],
+    "mgx_precond_mg_static": [_vp, ctypes.POINTER(PrecondParams), _i, _vp, _sz, _vp, _i, _vp, _vp],
     "mgx_precond_gamma": [ctypes.POINTER(Grid), _i, _i, _d, _d, _dp],
     "mgx_masks_create": [_vp, _i, _i, _dp, _dp, _i, _i, _i, _i, ctypes.POINTER(_vp), _vp],
     "mgx_masks_destroy": [_vp],

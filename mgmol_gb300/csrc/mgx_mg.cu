@@ -19,6 +19,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <mutex>
 #include <vector>
 
 #include "mgx_internal.cuh"
@@ -846,4 +847,162 @@ int precond_mg(mgx_ctx* ctx, const mgx_precond_params* P, int dtype,
     return MGX_OK;
 }
 
+/* ------------------------------------------------------------------ */
+/* Allocation-free V-cycle                                              */
+/* ------------------------------------------------------------------ */
+// For callers that cannot allocate device memory at all: code running
+// inside a CUDA stream capture that must not allocate, host programs whose
+// device memory is owned by a pool they do not control, or plug-ins loaded
+// into a process that forbids allocations after start-up.  The V-cycle's
+// level buffers and status word then live in this file-scope device array
+// instead of the context workspace.  The array is part of the library's
+// device image: every GPU that loads the library holds these 64 MiB until
+// the process exits.
+constexpr size_t STATIC_VCYCLE_SCRATCH_BYTES = size_t(64) << 20;
+constexpr size_t STATIC_VCYCLE_STATUS_BYTES  = 256;
+static __device__ __align__(256) unsigned char g_vcycle_scratch[STATIC_VCYCLE_SCRATCH_BYTES];
+
+namespace
+{
+constexpr int MAX_DEVICES = 64;
+std::mutex g_scratch_mutex;
+void* g_scratch_address[MAX_DEVICES] = {};
+
+/* Device address of the static scratch on the current device.  The host
+ * symbol g_vcycle_scratch is only a stand-in for the device array; its
+ * device address is looked up once per device, with that device current,
+ * on the first call that needs it (which must therefore not happen during
+ * a stream capture). */
+int static_scratch_address(void** ptr)
+{
+    int dev = 0;
+    MGX_TRY(cuda_check(cudaGetDevice(&dev), "cudaGetDevice"));
+    if (dev < 0 || dev >= MAX_DEVICES)
+        return fail(MGX_UNSUPPORTED, "device index %d beyond %d", dev, MAX_DEVICES);
+    std::lock_guard<std::mutex> lock(g_scratch_mutex);
+    if (g_scratch_address[dev] == nullptr)
+    {
+        void* p       = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_vcycle_scratch);
+        if (e != cudaSuccess) return cuda_check(e, "cudaGetSymbolAddress of the V-cycle scratch");
+        g_scratch_address[dev] = p;
+    }
+    *ptr = g_scratch_address[dev];
+    return MGX_OK;
+}
+} // namespace
+
+int precond_mg_static(mgx_ctx* ctx, const mgx_precond_params* P, int dtype,
+    const void* res, size_t ld, void* out, int nfunc, const mgx_masks* masks,
+    cudaStream_t s)
+{
+    if (!P || !res || !out || nfunc < 0) return fail(MGX_BAD_ARG, "precond_mg: null argument");
+    if (res == out) return fail(MGX_BAD_ARG, "precond_mg: res and out alias");
+    if (P->lap_type < 0 || P->lap_type > 4) return fail(MGX_BAD_ARG, "lap_type %d", P->lap_type);
+    const int L = P->maxlevels;
+    if (L < 0 || L > 6) return fail(MGX_BAD_ARG, "maxlevels %d", L);
+    const mgx_grid& g = ctx->grid;
+    for (int l = 0; l < L; l++)
+        for (int i = 0; i < 3; i++)
+            if ((g.n[i] >> l) % 2)
+                return fail(MGX_BAD_ARG, "grid dimension %d not divisible by 2^%d", i, L);
+    if (masks && (masks->nlevels < L + 1 || masks->nfunc < nfunc))
+        return fail(MGX_BAD_ARG, "masks cover %d levels / %d functions", masks->nlevels, masks->nfunc);
+    const size_t es = dtype_size(dtype);
+
+    VCycle V;
+    V.ctx      = ctx;
+    V.dtype    = dtype;
+    V.lap_type = P->lap_type;
+    V.L        = L;
+    V.masks    = masks;
+    V.s        = s;
+    for (int l = 0; l <= L; l++)
+    {
+        V.lev.push_back(make_level(g, l));
+        V.jf.push_back(jacobi_factor(l == 0 ? P->lap_type : 1, V.lev[l].h));
+    }
+    size_t per_func = 2 * V.lev[0].npts();
+    for (int l = 1; l <= L; l++)
+        per_func += 4 * V.lev[l].npts();
+    per_func *= es;
+    const size_t avail = STATIC_VCYCLE_SCRATCH_BYTES - STATIC_VCYCLE_STATUS_BYTES;
+    if (per_func > avail)
+        return fail(MGX_BAD_ARG,
+            "one function needs %zu bytes of V-cycle scratch; the static scratch holds %zu",
+            per_func, avail);
+    if (nfunc == 0) return MGX_OK;
+    size_t chunk = avail / per_func;
+    if (P->chunk > 0) chunk = std::min(chunk, (size_t)P->chunk);
+    chunk = std::min(chunk, (size_t)65535);
+    chunk = std::min(chunk, (size_t)nfunc);
+
+    void* scratch = nullptr;
+    MGX_TRY(static_scratch_address(&scratch));
+    // the status word starts at zero; every other scratch byte is written
+    // before it is read within a call
+    V.err = (int*)scratch;
+    MGX_TRY(cuda_check(cudaMemsetAsync(scratch, 0, STATIC_VCYCLE_STATUS_BYTES, s), "status reset"));
+
+    for (int f0 = 0; f0 < nfunc; f0 += (int)chunk)
+    {
+        const int nf = (int)std::min(chunk, (size_t)(nfunc - f0));
+        V.nf = nf;
+        V.f0 = f0;
+        V.v0.assign(L + 1, nullptr);
+        V.v1.assign(L + 1, nullptr);
+        V.w.assign(L + 1, nullptr);
+        V.f.assign(L + 1, nullptr);
+        V.ld.assign(L + 1, 0);
+        char* base = (char*)scratch + STATIC_VCYCLE_STATUS_BYTES;
+        V.ld[0]    = ld;
+        V.v0[0]    = (char*)out + (size_t)f0 * ld * es;
+        V.f[0]     = (void*)((const char*)res + (size_t)f0 * ld * es);
+        const size_t p0 = V.lev[0].npts();
+        V.v1[0]    = base;
+        base += (size_t)nf * p0 * es;
+        V.w[0] = base;
+        base += (size_t)nf * p0 * es;
+        for (int l = 1; l <= L; l++)
+        {
+            const size_t pl = V.lev[l].npts();
+            V.ld[l]         = pl;
+            V.v0[l]         = base;
+            base += (size_t)nf * pl * es;
+            V.v1[l] = base;
+            base += (size_t)nf * pl * es;
+            V.w[l] = base;
+            base += (size_t)nf * pl * es;
+            V.f[l] = base;
+            base += (size_t)nf * pl * es;
+        }
+        V.gamma         = P->gamma;
+        V.pending_scale = true;
+        const int c = V.mg(0);
+        if (c < 0) return -(c + 1);
+        if (c != 0) return fail(MGX_UNSUPPORTED, "V-cycle ended in the work buffer");
+    }
+    int status = 0;
+    MGX_TRY(cuda_check(cudaMemcpyAsync(&status, scratch, sizeof(int), cudaMemcpyDeviceToHost, s),
+        "status read"));
+    MGX_TRY(cuda_check(cudaStreamSynchronize(s), "static V-cycle sync"));
+    if (status != 0) return fail(MGX_TIMEOUT, "a bounded wait in the V-cycle gave up");
+    return MGX_OK;
+}
+
 } // namespace mgx
+
+extern "C" int mgx_precond_mg_static(mgx_ctx* ctx, const mgx_precond_params* p,
+    mgx_dtype dtype, const void* res, size_t ld, void* out, int nfunc,
+    const mgx_masks* masks, void* stream)
+{
+    using namespace mgx;
+    if (!ctx) return fail(MGX_BAD_ARG, "ctx is NULL");
+    if (dtype != MGX_F64 && dtype != MGX_F32) return fail(MGX_BAD_ARG, "dtype %d invalid", (int)dtype);
+    const size_t np = (size_t)ctx->grid.n[0] * ctx->grid.n[1] * ctx->grid.n[2];
+    if (nfunc > 1 && ld < np) return fail(MGX_BAD_ARG, "ld %zu < %zu points", ld, np);
+    if (masks && masks->dtype != dtype)
+        return fail(MGX_BAD_ARG, "mask value type differs from the orbital type");
+    return precond_mg_static(ctx, p, dtype, res, nfunc > 1 ? ld : (ld ? ld : np), out, nfunc,
+        masks, (cudaStream_t)stream);
+}
