@@ -38,7 +38,7 @@ CONFIGS = {
     "small": dict(n=(64, 64, 64), h=0.25, nfunc=256, wells=16, seed=7,
                   workload="small sweep: 256 orbitals, 64^3, Mehrstellen, FP32"),
 }
-METRIC = "orbital sweeps/s (Hpsi+precond+Gram)"
+METRIC = "orbital sweeps/s (ABPG step: Hpsi, Gram/H, residual, precond, update)"
 
 
 def _env_int(k, d):
@@ -133,7 +133,12 @@ def cpu_sweep_estimate(cfg, sample_funcs=4):
     t1 = time.perf_counter()
     O.precond(n, ll, 0, 2, 0.2, hp)
     t2 = time.perf_counter()
-    # S and H on a 64-orbital x 2^17-point slab: time per (pair, point)
+    # the linear part of the residual (B applied to the product) and the update
+    th = np.eye(sample_funcs)
+    O.residual(n, ll, psi, hp.astype(np.float32), th, 1)
+    t2b = time.perf_counter()
+    # S, H and Psi Theta on a 64-orbital x 2^17-point slab: time per
+    # (pair, point) of each product
     ns, ks = 64, min(1 << 17, n[0] * n[1] * n[2])
     rng = np.random.default_rng(0)
     slab = rng.standard_normal((ns, ks)).astype(np.float32)
@@ -141,19 +146,24 @@ def cpu_sweep_estimate(cfg, sample_funcs=4):
     O.gram(slab, vel)
     O.hmat(slab, slab, vel)
     t4 = time.perf_counter()
+    O.mult_matrix(slab, np.eye(ns))
+    t5 = time.perf_counter()
     P = n[0] * n[1] * n[2]
     pairs_s = ns * (ns + 1) / 2 + ns * ns
     per_pair_point = (t4 - t3) / (pairs_s * ks)
-    lin = (t2 - t0) * (N / sample_funcs)
-    quad = per_pair_point * (N * (N + 1) / 2 + N * N) * P
+    per_mm = (t5 - t4) / (ns * ns * ks)
+    lin = (t2b - t0) * (N / sample_funcs)
+    quad = per_pair_point * (N * (N + 1) / 2 + N * N) * P + per_mm * N * N * P
     per_sweep = lin + quad
+    t4 = t5
     cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
     return {
         "value": 1.0 / per_sweep, "unit": "sweeps/s", "cores": cores, "kind": "port",
         "sample": (f"oracle port of the reference loops (FP32 data, FP64 accumulation as the "
-                   f"USE_MP build), {cores} threads: H psi + V-cycle on {sample_funcs} of {N} "
-                   f"orbitals ({n[0]}^3), scaled by N; S and H timed on a 64-orbital x {ks}-point "
-                   f"slab, scaled by pairs x points; sample took {t4 - t0:.1f} s"),
+                   f"USE_MP build), {cores} threads: H psi, V-cycle and the residual stencil on "
+                   f"{sample_funcs} of {N} orbitals ({n[0]}^3), scaled by N; S, H and Psi Theta "
+                   f"timed on a 64-orbital x {ks}-point slab, scaled by pairs x points; sample "
+                   f"took {t4 - t0:.1f} s"),
         "seconds_per_sweep": per_sweep,
     }
 
@@ -298,6 +308,12 @@ def run_gpu(args, cfg):
         roof = {"kernel": "gram+hmat", "bound": "tensor", "achieved": achieved, "peak": bf16,
                 "unit": "TFLOP/s", "frac": achieved / bf16, "traffic": None,
                 "algorithmic": f"{gram_flops:.3e} flop per sweep (S lower incl. diagonal + H)"}
+    elif dominant == "residual":
+        rflops = 2.0 * N * N * npts
+        achieved = rflops / (phases["residual"] * 1e-3) / 1e12
+        roof = {"kernel": "residual (psi theta + B)", "bound": "tensor", "achieved": achieved,
+                "peak": bf16, "unit": "TFLOP/s", "frac": achieved / bf16, "traffic": None,
+                "algorithmic": f"{rflops:.3e} flop per sweep (psi theta)"}
     elif dominant == "hpsi":
         achieved = hpsi_bytes / (phases["hpsi"] * 1e-3) / 1e9
         roof = {"kernel": "hpsi", "bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",

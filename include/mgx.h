@@ -264,6 +264,78 @@ int mgx_inverse_from_cholesky(mgx_ctx* ctx, int n, const double* L,
 int mgx_trace_prod(mgx_ctx* ctx, int n, const double* H, const double* Sinv,
     double* trace, void* stream);
 
+/* ---------------------------------------------------------------- */
+/* Residual and orbital update (rows of the ABPG step).              */
+/* ---------------------------------------------------------------- */
+
+/* ProjectedMatrices::updateTheta (src/ProjectedMatrices.h:218-225):
+ * theta = Sinv H (n x n, FP64, column-major), Sinv read as symmetric from
+ * its lower triangle as BLAS symm('l', 'l') does. */
+int mgx_theta(mgx_ctx* ctx, int n, const double* Sinv, const double* H,
+    double* theta, void* stream);
+
+/* LocGridOrbitals::multiplyByMatrix (src/LocGridOrbitals.cc:793-830, the
+ * MPgemmNN of src/linear_algebra/mputils.cc:719-760):
+ * out_j = sum_i psi_i theta(i, j), theta FP64 column-major nfunc x nfunc.
+ * mode MGX_GEMM_FP64: FP64 accumulation (either dtype, as the reference);
+ * MGX_GEMM_FP32: FP32 orbitals, FP32 FMA; MGX_GEMM_TF32 / MGX_GEMM_BF16X3:
+ * FP32 orbitals on the tensor cores.  out may not alias psi. */
+int mgx_mult_matrix(mgx_ctx* ctx, int mode, mgx_dtype dtype, const void* psi,
+    size_t ld, int nfunc, const double* theta, void* out, void* stream);
+
+/* MGmol::computeResidualUsingHPhi (src/MGmol.cc:1227-1290):
+ * apply_B 1 (Mehrstellen): res = B(psi) theta - hpsi, computed as
+ * B(psi theta) - hpsi, with psi theta written to `work` (nfunc x ld block,
+ * or NULL for a block owned by ctx); apply_B 0: res = psi theta - hpsi.
+ * res may alias hpsi; neither res nor work may alias psi.  mode as for
+ * mgx_mult_matrix. */
+int mgx_residual(mgx_ctx* ctx, int mode, mgx_dtype dtype, const void* psi,
+    const void* hpsi, size_t ld, int nfunc, const double* theta, int apply_B,
+    void* work, void* res, void* stream);
+
+/* ---------------------------------------------------------------- */
+/* Poisson multigrid (pb::Mgm, src/pb/Mgm.h:20-112, with pb::Vcycle,  */
+/* src/pb/Vcycle.h:28-249) on one field of the context grid.          */
+/* ---------------------------------------------------------------- */
+
+/* Arguments of pb::Mgm: the fine operator (lap_type 0..4 as Laph4M,
+ * Laph2, Laph4, Laph6, Laph8; coarse levels keep Laph4M, the others use
+ * Laph2), cogr (at most max_levels coarsenings), max_sweeps V-cycles, the
+ * relative residual tolerance, nu1 / nu2 smoothing sweeps, and the ghost
+ * width of the caller's fine GridFunc (0: the operator's), which enters the
+ * coarsening test dim >= 2 * ghosts. */
+typedef struct mgx_mgm_params
+{
+    int lap_type;
+    int max_levels;
+    int max_sweeps;
+    double tol;
+    int nu1;
+    int nu2;
+    int ghosts;
+} mgx_mgm_params;
+
+/* The out-parameters of pb::Mgm, its bool result (converged) and the
+ * number of grids the cycle used. */
+typedef struct mgx_mgm_result
+{
+    double final_residual;
+    double final_relative_residual;
+    double residual_reduction;
+    int nb_sweeps;
+    int converged;
+    int levels;
+} mgx_mgm_result;
+
+/* Solves A vh = A.rhs(rho) (rho and vh ghost-free device fields of the
+ * context grid, periodic) from the initial vh, in place, as pb::Mgm with
+ * one task: rhs = B rho for Mehrstellen, rho otherwise; at most max_sweeps
+ * V-cycles, stopping when |rhs - A vh| < tol |rhs| (norms sqrt(sum x^2
+ * h^3)).  Not converging is reported in *result, not as an error.
+ * Synchronous (the residual norms are read on the host every cycle). */
+int mgx_mgm(mgx_ctx* ctx, const mgx_mgm_params* params, mgx_dtype dtype,
+    void* vh, const void* rho, mgx_mgm_result* result, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

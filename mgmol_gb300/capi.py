@@ -53,6 +53,18 @@ class PrecondParams(ctypes.Structure):
                 ("chunk", ctypes.c_int)]
 
 
+class MgmParams(ctypes.Structure):
+    _fields_ = [("lap_type", ctypes.c_int), ("max_levels", ctypes.c_int),
+                ("max_sweeps", ctypes.c_int), ("tol", ctypes.c_double), ("nu1", ctypes.c_int),
+                ("nu2", ctypes.c_int), ("ghosts", ctypes.c_int)]
+
+
+class MgmResult(ctypes.Structure):
+    _fields_ = [("final_residual", ctypes.c_double), ("final_relative_residual", ctypes.c_double),
+                ("residual_reduction", ctypes.c_double), ("nb_sweeps", ctypes.c_int),
+                ("converged", ctypes.c_int), ("levels", ctypes.c_int)]
+
+
 _LIB = None
 _vp = ctypes.c_void_p
 _i = ctypes.c_int
@@ -88,6 +100,10 @@ _SIGS = {
     "mgx_cholesky": [_vp, _i, _vp, _ip, _vp],
     "mgx_inverse_from_cholesky": [_vp, _i, _vp, _vp, _vp],
     "mgx_trace_prod": [_vp, _i, _vp, _vp, _vp, _vp],
+    "mgx_theta": [_vp, _i, _vp, _vp, _vp, _vp],
+    "mgx_mult_matrix": [_vp, _i, _i, _vp, _sz, _i, _vp, _vp, _vp],
+    "mgx_residual": [_vp, _i, _i, _vp, _vp, _sz, _i, _vp, _i, _vp, _vp, _vp],
+    "mgx_mgm": [_vp, ctypes.POINTER(MgmParams), _i, _vp, _vp, ctypes.POINTER(MgmResult), _vp],
 }
 
 # every entry point declared in include/mgx.h
@@ -154,6 +170,14 @@ def _block(t, npts):
 
 def _ptr(t):
     return ctypes.c_void_p(t.data_ptr()) if t is not None else None
+
+
+def axpy(alpha, x, y, stream=None):
+    """y += alpha x over whole blocks of the same dtype (mgx_axpy)."""
+    if x.dtype != y.dtype or x.numel() != y.numel() or not (x.is_contiguous() and y.is_contiguous()):
+        raise ValueError("axpy wants contiguous blocks of one dtype and size")
+    _check(load().mgx_axpy(x.numel(), float(alpha), _dtype(x), _ptr(x), _ptr(y), _stream(stream)))
+    return y
 
 
 class Context:
@@ -294,6 +318,60 @@ class Context:
         Sc = Sinv.T.contiguous()
         out = torch.empty(1, dtype=torch.float64, device=H.device)
         _check(load().mgx_trace_prod(self.handle, n, _ptr(Hc), _ptr(Sc), _ptr(out), _stream(stream)))
+        return out
+
+    # ------------------------------------------------------------ Poisson
+    def mgm(self, vh, rho, lap_type=LAP_MEHR4, max_levels=10, max_sweeps=10, tol=1e-16, nu1=2,
+            nu2=2, ghosts=0, stream=None):
+        """pb::Mgm on one field: vh (device, npts values) is solved in place;
+        returns the result fields as a dict."""
+        if vh.numel() != self.npts or rho.numel() != self.npts:
+            raise ValueError("vh and rho need one value per grid point")
+        if not (vh.is_contiguous() and rho.is_contiguous()) or vh.dtype != rho.dtype:
+            raise ValueError("vh and rho must be contiguous and of one dtype")
+        prm = MgmParams(lap_type, max_levels, max_sweeps, float(tol), nu1, nu2, ghosts)
+        res = MgmResult()
+        _check(load().mgx_mgm(self.handle, ctypes.byref(prm), _dtype(vh), _ptr(vh), _ptr(rho),
+                              ctypes.byref(res), _stream(stream)))
+        return {k: getattr(res, k) for k, _ in MgmResult._fields_}
+
+    # ------------------------------------------------------------ residual
+    def theta(self, Sinv, H, stream=None):
+        """theta = Sinv H (row-major tensors in and out; Sinv read from its
+        lower triangle)."""
+        n = H.shape[0]
+        Sc = Sinv.T.contiguous()
+        Hc = H.T.contiguous()
+        out = torch.empty((n, n), dtype=torch.float64, device=H.device)
+        _check(load().mgx_theta(self.handle, n, _ptr(Sc), _ptr(Hc), _ptr(out), _stream(stream)))
+        return out.T
+
+    @staticmethod
+    def _colmajor(theta):
+        t = theta.T
+        return t if t.is_contiguous() else t.contiguous()
+
+    def mult_matrix(self, psi, theta, mode=GEMM_FP64, out=None, stream=None):
+        """out_j = sum_i psi_i theta[i, j] (theta a row-major FP64 tensor)."""
+        p, ld, nf = _block(psi, self.npts)
+        out = torch.empty_like(psi) if out is None else out
+        po, ldo, _ = _block(out, self.npts)
+        assert ldo == ld
+        tc = self._colmajor(theta)
+        _check(load().mgx_mult_matrix(self.handle, mode, _dtype(psi), p, ld, nf, _ptr(tc), po,
+                                      _stream(stream)))
+        return out
+
+    def residual(self, psi, hpsi, theta, mode=GEMM_FP64, apply_B=True, work=None, out=None,
+                 stream=None):
+        """res = B(psi) theta - hpsi (apply_B) or psi theta - hpsi; out may be hpsi."""
+        p, ld, nf = _block(psi, self.npts)
+        ph, ldh, _ = _block(hpsi, self.npts)
+        assert ldh == ld
+        out = torch.empty_like(psi) if out is None else out
+        tc = self._colmajor(theta)
+        _check(load().mgx_residual(self.handle, mode, _dtype(psi), p, ph, ld, nf, _ptr(tc),
+                                   1 if apply_B else 0, _ptr(work), _ptr(out), _stream(stream)))
         return out
 
 

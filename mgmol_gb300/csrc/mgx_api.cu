@@ -78,6 +78,13 @@ int masks_apply(mgx_ctx*, const mgx_masks*, int, void*, size_t, int, cudaStream_
 int masks_expand(const mgx_masks*, int, void*, int*, cudaStream_t);
 int gram_cuda_cores(mgx_ctx*, int, const void*, const void*, size_t, size_t,
     int, double, int, double*, cudaStream_t);
+int psi_theta_cuda_cores(int, const void*, size_t, size_t, int, const double*,
+    double, const void*, void*, cudaStream_t);
+int psi_theta_tcgen05(mgx_ctx*, int, const float*, size_t, size_t, int,
+    const double*, float, const float*, float*, cudaStream_t);
+int theta_product(int, const double*, const double*, double*, cudaStream_t);
+int mgm_solve(mgx_ctx*, const mgx_mgm_params*, int, void*, const void*, mgx_mgm_result*,
+    cudaStream_t);
 int gram_tcgen05(mgx_ctx*, int, const void*, const void*, size_t, size_t, int,
     double, int, double*, cudaStream_t);
 int gram_hmat_tcgen05(mgx_ctx*, int, const void*, const void*, size_t, size_t, int,
@@ -544,6 +551,107 @@ int mgx_trace_prod(mgx_ctx* ctx, int n, const double* H, const double* Sinv,
 {
     if (!ctx) return fail(MGX_BAD_ARG, "ctx is NULL");
     return trace_prod(n, H, Sinv, trace, (cudaStream_t)stream);
+}
+
+int mgx_theta(mgx_ctx* ctx, int n, const double* Sinv, const double* H,
+    double* theta, void* stream)
+{
+    if (!ctx) return fail(MGX_BAD_ARG, "ctx is NULL");
+    if (theta == Sinv || theta == H) return fail(MGX_BAD_ARG, "theta aliases an input");
+    return theta_product(n, Sinv, H, theta, (cudaStream_t)stream);
+}
+}
+
+namespace mgx
+{
+/* out = psi theta + beta cin (cin may alias out, out may not alias psi) */
+static int mult_matrix(mgx_ctx* ctx, int mode, mgx_dtype dtype, const void* psi,
+    size_t ld, int nfunc, const double* theta, double beta, const void* cin,
+    void* out, cudaStream_t s)
+{
+    const size_t npts = make_level(ctx->grid, 0).npts();
+    const size_t ldv  = nfunc > 1 ? ld : npts;
+    switch (mode)
+    {
+        case MGX_GEMM_FP64:
+            // FP64 accumulation for either orbital type, as MPgemmNN does
+            return psi_theta_cuda_cores(dtype == MGX_F64 ? 0 : 1, psi, ldv, npts, nfunc,
+                theta, beta, cin, out, s);
+        case MGX_GEMM_FP32:
+        case MGX_GEMM_TF32:
+        case MGX_GEMM_BF16X3:
+            if (dtype != MGX_F32)
+                return fail(MGX_BAD_ARG, "gemm mode %d needs FP32 orbitals", mode);
+            if (mode == MGX_GEMM_FP32)
+                return psi_theta_cuda_cores(2, psi, ldv, npts, nfunc, theta, beta, cin, out,
+                    s);
+            return psi_theta_tcgen05(ctx, mode, (const float*)psi, ldv, npts, nfunc, theta,
+                (float)beta, (const float*)cin, (float*)out, s);
+    }
+    return fail(MGX_BAD_ARG, "gemm mode %d", mode);
+}
+} // namespace mgx
+
+extern "C" {
+
+int mgx_mult_matrix(mgx_ctx* ctx, int mode, mgx_dtype dtype, const void* psi,
+    size_t ld, int nfunc, const double* theta, void* out, void* stream)
+{
+    if (!ctx) return fail(MGX_BAD_ARG, "ctx is NULL");
+    MGX_TRY(check_dtype(dtype));
+    MGX_TRY(check_block(ctx->grid, psi, ld, nfunc, "psi"));
+    MGX_TRY(check_block(ctx->grid, out, ld, nfunc, "out"));
+    if (nfunc == 0) return MGX_OK;
+    if (!theta) return fail(MGX_BAD_ARG, "theta is NULL");
+    if (psi == out) return fail(MGX_BAD_ARG, "psi and out alias");
+    return mult_matrix(ctx, mode, dtype, psi, ld, nfunc, theta, 0., nullptr, out,
+        (cudaStream_t)stream);
+}
+
+int mgx_residual(mgx_ctx* ctx, int mode, mgx_dtype dtype, const void* psi,
+    const void* hpsi, size_t ld, int nfunc, const double* theta, int apply_B,
+    void* work, void* res, void* stream)
+{
+    if (!ctx) return fail(MGX_BAD_ARG, "ctx is NULL");
+    MGX_TRY(check_dtype(dtype));
+    MGX_TRY(check_block(ctx->grid, psi, ld, nfunc, "psi"));
+    MGX_TRY(check_block(ctx->grid, hpsi, ld, nfunc, "hpsi"));
+    MGX_TRY(check_block(ctx->grid, res, ld, nfunc, "res"));
+    if (nfunc == 0) return MGX_OK;
+    if (!theta) return fail(MGX_BAD_ARG, "theta is NULL");
+    if (res == psi) return fail(MGX_BAD_ARG, "psi and res alias");
+    cudaStream_t s = (cudaStream_t)stream;
+    if (!apply_B)
+        // res = psi theta - hpsi in one pass (res may be hpsi)
+        return mult_matrix(ctx, mode, dtype, psi, ld, nfunc, theta, -1., hpsi, res, s);
+    const Level L   = make_level(ctx->grid, 0);
+    const size_t lw = nfunc > 1 ? ld : L.npts();
+    if (!work)
+    {
+        MGX_TRY(ctx->resid.ensure(lw * nfunc * dtype_size(dtype)));
+        work = ctx->resid.ptr;
+    }
+    if (work == psi || work == hpsi || work == res)
+        return fail(MGX_BAD_ARG, "work aliases psi, hpsi or res");
+    // B (psi theta) = (B psi) theta: the product first, then one stencil
+    // pass res = B work - hpsi
+    MGX_TRY(mult_matrix(ctx, mode, dtype, psi, ld, nfunc, theta, 0., nullptr, work, s));
+    PlaneParams p = plane(ctx->grid);
+    p.u   = work;
+    p.ldu = lw;
+    p.f   = hpsi;
+    p.ldf = lw;
+    p.out = res;
+    p.ldo = lw;
+    return stencil_launch(OP_RHS_SUB, 0, dtype, dtype, p, L, 0., nfunc, s);
+}
+
+int mgx_mgm(mgx_ctx* ctx, const mgx_mgm_params* params, mgx_dtype dtype, void* vh,
+    const void* rho, mgx_mgm_result* result, void* stream)
+{
+    if (!ctx) return fail(MGX_BAD_ARG, "ctx is NULL");
+    MGX_TRY(check_dtype(dtype));
+    return mgm_solve(ctx, params, dtype, vh, rho, result, (cudaStream_t)stream);
 }
 
 } // extern "C"

@@ -151,11 +151,13 @@ int gram_cuda_cores(mgx_ctx* ctx, int dtype, const void* A, const void* B,
 /* ------------------------------------------------------------------ */
 /* generic FP64 GEMM, column-major: C = alpha op(A) op(B) + beta C        */
 /* ------------------------------------------------------------------ */
+// sym_a: A is symmetric and only its lower triangle is read (BLAS symm
+// with side 'l', uplo 'l'); used without TA.
 template <bool TA, bool TB>
 __global__ void __launch_bounds__(256) dgemm_kernel(int m, int n, int k,
     double alpha, const double* __restrict__ A, int lda,
     const double* __restrict__ B, int ldb, double beta, double* C, int ldc,
-    int lower_only)
+    int lower_only, int sym_a)
 {
     __shared__ double As[16][65];
     __shared__ double Bs[16][65];
@@ -172,7 +174,8 @@ __global__ void __launch_bounds__(256) dgemm_kernel(int m, int n, int k,
             const int mm = e % 64, kk = e / 64;
             const int i = i0 + mm, j = j0 + mm, kq = kc + kk;
             double av = 0., bv = 0.;
-            if (i < m && kq < k) av = TA ? A[(size_t)i * lda + kq] : A[(size_t)kq * lda + i];
+            if (i < m && kq < k)
+                av = (TA || (sym_a && kq > i)) ? A[(size_t)i * lda + kq] : A[(size_t)kq * lda + i];
             if (j < n && kq < k) bv = TB ? B[(size_t)kq * ldb + j] : B[(size_t)j * ldb + kq];
             As[kk][mm] = av;
             Bs[kk][mm] = bv;
@@ -212,20 +215,128 @@ __global__ void __launch_bounds__(256) dgemm_kernel(int m, int n, int k,
 
 static int dgemm(bool ta, bool tb, int m, int n, int k, double alpha,
     const double* A, int lda, const double* B, int ldb, double beta, double* C,
-    int ldc, int lower_only, cudaStream_t s)
+    int ldc, int lower_only, cudaStream_t s, int sym_a = 0)
 {
     if (m <= 0 || n <= 0) return MGX_OK;
     dim3 grid((m + 63) / 64, (n + 63) / 64);
     if (!ta && !tb)
-        dgemm_kernel<false, false><<<grid, 256, 0, s>>>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, lower_only);
+        dgemm_kernel<false, false><<<grid, 256, 0, s>>>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, lower_only, sym_a);
     else if (!ta && tb)
-        dgemm_kernel<false, true><<<grid, 256, 0, s>>>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, lower_only);
+        dgemm_kernel<false, true><<<grid, 256, 0, s>>>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, lower_only, sym_a);
     else if (ta && !tb)
-        dgemm_kernel<true, false><<<grid, 256, 0, s>>>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, lower_only);
+        dgemm_kernel<true, false><<<grid, 256, 0, s>>>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, lower_only, sym_a);
     else
-        dgemm_kernel<true, true><<<grid, 256, 0, s>>>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, lower_only);
+        dgemm_kernel<true, true><<<grid, 256, 0, s>>>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, lower_only, sym_a);
     MGX_LAUNCH_CHECK("dgemm_kernel");
     return MGX_OK;
+}
+
+/* ------------------------------------------------------------------ */
+/* orbital block times a small FP64 matrix on CUDA cores (MPgemmNN,      */
+/* src/linear_algebra/mputils.cc:719-760):                               */
+/*   out_j[p] = sum_i psi_i[p] theta(i, j) + beta cin_j[p]               */
+/* ACC double: FP64 accumulation as the reference does for both orbital  */
+/* types; ACC float: theta rounded to FP32 and FP32 FMA.  Tiles of 128   */
+/* points x 64 functions, 8 x 4 results per thread.  cin may alias out.  */
+/* ------------------------------------------------------------------ */
+template <typename T, typename ACC>
+__global__ void __launch_bounds__(256) psi_theta_kernel(size_t npts, int n,
+    const T* __restrict__ psi, size_t ld, const double* __restrict__ theta,
+    double beta, const T* cin, T* out)
+{
+    __shared__ ACC As[16][128];
+    __shared__ ACC Bs[16][65];
+    const size_t p0 = (size_t)blockIdx.x * 128;
+    const int j0 = blockIdx.y * 64;
+    const int tid = threadIdx.x, tx = tid % 16, ty = tid / 16;
+    ACC acc[8][4];
+#pragma unroll
+    for (int a = 0; a < 8; a++)
+#pragma unroll
+        for (int b = 0; b < 4; b++)
+            acc[a][b] = ACC(0);
+    for (int kc = 0; kc < n; kc += 16)
+    {
+#pragma unroll
+        for (int r = 0; r < 8; r++)
+        {
+            const int e = tid + r * 256;
+            const int mm = e % 128, kk = e / 128;
+            const size_t p = p0 + mm;
+            const int i = kc + kk;
+            As[kk][mm] = (p < npts && i < n) ? (ACC)psi[(size_t)i * ld + p] : ACC(0);
+        }
+#pragma unroll
+        for (int r = 0; r < 4; r++)
+        {
+            const int e = tid + r * 256;
+            const int kk = e % 16, jj = e / 16;
+            const int i = kc + kk, j = j0 + jj;
+            Bs[kk][jj] = (i < n && j < n) ? (ACC)theta[(size_t)j * n + i] : ACC(0);
+        }
+        __syncthreads();
+#pragma unroll
+        for (int kk = 0; kk < 16; kk++)
+        {
+            ACC a[8], b[4];
+#pragma unroll
+            for (int q = 0; q < 8; q++) a[q] = As[kk][tx + 16 * q];
+#pragma unroll
+            for (int q = 0; q < 4; q++) b[q] = Bs[kk][ty + 16 * q];
+#pragma unroll
+            for (int u = 0; u < 8; u++)
+#pragma unroll
+                for (int v = 0; v < 4; v++)
+                    acc[u][v] = fma(a[u], b[v], acc[u][v]);
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int v = 0; v < 4; v++)
+    {
+        const int j = j0 + ty + 16 * v;
+        if (j >= n) continue;
+#pragma unroll
+        for (int u = 0; u < 8; u++)
+        {
+            const size_t p = p0 + tx + 16 * u;
+            if (p >= npts) continue;
+            const size_t o = (size_t)j * ld + p;
+            double r = (double)acc[u][v];
+            if (beta != 0.) r += beta * (double)cin[o];
+            out[o] = (T)r;
+        }
+    }
+}
+
+/* kind 0: FP64 orbitals; 1: FP32 orbitals, FP64 accumulation; 2: FP32
+ * orbitals, FP32 accumulation */
+int psi_theta_cuda_cores(int kind, const void* psi, size_t ld, size_t npts, int n,
+    const double* theta, double beta, const void* cin, void* out, cudaStream_t s)
+{
+    if (n <= 0 || npts == 0) return MGX_OK;
+    dim3 grid((unsigned)((npts + 127) / 128), (unsigned)((n + 63) / 64));
+    if (grid.y > 65535) return fail(MGX_UNSUPPORTED, "too many functions");
+    if (kind == 0)
+        psi_theta_kernel<double, double><<<grid, 256, 0, s>>>(npts, n, (const double*)psi, ld,
+            theta, beta, (const double*)cin, (double*)out);
+    else if (kind == 1)
+        psi_theta_kernel<float, double><<<grid, 256, 0, s>>>(npts, n, (const float*)psi, ld,
+            theta, beta, (const float*)cin, (float*)out);
+    else
+        psi_theta_kernel<float, float><<<grid, 256, 0, s>>>(npts, n, (const float*)psi, ld,
+            theta, beta, (const float*)cin, (float*)out);
+    MGX_LAUNCH_CHECK("psi_theta_kernel");
+    return MGX_OK;
+}
+
+/* ProjectedMatrices::updateTheta (src/ProjectedMatrices.h:218-225):
+ * theta = Sinv H with Sinv symmetric, read from its lower triangle. */
+int theta_product(int n, const double* Sinv, const double* H, double* theta,
+    cudaStream_t s)
+{
+    if (n <= 0 || !Sinv || !H || !theta) return fail(MGX_BAD_ARG, "theta: bad arguments");
+    return dgemm(false, false, n, n, n, 1., Sinv, n, H, n, 0., theta, n, 0, s, 1);
 }
 
 /* ------------------------------------------------------------------ */

@@ -99,6 +99,10 @@ struct mgx_ctx
     mgx::DeviceBuffer flag;
     // tensor-core GEMM: bf16 hi/lo planes, tile list, status word
     mgx::DeviceBuffer tc_split, tc_tiles, tc_err;
+    // residual: Psi Theta when the caller passes no work block
+    mgx::DeviceBuffer resid;
+    // Poisson multigrid levels
+    mgx::DeviceBuffer mgm;
 };
 
 /* ---------------- PTX helpers: mbarrier + 1-D bulk copies ---------------- */

@@ -238,6 +238,8 @@ struct PointOp
         {
             return eval_rhs<T>(at);
         }
+        if (OP == OP_RHS_SUB)
+            return eval_rhs<T>(at) - reinterpret_cast<const T*>(p.f)[(size_t)f * p.ldf + idx];
         const T lap = eval_lap<T, LAP, R>(c, at);
         if (OP == OP_LAP) return lap;
         if (OP == OP_HPSI_B)
@@ -277,7 +279,7 @@ struct PointOp
 template <typename T, typename TV, int LAP, int OP, int R, int S, int NP>
 __global__ void __launch_bounds__(256) plane_kernel(PlaneParams p, DevCoef<T> c)
 {
-    constexpr bool MEHRLIKE = (LAP == 0) || (OP == OP_RHS);
+    constexpr bool MEHRLIKE = (LAP == 0) || is_rhs_op(OP);
     constexpr int RR        = MEHRLIKE ? 1 : R; // halo rows staged
     constexpr int HOLD      = MEHRLIKE ? 0 : R; // stages kept behind the newest
     constexpr bool STAGE_V  = (OP == OP_HPSI_B);
@@ -388,16 +390,18 @@ __global__ void __launch_bounds__(256) plane_kernel(PlaneParams p, DevCoef<T> c)
     T* __restrict__ outp     = reinterpret_cast<T*>(p.out) + (size_t)f * p.ldo;
     T* __restrict__ wp       = p.w ? reinterpret_cast<T*>(p.w) + (size_t)f * p.ldw : nullptr;
     const T* __restrict__ fp = p.f ? reinterpret_cast<const T*>(p.f) + (size_t)f * p.ldf : nullptr;
-    constexpr bool POINTWISE = (OP == OP_JACOBI) || (OP == OP_HPSI_V);
+    constexpr bool POINTWISE = (OP == OP_JACOBI) || (OP == OP_HPSI_V) || (OP == OP_RHS_SUB);
 
     // pv: the pointwise operand at the emitted point (f for Jacobi, V for
-    // V psi), loaded before the plane wait so that its latency overlaps it
+    // V psi, g for B u - g), loaded before the plane wait so that its
+    // latency overlaps it
     auto finish = [&](int k, int x, T lap, T ucen, T pv) {
         const int y      = y0 + yy[k];
         const int z      = zz[k];
         const size_t idx = ((size_t)x * ny + y) * nz + z;
         T r              = lap;
         if (OP == OP_HPSI_V) r = lap + (T)((TV)ucen * (TV)pv);
+        if (OP == OP_RHS_SUB) r = lap - pv;
         if (OP == OP_JACOBI)
         {
             T w = lap - pv;
@@ -427,7 +431,7 @@ __global__ void __launch_bounds__(256) plane_kernel(PlaneParams p, DevCoef<T> c)
                 {
                     const size_t idx = ((size_t)xe * ny + y0 + yy[k]) * nz + zz[k];
                     pv[k]            = (T)0;
-                    if (val[k]) pv[k] = (OP == OP_JACOBI) ? fp[idx] : (T)vbase[idx];
+                    if (val[k]) pv[k] = (OP != OP_HPSI_V) ? fp[idx] : (T)vbase[idx];
                 }
             }
         }
@@ -446,7 +450,7 @@ __global__ void __launch_bounds__(256) plane_kernel(PlaneParams p, DevCoef<T> c)
                 const T u = st[oc[k]], uzm = st[ozm[k]], uzp = st[ozp[k]];
                 const T uym = st[oc[k] - nz], uyp = st[oc[k] + nz];
                 T a, b;
-                if (OP == OP_RHS)
+                if (is_rhs_op(OP))
                 {
                     a = (T)0.5 * u + (T)(1. / 12.) * (uym + uyp + uzm + uzp);
                     b = (T)(1. / 12.) * u;
@@ -572,7 +576,7 @@ __global__ void __launch_bounds__(256) plane_vec_kernel(PlaneParams p, DevCoef<T
     using V4          = typename Vec16<T>::type;
     using VH          = Vec16<T>;
     constexpr int VEC = VH::N;
-    constexpr bool EDGES   = (LAP == 0) && (OP != OP_RHS);
+    constexpr bool EDGES   = (LAP == 0) && !is_rhs_op(OP);
     constexpr bool STAGE_V = (OP == OP_HPSI_B);
     extern __shared__ __align__(128) unsigned char smem_raw[];
 
@@ -678,7 +682,7 @@ __global__ void __launch_bounds__(256) plane_vec_kernel(PlaneParams p, DevCoef<T
     T* __restrict__ outp     = reinterpret_cast<T*>(p.out) + (size_t)f * p.ldo;
     T* __restrict__ wp       = p.w ? reinterpret_cast<T*>(p.w) + (size_t)f * p.ldw : nullptr;
     const T* __restrict__ fp = p.f ? reinterpret_cast<const T*>(p.f) + (size_t)f * p.ldf : nullptr;
-    constexpr bool POINTWISE = (OP == OP_JACOBI) || (OP == OP_HPSI_V);
+    constexpr bool POINTWISE = (OP == OP_JACOBI) || (OP == OP_HPSI_V) || (OP == OP_RHS_SUB);
     const T c12 = (T)(1. / 12.), c05 = (T)0.5;
 
     bool ok    = true;
@@ -695,7 +699,7 @@ __global__ void __launch_bounds__(256) plane_vec_kernel(PlaneParams p, DevCoef<T
             for (int k = 0; k < NG; k++)
                 if (val[k])
                     pv[k] = *reinterpret_cast<const V4*>(
-                        (OP == OP_JACOBI ? fp : vbase) + xoff + goff[k]);
+                        (OP != OP_HPSI_V ? fp : vbase) + xoff + goff[k]);
         }
         ok = ok && mbar_wait(bars + (i % S), (uint32_t)((i / S) & 1));
         if (ok) waited = i;
@@ -738,7 +742,7 @@ __global__ void __launch_bounds__(256) plane_vec_kernel(PlaneParams p, DevCoef<T
                 T uym       = VH::get(cmv, v);
                 T uyp       = VH::get(cpv, v);
                 T a, b;
-                if (OP == OP_RHS)
+                if (is_rhs_op(OP))
                 {
                     a = c05 * u + c12 * (uym + uyp + uzm + uzp);
                     b = c12 * u;
@@ -775,6 +779,7 @@ __global__ void __launch_bounds__(256) plane_vec_kernel(PlaneParams p, DevCoef<T
                     T ucen = U1[k][v];
                     T r    = lap;
                     if (OP == OP_HPSI_V) r = lap + ucen * VH::get(pv[k], v);
+                    if (OP == OP_RHS_SUB) r = lap - VH::get(pv[k], v);
                     if (OP == OP_JACOBI)
                     {
                         T fv;
@@ -881,7 +886,7 @@ template <int LAP, int OP, int R>
 constexpr int stages_for()
 {
     // ring depth: planes held behind the newest + 3 in flight
-    return ((LAP == 0) || (OP == OP_RHS)) ? 4 : R + 4;
+    return ((LAP == 0) || is_rhs_op(OP)) ? 4 : R + 4;
 }
 
 /* Can the vectorised radius-1 kernel run this launch?  It needs the
@@ -891,7 +896,7 @@ template <typename T, typename TV, int LAP, int OP, int R>
 static bool vec_ok(const PlaneParams& p, int force_direct)
 {
     if (force_direct || R != 1) return false;
-    if (!(LAP == 0 || LAP == 1 || OP == OP_RHS)) return false;
+    if (!(LAP == 0 || LAP == 1 || is_rhs_op(OP))) return false;
     if ((OP == OP_HPSI_B || OP == OP_HPSI_V) && sizeof(T) != sizeof(TV)) return false;
     const int nx = p.n[0], ny = p.n[1], nz = p.n[2];
     auto al = [](const void* q, size_t ld) {
@@ -950,7 +955,7 @@ static int launch_t(const PlaneParams& p0, const DevCoef<T>& c, int nfunc,
         return fail(MGX_UNSUPPORTED, "scaled first sweep needs the vector kernel");
     PlaneParams p = p0;
     constexpr int S  = stages_for<LAP, OP, R>();
-    constexpr int RR = ((LAP == 0) || (OP == OP_RHS)) ? 1 : R;
+    constexpr int RR = ((LAP == 0) || is_rhs_op(OP)) ? 1 : R;
     constexpr bool STAGE_V = (OP == OP_HPSI_B);
     const int nx = p.n[0], ny = p.n[1], nz = p.n[2];
     const size_t esz = sizeof(T) + (STAGE_V ? sizeof(TV) : 0);
@@ -1030,19 +1035,27 @@ int stencil_launch(int op, int lap_type, int dtype, int v_dtype,
     if (nfunc <= 0) return MGX_OK;
     if (nfunc > 65535) return fail(MGX_BAD_ARG, "nfunc %d > 65535 per launch", nfunc);
     {
-        const int R = (op == OP_RHS) ? 1 : lap_radius(lap_type);
+        const int R = is_rhs_op(op) ? 1 : lap_radius(lap_type);
         for (int i = 0; i < 3; i++)
             if (p.n[i] < R)
                 return fail(MGX_BAD_ARG, "grid dimension %d = %d below stencil radius %d",
                     i, p.n[i], R);
     }
-    const StencilCoeffs sc = stencil_coeffs(op == OP_RHS ? 1 : lap_type, L.h);
+    const StencilCoeffs sc = stencil_coeffs(is_rhs_op(op) ? 1 : lap_type, L.h);
     if (op == OP_RHS)
     {
         if (dtype == MGX_F64)
             return launch_t<double, double, 0, OP_RHS, 1>(
                 p, to_dev<double>(sc, jf), nfunc, stream, force_direct);
         return launch_t<float, float, 0, OP_RHS, 1>(
+            p, to_dev<float>(sc, jf), nfunc, stream, force_direct);
+    }
+    if (op == OP_RHS_SUB)
+    {
+        if (dtype == MGX_F64)
+            return launch_t<double, double, 0, OP_RHS_SUB, 1>(
+                p, to_dev<double>(sc, jf), nfunc, stream, force_direct);
+        return launch_t<float, float, 0, OP_RHS_SUB, 1>(
             p, to_dev<float>(sc, jf), nfunc, stream, force_direct);
     }
     if (dtype == MGX_F64)

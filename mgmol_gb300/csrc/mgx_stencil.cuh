@@ -17,8 +17,11 @@ enum StencilOp
     OP_HPSI_B = 1, // out = -Lap_M u + B(V u)          (Mehrstellen only)
     OP_HPSI_V = 2, // out = -Lap u + V u
     OP_JACOBI = 3, // w = -Lap u - f ; out = mask(u - jf w) ; w_out = mask(w)
-    OP_RHS    = 4  // out = B u
+    OP_RHS    = 4, // out = B u
+    OP_RHS_SUB = 5 // out = B u - g (g pointwise, passed as f)
 };
+
+__host__ __device__ constexpr bool is_rhs_op(int op) { return op == OP_RHS || op == OP_RHS_SUB; }
 
 /* Localization masks of one level in box form: for function f, values of
  * the box starting at (box[6f], box[6f+1], box[6f+2]) (periodic) with

@@ -137,10 +137,21 @@ struct Params
     int symmetric;  // only i >= j entries of C are produced
     double* C;      // column-major, leading dimension n, FP64, accumulated atomically
     int* err;
+    // store epilogue (points x functions products): tile t of the launch is
+    // (t / ntj, t % ntj); out[j * ldo + i] = acc(i, j) + beta * cin[j * ldo + i]
+    // for i < nrows, j < ncols (cin may alias out)
+    float* out       = nullptr;
+    const float* cin = nullptr;
+    size_t ldo       = 0;
+    float beta       = 0.f;
+    int nrows        = 0;
+    int ntj          = 1;
 };
 
-// KIND 0: tf32 (NPROD 1); KIND 1: bf16 (NPROD 1 plain, 3 for hi/lo split)
-template <int KIND, int NPROD, int BN, int STAGES>
+// KIND 0: tf32 (NPROD 1); KIND 1: bf16 (NPROD 1 plain, 3 for hi/lo split).
+// STORE false: FP64 atomic accumulation of split-K partial tiles into C;
+// STORE true: one CTA per output tile over the whole K range, FP32 store.
+template <int KIND, int NPROD, int BN, int STAGES, bool STORE = false>
 __global__ void __launch_bounds__(THREADS, 1) gram_kernel(
     const __grid_constant__ CUtensorMap mA0, const __grid_constant__ CUtensorMap mA1,
     const __grid_constant__ CUtensorMap mB0, const __grid_constant__ CUtensorMap mB1,
@@ -165,7 +176,8 @@ __global__ void __launch_bounds__(THREADS, 1) gram_kernel(
     uint32_t* tslot = reinterpret_cast<uint32_t*>(accf + 1);
 
     const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
-    const int2 tile = p.tiles[blockIdx.x];
+    const int2 tile = STORE ? make_int2((int)blockIdx.x / p.ntj, (int)blockIdx.x % p.ntj)
+                            : p.tiles[blockIdx.x];
     const int i0 = tile.x * BM, j0 = tile.y * BN;
     const int kb0 = blockIdx.y * p.kb_per_cta;
     const int kb1 = min(p.kblocks, kb0 + p.kb_per_cta);
@@ -269,7 +281,25 @@ __global__ void __launch_bounds__(THREADS, 1) gram_kernel(
             {
                 float v[32];
                 tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)c0, v);
-                if (i < p.n)
+                if (STORE)
+                {
+                    if (i < p.nrows)
+                    {
+                        // each store instruction of the warp covers 32
+                        // consecutive points of one function: 128 bytes
+#pragma unroll
+                        for (int t = 0; t < 32; t++)
+                        {
+                            const int j = j0 + c0 + t;
+                            if (j < p.ncols)
+                            {
+                                const size_t o = (size_t)j * p.ldo + i;
+                                p.out[o] = (p.beta != 0.f) ? v[t] + p.beta * p.cin[o] : v[t];
+                            }
+                        }
+                    }
+                }
+                else if (i < p.n)
                 {
 #pragma unroll
                     for (int t = 0; t < 32; t++)
@@ -324,6 +354,76 @@ __global__ void split_kernel(const float* __restrict__ x, size_t ld, int rows,
     }
 }
 
+// Points-major operand of the points x functions product: columns
+// [p0, p0 + P) of the orbital block x (n functions, leading dimension ld)
+// become rows of K = function values, row p at p * ldo.  BF16 writes the
+// hi / lo planes, otherwise one FP32 plane (TF32).  64 x 64 tiles pass
+// through shared memory so that reads run along points and writes along
+// functions; columns n .. ldo-1 are written as zeros.
+template <bool BF16>
+__global__ void __launch_bounds__(256) transpose_split_kernel(const float* __restrict__ x,
+    size_t ld, int n, size_t p0, int P, void* __restrict__ hi, void* __restrict__ lo,
+    size_t ldo)
+{
+    __shared__ float t[64][65];
+    const int ib    = blockIdx.y * 64;
+    const size_t pb = (size_t)blockIdx.x * 64;
+    const int c     = threadIdx.x % 64;
+    for (int r = threadIdx.x / 64; r < 64; r += 4)
+    {
+        const int i       = ib + r;
+        const size_t pp   = pb + c;
+        t[r][c] = (i < n && pp < (size_t)P) ? x[(size_t)i * ld + p0 + pp] : 0.f;
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < 64 * 32; e += 256)
+    {
+        const int r = e / 32, q = e % 32;
+        const size_t pp = pb + r;
+        const int i     = ib + 2 * q;
+        if (pp >= (size_t)P || (size_t)i >= ldo) continue;
+        const float a = t[2 * q][r], b = t[2 * q + 1][r];
+        const size_t o = pp * ldo + i;
+        if (BF16)
+        {
+            const __nv_bfloat16 ha = __float2bfloat16_rn(a), hb = __float2bfloat16_rn(b);
+            __nv_bfloat162 h2, l2;
+            h2.x = ha;
+            h2.y = hb;
+            l2.x = __float2bfloat16_rn(a - __bfloat162float(ha));
+            l2.y = __float2bfloat16_rn(b - __bfloat162float(hb));
+            *reinterpret_cast<__nv_bfloat162*>((__nv_bfloat16*)hi + o) = h2;
+            *reinterpret_cast<__nv_bfloat162*>((__nv_bfloat16*)lo + o) = l2;
+        }
+        else
+            *reinterpret_cast<float2*>((float*)hi + o) = make_float2(a, b);
+    }
+}
+
+// FP64 matrix theta (n x n, column-major) -> function-major operand rows
+// j = column j of theta, K = i, leading dimension ldo: bf16 hi / lo planes
+// (hi = bf16(x), lo = bf16(x - hi)) or one FP32 plane; zero padded.
+template <bool BF16>
+__global__ void matrix_split_kernel(const double* __restrict__ th, int n, void* hi,
+    void* lo, size_t ldo)
+{
+    const size_t total = (size_t)n * ldo;
+    for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+         t += (size_t)gridDim.x * blockDim.x)
+    {
+        const size_t j = t / ldo, i = t - j * ldo;
+        const double x = (i < (size_t)n) ? th[j * n + i] : 0.;
+        if (BF16)
+        {
+            const __nv_bfloat16 h = __float2bfloat16_rn((float)x);
+            ((__nv_bfloat16*)hi)[t] = h;
+            ((__nv_bfloat16*)lo)[t] = __float2bfloat16_rn((float)(x - (double)__bfloat162float(h)));
+        }
+        else
+            ((float*)hi)[t] = (float)x;
+    }
+}
+
 static PFN_cuTensorMapEncodeTiled_v12000 encoder()
 {
     static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
@@ -362,14 +462,14 @@ static int make_map(CUtensorMap* m, const void* base, bool bf16, size_t K,
     return MGX_OK;
 }
 
-template <int KIND, int NPROD, int BN, int STAGES>
+template <int KIND, int NPROD, int BN, int STAGES, bool STORE = false>
 static int launch(const CUtensorMap& a0, const CUtensorMap& a1, const CUtensorMap& b0,
     const CUtensorMap& b1, const Params& p, int ntiles, int ksplit, cudaStream_t s)
 {
     constexpr int NOP   = (NPROD == 3) ? 2 : 1;
     constexpr int STAGE = NOP * (BM * ROWB + BN * ROWB);
     const size_t smem   = (size_t)STAGES * STAGE + (2 * STAGES + 1) * 8 + 16 + 1024;
-    auto kern           = gram_kernel<KIND, NPROD, BN, STAGES>;
+    auto kern           = gram_kernel<KIND, NPROD, BN, STAGES, STORE>;
     MGX_TRY(cuda_check(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)smem),
         "gram_kernel smem attribute"));
@@ -631,6 +731,101 @@ int gram_hmat_tcgen05(mgx_ctx* ctx, int mode, const void* psi, const void* hpsi,
     MGX_TRY(product(ctx, mode, a, ((used + 255) / 256) * 256, hpsi, ld, K, n, H, 1, s));
     MGX_TRY(finish(S, n, vel, 1, s));
     MGX_TRY(finish(H, n, vel, 0, s));
+    return end(ctx, s);
+}
+
+/* out_j = sum_i psi_i theta(i, j) + beta * cin_j over npts points (the
+ * MPgemmNN product of LocGridOrbitals::multiplyByMatrix,
+ * src/LocGridOrbitals.cc:793-830) on the tensor cores.  M = points,
+ * N = functions, K = functions: the points are processed in chunks whose
+ * transposed operand (rows = points, K = functions) fits a bounded
+ * workspace; theta is converted once.  One CTA per 128 x BN output tile. */
+int psi_theta_tcgen05(mgx_ctx* ctx, int mode, const float* psi, size_t ld, size_t npts,
+    int n, const double* theta, float beta, const float* cin, float* out,
+    cudaStream_t s)
+{
+    using namespace tc;
+    const bool bf         = (mode == MGX_GEMM_BF16X3);
+    const size_t esz      = bf ? 2 : 4;
+    const int nplanes     = bf ? 2 : 1;
+    const size_t ldk      = bf ? ((n + 63) / 64) * 64 : ((n + 31) / 32) * 32;
+    const size_t b_plane  = ldk * (size_t)n * esz;
+    const size_t b_bytes  = ((nplanes * b_plane + 1023) / 1024) * 1024;
+    const size_t row_bytes = nplanes * ldk * esz; // one point of the A operand
+    // chunk of points: at most 2 GiB of A operand, a multiple of the tile;
+    // MGX_PSI_THETA_CHUNK (points) overrides the size for tuning and tests
+    size_t P = ((size_t)2 << 30) / row_bytes;
+    if (const char* e = getenv("MGX_PSI_THETA_CHUNK"))
+        if (atol(e) > 0) P = (size_t)atol(e);
+    P        = std::max<size_t>(BM, (P / BM) * BM);
+    P        = std::min(P, ((npts + BM - 1) / BM) * BM);
+    const size_t a_plane = ldk * P * esz;
+    MGX_TRY(ctx->tc_split.ensure(b_bytes + nplanes * a_plane + 1024));
+    MGX_TRY(begin(ctx, s));
+    char* ws = (char*)ctx->tc_split.ptr;
+    void* bhi = ws;
+    void* blo = ws + b_plane;
+    void* ahi = ws + b_bytes;
+    void* alo = ws + b_bytes + a_plane;
+    {
+        const int nb = (int)std::min<size_t>((n * ldk + 255) / 256, 1 << 16);
+        if (bf)
+            matrix_split_kernel<true><<<nb, 256, 0, s>>>(theta, n, bhi, blo, ldk);
+        else
+            matrix_split_kernel<false><<<nb, 256, 0, s>>>(theta, n, bhi, blo, ldk);
+        MGX_LAUNCH_CHECK("matrix_split_kernel");
+    }
+    const int BN = (n > 128) ? 256 : 128;
+    CUtensorMap mb0, mb1, ma0, ma1;
+    MGX_TRY(make_map(&mb0, bhi, bf, n, n, ldk, BN));
+    mb1 = mb0;
+    if (bf) MGX_TRY(make_map(&mb1, blo, true, n, n, ldk, BN));
+    const int kblocks = (int)((n + (bf ? 63 : 31)) / (bf ? 64 : 32));
+    const int ntj     = (n + BN - 1) / BN;
+    for (size_t p0 = 0; p0 < npts; p0 += P)
+    {
+        const int Pc = (int)std::min(P, npts - p0);
+        dim3 tg((Pc + 63) / 64, (n + 63) / 64);
+        if (tg.y > 65535) return fail(MGX_UNSUPPORTED, "too many functions");
+        if (bf)
+            transpose_split_kernel<true><<<tg, 256, 0, s>>>(psi, ld, n, p0, Pc, ahi, alo, ldk);
+        else
+            transpose_split_kernel<false><<<tg, 256, 0, s>>>(psi, ld, n, p0, Pc, ahi, alo, ldk);
+        MGX_LAUNCH_CHECK("transpose_split_kernel");
+        MGX_TRY(make_map(&ma0, ahi, bf, n, Pc, ldk, BM));
+        ma1 = ma0;
+        if (bf) MGX_TRY(make_map(&ma1, alo, true, n, Pc, ldk, BM));
+        Params p;
+        p.tiles      = nullptr;
+        p.kblocks    = kblocks;
+        p.kb_per_cta = kblocks;
+        p.n          = 0;
+        p.ncols      = n;
+        p.symmetric  = 0;
+        p.C          = nullptr;
+        p.err        = (int*)ctx->tc_err.ptr;
+        p.out        = out + p0;
+        p.cin        = cin ? cin + p0 : nullptr;
+        p.ldo        = ld;
+        p.beta       = cin ? beta : 0.f;
+        p.nrows      = Pc;
+        p.ntj        = ntj;
+        const int ntiles = ((Pc + BM - 1) / BM) * ntj;
+        if (BN == 256)
+        {
+            if (bf)
+                MGX_TRY((launch<1, 3, 256, 2, true>(ma0, ma1, mb0, mb1, p, ntiles, 1, s)));
+            else
+                MGX_TRY((launch<0, 1, 256, 4, true>(ma0, ma0, mb0, mb0, p, ntiles, 1, s)));
+        }
+        else
+        {
+            if (bf)
+                MGX_TRY((launch<1, 3, 128, 3, true>(ma0, ma1, mb0, mb1, p, ntiles, 1, s)));
+            else
+                MGX_TRY((launch<0, 1, 128, 6, true>(ma0, ma0, mb0, mb0, p, ntiles, 1, s)));
+        }
+    }
     return end(ctx, s);
 }
 } // namespace mgx

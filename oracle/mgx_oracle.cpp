@@ -1043,6 +1043,181 @@ static int precond_t(const int n[3], const double ll[3], int lap_type,
     return 0;
 }
 
+/* ------------------------------------------------------------------ */
+/* Poisson multigrid on one field: pb::Vcycle (src/pb/Vcycle.h:28-249)  */
+/* and pb::Mgm (src/pb/Mgm.h:20-112), one task, periodic.               */
+/* ------------------------------------------------------------------ */
+
+/* BLAS-style y += alpha x in the element type (GridFunc::operator-= and
+ * operator+=, src/pb/GridFunc.cc:306-319,497-505). */
+template <typename T>
+void taxpy(size_t n, T alpha, const T* x, T* y)
+{
+    for (size_t k = 0; k < n; k++)
+        y[k] += alpha * x[k];
+}
+
+/* GridFunc::norm2 (src/pb/GridFunc.cc:2745-2800,2856-2861): interior sum
+ * of squares in double, one partial dot per z line (MPdot) added in x, y
+ * order, times the volume element, square root. */
+template <typename T>
+double gf_norm(const Grid& g, const T* u)
+{
+    double d = 0.;
+    for (int ix = 0; ix < g.n[0]; ix++)
+        for (int iy = 0; iy < g.n[1]; iy++)
+        {
+            const T* line = u + (size_t)(ix + g.ng) * g.incx() + (iy + g.ng) * g.incy() + g.ng;
+            double t = 0.;
+            for (int iz = 0; iz < g.n[2]; iz++)
+                t += (double)line[iz] * (double)line[iz];
+            d += t;
+        }
+    return std::sqrt(d * g.vel());
+}
+
+/* Lap::jacobi (src/pb/Lap.cc:27-37): W = A x - B; x += -jf W. */
+template <typename T>
+void gf_jacobi(int op, const Grid& g, double jf, T* x, const T* b, T* w)
+{
+    const size_t n = g.sizeg();
+    trade(g, x, 1);
+    apply_lap(op, g, x, w, 1);
+    taxpy(n, (T)-1, b, w);
+    mpaxpy(n, -1. * jf, w, x);
+}
+
+/* getLowerOrderOp of each operator: Laph4M stays Laph4M (src/pb/Laph4M.h:57),
+ * Laph8 -> Laph6 -> Laph4 -> Laph2 -> Laph2 (src/pb/Laph8.h:79-87,
+ * Laph6.h:79-87, Laph4.h:75-83, Laph2.h:71-79). */
+static int lower_order(int op)
+{
+    switch (op)
+    {
+        case 0: return 0;
+        case 1: return 1;
+        case 2: return 1;
+        case 3: return 2;
+        case 4: return 3;
+    }
+    return -1;
+}
+
+/* Vcycle from x = 0.  op_ng: ghost width of the level operator's grid
+ * (the caller's on the fine level; below, the lower-order grid built with
+ * the lower operator's minimum ghost width), which sets the coarse
+ * function's ghost width max(op_ng - 1, 1) (src/pb/Vcycle.h:176-180). */
+template <typename T>
+void vcycle(int op, const Grid& g, int op_ng, int level, T* x, const T* rhs, int cogr,
+    int nu1, int nu2)
+{
+    const double jf = Precond<T, T>::jacobi_factor(op, g);
+    const size_t n  = g.sizeg();
+    std::vector<T> res(n, (T)0);
+    bool coarsen = true;
+    for (int i = 0; i < 3; i++)
+        if ((g.n[i] & 1) || g.n[i] < 2 * g.ng) coarsen = false;
+    for (int i = 0; i < nu1; i++)
+        gf_jacobi(op, g, jf, x, rhs, res.data());
+    if (level > -cogr && coarsen)
+    {
+        trade(g, x, 1);
+        apply_lap(op, g, x, res.data(), 1);
+        taxpy(n, (T)-1, rhs, res.data());
+        const Grid cg = g.coarse().with_ghosts(std::max(op_ng - 1, 1));
+        std::vector<T> rc(cg.sizeg(), (T)0), uc(cg.sizeg(), (T)0);
+        trade(g, res.data(), 1);
+        restrict3d(g, res.data(), cg, rc.data(), 1);
+        const int lop = lower_order(op);
+        vcycle(lop, cg, ghosts_for(lop), level - 1, uc.data(), rc.data(), cogr, nu1, nu2);
+        trade(cg, uc.data(), 1);
+        extend3d(cg, uc.data(), g, res.data(), 1);
+        taxpy(n, (T)-1, res.data(), x);
+    }
+    for (int i = 0; i < nu2; i++)
+        gf_jacobi(op, g, jf, x, rhs, res.data());
+}
+
+/* Mgm: rhs = A.rhs(rho) (B rho for Laph4M, rho otherwise); up to
+ * max_sweeps times: res = rhs - A vh, stop when |res| < tol |rhs|, else
+ * vh += Vcycle(res).  out = final residual, final relative residual,
+ * residual reduction, sweeps, converged, levels used. */
+template <typename T>
+static int mgm_t(const int n[3], const double ll[3], int lap_type, int ng, int cogr,
+    int max_sweeps, double tol, int nu1, int nu2, T* vh_io, const T* rho, double* out)
+{
+    if (ghosts_for(lap_type) < 0 || ng < ghosts_for(lap_type)) return 1;
+    const Grid g   = make_grid(n, ll, ng);
+    const size_t s = g.sizeg();
+    std::vector<T> vh(s, (T)0), rhs(s, (T)0), res(s, (T)0), lhs(s, (T)0), work(s, (T)0);
+    to_ghosted(g, vh_io, g.size(), vh.data(), 1);
+    to_ghosted(g, rho, g.size(), res.data(), 1);
+    if (lap_type == 0)
+    {
+        trade(g, res.data(), 1);
+        rhs_mehr1(g, res.data(), rhs.data(), 1);
+    }
+    else
+        rhs = res;
+    const double inv_rhs_norm = 1. / gf_norm(g, rhs.data());
+    double init = 1., fr = 0., frr = 0.;
+    bool conv = false;
+    int nb    = 0;
+    for (int i = 0; i < max_sweeps; i++)
+    {
+        trade(g, vh.data(), 1);
+        apply_lap(lap_type, g, vh.data(), lhs.data(), 1);
+        for (size_t k = 0; k < s; k++)
+            res[k] = rhs[k] - lhs[k];
+        const double rn = gf_norm(g, res.data());
+        if (i == 0) init = rn;
+        if (rn * inv_rhs_norm < tol)
+        {
+            fr   = rn;
+            frr  = rn * inv_rhs_norm;
+            conv = true;
+            break;
+        }
+        std::fill(work.begin(), work.end(), (T)0);
+        vcycle(lap_type, g, ng, 0, work.data(), res.data(), cogr, nu1, nu2);
+        nb++;
+        taxpy(s, (T)1, work.data(), vh.data());
+    }
+    if (!conv)
+    {
+        trade(g, vh.data(), 1);
+        apply_lap(lap_type, g, vh.data(), lhs.data(), 1);
+        taxpy(s, (T)-1, rhs.data(), lhs.data());
+        fr  = gf_norm(g, lhs.data());
+        frr = fr * inv_rhs_norm;
+    }
+    from_ghosted(g, vh.data(), vh_io, g.size(), 1);
+    // grids the cycle visits
+    int levels = 1;
+    {
+        Grid c  = g;
+        int cng = ng, op = lap_type;
+        for (int l = 0; l < cogr; l++)
+        {
+            bool ok = true;
+            for (int i = 0; i < 3; i++)
+                if ((c.n[i] & 1) || c.n[i] < 2 * c.ng) ok = false;
+            if (!ok) break;
+            c   = c.coarse().with_ghosts(std::max(cng - 1, 1));
+            op  = lower_order(op);
+            cng = ghosts_for(op);
+            levels++;
+        }
+    }
+    out[0] = fr;
+    out[1] = frr;
+    out[2] = fr / init;
+    out[3] = nb;
+    out[4] = conv ? 1. : 0.;
+    out[5] = levels;
+    return 0;
+}
+
 /* OrbitalsPreconditioning<T>::setGamma, src/OrbitalsPreconditioning.cc:119-145 */
 static double set_gamma(double inv_diag, int mg_levels, double vmax, double small_eig)
 {
@@ -1398,3 +1573,114 @@ double orc_trace_prod(int n, const double* H, const double* Sinv)
 }
 
 } // extern "C"
+
+/* ------------------------------------------------------------------ */
+/* Residual and update of the block preconditioned-gradient step.       */
+/* ------------------------------------------------------------------ */
+extern "C" {
+
+/* ProjectedMatrices::updateTheta (src/ProjectedMatrices.h:218-225):
+ * theta = S^-1 H with S^-1 used as symmetric (lower part), column-major. */
+int orc_theta(int n, const double* Sinv, const double* H, double* theta)
+{
+#pragma omp parallel for
+    for (int j = 0; j < n; j++)
+        for (int i = 0; i < n; i++)
+        {
+            double s = 0.;
+            for (int k = 0; k < n; k++)
+            {
+                const double a = (i >= k) ? Sinv[(size_t)k * n + i] : Sinv[(size_t)i * n + k];
+                s += a * H[(size_t)j * n + k];
+            }
+            theta[(size_t)j * n + i] = s;
+        }
+    return 0;
+}
+
+/* LocGridOrbitals::multiplyByMatrix (src/LocGridOrbitals.cc:793-830), one
+ * subdomain: out_j = sum_i psi_i theta(i, j), FP64 accumulation. */
+int orc_mult_matrix_d(const double* psi, long ld, int nfunc, long numpt,
+    const double* theta, double* out)
+{
+#pragma omp parallel for
+    for (long p = 0; p < numpt; p++)
+        for (int j = 0; j < nfunc; j++)
+        {
+            double s = 0.;
+            for (int i = 0; i < nfunc; i++)
+                s += psi[(size_t)i * ld + p] * theta[(size_t)j * nfunc + i];
+            out[(size_t)j * ld + p] = s;
+        }
+    return 0;
+}
+int orc_mult_matrix_f(const float* psi, long ld, int nfunc, long numpt,
+    const double* theta, float* out)
+{
+#pragma omp parallel for
+    for (long p = 0; p < numpt; p++)
+        for (int j = 0; j < nfunc; j++)
+        {
+            double s = 0.;
+            for (int i = 0; i < nfunc; i++)
+                s += (double)psi[(size_t)i * ld + p] * theta[(size_t)j * nfunc + i];
+            out[(size_t)j * ld + p] = (float)s;
+        }
+    return 0;
+}
+}
+
+/* MGmol::computeResidualUsingHPhi (src/MGmol.cc:1227-1290): with applyB,
+ * tmp = B psi for every function (Lap::rhs), then res = tmp theta - hpsi;
+ * without, res = psi theta - hpsi.  Rydberg units. */
+template <typename T>
+static int residual_t(const int* n, const double* ll, int apply_B, int nfunc,
+    const T* psi, const T* hpsi, const double* theta, T* res)
+{
+    const size_t np = (size_t)n[0] * n[1] * n[2];
+    std::vector<T> tmp(np * nfunc);
+    if (apply_B)
+        rhs_mehr_t(n, ll, nfunc, psi, tmp.data());
+    else
+        std::copy(psi, psi + np * nfunc, tmp.begin());
+    std::vector<T> prod(np * nfunc);
+#pragma omp parallel for
+    for (long p = 0; p < (long)np; p++)
+        for (int j = 0; j < nfunc; j++)
+        {
+            double s = 0.;
+            for (int i = 0; i < nfunc; i++)
+                s += (double)tmp[(size_t)i * np + p] * theta[(size_t)j * nfunc + i];
+            prod[(size_t)j * np + p] = (T)s;
+        }
+    // res.axpy(-1., hphi)
+    for (size_t k = 0; k < np * nfunc; k++)
+        res[k] = prod[k] + static_cast<T>(-1. * static_cast<double>(hpsi[k]));
+    return 0;
+}
+
+extern "C" {
+int orc_residual_d(const int* n, const double* ll, int apply_B, int nfunc,
+    const double* psi, const double* hpsi, const double* theta, double* res)
+{
+    return residual_t(n, ll, apply_B, nfunc, psi, hpsi, theta, res);
+}
+int orc_residual_f(const int* n, const double* ll, int apply_B, int nfunc,
+    const float* psi, const float* hpsi, const double* theta, float* res)
+{
+    return residual_t(n, ll, apply_B, nfunc, psi, hpsi, theta, res);
+}
+
+int orc_mgm_d(const int* n, const double* ll, int lap_type, int ng, int cogr,
+    int max_sweeps, double tol, int nu1, int nu2, double* vh, const double* rho,
+    double* out)
+{
+    return mgm_t(n, ll, lap_type, ng, cogr, max_sweeps, tol, nu1, nu2, vh, rho, out);
+}
+int orc_mgm_f(const int* n, const double* ll, int lap_type, int ng, int cogr,
+    int max_sweeps, double tol, int nu1, int nu2, float* vh, const float* rho,
+    double* out)
+{
+    return mgm_t(n, ll, lap_type, ng, cogr, max_sweeps, tol, nu1, nu2, vh, rho, out);
+}
+}

@@ -267,3 +267,64 @@ def trace_prod(H, Sinv):
     Hc = np.ascontiguousarray(np.asarray(H, dtype=np.float64).T)
     Sc = np.ascontiguousarray(np.asarray(Sinv, dtype=np.float64).T)
     return lib().orc_trace_prod(n, _p(Hc), _p(Sc))
+
+
+def theta(Sinv, H):
+    """theta = S^-1 H (row-major numpy in/out)."""
+    n = Sinv.shape[0]
+    Sc = np.ascontiguousarray(np.asarray(Sinv, dtype=np.float64).T)
+    Hc = np.ascontiguousarray(np.asarray(H, dtype=np.float64).T)
+    out = np.zeros((n, n))
+    _call(lib(), "orc_theta", n, _p(Sc), _p(Hc), _p(out))
+    return out.T.copy()
+
+
+def mult_matrix(psi, th, ref=False):
+    """out_j = sum_i psi_i theta[i, j] (theta row-major numpy)."""
+    psi = np.ascontiguousarray(psi)
+    nf, npt = psi.shape
+    tc = np.ascontiguousarray(np.asarray(th, dtype=np.float64).T)
+    out = np.zeros_like(psi)
+    if ref:
+        _call(ref_lib(), f"ref_mult_matrix_{_sfx(psi)}", npt, nf, _p(psi), _p(tc), _p(out))
+        return out
+    _call(lib(), f"orc_mult_matrix_{_sfx(psi)}", _p(psi), ctypes.c_long(npt), nf, ctypes.c_long(npt),
+          _p(tc), _p(out))
+    return out
+
+
+def residual(n, ll, psi, hpsi_, th, apply_B=1, ref=False):
+    """res = (B psi) theta - hpsi (computeResidualUsingHPhi)."""
+    psi = np.ascontiguousarray(psi)
+    hpsi_ = np.ascontiguousarray(hpsi_, dtype=psi.dtype)
+    tc = np.ascontiguousarray(np.asarray(th, dtype=np.float64).T)
+    out = np.zeros_like(psi)
+    gn, gl = _grid(n, ll)
+    if ref:
+        assert apply_B
+        _call(ref_lib(), f"ref_residual_{_sfx(psi)}", gn, gl, psi.shape[0], _p(psi), _p(hpsi_),
+              _p(tc), _p(out))
+        return out
+    _call(lib(), f"orc_residual_{_sfx(psi)}", gn, gl, apply_B, psi.shape[0], _p(psi), _p(hpsi_),
+          _p(tc), _p(out))
+    return out
+
+
+def mgm(n, ll, lap_type, vh, rho, ghosts=0, cogr=10, max_sweeps=10, tol=1e-16, nu1=2, nu2=2,
+        ref=False):
+    """pb::Mgm on one field: returns (vh after the solve, info dict).  ghosts:
+    ghost width of the fine grid (0: the operator's)."""
+    L = ref_lib() if ref else lib()
+    pre = "ref" if ref else "orc"
+    vh = np.array(vh, copy=True).reshape(-1)
+    rho = np.ascontiguousarray(rho, dtype=vh.dtype).reshape(-1)
+    ng = ghosts if ghosts > 0 else {0: 1, 1: 1, 2: 2, 3: 3, 4: 4}[lap_type]
+    out = np.zeros(6)
+    gn, gl = _grid(n, ll)
+    _call(L, f"{pre}_mgm_{_sfx(vh)}", gn, gl, lap_type, ng, cogr, max_sweeps, ctypes.c_double(tol),
+          nu1, nu2, _p(vh), _p(rho), _p(out))
+    info = {"final_residual": out[0], "final_relative_residual": out[1],
+            "residual_reduction": out[2], "nb_sweeps": int(out[3]), "converged": bool(out[4])}
+    if not ref:
+        info["levels"] = int(out[5])
+    return vh, info

@@ -73,8 +73,23 @@ template class Preconditioning<double>;
 #include "pb/GridFuncVector.h"
 #include "pb/MGkernels.h"
 
+#include "pb/Laph2.h"
+#include "pb/Laph4.h"
+#include "pb/Laph4M.h"
+#include "pb/Laph6.h"
+#include "pb/Laph8.h"
+#include "pb/Mgm.h"
+#include "mputils.h"
+#include "MGmol_MPI.h"
+
 #include <memory>
 #include <vector>
+
+// the V-cycle timers are defined with pb::SolverLap (src/pb/SolverLap.cc:20-23)
+Timer vcycle_repwrk_tm("vcycle_repwrk");
+Timer vcycle_repinit_tm("vcycle_repinit");
+Timer vcycle_repend_tm("vcycle_repend");
+Timer vcycle_repvcycle_tm("vcycle_repvcycle");
 
 namespace
 {
@@ -94,7 +109,8 @@ int ghosts_for(int lap_type)
 struct Env
 {
     pb::PEenv pe;
-    Env() : pe(MPI_COMM_WORLD) {}
+    // GridFunc::norm2 and friends reach MGmol_MPI::instance()
+    Env() : pe(MPI_COMM_WORLD) { MGmol_MPI::setup(MPI_COMM_WORLD, std::cout); }
 };
 Env& env()
 {
@@ -324,9 +340,89 @@ int mask_build(const int* n, const double* ll, int ng, int nlevels, int nfunc,
     forget_subcells();
     return 0;
 }
+/* pb::Mgm on one field: the reference template itself, with the operator
+ * class of lap_type on a fine grid of `ng` ghosts; out = final residual,
+ * final relative residual, residual reduction, sweeps, converged. */
+template <class Op, typename T>
+int mgm_op(const int* n, const double* ll, int ng, int cogr, int max_sweeps,
+    double tol, int nu1, int nu2, T* vh, const T* rho, double* out)
+{
+    pb::Grid g = make_grid(n, ll, ng);
+    Op A(g);
+    pb::GridFunc<T> gvh(g, 1, 1, 1), grho(g, 1, 1, 1);
+    gvh.assign(vh, 'd');
+    grho.assign(rho, 'd');
+    double fr = 0., frr = 0., red = 0.;
+    short nb  = 0;
+    const bool conv = pb::Mgm(A, gvh, grho, (short)cogr, (short)max_sweeps, tol,
+        (short)nu1, (short)nu2, false, fr, frr, red, nb);
+    gvh.init_vect(vh, 'd');
+    out[0] = fr;
+    out[1] = frr;
+    out[2] = red;
+    out[3] = nb;
+    out[4] = conv ? 1. : 0.;
+    return 0;
+}
+
+/* LocGridOrbitals::multiplyByMatrix: the reference's MPgemmNN on the block
+ * (src/LocGridOrbitals.cc:793-830). */
+template <typename T>
+int mult_matrix(int numpt, int nfunc, const T* psi, const double* theta, T* out)
+{
+    LinearAlgebraUtils<MemorySpace::Host>::MPgemmNN(numpt, nfunc, nfunc, 1., psi, numpt,
+        theta, nfunc, 0., out, numpt);
+    return 0;
+}
+
+/* MGmol::computeResidualUsingHPhi (src/MGmol.cc:1227-1290) with applyB:
+ * tmp_i = lapop->rhs(psi_i) per function, res = tmp theta (MPgemmNN),
+ * res.axpy(-1, hphi) (MPaxpy). */
+template <typename T>
+int residual(const int* n, const double* ll, int nfunc, const T* psi, const T* hphi,
+    const double* theta, T* res)
+{
+    pb::Grid g = make_grid(n, ll, 1);
+    const int np = (int)g.size();
+    pb::Laph4M<T> lap(g);
+    std::vector<T> tmp((size_t)np * nfunc);
+    for (int i = 0; i < nfunc; i++)
+    {
+        pb::GridFunc<T> gf(g, 1, 1, 1);
+        gf.assign(psi + (size_t)i * np, 'd');
+        lap.rhs(gf, tmp.data() + (size_t)i * np);
+    }
+    LinearAlgebraUtils<MemorySpace::Host>::MPgemmNN(np, nfunc, nfunc, 1., tmp.data(), np,
+        theta, nfunc, 0., res, np);
+    LinearAlgebraUtils<MemorySpace::Host>::MPaxpy(np * nfunc, -1., hphi, res);
+    return 0;
+}
+
+template <typename T>
+int mgm(const int* n, const double* ll, int lap_type, int ng, int cogr, int max_sweeps,
+    double tol, int nu1, int nu2, T* vh, const T* rho, double* out)
+{
+    switch (lap_type)
+    {
+        case 0: return mgm_op<pb::Laph4M<T>, T>(n, ll, ng, cogr, max_sweeps, tol, nu1, nu2, vh, rho, out);
+        case 1: return mgm_op<pb::Laph2<T>, T>(n, ll, ng, cogr, max_sweeps, tol, nu1, nu2, vh, rho, out);
+        case 2: return mgm_op<pb::Laph4<T>, T>(n, ll, ng, cogr, max_sweeps, tol, nu1, nu2, vh, rho, out);
+        case 3: return mgm_op<pb::Laph6<T>, T>(n, ll, ng, cogr, max_sweeps, tol, nu1, nu2, vh, rho, out);
+        case 4: return mgm_op<pb::Laph8<T>, T>(n, ll, ng, cogr, max_sweeps, tol, nu1, nu2, vh, rho, out);
+    }
+    return 1;
+}
 } // namespace
 
 extern "C" {
+int ref_mult_matrix_d(int np, int nf, const double* p, const double* th, double* o) { return mult_matrix(np, nf, p, th, o); }
+int ref_mult_matrix_f(int np, int nf, const float* p, const double* th, float* o) { return mult_matrix(np, nf, p, th, o); }
+int ref_residual_d(const int* n, const double* ll, int nf, const double* p, const double* h, const double* th, double* o) { return residual(n, ll, nf, p, h, th, o); }
+int ref_residual_f(const int* n, const double* ll, int nf, const float* p, const float* h, const double* th, float* o) { return residual(n, ll, nf, p, h, th, o); }
+int ref_mgm_d(const int* n, const double* ll, int t, int ng, int cogr, int ms, double tol, int nu1, int nu2, double* vh, const double* rho, double* out)
+{ return mgm(n, ll, t, ng, cogr, ms, tol, nu1, nu2, vh, rho, out); }
+int ref_mgm_f(const int* n, const double* ll, int t, int ng, int cogr, int ms, double tol, int nu1, int nu2, float* vh, const float* rho, double* out)
+{ return mgm(n, ll, t, ng, cogr, ms, tol, nu1, nu2, vh, rho, out); }
 int ref_fd_apply_d(const int* n, const double* ll, int t, int nf, const double* u, double* o) { return fd_apply(n, ll, t, nf, u, o); }
 int ref_fd_apply_f(const int* n, const double* ll, int t, int nf, const float* u, float* o) { return fd_apply(n, ll, t, nf, u, o); }
 int ref_rhs_mehr_d(const int* n, const double* ll, int nf, const double* u, double* o) { return rhs_mehr(n, ll, nf, u, o); }

@@ -67,6 +67,42 @@ def main():
     out["mask1_state"] = st1
     out["mask1_values_0"] = vals1[0]
     out["pc0_masked_d"] = O.precond(n, ll, 0, 2, 0.3, res, masks=(centers, radii), ref=True)
+    # Psi Theta (MPgemmNN) and the Mehrstellen residual B(psi) theta - hpsi
+    n = (16, 12, 20)
+    ll = (16 * 0.35, 12 * 0.35, 20 * 0.35)
+    psi, _, _ = synth.gaussian_orbitals(n, ll, 7, 1004)
+    V = synth.gaussian_wells(n, ll, 4, 1004)
+    rng = np.random.default_rng(1004)
+    th = np.eye(7) + rng.standard_normal((7, 7)) / 7
+    out["res_n"] = np.array(n)
+    out["res_ll"] = np.array(ll)
+    out["res_psi"] = psi
+    out["res_theta"] = th
+    for tag, dt in (("d", np.float64), ("f", np.float32)):
+        p = psi.astype(dt)
+        hp = O.hpsi(n, ll, 0, p, V, ref=True)
+        out[f"res_hpsi_{tag}"] = hp
+        out[f"mm_{tag}"] = O.mult_matrix(p, th, ref=True)
+        out[f"res_{tag}"] = O.residual(n, ll, p, hp, th, ref=True)
+    # pb::Mgm on one field, every operator (6 V-cycles, nu1 = nu2 = 2)
+    n = (16, 12, 20)
+    ll = (16 * 0.4, 12 * 0.4, 20 * 0.4)
+    rho = synth.gaussian_wells(n, ll, 6, 1005)
+    rho = rho - rho.mean()
+    vh0 = 0.1 * synth.gaussian_wells(n, ll, 3, 1006)
+    out["mgm_n"] = np.array(n)
+    out["mgm_ll"] = np.array(ll)
+    out["mgm_rho"] = rho
+    out["mgm_vh0"] = vh0
+    for t in range(5):
+        vh, info = O.mgm(n, ll, t, vh0, rho, max_sweeps=6, tol=1e-10, ref=True)
+        out[f"mgm{t}_vh"] = vh
+        out[f"mgm{t}_info"] = np.array([info["final_residual"], info["final_relative_residual"],
+                                        info["residual_reduction"], info["nb_sweeps"],
+                                        info["converged"]])
+    vh, info = O.mgm(n, ll, 0, vh0.astype(np.float32), rho.astype(np.float32), max_sweeps=3,
+                     tol=1e-10, ref=True)
+    out["mgm0_vh_f"] = vh
     np.savez_compressed(os.path.join(HERE, "ref_vectors.npz"), **out)
     print("wrote", os.path.join(HERE, "ref_vectors.npz"), len(out), "arrays")
 

@@ -44,6 +44,33 @@ def test_precond_matches_reference_vectors(G, tag, dt, lap):
     assert np.array_equal(out, G[f"pc{lap}_{tag}"])
 
 
+@pytest.mark.parametrize("tag,dt", [("d", np.float64), ("f", np.float32)])
+def test_residual_matches_reference_vectors(G, tag, dt):
+    n = tuple(int(x) for x in G["res_n"])
+    ll = tuple(float(x) for x in G["res_ll"])
+    psi = G["res_psi"].astype(dt)
+    th = G["res_theta"]
+    assert np.array_equal(O.mult_matrix(psi, th), G[f"mm_{tag}"])
+    hp = G[f"res_hpsi_{tag}"]
+    assert np.array_equal(O.residual(n, ll, psi, hp, th), G[f"res_{tag}"])
+
+
+@pytest.mark.parametrize("lap", range(5))
+def test_mgm_matches_reference_vectors(G, lap):
+    n = tuple(int(x) for x in G["mgm_n"])
+    ll = tuple(float(x) for x in G["mgm_ll"])
+    vh, info = O.mgm(n, ll, lap, G["mgm_vh0"], G["mgm_rho"], max_sweeps=6, tol=1e-10)
+    assert np.array_equal(vh, G[f"mgm{lap}_vh"])
+    ref = G[f"mgm{lap}_info"]
+    got = [info["final_residual"], info["final_relative_residual"], info["residual_reduction"],
+           info["nb_sweeps"], info["converged"]]
+    assert np.array_equal(np.array(got, dtype=np.float64), ref)
+    if lap == 0:
+        vf, _ = O.mgm(n, ll, 0, G["mgm_vh0"].astype(np.float32), G["mgm_rho"].astype(np.float32),
+                      max_sweeps=3, tol=1e-10)
+        assert np.array_equal(vf, G["mgm0_vh_f"])
+
+
 def test_masks_match_reference_vectors(G):
     n = tuple(int(x) for x in G["pc_n"])
     ll = tuple(float(x) for x in G["pc_ll"])

@@ -1,0 +1,182 @@
+"""Theta, Psi Theta and the residual (computeResidualUsingHPhi) on the GPU
+vs the oracle.
+
+Error bars, relative to max |reference|:
+  FP64 mode, FP64 orbitals                                    <= 1e-12
+  FP64 mode, FP32 orbitals (FP64 accumulation, FP32 result)   <= 3e-7
+  FP32 CUDA-core mode (FP32 FMA)                              <= 2e-5
+  BF16X3 tensor cores                                         <= 6e-5
+  TF32 tensor cores                                           <= 2e-3
+The BF16X3 bar: each operand is hi + lo with |x - hi - lo| <= 2^-16 |x|
+(bf16 unit roundoff 2^-8, twice), so one product carries up to ~2^-15
+relative error; with theta close to diagonal a single term dominates each
+output and nothing averages it out (the Gram sums over grid points do).
+"""
+import os
+
+import numpy as np
+import pytest
+import torch
+
+import oracle as O
+from helpers import TOL_F64, rel_err
+from mgmol_gb300 import capi, synth
+
+pytestmark = pytest.mark.gpu
+
+TOL = {capi.GEMM_FP32: 2e-5, capi.GEMM_TF32: 2e-3, capi.GEMM_BF16X3: 6e-5}
+
+
+def _dev(a, dt=np.float64):
+    return torch.from_numpy(np.ascontiguousarray(a.astype(dt))).cuda()
+
+
+def _theta(nf, seed):
+    rng = np.random.default_rng(seed)
+    return np.eye(nf) + rng.standard_normal((nf, nf)) / nf
+
+
+def test_theta_reads_lower_triangle():
+    n = 150
+    rng = np.random.default_rng(150)
+    A = rng.standard_normal((n, n))
+    Sinv = A @ A.T / n + np.eye(n)
+    H = rng.standard_normal((n, n))
+    junk = np.tril(Sinv) + np.triu(np.full((n, n), 7.0), 1)
+    ctx = capi.Context((8, 8, 8), (1, 1, 1))
+    th = ctx.theta(_dev(junk), _dev(H)).cpu().numpy()
+    assert rel_err(th, O.theta(Sinv, H)) < TOL_F64
+    assert rel_err(th, Sinv @ H) < TOL_F64
+
+
+@pytest.mark.parametrize("grid,nf", [((16, 16, 16), 5), ((15, 13, 11), 70), ((16, 16, 16), 130)])
+def test_mult_matrix_fp64(grid, nf):
+    ll = tuple(x * 0.35 for x in grid)
+    psi, _, _ = synth.gaussian_orbitals(grid, ll, nf, 31)
+    th = _theta(nf, 31)
+    ctx = capi.Context(grid, ll)
+    out = ctx.mult_matrix(_dev(psi), _dev(th)).cpu().numpy()
+    assert rel_err(out, O.mult_matrix(psi, th)) < TOL_F64
+
+
+def test_mult_matrix_fp32_orbitals_fp64_accumulation():
+    grid, nf = (16, 16, 16), 96
+    ll = tuple(x * 0.35 for x in grid)
+    psi, _, _ = synth.gaussian_orbitals(grid, ll, nf, 4)
+    p32 = psi.astype(np.float32)
+    th = _theta(nf, 4)
+    ctx = capi.Context(grid, ll)
+    out = ctx.mult_matrix(_dev(p32, np.float32), _dev(th)).cpu().numpy()
+    ref = O.mult_matrix(p32, th)
+    assert ref.dtype == np.float32
+    assert rel_err(out, ref) < 3e-7
+
+
+@pytest.mark.parametrize("mode", [capi.GEMM_FP32, capi.GEMM_TF32, capi.GEMM_BF16X3])
+@pytest.mark.parametrize("grid,nf", [((16, 16, 16), 64), ((15, 13, 11), 37), ((32, 24, 20), 200),
+                                     ((20, 20, 20), 300)])
+def test_mult_matrix_fp32_modes(mode, grid, nf):
+    ll = tuple(x * 0.35 for x in grid)
+    psi, _, _ = synth.gaussian_orbitals(grid, ll, nf, 8)
+    p32 = psi.astype(np.float32)
+    th = _theta(nf, 8)
+    ctx = capi.Context(grid, ll)
+    out = ctx.mult_matrix(_dev(p32, np.float32), _dev(th), mode=mode).cpu().numpy()
+    ref = O.mult_matrix(p32.astype(np.float64), th)
+    assert rel_err(out, ref) < TOL[mode]
+
+
+def test_mult_matrix_tc_chunks_match():
+    """Point chunks of the tensor-core product give the same bits as one pass."""
+    grid, nf = (24, 24, 20), 260
+    ll = tuple(x * 0.35 for x in grid)
+    psi, _, _ = synth.gaussian_orbitals(grid, ll, nf, 12)
+    p = _dev(psi, np.float32)
+    th = _dev(_theta(nf, 12))
+    ctx = capi.Context(grid, ll)
+    one = ctx.mult_matrix(p, th, mode=capi.GEMM_BF16X3)
+    os.environ["MGX_PSI_THETA_CHUNK"] = "1000"   # 8 tiles of 128 points per chunk
+    try:
+        many = ctx.mult_matrix(p, th, mode=capi.GEMM_BF16X3)
+    finally:
+        del os.environ["MGX_PSI_THETA_CHUNK"]
+    assert torch.equal(one, many)
+
+
+@pytest.mark.parametrize("apply_B", [1, 0])
+@pytest.mark.parametrize("grid,nf", [((16, 16, 16), 8), ((15, 13, 11), 70)])
+def test_residual_fp64(apply_B, grid, nf):
+    ll = tuple(x * 0.35 for x in grid)
+    psi, _, _ = synth.gaussian_orbitals(grid, ll, nf, 21)
+    V = synth.gaussian_wells(grid, ll, 5, 21)
+    hp = O.hpsi(grid, ll, 0, psi, V)
+    th = _theta(nf, 21)
+    ref = O.residual(grid, ll, psi, hp, th, apply_B)
+    ctx = capi.Context(grid, ll)
+    res = ctx.residual(_dev(psi), _dev(hp), _dev(th), apply_B=apply_B).cpu().numpy()
+    assert rel_err(res, ref) < TOL_F64
+    # in place on hpsi, with a caller work block
+    hd = _dev(hp)
+    work = torch.empty_like(hd)
+    ctx.residual(_dev(psi), hd, _dev(th), apply_B=apply_B, work=work, out=hd)
+    assert rel_err(hd.cpu().numpy(), ref) < TOL_F64
+
+
+@pytest.mark.parametrize("mode", [capi.GEMM_FP64, capi.GEMM_FP32, capi.GEMM_BF16X3])
+def test_residual_fp32(mode):
+    grid, nf = (16, 16, 16), 130
+    ll = tuple(x * 0.35 for x in grid)
+    psi, _, _ = synth.gaussian_orbitals(grid, ll, nf, 22)
+    V = synth.gaussian_wells(grid, ll, 5, 22)
+    p32 = psi.astype(np.float32)
+    hp = O.hpsi(grid, ll, 0, p32, V).astype(np.float32)
+    th = _theta(nf, 22)
+    ref = O.residual(grid, ll, p32.astype(np.float64), hp.astype(np.float64), th, 1)
+    ctx = capi.Context(grid, ll)
+    res = ctx.residual(_dev(p32, np.float32), _dev(hp, np.float32), _dev(th), mode=mode).cpu().numpy()
+    scale = max(np.max(np.abs(ref)), np.max(np.abs(hp)))
+    err = np.max(np.abs(res - ref)) / scale
+    assert err < (3e-7 if mode == capi.GEMM_FP64 else TOL[mode])
+
+
+def test_residual_rejects_aliases():
+    grid, nf = (8, 8, 8), 3
+    ctx = capi.Context(grid, (2.8, 2.8, 2.8))
+    a = torch.zeros((nf, 512), dtype=torch.float64, device="cuda")
+    b = torch.zeros_like(a)
+    th = torch.eye(nf, dtype=torch.float64, device="cuda")
+    with pytest.raises(capi.MgxError):
+        ctx.residual(a, b, th, out=a)
+    with pytest.raises(capi.MgxError):
+        ctx.residual(a, b, th, work=b)
+    with pytest.raises(capi.MgxError):
+        ctx.mult_matrix(a, th, mode=capi.GEMM_BF16X3)   # needs FP32 orbitals
+
+
+def test_abpg_step_fp64_matches_oracle_chain():
+    """One full sweep (H psi, S/H, Cholesky, inverse, theta, residual,
+    V-cycle, update) in FP64 against the same chain of oracle calls."""
+    from mgmol_gb300.sweep import OrbitalSweep
+    grid, nf = (16, 16, 16), 12
+    ll = tuple(x * 0.35 for x in grid)
+    psi, _, _ = synth.gaussian_orbitals(grid, ll, nf, 41, sigma=(0.9, 1.3))
+    V = synth.gaussian_wells(grid, ll, 4, 41)
+    ctx = capi.Context(grid, ll)
+    sw = OrbitalSweep(ctx, torch.from_numpy(V), nf, mode="plain", maxlevels=2)
+    pd = _dev(psi)
+    e = float(sw.run(pd).cpu()[0])
+    vel = ctx.vel
+    hp = O.hpsi(grid, ll, 0, psi, V)
+    S = O.gram(psi, vel)
+    H = O.hmat(psi, hp, vel)
+    info, L = O.potrf(S)
+    assert info == 0
+    Sinv = O.inverse_from_chol(L)
+    assert abs(e - O.trace_prod(H, Sinv)) < 1e-11 * abs(e)
+    th = O.theta(Sinv, H)
+    res = O.residual(grid, ll, psi, hp, th, 1)
+    corr = O.precond(grid, ll, 0, 2, sw.gamma, res)
+    assert rel_err(sw.hpsi.cpu().numpy(), res) < TOL_F64
+    assert rel_err(sw.corr.cpu().numpy(), corr) < TOL_F64
+    ref = psi + sw.alpha * corr
+    assert rel_err(pd.cpu().numpy(), ref) < TOL_F64
