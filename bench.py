@@ -35,6 +35,8 @@ CONFIGS = {
                    workload="profiling slice: 256 orbitals on the 192^3 grid, h=0.25, Mehrstellen, FP32"),
     "c5_32": dict(n=(192, 192, 192), h=0.25, nfunc=32, wells=64, seed=1005,
                   workload="profiling slice: 32 orbitals on the 192^3 grid, h=0.25, Mehrstellen, FP32"),
+    "medium": dict(n=(64, 64, 64), h=0.25, nfunc=512, wells=16, seed=8,
+                   workload="medium sweep: 512 orbitals, 64^3, Mehrstellen, FP32 (profiling case)"),
     "small": dict(n=(64, 64, 64), h=0.25, nfunc=256, wells=16, seed=7,
                   workload="small sweep: 256 orbitals, 64^3, Mehrstellen, FP32"),
 }
@@ -137,9 +139,9 @@ def cpu_sweep_estimate(cfg, sample_funcs=4):
     th = np.eye(sample_funcs)
     O.residual(n, ll, psi, hp.astype(np.float32), th, 1)
     t2b = time.perf_counter()
-    # S, H and Psi Theta on a 64-orbital x 2^17-point slab: time per
+    # S, H and Psi Theta on a 128-orbital x 2^19-point slab: time per
     # (pair, point) of each product
-    ns, ks = 64, min(1 << 17, n[0] * n[1] * n[2])
+    ns, ks = 128, min(1 << 19, n[0] * n[1] * n[2])
     rng = np.random.default_rng(0)
     slab = rng.standard_normal((ns, ks)).astype(np.float32)
     t3 = time.perf_counter()
@@ -162,7 +164,7 @@ def cpu_sweep_estimate(cfg, sample_funcs=4):
         "sample": (f"oracle port of the reference loops (FP32 data, FP64 accumulation as the "
                    f"USE_MP build), {cores} threads: H psi, V-cycle and the residual stencil on "
                    f"{sample_funcs} of {N} orbitals ({n[0]}^3), scaled by N; S, H and Psi Theta "
-                   f"timed on a 64-orbital x {ks}-point slab, scaled by pairs x points; sample "
+                   f"timed on a {ns}-orbital x {ks}-point slab, scaled by pairs x points; sample "
                    f"took {t4 - t0:.1f} s"),
         "seconds_per_sweep": per_sweep,
     }
@@ -193,29 +195,11 @@ def run_reference(args, cfg):
 
 
 # --------------------------------------------------------------------- GPU leg
-def vcycle_bytes(N, npts, s, maxlevels):
-    """Minimal HBM bytes of one V-cycle application on N functions of npts
-    points (element size s), following the kernel schedule: level 0 -- first
-    sweep from f (read f, write v), second pre-sweep (read v, f; write v, w),
-    restriction (read w, write the coarse rhs), prolongation-correction (read
-    coarse, read and write v), two post-sweeps (read v, f; write v); coarse
-    levels add a zero fill of v and 4 sweeps on the coarsest grid."""
-    total = 0.0
-    for l in range(maxlevels + 1):
-        P = N * npts / 8 ** l
-        if l == maxlevels:
-            total += P * s * (1 + 4 * 3)
-            continue
-        first = 2 if l == 0 else 1 + 3       # level 0 starts from f; others zero-fill
-        total += P * s * (first + 4 + 1.125 + 2.125 + 2 * 3)
-    return total
-
-
 def run_gpu(args, cfg):
     import torch
     import torch.distributed as dist
     from mgmol_gb300 import capi, synth
-    from mgmol_gb300.sweep import OrbitalSweep
+    from mgmol_gb300.sweep import OrbitalSweep, vcycle_bytes
 
     world = _env_int("WORLD_SIZE", 1)
     rank = _env_int("RANK", 0)
@@ -236,7 +220,15 @@ def run_gpu(args, cfg):
     # replicas only: every rank runs the same workload on its own GPU
     psi, _, _ = synth.gaussian_orbitals_device(n, ll, N, cfg["seed"] + rank, dt)
     V = synth.gaussian_wells_device(n, ll, cfg["wells"], cfg["seed"])
-    sw = OrbitalSweep(ctx, V, N, mode=mode, gemm=gemm, precond_chunk=args.chunk)
+    lean = args.lean
+    if lean < 0:
+        # three full blocks plus the GEMM workspace must fit, else walk the
+        # residual / preconditioner in chunks of 128 functions
+        free, _ = torch.cuda.mem_get_info()
+        block = N * ctx.npts * (8 if mode == "plain" else 4)
+        lean = 0 if 3.6 * block < free else 128
+    sw = OrbitalSweep(ctx, V, N, mode=mode, gemm=gemm, precond_chunk=args.chunk,
+                      chunk_funcs=lean)
     torch.cuda.synchronize()
 
     for _ in range(args.warmup):
@@ -334,6 +326,7 @@ def run_gpu(args, cfg):
         "config": {"workload": cfg["workload"], "grid": list(n), "h": cfg["h"], "orbitals": N,
                    "mode": mode, "gemm": args.gemm if mode == "mixed" else "fp64",
                    "lap_type": "mehrstellen", "precond": "V-cycle 2 coarse levels",
+                   "schedule": f"column chunks of {sw.chunk}" if sw.chunk else "full blocks",
                    "l2": "inputs larger than L2 (no flush)", "parallelism": f"replicas x{world}"},
         "phases_ms": phases, "phase_share": shares, "energy_trace_ry": energy,
         "roofline": roof, "gpu_launches": launches, "clocks": clocks.summary(),
@@ -357,7 +350,10 @@ def main():
     ap.add_argument("--mode", default="mixed", choices=["mixed", "plain"])
     ap.add_argument("--gemm", default="bf16x3", choices=["fp32", "tf32", "bf16x3"])
     ap.add_argument("--chunk", type=int, default=0, help="V-cycle orbital chunk (0 = auto)")
-    ap.add_argument("--cpu-sample", type=int, default=4)
+    ap.add_argument("--lean", type=int, default=-1,
+                    help="residual / preconditioner column chunk (0 = full blocks, -1 = auto)")
+    ap.add_argument("--cpu-sample", type=int, default=32,
+                    help="orbitals of the timed CPU sample of the linear phases")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", dest="e2e", action="store_false")
     args = ap.parse_args()

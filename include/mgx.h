@@ -1,8 +1,9 @@
 /*
  * mgx.h -- C ABI of the GB300 (sm_103a) implementation of MGmol's orbital
  * hot path: the local Hamiltonian on a block of orbitals, the block
- * multigrid V-cycle used as orbital preconditioner, localization masks, and
- * the Gram / H-matrix contractions with FP64 Cholesky, inverse and trace.
+ * multigrid V-cycle used as orbital preconditioner, localization masks, the
+ * Gram / H-matrix contractions with FP64 Cholesky, inverse and trace, the
+ * residual and update of one ABPG step, and the pb::Mgm Poisson solver.
  *
  * Conventions
  *  - Every call returns an mgx_status; mgx_last_error_string() gives the
@@ -260,7 +261,8 @@ int mgx_cholesky(mgx_ctx* ctx, int n, double* A, int* info, void* stream);
 int mgx_inverse_from_cholesky(mgx_ctx* ctx, int n, const double* L,
     double* Sinv, void* stream);
 /* ProjectedMatrices::getEigSum (src/ProjectedMatrices.cc:550-566):
- * *trace (device) = tr(H Sinv), H taken symmetric from its lower part. */
+ * *trace (device) = tr(H Sinv), H and Sinv taken symmetric from their lower
+ * parts. */
 int mgx_trace_prod(mgx_ctx* ctx, int n, const double* H, const double* Sinv,
     double* trace, void* stream);
 
@@ -291,6 +293,17 @@ int mgx_mult_matrix(mgx_ctx* ctx, int mode, mgx_dtype dtype, const void* psi,
  * mgx_mult_matrix. */
 int mgx_residual(mgx_ctx* ctx, int mode, mgx_dtype dtype, const void* psi,
     const void* hpsi, size_t ld, int nfunc, const double* theta, int apply_B,
+    void* work, void* res, void* stream);
+
+/* mgx_residual for the output functions j0 .. j0+ncols-1 only: theta points
+ * at column j0 of the nfunc x nfunc matrix (theta + j0 * nfunc), hpsi and
+ * res at function j0 of their blocks, work (or the ctx block) holds ncols
+ * functions.  Lets a caller bound the memory of the residual and of the
+ * preconditioner that follows by walking the block in column chunks.  This
+ * entry point has no counterpart in the reference, which always forms the
+ * whole block. */
+int mgx_residual_cols(mgx_ctx* ctx, int mode, mgx_dtype dtype, const void* psi,
+    const void* hpsi, size_t ld, int nfunc, const double* theta, int ncols, int apply_B,
     void* work, void* res, void* stream);
 
 /* ---------------------------------------------------------------- */

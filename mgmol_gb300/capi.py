@@ -103,6 +103,7 @@ _SIGS = {
     "mgx_theta": [_vp, _i, _vp, _vp, _vp, _vp],
     "mgx_mult_matrix": [_vp, _i, _i, _vp, _sz, _i, _vp, _vp, _vp],
     "mgx_residual": [_vp, _i, _i, _vp, _vp, _sz, _i, _vp, _i, _vp, _vp, _vp],
+    "mgx_residual_cols": [_vp, _i, _i, _vp, _vp, _sz, _i, _vp, _i, _i, _vp, _vp, _vp],
     "mgx_mgm": [_vp, ctypes.POINTER(MgmParams), _i, _vp, _vp, ctypes.POINTER(MgmResult), _vp],
 }
 
@@ -318,6 +319,21 @@ class Context:
         Sc = Sinv.T.contiguous()
         out = torch.empty(1, dtype=torch.float64, device=H.device)
         _check(load().mgx_trace_prod(self.handle, n, _ptr(Hc), _ptr(Sc), _ptr(out), _stream(stream)))
+        return out
+
+    def residual_cols(self, psi, hpsi, theta_cols, mode=GEMM_FP64, apply_B=True, work=None,
+                      out=None, stream=None):
+        """Residual of ncols output functions: theta_cols is the column-major
+        (ncols, nfunc) slice theta[:, j0:j0+ncols].T (contiguous), hpsi and out
+        (ncols, npts) views of the chunk; out may be hpsi."""
+        p, ld, nf = _block(psi, self.npts)
+        ph, ldh, nc = _block(hpsi, self.npts)
+        if theta_cols.shape != (nc, nf) or not theta_cols.is_contiguous():
+            raise ValueError("theta_cols must be a contiguous (ncols, nfunc) tensor")
+        out = torch.empty_like(hpsi) if out is None else out
+        _check(load().mgx_residual_cols(self.handle, mode, _dtype(psi), p, ph, ld, nf,
+                                        _ptr(theta_cols), nc, 1 if apply_B else 0, _ptr(work),
+                                        _ptr(out), _stream(stream)))
         return out
 
     # ------------------------------------------------------------ Poisson

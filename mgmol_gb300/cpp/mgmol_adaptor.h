@@ -367,6 +367,21 @@ public:
         check(mgx_hmat(ctx_, mode, psi_.data(), other.psi(0), numpt(), nfunc_, H.data(), nullptr),
             "LocGridOrbitals::computeLocalProduct");
     }
+    /* LocGridOrbitals::multiplyByMatrix(matrix, product): product_j =
+     * sum_i psi_i theta(i, j), theta FP64 column-major on the device */
+    void multiplyByMatrix(const DeviceArray<double>& theta, OrbitalBlock& product, int mode = -1) const
+    {
+        if (mode < 0) mode = MGX_GEMM_FP64;
+        check(mgx_mult_matrix(ctx_, mode, dtype_of<T>(), psi_.data(), numpt(), nfunc_,
+                  theta.data(), product.psi(0), nullptr),
+            "LocGridOrbitals::multiplyByMatrix");
+    }
+    /* LocGridOrbitals::axpy: psi += alpha x */
+    void axpy(double alpha, const OrbitalBlock& x)
+    {
+        check(mgx_axpy(psi_.size(), alpha, dtype_of<T>(), x.psi(0), psi_.data(), nullptr),
+            "LocGridOrbitals::axpy");
+    }
 };
 
 /* Hamiltonian<T>::applyLocal: hphi = -Lap_M phi + B(V phi) (Mehrstellen)
@@ -421,6 +436,18 @@ public:
     }
 };
 
+/* MGmol::computeResidualUsingHPhi: res = B(psi) theta - hphi (applyB) or
+ * psi theta - hphi; res may be hphi itself */
+template <typename T>
+void computeResidualUsingHPhi(const OrbitalBlock<T>& psi, const OrbitalBlock<T>& hphi,
+    const DeviceArray<double>& theta, OrbitalBlock<T>& res, bool applyB, int mode = -1)
+{
+    if (mode < 0) mode = MGX_GEMM_FP64;
+    check(mgx_residual(psi.ctx(), mode, dtype_of<T>(), psi.psi(0), hphi.psi(0), psi.numpt(),
+              psi.chromatic_number(), theta.data(), applyB ? 1 : 0, nullptr, res.psi(0), nullptr),
+        "MGmol::computeResidualUsingHPhi");
+}
+
 /* GramMatrix: Cholesky factor, inverse and the energy trace, FP64 device */
 class GramMatrix
 {
@@ -442,6 +469,12 @@ public:
             "GramMatrix::computeInverse");
     }
     const DeviceArray<double>& getInverse() const { return inv_; }
+    /* ProjectedMatrices::updateTheta: theta = S^-1 H (FP64 column-major) */
+    void updateTheta(const DeviceArray<double>& H, DeviceArray<double>& theta) const
+    {
+        check(mgx_theta(ctx_, n_, inv_.data(), H.data(), theta.data(), nullptr),
+            "ProjectedMatrices::updateTheta");
+    }
     const DeviceArray<double>& getCholeskyL() const { return ls_; }
     /* ProjectedMatrices::getEigSum: tr(H S^-1) in Ry */
     double traceProduct(const DeviceArray<double>& H) const
@@ -453,5 +486,32 @@ public:
         return v;
     }
 };
+
+namespace pb
+{
+/* pb::Mgm(A, vh, rho, cogr, max_sweeps, tol, nu1, nu2, gather_coarse_level,
+ * final_residual, final_relative_residual, residual_reduction, nb_sweeps)
+ * (src/pb/Mgm.h:20-26) on one device field of the grid; A is one of the
+ * Laph* operators above.  Returns whether the solve converged. */
+template <typename T, class Op>
+bool Mgm(const Op& A, const Grid& grid, T* vh, const T* rho, short cogr, short max_sweeps,
+    double tol, short nu1, short nu2, bool /*gather_coarse_level*/, double& final_residual,
+    double& final_relative_residual, double& residual_reduction, short& nb_sweeps,
+    int ghosts = 0)
+{
+    mgx_ctx* ctx = nullptr;
+    check(mgx_create(&grid.raw(), &ctx), "mgx_create");
+    mgx_mgm_params p{ A.type(), cogr, max_sweeps, tol, nu1, nu2, ghosts };
+    mgx_mgm_result r{};
+    const int st = mgx_mgm(ctx, &p, dtype_of<T>(), vh, rho, &r, nullptr);
+    mgx_destroy(ctx);
+    check(st, "pb::Mgm");
+    final_residual          = r.final_residual;
+    final_relative_residual = r.final_relative_residual;
+    residual_reduction      = r.residual_reduction;
+    nb_sweeps               = (short)r.nb_sweeps;
+    return r.converged != 0;
+}
+} // namespace pb
 
 } // namespace mgx

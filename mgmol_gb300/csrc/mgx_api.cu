@@ -78,10 +78,10 @@ int masks_apply(mgx_ctx*, const mgx_masks*, int, void*, size_t, int, cudaStream_
 int masks_expand(const mgx_masks*, int, void*, int*, cudaStream_t);
 int gram_cuda_cores(mgx_ctx*, int, const void*, const void*, size_t, size_t,
     int, double, int, double*, cudaStream_t);
-int psi_theta_cuda_cores(int, const void*, size_t, size_t, int, const double*,
+int psi_theta_cuda_cores(int, const void*, size_t, size_t, int, const double*, int, int,
     double, const void*, void*, cudaStream_t);
 int psi_theta_tcgen05(mgx_ctx*, int, const float*, size_t, size_t, int,
-    const double*, float, const float*, float*, cudaStream_t);
+    const double*, int, int, float, const float*, float*, cudaStream_t);
 int theta_product(int, const double*, const double*, double*, cudaStream_t);
 int mgm_solve(mgx_ctx*, const mgx_mgm_params*, int, void*, const void*, mgx_mgm_result*,
     cudaStream_t);
@@ -91,7 +91,7 @@ int gram_hmat_tcgen05(mgx_ctx*, int, const void*, const void*, size_t, size_t, i
     double, double*, double*, cudaStream_t);
 int cholesky(mgx_ctx*, int, double*, int*, cudaStream_t);
 int inverse_from_cholesky(mgx_ctx*, int, const double*, double*, cudaStream_t);
-int trace_prod(int, const double*, const double*, double*, cudaStream_t);
+int trace_prod(mgx_ctx*, int, const double*, const double*, double*, cudaStream_t);
 
 static int check_grid(const mgx_grid* g)
 {
@@ -550,7 +550,7 @@ int mgx_trace_prod(mgx_ctx* ctx, int n, const double* H, const double* Sinv,
     double* trace, void* stream)
 {
     if (!ctx) return fail(MGX_BAD_ARG, "ctx is NULL");
-    return trace_prod(n, H, Sinv, trace, (cudaStream_t)stream);
+    return trace_prod(ctx, n, H, Sinv, trace, (cudaStream_t)stream);
 }
 
 int mgx_theta(mgx_ctx* ctx, int n, const double* Sinv, const double* H,
@@ -564,31 +564,68 @@ int mgx_theta(mgx_ctx* ctx, int n, const double* Sinv, const double* H,
 
 namespace mgx
 {
-/* out = psi theta + beta cin (cin may alias out, out may not alias psi) */
+/* out_j = sum_i psi_i theta(i, j) + beta cin_j for the ncols columns of
+ * theta at theta + j * nfunc (cin may alias out, out may not alias psi) */
 static int mult_matrix(mgx_ctx* ctx, int mode, mgx_dtype dtype, const void* psi,
-    size_t ld, int nfunc, const double* theta, double beta, const void* cin,
+    size_t ld, int nfunc, const double* theta, int ncols, double beta, const void* cin,
     void* out, cudaStream_t s)
 {
     const size_t npts = make_level(ctx->grid, 0).npts();
-    const size_t ldv  = nfunc > 1 ? ld : npts;
+    const size_t ldv  = (nfunc > 1 || ncols > 1) ? ld : npts;
     switch (mode)
     {
         case MGX_GEMM_FP64:
             // FP64 accumulation for either orbital type, as MPgemmNN does
             return psi_theta_cuda_cores(dtype == MGX_F64 ? 0 : 1, psi, ldv, npts, nfunc,
-                theta, beta, cin, out, s);
+                theta, nfunc, ncols, beta, cin, out, s);
         case MGX_GEMM_FP32:
         case MGX_GEMM_TF32:
         case MGX_GEMM_BF16X3:
             if (dtype != MGX_F32)
                 return fail(MGX_BAD_ARG, "gemm mode %d needs FP32 orbitals", mode);
             if (mode == MGX_GEMM_FP32)
-                return psi_theta_cuda_cores(2, psi, ldv, npts, nfunc, theta, beta, cin, out,
-                    s);
+                return psi_theta_cuda_cores(2, psi, ldv, npts, nfunc, theta, nfunc, ncols, beta,
+                    cin, out, s);
             return psi_theta_tcgen05(ctx, mode, (const float*)psi, ldv, npts, nfunc, theta,
-                (float)beta, (const float*)cin, (float*)out, s);
+                nfunc, ncols, (float)beta, (const float*)cin, (float*)out, s);
     }
     return fail(MGX_BAD_ARG, "gemm mode %d", mode);
+}
+
+/* res_j = B(sum_i psi_i theta(i, j)) - hpsi_j (apply_B) or without B, for
+ * the ncols columns of theta given; hpsi, work and res hold ncols
+ * functions */
+static int residual_cols(mgx_ctx* ctx, int mode, mgx_dtype dtype, const void* psi,
+    const void* hpsi, size_t ld, int nfunc, const double* theta, int ncols, int apply_B,
+    void* work, void* res, cudaStream_t s)
+{
+    if (ncols == 0 || nfunc == 0) return MGX_OK;
+    if (!theta) return fail(MGX_BAD_ARG, "theta is NULL");
+    if (ncols < 0 || ncols > nfunc) return fail(MGX_BAD_ARG, "ncols %d of %d", ncols, nfunc);
+    if (res == psi) return fail(MGX_BAD_ARG, "psi and res alias");
+    if (!apply_B)
+        // res = psi theta - hpsi in one pass (res may be hpsi)
+        return mult_matrix(ctx, mode, dtype, psi, ld, nfunc, theta, ncols, -1., hpsi, res, s);
+    const Level L   = make_level(ctx->grid, 0);
+    const size_t lw = (nfunc > 1 || ncols > 1) ? ld : L.npts();
+    if (!work)
+    {
+        MGX_TRY(ctx->resid.ensure(lw * ncols * dtype_size(dtype)));
+        work = ctx->resid.ptr;
+    }
+    if (work == psi || work == hpsi || work == res)
+        return fail(MGX_BAD_ARG, "work aliases psi, hpsi or res");
+    // B (psi theta) = (B psi) theta: the product first, then one stencil
+    // pass res = B work - hpsi
+    MGX_TRY(mult_matrix(ctx, mode, dtype, psi, ld, nfunc, theta, ncols, 0., nullptr, work, s));
+    PlaneParams p = plane(ctx->grid);
+    p.u   = work;
+    p.ldu = lw;
+    p.f   = hpsi;
+    p.ldf = lw;
+    p.out = res;
+    p.ldo = lw;
+    return stencil_launch(OP_RHS_SUB, 0, dtype, dtype, p, L, 0., ncols, s);
 }
 } // namespace mgx
 
@@ -604,7 +641,7 @@ int mgx_mult_matrix(mgx_ctx* ctx, int mode, mgx_dtype dtype, const void* psi,
     if (nfunc == 0) return MGX_OK;
     if (!theta) return fail(MGX_BAD_ARG, "theta is NULL");
     if (psi == out) return fail(MGX_BAD_ARG, "psi and out alias");
-    return mult_matrix(ctx, mode, dtype, psi, ld, nfunc, theta, 0., nullptr, out,
+    return mult_matrix(ctx, mode, dtype, psi, ld, nfunc, theta, nfunc, 0., nullptr, out,
         (cudaStream_t)stream);
 }
 
@@ -617,33 +654,23 @@ int mgx_residual(mgx_ctx* ctx, int mode, mgx_dtype dtype, const void* psi,
     MGX_TRY(check_block(ctx->grid, psi, ld, nfunc, "psi"));
     MGX_TRY(check_block(ctx->grid, hpsi, ld, nfunc, "hpsi"));
     MGX_TRY(check_block(ctx->grid, res, ld, nfunc, "res"));
-    if (nfunc == 0) return MGX_OK;
-    if (!theta) return fail(MGX_BAD_ARG, "theta is NULL");
-    if (res == psi) return fail(MGX_BAD_ARG, "psi and res alias");
-    cudaStream_t s = (cudaStream_t)stream;
-    if (!apply_B)
-        // res = psi theta - hpsi in one pass (res may be hpsi)
-        return mult_matrix(ctx, mode, dtype, psi, ld, nfunc, theta, -1., hpsi, res, s);
-    const Level L   = make_level(ctx->grid, 0);
-    const size_t lw = nfunc > 1 ? ld : L.npts();
-    if (!work)
-    {
-        MGX_TRY(ctx->resid.ensure(lw * nfunc * dtype_size(dtype)));
-        work = ctx->resid.ptr;
-    }
-    if (work == psi || work == hpsi || work == res)
-        return fail(MGX_BAD_ARG, "work aliases psi, hpsi or res");
-    // B (psi theta) = (B psi) theta: the product first, then one stencil
-    // pass res = B work - hpsi
-    MGX_TRY(mult_matrix(ctx, mode, dtype, psi, ld, nfunc, theta, 0., nullptr, work, s));
-    PlaneParams p = plane(ctx->grid);
-    p.u   = work;
-    p.ldu = lw;
-    p.f   = hpsi;
-    p.ldf = lw;
-    p.out = res;
-    p.ldo = lw;
-    return stencil_launch(OP_RHS_SUB, 0, dtype, dtype, p, L, 0., nfunc, s);
+    return residual_cols(ctx, mode, dtype, psi, hpsi, ld, nfunc, theta, nfunc, apply_B, work,
+        res, (cudaStream_t)stream);
+}
+
+int mgx_residual_cols(mgx_ctx* ctx, int mode, mgx_dtype dtype, const void* psi,
+    const void* hpsi, size_t ld, int nfunc, const double* theta, int ncols, int apply_B,
+    void* work, void* res, void* stream)
+{
+    if (!ctx) return fail(MGX_BAD_ARG, "ctx is NULL");
+    MGX_TRY(check_dtype(dtype));
+    MGX_TRY(check_block(ctx->grid, psi, ld, nfunc, "psi"));
+    MGX_TRY(check_block(ctx->grid, hpsi, ld, ncols, "hpsi"));
+    MGX_TRY(check_block(ctx->grid, res, ld, ncols, "res"));
+    if (nfunc > 1 && ncols == 1 && ld < make_level(ctx->grid, 0).npts())
+        return fail(MGX_BAD_ARG, "ld below the grid size");
+    return residual_cols(ctx, mode, dtype, psi, hpsi, ld, nfunc, theta, ncols, apply_B, work,
+        res, (cudaStream_t)stream);
 }
 
 int mgx_mgm(mgx_ctx* ctx, const mgx_mgm_params* params, mgx_dtype dtype, void* vh,

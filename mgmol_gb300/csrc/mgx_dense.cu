@@ -234,15 +234,16 @@ static int dgemm(bool ta, bool tb, int m, int n, int k, double alpha,
 /* ------------------------------------------------------------------ */
 /* orbital block times a small FP64 matrix on CUDA cores (MPgemmNN,      */
 /* src/linear_algebra/mputils.cc:719-760):                               */
-/*   out_j[p] = sum_i psi_i[p] theta(i, j) + beta cin_j[p]               */
+/*   out_j[p] = sum_i psi_i[p] theta(i, j) + beta cin_j[p], j < ncols,   */
+/*   theta column j at theta + j * ldt                                   */
 /* ACC double: FP64 accumulation as the reference does for both orbital  */
 /* types; ACC float: theta rounded to FP32 and FP32 FMA.  Tiles of 128   */
 /* points x 64 functions, 8 x 4 results per thread.  cin may alias out.  */
 /* ------------------------------------------------------------------ */
 template <typename T, typename ACC>
 __global__ void __launch_bounds__(256) psi_theta_kernel(size_t npts, int n,
-    const T* __restrict__ psi, size_t ld, const double* __restrict__ theta,
-    double beta, const T* cin, T* out)
+    const T* __restrict__ psi, size_t ld, const double* __restrict__ theta, int ldt,
+    int ncols, double beta, const T* cin, T* out)
 {
     __shared__ ACC As[16][128];
     __shared__ ACC Bs[16][65];
@@ -272,7 +273,7 @@ __global__ void __launch_bounds__(256) psi_theta_kernel(size_t npts, int n,
             const int e = tid + r * 256;
             const int kk = e % 16, jj = e / 16;
             const int i = kc + kk, j = j0 + jj;
-            Bs[kk][jj] = (i < n && j < n) ? (ACC)theta[(size_t)j * n + i] : ACC(0);
+            Bs[kk][jj] = (i < n && j < ncols) ? (ACC)theta[(size_t)j * ldt + i] : ACC(0);
         }
         __syncthreads();
 #pragma unroll
@@ -295,7 +296,7 @@ __global__ void __launch_bounds__(256) psi_theta_kernel(size_t npts, int n,
     for (int v = 0; v < 4; v++)
     {
         const int j = j0 + ty + 16 * v;
-        if (j >= n) continue;
+        if (j >= ncols) continue;
 #pragma unroll
         for (int u = 0; u < 8; u++)
         {
@@ -312,20 +313,21 @@ __global__ void __launch_bounds__(256) psi_theta_kernel(size_t npts, int n,
 /* kind 0: FP64 orbitals; 1: FP32 orbitals, FP64 accumulation; 2: FP32
  * orbitals, FP32 accumulation */
 int psi_theta_cuda_cores(int kind, const void* psi, size_t ld, size_t npts, int n,
-    const double* theta, double beta, const void* cin, void* out, cudaStream_t s)
+    const double* theta, int ldt, int ncols, double beta, const void* cin, void* out,
+    cudaStream_t s)
 {
-    if (n <= 0 || npts == 0) return MGX_OK;
-    dim3 grid((unsigned)((npts + 127) / 128), (unsigned)((n + 63) / 64));
+    if (n <= 0 || ncols <= 0 || npts == 0) return MGX_OK;
+    dim3 grid((unsigned)((npts + 127) / 128), (unsigned)((ncols + 63) / 64));
     if (grid.y > 65535) return fail(MGX_UNSUPPORTED, "too many functions");
     if (kind == 0)
         psi_theta_kernel<double, double><<<grid, 256, 0, s>>>(npts, n, (const double*)psi, ld,
-            theta, beta, (const double*)cin, (double*)out);
+            theta, ldt, ncols, beta, (const double*)cin, (double*)out);
     else if (kind == 1)
         psi_theta_kernel<float, double><<<grid, 256, 0, s>>>(npts, n, (const float*)psi, ld,
-            theta, beta, (const float*)cin, (float*)out);
+            theta, ldt, ncols, beta, (const float*)cin, (float*)out);
     else
         psi_theta_kernel<float, float><<<grid, 256, 0, s>>>(npts, n, (const float*)psi, ld,
-            theta, beta, (const float*)cin, (float*)out);
+            theta, ldt, ncols, beta, (const float*)cin, (float*)out);
     MGX_LAUNCH_CHECK("psi_theta_kernel");
     return MGX_OK;
 }
@@ -558,22 +560,44 @@ int inverse_from_cholesky(mgx_ctx* ctx, int n, const double* L, double* Sinv,
     return MGX_OK;
 }
 
-__global__ void trace_prod_kernel(const double* H, const double* Sinv, int n,
-    double* out)
+/* tr(H Sinv) with both matrices symmetric and read from their lower
+ * triangles: sum_k [H(k,k) S(k,k) + 2 sum_{i>k} H(i,k) S(i,k)], columns
+ * spread over the blocks (coalesced column reads), one partial per block,
+ * then a fixed-order sum of the partials. */
+constexpr int TRACE_BLOCKS = 256;
+
+__global__ void __launch_bounds__(256) trace_partial_kernel(const double* __restrict__ H,
+    const double* __restrict__ Sinv, int n, double* __restrict__ part)
 {
     __shared__ double red[256];
-    double acc      = 0.;
-    const size_t nn = (size_t)n * n;
-    for (size_t t = threadIdx.x; t < nn; t += blockDim.x)
+    double acc = 0.;
+    for (int k = blockIdx.x; k < n; k += gridDim.x)
     {
-        const int i = (int)(t % n), k = (int)(t / n);
-        // H used as symmetric from its lower triangle; Sinv(k, i)
-        const double h = (i >= k) ? H[(size_t)k * n + i] : H[(size_t)i * n + k];
-        acc += h * Sinv[(size_t)i * n + k];
+        const double* h = H + (size_t)k * n;
+        const double* q = Sinv + (size_t)k * n;
+        for (int i = k + threadIdx.x; i < n; i += blockDim.x)
+            acc += (i == k ? 1. : 2.) * h[i] * q[i];
     }
     red[threadIdx.x] = acc;
     __syncthreads();
-    for (int o = blockDim.x / 2; o > 0; o >>= 1)
+    for (int o = 128; o > 0; o >>= 1)
+    {
+        if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) part[blockIdx.x] = red[0];
+}
+
+__global__ void __launch_bounds__(256) trace_sum_kernel(const double* __restrict__ part, int n,
+    double* __restrict__ out)
+{
+    __shared__ double red[256];
+    double acc = 0.;
+    for (int i = threadIdx.x; i < n; i += blockDim.x)
+        acc += part[i];
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1)
     {
         if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
         __syncthreads();
@@ -581,12 +605,16 @@ __global__ void trace_prod_kernel(const double* H, const double* Sinv, int n,
     if (threadIdx.x == 0) *out = red[0];
 }
 
-int trace_prod(int n, const double* H, const double* Sinv, double* out,
+int trace_prod(mgx_ctx* ctx, int n, const double* H, const double* Sinv, double* out,
     cudaStream_t s)
 {
     if (n <= 0 || !H || !Sinv || !out) return fail(MGX_BAD_ARG, "trace: bad arguments");
-    trace_prod_kernel<<<1, 256, 0, s>>>(H, Sinv, n, out);
-    MGX_LAUNCH_CHECK("trace_prod_kernel");
+    MGX_TRY(ctx->red.ensure(TRACE_BLOCKS * sizeof(double)));
+    double* part = (double*)ctx->red.ptr;
+    trace_partial_kernel<<<TRACE_BLOCKS, 256, 0, s>>>(H, Sinv, n, part);
+    MGX_LAUNCH_CHECK("trace_partial_kernel");
+    trace_sum_kernel<<<1, 256, 0, s>>>(part, TRACE_BLOCKS, out);
+    MGX_LAUNCH_CHECK("trace_sum_kernel");
     return MGX_OK;
 }
 

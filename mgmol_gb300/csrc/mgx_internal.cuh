@@ -103,6 +103,8 @@ struct mgx_ctx
     mgx::DeviceBuffer resid;
     // Poisson multigrid levels
     mgx::DeviceBuffer mgm;
+    // partial sums of the reductions
+    mgx::DeviceBuffer red;
 };
 
 /* ---------------- PTX helpers: mbarrier + 1-D bulk copies ---------------- */

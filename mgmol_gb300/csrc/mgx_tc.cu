@@ -36,17 +36,21 @@ int gram_cuda_cores(mgx_ctx*, int, const void*, const void*, size_t, size_t,
 namespace tc
 {
 constexpr int BM      = 128;
-constexpr int ROWB    = 128; // bytes of one K slice row (one 128B swizzle atom)
 constexpr int THREADS = 192;
 
-__device__ __forceinline__ uint64_t desc_sw128(uint32_t saddr)
+// Shared-memory operand descriptor of a K-major tile whose rows are one
+// swizzle atom of SW bytes (128 or 64): stride between 8-row groups 8 * SW,
+// layout SWIZZLE_128B (2) or SWIZZLE_64B (4).
+template <int SW>
+__device__ __forceinline__ uint64_t desc_sw(uint32_t saddr)
 {
+    static_assert(SW == 128 || SW == 64, "swizzle atom");
     uint64_t d = 0;
     d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);
-    d |= (uint64_t)1 << 16;            // leading byte offset (unused, K-major swizzled)
-    d |= (uint64_t)(1024 >> 4) << 32;  // stride byte offset: 8 rows x 128 B
-    d |= (uint64_t)1 << 46;            // descriptor version for tcgen05
-    d |= (uint64_t)2 << 61;            // SWIZZLE_128B
+    d |= (uint64_t)1 << 16;                 // leading byte offset (unused, K-major swizzled)
+    d |= (uint64_t)((8 * SW) >> 4) << 32;   // stride byte offset: 8 rows x SW bytes
+    d |= (uint64_t)1 << 46;                 // descriptor version for tcgen05
+    d |= (uint64_t)(SW == 128 ? 2 : 4) << 61;
     return d;
 }
 
@@ -66,6 +70,18 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map,
         "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes "
         "[%0], [%1, {%2, %3}], [%4];" ::"r"(smem_u32(dst)),
         "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(smem_u32(bar))
+        : "memory");
+}
+
+// 3-D box of a K-blocked operand: (element within the 64-element K block,
+// row, K block)
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map,
+    int c0, int c1, int c2, uint64_t* bar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes "
+        "[%0], [%1, {%2, %3, %4}], [%5];" ::"r"(smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(smem_u32(bar))
         : "memory");
 }
 
@@ -146,25 +162,30 @@ struct Params
     float beta       = 0.f;
     int nrows        = 0;
     int ntj          = 1;
+    // the operand maps are K-blocked 3-D maps (rows of 64 K elements, one
+    // contiguous block of all rows per 64 K) instead of row-major 2-D maps
+    int blocked = 0;
 };
 
 // KIND 0: tf32 (NPROD 1); KIND 1: bf16 (NPROD 1 plain, 3 for hi/lo split).
 // STORE false: FP64 atomic accumulation of split-K partial tiles into C;
 // STORE true: one CTA per output tile over the whole K range, FP32 store.
-template <int KIND, int NPROD, int BN, int STAGES, bool STORE = false>
+// SW: bytes of K per tile row and stage (128: SWIZZLE_128B; 64: SWIZZLE_64B,
+// half the K per stage and twice the stages in the same shared memory).
+template <int KIND, int NPROD, int BN, int STAGES, bool STORE = false, int SW = 128>
 __global__ void __launch_bounds__(THREADS, 1) gram_kernel(
     const __grid_constant__ CUtensorMap mA0, const __grid_constant__ CUtensorMap mA1,
     const __grid_constant__ CUtensorMap mB0, const __grid_constant__ CUtensorMap mB1,
     Params p)
 {
     constexpr int NOP     = (NPROD == 3) ? 2 : 1;       // planes per operand
-    constexpr int A_BYTES = BM * ROWB;                  // 16 KB
-    constexpr int B_BYTES = BN * ROWB;
+    constexpr int A_BYTES = BM * SW;
+    constexpr int B_BYTES = BN * SW;
     constexpr int STAGE   = NOP * (A_BYTES + B_BYTES);
     constexpr int KSTEP   = 32;                          // bytes of K per MMA
-    constexpr int NK      = ROWB / KSTEP;                // MMAs per plane pair
+    constexpr int NK      = SW / KSTEP;                  // MMAs per plane pair
     constexpr int ELEM    = (KIND == 0) ? 4 : 2;
-    constexpr int BK      = ROWB / ELEM;                 // K elements per block
+    constexpr int BK      = SW / ELEM;                   // K elements per block
     constexpr uint32_t TMEM_COLS = BN;                   // power of two >= 32
 
     extern __shared__ unsigned char smem_raw[];
@@ -225,12 +246,26 @@ __global__ void __launch_bounds__(THREADS, 1) gram_kernel(
             unsigned char* st = smem + s * STAGE;
             mbar_arrive_expect_tx(full + s, STAGE);
             const int kc = (kb0 + it) * BK;
-            tma_load_2d(st, &mA0, kc, i0, full + s);
-            tma_load_2d(st + NOP * A_BYTES, &mB0, kc, j0, full + s);
-            if (NPROD == 3)
+            if (p.blocked)
             {
-                tma_load_2d(st + A_BYTES, &mA1, kc, i0, full + s);
-                tma_load_2d(st + NOP * A_BYTES + B_BYTES, &mB1, kc, j0, full + s);
+                const int e0 = kc % 64, kb = kc / 64;
+                tma_load_3d(st, &mA0, e0, i0, kb, full + s);
+                tma_load_3d(st + NOP * A_BYTES, &mB0, e0, j0, kb, full + s);
+                if (NPROD == 3)
+                {
+                    tma_load_3d(st + A_BYTES, &mA1, e0, i0, kb, full + s);
+                    tma_load_3d(st + NOP * A_BYTES + B_BYTES, &mB1, e0, j0, kb, full + s);
+                }
+            }
+            else
+            {
+                tma_load_2d(st, &mA0, kc, i0, full + s);
+                tma_load_2d(st + NOP * A_BYTES, &mB0, kc, j0, full + s);
+                if (NPROD == 3)
+                {
+                    tma_load_2d(st + A_BYTES, &mA1, kc, i0, full + s);
+                    tma_load_2d(st + NOP * A_BYTES + B_BYTES, &mB1, kc, j0, full + s);
+                }
             }
         }
     }
@@ -250,13 +285,13 @@ __global__ void __launch_bounds__(THREADS, 1) gram_kernel(
 #pragma unroll
             for (int kk = 0; kk < NK; kk++)
             {
-                const uint64_t ad = desc_sw128(a0 + kk * KSTEP);
-                const uint64_t bd = desc_sw128(b0 + kk * KSTEP);
+                const uint64_t ad = desc_sw<SW>(a0 + kk * KSTEP);
+                const uint64_t bd = desc_sw<SW>(b0 + kk * KSTEP);
                 mma<KIND>(tmem, ad, bd, idesc, (it > 0 || kk > 0) ? 1u : 0u);
                 if (NPROD == 3)
                 {
-                    const uint64_t bl = desc_sw128(b0 + B_BYTES + kk * KSTEP);
-                    const uint64_t al = desc_sw128(a0 + A_BYTES + kk * KSTEP);
+                    const uint64_t bl = desc_sw<SW>(b0 + B_BYTES + kk * KSTEP);
+                    const uint64_t al = desc_sw<SW>(a0 + A_BYTES + kk * KSTEP);
                     mma<KIND>(tmem, ad, bl, idesc, 1u);
                     mma<KIND>(tmem, al, bd, idesc, 1u);
                 }
@@ -354,6 +389,35 @@ __global__ void split_kernel(const float* __restrict__ x, size_t ld, int rows,
     }
 }
 
+// fp32 -> bf16 hi + lo planes in the K-blocked layout: element (r, k) at
+// ((k / 64) * rows + r) * 64 + k % 64, so that the 64-element K slice of
+// every row of a block is one contiguous run (a TMA box of 128 rows is
+// 16 KB of consecutive memory instead of 128 rows a full row stride apart).
+// K is padded with zeros to kblocks * 64.
+__global__ void split_blocked_kernel(const float* __restrict__ x, size_t ld, int rows,
+    size_t K, size_t kblocks, __nv_bfloat16* __restrict__ hi, __nv_bfloat16* __restrict__ lo)
+{
+    const size_t total = (size_t)rows * kblocks * 32; // element pairs
+    for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+         t += (size_t)gridDim.x * blockDim.x)
+    {
+        const size_t per_row = kblocks * 32;
+        const size_t r = t / per_row, k = 2 * (t - r * per_row);
+        float a = 0.f, b = 0.f;
+        if (k < K) a = x[r * ld + k];
+        if (k + 1 < K) b = x[r * ld + k + 1];
+        const __nv_bfloat16 ha = __float2bfloat16_rn(a), hb = __float2bfloat16_rn(b);
+        __nv_bfloat162 h2, l2;
+        h2.x = ha;
+        h2.y = hb;
+        l2.x = __float2bfloat16_rn(a - __bfloat162float(ha));
+        l2.y = __float2bfloat16_rn(b - __bfloat162float(hb));
+        const size_t o = ((k / 64) * rows + r) * 64 + (k % 64);
+        *reinterpret_cast<__nv_bfloat162*>(hi + o) = h2;
+        *reinterpret_cast<__nv_bfloat162*>(lo + o) = l2;
+    }
+}
+
 // Points-major operand of the points x functions product: columns
 // [p0, p0 + P) of the orbital block x (n functions, leading dimension ld)
 // become rows of K = function values, row p at p * ldo.  BF16 writes the
@@ -400,19 +464,20 @@ __global__ void __launch_bounds__(256) transpose_split_kernel(const float* __res
     }
 }
 
-// FP64 matrix theta (n x n, column-major) -> function-major operand rows
-// j = column j of theta, K = i, leading dimension ldo: bf16 hi / lo planes
-// (hi = bf16(x), lo = bf16(x - hi)) or one FP32 plane; zero padded.
+// FP64 matrix theta (n rows, ncols columns, column j at th + j * ldt) ->
+// function-major operand rows j = column j of theta, K = i, leading
+// dimension ldo: bf16 hi / lo planes (hi = bf16(x), lo = bf16(x - hi)) or
+// one FP32 plane; zero padded.
 template <bool BF16>
-__global__ void matrix_split_kernel(const double* __restrict__ th, int n, void* hi,
-    void* lo, size_t ldo)
+__global__ void matrix_split_kernel(const double* __restrict__ th, int n, int ldt,
+    int ncols, void* hi, void* lo, size_t ldo)
 {
-    const size_t total = (size_t)n * ldo;
+    const size_t total = (size_t)ncols * ldo;
     for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < total;
          t += (size_t)gridDim.x * blockDim.x)
     {
         const size_t j = t / ldo, i = t - j * ldo;
-        const double x = (i < (size_t)n) ? th[j * n + i] : 0.;
+        const double x = (i < (size_t)n) ? th[j * ldt + i] : 0.;
         if (BF16)
         {
             const __nv_bfloat16 h = __float2bfloat16_rn((float)x);
@@ -441,9 +506,10 @@ static PFN_cuTensorMapEncodeTiled_v12000 encoder()
 }
 
 // 2-D map over a row-major (rows x K) array with leading dimension ld
-// (elements); box = 128-byte K slice x box_rows rows, SWIZZLE_128B.
+// (elements); box = sw-byte K slice x box_rows rows, SWIZZLE_128B (sw 128)
+// or SWIZZLE_64B (sw 64).
 static int make_map(CUtensorMap* m, const void* base, bool bf16, size_t K,
-    size_t rows, size_t ld, int box_rows)
+    size_t rows, size_t ld, int box_rows, int sw = 128)
 {
     auto enc = encoder();
     if (!enc) return fail(MGX_CUDA_ERROR, "cuTensorMapEncodeTiled unavailable");
@@ -452,24 +518,45 @@ static int make_map(CUtensorMap* m, const void* base, bool bf16, size_t K,
         return fail(MGX_BAD_ARG, "tensor-core operands need 16-byte aligned rows");
     cuuint64_t dims[2]    = { (cuuint64_t)K, (cuuint64_t)rows };
     cuuint64_t strides[1] = { (cuuint64_t)(ld * esz) };
-    cuuint32_t box[2]     = { (cuuint32_t)(ROWB / esz), (cuuint32_t)box_rows };
+    cuuint32_t box[2]     = { (cuuint32_t)(sw / esz), (cuuint32_t)box_rows };
     cuuint32_t estr[2]    = { 1, 1 };
     CUresult r = enc(m, bf16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32,
         2, const_cast<void*>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
-        CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+        sw == 128 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B,
+        CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) return fail(MGX_CUDA_ERROR, "cuTensorMapEncodeTiled failed (%d)", (int)r);
     return MGX_OK;
 }
 
-template <int KIND, int NPROD, int BN, int STAGES, bool STORE = false>
+// 3-D map over a K-blocked bf16 operand (rows x kblocks * 64): dims
+// (64, rows, kblocks), box (sw / 2, box_rows, 1), SWIZZLE_128B / _64B.
+static int make_map_blocked(CUtensorMap* m, const void* base, size_t rows, size_t kblocks,
+    int box_rows, int sw = 128)
+{
+    auto enc = encoder();
+    if (!enc) return fail(MGX_CUDA_ERROR, "cuTensorMapEncodeTiled unavailable");
+    if ((uintptr_t)base % 16) return fail(MGX_BAD_ARG, "tensor-core operands need 16-byte alignment");
+    cuuint64_t dims[3]    = { 64, (cuuint64_t)rows, (cuuint64_t)kblocks };
+    cuuint64_t strides[2] = { 128, (cuuint64_t)(rows * 128) };
+    cuuint32_t box[3]     = { (cuuint32_t)(sw / 2), (cuuint32_t)box_rows, 1 };
+    cuuint32_t estr[3]    = { 1, 1, 1 };
+    CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<void*>(base), dims,
+        strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+        sw == 128 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B,
+        CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return fail(MGX_CUDA_ERROR, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+    return MGX_OK;
+}
+
+template <int KIND, int NPROD, int BN, int STAGES, bool STORE = false, int SW = 128>
 static int launch(const CUtensorMap& a0, const CUtensorMap& a1, const CUtensorMap& b0,
     const CUtensorMap& b1, const Params& p, int ntiles, int ksplit, cudaStream_t s)
 {
     constexpr int NOP   = (NPROD == 3) ? 2 : 1;
-    constexpr int STAGE = NOP * (BM * ROWB + BN * ROWB);
+    constexpr int STAGE = NOP * (BM * SW + BN * SW);
     const size_t smem   = (size_t)STAGES * STAGE + (2 * STAGES + 1) * 8 + 16 + 1024;
-    auto kern           = gram_kernel<KIND, NPROD, BN, STAGES, STORE>;
+    auto kern           = gram_kernel<KIND, NPROD, BN, STAGES, STORE, SW>;
     MGX_TRY(cuda_check(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)smem),
         "gram_kernel smem attribute"));
@@ -505,14 +592,65 @@ struct Operand
     bool bf16         = false;
     size_t K = 0, ld = 0;
     int rows = 0;
+    int sw   = 128;
+    bool blocked = false; // K-blocked planes (bf16 only)
 };
+
+/* K bytes per tile row of the BF16X3 kernels: 128 (SWIZZLE_128B, 2 stages
+ * at 128 x 256 tiles) or 64 (SWIZZLE_64B, 4 stages); MGX_TC_SWIZZLE
+ * (64 or 128) overrides the default for tuning. */
+int bf16_swizzle()
+{
+    static int sw = 0;
+    if (!sw)
+    {
+        const char* e = getenv("MGX_TC_SWIZZLE");
+        sw            = (e && atoi(e) == 64) ? 64 : (e && atoi(e) == 128) ? 128 : 128;
+    }
+    return sw;
+}
+
+/* Extra elements (a multiple of 64) appended to every row of the BF16
+ * planes of the K-major operands; MGX_TC_LDPAD overrides the default for
+ * tuning the DRAM access pattern of the row-strided TMA boxes. */
+size_t plane_pad()
+{
+    static long pad = -1;
+    if (pad < 0)
+    {
+        const char* e = getenv("MGX_TC_LDPAD");
+        pad           = e ? std::max(0L, atol(e)) : 0;
+        pad           = (pad / 64) * 64;
+    }
+    return (size_t)pad;
+}
+
+/* BF16 planes of the K-major operands in the K-blocked layout (default) or
+ * row-major with leading dimension K (MGX_TC_BLOCKED=0, for comparison). */
+bool blocked_planes()
+{
+    static int b = -1;
+    if (b < 0)
+    {
+        const char* e = getenv("MGX_TC_BLOCKED");
+        b             = (e && atoi(e) == 0) ? 0 : 1;
+    }
+    return b == 1;
+}
 
 /* re-encodes the maps of an operand with another box height */
 int rebox(Operand& op, int box_rows)
 {
-    MGX_TRY(tc::make_map(&op.m0, op.base0, op.bf16, op.K, op.rows, op.ld, box_rows));
+    if (op.blocked)
+    {
+        const size_t kb = (op.K + 63) / 64;
+        MGX_TRY(tc::make_map_blocked(&op.m0, op.base0, op.rows, kb, box_rows, op.sw));
+        MGX_TRY(tc::make_map_blocked(&op.m1, op.base1, op.rows, kb, box_rows, op.sw));
+        return MGX_OK;
+    }
+    MGX_TRY(tc::make_map(&op.m0, op.base0, op.bf16, op.K, op.rows, op.ld, box_rows, op.sw));
     if (op.base1)
-        MGX_TRY(tc::make_map(&op.m1, op.base1, op.bf16, op.K, op.rows, op.ld, box_rows));
+        MGX_TRY(tc::make_map(&op.m1, op.base1, op.bf16, op.K, op.rows, op.ld, box_rows, op.sw));
     else
         op.m1 = op.m0;
     return MGX_OK;
@@ -549,15 +687,28 @@ int prepare(int mode, const void* X, size_t ld, size_t K, int rows, int box_rows
         op.rows  = rows;
         return MGX_OK;
     }
-    const size_t ldo   = ((K + 63) / 64) * 64;
-    const size_t plane = ldo * (size_t)rows * sizeof(__nv_bfloat16);
-    auto* hi           = (__nv_bfloat16*)ws;
-    auto* lo           = (__nv_bfloat16*)(ws + plane);
-    const int nb       = (int)std::min<size_t>((ldo / 2 * rows + 255) / 256, 1 << 20);
-    split_kernel<<<nb, 256, 0, s>>>((const float*)X, ld, rows, K, hi, lo, ldo);
-    MGX_LAUNCH_CHECK("split_kernel");
-    MGX_TRY(make_map(&op.m0, hi, true, K, rows, ldo, box_rows));
-    MGX_TRY(make_map(&op.m1, lo, true, K, rows, ldo, box_rows));
+    op.sw      = bf16_swizzle();
+    op.blocked = blocked_planes();
+    const size_t kblocks = (K + 63) / 64;
+    const size_t ldo     = op.blocked ? kblocks * 64 : kblocks * 64 + plane_pad();
+    const size_t plane   = ldo * (size_t)rows * sizeof(__nv_bfloat16);
+    auto* hi             = (__nv_bfloat16*)ws;
+    auto* lo             = (__nv_bfloat16*)(ws + plane);
+    const int nb         = (int)std::min<size_t>((ldo / 2 * rows + 255) / 256, 1 << 20);
+    if (op.blocked)
+    {
+        split_blocked_kernel<<<nb, 256, 0, s>>>((const float*)X, ld, rows, K, kblocks, hi, lo);
+        MGX_LAUNCH_CHECK("split_blocked_kernel");
+        MGX_TRY(make_map_blocked(&op.m0, hi, rows, kblocks, box_rows, op.sw));
+        MGX_TRY(make_map_blocked(&op.m1, lo, rows, kblocks, box_rows, op.sw));
+    }
+    else
+    {
+        split_kernel<<<nb, 256, 0, s>>>((const float*)X, ld, rows, K, hi, lo, ldo);
+        MGX_LAUNCH_CHECK("split_kernel");
+        MGX_TRY(make_map(&op.m0, hi, true, K, rows, ldo, box_rows, op.sw));
+        MGX_TRY(make_map(&op.m1, lo, true, K, rows, ldo, box_rows, op.sw));
+    }
     op.base0 = hi;
     op.base1 = lo;
     op.bf16  = true;
@@ -571,7 +722,7 @@ int prepare(int mode, const void* X, size_t ld, size_t K, int rows, int box_rows
 size_t operand_bytes(int mode, size_t K, int rows)
 {
     if (mode == MGX_GEMM_TF32) return ((K + 31) / 32) * 32 * (size_t)rows * 4;
-    return 2 * ((K + 63) / 64) * 64 * (size_t)rows * sizeof(__nv_bfloat16);
+    return 2 * (((K + 63) / 64) * 64 + plane_pad()) * (size_t)rows * sizeof(__nv_bfloat16);
 }
 
 /* C[0:nrows, 0:ncols] (leading dimension ldc) += A B^T over K.  Output
@@ -587,9 +738,12 @@ int run(mgx_ctx* ctx, int mode, const Operand& a, const Operand& b, int nrows, i
         for (int i = 0; i < nti; i++)
             if (!symmetric || (i * BM + BM - 1) >= j * BN) tiles.push_back(make_int2(i, j));
     const int ntiles  = (int)tiles.size();
-    const int bk      = (mode == MGX_GEMM_BF16X3) ? 64 : 32;
+    // K elements per block; a CTA covers at most 32768 K elements (the FP32
+    // accumulation bound)
+    const int bk      = (mode == MGX_GEMM_BF16X3) ? a.sw / 2 : 32;
     const int kblocks = (int)((K + bk - 1) / bk);
-    int ksplit = std::max((4 * ctx->sm_count + ntiles - 1) / ntiles, (kblocks + 511) / 512);
+    const int kbcap   = 32768 / bk;
+    int ksplit = std::max((4 * ctx->sm_count + ntiles - 1) / ntiles, (kblocks + kbcap - 1) / kbcap);
     ksplit     = std::min(ksplit, kblocks);
     const int kb_per = (kblocks + ksplit - 1) / ksplit;
     ksplit           = (kblocks + kb_per - 1) / kb_per;
@@ -610,14 +764,21 @@ int run(mgx_ctx* ctx, int mode, const Operand& a, const Operand& b, int nrows, i
     p.C          = C;
     p.err        = (int*)ctx->tc_err.ptr;
     (void)nrows;
+    if (mode == MGX_GEMM_BF16X3 && (a.sw != b.sw || a.blocked != b.blocked))
+        return fail(MGX_BAD_ARG, "operands with different layouts");
+    p.blocked = a.blocked ? 1 : 0;
     if (BN == 256)
     {
         if (mode == MGX_GEMM_TF32)
             return launch<0, 1, 256, 4>(a.m0, a.m0, b.m0, b.m0, p, ntiles, ksplit, s);
+        if (a.sw == 64)
+            return launch<1, 3, 256, 4, false, 64>(a.m0, a.m1, b.m0, b.m1, p, ntiles, ksplit, s);
         return launch<1, 3, 256, 2>(a.m0, a.m1, b.m0, b.m1, p, ntiles, ksplit, s);
     }
     if (mode == MGX_GEMM_TF32)
         return launch<0, 1, 128, 6>(a.m0, a.m0, b.m0, b.m0, p, ntiles, ksplit, s);
+    if (a.sw == 64)
+        return launch<1, 3, 128, 6, false, 64>(a.m0, a.m1, b.m0, b.m1, p, ntiles, ksplit, s);
     return launch<1, 3, 128, 3>(a.m0, a.m1, b.m0, b.m1, p, ntiles, ksplit, s);
 }
 
@@ -734,14 +895,15 @@ int gram_hmat_tcgen05(mgx_ctx* ctx, int mode, const void* psi, const void* hpsi,
     return end(ctx, s);
 }
 
-/* out_j = sum_i psi_i theta(i, j) + beta * cin_j over npts points (the
+/* out_j = sum_i psi_i theta(i, j) + beta * cin_j, j < ncols (column j of
+ * theta at theta + j * ldt), over npts points (the
  * MPgemmNN product of LocGridOrbitals::multiplyByMatrix,
  * src/LocGridOrbitals.cc:793-830) on the tensor cores.  M = points,
  * N = functions, K = functions: the points are processed in chunks whose
  * transposed operand (rows = points, K = functions) fits a bounded
  * workspace; theta is converted once.  One CTA per 128 x BN output tile. */
 int psi_theta_tcgen05(mgx_ctx* ctx, int mode, const float* psi, size_t ld, size_t npts,
-    int n, const double* theta, float beta, const float* cin, float* out,
+    int n, const double* theta, int ldt, int ncols, float beta, const float* cin, float* out,
     cudaStream_t s)
 {
     using namespace tc;
@@ -749,7 +911,7 @@ int psi_theta_tcgen05(mgx_ctx* ctx, int mode, const float* psi, size_t ld, size_
     const size_t esz      = bf ? 2 : 4;
     const int nplanes     = bf ? 2 : 1;
     const size_t ldk      = bf ? ((n + 63) / 64) * 64 : ((n + 31) / 32) * 32;
-    const size_t b_plane  = ldk * (size_t)n * esz;
+    const size_t b_plane  = ldk * (size_t)ncols * esz;
     const size_t b_bytes  = ((nplanes * b_plane + 1023) / 1024) * 1024;
     const size_t row_bytes = nplanes * ldk * esz; // one point of the A operand
     // chunk of points: at most 2 GiB of A operand, a multiple of the tile;
@@ -768,20 +930,22 @@ int psi_theta_tcgen05(mgx_ctx* ctx, int mode, const float* psi, size_t ld, size_
     void* ahi = ws + b_bytes;
     void* alo = ws + b_bytes + a_plane;
     {
-        const int nb = (int)std::min<size_t>((n * ldk + 255) / 256, 1 << 16);
+        const int nb = (int)std::min<size_t>((ncols * ldk + 255) / 256, 1 << 16);
         if (bf)
-            matrix_split_kernel<true><<<nb, 256, 0, s>>>(theta, n, bhi, blo, ldk);
+            matrix_split_kernel<true><<<nb, 256, 0, s>>>(theta, n, ldt, ncols, bhi, blo, ldk);
         else
-            matrix_split_kernel<false><<<nb, 256, 0, s>>>(theta, n, bhi, blo, ldk);
+            matrix_split_kernel<false><<<nb, 256, 0, s>>>(theta, n, ldt, ncols, bhi, blo, ldk);
         MGX_LAUNCH_CHECK("matrix_split_kernel");
     }
-    const int BN = (n > 128) ? 256 : 128;
+    const int BN = (ncols > 128) ? 256 : 128;
+    const int sw = bf ? bf16_swizzle() : 128;
     CUtensorMap mb0, mb1, ma0, ma1;
-    MGX_TRY(make_map(&mb0, bhi, bf, n, n, ldk, BN));
+    MGX_TRY(make_map(&mb0, bhi, bf, n, ncols, ldk, BN, sw));
     mb1 = mb0;
-    if (bf) MGX_TRY(make_map(&mb1, blo, true, n, n, ldk, BN));
-    const int kblocks = (int)((n + (bf ? 63 : 31)) / (bf ? 64 : 32));
-    const int ntj     = (n + BN - 1) / BN;
+    if (bf) MGX_TRY(make_map(&mb1, blo, true, n, ncols, ldk, BN, sw));
+    const int bkk     = bf ? sw / 2 : 32;
+    const int kblocks = (int)((n + bkk - 1) / bkk);
+    const int ntj     = (ncols + BN - 1) / BN;
     for (size_t p0 = 0; p0 < npts; p0 += P)
     {
         const int Pc = (int)std::min(P, npts - p0);
@@ -792,15 +956,15 @@ int psi_theta_tcgen05(mgx_ctx* ctx, int mode, const float* psi, size_t ld, size_
         else
             transpose_split_kernel<false><<<tg, 256, 0, s>>>(psi, ld, n, p0, Pc, ahi, alo, ldk);
         MGX_LAUNCH_CHECK("transpose_split_kernel");
-        MGX_TRY(make_map(&ma0, ahi, bf, n, Pc, ldk, BM));
+        MGX_TRY(make_map(&ma0, ahi, bf, n, Pc, ldk, BM, sw));
         ma1 = ma0;
-        if (bf) MGX_TRY(make_map(&ma1, alo, true, n, Pc, ldk, BM));
+        if (bf) MGX_TRY(make_map(&ma1, alo, true, n, Pc, ldk, BM, sw));
         Params p;
         p.tiles      = nullptr;
         p.kblocks    = kblocks;
         p.kb_per_cta = kblocks;
         p.n          = 0;
-        p.ncols      = n;
+        p.ncols      = ncols;
         p.symmetric  = 0;
         p.C          = nullptr;
         p.err        = (int*)ctx->tc_err.ptr;
@@ -813,14 +977,18 @@ int psi_theta_tcgen05(mgx_ctx* ctx, int mode, const float* psi, size_t ld, size_
         const int ntiles = ((Pc + BM - 1) / BM) * ntj;
         if (BN == 256)
         {
-            if (bf)
+            if (bf && sw == 64)
+                MGX_TRY((launch<1, 3, 256, 4, true, 64>(ma0, ma1, mb0, mb1, p, ntiles, 1, s)));
+            else if (bf)
                 MGX_TRY((launch<1, 3, 256, 2, true>(ma0, ma1, mb0, mb1, p, ntiles, 1, s)));
             else
                 MGX_TRY((launch<0, 1, 256, 4, true>(ma0, ma0, mb0, mb0, p, ntiles, 1, s)));
         }
         else
         {
-            if (bf)
+            if (bf && sw == 64)
+                MGX_TRY((launch<1, 3, 128, 6, true, 64>(ma0, ma1, mb0, mb1, p, ntiles, 1, s)));
+            else if (bf)
                 MGX_TRY((launch<1, 3, 128, 3, true>(ma0, ma1, mb0, mb1, p, ntiles, 1, s)));
             else
                 MGX_TRY((launch<0, 1, 128, 6, true>(ma0, ma0, mb0, mb0, p, ntiles, 1, s)));

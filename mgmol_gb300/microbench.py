@@ -1,0 +1,132 @@
+"""Per-kernel timing of the orbital hot path at a chosen shape.
+
+    python -m mgmol_gb300.microbench gram_hmat --grid 96 96 32 --nfunc 2048
+    python -m mgmol_gb300.microbench all --grid 192 192 192 --nfunc 256
+
+Each operation runs through the C ABI on device-resident synthetic inputs
+(seeded Gaussian orbitals and wells), `--warmup` untimed and `--reps` timed
+calls bracketed by CUDA events on the current stream; one JSON line per
+operation gives milliseconds per call and the achieved rate against the
+algorithmic work (flop for the products, bytes for the stencil passes).
+"""
+import argparse
+import json
+import sys
+
+import torch
+
+from . import capi, synth
+from .sweep import vcycle_bytes
+
+GEMM = {"fp64": capi.GEMM_FP64, "fp32": capi.GEMM_FP32, "tf32": capi.GEMM_TF32,
+        "bf16x3": capi.GEMM_BF16X3}
+
+
+def _time(fn, warmup, reps):
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(reps):
+        fn()
+    b.record()
+    torch.cuda.synchronize()
+    return a.elapsed_time(b) / reps
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("op", choices=["gram", "hmat", "gram_hmat", "mult", "residual", "hpsi",
+                                   "precond", "mgm", "dense", "all"])
+    ap.add_argument("--grid", type=int, nargs=3, default=[96, 96, 32])
+    ap.add_argument("--h", type=float, default=0.25)
+    ap.add_argument("--nfunc", type=int, default=2048)
+    ap.add_argument("--gemm", default="bf16x3", choices=sorted(GEMM))
+    ap.add_argument("--fp64", action="store_true", help="FP64 orbitals (GEMM mode fp64)")
+    ap.add_argument("--warmup", type=int, default=2)
+    ap.add_argument("--reps", type=int, default=5)
+    args = ap.parse_args(argv)
+
+    n = tuple(args.grid)
+    ll = tuple(x * args.h for x in n)
+    N = args.nfunc
+    dt = torch.float64 if args.fp64 else torch.float32
+    mode = capi.GEMM_FP64 if args.fp64 else GEMM[args.gemm]
+    ctx = capi.Context(n, ll)
+    npts = ctx.npts
+    s = 8 if args.fp64 else 4
+    psi, _, _ = synth.gaussian_orbitals_device(n, ll, N, 11, dt)
+    V = synth.gaussian_wells_device(n, ll, 16, 11).to(dt)
+    hpsi = ctx.hpsi(psi, V)
+    torch.cuda.synchronize()
+    ops = ["gram", "hmat", "gram_hmat", "mult", "residual", "hpsi", "precond", "dense", "mgm"] \
+        if args.op == "all" else [args.op]
+    out = []
+    for op in ops:
+        if op == "gram":
+            ms = _time(lambda: ctx.gram(psi, mode), args.warmup, args.reps)
+            work, unit = N * (N + 1) * npts, "TFLOP/s"
+        elif op == "hmat":
+            ms = _time(lambda: ctx.hmat(psi, hpsi, mode), args.warmup, args.reps)
+            work, unit = 2.0 * N * N * npts, "TFLOP/s"
+        elif op == "gram_hmat":
+            ms = _time(lambda: ctx.gram_hmat(psi, hpsi, mode), args.warmup, args.reps)
+            work, unit = N * (N + 1) * npts + 2.0 * N * N * npts, "TFLOP/s"
+        elif op in ("mult", "residual"):
+            th = (torch.eye(N, dtype=torch.float64, device="cuda")
+                  + torch.randn(N, N, dtype=torch.float64, device="cuda") / N)
+            dst = torch.empty_like(psi)
+            if op == "mult":
+                ms = _time(lambda: ctx.mult_matrix(psi, th, mode, out=dst), args.warmup, args.reps)
+            else:
+                work_blk = torch.empty_like(psi)
+                ms = _time(lambda: ctx.residual(psi, hpsi, th, mode, True, work=work_blk, out=dst),
+                           args.warmup, args.reps)
+                del work_blk
+            del dst
+            work, unit = 2.0 * N * N * npts, "TFLOP/s"
+        elif op == "hpsi":
+            dst = torch.empty_like(psi)
+            ms = _time(lambda: ctx.hpsi(psi, V, out=dst), args.warmup, args.reps)
+            del dst
+            work, unit = N * npts * 2 * s + npts * s, "GB/s"
+        elif op == "precond":
+            dst = torch.empty_like(psi)
+            gamma = ctx.gamma(capi.LAP_MEHR4, 2, float(V.max()), float(V.min()))
+            ms = _time(lambda: ctx.precond_mg(hpsi, capi.LAP_MEHR4, 2, gamma, out=dst),
+                       args.warmup, args.reps)
+            del dst
+            work, unit = vcycle_bytes(N, npts, s, 2), "GB/s"
+        elif op == "dense":
+            S, H = ctx.gram_hmat(psi, hpsi, mode)
+
+            def dense():
+                L = ctx.cholesky(S)
+                Sinv = ctx.inverse_from_cholesky(L)
+                ctx.trace_prod(H, Sinv.contiguous())
+                ctx.theta(Sinv, H)
+            ms = _time(dense, args.warmup, args.reps)
+            work, unit = (N ** 3 / 3 + 4 * N ** 3 / 3 + 2 * N ** 3), "TFLOP/s"
+        elif op == "mgm":
+            rho = V[0:npts].double() - V.double().mean()
+            vh = torch.zeros(npts, dtype=torch.float64, device="cuda")
+
+            def solve():
+                vh.zero_()
+                ctx.mgm(vh, rho, max_sweeps=10, tol=1e-10)
+            ms = _time(solve, 1, max(1, args.reps // 2))
+            work, unit = None, None
+        rate = None
+        if work is not None:
+            scale = 1e12 if unit == "TFLOP/s" else 1e9
+            rate = work / (ms * 1e-3) / scale
+        line = {"op": op, "grid": list(n), "nfunc": N, "dtype": "f64" if args.fp64 else "f32",
+                "gemm": "fp64" if args.fp64 else args.gemm, "ms": ms, "achieved": rate, "unit": unit}
+        out.append(line)
+        print(json.dumps(line), flush=True)
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -29,10 +29,40 @@ import torch
 from . import capi
 
 
+def vcycle_bytes(N, npts, s, maxlevels):
+    """Minimal HBM bytes of one V-cycle application on N functions of npts
+    points (element size s), following the kernel schedule: level 0 -- first
+    sweep from f (read f, write v), second pre-sweep (read v, f; write v, w),
+    restriction (read w, write the coarse rhs), prolongation-correction (read
+    coarse, read and write v), two post-sweeps (read v, f; write v); coarse
+    levels add a zero fill of v and 4 sweeps on the coarsest grid."""
+    total = 0.0
+    for l in range(maxlevels + 1):
+        P = N * npts / 8 ** l
+        if l == maxlevels:
+            total += P * s * (1 + 4 * 3)
+            continue
+        first = 2 if l == 0 else 1 + 3       # level 0 starts from f; others zero-fill
+        total += P * s * (first + 4 + 1.125 + 2.125 + 2 * 3)
+    return total
+
+
+
 class OrbitalSweep:
+    """One ABPG step per run() on a device block of orbitals.
+
+    chunk_funcs > 0 selects the memory-lean schedule: the residual and the
+    preconditioner walk the block in chunks of that many output functions
+    (mgx_residual_cols), each chunk's correction is parked in its slice of
+    the H psi block, and one update closes the step.  The block then needs
+    psi, H psi and two chunk buffers instead of three full blocks, which is
+    what lets the FP64 path hold 2048 orbitals on 192^3 in one GPU."""
+
+    PHASES = ("hpsi", "gram", "dense", "residual", "precond", "update")
+
     def __init__(self, ctx, V, nfunc, mode="mixed", gemm=None, lap_type=capi.LAP_MEHR4,
                  maxlevels=2, gamma=None, precond_chunk=0, precond_factor=1.0,
-                 device="cuda"):
+                 chunk_funcs=0, device="cuda"):
         self.ctx = ctx
         self.mode = mode
         self.lap_type = lap_type
@@ -42,8 +72,14 @@ class OrbitalSweep:
         self.gemm = gemm if gemm is not None else (capi.GEMM_FP64 if mode == "plain" else capi.GEMM_FP32)
         self.V = V.to(device=device, dtype=self.dtype).contiguous()
         npts = ctx.npts
+        self.chunk = int(chunk_funcs) if chunk_funcs and chunk_funcs < nfunc else 0
         self.hpsi = torch.empty((nfunc, npts), dtype=self.dtype, device=device)
-        self.corr = torch.empty((nfunc, npts), dtype=self.dtype, device=device)
+        if self.chunk:
+            self.corr = torch.empty((self.chunk, npts), dtype=self.dtype, device=device)
+            self.work = torch.empty((self.chunk, npts), dtype=self.dtype, device=device)
+        else:
+            self.corr = torch.empty((nfunc, npts), dtype=self.dtype, device=device)
+            self.work = None
         self.S = torch.empty((nfunc, nfunc), dtype=torch.float64, device=device)
         self.Hm = torch.empty((nfunc, nfunc), dtype=torch.float64, device=device)
         self.precond_chunk = precond_chunk
@@ -53,53 +89,76 @@ class OrbitalSweep:
             vmax = float(self.V.max())
             gamma = ctx.gamma(lap_type, maxlevels, vmax, float(self.V.min()))
         self.gamma = gamma
-        self.events = {}
+        self.marks = []
+        self.timed_runs = 0
 
-    def _ev(self, name):
+    def _mark(self, timed, phase=None):
+        """Closes the open phase interval and opens `phase` (None: close only)."""
+        if not timed:
+            return
         e = torch.cuda.Event(enable_timing=True)
         e.record()
-        self.events.setdefault(name, []).append(e)
+        if self.marks and self.marks[-1][2] is None:
+            self.marks[-1][2] = e
+        if phase is not None:
+            self.marks.append([phase, e, None])
 
     def run(self, psi, timed=False, update=True):
         """One sweep; psi is updated in place (unless update is False).
         Returns the device tensor holding tr(S^-1 H) (Ry)."""
         ctx = self.ctx
-        if timed:
-            self._ev("hpsi0")
+        apply_B = self.lap_type == capi.LAP_MEHR4
+        self._mark(timed, "hpsi")
         ctx.hpsi(psi, self.V, self.lap_type, True, out=self.hpsi)
-        if timed:
-            self._ev("gram0")
+        self._mark(timed, "gram")
         ctx.gram_hmat(psi, self.hpsi, self.gemm, S=self.S, H=self.Hm)
-        if timed:
-            self._ev("dense0")
+        self._mark(timed, "dense")
         L = ctx.cholesky(self.S)
         Sinv = ctx.inverse_from_cholesky(L)
         # Hm holds H column-major; the matrix calls want the row-major view
         e = ctx.trace_prod(self.Hm.T, Sinv.contiguous())
         self.theta = ctx.theta(Sinv, self.Hm.T)
+        if not self.chunk:
+            self._mark(timed, "residual")
+            ctx.residual(psi, self.hpsi, self.theta, mode=self.gemm, apply_B=apply_B,
+                         work=self.corr, out=self.hpsi)
+            self._mark(timed, "precond")
+            ctx.precond_mg(self.hpsi, self.lap_type, self.maxlevels, self.gamma,
+                           chunk=self.precond_chunk, out=self.corr)
+            self._mark(timed, "update")
+            if update:
+                capi.axpy(self.alpha, self.corr, psi)
+        else:
+            # theta.T is the column-major buffer: row j holds column j
+            thc = self.theta.T
+            for j0 in range(0, self.nfunc, self.chunk):
+                j1 = min(self.nfunc, j0 + self.chunk)
+                hc = self.hpsi[j0:j1]
+                cb = self.corr[: j1 - j0]
+                self._mark(timed, "residual")
+                ctx.residual_cols(psi, hc, thc[j0:j1], mode=self.gemm, apply_B=apply_B,
+                                  work=self.work[: j1 - j0], out=hc)
+                self._mark(timed, "precond")
+                ctx.precond_mg(hc, self.lap_type, self.maxlevels, self.gamma,
+                               chunk=self.precond_chunk, out=cb)
+                hc.copy_(cb)
+            self._mark(timed, "update")
+            if update:
+                capi.axpy(self.alpha, self.hpsi, psi)
+        self._mark(timed)
         if timed:
-            self._ev("residual0")
-        ctx.residual(psi, self.hpsi, self.theta, mode=self.gemm,
-                     apply_B=(self.lap_type == capi.LAP_MEHR4), work=self.corr, out=self.hpsi)
-        if timed:
-            self._ev("precond0")
-        ctx.precond_mg(self.hpsi, self.lap_type, self.maxlevels, self.gamma,
-                       chunk=self.precond_chunk, out=self.corr)
-        if timed:
-            self._ev("update0")
-        if update:
-            capi.axpy(self.alpha, self.corr, psi)
-        if timed:
-            self._ev("end")
+            self.timed_runs += 1
         return e
+
+    def correction(self):
+        """P(res) of the last run (the block psi was moved along)."""
+        return self.hpsi if self.chunk else self.corr
 
     def phase_ms(self):
         """Average milliseconds per phase over the timed sweeps."""
         torch.cuda.synchronize()
-        names = ["hpsi0", "gram0", "dense0", "residual0", "precond0", "update0", "end"]
-        out = {}
-        k = len(self.events.get("end", []))
-        for a, b in zip(names[:-1], names[1:]):
-            tot = sum(self.events[a][i].elapsed_time(self.events[b][i]) for i in range(k))
-            out[a[:-1]] = tot / max(k, 1)
-        return out
+        out = {p: 0.0 for p in self.PHASES}
+        for phase, a, b in self.marks:
+            out[phase] += a.elapsed_time(b)
+        k = max(self.timed_runs, 1)
+        return {p: v / k for p, v in out.items()}

@@ -3,7 +3,8 @@
 //   testLaph4 / testBatchLaph4 (tests/testLaph4.cc:7-86, testBatchLaph4.cc:7-110)
 //   testMGkernels (tests/testMGkernels.cc:8-85)
 //   testGramMatrix, single task (tests/testGramMatrix.cc:21-120)
-// plus checks of Hamiltonian::applyLocal and OrbitalsPreconditioning.
+// plus checks of Hamiltonian::applyLocal, OrbitalsPreconditioning, the
+// residual / orbital update and pb::Mgm.
 // Prints one line per check and exits non-zero on the first failure.
 #include "mgmol_adaptor.h"
 
@@ -218,6 +219,73 @@ static void test_hamiltonian_and_precond()
     std::printf("ok   Hamiltonian::applyLocal, OrbitalsPreconditioning, computeGram\n");
 }
 
+/* computeResidualUsingHPhi without B and with theta = 2 I: res = 2 phi -
+ * hphi; then pb::Mgm with Laph2 on one sine mode, whose discrete solution
+ * is rho / lambda, lambda = (2 - 2 cos(k h)) / h^2. */
+static void test_residual_and_mgm()
+{
+    const double origin[3] = { 0., 0., 0. }, ll[3] = { 6.4, 4.8, 8.0 };
+    const unsigned n[3] = { 32, 24, 40 };
+    pb::Grid grid(origin, ll, n, 1);
+    const int nf = 3;
+    OrbitalBlock<double> phi(grid, nf), hphi(grid, nf), res(grid, nf);
+    std::vector<double> u, ex, all;
+    sine_field(grid, u, ex);
+    for (int f = 0; f < nf; f++)
+        for (double x : u) all.push_back((f + 1) * x);
+    phi.set(all.data());
+    std::vector<double> hp(all.size());
+    for (size_t i = 0; i < hp.size(); i++) hp[i] = 0.25 * all[i] + 1.;
+    hphi.set(hp.data());
+    std::vector<double> th((size_t)nf * nf, 0.);
+    for (int i = 0; i < nf; i++) th[(size_t)i * nf + i] = 2.;
+    DeviceArray<double> theta(th.size());
+    theta.upload(th.data(), th.size());
+    computeResidualUsingHPhi(phi, hphi, theta, res, false);
+    std::vector<double> r(all.size());
+    res.get(r.data());
+    double err = 0.;
+    for (size_t i = 0; i < r.size(); i++) err = std::max(err, std::fabs(r[i] - (2. * all[i] - hp[i])));
+    CHECK(err < 1e-13, "residual without B: %g", err);
+    // multiplyByMatrix with the same theta doubles the block, then axpy undoes it
+    phi.multiplyByMatrix(theta, res);
+    res.axpy(-1., phi);
+    res.get(r.data());
+    err = 0.;
+    for (size_t i = 0; i < r.size(); i++) err = std::max(err, std::fabs(r[i] - all[i]));
+    CHECK(err < 1e-13, "multiplyByMatrix / axpy: %g", err);
+
+    const double kx = 2 * M_PI / ll[0], h = grid.hgrid(0);
+    const double lambda = (2. - 2. * std::cos(kx * h)) / (h * h);
+    std::vector<double> rho(grid.size()), exact(grid.size());
+    for (unsigned x = 0; x < n[0]; x++)
+        for (unsigned y = 0; y < n[1]; y++)
+            for (unsigned z = 0; z < n[2]; z++)
+            {
+                const size_t i = ((size_t)x * n[1] + y) * n[2] + z;
+                rho[i]   = std::sin(kx * x * h);
+                exact[i] = rho[i] / lambda;
+            }
+    DeviceArray<double> vh(grid.size()), drho(grid.size());
+    drho.upload(rho.data(), rho.size());
+    pb::Laph2<double> A(grid);
+    double fr = 0., frr = 0., red = 0.;
+    short nb  = 0;
+    const bool conv = pb::Mgm(A, grid, vh.data(), drho.data(), 10, 30, 1e-11, 2, 2, false, fr,
+        frr, red, nb);
+    std::vector<double> sol(grid.size());
+    vh.download(sol.data(), sol.size());
+    double e2 = 0., m2 = 0.;
+    for (size_t i = 0; i < sol.size(); i++)
+    {
+        e2 = std::max(e2, std::fabs(sol[i] - exact[i]));
+        m2 = std::max(m2, std::fabs(exact[i]));
+    }
+    CHECK(conv && frr < 1e-11 && nb > 0, "Mgm converged %d, rel %g, sweeps %d", (int)conv, frr, nb);
+    CHECK(e2 < 1e-9 * m2, "Mgm vs the discrete solution: %g", e2 / m2);
+    std::printf("ok   computeResidualUsingHPhi, multiplyByMatrix, pb::Mgm (%d V-cycles)\n", nb);
+}
+
 int main()
 {
     try
@@ -227,6 +295,7 @@ int main()
         test_mgkernels();
         test_gram_matrix();
         test_hamiltonian_and_precond();
+        test_residual_and_mgm();
     }
     catch (const std::exception& e)
     {
