@@ -274,7 +274,7 @@ def run_gpu(args, cfg):
         t0.record()
         ksteps = max(1, min(args.steps, 3))
         for _ in range(ksteps):
-            dev.copy_(host, non_blocking=True)
+            capi.copy(dev, host)   # SM-driven copy of the pinned host block
             ee = sw.run(dev)
             e_host.copy_(ee, non_blocking=True)
             s_host.copy_(sw.S, non_blocking=True)

@@ -137,6 +137,14 @@ int mgx_trade_boundaries(const mgx_grid* grid, int ghosts, mgx_dtype dtype,
 int mgx_axpy(size_t n, double alpha, mgx_dtype dtype, const void* x, void* y,
     void* stream);
 
+/* Copies `bytes` from src to dst, either of which may be device memory or
+ * pinned host memory.  When both are device-addressable and 16-byte
+ * aligned the copy is a kernel whose loads and stores run on all SMs (for
+ * host memory, through its mapped device address over the CPU-GPU link);
+ * otherwise it is one cudaMemcpyAsync.  Not a reference function: it moves
+ * orbital blocks in and out of the device for end-to-end use. */
+int mgx_copy(void* dst, const void* src, size_t bytes, void* stream);
+
 /* ---------------------------------------------------------------- */
 /* Fused path on ghost-free blocks (periodic halo handled in the tile    */
 /* loaders).                                                            */
@@ -185,6 +193,17 @@ typedef struct mgx_precond_params
 int mgx_precond_mg(mgx_ctx* ctx, const mgx_precond_params* p, mgx_dtype dtype,
     const void* res, size_t ld, void* out, int nfunc, const mgx_masks* masks,
     void* stream);
+
+/* One preconditioned ABPG update, ABPG<T>::update_states without
+ * acceleration (src/ABPG.cc:72-140): psi += alpha * V-cycle(res), with
+ * alpha = 0.5 * precond_factor.  The V-cycle is mgx_precond_mg's; its last
+ * fine-level sweep adds its result to psi instead of storing it, so the
+ * correction block is never written.  work (nfunc x ld, or NULL for a
+ * block owned by ctx) holds the fine-level iterate.  res, psi and work may
+ * not alias. */
+int mgx_precond_mg_update(mgx_ctx* ctx, const mgx_precond_params* p,
+    mgx_dtype dtype, const void* res, size_t ld, void* psi, double alpha, int nfunc,
+    const mgx_masks* masks, void* work, void* stream);
 
 /* mgx_precond_mg without any device allocation.  This entry point has no
  * counterpart in the reference; it serves callers that cannot allocate
@@ -275,6 +294,17 @@ int mgx_trace_prod(mgx_ctx* ctx, int n, const double* H, const double* Sinv,
  * its lower triangle as BLAS symm('l', 'l') does. */
 int mgx_theta(mgx_ctx* ctx, int n, const double* Sinv, const double* H,
     double* theta, void* stream);
+
+/* theta = S^-1 H straight from the Cholesky factor L of S (mgx_cholesky),
+ * by forward and back substitution with the columns of H as right-hand
+ * sides, without forming S^-1 (2 n^3 flop instead of the 4.3 n^3 of
+ * mgx_inverse_from_cholesky followed by mgx_theta).  *trace (device; NULL to
+ * skip) receives tr(theta) = tr(S^-1 H), the energy of
+ * ProjectedMatrices::getEigSum.  This combination has no single counterpart
+ * in the reference, which forms the inverse (GramMatrix::computeInverse)
+ * and multiplies (ProjectedMatrices::updateTheta). */
+int mgx_theta_from_cholesky(mgx_ctx* ctx, int n, const double* L, const double* H,
+    double* theta, double* trace, void* stream);
 
 /* LocGridOrbitals::multiplyByMatrix (src/LocGridOrbitals.cc:793-830, the
  * MPgemmNN of src/linear_algebra/mputils.cc:719-760):

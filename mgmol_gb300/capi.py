@@ -88,6 +88,8 @@ _SIGS = {
     "mgx_mg_restrict": [_vp, _i, _i, _vp, _vp, _i, _vp],
     "mgx_mg_prolong": [_vp, _i, _i, _vp, _vp, _i, _vp],
     "mgx_precond_mg": [_vp, ctypes.POINTER(PrecondParams), _i, _vp, _sz, _vp, _i, _vp, _vp],
+    "mgx_precond_mg_update": [_vp, ctypes.POINTER(PrecondParams), _i, _vp, _sz, _vp, _d, _i, _vp,
+                              _vp, _vp],
     "mgx_precond_mg_static": [_vp, ctypes.POINTER(PrecondParams), _i, _vp, _sz, _vp, _i, _vp, _vp],
     "mgx_precond_gamma": [ctypes.POINTER(Grid), _i, _i, _d, _d, _dp],
     "mgx_masks_create": [_vp, _i, _i, _dp, _dp, _i, _i, _i, _i, ctypes.POINTER(_vp), _vp],
@@ -101,6 +103,8 @@ _SIGS = {
     "mgx_inverse_from_cholesky": [_vp, _i, _vp, _vp, _vp],
     "mgx_trace_prod": [_vp, _i, _vp, _vp, _vp, _vp],
     "mgx_theta": [_vp, _i, _vp, _vp, _vp, _vp],
+    "mgx_copy": [_vp, _vp, _sz, _vp],
+    "mgx_theta_from_cholesky": [_vp, _i, _vp, _vp, _vp, _vp, _vp],
     "mgx_mult_matrix": [_vp, _i, _i, _vp, _sz, _i, _vp, _vp, _vp],
     "mgx_residual": [_vp, _i, _i, _vp, _vp, _sz, _i, _vp, _i, _vp, _vp, _vp],
     "mgx_residual_cols": [_vp, _i, _i, _vp, _vp, _sz, _i, _vp, _i, _i, _vp, _vp, _vp],
@@ -179,6 +183,16 @@ def axpy(alpha, x, y, stream=None):
         raise ValueError("axpy wants contiguous blocks of one dtype and size")
     _check(load().mgx_axpy(x.numel(), float(alpha), _dtype(x), _ptr(x), _ptr(y), _stream(stream)))
     return y
+
+
+def copy(dst, src, stream=None):
+    """dst <- src (same byte size; either may be a pinned host tensor) with
+    the library's SM-driven copy (mgx_copy)."""
+    nb = src.numel() * src.element_size()
+    if dst.numel() * dst.element_size() != nb or not (dst.is_contiguous() and src.is_contiguous()):
+        raise ValueError("copy wants contiguous tensors of one byte size")
+    _check(load().mgx_copy(_ptr(dst), _ptr(src), nb, _stream(stream)))
+    return dst
 
 
 class Context:
@@ -263,6 +277,20 @@ class Context:
         _check(load().mgx_precond_mg(self.handle, ctypes.byref(prm), _dtype(res), p, ld, _ptr(out), nf,
                                      masks.handle if masks is not None else None, _stream(stream)))
         return out
+
+    def precond_update(self, res, psi, alpha, lap_type, maxlevels, gamma, masks=None, chunk=0,
+                       work=None, stream=None):
+        """psi += alpha * V-cycle(res) (the update fused into the last sweep);
+        work: optional scratch block of res's shape."""
+        p, ld, nf = _block(res, self.npts)
+        pp, ldp, _ = _block(psi, self.npts)
+        assert ldp == ld
+        prm = PrecondParams(lap_type, maxlevels, float(gamma), int(chunk))
+        _check(load().mgx_precond_mg_update(self.handle, ctypes.byref(prm), _dtype(res), p, ld, pp,
+                                            float(alpha), nf,
+                                            masks.handle if masks is not None else None,
+                                            _ptr(work), _stream(stream)))
+        return psi
 
     def gamma(self, lap_type, mg_levels, vmax, small_eig):
         g = ctypes.c_double()
@@ -361,6 +389,18 @@ class Context:
         out = torch.empty((n, n), dtype=torch.float64, device=H.device)
         _check(load().mgx_theta(self.handle, n, _ptr(Sc), _ptr(Hc), _ptr(out), _stream(stream)))
         return out.T
+
+    def theta_from_cholesky(self, L, H, stream=None):
+        """(theta, trace): theta = S^-1 H from the row-major lower factor L of
+        S (as returned by cholesky) by substitution; trace = tr(theta)."""
+        n = H.shape[0]
+        Lc = L.T.contiguous()
+        Hc = H.T.contiguous()
+        out = torch.empty((n, n), dtype=torch.float64, device=H.device)
+        tr = torch.empty(1, dtype=torch.float64, device=H.device)
+        _check(load().mgx_theta_from_cholesky(self.handle, n, _ptr(Lc), _ptr(Hc), _ptr(out),
+                                              _ptr(tr), _stream(stream)))
+        return out.T, tr
 
     @staticmethod
     def _colmajor(theta):

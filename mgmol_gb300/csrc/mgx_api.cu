@@ -67,7 +67,7 @@ void DeviceBuffer::release()
 
 // defined in the other translation units
 int precond_mg(mgx_ctx*, const mgx_precond_params*, int, const void*, size_t,
-    void*, int, const mgx_masks*, cudaStream_t);
+    void*, int, const mgx_masks*, cudaStream_t, void* upd = nullptr, double alpha = 0.);
 int restrict_launch(int, const Level&, const void*, size_t, void*, size_t, int,
     const MaskDev&, cudaStream_t);
 int prolong_launch(int, int, const Level&, const void*, size_t, void*, size_t,
@@ -83,6 +83,8 @@ int psi_theta_cuda_cores(int, const void*, size_t, size_t, int, const double*, i
 int psi_theta_tcgen05(mgx_ctx*, int, const float*, size_t, size_t, int,
     const double*, int, int, float, const float*, float*, cudaStream_t);
 int theta_product(int, const double*, const double*, double*, cudaStream_t);
+int theta_from_cholesky(mgx_ctx*, int, const double*, const double*, double*, double*,
+    cudaStream_t);
 int mgm_solve(mgx_ctx*, const mgx_mgm_params*, int, void*, const void*, mgx_mgm_result*,
     cudaStream_t);
 int gram_tcgen05(mgx_ctx*, int, const void*, const void*, size_t, size_t, int,
@@ -175,11 +177,56 @@ __global__ void axpy_kernel(size_t n, T alpha, const T* __restrict__ x, T* __res
          i += (size_t)gridDim.x * blockDim.x)
         y[i] += alpha * x[i];
 }
+// 16-byte grid-stride copy between device-accessible addresses (device
+// memory, or pinned host memory through its mapped device address)
+__global__ void copy16_kernel(const uint4* __restrict__ src, uint4* __restrict__ dst, size_t n)
+{
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (size_t)gridDim.x * blockDim.x)
+        dst[i] = src[i];
+}
+
+// the device-side address of p, or nullptr when the device cannot address it
+static void* device_address(const void* p)
+{
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess)
+    {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged)
+        return const_cast<void*>(p);
+    if (a.type == cudaMemoryTypeHost) return a.devicePointer;
+    return nullptr;
+}
 } // namespace mgx
 
 using namespace mgx;
 
 extern "C" {
+
+int mgx_copy(void* dst, const void* src, size_t bytes, void* stream)
+{
+    if (bytes == 0) return MGX_OK;
+    if (!dst || !src) return fail(MGX_BAD_ARG, "NULL buffer");
+    cudaStream_t s = (cudaStream_t)stream;
+    void* d       = device_address(dst);
+    void* r       = device_address(src);
+    if (d && r && ((uintptr_t)d % 16) == 0 && ((uintptr_t)r % 16) == 0 && (bytes % 16) == 0)
+    {
+        int dev = 0, sms = 0;
+        MGX_TRY(cuda_check(cudaGetDevice(&dev), "device"));
+        MGX_TRY(cuda_check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev),
+            "SM count"));
+        const size_t n = bytes / 16;
+        const int nb   = (int)std::min<size_t>((n + 255) / 256, (size_t)sms * 8);
+        copy16_kernel<<<nb, 256, 0, s>>>((const uint4*)r, (uint4*)d, n);
+        MGX_LAUNCH_CHECK("copy16_kernel");
+        return MGX_OK;
+    }
+    return cuda_check(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDefault, s), "copy");
+}
 
 const char* mgx_last_error_string(void) { return g_err; }
 
@@ -402,6 +449,23 @@ int mgx_precond_mg(mgx_ctx* ctx, const mgx_precond_params* p, mgx_dtype dtype,
     return MGX_OK;
 }
 
+int mgx_precond_mg_update(mgx_ctx* ctx, const mgx_precond_params* p, mgx_dtype dtype,
+    const void* res, size_t ld, void* psi, double alpha, int nfunc, const mgx_masks* masks,
+    void* work, void* stream)
+{
+    if (!ctx) return fail(MGX_BAD_ARG, "ctx is NULL");
+    MGX_TRY(check_dtype(dtype));
+    MGX_TRY(check_block(ctx->grid, res, ld, nfunc, "res"));
+    MGX_TRY(check_block(ctx->grid, psi, ld, nfunc, "psi"));
+    if (masks && masks->dtype != dtype)
+        return fail(MGX_BAD_ARG, "mask value type differs from the orbital type");
+    const size_t np  = (size_t)ctx->grid.n[0] * ctx->grid.n[1] * ctx->grid.n[2];
+    const size_t ldv = nfunc > 1 ? ld : (ld ? ld : np);
+    if (work) MGX_TRY(check_block(ctx->grid, work, ld, nfunc, "work"));
+    return precond_mg(ctx, p, dtype, res, ldv, work, nfunc, masks, (cudaStream_t)stream, psi,
+        alpha);
+}
+
 int mgx_precond_gamma(const mgx_grid* grid, int lap_type, int mg_levels,
     double vmax, double small_eig, double* gamma)
 {
@@ -551,6 +615,13 @@ int mgx_trace_prod(mgx_ctx* ctx, int n, const double* H, const double* Sinv,
 {
     if (!ctx) return fail(MGX_BAD_ARG, "ctx is NULL");
     return trace_prod(ctx, n, H, Sinv, trace, (cudaStream_t)stream);
+}
+
+int mgx_theta_from_cholesky(mgx_ctx* ctx, int n, const double* L, const double* H,
+    double* theta, double* trace, void* stream)
+{
+    if (!ctx) return fail(MGX_BAD_ARG, "ctx is NULL");
+    return theta_from_cholesky(ctx, n, L, H, theta, trace, (cudaStream_t)stream);
 }
 
 int mgx_theta(mgx_ctx* ctx, int n, const double* Sinv, const double* H,

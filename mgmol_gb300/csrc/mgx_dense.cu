@@ -532,31 +532,133 @@ __global__ void __launch_bounds__(256) trinv_diag_kernel(const double* L, int n,
     }
 }
 
+/* forward substitution L Y = B in place on Y (n x ncols, leading dimension
+ * n), with the inverses of L's diagonal blocks in the diagonal blocks of
+ * X: per 64-row block, Y_k <- W_k Y_k through the panel, then the rows
+ * below lose L[below, k] Y_k (one (n - k) x ncols x 64 product, parallel
+ * over all of Y's columns) */
+static int forward_subst(int n, const double* L, const double* X, double* Y, int ncols,
+    double* panel, cudaStream_t s)
+{
+    const int nbk = (n + NB - 1) / NB;
+    for (int kb = 0; kb < nbk; kb++)
+    {
+        const int k0 = kb * NB, nb = std::min(NB, n - k0);
+        MGX_TRY(dgemm(false, false, nb, ncols, nb, 1., X + (size_t)k0 * n + k0, n, Y + k0, n,
+            0., panel, NB, 0, s));
+        copy_panel_kernel<<<std::min(1024, (nb * ncols + 255) / 256), 256, 0, s>>>(panel, NB,
+            Y + k0, n, nb, ncols);
+        MGX_LAUNCH_CHECK("copy_panel_kernel");
+        const int m = n - k0 - nb;
+        if (m > 0)
+            MGX_TRY(dgemm(false, false, m, ncols, nb, -1., L + (size_t)k0 * n + k0 + nb, n,
+                Y + k0, n, 1., Y + k0 + nb, n, 0, s));
+    }
+    return MGX_OK;
+}
+
+__global__ void identity_kernel(double* X, int n)
+{
+    const size_t nn = (size_t)n * n;
+    for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < nn;
+         t += (size_t)gridDim.x * blockDim.x)
+        X[t] = ((t % n) == (t / n)) ? 1. : 0.;
+}
+
+/* Sinv = (L L^T)^-1 = X^T X with X = L^-1 formed by forward substitution
+ * on the identity (parallel over its n columns), then one product. */
 int inverse_from_cholesky(mgx_ctx* ctx, int n, const double* L, double* Sinv,
     cudaStream_t s)
 {
     if (n <= 0 || !L || !Sinv) return fail(MGX_BAD_ARG, "inverse: bad arguments");
+    if (Sinv == L) return fail(MGX_BAD_ARG, "inverse: Sinv aliases L");
     double *winv, *panel, *X;
     int* dinfo;
     MGX_TRY(dense_ws(ctx, n, &winv, &panel, &X, &dinfo));
-    MGX_TRY(cuda_check(cudaMemsetAsync(X, 0, (size_t)n * n * 8, s), "X zero"));
+    const int nbk = (n + NB - 1) / NB;
+    MGX_TRY(cuda_check(cudaFuncSetAttribute(trinv_diag_kernel,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize, DIAG_SMEM),
+        "trinv smem attribute"));
+    // inverses of the diagonal blocks into X, then Y = I in Sinv, solved
+    trinv_diag_kernel<<<nbk, 256, DIAG_SMEM, s>>>(L, n, X);
+    MGX_LAUNCH_CHECK("trinv_diag_kernel");
+    const int nb = (int)std::min<size_t>(((size_t)n * n + 255) / 256, 4096);
+    identity_kernel<<<nb, 256, 0, s>>>(Sinv, n);
+    MGX_LAUNCH_CHECK("identity_kernel");
+    MGX_TRY(forward_subst(n, L, X, Sinv, n, panel, s));
+    // X <- L^-1, then S^-1 = X^T X
+    MGX_TRY(cuda_check(cudaMemcpyAsync(X, Sinv, (size_t)n * n * 8, cudaMemcpyDeviceToDevice, s),
+        "L^-1 copy"));
+    MGX_TRY(dgemm(true, false, n, n, n, 1., X, n, X, n, 0., Sinv, n, 0, s));
+    return MGX_OK;
+}
+
+/* theta = S^-1 H = L^-T (L^-1 H) from the Cholesky factor L, without
+ * forming S^-1: blocked forward substitution L Y = H and back substitution
+ * L^T theta = Y with the n columns of H as right-hand sides.  The diagonal
+ * blocks are applied through their inverses (trinv_diag_kernel); the
+ * off-diagonal updates are (n - k) x n x 64 products with full-width
+ * parallelism.  2 n^3 flop instead of the n^3 / 3 + 2 n^3 + 2 n^3 of
+ * computeInverse followed by updateTheta (src/GramMatrix.cc:75-91,
+ * src/ProjectedMatrices.h:218-225).  trace (device, may be NULL) receives
+ * tr(theta) = tr(S^-1 H). */
+__global__ void diag_sum_kernel(const double* __restrict__ A, int n, double* __restrict__ out)
+{
+    __shared__ double red[256];
+    double acc = 0.;
+    for (int i = threadIdx.x; i < n; i += blockDim.x)
+        acc += A[(size_t)i * n + i];
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1)
+    {
+        if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *out = red[0];
+}
+
+int theta_from_cholesky(mgx_ctx* ctx, int n, const double* L, const double* H,
+    double* theta, double* trace, cudaStream_t s)
+{
+    if (n <= 0 || !L || !H || !theta) return fail(MGX_BAD_ARG, "theta: bad arguments");
+    if (theta == H || theta == L) return fail(MGX_BAD_ARG, "theta aliases an input");
+    double *winv, *panel, *X;
+    int* dinfo;
+    MGX_TRY(dense_ws(ctx, n, &winv, &panel, &X, &dinfo));
     const int nbk = (n + NB - 1) / NB;
     MGX_TRY(cuda_check(cudaFuncSetAttribute(trinv_diag_kernel,
                            cudaFuncAttributeMaxDynamicSharedMemorySize, DIAG_SMEM),
         "trinv smem attribute"));
     trinv_diag_kernel<<<nbk, 256, DIAG_SMEM, s>>>(L, n, X);
     MGX_LAUNCH_CHECK("trinv_diag_kernel");
-    for (int kb = 1; kb < nbk; kb++)
+    MGX_TRY(cuda_check(cudaMemcpyAsync(theta, H, (size_t)n * n * 8, cudaMemcpyDeviceToDevice, s),
+        "theta init"));
+    auto apply_diag = [&](int k0, int nb, bool transpose) -> int {
+        // rows k0..k0+nb of theta <- W^(T) * rows k0..k0+nb, through the panel
+        MGX_TRY(dgemm(transpose, false, nb, n, nb, 1., X + (size_t)k0 * n + k0, n, theta + k0,
+            n, 0., panel, NB, 0, s));
+        copy_panel_kernel<<<std::min(1024, (nb * n + 255) / 256), 256, 0, s>>>(panel, NB,
+            theta + k0, n, nb, n);
+        MGX_LAUNCH_CHECK("copy_panel_kernel");
+        return MGX_OK;
+    };
+    // forward: L Y = H
+    MGX_TRY(forward_subst(n, L, X, theta, n, panel, s));
+    // backward: L^T theta = Y
+    for (int kb = nbk - 1; kb >= 0; kb--)
     {
         const int k0 = kb * NB, nb = std::min(NB, n - k0);
-        // panel(nb x k0) = L[k0:k0+nb, 0:k0] * X[0:k0, 0:k0]
-        MGX_TRY(dgemm(false, false, nb, k0, k0, 1., L + k0, n, X, n, 0., panel, nb, 0, s));
-        // X[k0:k0+nb, 0:k0] = -X_kk * panel
-        MGX_TRY(dgemm(false, false, nb, k0, nb, -1., X + (size_t)k0 * n + k0, n, panel,
-            nb, 0., X + k0, n, 0, s));
+        MGX_TRY(apply_diag(k0, nb, true));
+        if (k0 > 0)
+            MGX_TRY(dgemm(true, false, k0, n, nb, -1., L + k0, n, theta + k0, n, 1., theta, n,
+                0, s));
     }
-    // S^-1 = X^T X
-    MGX_TRY(dgemm(true, false, n, n, n, 1., X, n, X, n, 0., Sinv, n, 0, s));
+    if (trace)
+    {
+        diag_sum_kernel<<<1, 256, 0, s>>>(theta, n, trace);
+        MGX_LAUNCH_CHECK("diag_sum_kernel");
+    }
     return MGX_OK;
 }
 

@@ -711,10 +711,20 @@ struct VCycle
 
     double gamma = 0.;
     bool pending_scale = false; // level-0 iterate still to be set to gamma*f
+    // fused update: the last level-0 sweep adds upd_alpha * v to upd0
+    // (chunk base) instead of storing v
+    void* upd0       = nullptr;
+    double upd_alpha = 0.;
 
-    int jacobi(int l, int cur, bool write_w)
+    int jacobi(int l, int cur, bool write_w, bool last = false)
     {
         PlaneParams p;
+        if (last && l == 0 && upd0)
+        {
+            p.upd       = upd0;
+            p.ldupd     = ld[0];
+            p.upd_alpha = upd_alpha;
+        }
         if (l == 0 && pending_scale)
         {
             // first sweep straight from f with u = gamma f
@@ -786,7 +796,7 @@ struct VCycle
         if (st != MGX_OK) return -st - 1;
         for (int it = 0; it < 2; it++)
         {
-            st = jacobi(l, cur, false);
+            st = jacobi(l, cur, false, it == 1);
             if (st != MGX_OK) return -st - 1;
             cur ^= 1;
         }
@@ -794,12 +804,17 @@ struct VCycle
     }
 };
 
+/* out = V-cycle(res); or, with upd set, upd += alpha * V-cycle(res)
+ * through the last fine-level sweep, and out (nfunc x ld, may be NULL) is
+ * only scratch for the fine-level iterate */
 int precond_mg(mgx_ctx* ctx, const mgx_precond_params* P, int dtype,
     const void* res, size_t ld, void* out, int nfunc, const mgx_masks* masks,
-    cudaStream_t s)
+    cudaStream_t s, void* upd = nullptr, double alpha = 0.)
 {
-    if (!P || !res || !out || nfunc < 0) return fail(MGX_BAD_ARG, "precond_mg: null argument");
-    if (res == out) return fail(MGX_BAD_ARG, "precond_mg: res and out alias");
+    if (!P || !res || (!out && !upd) || nfunc < 0)
+        return fail(MGX_BAD_ARG, "precond_mg: null argument");
+    if (res == out || res == upd || (upd && upd == out))
+        return fail(MGX_BAD_ARG, "precond_mg: res, out and the update block alias");
     if (P->lap_type < 0 || P->lap_type > 4) return fail(MGX_BAD_ARG, "lap_type %d", P->lap_type);
     const int L = P->maxlevels;
     if (L < 0 || L > 6) return fail(MGX_BAD_ARG, "maxlevels %d", L);
@@ -825,8 +840,12 @@ int precond_mg(mgx_ctx* ctx, const mgx_precond_params* P, int dtype,
         V.lev.push_back(make_level(g, l));
         V.jf.push_back(jacobi_factor(l == 0 ? P->lap_type : 1, V.lev[l].h));
     }
-    // workspace per function: level 0: v1 + w ; level l>0: v0, v1, w, f
-    size_t per_func = 2 * V.lev[0].npts();
+    // workspace per function: level 0: v1 + w (+ v0 when the update is
+    // fused and the caller gave no scratch block), each with the caller's
+    // leading dimension ld, as every level-0 array is addressed with it;
+    // level l>0: v0, v1, w, f
+    const bool own_v0 = upd && !out;
+    size_t per_func   = (own_v0 ? 3 : 2) * ld;
     for (int l = 1; l <= L; l++)
         per_func += 4 * V.lev[l].npts();
     per_func *= es;
@@ -858,13 +877,23 @@ int precond_mg(mgx_ctx* ctx, const mgx_precond_params* P, int dtype,
         V.ld.assign(L + 1, 0);
         char* base = (char*)ctx->vc.ptr;
         V.ld[0]    = ld;
-        V.v0[0]    = (char*)out + (size_t)f0 * ld * es;
         V.f[0]     = (void*)((const char*)res + (size_t)f0 * ld * es);
-        const size_t p0 = V.lev[0].npts();
+        if (own_v0)
+        {
+            V.v0[0] = base;
+            base += (size_t)nf * ld * es;
+        }
+        else
+            V.v0[0] = (char*)out + (size_t)f0 * ld * es;
+        if (upd)
+        {
+            V.upd0      = (char*)upd + (size_t)f0 * ld * es;
+            V.upd_alpha = alpha;
+        }
         V.v1[0]    = base;
-        base += (size_t)nf * p0 * es;
+        base += (size_t)nf * ld * es;
         V.w[0] = base;
-        base += (size_t)nf * p0 * es;
+        base += (size_t)nf * ld * es;
         for (int l = 1; l <= L; l++)
         {
             const size_t pl = V.lev[l].npts();
@@ -963,7 +992,8 @@ int precond_mg_static(mgx_ctx* ctx, const mgx_precond_params* P, int dtype,
         V.lev.push_back(make_level(g, l));
         V.jf.push_back(jacobi_factor(l == 0 ? P->lap_type : 1, V.lev[l].h));
     }
-    size_t per_func = 2 * V.lev[0].npts();
+    // level-0 arrays are addressed with the caller's leading dimension ld
+    size_t per_func = 2 * ld;
     for (int l = 1; l <= L; l++)
         per_func += 4 * V.lev[l].npts();
     per_func *= es;
@@ -999,11 +1029,10 @@ int precond_mg_static(mgx_ctx* ctx, const mgx_precond_params* P, int dtype,
         V.ld[0]    = ld;
         V.v0[0]    = (char*)out + (size_t)f0 * ld * es;
         V.f[0]     = (void*)((const char*)res + (size_t)f0 * ld * es);
-        const size_t p0 = V.lev[0].npts();
         V.v1[0]    = base;
-        base += (size_t)nf * p0 * es;
+        base += (size_t)nf * ld * es;
         V.w[0] = base;
-        base += (size_t)nf * p0 * es;
+        base += (size_t)nf * ld * es;
         for (int l = 1; l <= L; l++)
         {
             const size_t pl = V.lev[l].npts();

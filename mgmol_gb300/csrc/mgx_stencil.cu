@@ -388,6 +388,10 @@ __global__ void __launch_bounds__(256) plane_kernel(PlaneParams p, DevCoef<T> c)
     }
 
     T* __restrict__ outp     = reinterpret_cast<T*>(p.out) + (size_t)f * p.ldo;
+    T* __restrict__ updp     = (OP == OP_JACOBI && p.upd)
+                                   ? reinterpret_cast<T*>(p.upd) + (size_t)f * p.ldupd
+                                   : nullptr;
+    const T ualpha           = (T)p.upd_alpha;
     T* __restrict__ wp       = p.w ? reinterpret_cast<T*>(p.w) + (size_t)f * p.ldw : nullptr;
     const T* __restrict__ fp = p.f ? reinterpret_cast<const T*>(p.f) + (size_t)f * p.ldf : nullptr;
     constexpr bool POINTWISE = (OP == OP_JACOBI) || (OP == OP_HPSI_V) || (OP == OP_RHS_SUB);
@@ -413,7 +417,10 @@ __global__ void __launch_bounds__(256) plane_kernel(PlaneParams p, DevCoef<T> c)
             }
             if (wp != nullptr) wp[idx] = w;
         }
-        outp[idx] = r;
+        if (OP == OP_JACOBI && updp != nullptr)
+            updp[idx] = updp[idx] + ualpha * r;
+        else
+            outp[idx] = r;
     };
 
     bool ok    = true;
@@ -680,6 +687,10 @@ __global__ void __launch_bounds__(256) plane_vec_kernel(PlaneParams p, DevCoef<T
             A1[k][v] = B1[k][v] = B2[k][v] = U1[k][v] = (T)0;
 
     T* __restrict__ outp     = reinterpret_cast<T*>(p.out) + (size_t)f * p.ldo;
+    T* __restrict__ updp     = (OP == OP_JACOBI && p.upd)
+                                   ? reinterpret_cast<T*>(p.upd) + (size_t)f * p.ldupd
+                                   : nullptr;
+    const T ualpha           = (T)p.upd_alpha;
     T* __restrict__ wp       = p.w ? reinterpret_cast<T*>(p.w) + (size_t)f * p.ldw : nullptr;
     const T* __restrict__ fp = p.f ? reinterpret_cast<const T*>(p.f) + (size_t)f * p.ldf : nullptr;
     constexpr bool POINTWISE = (OP == OP_JACOBI) || (OP == OP_HPSI_V) || (OP == OP_RHS_SUB);
@@ -811,7 +822,16 @@ __global__ void __launch_bounds__(256) plane_vec_kernel(PlaneParams p, DevCoef<T
             }
             if (emit)
             {
-                *reinterpret_cast<V4*>(outp + xoff + goff[k]) = res;
+                if (OP == OP_JACOBI && updp != nullptr)
+                {
+                    V4 q = *reinterpret_cast<const V4*>(updp + xoff + goff[k]);
+#pragma unroll
+                    for (int v = 0; v < VEC; v++)
+                        VH::set(q, v, VH::get(q, v) + ualpha * VH::get(res, v));
+                    *reinterpret_cast<V4*>(updp + xoff + goff[k]) = q;
+                }
+                else
+                    *reinterpret_cast<V4*>(outp + xoff + goff[k]) = res;
                 if (OP == OP_JACOBI && wp != nullptr)
                     *reinterpret_cast<V4*>(wp + xoff + goff[k]) = wres;
             }
@@ -873,7 +893,13 @@ __global__ void __launch_bounds__(256) direct_kernel(PlaneParams p, DevCoef<T> c
             if (p.w != nullptr)
                 reinterpret_cast<T*>(p.w)[(size_t)f * p.ldw + idx] = wres;
         }
-        reinterpret_cast<T*>(p.out)[(size_t)f * p.ldo + idx] = r;
+        if (OP == OP_JACOBI && p.upd != nullptr)
+        {
+            T* u = reinterpret_cast<T*>(p.upd) + (size_t)f * p.ldupd + idx;
+            *u   = *u + (T)p.upd_alpha * r;
+        }
+        else
+            reinterpret_cast<T*>(p.out)[(size_t)f * p.ldo + idx] = r;
     }
 }
 
@@ -903,7 +929,9 @@ static bool vec_ok(const PlaneParams& p, int force_direct)
         return q == nullptr || (((uintptr_t)q % 16) == 0 && (ld * sizeof(T)) % 16 == 0);
     };
     if ((nz * sizeof(T)) % 16) return false;
-    if (!al(p.u, p.ldu) || !al(p.out, p.ldo) || !al(p.w, p.ldw) || !al(p.f, p.ldf)) return false;
+    if (!al(p.u, p.ldu) || !al(p.out, p.ldo) || !al(p.w, p.ldw) || !al(p.f, p.ldf)
+        || !al(p.upd, p.ldupd))
+        return false;
     if (p.V && ((uintptr_t)p.V % 16)) return false;
     if (ny < 3 || nx < 1 || nz > 256 * 2 * (16 / (int)sizeof(T))) return false;
     return true;

@@ -57,6 +57,12 @@ struct PlaneParams
     // iterate is u = gamma_in * f (the first sweep of the V-cycle started
     // from gamma * res, src/OrbitalsPreconditioning.cc:102-107)
     double gamma_in = 0.;
+    // OP_JACOBI only: when set, the sweep's result r is not stored to out;
+    // instead upd += upd_alpha * r (the orbital update of an ABPG step
+    // fused into the last smoothing sweep of the preconditioner)
+    void* upd        = nullptr;
+    size_t ldupd     = 0;
+    double upd_alpha = 0.;
 };
 
 int stencil_launch(int op, int lap_type, int dtype, int v_dtype,

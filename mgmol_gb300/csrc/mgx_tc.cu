@@ -464,6 +464,67 @@ __global__ void __launch_bounds__(256) transpose_split_kernel(const float* __res
     }
 }
 
+// Points-major BF16 hi / lo planes of columns [p0, p0 + P) of the orbital
+// block in the K-blocked layout: element (point p, function i) at
+// ((i / 64) * P + p) * 64 + i % 64.  A block converts 64 functions x 128
+// points through shared memory: reads run along points (512 bytes per row;
+// the tile's row stride of 129 floats keeps both shared-memory phases free
+// of bank conflicts), and the block's output is two contiguous 16 KB runs.
+constexpr int TB_P = 128;
+
+__global__ void __launch_bounds__(256) transpose_split_blocked_kernel(const float* __restrict__ x,
+    size_t ld, int n, size_t p0, int P, __nv_bfloat16* __restrict__ hi,
+    __nv_bfloat16* __restrict__ lo)
+{
+    __shared__ float t[64][TB_P + 1];
+    const int kb    = blockIdx.y;
+    const int ib    = kb * 64;
+    const size_t pb = (size_t)blockIdx.x * TB_P;
+    for (int e = threadIdx.x; e < 64 * TB_P; e += blockDim.x)
+    {
+        const int r = e / TB_P, c = e % TB_P;
+        t[r][c] = (ib + r < n && pb + c < (size_t)P) ? x[(size_t)(ib + r) * ld + p0 + pb + c] : 0.f;
+    }
+    __syncthreads();
+    // 8 consecutive functions of one point per item: one 16-byte store per plane
+    for (int e = threadIdx.x; e < TB_P * 8; e += blockDim.x)
+    {
+        const int c = e / 8, g = 8 * (e % 8);
+        const size_t pp = pb + c;
+        if (pp >= (size_t)P) continue;
+        __align__(16) __nv_bfloat16 h[8], l[8];
+#pragma unroll
+        for (int q = 0; q < 8; q++)
+        {
+            const float a = t[g + q][c];
+            h[q] = __float2bfloat16_rn(a);
+            l[q] = __float2bfloat16_rn(a - __bfloat162float(h[q]));
+        }
+        const size_t o = ((size_t)kb * P + pp) * 64 + g;
+        *reinterpret_cast<uint4*>(hi + o) = *reinterpret_cast<const uint4*>(h);
+        *reinterpret_cast<uint4*>(lo + o) = *reinterpret_cast<const uint4*>(l);
+    }
+}
+
+// theta columns as K-blocked BF16 hi / lo planes: element (row j, K = i) at
+// ((i / 64) * ncols + j) * 64 + i % 64, zero padded to kblocks * 64.
+__global__ void matrix_split_blocked_kernel(const double* __restrict__ th, int n, int ldt,
+    int ncols, int kblocks, __nv_bfloat16* __restrict__ hi, __nv_bfloat16* __restrict__ lo)
+{
+    const size_t total = (size_t)ncols * kblocks * 64;
+    for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+         t += (size_t)gridDim.x * blockDim.x)
+    {
+        const size_t kb = t / ((size_t)ncols * 64);
+        const size_t rem = t - kb * (size_t)ncols * 64;
+        const size_t j = rem / 64, i = kb * 64 + rem % 64;
+        const double v = (i < (size_t)n) ? th[j * ldt + i] : 0.;
+        const __nv_bfloat16 h = __float2bfloat16_rn((float)v);
+        hi[t] = h;
+        lo[t] = __float2bfloat16_rn((float)(v - (double)__bfloat162float(h)));
+    }
+}
+
 // FP64 matrix theta (n rows, ncols columns, column j at th + j * ldt) ->
 // function-major operand rows j = column j of theta, K = i, leading
 // dimension ldo: bf16 hi / lo planes (hi = bf16(x), lo = bf16(x - hi)) or
@@ -596,16 +657,17 @@ struct Operand
     bool blocked = false; // K-blocked planes (bf16 only)
 };
 
-/* K bytes per tile row of the BF16X3 kernels: 128 (SWIZZLE_128B, 2 stages
- * at 128 x 256 tiles) or 64 (SWIZZLE_64B, 4 stages); MGX_TC_SWIZZLE
- * (64 or 128) overrides the default for tuning. */
+/* K bytes per tile row of the BF16X3 kernels: 64 (SWIZZLE_64B, 4 stages
+ * at 128 x 256 tiles; the default, 8 % faster than 128 on the Gram and the
+ * Psi Theta product at 2048 orbitals on 192^3) or 128 (SWIZZLE_128B, 2
+ * stages); MGX_TC_SWIZZLE (64 or 128) overrides the default for tuning. */
 int bf16_swizzle()
 {
     static int sw = 0;
     if (!sw)
     {
         const char* e = getenv("MGX_TC_SWIZZLE");
-        sw            = (e && atoi(e) == 64) ? 64 : (e && atoi(e) == 128) ? 128 : 128;
+        sw            = (e && atoi(e) == 128) ? 128 : 64;
     }
     return sw;
 }
@@ -929,9 +991,14 @@ int psi_theta_tcgen05(mgx_ctx* ctx, int mode, const float* psi, size_t ld, size_
     void* blo = ws + b_plane;
     void* ahi = ws + b_bytes;
     void* alo = ws + b_bytes + a_plane;
+    const bool blk = bf && blocked_planes();
+    const int nkb  = (int)(ldk / 64);
     {
         const int nb = (int)std::min<size_t>((ncols * ldk + 255) / 256, 1 << 16);
-        if (bf)
+        if (blk)
+            matrix_split_blocked_kernel<<<nb, 256, 0, s>>>(theta, n, ldt, ncols, nkb,
+                (__nv_bfloat16*)bhi, (__nv_bfloat16*)blo);
+        else if (bf)
             matrix_split_kernel<true><<<nb, 256, 0, s>>>(theta, n, ldt, ncols, bhi, blo, ldk);
         else
             matrix_split_kernel<false><<<nb, 256, 0, s>>>(theta, n, ldt, ncols, bhi, blo, ldk);
@@ -940,25 +1007,45 @@ int psi_theta_tcgen05(mgx_ctx* ctx, int mode, const float* psi, size_t ld, size_
     const int BN = (ncols > 128) ? 256 : 128;
     const int sw = bf ? bf16_swizzle() : 128;
     CUtensorMap mb0, mb1, ma0, ma1;
-    MGX_TRY(make_map(&mb0, bhi, bf, n, ncols, ldk, BN, sw));
-    mb1 = mb0;
-    if (bf) MGX_TRY(make_map(&mb1, blo, true, n, ncols, ldk, BN, sw));
+    if (blk)
+    {
+        MGX_TRY(make_map_blocked(&mb0, bhi, ncols, nkb, BN, sw));
+        MGX_TRY(make_map_blocked(&mb1, blo, ncols, nkb, BN, sw));
+    }
+    else
+    {
+        MGX_TRY(make_map(&mb0, bhi, bf, n, ncols, ldk, BN, sw));
+        mb1 = mb0;
+        if (bf) MGX_TRY(make_map(&mb1, blo, true, n, ncols, ldk, BN, sw));
+    }
     const int bkk     = bf ? sw / 2 : 32;
     const int kblocks = (int)((n + bkk - 1) / bkk);
     const int ntj     = (ncols + BN - 1) / BN;
     for (size_t p0 = 0; p0 < npts; p0 += P)
     {
         const int Pc = (int)std::min(P, npts - p0);
-        dim3 tg((Pc + 63) / 64, (n + 63) / 64);
-        if (tg.y > 65535) return fail(MGX_UNSUPPORTED, "too many functions");
-        if (bf)
-            transpose_split_kernel<true><<<tg, 256, 0, s>>>(psi, ld, n, p0, Pc, ahi, alo, ldk);
+        if (blk)
+        {
+            dim3 tg((Pc + TB_P - 1) / TB_P, nkb);
+            transpose_split_blocked_kernel<<<tg, 256, 0, s>>>(psi, ld, n, p0, Pc,
+                (__nv_bfloat16*)ahi, (__nv_bfloat16*)alo);
+            MGX_LAUNCH_CHECK("transpose_split_blocked_kernel");
+            MGX_TRY(make_map_blocked(&ma0, ahi, Pc, nkb, BM, sw));
+            MGX_TRY(make_map_blocked(&ma1, alo, Pc, nkb, BM, sw));
+        }
         else
-            transpose_split_kernel<false><<<tg, 256, 0, s>>>(psi, ld, n, p0, Pc, ahi, alo, ldk);
-        MGX_LAUNCH_CHECK("transpose_split_kernel");
-        MGX_TRY(make_map(&ma0, ahi, bf, n, Pc, ldk, BM, sw));
-        ma1 = ma0;
-        if (bf) MGX_TRY(make_map(&ma1, alo, true, n, Pc, ldk, BM, sw));
+        {
+            dim3 tg((Pc + 63) / 64, (n + 63) / 64);
+            if (tg.y > 65535) return fail(MGX_UNSUPPORTED, "too many functions");
+            if (bf)
+                transpose_split_kernel<true><<<tg, 256, 0, s>>>(psi, ld, n, p0, Pc, ahi, alo, ldk);
+            else
+                transpose_split_kernel<false><<<tg, 256, 0, s>>>(psi, ld, n, p0, Pc, ahi, alo, ldk);
+            MGX_LAUNCH_CHECK("transpose_split_kernel");
+            MGX_TRY(make_map(&ma0, ahi, bf, n, Pc, ldk, BM, sw));
+            ma1 = ma0;
+            if (bf) MGX_TRY(make_map(&ma1, alo, true, n, Pc, ldk, BM, sw));
+        }
         Params p;
         p.tiles      = nullptr;
         p.kblocks    = kblocks;
@@ -974,6 +1061,7 @@ int psi_theta_tcgen05(mgx_ctx* ctx, int mode, const float* psi, size_t ld, size_
         p.beta       = cin ? beta : 0.f;
         p.nrows      = Pc;
         p.ntj        = ntj;
+        p.blocked    = blk ? 1 : 0;
         const int ntiles = ((Pc + BM - 1) / BM) * ntj;
         if (BN == 256)
         {

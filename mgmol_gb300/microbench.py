@@ -38,7 +38,8 @@ def _time(fn, warmup, reps):
 def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("op", choices=["gram", "hmat", "gram_hmat", "mult", "residual", "hpsi",
-                                   "precond", "mgm", "dense", "all"])
+                                   "precond", "mgm", "dense", "h2d", "h2d_kernel", "all"])
+    ap.add_argument("--streams", type=int, default=1, help="h2d: concurrent copy streams")
     ap.add_argument("--grid", type=int, nargs=3, default=[96, 96, 32])
     ap.add_argument("--h", type=float, default=0.25)
     ap.add_argument("--nfunc", type=int, default=2048)
@@ -47,6 +48,7 @@ def main(argv=None):
     ap.add_argument("--warmup", type=int, default=2)
     ap.add_argument("--reps", type=int, default=5)
     args = ap.parse_args(argv)
+    torch.manual_seed(0)
 
     n = tuple(args.grid)
     ll = tuple(x * args.h for x in n)
@@ -108,6 +110,33 @@ def main(argv=None):
                 ctx.theta(Sinv, H)
             ms = _time(dense, args.warmup, args.reps)
             work, unit = (N ** 3 / 3 + 4 * N ** 3 / 3 + 2 * N ** 3), "TFLOP/s"
+        elif op == "h2d":
+            # pinned host block -> device block, split over --streams streams
+            host = torch.empty(psi.shape, dtype=dt, pin_memory=True)
+            host.copy_(psi)
+            dst = torch.empty_like(psi)
+            streams = [torch.cuda.Stream() for _ in range(args.streams)]
+            parts = list(zip(host.chunk(args.streams), dst.chunk(args.streams)))
+
+            def copy():
+                cur = torch.cuda.current_stream()
+                for st, (h, d) in zip(streams, parts):
+                    st.wait_stream(cur)
+                    with torch.cuda.stream(st):
+                        d.copy_(h, non_blocking=True)
+                for st in streams:
+                    cur.wait_stream(st)
+            ms = _time(copy, 1, args.reps)
+            work, unit = host.numel() * host.element_size(), "GB/s"
+            del host, dst
+        elif op == "h2d_kernel":
+            host = torch.empty(psi.shape, dtype=dt, pin_memory=True)
+            host.copy_(psi)
+            dst = torch.empty_like(psi)
+            ms = _time(lambda: capi.copy(dst, host), 1, args.reps)
+            assert torch.equal(dst, psi)
+            work, unit = host.numel() * host.element_size(), "GB/s"
+            del host, dst
         elif op == "mgm":
             rho = V[0:npts].double() - V.double().mean()
             vh = torch.zeros(npts, dtype=torch.float64, device="cuda")

@@ -62,7 +62,7 @@ class OrbitalSweep:
 
     def __init__(self, ctx, V, nfunc, mode="mixed", gemm=None, lap_type=capi.LAP_MEHR4,
                  maxlevels=2, gamma=None, precond_chunk=0, precond_factor=1.0,
-                 chunk_funcs=0, device="cuda"):
+                 chunk_funcs=0, fuse_update=True, device="cuda"):
         self.ctx = ctx
         self.mode = mode
         self.lap_type = lap_type
@@ -83,6 +83,9 @@ class OrbitalSweep:
         self.S = torch.empty((nfunc, nfunc), dtype=torch.float64, device=device)
         self.Hm = torch.empty((nfunc, nfunc), dtype=torch.float64, device=device)
         self.precond_chunk = precond_chunk
+        # the update psi += alpha P(res) inside the last fine-level sweep
+        # (full-block schedule only; the chunked one defers the update)
+        self.fuse_update = bool(fuse_update) and not self.chunk
         self.alpha = 0.5 * precond_factor
         self.theta = None
         if gamma is None:
@@ -123,11 +126,16 @@ class OrbitalSweep:
             ctx.residual(psi, self.hpsi, self.theta, mode=self.gemm, apply_B=apply_B,
                          work=self.corr, out=self.hpsi)
             self._mark(timed, "precond")
-            ctx.precond_mg(self.hpsi, self.lap_type, self.maxlevels, self.gamma,
-                           chunk=self.precond_chunk, out=self.corr)
-            self._mark(timed, "update")
-            if update:
-                capi.axpy(self.alpha, self.corr, psi)
+            if self.fuse_update and update:
+                ctx.precond_update(self.hpsi, psi, self.alpha, self.lap_type, self.maxlevels,
+                                   self.gamma, chunk=self.precond_chunk, work=self.corr)
+                self._mark(timed, "update")
+            else:
+                ctx.precond_mg(self.hpsi, self.lap_type, self.maxlevels, self.gamma,
+                               chunk=self.precond_chunk, out=self.corr)
+                self._mark(timed, "update")
+                if update:
+                    capi.axpy(self.alpha, self.corr, psi)
         else:
             # theta.T is the column-major buffer: row j holds column j
             thc = self.theta.T
@@ -151,7 +159,10 @@ class OrbitalSweep:
         return e
 
     def correction(self):
-        """P(res) of the last run (the block psi was moved along)."""
+        """P(res) of the last run (the block psi was moved along); not kept
+        when the update is fused into the preconditioner."""
+        if self.fuse_update:
+            raise RuntimeError("the fused update does not keep P(res)")
         return self.hpsi if self.chunk else self.corr
 
     def phase_ms(self):

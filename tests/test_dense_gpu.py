@@ -89,3 +89,24 @@ def test_gram_pipeline_on_orbitals(n):
     L = ctx.cholesky(S)
     Sinv = ctx.inverse_from_cholesky(L).cpu().numpy()
     assert np.max(np.abs(Sinv @ S_np - np.eye(n))) < 1e-9 * np.linalg.cond(S_np)
+
+
+@pytest.mark.parametrize("n", [64, 213, 512])
+def test_theta_from_cholesky(n):
+    """theta = S^-1 H by substitution equals the inverse-then-multiply path
+    (GramMatrix::computeInverse + ProjectedMatrices::updateTheta) and its
+    trace the energy tr(S^-1 H)."""
+    rng = np.random.default_rng(n)
+    A = rng.standard_normal((n, n))
+    S = A @ A.T / n + np.eye(n)
+    H = rng.standard_normal((n, n))
+    H = H + H.T
+    ctx = capi.Context((8, 8, 8), (1, 1, 1))
+    L = ctx.cholesky(_dev(S))
+    th, tr = ctx.theta_from_cholesky(L, _dev(H))
+    Sinv = O.inverse_from_chol(L.cpu().numpy())
+    ref = O.theta(Sinv, H)
+    assert rel_err(th.cpu().numpy(), ref) < 1e-12 * max(1.0, np.linalg.cond(S) / 10)
+    t = float(tr.cpu()[0])
+    tref = O.trace_prod(H, Sinv)
+    assert abs(t - tref) < 1e-12 * max(1.0, abs(tref)) * n

@@ -134,3 +134,51 @@ def test_masked_precond_float32():
     M = capi.Masks(ctx, 3, centers, radii, func=0, kind=0, dtype=torch.float32)
     out = ctx.precond_mg(_dev(res, np.float32), 0, 2, 0.3, masks=M).cpu().numpy()
     assert rel_err(out, ref) < 1e-4
+
+
+@pytest.mark.parametrize("dt,tol", [(np.float64, 1e-14), (np.float32, 2e-6)])
+def test_precond_update_fused(dt, tol):
+    """psi += alpha P(res) through the last fine sweep equals the V-cycle
+    followed by an axpy (the update of ABPG::update_states)."""
+    n = (32, 32, 32)
+    ll = tuple(x * 0.3 for x in n)
+    res, _, _ = synth.gaussian_orbitals(n, ll, 5, 61)
+    psi, _, _ = synth.gaussian_orbitals(n, ll, 5, 62)
+    ctx = capi.Context(n, ll)
+    r = _dev(res, dt)
+    corr = ctx.precond_mg(r, 0, 2, 0.3)
+    ref = _dev(psi, dt)
+    capi.axpy(0.5, corr, ref)
+    got = _dev(psi, dt)
+    ctx.precond_update(r, got, 0.5, 0, 2, 0.3)
+    assert rel_err(got.cpu().numpy(), ref.cpu().numpy()) < tol
+    # with a caller scratch block for the fine-level iterate
+    got = _dev(psi, dt)
+    ctx.precond_update(r, got, 0.5, 0, 2, 0.3, work=torch.empty_like(r))
+    assert rel_err(got.cpu().numpy(), ref.cpu().numpy()) < tol
+    # through the masked V-cycle too
+    centers = np.array([[4.8, 4.8, 4.8]] * 5)
+    radii = np.full(5, 3.0)
+    masks = capi.Masks(ctx, 3, centers, radii, dtype=torch.float64 if dt == np.float64 else torch.float32)
+    corr = ctx.precond_mg(r, 0, 2, 0.3, masks=masks)
+    ref = _dev(psi, dt)
+    capi.axpy(0.5, corr, ref)
+    got = _dev(psi, dt)
+    ctx.precond_update(r, got, 0.5, 0, 2, 0.3, masks=masks)
+    assert rel_err(got.cpu().numpy(), ref.cpu().numpy()) < tol
+
+
+def test_precond_leading_dimension_above_points():
+    """Blocks whose functions are spaced wider than the grid (ld > points)."""
+    n = (16, 16, 16)
+    ll = tuple(x * 0.35 for x in n)
+    res, _, _ = synth.gaussian_orbitals(n, ll, 4, 63)
+    ctx = capi.Context(n, ll)
+    npts = ctx.npts
+    wide = torch.zeros((4, npts + 96), dtype=torch.float64, device="cuda")
+    wide[:, :npts] = _dev(res)
+    out_wide = torch.full((4, npts + 96), 7.0, dtype=torch.float64, device="cuda")
+    ctx.precond_mg(wide[:, :npts], 0, 2, 0.3, out=out_wide[:, :npts])
+    ref = ctx.precond_mg(_dev(res), 0, 2, 0.3)
+    assert torch.equal(out_wide[:, :npts], ref)
+    assert torch.all(out_wide[:, npts:] == 7.0)

@@ -162,7 +162,7 @@ def test_abpg_step_fp64_matches_oracle_chain():
     psi, _, _ = synth.gaussian_orbitals(grid, ll, nf, 41, sigma=(0.9, 1.3))
     V = synth.gaussian_wells(grid, ll, 4, 41)
     ctx = capi.Context(grid, ll)
-    sw = OrbitalSweep(ctx, torch.from_numpy(V), nf, mode="plain", maxlevels=2)
+    sw = OrbitalSweep(ctx, torch.from_numpy(V), nf, mode="plain", maxlevels=2, fuse_update=False)
     pd = _dev(psi)
     e = float(sw.run(pd).cpu()[0])
     vel = ctx.vel
@@ -185,7 +185,8 @@ def test_abpg_step_fp64_matches_oracle_chain():
 @pytest.mark.parametrize("mode,gemm", [("plain", capi.GEMM_FP64), ("mixed", capi.GEMM_BF16X3)])
 def test_abpg_step_lean_schedule_matches_full(mode, gemm):
     """The column-chunked schedule (residual / preconditioner over chunks of
-    output functions) moves psi exactly as the full-block schedule."""
+    output functions) and the schedule with the update fused into the
+    preconditioner move psi as the full-block schedule does."""
     from mgmol_gb300.sweep import OrbitalSweep
     grid, nf = (16, 16, 16), 12
     ll = tuple(x * 0.35 for x in grid)
@@ -194,13 +195,18 @@ def test_abpg_step_lean_schedule_matches_full(mode, gemm):
     dt = np.float64 if mode == "plain" else np.float32
     ctx = capi.Context(grid, ll)
     a, b = _dev(psi, dt), _dev(psi, dt)
-    full = OrbitalSweep(ctx, V, nf, mode=mode, gemm=gemm, maxlevels=2)
+    full = OrbitalSweep(ctx, V, nf, mode=mode, gemm=gemm, maxlevels=2, fuse_update=False)
+    fused = OrbitalSweep(ctx, V, nf, mode=mode, gemm=gemm, maxlevels=2)
     lean = OrbitalSweep(ctx, V, nf, mode=mode, gemm=gemm, maxlevels=2, chunk_funcs=5)
+    c = _dev(psi, dt)
     ea = float(full.run(a).cpu()[0])
     eb = float(lean.run(b).cpu()[0])
+    fused.run(c)
     # the split-K Gram sums K slices with atomics, so S and H (and what
     # follows) agree to rounding between runs, not bit for bit
     assert abs(ea - eb) <= 1e-13 * abs(ea)
     tol = 1e-12 if mode == "plain" else 1e-6
     assert rel_err(b.cpu().numpy(), a.cpu().numpy()) < tol
     assert rel_err(lean.correction().cpu().numpy(), full.correction().cpu().numpy()) < tol * 100
+    # the update fused into the last smoothing sweep moves psi the same way
+    assert rel_err(c.cpu().numpy(), a.cpu().numpy()) < (1e-12 if mode == "plain" else 1e-6)
