@@ -215,7 +215,7 @@ def run_gpu(args, cfg):
     mode = args.mode
     dt = torch.float64 if mode == "plain" else torch.float32
     gemm = {"fp64": capi.GEMM_FP64, "fp32": capi.GEMM_FP32, "tf32": capi.GEMM_TF32,
-            "bf16x3": capi.GEMM_BF16X3}[args.gemm if mode == "mixed" else "fp64"]
+            "bf16x3": capi.GEMM_BF16X3, "fp16x3": capi.GEMM_FP16X3}[args.gemm if mode == "mixed" else "fp64"]
     ctx = capi.Context(n, ll)
     # replicas only: every rank runs the same workload on its own GPU
     psi, _, _ = synth.gaussian_orbitals_device(n, ll, N, cfg["seed"] + rank, dt)
@@ -348,7 +348,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--config", default="c5", choices=sorted(CONFIGS))
     ap.add_argument("--mode", default="mixed", choices=["mixed", "plain"])
-    ap.add_argument("--gemm", default="bf16x3", choices=["fp32", "tf32", "bf16x3"])
+    ap.add_argument("--gemm", default="bf16x3", choices=["fp32", "tf32", "bf16x3", "fp16x3"])
     ap.add_argument("--chunk", type=int, default=0, help="V-cycle orbital chunk (0 = auto)")
     ap.add_argument("--lean", type=int, default=-1,
                     help="residual / preconditioner column chunk (0 = full blocks, -1 = auto)")

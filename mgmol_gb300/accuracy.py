@@ -2,11 +2,12 @@
 
     python -m mgmol_gb300.accuracy --grid 192 192 192 --nfunc 256 --iters 30
 
-Both runs start from the same seeded orbitals and potential and take the
-same number of ABPG steps (H psi, S and H, theta, residual, V-cycle,
-update).  The energy of a step is the band-structure term tr(S^-1 H)
-(ProjectedMatrices::getEigSum, Rydberg); the report gives it per step for
-both runs and the largest difference in Hartree (Ry / 2), one JSON line.
+The FP64 run and one mixed run per GEMM mode start from the same seeded
+orbitals and potential and take the same number of ABPG steps (H psi, S
+and H, theta, residual, V-cycle, update).  The energy of a step is the
+band-structure term tr(S^-1 H) (ProjectedMatrices::getEigSum, Rydberg); the
+report gives it per step, the differences in Hartree (Ry / 2) and the
+condition number of S at the first and last step, one JSON line.
 """
 import argparse
 import json
@@ -18,44 +19,52 @@ import torch
 from . import capi, synth
 from .sweep import OrbitalSweep
 
-GEMM = {"fp32": capi.GEMM_FP32, "tf32": capi.GEMM_TF32, "bf16x3": capi.GEMM_BF16X3}
+GEMM = {"fp32": capi.GEMM_FP32, "tf32": capi.GEMM_TF32, "bf16x3": capi.GEMM_BF16X3,
+        "fp16x3": capi.GEMM_FP16X3}
 
 
-def run(grid, h, nfunc, iters, gemm, wells, seed, lean=0):
+def _trajectory(ctx, V, n, ll, nfunc, iters, seed, mode, gemm, lean, gamma):
+    dt = torch.float64 if mode == "plain" else torch.float32
+    psi, _, _ = synth.gaussian_orbitals_device(n, ll, nfunc, seed, torch.float64)
+    psi = psi.to(dt)
+    sw = OrbitalSweep(ctx, V, nfunc, mode=mode, gemm=gemm, chunk_funcs=lean)
+    if gamma is not None:
+        sw.gamma = gamma
+    energies, conds = [], []
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for it in range(iters):
+        e = sw.run(psi)
+        energies.append(float(e.cpu()[0]))
+        if it in (0, iters - 1):
+            w = torch.linalg.eigvalsh(sw.S)
+            conds.append(float(w[-1] / w[0]))
+    torch.cuda.synchronize()
+    out = {"energies_ry": energies, "seconds": time.perf_counter() - t0, "gamma": sw.gamma,
+           "cond_S": conds}
+    del sw, psi
+    torch.cuda.empty_cache()
+    return out
+
+
+def run(grid, h, nfunc, iters, gemms, wells, seed, lean=0):
     n = tuple(grid)
     ll = tuple(x * h for x in n)
     ctx = capi.Context(n, ll)
     V = synth.gaussian_wells_device(n, ll, wells, seed)
-    out = {}
-    for mode in ("plain", "mixed"):
-        dt = torch.float64 if mode == "plain" else torch.float32
-        psi, _, _ = synth.gaussian_orbitals_device(n, ll, nfunc, seed, torch.float64)
-        psi = psi.to(dt)
-        sw = OrbitalSweep(ctx, V, nfunc, mode=mode,
-                          gemm=capi.GEMM_FP64 if mode == "plain" else GEMM[gemm],
-                          chunk_funcs=lean if mode == "plain" else 0)
-        # both modes use the FP64 run's preconditioner scale
-        if mode == "mixed":
-            sw.gamma = out["plain"]["gamma"]
-        energies = []
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        for _ in range(iters):
-            e = sw.run(psi)
-            energies.append(float(e.cpu()[0]))
-        torch.cuda.synchronize()
-        out[mode] = {"energies_ry": energies, "seconds": time.perf_counter() - t0,
-                     "gamma": sw.gamma}
-        del sw, psi
-        torch.cuda.empty_cache()
-    dE = [abs(a - b) / 2 for a, b in zip(out["plain"]["energies_ry"], out["mixed"]["energies_ry"])]
-    return {
-        "grid": list(n), "h": h, "orbitals": nfunc, "iters": iters, "gemm": gemm,
-        "max_abs_dE_ha": max(dE), "final_abs_dE_ha": dE[-1], "dE_ha_per_step": dE,
-        "E_plain_ry": out["plain"]["energies_ry"], "E_mixed_ry": out["mixed"]["energies_ry"],
-        "plain_s_per_step": out["plain"]["seconds"] / iters,
-        "mixed_s_per_step": out["mixed"]["seconds"] / iters,
-    }
+    plain = _trajectory(ctx, V, n, ll, nfunc, iters, seed, "plain", capi.GEMM_FP64, lean, None)
+    res = {"grid": list(n), "h": h, "orbitals": nfunc, "iters": iters,
+           "E_plain_ry": plain["energies_ry"], "cond_S_plain": plain["cond_S"],
+           "plain_s_per_step": plain["seconds"] / iters, "mixed": {}}
+    for g in gemms:
+        mixed = _trajectory(ctx, V, n, ll, nfunc, iters, seed, "mixed", GEMM[g], 0,
+                            plain["gamma"])
+        dE = [abs(a - b) / 2 for a, b in zip(plain["energies_ry"], mixed["energies_ry"])]
+        res["mixed"][g] = {"max_abs_dE_ha": max(dE), "first_abs_dE_ha": dE[0],
+                           "final_abs_dE_ha": dE[-1], "dE_ha_per_step": dE,
+                           "E_mixed_ry": mixed["energies_ry"],
+                           "s_per_step": mixed["seconds"] / iters}
+    return res
 
 
 def main(argv=None):
@@ -64,13 +73,17 @@ def main(argv=None):
     ap.add_argument("--h", type=float, default=0.25)
     ap.add_argument("--nfunc", type=int, default=256)
     ap.add_argument("--iters", type=int, default=30)
-    ap.add_argument("--gemm", default="bf16x3", choices=sorted(GEMM))
+    ap.add_argument("--gemm", default="bf16x3",
+                    help="comma-separated GEMM modes of the mixed runs (" + ", ".join(sorted(GEMM)) + ")")
     ap.add_argument("--wells", type=int, default=16)
     ap.add_argument("--seed", type=int, default=1005)
     ap.add_argument("--lean", type=int, default=0, help="column chunk of the FP64 run (0 = full)")
     args = ap.parse_args(argv)
-    res = run(args.grid, args.h, args.nfunc, args.iters, args.gemm, args.wells, args.seed,
-              args.lean)
+    gemms = [g for g in args.gemm.split(",") if g]
+    for g in gemms:
+        if g not in GEMM:
+            raise SystemExit(f"unknown GEMM mode {g}")
+    res = run(args.grid, args.h, args.nfunc, args.iters, gemms, args.wells, args.seed, args.lean)
     print(json.dumps(res), flush=True)
     return 0
 

@@ -22,7 +22,7 @@ LIB_PATH = os.path.join(HERE, "libmgx.so")
 MGX_OK, MGX_BAD_ARG, MGX_NOT_SPD, MGX_NONFINITE, MGX_TIMEOUT, MGX_CUDA_ERROR, \
     MGX_UNSUPPORTED, MGX_NO_MEMORY = range(8)
 F64, F32 = 0, 1
-GEMM_FP64, GEMM_FP32, GEMM_TF32, GEMM_BF16X3 = 0, 1, 2, 3
+GEMM_FP64, GEMM_FP32, GEMM_TF32, GEMM_BF16X3, GEMM_FP16X3 = 0, 1, 2, 3, 4
 LAP_MEHR4, LAP_2ND, LAP_4TH, LAP_6TH, LAP_8TH = 0, 1, 2, 3, 4
 
 _STATUS = {0: "MGX_OK", 1: "MGX_BAD_ARG", 2: "MGX_NOT_SPD", 3: "MGX_NONFINITE", 4: "MGX_TIMEOUT",

@@ -547,6 +547,7 @@ int mgx_gram(mgx_ctx* ctx, int mode, const void* psi, size_t ld, int nfunc,
             return gram_cuda_cores(ctx, MGX_F32, psi, psi, ldv, L.npts(), nfunc, vel, 1, S, s);
         case MGX_GEMM_TF32:
         case MGX_GEMM_BF16X3:
+        case MGX_GEMM_FP16X3:
             return gram_tcgen05(ctx, mode, psi, psi, ldv, L.npts(), nfunc, vel, 1, S, s);
     }
     return fail(MGX_BAD_ARG, "gemm mode %d", mode);
@@ -572,6 +573,7 @@ int mgx_hmat(mgx_ctx* ctx, int mode, const void* psi, const void* hpsi, size_t l
             return gram_cuda_cores(ctx, MGX_F32, psi, hpsi, ldv, L.npts(), nfunc, vel, 0, H, s);
         case MGX_GEMM_TF32:
         case MGX_GEMM_BF16X3:
+        case MGX_GEMM_FP16X3:
             return gram_tcgen05(ctx, mode, psi, hpsi, ldv, L.npts(), nfunc, vel, 0, H, s);
     }
     return fail(MGX_BAD_ARG, "gemm mode %d", mode);
@@ -585,7 +587,7 @@ int mgx_gram_hmat(mgx_ctx* ctx, int mode, const void* psi, const void* hpsi,
     MGX_TRY(check_block(ctx->grid, hpsi, ld, nfunc, "hpsi"));
     if (nfunc == 0) return MGX_OK;
     if (!S || !H) return fail(MGX_BAD_ARG, "S or H is NULL");
-    if (mode == MGX_GEMM_TF32 || mode == MGX_GEMM_BF16X3)
+    if (mode == MGX_GEMM_TF32 || mode == MGX_GEMM_BF16X3 || mode == MGX_GEMM_FP16X3)
     {
         const Level L    = make_level(ctx->grid, 0);
         const double vel = L.h[0] * L.h[1] * L.h[2];
@@ -652,6 +654,7 @@ static int mult_matrix(mgx_ctx* ctx, int mode, mgx_dtype dtype, const void* psi,
         case MGX_GEMM_FP32:
         case MGX_GEMM_TF32:
         case MGX_GEMM_BF16X3:
+        case MGX_GEMM_FP16X3:
             if (dtype != MGX_F32)
                 return fail(MGX_BAD_ARG, "gemm mode %d needs FP32 orbitals", mode);
             if (mode == MGX_GEMM_FP32)

@@ -13,13 +13,18 @@
 // Modes:
 //   TF32   -- the FP32 orbitals feed kind::tf32 directly;
 //   BF16X3 -- each operand is split once into bf16 hi + lo planes
-//             (x = hi + lo to ~2^-17 relative), and every K step issues
-//             hi*hi + hi*lo + lo*hi into the same FP32 accumulator.
+//             (x = hi + lo to 2^-16 relative), and every K step issues
+//             hi*hi + hi*lo + lo*hi into the same FP32 accumulator;
+//   FP16X3 -- the same with fp16 planes of the operand scaled by a power of
+//             two (max |x| 2^s < 2^14, found by a device max reduction):
+//             x 2^s = hi + lo to 2^-22, same cost; the scales come off
+//             exactly in the epilogue or the finishing pass.
 // The K range of a CTA is bounded (at most 512 K blocks) so that the FP32
 // accumulation error stays small; partial tiles meet in FP64.
 #include <cuda.h>
 #include <cudaTypedefs.h>
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -54,14 +59,26 @@ __device__ __forceinline__ uint64_t desc_sw(uint32_t saddr)
     return d;
 }
 
-// kind::tf32 (format 2) or kind::f16 with bf16 operands (format 1), FP32 D,
-// both operands K-major
+// kind::tf32 (KIND 0, operand format 2), kind::f16 with bf16 operands
+// (KIND 1, format 1) or with fp16 operands (KIND 2, format 0); FP32 D, both
+// operands K-major
 template <int KIND>
 __host__ __device__ constexpr uint32_t instr_desc(int M, int N)
 {
-    return (1u << 4) | ((KIND == 0 ? 2u : 1u) << 7) | ((KIND == 0 ? 2u : 1u) << 10)
-           | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+    return (1u << 4) | ((KIND == 0 ? 2u : KIND == 1 ? 1u : 0u) << 7)
+           | ((KIND == 0 ? 2u : KIND == 1 ? 1u : 0u) << 10) | ((uint32_t)(N >> 3) << 17)
+           | ((uint32_t)(M >> 4) << 24);
 }
+
+// Power-of-two scale of an operand for the fp16 split: maxbits is the bit
+// pattern of max |x| (atomicMax on the bits of non-negative floats), up =
+// 2^s with s chosen so that max |x| 2^s < 2^14, down = 2^-s.
+struct ScaleSlot
+{
+    unsigned maxbits;
+    float up;
+    double down;
+};
 
 __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map,
     int c0, int c1, uint64_t* bar)
@@ -165,6 +182,10 @@ struct Params
     // the operand maps are K-blocked 3-D maps (rows of 64 K elements, one
     // contiguous block of all rows per 64 K) instead of row-major 2-D maps
     int blocked = 0;
+    // fp16 split: the products carry the operands' scales; the store
+    // epilogue multiplies by sa->down * sb->down
+    const ScaleSlot* sa = nullptr;
+    const ScaleSlot* sb = nullptr;
 };
 
 // KIND 0: tf32 (NPROD 1); KIND 1: bf16 (NPROD 1 plain, 3 for hi/lo split).
@@ -318,6 +339,13 @@ __global__ void __launch_bounds__(THREADS, 1) gram_kernel(
                 tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)c0, v);
                 if (STORE)
                 {
+                    if (KIND == 2)
+                    {
+                        const float ds = (float)(p.sa->down * p.sb->down);
+#pragma unroll
+                        for (int t = 0; t < 32; t++)
+                            v[t] *= ds;
+                    }
                     if (i < p.nrows)
                     {
                         // each store instruction of the warp covers 32
@@ -386,6 +414,104 @@ __global__ void split_kernel(const float* __restrict__ x, size_t ld, int rows,
             *reinterpret_cast<__nv_bfloat162*>(hi + r * ldo + k) = h2;
             *reinterpret_cast<__nv_bfloat162*>(lo + r * ldo + k) = l2;
         }
+    }
+}
+
+// max |x| over rows x K (leading dimension ld) into slot->maxbits: one
+// block per row, threads along K
+__global__ void __launch_bounds__(256) maxabs_kernel(const float* __restrict__ x, size_t ld,
+    int rows, size_t K, ScaleSlot* slot)
+{
+    __shared__ float red[256];
+    float m = 0.f;
+    for (int r = blockIdx.x; r < rows; r += gridDim.x)
+        for (size_t k = threadIdx.x; k < K; k += blockDim.x)
+            m = fmaxf(m, fabsf(x[(size_t)r * ld + k]));
+    red[threadIdx.x] = m;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1)
+    {
+        if (threadIdx.x < o) red[threadIdx.x] = fmaxf(red[threadIdx.x], red[threadIdx.x + o]);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) atomicMax(&slot->maxbits, __float_as_uint(red[0]));
+}
+
+// max |theta(i, j)| over n rows and ncols columns (column j at th + j * ldt)
+__global__ void __launch_bounds__(256) maxabs_f64_kernel(const double* __restrict__ th, int n,
+    int ldt, int ncols, ScaleSlot* slot)
+{
+    __shared__ float red[256];
+    float m = 0.f;
+    for (int j = blockIdx.x; j < ncols; j += gridDim.x)
+        for (int i = threadIdx.x; i < n; i += blockDim.x)
+            m = fmaxf(m, (float)fabs(th[(size_t)j * ldt + i]));
+    red[threadIdx.x] = m;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1)
+    {
+        if (threadIdx.x < o) red[threadIdx.x] = fmaxf(red[threadIdx.x], red[threadIdx.x + o]);
+        __syncthreads();
+    }
+    // a float that rounded below the double maximum still leaves a margin
+    // of 2x under the 2^15 bound of the scaled values
+    if (threadIdx.x == 0) atomicMax(&slot->maxbits, __float_as_uint(red[0]));
+}
+
+__global__ void set_scale_kernel(ScaleSlot* slot)
+{
+    const float m = __uint_as_float(slot->maxbits);
+    int e         = 0;
+    if (m > 0.f && isfinite(m)) frexpf(m, &e); // m = f 2^e, 0.5 <= f < 1
+    int sc = 14 - e;
+    sc     = max(-100, min(100, sc));
+    slot->up   = ldexpf(1.f, sc);
+    slot->down = ldexp(1., -sc);
+}
+
+// hi / lo split of one value in the plane element type: bf16 (no scale) or
+// fp16 (after the power-of-two scale)
+template <typename E> struct Split;
+template <> struct Split<__nv_bfloat16>
+{
+    __device__ static void go(float x, float, __nv_bfloat16& h, __nv_bfloat16& l)
+    {
+        h = __float2bfloat16_rn(x);
+        l = __float2bfloat16_rn(x - __bfloat162float(h));
+    }
+};
+template <> struct Split<__half>
+{
+    __device__ static void go(float x, float up, __half& h, __half& l)
+    {
+        const float a = x * up;
+        h             = __float2half_rn(a);
+        l             = __float2half_rn(a - __half2float(h));
+    }
+};
+
+// fp32 -> hi + lo planes (bf16, or scaled fp16) in the K-blocked layout
+template <typename E>
+__global__ void split_blocked_e_kernel(const float* __restrict__ x, size_t ld, int rows,
+    size_t K, size_t kblocks, E* __restrict__ hi, E* __restrict__ lo,
+    const ScaleSlot* __restrict__ sc)
+{
+    const float up     = sc ? sc->up : 1.f;
+    const size_t total = (size_t)rows * kblocks * 32; // element pairs
+    for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+         t += (size_t)gridDim.x * blockDim.x)
+    {
+        const size_t per_row = kblocks * 32;
+        const size_t r = t / per_row, k = 2 * (t - r * per_row);
+        float a = 0.f, b = 0.f;
+        if (k < K) a = x[r * ld + k];
+        if (k + 1 < K) b = x[r * ld + k + 1];
+        E h[2], l[2];
+        Split<E>::go(a, up, h[0], l[0]);
+        Split<E>::go(b, up, h[1], l[1]);
+        const size_t o = ((k / 64) * rows + r) * 64 + (k % 64);
+        *reinterpret_cast<uint32_t*>(hi + o) = *reinterpret_cast<const uint32_t*>(h);
+        *reinterpret_cast<uint32_t*>(lo + o) = *reinterpret_cast<const uint32_t*>(l);
     }
 }
 
@@ -472,10 +598,12 @@ __global__ void __launch_bounds__(256) transpose_split_kernel(const float* __res
 // of bank conflicts), and the block's output is two contiguous 16 KB runs.
 constexpr int TB_P = 128;
 
+template <typename E>
 __global__ void __launch_bounds__(256) transpose_split_blocked_kernel(const float* __restrict__ x,
-    size_t ld, int n, size_t p0, int P, __nv_bfloat16* __restrict__ hi,
-    __nv_bfloat16* __restrict__ lo)
+    size_t ld, int n, size_t p0, int P, E* __restrict__ hi, E* __restrict__ lo,
+    const ScaleSlot* __restrict__ sc)
 {
+    const float up = sc ? sc->up : 1.f;
     __shared__ float t[64][TB_P + 1];
     const int kb    = blockIdx.y;
     const int ib    = kb * 64;
@@ -492,25 +620,37 @@ __global__ void __launch_bounds__(256) transpose_split_blocked_kernel(const floa
         const int c = e / 8, g = 8 * (e % 8);
         const size_t pp = pb + c;
         if (pp >= (size_t)P) continue;
-        __align__(16) __nv_bfloat16 h[8], l[8];
+        __align__(16) E h[8], l[8];
 #pragma unroll
         for (int q = 0; q < 8; q++)
-        {
-            const float a = t[g + q][c];
-            h[q] = __float2bfloat16_rn(a);
-            l[q] = __float2bfloat16_rn(a - __bfloat162float(h[q]));
-        }
+            Split<E>::go(t[g + q][c], up, h[q], l[q]);
         const size_t o = ((size_t)kb * P + pp) * 64 + g;
         *reinterpret_cast<uint4*>(hi + o) = *reinterpret_cast<const uint4*>(h);
         *reinterpret_cast<uint4*>(lo + o) = *reinterpret_cast<const uint4*>(l);
     }
 }
 
-// theta columns as K-blocked BF16 hi / lo planes: element (row j, K = i) at
-// ((i / 64) * ncols + j) * 64 + i % 64, zero padded to kblocks * 64.
-__global__ void matrix_split_blocked_kernel(const double* __restrict__ th, int n, int ldt,
-    int ncols, int kblocks, __nv_bfloat16* __restrict__ hi, __nv_bfloat16* __restrict__ lo)
+// theta columns as K-blocked hi / lo planes (bf16, or fp16 after the
+// scale): element (row j, K = i) at ((i / 64) * ncols + j) * 64 + i % 64,
+// zero padded to kblocks * 64; lo is formed from the FP64 value.
+__device__ __forceinline__ void split64(double v, float, __nv_bfloat16& h, __nv_bfloat16& l)
 {
+    h = __float2bfloat16_rn((float)v);
+    l = __float2bfloat16_rn((float)(v - (double)__bfloat162float(h)));
+}
+__device__ __forceinline__ void split64(double v, float up, __half& h, __half& l)
+{
+    const double a = v * (double)up;
+    h              = __float2half_rn((float)a);
+    l              = __float2half_rn((float)(a - (double)__half2float(h)));
+}
+
+template <typename E>
+__global__ void matrix_split_blocked_kernel(const double* __restrict__ th, int n, int ldt,
+    int ncols, int kblocks, E* __restrict__ hi, E* __restrict__ lo,
+    const ScaleSlot* __restrict__ sc)
+{
+    const float up     = sc ? sc->up : 1.f;
     const size_t total = (size_t)ncols * kblocks * 64;
     for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < total;
          t += (size_t)gridDim.x * blockDim.x)
@@ -519,9 +659,7 @@ __global__ void matrix_split_blocked_kernel(const double* __restrict__ th, int n
         const size_t rem = t - kb * (size_t)ncols * 64;
         const size_t j = rem / 64, i = kb * 64 + rem % 64;
         const double v = (i < (size_t)n) ? th[j * ldt + i] : 0.;
-        const __nv_bfloat16 h = __float2bfloat16_rn((float)v);
-        hi[t] = h;
-        lo[t] = __float2bfloat16_rn((float)(v - (double)__bfloat162float(h)));
+        split64(v, up, hi[t], lo[t]);
     }
 }
 
@@ -593,7 +731,7 @@ static int make_map(CUtensorMap* m, const void* base, bool bf16, size_t K,
 // 3-D map over a K-blocked bf16 operand (rows x kblocks * 64): dims
 // (64, rows, kblocks), box (sw / 2, box_rows, 1), SWIZZLE_128B / _64B.
 static int make_map_blocked(CUtensorMap* m, const void* base, size_t rows, size_t kblocks,
-    int box_rows, int sw = 128)
+    int box_rows, int sw = 128, bool half = false)
 {
     auto enc = encoder();
     if (!enc) return fail(MGX_CUDA_ERROR, "cuTensorMapEncodeTiled unavailable");
@@ -602,7 +740,8 @@ static int make_map_blocked(CUtensorMap* m, const void* base, size_t rows, size_
     cuuint64_t strides[2] = { 128, (cuuint64_t)(rows * 128) };
     cuuint32_t box[3]     = { (cuuint32_t)(sw / 2), (cuuint32_t)box_rows, 1 };
     cuuint32_t estr[3]    = { 1, 1, 1 };
-    CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<void*>(base), dims,
+    CUresult r = enc(m, half ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16,
+        3, const_cast<void*>(base), dims,
         strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
         sw == 128 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B,
         CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
@@ -627,15 +766,18 @@ static int launch(const CUtensorMap& a0, const CUtensorMap& a1, const CUtensorMa
     return MGX_OK;
 }
 
-__global__ void finish_kernel(double* C, int n, double vel, int symmetric)
+__global__ void finish_kernel(double* C, int n, double vel, int symmetric,
+    const ScaleSlot* sa, const ScaleSlot* sb)
 {
     const size_t nn = (size_t)n * n;
+    // the fp16 split's scales are powers of two: removing them is exact
+    const double un = (sa && sb) ? sa->down * sb->down : 1.;
     for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < nn;
          t += (size_t)gridDim.x * blockDim.x)
     {
         const int i = (int)(t % n), j = (int)(t / n);
         if (symmetric && i < j) continue;
-        double x = C[t] * vel;
+        double x = (C[t] * un) * vel;
         if (!(fabs(x) > 1.e-14)) x = 0.;
         C[t] = x;
         if (symmetric && i != j) C[(size_t)i * n + j] = x;
@@ -654,8 +796,29 @@ struct Operand
     size_t K = 0, ld = 0;
     int rows = 0;
     int sw   = 128;
-    bool blocked = false; // K-blocked planes (bf16 only)
+    bool blocked = false; // K-blocked planes (bf16 / fp16)
+    bool half    = false; // fp16 planes of the scaled operand
+    const tc::ScaleSlot* scale = nullptr;
 };
+
+bool split_mode(int mode) { return mode == MGX_GEMM_BF16X3 || mode == MGX_GEMM_FP16X3; }
+
+/* the scale slots live after the status word in ctx->tc_err */
+tc::ScaleSlot* scale_slot(mgx_ctx* ctx, int i)
+{
+    return reinterpret_cast<tc::ScaleSlot*>((char*)ctx->tc_err.ptr + 64 + 32 * i);
+}
+
+/* power-of-two scale of the fp32 operand X (rows x K, leading dimension ld) */
+int compute_scale(const void* X, size_t ld, int rows, size_t K, tc::ScaleSlot* slot,
+    cudaStream_t s)
+{
+    tc::maxabs_kernel<<<std::min(rows, 4096), 256, 0, s>>>((const float*)X, ld, rows, K, slot);
+    MGX_LAUNCH_CHECK("maxabs_kernel");
+    tc::set_scale_kernel<<<1, 1, 0, s>>>(slot);
+    MGX_LAUNCH_CHECK("set_scale_kernel");
+    return MGX_OK;
+}
 
 /* K bytes per tile row of the BF16X3 kernels: 64 (SWIZZLE_64B, 4 stages
  * at 128 x 256 tiles; the default, 8 % faster than 128 on the Gram and the
@@ -706,8 +869,8 @@ int rebox(Operand& op, int box_rows)
     if (op.blocked)
     {
         const size_t kb = (op.K + 63) / 64;
-        MGX_TRY(tc::make_map_blocked(&op.m0, op.base0, op.rows, kb, box_rows, op.sw));
-        MGX_TRY(tc::make_map_blocked(&op.m1, op.base1, op.rows, kb, box_rows, op.sw));
+        MGX_TRY(tc::make_map_blocked(&op.m0, op.base0, op.rows, kb, box_rows, op.sw, op.half));
+        MGX_TRY(tc::make_map_blocked(&op.m1, op.base1, op.rows, kb, box_rows, op.sw, op.half));
         return MGX_OK;
     }
     MGX_TRY(tc::make_map(&op.m0, op.base0, op.bf16, op.K, op.rows, op.ld, box_rows, op.sw));
@@ -723,10 +886,36 @@ int rebox(Operand& op, int box_rows)
  * BF16X3 writes the hi / lo planes into `ws`.  Returns the workspace bytes
  * used in *used. */
 int prepare(int mode, const void* X, size_t ld, size_t K, int rows, int box_rows,
-    char* ws, size_t* used, Operand& op, cudaStream_t s)
+    char* ws, size_t* used, Operand& op, cudaStream_t s, const tc::ScaleSlot* sc = nullptr)
 {
     using namespace tc;
     *used = 0;
+    if (mode == MGX_GEMM_FP16X3)
+    {
+        // K-blocked fp16 hi / lo planes of the scaled operand, SWIZZLE_64B
+        op.sw      = 64;
+        op.blocked = true;
+        op.half    = true;
+        op.scale   = sc;
+        const size_t kblocks = (K + 63) / 64;
+        const size_t plane   = kblocks * 64 * (size_t)rows * sizeof(__half);
+        auto* hi             = (__half*)ws;
+        auto* lo             = (__half*)(ws + plane);
+        const int nb = (int)std::min<size_t>((kblocks * 32 * rows + 255) / 256, 1 << 20);
+        split_blocked_e_kernel<__half><<<nb, 256, 0, s>>>((const float*)X, ld, rows, K, kblocks,
+            hi, lo, sc);
+        MGX_LAUNCH_CHECK("split_blocked_e_kernel");
+        MGX_TRY(make_map_blocked(&op.m0, hi, rows, kblocks, box_rows, 64, true));
+        MGX_TRY(make_map_blocked(&op.m1, lo, rows, kblocks, box_rows, 64, true));
+        op.base0 = hi;
+        op.base1 = lo;
+        op.bf16  = true;
+        op.K     = K;
+        op.ld    = kblocks * 64;
+        op.rows  = rows;
+        *used    = 2 * plane;
+        return MGX_OK;
+    }
     if (mode == MGX_GEMM_TF32)
     {
         if (((uintptr_t)X % 16) || ((ld * 4) % 16))
@@ -802,7 +991,7 @@ int run(mgx_ctx* ctx, int mode, const Operand& a, const Operand& b, int nrows, i
     const int ntiles  = (int)tiles.size();
     // K elements per block; a CTA covers at most 32768 K elements (the FP32
     // accumulation bound)
-    const int bk      = (mode == MGX_GEMM_BF16X3) ? a.sw / 2 : 32;
+    const int bk      = split_mode(mode) ? a.sw / 2 : 32;
     const int kblocks = (int)((K + bk - 1) / bk);
     const int kbcap   = 32768 / bk;
     int ksplit = std::max((4 * ctx->sm_count + ntiles - 1) / ntiles, (kblocks + kbcap - 1) / kbcap);
@@ -826,9 +1015,17 @@ int run(mgx_ctx* ctx, int mode, const Operand& a, const Operand& b, int nrows, i
     p.C          = C;
     p.err        = (int*)ctx->tc_err.ptr;
     (void)nrows;
-    if (mode == MGX_GEMM_BF16X3 && (a.sw != b.sw || a.blocked != b.blocked))
+    if (split_mode(mode) && (a.sw != b.sw || a.blocked != b.blocked || a.half != b.half))
         return fail(MGX_BAD_ARG, "operands with different layouts");
     p.blocked = a.blocked ? 1 : 0;
+    p.sa      = a.scale;
+    p.sb      = b.scale;
+    if (mode == MGX_GEMM_FP16X3)
+    {
+        if (BN == 256)
+            return launch<2, 3, 256, 4, false, 64>(a.m0, a.m1, b.m0, b.m1, p, ntiles, ksplit, s);
+        return launch<2, 3, 128, 6, false, 64>(a.m0, a.m1, b.m0, b.m1, p, ntiles, ksplit, s);
+    }
     if (BN == 256)
     {
         if (mode == MGX_GEMM_TF32)
@@ -873,8 +1070,9 @@ int run_sym(mgx_ctx* ctx, int mode, const Operand& a, int n, double* C, size_t K
 int begin(mgx_ctx* ctx, cudaStream_t s)
 {
     MGX_TRY(ctx->tc_tiles.ensure(2 * 64 * 1024 * sizeof(int2)));
-    MGX_TRY(ctx->tc_err.ensure(16));
-    return cuda_check(cudaMemsetAsync(ctx->tc_err.ptr, 0, 16, s), "err reset");
+    // status word, then three scale slots (zeroed: their maxima start at 0)
+    MGX_TRY(ctx->tc_err.ensure(256));
+    return cuda_check(cudaMemsetAsync(ctx->tc_err.ptr, 0, 256, s), "err reset");
 }
 
 int end(mgx_ctx* ctx, cudaStream_t s)
@@ -888,10 +1086,11 @@ int end(mgx_ctx* ctx, cudaStream_t s)
     return MGX_OK;
 }
 
-int finish(double* C, int n, double vel, int symmetric, cudaStream_t s)
+int finish(double* C, int n, double vel, int symmetric, cudaStream_t s,
+    const tc::ScaleSlot* sa = nullptr, const tc::ScaleSlot* sb = nullptr)
 {
     const int nbf = (int)std::min<size_t>(((size_t)n * n + 255) / 256, 4096);
-    tc::finish_kernel<<<nbf, 256, 0, s>>>(C, n, vel, symmetric);
+    tc::finish_kernel<<<nbf, 256, 0, s>>>(C, n, vel, symmetric, sa, sb);
     MGX_LAUNCH_CHECK("finish_kernel");
     return MGX_OK;
 }
@@ -901,7 +1100,8 @@ constexpr int CHUNK = 512;
 
 /* C = A B^T over K with B processed CHUNK rows at a time; A prepared once */
 int product(mgx_ctx* ctx, int mode, const Operand& a, size_t a_used, const void* B,
-    size_t ld, size_t K, int n, double* C, int tile_slot, cudaStream_t s)
+    size_t ld, size_t K, int n, double* C, int tile_slot, cudaStream_t s,
+    const tc::ScaleSlot* sb = nullptr)
 {
     for (int j0 = 0; j0 < n; j0 += CHUNK)
     {
@@ -910,7 +1110,8 @@ int product(mgx_ctx* ctx, int mode, const Operand& a, size_t a_used, const void*
         size_t used = 0;
         const void* Bj = (const char*)B + (size_t)j0 * ld * 4;
         const int BN = tile_n(nc);
-        MGX_TRY(prepare(mode, Bj, ld, K, nc, BN, (char*)ctx->tc_split.ptr + a_used, &used, b, s));
+        MGX_TRY(prepare(mode, Bj, ld, K, nc, BN, (char*)ctx->tc_split.ptr + a_used, &used, b, s,
+            sb));
         MGX_TRY(run(ctx, mode, a, b, n, nc, 0, C + (size_t)j0 * n, n, K, tile_slot, BN, s));
     }
     return MGX_OK;
@@ -926,14 +1127,27 @@ int gram_tcgen05(mgx_ctx* ctx, int mode, const void* A, const void* B, size_t ld
     MGX_TRY(ctx->tc_split.ensure(a_bytes + b_bytes + 256));
     MGX_TRY(begin(ctx, s));
     MGX_TRY(cuda_check(cudaMemsetAsync(C, 0, (size_t)n * n * sizeof(double), s), "C zero"));
+    tc::ScaleSlot* sa = nullptr;
+    tc::ScaleSlot* sb = nullptr;
+    if (mode == MGX_GEMM_FP16X3)
+    {
+        sa = scale_slot(ctx, 0);
+        MGX_TRY(compute_scale(A, ld, n, K, sa, s));
+        sb = sa;
+        if (!same)
+        {
+            sb = scale_slot(ctx, 1);
+            MGX_TRY(compute_scale(B, ld, n, K, sb, s));
+        }
+    }
     Operand a;
     size_t used = 0;
-    MGX_TRY(prepare(mode, A, ld, K, n, tc::BM, (char*)ctx->tc_split.ptr, &used, a, s));
+    MGX_TRY(prepare(mode, A, ld, K, n, tc::BM, (char*)ctx->tc_split.ptr, &used, a, s, sa));
     if (same)
         MGX_TRY(run_sym(ctx, mode, a, n, C, K, 0, s));
     else
-        MGX_TRY(product(ctx, mode, a, ((used + 255) / 256) * 256, B, ld, K, n, C, 0, s));
-    MGX_TRY(finish(C, n, vel, same ? 1 : 0, s));
+        MGX_TRY(product(ctx, mode, a, ((used + 255) / 256) * 256, B, ld, K, n, C, 0, s, sb));
+    MGX_TRY(finish(C, n, vel, same ? 1 : 0, s, sa, sb));
     return end(ctx, s);
 }
 
@@ -947,13 +1161,22 @@ int gram_hmat_tcgen05(mgx_ctx* ctx, int mode, const void* psi, const void* hpsi,
     MGX_TRY(begin(ctx, s));
     MGX_TRY(cuda_check(cudaMemsetAsync(S, 0, (size_t)n * n * sizeof(double), s), "S zero"));
     MGX_TRY(cuda_check(cudaMemsetAsync(H, 0, (size_t)n * n * sizeof(double), s), "H zero"));
+    tc::ScaleSlot* sa = nullptr;
+    tc::ScaleSlot* sb = nullptr;
+    if (mode == MGX_GEMM_FP16X3)
+    {
+        sa = scale_slot(ctx, 0);
+        sb = scale_slot(ctx, 1);
+        MGX_TRY(compute_scale(psi, ld, n, K, sa, s));
+        MGX_TRY(compute_scale(hpsi, ld, n, K, sb, s));
+    }
     Operand a;
     size_t used = 0;
-    MGX_TRY(prepare(mode, psi, ld, K, n, tc::BM, (char*)ctx->tc_split.ptr, &used, a, s));
+    MGX_TRY(prepare(mode, psi, ld, K, n, tc::BM, (char*)ctx->tc_split.ptr, &used, a, s, sa));
     MGX_TRY(run_sym(ctx, mode, a, n, S, K, 0, s));
-    MGX_TRY(product(ctx, mode, a, ((used + 255) / 256) * 256, hpsi, ld, K, n, H, 1, s));
-    MGX_TRY(finish(S, n, vel, 1, s));
-    MGX_TRY(finish(H, n, vel, 0, s));
+    MGX_TRY(product(ctx, mode, a, ((used + 255) / 256) * 256, hpsi, ld, K, n, H, 1, s, sb));
+    MGX_TRY(finish(S, n, vel, 1, s, sa, sa));
+    MGX_TRY(finish(H, n, vel, 0, s, sa, sb));
     return end(ctx, s);
 }
 
@@ -969,7 +1192,8 @@ int psi_theta_tcgen05(mgx_ctx* ctx, int mode, const float* psi, size_t ld, size_
     cudaStream_t s)
 {
     using namespace tc;
-    const bool bf         = (mode == MGX_GEMM_BF16X3);
+    const bool half       = (mode == MGX_GEMM_FP16X3);
+    const bool bf         = split_mode(mode);
     const size_t esz      = bf ? 2 : 4;
     const int nplanes     = bf ? 2 : 1;
     const size_t ldk      = bf ? ((n + 63) / 64) * 64 : ((n + 31) / 32) * 32;
@@ -991,13 +1215,28 @@ int psi_theta_tcgen05(mgx_ctx* ctx, int mode, const float* psi, size_t ld, size_
     void* blo = ws + b_plane;
     void* ahi = ws + b_bytes;
     void* alo = ws + b_bytes + a_plane;
-    const bool blk = bf && blocked_planes();
+    const bool blk = half || (bf && blocked_planes());
     const int nkb  = (int)(ldk / 64);
+    ScaleSlot* sa  = nullptr;
+    ScaleSlot* sb  = nullptr;
+    if (half)
+    {
+        sa = scale_slot(ctx, 0);
+        sb = scale_slot(ctx, 2);
+        MGX_TRY(compute_scale(psi, ld, n, npts, sa, s));
+        maxabs_f64_kernel<<<std::min(ncols, 4096), 256, 0, s>>>(theta, n, ldt, ncols, sb);
+        MGX_LAUNCH_CHECK("maxabs_f64_kernel");
+        set_scale_kernel<<<1, 1, 0, s>>>(sb);
+        MGX_LAUNCH_CHECK("set_scale_kernel");
+    }
     {
         const int nb = (int)std::min<size_t>((ncols * ldk + 255) / 256, 1 << 16);
-        if (blk)
-            matrix_split_blocked_kernel<<<nb, 256, 0, s>>>(theta, n, ldt, ncols, nkb,
-                (__nv_bfloat16*)bhi, (__nv_bfloat16*)blo);
+        if (half)
+            matrix_split_blocked_kernel<__half><<<nb, 256, 0, s>>>(theta, n, ldt, ncols, nkb,
+                (__half*)bhi, (__half*)blo, sb);
+        else if (blk)
+            matrix_split_blocked_kernel<__nv_bfloat16><<<nb, 256, 0, s>>>(theta, n, ldt, ncols, nkb,
+                (__nv_bfloat16*)bhi, (__nv_bfloat16*)blo, nullptr);
         else if (bf)
             matrix_split_kernel<true><<<nb, 256, 0, s>>>(theta, n, ldt, ncols, bhi, blo, ldk);
         else
@@ -1005,12 +1244,12 @@ int psi_theta_tcgen05(mgx_ctx* ctx, int mode, const float* psi, size_t ld, size_
         MGX_LAUNCH_CHECK("matrix_split_kernel");
     }
     const int BN = (ncols > 128) ? 256 : 128;
-    const int sw = bf ? bf16_swizzle() : 128;
+    const int sw = half ? 64 : bf ? bf16_swizzle() : 128;
     CUtensorMap mb0, mb1, ma0, ma1;
     if (blk)
     {
-        MGX_TRY(make_map_blocked(&mb0, bhi, ncols, nkb, BN, sw));
-        MGX_TRY(make_map_blocked(&mb1, blo, ncols, nkb, BN, sw));
+        MGX_TRY(make_map_blocked(&mb0, bhi, ncols, nkb, BN, sw, half));
+        MGX_TRY(make_map_blocked(&mb1, blo, ncols, nkb, BN, sw, half));
     }
     else
     {
@@ -1027,11 +1266,15 @@ int psi_theta_tcgen05(mgx_ctx* ctx, int mode, const float* psi, size_t ld, size_
         if (blk)
         {
             dim3 tg((Pc + TB_P - 1) / TB_P, nkb);
-            transpose_split_blocked_kernel<<<tg, 256, 0, s>>>(psi, ld, n, p0, Pc,
-                (__nv_bfloat16*)ahi, (__nv_bfloat16*)alo);
+            if (half)
+                transpose_split_blocked_kernel<__half><<<tg, 256, 0, s>>>(psi, ld, n, p0, Pc,
+                    (__half*)ahi, (__half*)alo, sa);
+            else
+                transpose_split_blocked_kernel<__nv_bfloat16><<<tg, 256, 0, s>>>(psi, ld, n, p0,
+                    Pc, (__nv_bfloat16*)ahi, (__nv_bfloat16*)alo, nullptr);
             MGX_LAUNCH_CHECK("transpose_split_blocked_kernel");
-            MGX_TRY(make_map_blocked(&ma0, ahi, Pc, nkb, BM, sw));
-            MGX_TRY(make_map_blocked(&ma1, alo, Pc, nkb, BM, sw));
+            MGX_TRY(make_map_blocked(&ma0, ahi, Pc, nkb, BM, sw, half));
+            MGX_TRY(make_map_blocked(&ma1, alo, Pc, nkb, BM, sw, half));
         }
         else
         {
@@ -1062,8 +1305,17 @@ int psi_theta_tcgen05(mgx_ctx* ctx, int mode, const float* psi, size_t ld, size_
         p.nrows      = Pc;
         p.ntj        = ntj;
         p.blocked    = blk ? 1 : 0;
+        p.sa         = sa;
+        p.sb         = sb;
         const int ntiles = ((Pc + BM - 1) / BM) * ntj;
-        if (BN == 256)
+        if (half)
+        {
+            if (BN == 256)
+                MGX_TRY((launch<2, 3, 256, 4, true, 64>(ma0, ma1, mb0, mb1, p, ntiles, 1, s)));
+            else
+                MGX_TRY((launch<2, 3, 128, 6, true, 64>(ma0, ma1, mb0, mb1, p, ntiles, 1, s)));
+        }
+        else if (BN == 256)
         {
             if (bf && sw == 64)
                 MGX_TRY((launch<1, 3, 256, 4, true, 64>(ma0, ma1, mb0, mb1, p, ntiles, 1, s)));

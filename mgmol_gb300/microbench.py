@@ -19,7 +19,7 @@ from . import capi, synth
 from .sweep import vcycle_bytes
 
 GEMM = {"fp64": capi.GEMM_FP64, "fp32": capi.GEMM_FP32, "tf32": capi.GEMM_TF32,
-        "bf16x3": capi.GEMM_BF16X3}
+        "bf16x3": capi.GEMM_BF16X3, "fp16x3": capi.GEMM_FP16X3}
 
 
 def _time(fn, warmup, reps):

@@ -6,6 +6,7 @@ Error bars, relative to max |reference|:
   FP64 mode, FP32 orbitals (FP64 accumulation, FP32 result)   <= 3e-7
   FP32 CUDA-core mode (FP32 FMA)                              <= 2e-5
   BF16X3 tensor cores                                         <= 6e-5
+  FP16X3 tensor cores (scaled fp16 hi / lo, 2^-22 split)      <= 3e-6
   TF32 tensor cores                                           <= 2e-3
 The BF16X3 bar: each operand is hi + lo with |x - hi - lo| <= 2^-16 |x|
 (bf16 unit roundoff 2^-8, twice), so one product carries up to ~2^-15
@@ -24,7 +25,8 @@ from mgmol_gb300 import capi, synth
 
 pytestmark = pytest.mark.gpu
 
-TOL = {capi.GEMM_FP32: 2e-5, capi.GEMM_TF32: 2e-3, capi.GEMM_BF16X3: 6e-5}
+TOL = {capi.GEMM_FP32: 2e-5, capi.GEMM_TF32: 2e-3, capi.GEMM_BF16X3: 6e-5,
+       capi.GEMM_FP16X3: 3e-6}
 
 
 def _dev(a, dt=np.float64):
@@ -72,7 +74,8 @@ def test_mult_matrix_fp32_orbitals_fp64_accumulation():
     assert rel_err(out, ref) < 3e-7
 
 
-@pytest.mark.parametrize("mode", [capi.GEMM_FP32, capi.GEMM_TF32, capi.GEMM_BF16X3])
+@pytest.mark.parametrize("mode", [capi.GEMM_FP32, capi.GEMM_TF32, capi.GEMM_BF16X3,
+                                  capi.GEMM_FP16X3])
 @pytest.mark.parametrize("grid,nf", [((16, 16, 16), 64), ((15, 13, 11), 37), ((32, 24, 20), 200),
                                      ((20, 20, 20), 300)])
 def test_mult_matrix_fp32_modes(mode, grid, nf):
@@ -122,7 +125,8 @@ def test_residual_fp64(apply_B, grid, nf):
     assert rel_err(hd.cpu().numpy(), ref) < TOL_F64
 
 
-@pytest.mark.parametrize("mode", [capi.GEMM_FP64, capi.GEMM_FP32, capi.GEMM_BF16X3])
+@pytest.mark.parametrize("mode", [capi.GEMM_FP64, capi.GEMM_FP32, capi.GEMM_BF16X3,
+                                  capi.GEMM_FP16X3])
 def test_residual_fp32(mode):
     grid, nf = (16, 16, 16), 130
     ll = tuple(x * 0.35 for x in grid)

@@ -3,6 +3,7 @@
 Error bars, relative to max |S| (resp. max |H|):
   TF32   (10-bit mantissa products, FP32 accumulation)        <= 2e-3
   BF16X3 (hi*hi + hi*lo + lo*hi, FP32 accumulation)           <= 2e-5
+  FP16X3 (scaled fp16 hi / lo, split error 2^-22)             <= 2e-6
 and the FP32 CUDA-core mode for comparison <= 1e-5.
 """
 import numpy as np
@@ -15,14 +16,14 @@ from mgmol_gb300 import capi, synth
 
 pytestmark = pytest.mark.gpu
 
-TOL = {capi.GEMM_TF32: 2e-3, capi.GEMM_BF16X3: 2e-5}
+TOL = {capi.GEMM_TF32: 2e-3, capi.GEMM_BF16X3: 2e-5, capi.GEMM_FP16X3: 2e-6}
 
 
 def _dev(a, dt=np.float32):
     return torch.from_numpy(np.ascontiguousarray(a.astype(dt))).cuda()
 
 
-@pytest.mark.parametrize("mode", [capi.GEMM_TF32, capi.GEMM_BF16X3])
+@pytest.mark.parametrize("mode", [capi.GEMM_TF32, capi.GEMM_BF16X3, capi.GEMM_FP16X3])
 @pytest.mark.parametrize("grid,nf", [((16, 16, 16), 64), ((32, 24, 20), 200), ((20, 20, 20), 130),
                                      ((64, 32, 32), 300)])
 def test_tc_gram_hmat(mode, grid, nf):
@@ -48,7 +49,7 @@ def test_tc_gram_odd_sizes():
     psi, _, _ = synth.gaussian_orbitals(grid, ll, 37, 2)
     ctx = capi.Context(grid, ll)
     p32 = psi.astype(np.float32)
-    for mode in (capi.GEMM_TF32, capi.GEMM_BF16X3):
+    for mode in (capi.GEMM_TF32, capi.GEMM_BF16X3, capi.GEMM_FP16X3):
         S = ctx.gram(_dev(p32), mode=mode).cpu().numpy()
         assert rel_err(S, O.gram(p32, ctx.vel)) < TOL[mode]
 
