@@ -766,8 +766,8 @@ struct VCycle
             p.n[i] = lev[l].n[i];
         p.mask = mask_slice(masks, l, f0);
         p.err  = err;
-        return stencil_launch(OP_JACOBI, l == 0 ? lap_type : 1, dtype, dtype, p,
-            lev[l], jf[l], nf, s);
+        return stencil_launch(p.upd ? OP_JACOBI_UPD : OP_JACOBI, l == 0 ? lap_type : 1, dtype,
+            dtype, p, lev[l], jf[l], nf, s);
     }
 
     // returns the buffer index holding the result at level l
@@ -777,7 +777,8 @@ struct VCycle
         const int ncycl = (l == L) ? 4 : 2;
         for (int it = 0; it < ncycl; it++)
         {
-            const int st = jacobi(l, cur, (it == ncycl - 1) && (l < L));
+            // without coarse levels the last of these sweeps is the final one
+            const int st = jacobi(l, cur, (it == ncycl - 1) && (l < L), (l == L) && (it == ncycl - 1));
             if (st != MGX_OK) return -st - 1;
             cur ^= 1;
         }

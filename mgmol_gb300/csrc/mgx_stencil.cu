@@ -388,13 +388,13 @@ __global__ void __launch_bounds__(256) plane_kernel(PlaneParams p, DevCoef<T> c)
     }
 
     T* __restrict__ outp     = reinterpret_cast<T*>(p.out) + (size_t)f * p.ldo;
-    T* __restrict__ updp     = (OP == OP_JACOBI && p.upd)
+    T* __restrict__ updp     = (OP == OP_JACOBI_UPD)
                                    ? reinterpret_cast<T*>(p.upd) + (size_t)f * p.ldupd
                                    : nullptr;
     const T ualpha           = (T)p.upd_alpha;
     T* __restrict__ wp       = p.w ? reinterpret_cast<T*>(p.w) + (size_t)f * p.ldw : nullptr;
     const T* __restrict__ fp = p.f ? reinterpret_cast<const T*>(p.f) + (size_t)f * p.ldf : nullptr;
-    constexpr bool POINTWISE = (OP == OP_JACOBI) || (OP == OP_HPSI_V) || (OP == OP_RHS_SUB);
+    constexpr bool POINTWISE = is_jacobi(OP) || (OP == OP_HPSI_V) || (OP == OP_RHS_SUB);
 
     // pv: the pointwise operand at the emitted point (f for Jacobi, V for
     // V psi, g for B u - g), loaded before the plane wait so that its
@@ -406,7 +406,7 @@ __global__ void __launch_bounds__(256) plane_kernel(PlaneParams p, DevCoef<T> c)
         T r              = lap;
         if (OP == OP_HPSI_V) r = lap + (T)((TV)ucen * (TV)pv);
         if (OP == OP_RHS_SUB) r = lap - pv;
-        if (OP == OP_JACOBI)
+        if (is_jacobi(OP))
         {
             T w = lap - pv;
             r   = ucen - c.jf * w;
@@ -417,7 +417,7 @@ __global__ void __launch_bounds__(256) plane_kernel(PlaneParams p, DevCoef<T> c)
             }
             if (wp != nullptr) wp[idx] = w;
         }
-        if (OP == OP_JACOBI && updp != nullptr)
+        if (OP == OP_JACOBI_UPD)
             updp[idx] = updp[idx] + ualpha * r;
         else
             outp[idx] = r;
@@ -597,7 +597,7 @@ __global__ void __launch_bounds__(256) plane_vec_kernel(PlaneParams p, DevCoef<T
     const int x0      = tile_x * p.xc;
     const int xcount  = min(p.xc, nx - x0);
     const int nplanes = xcount + 2;
-    const bool scaled = (OP == OP_JACOBI) && (p.gamma_in != 0.);
+    const bool scaled = is_jacobi(OP) && (p.gamma_in != 0.);
     const T gam       = (T)p.gamma_in;
 
     const size_t stage_elems = (size_t)rows * nz;
@@ -687,13 +687,13 @@ __global__ void __launch_bounds__(256) plane_vec_kernel(PlaneParams p, DevCoef<T
             A1[k][v] = B1[k][v] = B2[k][v] = U1[k][v] = (T)0;
 
     T* __restrict__ outp     = reinterpret_cast<T*>(p.out) + (size_t)f * p.ldo;
-    T* __restrict__ updp     = (OP == OP_JACOBI && p.upd)
+    T* __restrict__ updp     = (OP == OP_JACOBI_UPD)
                                    ? reinterpret_cast<T*>(p.upd) + (size_t)f * p.ldupd
                                    : nullptr;
     const T ualpha           = (T)p.upd_alpha;
     T* __restrict__ wp       = p.w ? reinterpret_cast<T*>(p.w) + (size_t)f * p.ldw : nullptr;
     const T* __restrict__ fp = p.f ? reinterpret_cast<const T*>(p.f) + (size_t)f * p.ldf : nullptr;
-    constexpr bool POINTWISE = (OP == OP_JACOBI) || (OP == OP_HPSI_V) || (OP == OP_RHS_SUB);
+    constexpr bool POINTWISE = is_jacobi(OP) || (OP == OP_HPSI_V) || (OP == OP_RHS_SUB);
     const T c12 = (T)(1. / 12.), c05 = (T)0.5;
 
     bool ok    = true;
@@ -704,13 +704,18 @@ __global__ void __launch_bounds__(256) plane_vec_kernel(PlaneParams p, DevCoef<T
         const bool emit = (i >= 2);
         const size_t xoff = (size_t)(emit ? xe : 0) * ny * nz;
         V4 pv[NG];
+        V4 uv[NG]; // OP_JACOBI_UPD: the block being updated, fetched with pv
         if (POINTWISE && emit && !scaled)
         {
 #pragma unroll
             for (int k = 0; k < NG; k++)
                 if (val[k])
+                {
                     pv[k] = *reinterpret_cast<const V4*>(
                         (OP != OP_HPSI_V ? fp : vbase) + xoff + goff[k]);
+                    if (OP == OP_JACOBI_UPD)
+                        uv[k] = *reinterpret_cast<const V4*>(updp + xoff + goff[k]);
+                }
         }
         ok = ok && mbar_wait(bars + (i % S), (uint32_t)((i / S) & 1));
         if (ok) waited = i;
@@ -791,7 +796,7 @@ __global__ void __launch_bounds__(256) plane_vec_kernel(PlaneParams p, DevCoef<T
                     T r    = lap;
                     if (OP == OP_HPSI_V) r = lap + ucen * VH::get(pv[k], v);
                     if (OP == OP_RHS_SUB) r = lap - VH::get(pv[k], v);
-                    if (OP == OP_JACOBI)
+                    if (is_jacobi(OP))
                     {
                         T fv;
                         if (scaled)
@@ -822,9 +827,11 @@ __global__ void __launch_bounds__(256) plane_vec_kernel(PlaneParams p, DevCoef<T
             }
             if (emit)
             {
-                if (OP == OP_JACOBI && updp != nullptr)
+                if (OP == OP_JACOBI_UPD)
                 {
-                    V4 q = *reinterpret_cast<const V4*>(updp + xoff + goff[k]);
+                    // the sweep that starts from gamma f (scaled) is never the
+                    // last one, so uv was fetched above
+                    V4 q = uv[k];
 #pragma unroll
                     for (int v = 0; v < VEC; v++)
                         VH::set(q, v, VH::get(q, v) + ualpha * VH::get(res, v));
@@ -832,7 +839,7 @@ __global__ void __launch_bounds__(256) plane_vec_kernel(PlaneParams p, DevCoef<T
                 }
                 else
                     *reinterpret_cast<V4*>(outp + xoff + goff[k]) = res;
-                if (OP == OP_JACOBI && wp != nullptr)
+                if (is_jacobi(OP) && wp != nullptr)
                     *reinterpret_cast<V4*>(wp + xoff + goff[k]) = wres;
             }
         }
@@ -883,7 +890,7 @@ __global__ void __launch_bounds__(256) direct_kernel(PlaneParams p, DevCoef<T> c
         };
         T wres = (T)0;
         T r    = PointOp<T, TV, LAP, OP, R>::apply(p, c, at, vat, f, idx, &wres);
-        if (OP == OP_JACOBI)
+        if (is_jacobi(OP))
         {
             if (p.mask.state != nullptr)
             {
@@ -893,7 +900,7 @@ __global__ void __launch_bounds__(256) direct_kernel(PlaneParams p, DevCoef<T> c
             if (p.w != nullptr)
                 reinterpret_cast<T*>(p.w)[(size_t)f * p.ldw + idx] = wres;
         }
-        if (OP == OP_JACOBI && p.upd != nullptr)
+        if (OP == OP_JACOBI_UPD)
         {
             T* u = reinterpret_cast<T*>(p.upd) + (size_t)f * p.ldupd + idx;
             *u   = *u + (T)p.upd_alpha * r;
@@ -1095,6 +1102,8 @@ int stencil_launch(int op, int lap_type, int dtype, int v_dtype,
                 return dispatch_lap<double, double, OP_LAP>(lap_type, p, c, nfunc, stream, force_direct);
             case OP_JACOBI:
                 return dispatch_lap<double, double, OP_JACOBI>(lap_type, p, c, nfunc, stream, force_direct);
+            case OP_JACOBI_UPD:
+                return dispatch_lap<double, double, OP_JACOBI_UPD>(lap_type, p, c, nfunc, stream, force_direct);
             case OP_HPSI_B:
                 if (v_dtype == MGX_F64)
                     return launch_t<double, double, 0, OP_HPSI_B, 1>(p, c, nfunc, stream, force_direct);
@@ -1114,6 +1123,8 @@ int stencil_launch(int op, int lap_type, int dtype, int v_dtype,
                 return dispatch_lap<float, float, OP_LAP>(lap_type, p, c, nfunc, stream, force_direct);
             case OP_JACOBI:
                 return dispatch_lap<float, float, OP_JACOBI>(lap_type, p, c, nfunc, stream, force_direct);
+            case OP_JACOBI_UPD:
+                return dispatch_lap<float, float, OP_JACOBI_UPD>(lap_type, p, c, nfunc, stream, force_direct);
             case OP_HPSI_B:
                 if (v_dtype == MGX_F64)
                     return launch_t<float, double, 0, OP_HPSI_B, 1>(p, c, nfunc, stream, force_direct);

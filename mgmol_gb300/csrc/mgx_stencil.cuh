@@ -18,10 +18,12 @@ enum StencilOp
     OP_HPSI_V = 2, // out = -Lap u + V u
     OP_JACOBI = 3, // w = -Lap u - f ; out = mask(u - jf w) ; w_out = mask(w)
     OP_RHS    = 4, // out = B u
-    OP_RHS_SUB = 5 // out = B u - g (g pointwise, passed as f)
+    OP_RHS_SUB = 5, // out = B u - g (g pointwise, passed as f)
+    OP_JACOBI_UPD = 6 // OP_JACOBI whose result r is added into upd: upd += upd_alpha r
 };
 
 __host__ __device__ constexpr bool is_rhs_op(int op) { return op == OP_RHS || op == OP_RHS_SUB; }
+__host__ __device__ constexpr bool is_jacobi(int op) { return op == OP_JACOBI || op == OP_JACOBI_UPD; }
 
 /* Localization masks of one level in box form: for function f, values of
  * the box starting at (box[6f], box[6f+1], box[6f+2]) (periodic) with
@@ -57,9 +59,10 @@ struct PlaneParams
     // iterate is u = gamma_in * f (the first sweep of the V-cycle started
     // from gamma * res, src/OrbitalsPreconditioning.cc:102-107)
     double gamma_in = 0.;
-    // OP_JACOBI only: when set, the sweep's result r is not stored to out;
+    // OP_JACOBI_UPD only: the sweep's result r is not stored to out;
     // instead upd += upd_alpha * r (the orbital update of an ABPG step
-    // fused into the last smoothing sweep of the preconditioner)
+    // fused into the last smoothing sweep of the preconditioner).  A
+    // separate operator so that the plain sweeps compile without it.
     void* upd        = nullptr;
     size_t ldupd     = 0;
     double upd_alpha = 0.;

@@ -152,6 +152,13 @@ def test_precond_update_fused(dt, tol):
     got = _dev(psi, dt)
     ctx.precond_update(r, got, 0.5, 0, 2, 0.3)
     assert rel_err(got.cpu().numpy(), ref.cpu().numpy()) < tol
+    # without coarse levels (the update rides on the last coarsest-level sweep)
+    c0 = ctx.precond_mg(r, 0, 0, 0.3)
+    ref0 = _dev(psi, dt)
+    capi.axpy(0.5, c0, ref0)
+    got0 = _dev(psi, dt)
+    ctx.precond_update(r, got0, 0.5, 0, 0, 0.3)
+    assert rel_err(got0.cpu().numpy(), ref0.cpu().numpy()) < tol
     # with a caller scratch block for the fine-level iterate
     got = _dev(psi, dt)
     ctx.precond_update(r, got, 0.5, 0, 2, 0.3, work=torch.empty_like(r))

@@ -6,7 +6,8 @@ Error bars, relative to max |reference|:
   FP64 mode, FP32 orbitals (FP64 accumulation, FP32 result)   <= 3e-7
   FP32 CUDA-core mode (FP32 FMA)                              <= 2e-5
   BF16X3 tensor cores                                         <= 6e-5
-  FP16X3 tensor cores (scaled fp16 hi / lo, 2^-22 split)      <= 3e-6
+  FP16X3 tensor cores (scaled fp16 hi / lo, 2^-22 split; the
+  FP32 accumulation sets the bar)                             <= 5e-6
   TF32 tensor cores                                           <= 2e-3
 The BF16X3 bar: each operand is hi + lo with |x - hi - lo| <= 2^-16 |x|
 (bf16 unit roundoff 2^-8, twice), so one product carries up to ~2^-15
@@ -26,7 +27,7 @@ from mgmol_gb300 import capi, synth
 pytestmark = pytest.mark.gpu
 
 TOL = {capi.GEMM_FP32: 2e-5, capi.GEMM_TF32: 2e-3, capi.GEMM_BF16X3: 6e-5,
-       capi.GEMM_FP16X3: 3e-6}
+       capi.GEMM_FP16X3: 5e-6}
 
 
 def _dev(a, dt=np.float64):
