@@ -28,7 +28,7 @@ sys.path.insert(0, ROOT)
 CONFIGS = {
     # name: grid, h, nfunc, wells, lap_type, seed
     "c5": dict(n=(192, 192, 192), h=0.25, nfunc=2048, wells=64, seed=1005,
-               workload="full sweep at scale: 2048 orbitals, 192^3, h=0.25, Mehrstellen, FP32 orbitals"),
+               workload="full sweep at scale: 2048 orbitals, 192^3, h=0.25, Mehrstellen"),
     "c1": dict(n=(64, 64, 64), h=0.35, nfunc=64, wells=8, seed=1001,
                workload="plain FP64 case: 64 orbitals, 64^3, h=0.35, Mehrstellen"),
     "c5_256": dict(n=(192, 192, 192), h=0.25, nfunc=256, wells=64, seed=1005,
