@@ -538,23 +538,38 @@ __global__ void __launch_bounds__(256) trinv_diag_kernel(const double* L, int n,
  * below lose L[below, k] Y_k (one (n - k) x ncols x 64 product, parallel
  * over all of Y's columns) */
 static int forward_subst(int n, const double* L, const double* X, double* Y, int ncols,
-    double* panel, cudaStream_t s)
+    double* panel, cudaStream_t s, bool lower_rhs = false)
 {
     const int nbk = (n + NB - 1) / NB;
     for (int kb = 0; kb < nbk; kb++)
     {
         const int k0 = kb * NB, nb = std::min(NB, n - k0);
-        MGX_TRY(dgemm(false, false, nb, ncols, nb, 1., X + (size_t)k0 * n + k0, n, Y + k0, n,
+        // a lower-triangular right-hand side (the identity) keeps Y lower
+        // triangular: columns past this block row are still zero
+        const int nc = lower_rhs ? std::min(ncols, k0 + nb) : ncols;
+        MGX_TRY(dgemm(false, false, nb, nc, nb, 1., X + (size_t)k0 * n + k0, n, Y + k0, n,
             0., panel, NB, 0, s));
-        copy_panel_kernel<<<std::min(1024, (nb * ncols + 255) / 256), 256, 0, s>>>(panel, NB,
-            Y + k0, n, nb, ncols);
+        copy_panel_kernel<<<std::min(1024, (nb * nc + 255) / 256), 256, 0, s>>>(panel, NB,
+            Y + k0, n, nb, nc);
         MGX_LAUNCH_CHECK("copy_panel_kernel");
         const int m = n - k0 - nb;
         if (m > 0)
-            MGX_TRY(dgemm(false, false, m, ncols, nb, -1., L + (size_t)k0 * n + k0 + nb, n,
+            MGX_TRY(dgemm(false, false, m, nc, nb, -1., L + (size_t)k0 * n + k0 + nb, n,
                 Y + k0, n, 1., Y + k0 + nb, n, 0, s));
     }
     return MGX_OK;
+}
+
+// upper triangle <- lower triangle
+__global__ void mirror_lower_kernel(double* A, int n)
+{
+    const size_t nn = (size_t)n * n;
+    for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < nn;
+         t += (size_t)gridDim.x * blockDim.x)
+    {
+        const size_t i = t % n, j = t / n;
+        if (i < j) A[t] = A[i * n + j];
+    }
 }
 
 __global__ void identity_kernel(double* X, int n)
@@ -585,11 +600,13 @@ int inverse_from_cholesky(mgx_ctx* ctx, int n, const double* L, double* Sinv,
     const int nb = (int)std::min<size_t>(((size_t)n * n + 255) / 256, 4096);
     identity_kernel<<<nb, 256, 0, s>>>(Sinv, n);
     MGX_LAUNCH_CHECK("identity_kernel");
-    MGX_TRY(forward_subst(n, L, X, Sinv, n, panel, s));
-    // X <- L^-1, then S^-1 = X^T X
+    MGX_TRY(forward_subst(n, L, X, Sinv, n, panel, s, true));
+    // X <- L^-1, then the lower triangle of S^-1 = X^T X, mirrored
     MGX_TRY(cuda_check(cudaMemcpyAsync(X, Sinv, (size_t)n * n * 8, cudaMemcpyDeviceToDevice, s),
         "L^-1 copy"));
-    MGX_TRY(dgemm(true, false, n, n, n, 1., X, n, X, n, 0., Sinv, n, 0, s));
+    MGX_TRY(dgemm(true, false, n, n, n, 1., X, n, X, n, 0., Sinv, n, 1, s));
+    mirror_lower_kernel<<<nb, 256, 0, s>>>(Sinv, n);
+    MGX_LAUNCH_CHECK("mirror_lower_kernel");
     return MGX_OK;
 }
 

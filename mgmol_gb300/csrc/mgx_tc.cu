@@ -490,59 +490,54 @@ template <> struct Split<__half>
     }
 };
 
-// fp32 -> hi + lo planes (bf16, or scaled fp16) in the K-blocked layout
+// fp32 -> hi + lo planes (bf16, or scaled fp16) in the K-blocked layout:
+// element (r, k) at ((k / 64) * rows + r) * 64 + k % 64, so that the
+// 64-element K slice of every row of a block is one contiguous run (a TMA
+// box of 128 rows is 16 KB of consecutive memory instead of 128 rows a full
+// row stride apart); K is padded with zeros to kblocks * 64.  8 consecutive
+// K elements per thread: two 16-byte loads (when vec4) and one 16-byte
+// store per plane; the 8 threads of a row's K block cover its 256 input and
+// 128 output bytes.
 template <typename E>
-__global__ void split_blocked_e_kernel(const float* __restrict__ x, size_t ld, int rows,
-    size_t K, size_t kblocks, E* __restrict__ hi, E* __restrict__ lo,
-    const ScaleSlot* __restrict__ sc)
+__global__ void __launch_bounds__(256) split8_kernel(const float* __restrict__ x, size_t ld,
+    int rows, size_t K, size_t kblocks, E* __restrict__ hi, E* __restrict__ lo,
+    const ScaleSlot* __restrict__ sc, int vec4)
 {
     const float up     = sc ? sc->up : 1.f;
-    const size_t total = (size_t)rows * kblocks * 32; // element pairs
+    const size_t total = (size_t)rows * kblocks * 8;
     for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < total;
          t += (size_t)gridDim.x * blockDim.x)
     {
-        const size_t per_row = kblocks * 32;
-        const size_t r = t / per_row, k = 2 * (t - r * per_row);
-        float a = 0.f, b = 0.f;
-        if (k < K) a = x[r * ld + k];
-        if (k + 1 < K) b = x[r * ld + k + 1];
-        E h[2], l[2];
-        Split<E>::go(a, up, h[0], l[0]);
-        Split<E>::go(b, up, h[1], l[1]);
-        const size_t o = ((k / 64) * rows + r) * 64 + (k % 64);
-        *reinterpret_cast<uint32_t*>(hi + o) = *reinterpret_cast<const uint32_t*>(h);
-        *reinterpret_cast<uint32_t*>(lo + o) = *reinterpret_cast<const uint32_t*>(l);
+        const size_t g  = t % 8;
+        const size_t rk = t / 8;                 // row-major over (row, K block)
+        const size_t kb = rk % kblocks, r = rk / kblocks;
+        const size_t k  = kb * 64 + g * 8;
+        const float* src = x + r * ld + k;
+        float v[8];
+        if (vec4 && k + 8 <= K)
+        {
+            const float4 a = *reinterpret_cast<const float4*>(src);
+            const float4 b = *reinterpret_cast<const float4*>(src + 4);
+            v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+            v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+        }
+        else
+        {
+#pragma unroll
+            for (int q = 0; q < 8; q++)
+                v[q] = (k + q < K) ? src[q] : 0.f;
+        }
+        __align__(16) E h[8], l[8];
+#pragma unroll
+        for (int q = 0; q < 8; q++)
+            Split<E>::go(v[q], up, h[q], l[q]);
+        const size_t o = (kb * rows + r) * 64 + g * 8;
+        *reinterpret_cast<uint4*>(hi + o) = *reinterpret_cast<const uint4*>(h);
+        *reinterpret_cast<uint4*>(lo + o) = *reinterpret_cast<const uint4*>(l);
     }
 }
 
-// fp32 -> bf16 hi + lo planes in the K-blocked layout: element (r, k) at
-// ((k / 64) * rows + r) * 64 + k % 64, so that the 64-element K slice of
-// every row of a block is one contiguous run (a TMA box of 128 rows is
-// 16 KB of consecutive memory instead of 128 rows a full row stride apart).
-// K is padded with zeros to kblocks * 64.
-__global__ void split_blocked_kernel(const float* __restrict__ x, size_t ld, int rows,
-    size_t K, size_t kblocks, __nv_bfloat16* __restrict__ hi, __nv_bfloat16* __restrict__ lo)
-{
-    const size_t total = (size_t)rows * kblocks * 32; // element pairs
-    for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < total;
-         t += (size_t)gridDim.x * blockDim.x)
-    {
-        const size_t per_row = kblocks * 32;
-        const size_t r = t / per_row, k = 2 * (t - r * per_row);
-        float a = 0.f, b = 0.f;
-        if (k < K) a = x[r * ld + k];
-        if (k + 1 < K) b = x[r * ld + k + 1];
-        const __nv_bfloat16 ha = __float2bfloat16_rn(a), hb = __float2bfloat16_rn(b);
-        __nv_bfloat162 h2, l2;
-        h2.x = ha;
-        h2.y = hb;
-        l2.x = __float2bfloat16_rn(a - __bfloat162float(ha));
-        l2.y = __float2bfloat16_rn(b - __bfloat162float(hb));
-        const size_t o = ((k / 64) * rows + r) * 64 + (k % 64);
-        *reinterpret_cast<__nv_bfloat162*>(hi + o) = h2;
-        *reinterpret_cast<__nv_bfloat162*>(lo + o) = l2;
-    }
-}
+
 
 // Points-major operand of the points x functions product: columns
 // [p0, p0 + P) of the orbital block x (n functions, leading dimension ld)
@@ -901,10 +896,11 @@ int prepare(int mode, const void* X, size_t ld, size_t K, int rows, int box_rows
         const size_t plane   = kblocks * 64 * (size_t)rows * sizeof(__half);
         auto* hi             = (__half*)ws;
         auto* lo             = (__half*)(ws + plane);
-        const int nb = (int)std::min<size_t>((kblocks * 32 * rows + 255) / 256, 1 << 20);
-        split_blocked_e_kernel<__half><<<nb, 256, 0, s>>>((const float*)X, ld, rows, K, kblocks,
-            hi, lo, sc);
-        MGX_LAUNCH_CHECK("split_blocked_e_kernel");
+        const int vec4 = ((ld % 4) == 0 && ((uintptr_t)X % 16) == 0) ? 1 : 0;
+        const int nb8  = (int)std::min<size_t>((kblocks * 8 * rows + 255) / 256, 1 << 20);
+        split8_kernel<__half><<<nb8, 256, 0, s>>>((const float*)X, ld, rows, K, kblocks, hi, lo,
+            sc, vec4);
+        MGX_LAUNCH_CHECK("split8_kernel");
         MGX_TRY(make_map_blocked(&op.m0, hi, rows, kblocks, box_rows, 64, true));
         MGX_TRY(make_map_blocked(&op.m1, lo, rows, kblocks, box_rows, 64, true));
         op.base0 = hi;
@@ -948,8 +944,11 @@ int prepare(int mode, const void* X, size_t ld, size_t K, int rows, int box_rows
     const int nb         = (int)std::min<size_t>((ldo / 2 * rows + 255) / 256, 1 << 20);
     if (op.blocked)
     {
-        split_blocked_kernel<<<nb, 256, 0, s>>>((const float*)X, ld, rows, K, kblocks, hi, lo);
-        MGX_LAUNCH_CHECK("split_blocked_kernel");
+        const int vec4 = ((ld % 4) == 0 && ((uintptr_t)X % 16) == 0) ? 1 : 0;
+        const int nb8  = (int)std::min<size_t>((kblocks * 8 * rows + 255) / 256, 1 << 20);
+        split8_kernel<__nv_bfloat16><<<nb8, 256, 0, s>>>((const float*)X, ld, rows, K, kblocks,
+            hi, lo, nullptr, vec4);
+        MGX_LAUNCH_CHECK("split8_kernel");
         MGX_TRY(make_map_blocked(&op.m0, hi, rows, kblocks, box_rows, op.sw));
         MGX_TRY(make_map_blocked(&op.m1, lo, rows, kblocks, box_rows, op.sw));
     }
