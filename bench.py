@@ -1,8 +1,12 @@
 """Orbital-sweep benchmark of the GB300 implementation of MGmol's hot path.
 
-One step = one orbital sweep over all N orbitals (H psi with the Mehrstellen
-operator and B(V psi), S and H matrices, FP64 Cholesky / inverse / trace,
-one V-cycle preconditioner application), on seeded synthetic orbitals.
+One step = one orbital sweep over all N orbitals, the reference's
+iteration for a Mehrstellen operator: normalization of the block, H psi
+(Mehrstellen operator and B(V psi)), the S, H and B matrices, FP64
+Cholesky / inverse of S, theta = B^-1 H, HB and the energy tr(HB S^-1), the
+residual B(psi) theta - H psi, one V-cycle preconditioner application and
+the orbital update, on seeded synthetic orbitals.  --theta gram runs the
+form with theta = S^-1 H and energy tr(S^-1 H) instead (no B matrix).
 
 Default workload: 2048 orbitals on a 192^3 periodic grid (h = 0.25 bohr,
 FP32 orbitals, 64 Gaussian wells) -- the configuration the metric is quoted
@@ -40,7 +44,7 @@ CONFIGS = {
     "small": dict(n=(64, 64, 64), h=0.25, nfunc=256, wells=16, seed=7,
                   workload="small sweep: 256 orbitals, 64^3, Mehrstellen, FP32"),
 }
-METRIC = "orbital sweeps/s (ABPG step: Hpsi, Gram/H, residual, precond, update)"
+METRIC = "orbital sweeps/s (ABPG step: normalize, Hpsi, S/H/B, theta, residual, precond, update)"
 
 
 def _env_int(k, d):
@@ -118,7 +122,10 @@ def _peaks():
 def cpu_sweep_estimate(cfg, sample_funcs=4):
     """Times the oracle port (all host threads) of one sweep on
     `sample_funcs` orbitals of the workload grid and extrapolates to N:
-    H psi and the V-cycle scale with N, S and H with N^2."""
+    normalize, H psi, the B psi of computeMatB, the V-cycle and the
+    residual stencil scale with N; S, H, B and Psi Theta with N^2 (B as the
+    reference forms it, full N x N).  The N x N FP64 algebra is not timed
+    (a few GFLOP against the products' tens of TFLOP)."""
     import numpy as np
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
@@ -131,7 +138,9 @@ def cpu_sweep_estimate(cfg, sample_funcs=4):
     V = synth.gaussian_wells(n, ll, cfg["wells"], cfg["seed"])
     vel = (cfg["h"]) ** 3
     t0 = time.perf_counter()
+    O.normalize(n, ll, psi)
     hp = O.hpsi(n, ll, 0, psi, V)
+    O.rhs_mehr(n, ll, psi)
     t1 = time.perf_counter()
     O.precond(n, ll, 0, 2, 0.2, hp)
     t2 = time.perf_counter()
@@ -155,17 +164,17 @@ def cpu_sweep_estimate(cfg, sample_funcs=4):
     per_pair_point = (t4 - t3) / (pairs_s * ks)
     per_mm = (t5 - t4) / (ns * ns * ks)
     lin = (t2b - t0) * (N / sample_funcs)
-    quad = per_pair_point * (N * (N + 1) / 2 + N * N) * P + per_mm * N * N * P
+    quad = per_pair_point * (N * (N + 1) / 2 + 2 * N * N) * P + per_mm * N * N * P
     per_sweep = lin + quad
     t4 = t5
     cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
     return {
         "value": 1.0 / per_sweep, "unit": "sweeps/s", "cores": cores, "kind": "port",
         "sample": (f"oracle port of the reference loops (FP32 data, FP64 accumulation as the "
-                   f"USE_MP build), {cores} threads: H psi, V-cycle and the residual stencil on "
-                   f"{sample_funcs} of {N} orbitals ({n[0]}^3), scaled by N; S, H and Psi Theta "
-                   f"timed on a {ns}-orbital x {ks}-point slab, scaled by pairs x points; sample "
-                   f"took {t4 - t0:.1f} s"),
+                   f"USE_MP build), {cores} threads: normalize, H psi, B psi, V-cycle and the "
+                   f"residual stencil on {sample_funcs} of {N} orbitals ({n[0]}^3), scaled by N; "
+                   f"S, H, B and Psi Theta timed on a {ns}-orbital x {ks}-point slab, scaled by "
+                   f"pairs x points; N x N FP64 algebra not timed; sample took {t4 - t0:.1f} s"),
         "seconds_per_sweep": per_sweep,
     }
 
@@ -228,7 +237,7 @@ def run_gpu(args, cfg):
         block = N * ctx.npts * (8 if mode == "plain" else 4)
         lean = 0 if 3.6 * block < free else 128
     sw = OrbitalSweep(ctx, V, N, mode=mode, gemm=gemm, precond_chunk=args.chunk,
-                      chunk_funcs=lean)
+                      chunk_funcs=lean, use_matb=args.theta == "b")
     torch.cuda.synchronize()
 
     for _ in range(args.warmup):
@@ -292,14 +301,16 @@ def run_gpu(args, cfg):
     s = 4 if dt == torch.float32 else 8
     # algorithmic work per sweep phase
     hpsi_bytes = N * npts * 2 * s + npts * s
-    gram_flops = N * (N + 1) * npts + 2.0 * N * N * npts
+    # S and B lower triangles including the diagonal, H full
+    gram_flops = (2 if sw.use_matb else 1) * N * (N + 1) * npts + 2.0 * N * N * npts
     shares = {k: v / sum(phases.values()) for k, v in phases.items()}
     dominant = max(phases, key=phases.get)
     if dominant == "gram":
         achieved = gram_flops / (phases["gram"] * 1e-3) / 1e12
         roof = {"kernel": "gram+hmat", "bound": "tensor", "achieved": achieved, "peak": bf16,
                 "unit": "TFLOP/s", "frac": achieved / bf16, "traffic": None,
-                "algorithmic": f"{gram_flops:.3e} flop per sweep (S lower incl. diagonal + H)"}
+                "algorithmic": f"{gram_flops:.3e} flop per sweep (S{' and B' if sw.use_matb else ''} "
+                               f"lower incl. diagonal + H)"}
     elif dominant == "residual":
         rflops = 2.0 * N * N * npts
         achieved = rflops / (phases["residual"] * 1e-3) / 1e12
@@ -326,6 +337,8 @@ def run_gpu(args, cfg):
         "config": {"workload": cfg["workload"], "grid": list(n), "h": cfg["h"], "orbitals": N,
                    "mode": mode, "gemm": args.gemm if mode == "mixed" else "fp64",
                    "lap_type": "mehrstellen", "precond": "V-cycle 2 coarse levels",
+                   "theta": "B^-1 H (ProjectedMatricesMehrstellen)" if sw.use_matb
+                   else "S^-1 H (ProjectedMatrices)",
                    "schedule": f"column chunks of {sw.chunk}" if sw.chunk else "full blocks",
                    "l2": "inputs larger than L2 (no flush)", "parallelism": f"replicas x{world}"},
         "phases_ms": phases, "phase_share": shares, "energy_trace_ry": energy,
@@ -350,6 +363,9 @@ def main():
     ap.add_argument("--mode", default="mixed", choices=["mixed", "plain"])
     ap.add_argument("--gemm", default="bf16x3", choices=["fp32", "tf32", "bf16x3", "fp16x3"])
     ap.add_argument("--chunk", type=int, default=0, help="V-cycle orbital chunk (0 = auto)")
+    ap.add_argument("--theta", default="b", choices=["b", "gram"],
+                    help="b: theta = B^-1 H as the reference for a Mehrstellen operator; "
+                         "gram: theta = S^-1 H")
     ap.add_argument("--lean", type=int, default=-1,
                     help="residual / preconditioner column chunk (0 = full blocks, -1 = auto)")
     ap.add_argument("--cpu-sample", type=int, default=32,

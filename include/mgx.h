@@ -201,12 +201,16 @@ int mgx_precond_mg(mgx_ctx* ctx, const mgx_precond_params* p, mgx_dtype dtype,
  * acceleration (src/ABPG.cc:72-140): psi += alpha * V-cycle(res), with
  * alpha = 0.5 * precond_factor.  The V-cycle is mgx_precond_mg's; its last
  * fine-level sweep adds its result to psi instead of storing it, so the
- * correction block is never written.  work (nfunc x ld, or NULL for a
- * block owned by ctx) holds the fine-level iterate.  res, psi and work may
- * not alias. */
+ * correction block is never written.  With psi_scale (device, nfunc FP64
+ * values; NULL for none) the stored result is
+ * psi_j = psi_scale[j] * (psi_j + alpha * V-cycle(res)_j): the column
+ * scaling of a block whose normalization was deferred into this update
+ * (mgx_normalize_scales).  work (nfunc x ld, or NULL for a block owned by
+ * ctx) holds the fine-level iterate.  res, psi and work may not alias. */
 int mgx_precond_mg_update(mgx_ctx* ctx, const mgx_precond_params* p,
-    mgx_dtype dtype, const void* res, size_t ld, void* psi, double alpha, int nfunc,
-    const mgx_masks* masks, void* work, void* stream);
+    mgx_dtype dtype, const void* res, size_t ld, void* psi, double alpha,
+    const double* psi_scale, int nfunc, const mgx_masks* masks, void* work,
+    void* stream);
 
 /* mgx_precond_mg without any device allocation.  This entry point has no
  * counterpart in the reference; it serves callers that cannot allocate
@@ -272,6 +276,52 @@ int mgx_hmat(mgx_ctx* ctx, int mode, const void* psi, const void* hpsi,
  * same conventions as mgx_gram and mgx_hmat. */
 int mgx_gram_hmat(mgx_ctx* ctx, int mode, const void* psi, const void* hpsi,
     size_t ld, int nfunc, double* S, double* H, void* stream);
+
+/* LocGridOrbitals::computeMatB (src/LocGridOrbitals.cc:1428-1487), the
+ * matrix of the Mehrstellen generalized eigenproblem:
+ * Bm = Psi^T (B Psi) * vel, B the Mehrstellen right-hand-side operator
+ * (pb::Laph4M::rhs, FDkernelRHS_4th_Mehr1), FP64 n x n.  Only the lower
+ * triangle is formed -- the reference's consumers (potrf / potri with uplo
+ * 'l' in ProjectedMatricesMehrstellen::computeInvB) read no other part --
+ * and it is mirrored into the upper one.  B Psi is formed in `work`, a
+ * block of work_funcs >= 1 functions (leading dimension ld, the orbital
+ * type), work_funcs functions at a time; or, for a NULL work, in a block of
+ * at most 512 functions owned by ctx.  work may not alias psi.  mode as for
+ * mgx_gram. */
+int mgx_matb(mgx_ctx* ctx, int mode, const void* psi, size_t ld, int nfunc,
+    double* Bm, void* work, int work_funcs, void* stream);
+
+/* S, H and B (mgx_gram, mgx_hmat, mgx_matb) in one call; the tensor-core
+ * modes convert Psi once for the three products. */
+int mgx_gram_hmat_matb(mgx_ctx* ctx, int mode, const void* psi, const void* hpsi,
+    size_t ld, int nfunc, double* S, double* H, double* Bm, void* work, int work_funcs,
+    void* stream);
+
+/* ProjectedMatricesMehrstellen::updateHB
+ * (src/ProjectedMatricesMehrstellen.h:55-62): HB = S theta, S read as
+ * symmetric from its lower triangle (symm 'l', 'l'), then
+ * HB = 0.5 HB + 0.5 HB^T.  With theta = B^-1 H, tr(HB S^-1)
+ * (mgx_trace_prod(HB, Sinv)) is the energy of ProjectedMatrices::getEigSum
+ * for a Mehrstellen operator. */
+int mgx_update_hb(mgx_ctx* ctx, int n, const double* S, const double* theta,
+    double* HB, void* stream);
+
+/* LocGridOrbitals::normalize (src/LocGridOrbitals.cc:2230-2311, the branch
+ * without short-sighted matrices): diagS_i = vel * psi_i . psi_i with FP64
+ * accumulation (MPdot), then psi_i <- psi_i / sqrt(diagS_i) computed in
+ * FP64 and rounded to the orbital type (MPscal).  diagS (device, nfunc
+ * values) may be NULL.  A diagS_i <= 1e-15, which the reference asserts
+ * against, returns MGX_NOT_SPD with psi unchanged.  Synchronous. */
+int mgx_normalize(mgx_ctx* ctx, mgx_dtype dtype, void* psi, size_t ld, int nfunc,
+    double* diagS, void* stream);
+
+/* scale_i = 1 / sqrt(S(i, i)) (device, n values): the factors by which
+ * LocGridOrbitals::normalize would scale functions whose Gram matrix is S.
+ * With these, the normalization of a block can be folded into the update
+ * of mgx_precond_mg_update (its psi_scale) instead of a separate pass over
+ * the block.  No counterpart in the reference. */
+int mgx_normalize_scales(mgx_ctx* ctx, int n, const double* S, double* scale,
+    void* stream);
 
 /* GramMatrix::updateLS (src/GramMatrix.cc:180-191): A (n x n, FP64) is
  * overwritten by its lower Cholesky factor (upper part zeroed).  *info

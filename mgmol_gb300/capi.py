@@ -88,8 +88,8 @@ _SIGS = {
     "mgx_mg_restrict": [_vp, _i, _i, _vp, _vp, _i, _vp],
     "mgx_mg_prolong": [_vp, _i, _i, _vp, _vp, _i, _vp],
     "mgx_precond_mg": [_vp, ctypes.POINTER(PrecondParams), _i, _vp, _sz, _vp, _i, _vp, _vp],
-    "mgx_precond_mg_update": [_vp, ctypes.POINTER(PrecondParams), _i, _vp, _sz, _vp, _d, _i, _vp,
-                              _vp, _vp],
+    "mgx_precond_mg_update": [_vp, ctypes.POINTER(PrecondParams), _i, _vp, _sz, _vp, _d, _vp, _i,
+                              _vp, _vp, _vp],
     "mgx_precond_mg_static": [_vp, ctypes.POINTER(PrecondParams), _i, _vp, _sz, _vp, _i, _vp, _vp],
     "mgx_precond_gamma": [ctypes.POINTER(Grid), _i, _i, _d, _d, _dp],
     "mgx_masks_create": [_vp, _i, _i, _dp, _dp, _i, _i, _i, _i, ctypes.POINTER(_vp), _vp],
@@ -99,6 +99,11 @@ _SIGS = {
     "mgx_gram": [_vp, _i, _vp, _sz, _i, _vp, _vp],
     "mgx_hmat": [_vp, _i, _vp, _vp, _sz, _i, _vp, _vp],
     "mgx_gram_hmat": [_vp, _i, _vp, _vp, _sz, _i, _vp, _vp, _vp],
+    "mgx_matb": [_vp, _i, _vp, _sz, _i, _vp, _vp, _i, _vp],
+    "mgx_gram_hmat_matb": [_vp, _i, _vp, _vp, _sz, _i, _vp, _vp, _vp, _vp, _i, _vp],
+    "mgx_update_hb": [_vp, _i, _vp, _vp, _vp, _vp],
+    "mgx_normalize": [_vp, _i, _vp, _sz, _i, _vp, _vp],
+    "mgx_normalize_scales": [_vp, _i, _vp, _vp, _vp],
     "mgx_cholesky": [_vp, _i, _vp, _ip, _vp],
     "mgx_inverse_from_cholesky": [_vp, _i, _vp, _vp, _vp],
     "mgx_trace_prod": [_vp, _i, _vp, _vp, _vp, _vp],
@@ -279,15 +284,20 @@ class Context:
         return out
 
     def precond_update(self, res, psi, alpha, lap_type, maxlevels, gamma, masks=None, chunk=0,
-                       work=None, stream=None):
+                       work=None, psi_scale=None, stream=None):
         """psi += alpha * V-cycle(res) (the update fused into the last sweep);
-        work: optional scratch block of res's shape."""
+        with psi_scale (FP64 device vector, one value per function) psi_j =
+        psi_scale[j] * (psi_j + alpha * V-cycle(res)_j); work: optional
+        scratch block of res's shape."""
         p, ld, nf = _block(res, self.npts)
         pp, ldp, _ = _block(psi, self.npts)
         assert ldp == ld
+        if psi_scale is not None and (psi_scale.dtype != torch.float64 or psi_scale.numel() < nf
+                                      or not psi_scale.is_contiguous()):
+            raise ValueError("psi_scale must be a contiguous FP64 vector of nfunc values")
         prm = PrecondParams(lap_type, maxlevels, float(gamma), int(chunk))
         _check(load().mgx_precond_mg_update(self.handle, ctypes.byref(prm), _dtype(res), p, ld, pp,
-                                            float(alpha), nf,
+                                            float(alpha), _ptr(psi_scale), nf,
                                             masks.handle if masks is not None else None,
                                             _ptr(work), _stream(stream)))
         return psi
@@ -323,6 +333,67 @@ class Context:
         H = torch.empty((nf, nf), dtype=torch.float64, device=psi.device) if H is None else H
         _check(load().mgx_gram_hmat(self.handle, mode, p, ph, ld, nf, _ptr(S), _ptr(H), _stream(stream)))
         return S, H.T
+
+    def _work(self, work, ld, dtype):
+        """(pointer, functions) of a B Psi work block (None: owned by ctx)."""
+        if work is None:
+            return None, 0
+        pw, ldw, nw = _block(work, self.npts)
+        if ldw != ld and nw > 1:
+            raise ValueError("work must have the leading dimension of psi")
+        if work.dtype != dtype:
+            raise ValueError("work must have the orbital type")
+        return pw, nw
+
+    def matb(self, psi, mode=GEMM_FP64, work=None, out=None, stream=None):
+        """B = Psi^T (B Psi) * vel (computeMatB), symmetric FP64 (nfunc, nfunc);
+        work: optional (k, npts) block for B Psi, k >= 1 functions."""
+        p, ld, nf = _block(psi, self.npts)
+        B = torch.empty((nf, nf), dtype=torch.float64, device=psi.device) if out is None else out
+        pw, nw = self._work(work, ld, psi.dtype)
+        _check(load().mgx_matb(self.handle, mode, p, ld, nf, _ptr(B), pw, nw, _stream(stream)))
+        return B
+
+    def gram_hmat_matb(self, psi, hpsi, mode=GEMM_FP64, S=None, H=None, B=None, work=None,
+                       stream=None):
+        """(S, H, B) in one call, H as the row-major view."""
+        p, ld, nf = _block(psi, self.npts)
+        ph, ldh, _ = _block(hpsi, self.npts)
+        assert ldh == ld
+        mk = lambda: torch.empty((nf, nf), dtype=torch.float64, device=psi.device)  # noqa: E731
+        S = mk() if S is None else S
+        H = mk() if H is None else H
+        B = mk() if B is None else B
+        pw, nw = self._work(work, ld, psi.dtype)
+        _check(load().mgx_gram_hmat_matb(self.handle, mode, p, ph, ld, nf, _ptr(S), _ptr(H), _ptr(B),
+                                         pw, nw, _stream(stream)))
+        return S, H.T, B
+
+    def update_hb(self, S, theta, stream=None):
+        """HB = sym(S theta) (ProjectedMatricesMehrstellen::updateHB); row-major
+        tensors in and out, S read from its lower triangle."""
+        n = S.shape[0]
+        Sc = self._colmajor(S)
+        tc = self._colmajor(theta)
+        out = torch.empty((n, n), dtype=torch.float64, device=S.device)
+        _check(load().mgx_update_hb(self.handle, n, _ptr(Sc), _ptr(tc), _ptr(out), _stream(stream)))
+        return out.T
+
+    def normalize(self, psi, diag=None, stream=None):
+        """LocGridOrbitals::normalize in place; returns diagS (FP64 device)."""
+        p, ld, nf = _block(psi, self.npts)
+        d = torch.empty(nf, dtype=torch.float64, device=psi.device) if diag is None else diag
+        _check(load().mgx_normalize(self.handle, _dtype(psi), p, ld, nf, _ptr(d), _stream(stream)))
+        return d
+
+    def normalize_scales(self, S, out=None, stream=None):
+        """1 / sqrt(diag(S)) as an FP64 device vector."""
+        n = S.shape[0]
+        if S.stride() != (n, 1) and S.stride() != (1, n):
+            raise ValueError("S must be a dense (n, n) tensor")
+        d = torch.empty(n, dtype=torch.float64, device=S.device) if out is None else out
+        _check(load().mgx_normalize_scales(self.handle, n, _ptr(S), _ptr(d), _stream(stream)))
+        return d
 
     def cholesky(self, S, stream=None):
         """Lower factor L (returned as a row-major tensor) of symmetric S."""

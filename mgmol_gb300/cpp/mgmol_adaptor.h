@@ -15,6 +15,11 @@
 //                             src/LocGridOrbitals.cc:1504-1738
 //   GramMatrix::updateLS / computeInverse, ProjectedMatrices::getEigSum
 //                             src/GramMatrix.cc:75-191, src/ProjectedMatrices.cc:550-566
+//   LocGridOrbitals::computeMatB / normalize
+//                             src/LocGridOrbitals.cc:1428-1487,2230-2311
+//   ProjectedMatricesMehrstellen::computeInvB / updateTheta / updateHB
+//                             src/ProjectedMatricesMehrstellen.cc:38-64,
+//                             src/ProjectedMatricesMehrstellen.h:49-62
 // Where the reference aborts (unsupported operator, failed Cholesky), these
 // classes throw mgx::Error carrying the C-ABI status.  Header only; link
 // against libmgx.so and the CUDA runtime.
@@ -376,6 +381,21 @@ public:
                   theta.data(), product.psi(0), nullptr),
             "LocGridOrbitals::multiplyByMatrix");
     }
+    /* LocGridOrbitals::computeMatB(orbitals, LapOper): B = Psi^T (B Psi) vel
+     * with the Mehrstellen right-hand side (device, n x n, symmetric) */
+    void computeMatB(DeviceArray<double>& B, int mode = -1) const
+    {
+        if (mode < 0) mode = std::is_same<T, double>::value ? MGX_GEMM_FP64 : MGX_GEMM_BF16X3;
+        check(mgx_matb(ctx_, mode, psi_.data(), numpt(), nfunc_, B.data(), nullptr, 0, nullptr),
+            "LocGridOrbitals::computeMatB");
+    }
+    /* LocGridOrbitals::normalize: psi_i /= sqrt(vel |psi_i|^2); throws
+     * (status MGX_NOT_SPD) where the reference asserts */
+    void normalize()
+    {
+        check(mgx_normalize(ctx_, dtype_of<T>(), psi_.data(), numpt(), nfunc_, nullptr, nullptr),
+            "LocGridOrbitals::normalize");
+    }
     /* LocGridOrbitals::axpy: psi += alpha x */
     void axpy(double alpha, const OrbitalBlock& x)
     {
@@ -484,6 +504,54 @@ public:
         double v = 0.;
         t.download(&v, 1);
         return v;
+    }
+};
+
+/* ProjectedMatricesMehrstellen: the matrix B of the Mehrstellen
+ * generalized eigenproblem, its inverse, theta = B^-1 H and HB (FP64
+ * column-major device matrices) */
+class ProjectedMatricesMehrstellen
+{
+    mgx_ctx* ctx_;
+    int n_;
+    DeviceArray<double> matB_, ls_, invB_;
+
+public:
+    ProjectedMatricesMehrstellen(mgx_ctx* ctx, int n)
+        : ctx_(ctx), n_(n), matB_((size_t)n * n), ls_((size_t)n * n), invB_((size_t)n * n)
+    {
+    }
+    /* initializeMatB(ss): B from LocGridOrbitals::computeMatB */
+    void initializeMatB(const DeviceArray<double>& B)
+    {
+        cuda(cudaMemcpy(matB_.data(), B.data(), (size_t)n_ * n_ * 8, cudaMemcpyDeviceToDevice),
+            "initializeMatB copy");
+    }
+    /* computeInvB (src/ProjectedMatricesMehrstellen.cc:38-64): potrf + potri
+     * with uplo 'l'; throws (status MGX_NOT_SPD) where the reference prints
+     * the matrix and carries on */
+    void computeInvB()
+    {
+        cuda(cudaMemcpy(ls_.data(), matB_.data(), (size_t)n_ * n_ * 8, cudaMemcpyDeviceToDevice),
+            "computeInvB copy");
+        int info = 0;
+        check(mgx_cholesky(ctx_, n_, ls_.data(), &info, nullptr), "computeInvB potrf");
+        check(mgx_inverse_from_cholesky(ctx_, n_, ls_.data(), invB_.data(), nullptr),
+            "computeInvB potri");
+    }
+    const DeviceArray<double>& getInvB() const { return invB_; }
+    /* updateTheta: theta = invB H (symm 'l', 'l') */
+    void updateTheta(const DeviceArray<double>& H, DeviceArray<double>& theta) const
+    {
+        check(mgx_theta(ctx_, n_, invB_.data(), H.data(), theta.data(), nullptr),
+            "ProjectedMatricesMehrstellen::updateTheta");
+    }
+    /* updateHB: HB = sym(S theta) */
+    void updateHB(const DeviceArray<double>& S, const DeviceArray<double>& theta,
+        DeviceArray<double>& HB) const
+    {
+        check(mgx_update_hb(ctx_, n_, S.data(), theta.data(), HB.data(), nullptr),
+            "ProjectedMatricesMehrstellen::updateHB");
     }
 };
 

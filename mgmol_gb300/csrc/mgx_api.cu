@@ -67,7 +67,8 @@ void DeviceBuffer::release()
 
 // defined in the other translation units
 int precond_mg(mgx_ctx*, const mgx_precond_params*, int, const void*, size_t,
-    void*, int, const mgx_masks*, cudaStream_t, void* upd = nullptr, double alpha = 0.);
+    void*, int, const mgx_masks*, cudaStream_t, void* upd = nullptr, double alpha = 0.,
+    const double* scale = nullptr);
 int restrict_launch(int, const Level&, const void*, size_t, void*, size_t, int,
     const MaskDev&, cudaStream_t);
 int prolong_launch(int, int, const Level&, const void*, size_t, void*, size_t,
@@ -90,7 +91,15 @@ int mgm_solve(mgx_ctx*, const mgx_mgm_params*, int, void*, const void*, mgx_mgm_
 int gram_tcgen05(mgx_ctx*, int, const void*, const void*, size_t, size_t, int,
     double, int, double*, cudaStream_t);
 int gram_hmat_tcgen05(mgx_ctx*, int, const void*, const void*, size_t, size_t, int,
-    double, double*, double*, cudaStream_t);
+    double, double*, double*, cudaStream_t, double* Bm = nullptr, void* work = nullptr,
+    int work_funcs = 0);
+int matb_cuda_cores(mgx_ctx*, int, const void*, size_t, size_t, int, double, double*,
+    void*, int, cudaStream_t);
+int matb_tcgen05(mgx_ctx*, int, const void*, size_t, size_t, int, double, double*, void*, int,
+    cudaStream_t);
+int update_hb(int, const double*, const double*, double*, cudaStream_t);
+int normalize(mgx_ctx*, int, void*, size_t, size_t, int, double, double*, cudaStream_t);
+int diag_rsqrt(mgx_ctx*, int, const double*, double*, cudaStream_t);
 int cholesky(mgx_ctx*, int, double*, int*, cudaStream_t);
 int inverse_from_cholesky(mgx_ctx*, int, const double*, double*, cudaStream_t);
 int trace_prod(mgx_ctx*, int, const double*, const double*, double*, cudaStream_t);
@@ -132,6 +141,17 @@ static PlaneParams plane(const mgx_grid& g)
     for (int i = 0; i < 3; i++)
         p.n[i] = g.n[i];
     return p;
+}
+
+int rhs_block(const mgx_grid& g, int dtype, const void* u, size_t ldu, void* out,
+    size_t ldo, int nfunc, cudaStream_t s)
+{
+    PlaneParams p = plane(g);
+    p.u   = u;
+    p.ldu = ldu;
+    p.out = out;
+    p.ldo = ldo;
+    return stencil_launch(OP_RHS, 0, dtype, dtype, p, make_level(g, 0), 0., nfunc, s);
 }
 // ghosted restriction / extension: strip ghosts of the fine (resp. coarse)
 // block, run the ghost-free kernel, write back inside the ghosted target.
@@ -450,8 +470,8 @@ int mgx_precond_mg(mgx_ctx* ctx, const mgx_precond_params* p, mgx_dtype dtype,
 }
 
 int mgx_precond_mg_update(mgx_ctx* ctx, const mgx_precond_params* p, mgx_dtype dtype,
-    const void* res, size_t ld, void* psi, double alpha, int nfunc, const mgx_masks* masks,
-    void* work, void* stream)
+    const void* res, size_t ld, void* psi, double alpha, const double* psi_scale, int nfunc,
+    const mgx_masks* masks, void* work, void* stream)
 {
     if (!ctx) return fail(MGX_BAD_ARG, "ctx is NULL");
     MGX_TRY(check_dtype(dtype));
@@ -463,7 +483,7 @@ int mgx_precond_mg_update(mgx_ctx* ctx, const mgx_precond_params* p, mgx_dtype d
     const size_t ldv = nfunc > 1 ? ld : (ld ? ld : np);
     if (work) MGX_TRY(check_block(ctx->grid, work, ld, nfunc, "work"));
     return precond_mg(ctx, p, dtype, res, ldv, work, nfunc, masks, (cudaStream_t)stream, psi,
-        alpha);
+        alpha, psi_scale);
 }
 
 int mgx_precond_gamma(const mgx_grid* grid, int lap_type, int mg_levels,
@@ -597,6 +617,109 @@ int mgx_gram_hmat(mgx_ctx* ctx, int mode, const void* psi, const void* hpsi,
     }
     MGX_TRY(mgx_gram(ctx, mode, psi, ld, nfunc, S, stream));
     return mgx_hmat(ctx, mode, psi, hpsi, ld, nfunc, H, stream);
+}
+
+/* the block that holds B Psi: the caller's (work_funcs functions) or, for a
+ * NULL work, ctx's residual block grown to at most 512 functions */
+static int matb_work(mgx_ctx* ctx, int mode, size_t ld, int nfunc, void** work, int* wf)
+{
+    if (*work)
+    {
+        if (*wf < 1) return fail(MGX_BAD_ARG, "work_funcs %d < 1", *wf);
+        *wf = std::min(*wf, nfunc);
+        return MGX_OK;
+    }
+    const size_t es = mode == MGX_GEMM_FP64 ? 8 : 4;
+    *wf             = std::min(nfunc, 512);
+    MGX_TRY(ctx->resid.ensure((size_t)(*wf) * ld * es + 256));
+    *work = ctx->resid.ptr;
+    return MGX_OK;
+}
+
+static int check_gemm_mode(int mode)
+{
+    switch (mode)
+    {
+        case MGX_GEMM_FP64:
+        case MGX_GEMM_FP32:
+        case MGX_GEMM_TF32:
+        case MGX_GEMM_BF16X3:
+        case MGX_GEMM_FP16X3: return MGX_OK;
+    }
+    return fail(MGX_BAD_ARG, "gemm mode %d", mode);
+}
+
+int mgx_matb(mgx_ctx* ctx, int mode, const void* psi, size_t ld, int nfunc, double* Bm,
+    void* work, int work_funcs, void* stream)
+{
+    if (!ctx) return fail(MGX_BAD_ARG, "ctx is NULL");
+    MGX_TRY(check_gemm_mode(mode));
+    MGX_TRY(check_block(ctx->grid, psi, ld, nfunc, "psi"));
+    if (nfunc == 0) return MGX_OK;
+    if (!Bm) return fail(MGX_BAD_ARG, "B is NULL");
+    if (work == psi) return fail(MGX_BAD_ARG, "work aliases psi");
+    const Level L    = make_level(ctx->grid, 0);
+    const double vel = L.h[0] * L.h[1] * L.h[2];
+    const size_t ldv = nfunc > 1 ? ld : L.npts();
+    int wf = work_funcs;
+    MGX_TRY(matb_work(ctx, mode, ldv, nfunc, &work, &wf));
+    cudaStream_t s = (cudaStream_t)stream;
+    if (mode == MGX_GEMM_FP64 || mode == MGX_GEMM_FP32)
+        return matb_cuda_cores(ctx, mode == MGX_GEMM_FP64 ? MGX_F64 : MGX_F32, psi, ldv,
+            L.npts(), nfunc, vel, Bm, work, wf, s);
+    return matb_tcgen05(ctx, mode, psi, ldv, L.npts(), nfunc, vel, Bm, work, wf, s);
+}
+
+int mgx_gram_hmat_matb(mgx_ctx* ctx, int mode, const void* psi, const void* hpsi,
+    size_t ld, int nfunc, double* S, double* H, double* Bm, void* work, int work_funcs,
+    void* stream)
+{
+    if (!ctx) return fail(MGX_BAD_ARG, "ctx is NULL");
+    MGX_TRY(check_gemm_mode(mode));
+    MGX_TRY(check_block(ctx->grid, psi, ld, nfunc, "psi"));
+    MGX_TRY(check_block(ctx->grid, hpsi, ld, nfunc, "hpsi"));
+    if (nfunc == 0) return MGX_OK;
+    if (!S || !H || !Bm) return fail(MGX_BAD_ARG, "S, H or B is NULL");
+    if (work == psi || work == hpsi) return fail(MGX_BAD_ARG, "work aliases psi or hpsi");
+    if (mode == MGX_GEMM_TF32 || mode == MGX_GEMM_BF16X3 || mode == MGX_GEMM_FP16X3)
+    {
+        const Level L    = make_level(ctx->grid, 0);
+        const double vel = L.h[0] * L.h[1] * L.h[2];
+        const size_t ldv = nfunc > 1 ? ld : L.npts();
+        int wf = work_funcs;
+        MGX_TRY(matb_work(ctx, mode, ldv, nfunc, &work, &wf));
+        return gram_hmat_tcgen05(ctx, mode, psi, hpsi, ldv, L.npts(), nfunc, vel, S, H,
+            (cudaStream_t)stream, Bm, work, wf);
+    }
+    MGX_TRY(mgx_gram(ctx, mode, psi, ld, nfunc, S, stream));
+    MGX_TRY(mgx_hmat(ctx, mode, psi, hpsi, ld, nfunc, H, stream));
+    return mgx_matb(ctx, mode, psi, ld, nfunc, Bm, work, work_funcs, stream);
+}
+
+int mgx_update_hb(mgx_ctx* ctx, int n, const double* S, const double* theta, double* HB,
+    void* stream)
+{
+    if (!ctx) return fail(MGX_BAD_ARG, "ctx is NULL");
+    return update_hb(n, S, theta, HB, (cudaStream_t)stream);
+}
+
+int mgx_normalize(mgx_ctx* ctx, mgx_dtype dtype, void* psi, size_t ld, int nfunc,
+    double* diagS, void* stream)
+{
+    if (!ctx) return fail(MGX_BAD_ARG, "ctx is NULL");
+    MGX_TRY(check_dtype(dtype));
+    MGX_TRY(check_block(ctx->grid, psi, ld, nfunc, "psi"));
+    if (nfunc == 0) return MGX_OK;
+    const Level L    = make_level(ctx->grid, 0);
+    const double vel = L.h[0] * L.h[1] * L.h[2];
+    const size_t ldv = nfunc > 1 ? ld : L.npts();
+    return normalize(ctx, dtype, psi, ldv, L.npts(), nfunc, vel, diagS, (cudaStream_t)stream);
+}
+
+int mgx_normalize_scales(mgx_ctx* ctx, int n, const double* S, double* scale, void* stream)
+{
+    if (!ctx) return fail(MGX_BAD_ARG, "ctx is NULL");
+    return diag_rsqrt(ctx, n, S, scale, (cudaStream_t)stream);
 }
 
 int mgx_cholesky(mgx_ctx* ctx, int n, double* A, int* info, void* stream)

@@ -17,6 +17,7 @@
 #include <vector>
 
 #include "mgx_internal.cuh"
+#include "mgx_stencil.cuh"
 
 namespace mgx
 {
@@ -30,7 +31,7 @@ constexpr int GKC = 32; // k chunk
 
 template <typename T>
 __global__ void __launch_bounds__(256) gram_splitk_kernel(const T* __restrict__ A,
-    const T* __restrict__ B, size_t ld, int n, size_t K, size_t kslice,
+    const T* __restrict__ B, size_t ld, int n, int ncols, size_t K, size_t kslice,
     const int2* __restrict__ tiles, double* __restrict__ C)
 {
     __shared__ T As[GKC][GT + 1];
@@ -61,7 +62,7 @@ __global__ void __launch_bounds__(256) gram_splitk_kernel(const T* __restrict__ 
             if (k < k1)
             {
                 if (i0 + row < n) av = A[(size_t)(i0 + row) * ld + k];
-                if (j0 + row < n) bv = B[(size_t)(j0 + row) * ld + k];
+                if (j0 + row < ncols) bv = B[(size_t)(j0 + row) * ld + k];
             }
             As[kk][row] = av;
             Bs[kk][row] = bv;
@@ -91,7 +92,7 @@ __global__ void __launch_bounds__(256) gram_splitk_kernel(const T* __restrict__ 
         for (int q = 0; q < 4; q++)
         {
             const int i = i0 + ty + 16 * p, j = j0 + tx + 16 * q;
-            if (i < n && j < n) atomicAdd(&C[(size_t)j * n + i], (double)acc[p][q]);
+            if (i < n && j < ncols) atomicAdd(&C[(size_t)j * n + i], (double)acc[p][q]);
         }
 }
 
@@ -135,15 +136,73 @@ int gram_cuda_cores(mgx_ctx* ctx, int dtype, const void* A, const void* B,
     dim3 grid(ntiles, ksplit);
     if (dtype == MGX_F64)
         gram_splitk_kernel<double><<<grid, 256, 0, s>>>((const double*)A,
-            (const double*)B, ld, n, K, kslice, (const int2*)ctx->gemm_ws.ptr, C);
+            (const double*)B, ld, n, n, K, kslice, (const int2*)ctx->gemm_ws.ptr, C);
     else
         gram_splitk_kernel<float><<<grid, 256, 0, s>>>((const float*)A,
-            (const float*)B, ld, n, K, kslice, (const int2*)ctx->gemm_ws.ptr, C);
+            (const float*)B, ld, n, n, K, kslice, (const int2*)ctx->gemm_ws.ptr, C);
     MGX_LAUNCH_CHECK("gram_splitk_kernel");
     // the tile list must stay alive until the kernel has read it
     MGX_TRY(cuda_check(cudaStreamSynchronize(s), "gram sync"));
     const int nb = (int)std::min<size_t>(((size_t)n * n + 255) / 256, 4096);
     gram_finish_kernel<<<nb, 256, 0, s>>>(C, n, vel, symmetric);
+    MGX_LAUNCH_CHECK("gram_finish_kernel");
+    return MGX_OK;
+}
+
+/* B = Psi^T (B Psi) * vel (LocGridOrbitals::computeMatB,
+ * src/LocGridOrbitals.cc:1428-1487) on CUDA cores: B Psi is formed `wf`
+ * functions at a time in `work` (leading dimension ld) by the Mehrstellen
+ * right-hand-side stencil, and only output tiles that reach the lower
+ * triangle are computed; the finishing pass mirrors the lower triangle. */
+int matb_cuda_cores(mgx_ctx* ctx, int dtype, const void* psi, size_t ld, size_t K, int n,
+    double vel, double* C, void* work, int wf, cudaStream_t s)
+{
+    if (wf <= 0) return fail(MGX_BAD_ARG, "matB: empty work block");
+    const size_t es = dtype_size(dtype);
+    const int nt    = (n + GT - 1) / GT;
+    std::vector<int2> tiles;
+    std::vector<size_t> first;
+    for (int c0 = 0; c0 < n; c0 += wf)
+    {
+        const int nc = std::min(wf, n - c0);
+        first.push_back(tiles.size());
+        for (int j = 0; j < (nc + GT - 1) / GT; j++)
+            for (int i = 0; i < nt; i++)
+                if (i * GT + GT - 1 >= c0 + j * GT) tiles.push_back(make_int2(i, j));
+    }
+    first.push_back(tiles.size());
+    const int nchunks = (int)first.size() - 1;
+    const int avg     = std::max(1, (int)(tiles.size() / nchunks));
+    int ksplit        = std::max(1, (8 * ctx->sm_count + avg - 1) / avg);
+    size_t kslice     = (K + ksplit - 1) / ksplit;
+    kslice            = ((kslice + GKC - 1) / GKC) * GKC;
+    ksplit            = (int)((K + kslice - 1) / kslice);
+    if (ksplit > 65535) return fail(MGX_UNSUPPORTED, "K too large for split");
+    MGX_TRY(ctx->gemm_ws.ensure(tiles.size() * sizeof(int2)));
+    const int2* dt = (const int2*)ctx->gemm_ws.ptr;
+    MGX_TRY(cuda_check(cudaMemcpyAsync(ctx->gemm_ws.ptr, tiles.data(),
+                           tiles.size() * sizeof(int2), cudaMemcpyHostToDevice, s),
+        "matB tiles upload"));
+    MGX_TRY(cuda_check(cudaMemsetAsync(C, 0, (size_t)n * n * sizeof(double), s), "matB zero"));
+    for (int c = 0; c < nchunks; c++)
+    {
+        const int c0 = c * wf, nc = std::min(wf, n - c0);
+        const int nct = (int)(first[c + 1] - first[c]);
+        MGX_TRY(rhs_block(ctx->grid, dtype, (const char*)psi + (size_t)c0 * ld * es, ld, work,
+            ld, nc, s));
+        dim3 grid(nct, ksplit);
+        if (dtype == MGX_F64)
+            gram_splitk_kernel<double><<<grid, 256, 0, s>>>((const double*)psi,
+                (const double*)work, ld, n, nc, K, kslice, dt + first[c], C + (size_t)c0 * n);
+        else
+            gram_splitk_kernel<float><<<grid, 256, 0, s>>>((const float*)psi,
+                (const float*)work, ld, n, nc, K, kslice, dt + first[c], C + (size_t)c0 * n);
+        MGX_LAUNCH_CHECK("gram_splitk_kernel");
+    }
+    // the tile list must stay alive until the kernels have read it
+    MGX_TRY(cuda_check(cudaStreamSynchronize(s), "matB sync"));
+    const int nb = (int)std::min<size_t>(((size_t)n * n + 255) / 256, 4096);
+    gram_finish_kernel<<<nb, 256, 0, s>>>(C, n, vel, 1);
     MGX_LAUNCH_CHECK("gram_finish_kernel");
     return MGX_OK;
 }
@@ -734,6 +793,155 @@ int trace_prod(mgx_ctx* ctx, int n, const double* H, const double* Sinv, double*
     MGX_LAUNCH_CHECK("trace_partial_kernel");
     trace_sum_kernel<<<1, 256, 0, s>>>(part, TRACE_BLOCKS, out);
     MGX_LAUNCH_CHECK("trace_sum_kernel");
+    return MGX_OK;
+}
+
+/* ProjectedMatricesMehrstellen::updateHB
+ * (src/ProjectedMatricesMehrstellen.h:55-62): HB = S theta with S read as
+ * symmetric from its lower triangle (symm 'l', 'l'), then
+ * HB = 0.5 HB + 0.5 HB^T (the transpose(0.5, copy, 0.5) of the reference);
+ * element (i, j) and (j, i) receive the same sum 0.5 a_ij + 0.5 a_ji. */
+__global__ void sym_average_kernel(double* A, int n)
+{
+    const size_t nn = (size_t)n * n;
+    for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < nn;
+         t += (size_t)gridDim.x * blockDim.x)
+    {
+        const int i = (int)(t % n), j = (int)(t / n);
+        if (i <= j) continue;
+        const double x = 0.5 * A[(size_t)j * n + i] + 0.5 * A[(size_t)i * n + j];
+        A[(size_t)j * n + i] = x;
+        A[(size_t)i * n + j] = x;
+    }
+}
+
+int update_hb(int n, const double* S, const double* theta, double* HB, cudaStream_t s)
+{
+    if (n <= 0 || !S || !theta || !HB) return fail(MGX_BAD_ARG, "updateHB: bad arguments");
+    if (HB == S || HB == theta) return fail(MGX_BAD_ARG, "HB aliases an input");
+    MGX_TRY(dgemm(false, false, n, n, n, 1., S, n, theta, n, 0., HB, n, 0, s, 1));
+    const int nb = (int)std::min<size_t>(((size_t)n * n + 255) / 256, 4096);
+    sym_average_kernel<<<nb, 256, 0, s>>>(HB, n);
+    MGX_LAUNCH_CHECK("sym_average_kernel");
+    return MGX_OK;
+}
+
+/* LocGridOrbitals::normalize (src/LocGridOrbitals.cc:2230-2311, the branch
+ * without short-sighted matrices): diagS_i = vel * psi_i . psi_i with FP64
+ * accumulation (BlockVector::dot -> MPdot, src/linear_algebra/mputils.cc:
+ * 145-166), then psi_i <- (T)(diagS_i^-1/2 * (double)psi_i) (MPscal,
+ * mputils.cc:61-80).  The dot products are deterministic: NORM_BLOCKS
+ * partial sums per function, then a fixed-order sum. */
+constexpr int NORM_BLOCKS = 64;
+
+template <typename T>
+__global__ void __launch_bounds__(256) sumsq_partial_kernel(const T* __restrict__ psi,
+    size_t ld, size_t npts, double* __restrict__ part)
+{
+    __shared__ double red[256];
+    const int f    = blockIdx.y;
+    const T* p     = psi + (size_t)f * ld;
+    double acc     = 0.;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < npts;
+         i += (size_t)gridDim.x * blockDim.x)
+    {
+        const double v = (double)p[i];
+        acc += v * v;
+    }
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1)
+    {
+        if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) part[(size_t)f * gridDim.x + blockIdx.x] = red[0];
+}
+
+// one thread per function: diagS = vel * sum of the partials; alpha =
+// 1 / sqrt(diagS); a diagS <= 1e-15 (the reference asserts) raises *bad
+__global__ void norm_finish_kernel(const double* __restrict__ part, int nblk, int nfunc,
+    double vel, double* __restrict__ diag, double* __restrict__ alpha, int* bad)
+{
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= nfunc) return;
+    double acc = 0.;
+    for (int b = 0; b < nblk; b++)
+        acc += part[(size_t)f * nblk + b];
+    const double d = vel * acc;
+    if (diag) diag[f] = d;
+    if (!(d > 1.e-15))
+    {
+        atomicExch(bad, 1);
+        alpha[f] = 1.;
+    }
+    else
+        alpha[f] = 1. / sqrt(d);
+}
+
+// psi_f <- (T)(alpha_f * (double)psi_f), skipped entirely when *bad is set
+template <typename T>
+__global__ void __launch_bounds__(256) scale_columns_kernel(T* __restrict__ psi, size_t ld,
+    size_t npts, const double* __restrict__ alpha, const int* __restrict__ bad)
+{
+    if (bad && *bad) return;
+    const int f    = blockIdx.y;
+    const double a = alpha[f];
+    T* p           = psi + (size_t)f * ld;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < npts;
+         i += (size_t)gridDim.x * blockDim.x)
+        p[i] = (T)(a * (double)p[i]);
+}
+
+int normalize(mgx_ctx* ctx, int dtype, void* psi, size_t ld, size_t npts, int nfunc,
+    double vel, double* diag, cudaStream_t s)
+{
+    if (nfunc <= 0) return MGX_OK;
+    if (nfunc > 65535) return fail(MGX_UNSUPPORTED, "normalize: more than 65535 functions");
+    const size_t part_bytes = (size_t)nfunc * NORM_BLOCKS * sizeof(double);
+    MGX_TRY(ctx->red.ensure(part_bytes + (size_t)nfunc * sizeof(double) + 256));
+    double* part  = (double*)ctx->red.ptr;
+    double* alpha = part + (size_t)nfunc * NORM_BLOCKS;
+    int* bad      = (int*)(alpha + nfunc);
+    MGX_TRY(cuda_check(cudaMemsetAsync(bad, 0, sizeof(int), s), "normalize flag"));
+    dim3 grid(NORM_BLOCKS, nfunc);
+    if (dtype == MGX_F64)
+        sumsq_partial_kernel<double><<<grid, 256, 0, s>>>((const double*)psi, ld, npts, part);
+    else
+        sumsq_partial_kernel<float><<<grid, 256, 0, s>>>((const float*)psi, ld, npts, part);
+    MGX_LAUNCH_CHECK("sumsq_partial_kernel");
+    norm_finish_kernel<<<(nfunc + 127) / 128, 128, 0, s>>>(part, NORM_BLOCKS, nfunc, vel, diag,
+        alpha, bad);
+    MGX_LAUNCH_CHECK("norm_finish_kernel");
+    const int sblk = (int)std::min<size_t>((npts + 255) / 256, 256);
+    dim3 sgrid(sblk, nfunc);
+    if (dtype == MGX_F64)
+        scale_columns_kernel<double><<<sgrid, 256, 0, s>>>((double*)psi, ld, npts, alpha, bad);
+    else
+        scale_columns_kernel<float><<<sgrid, 256, 0, s>>>((float*)psi, ld, npts, alpha, bad);
+    MGX_LAUNCH_CHECK("scale_columns_kernel");
+    int hbad = 0;
+    MGX_TRY(cuda_check(cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, s),
+        "normalize flag read"));
+    MGX_TRY(cuda_check(cudaStreamSynchronize(s), "normalize sync"));
+    if (hbad) return fail(MGX_NOT_SPD, "normalize: a function with vel * |psi|^2 <= 1e-15");
+    return MGX_OK;
+}
+
+/* d_i = 1 / sqrt(S(i, i)): the normalization factors of the functions
+ * whose Gram matrix is S (LocGridOrbitals::normalize takes the same
+ * diagonal from its own dot products) */
+__global__ void diag_rsqrt_kernel(const double* __restrict__ S, int n, double* __restrict__ d)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) d[i] = 1. / sqrt(S[(size_t)i * n + i]);
+}
+
+int diag_rsqrt(mgx_ctx*, int n, const double* S, double* d, cudaStream_t s)
+{
+    if (n <= 0 || !S || !d) return fail(MGX_BAD_ARG, "diag_rsqrt: bad arguments");
+    diag_rsqrt_kernel<<<(n + 255) / 256, 256, 0, s>>>(S, n, d);
+    MGX_LAUNCH_CHECK("diag_rsqrt_kernel");
     return MGX_OK;
 }
 

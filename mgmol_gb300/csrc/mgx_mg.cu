@@ -715,6 +715,7 @@ struct VCycle
     // (chunk base) instead of storing v
     void* upd0       = nullptr;
     double upd_alpha = 0.;
+    const double* upd_scale0 = nullptr; // per-function scale of the update (chunk base)
 
     int jacobi(int l, int cur, bool write_w, bool last = false)
     {
@@ -724,6 +725,7 @@ struct VCycle
             p.upd       = upd0;
             p.ldupd     = ld[0];
             p.upd_alpha = upd_alpha;
+            p.upd_scale = upd_scale0;
         }
         if (l == 0 && pending_scale)
         {
@@ -806,11 +808,12 @@ struct VCycle
 };
 
 /* out = V-cycle(res); or, with upd set, upd += alpha * V-cycle(res)
- * through the last fine-level sweep, and out (nfunc x ld, may be NULL) is
- * only scratch for the fine-level iterate */
+ * through the last fine-level sweep (upd_j = scale_j (upd_j + alpha
+ * V-cycle(res)_j) when scale is given), and out (nfunc x ld, may be NULL)
+ * is only scratch for the fine-level iterate */
 int precond_mg(mgx_ctx* ctx, const mgx_precond_params* P, int dtype,
     const void* res, size_t ld, void* out, int nfunc, const mgx_masks* masks,
-    cudaStream_t s, void* upd = nullptr, double alpha = 0.)
+    cudaStream_t s, void* upd = nullptr, double alpha = 0., const double* scale = nullptr)
 {
     if (!P || !res || (!out && !upd) || nfunc < 0)
         return fail(MGX_BAD_ARG, "precond_mg: null argument");
@@ -888,8 +891,9 @@ int precond_mg(mgx_ctx* ctx, const mgx_precond_params* P, int dtype,
             V.v0[0] = (char*)out + (size_t)f0 * ld * es;
         if (upd)
         {
-            V.upd0      = (char*)upd + (size_t)f0 * ld * es;
-            V.upd_alpha = alpha;
+            V.upd0       = (char*)upd + (size_t)f0 * ld * es;
+            V.upd_alpha  = alpha;
+            V.upd_scale0 = scale ? scale + f0 : nullptr;
         }
         V.v1[0]    = base;
         base += (size_t)nf * ld * es;

@@ -392,6 +392,7 @@ __global__ void __launch_bounds__(256) plane_kernel(PlaneParams p, DevCoef<T> c)
                                    ? reinterpret_cast<T*>(p.upd) + (size_t)f * p.ldupd
                                    : nullptr;
     const T ualpha           = (T)p.upd_alpha;
+    const T uscale           = (OP == OP_JACOBI_UPD && p.upd_scale) ? (T)p.upd_scale[f] : (T)1;
     T* __restrict__ wp       = p.w ? reinterpret_cast<T*>(p.w) + (size_t)f * p.ldw : nullptr;
     const T* __restrict__ fp = p.f ? reinterpret_cast<const T*>(p.f) + (size_t)f * p.ldf : nullptr;
     constexpr bool POINTWISE = is_jacobi(OP) || (OP == OP_HPSI_V) || (OP == OP_RHS_SUB);
@@ -418,7 +419,7 @@ __global__ void __launch_bounds__(256) plane_kernel(PlaneParams p, DevCoef<T> c)
             if (wp != nullptr) wp[idx] = w;
         }
         if (OP == OP_JACOBI_UPD)
-            updp[idx] = updp[idx] + ualpha * r;
+            updp[idx] = uscale * (updp[idx] + ualpha * r);
         else
             outp[idx] = r;
     };
@@ -691,6 +692,7 @@ __global__ void __launch_bounds__(256) plane_vec_kernel(PlaneParams p, DevCoef<T
                                    ? reinterpret_cast<T*>(p.upd) + (size_t)f * p.ldupd
                                    : nullptr;
     const T ualpha           = (T)p.upd_alpha;
+    const T uscale           = (OP == OP_JACOBI_UPD && p.upd_scale) ? (T)p.upd_scale[f] : (T)1;
     T* __restrict__ wp       = p.w ? reinterpret_cast<T*>(p.w) + (size_t)f * p.ldw : nullptr;
     const T* __restrict__ fp = p.f ? reinterpret_cast<const T*>(p.f) + (size_t)f * p.ldf : nullptr;
     constexpr bool POINTWISE = is_jacobi(OP) || (OP == OP_HPSI_V) || (OP == OP_RHS_SUB);
@@ -834,7 +836,7 @@ __global__ void __launch_bounds__(256) plane_vec_kernel(PlaneParams p, DevCoef<T
                     V4 q = uv[k];
 #pragma unroll
                     for (int v = 0; v < VEC; v++)
-                        VH::set(q, v, VH::get(q, v) + ualpha * VH::get(res, v));
+                        VH::set(q, v, uscale * (VH::get(q, v) + ualpha * VH::get(res, v)));
                     *reinterpret_cast<V4*>(updp + xoff + goff[k]) = q;
                 }
                 else
@@ -903,7 +905,7 @@ __global__ void __launch_bounds__(256) direct_kernel(PlaneParams p, DevCoef<T> c
         if (OP == OP_JACOBI_UPD)
         {
             T* u = reinterpret_cast<T*>(p.upd) + (size_t)f * p.ldupd + idx;
-            *u   = *u + (T)p.upd_alpha * r;
+            *u   = (p.upd_scale ? (T)p.upd_scale[f] : (T)1) * (*u + (T)p.upd_alpha * r);
         }
         else
             reinterpret_cast<T*>(p.out)[(size_t)f * p.ldo + idx] = r;

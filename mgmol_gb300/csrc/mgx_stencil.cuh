@@ -66,11 +66,19 @@ struct PlaneParams
     void* upd        = nullptr;
     size_t ldupd     = 0;
     double upd_alpha = 0.;
+    // OP_JACOBI_UPD only, or NULL: upd = upd_scale[f] * (upd + upd_alpha r),
+    // the column normalization of the updated block folded into the store
+    const double* upd_scale = nullptr;
 };
 
 int stencil_launch(int op, int lap_type, int dtype, int v_dtype,
     const PlaneParams& p, const Level& L, double jf, int nfunc,
     cudaStream_t stream, int force_direct = 0);
+
+/* out = B u (the Mehrstellen right-hand-side operator) for nfunc ghost-free
+ * functions of grid level 0; u and out with leading dimensions ldu, ldo. */
+int rhs_block(const mgx_grid& g, int dtype, const void* u, size_t ldu, void* out,
+    size_t ldo, int nfunc, cudaStream_t s);
 
 int ghosted_del2(const mgx_grid& g, int ghosts, int lap_type, int dtype,
     const void* v, void* b, size_t nfunc, cudaStream_t s);

@@ -32,6 +32,7 @@
 #include <vector>
 
 #include "mgx_internal.cuh"
+#include "mgx_stencil.cuh"
 
 namespace mgx
 {
@@ -167,7 +168,8 @@ struct Params
     int kb_per_cta; // K blocks per CTA
     int n;          // rows of C (and its leading dimension)
     int ncols;      // columns of C produced by this launch
-    int symmetric;  // only i >= j entries of C are produced
+    int symmetric;  // only i >= j + col0 entries of C are produced
+    int col0 = 0;   // global column of the launch's first column (C points there)
     double* C;      // column-major, leading dimension n, FP64, accumulated atomically
     int* err;
     // store epilogue (points x functions products): tile t of the launch is
@@ -368,7 +370,7 @@ __global__ void __launch_bounds__(THREADS, 1) gram_kernel(
                     for (int t = 0; t < 32; t++)
                     {
                         const int j = j0 + c0 + t;
-                        if (j < p.ncols && (!p.symmetric || i >= j))
+                        if (j < p.ncols && (!p.symmetric || i >= j + p.col0))
                             atomicAdd(p.C + (size_t)j * p.n + i, (double)v[t]);
                     }
                 }
@@ -979,14 +981,15 @@ size_t operand_bytes(int mode, size_t K, int rows)
  * tiles are 128 x 256 (128 x 128 when ncols <= 128); the B operand map must
  * have been built with the matching box height. */
 int run(mgx_ctx* ctx, int mode, const Operand& a, const Operand& b, int nrows, int ncols,
-    int symmetric, double* C, int ldc, size_t K, int tile_slot, int BN, cudaStream_t s)
+    int symmetric, double* C, int ldc, size_t K, int tile_slot, int BN, cudaStream_t s,
+    int col0 = 0)
 {
     using namespace tc;
     const int nti = (nrows + BM - 1) / BM, ntj = (ncols + BN - 1) / BN;
     std::vector<int2> tiles;
     for (int j = 0; j < ntj; j++)
         for (int i = 0; i < nti; i++)
-            if (!symmetric || (i * BM + BM - 1) >= j * BN) tiles.push_back(make_int2(i, j));
+            if (!symmetric || (i * BM + BM - 1) >= col0 + j * BN) tiles.push_back(make_int2(i, j));
     const int ntiles  = (int)tiles.size();
     // K elements per block; a CTA covers at most 32768 K elements (the FP32
     // accumulation bound)
@@ -1011,6 +1014,7 @@ int run(mgx_ctx* ctx, int mode, const Operand& a, const Operand& b, int nrows, i
     p.n          = ldc;
     p.ncols      = ncols;
     p.symmetric  = symmetric;
+    p.col0       = col0;
     p.C          = C;
     p.err        = (int*)ctx->tc_err.ptr;
     (void)nrows;
@@ -1115,7 +1119,56 @@ int product(mgx_ctx* ctx, int mode, const Operand& a, size_t a_used, const void*
     }
     return MGX_OK;
 }
+/* lower triangle (rows >= columns) of A (B Psi)^T, B the Mehrstellen
+ * right-hand-side operator: B Psi is formed in `work` (leading dimension
+ * ld) `step` functions at a time, converted and multiplied; only the
+ * output tiles that reach the lower triangle run. */
+int matb_product(mgx_ctx* ctx, int mode, const Operand& a, size_t a_used, const void* psi,
+    size_t ld, size_t K, int n, double* C, int tile_slot, cudaStream_t s,
+    const tc::ScaleSlot* sb, void* work, int work_funcs)
+{
+    const int step = std::min(std::max(work_funcs, 1), CHUNK);
+    for (int j0 = 0; j0 < n; j0 += step)
+    {
+        const int nc = std::min(step, n - j0);
+        MGX_TRY(rhs_block(ctx->grid, MGX_F32, (const float*)psi + (size_t)j0 * ld, ld, work, ld,
+            nc, s));
+        Operand b;
+        size_t used = 0;
+        const int BN = tile_n(nc);
+        MGX_TRY(prepare(mode, work, ld, K, nc, BN, (char*)ctx->tc_split.ptr + a_used, &used, b,
+            s, sb));
+        MGX_TRY(run(ctx, mode, a, b, n, nc, 1, C + (size_t)j0 * n, n, K, tile_slot, BN, s, j0));
+    }
+    return MGX_OK;
+}
 } // namespace
+
+/* B = Psi^T (B Psi) * vel, lower triangle mirrored (the |B u| <= max |u|
+ * bound of the Mehrstellen operator, whose coefficients are positive and
+ * sum to 1, lets the fp16 split of B Psi reuse the scale of Psi) */
+int matb_tcgen05(mgx_ctx* ctx, int mode, const void* psi, size_t ld, size_t K, int n,
+    double vel, double* Bm, void* work, int work_funcs, cudaStream_t s)
+{
+    const size_t a_bytes = operand_bytes(mode, K, n);
+    const size_t b_bytes = operand_bytes(mode, K, std::min(n, CHUNK));
+    MGX_TRY(ctx->tc_split.ensure(a_bytes + b_bytes + 512));
+    MGX_TRY(begin(ctx, s));
+    MGX_TRY(cuda_check(cudaMemsetAsync(Bm, 0, (size_t)n * n * sizeof(double), s), "B zero"));
+    tc::ScaleSlot* sa = nullptr;
+    if (mode == MGX_GEMM_FP16X3)
+    {
+        sa = scale_slot(ctx, 0);
+        MGX_TRY(compute_scale(psi, ld, n, K, sa, s));
+    }
+    Operand a;
+    size_t used = 0;
+    MGX_TRY(prepare(mode, psi, ld, K, n, tc::BM, (char*)ctx->tc_split.ptr, &used, a, s, sa));
+    MGX_TRY(matb_product(ctx, mode, a, ((used + 255) / 256) * 256, psi, ld, K, n, Bm, 0, s, sa,
+        work, work_funcs));
+    MGX_TRY(finish(Bm, n, vel, 1, s, sa, sa));
+    return end(ctx, s);
+}
 
 int gram_tcgen05(mgx_ctx* ctx, int mode, const void* A, const void* B, size_t ld,
     size_t K, int n, double vel, int symmetric, double* C, cudaStream_t s)
@@ -1150,9 +1203,12 @@ int gram_tcgen05(mgx_ctx* ctx, int mode, const void* A, const void* B, size_t ld
     return end(ctx, s);
 }
 
-/* S = Psi^T Psi * vel and H = Psi^T (H Psi) * vel with one conversion of Psi */
+/* S = Psi^T Psi * vel and H = Psi^T (H Psi) * vel with one conversion of
+ * Psi; with Bm, also B = Psi^T (B Psi) * vel (lower triangle mirrored),
+ * B Psi formed in `work` */
 int gram_hmat_tcgen05(mgx_ctx* ctx, int mode, const void* psi, const void* hpsi,
-    size_t ld, size_t K, int n, double vel, double* S, double* H, cudaStream_t s)
+    size_t ld, size_t K, int n, double vel, double* S, double* H, cudaStream_t s,
+    double* Bm, void* work, int work_funcs)
 {
     const size_t a_bytes = operand_bytes(mode, K, n);
     const size_t b_bytes = operand_bytes(mode, K, std::min(n, CHUNK));
@@ -1176,6 +1232,13 @@ int gram_hmat_tcgen05(mgx_ctx* ctx, int mode, const void* psi, const void* hpsi,
     MGX_TRY(product(ctx, mode, a, ((used + 255) / 256) * 256, hpsi, ld, K, n, H, 1, s, sb));
     MGX_TRY(finish(S, n, vel, 1, s, sa, sa));
     MGX_TRY(finish(H, n, vel, 0, s, sa, sb));
+    if (Bm)
+    {
+        MGX_TRY(cuda_check(cudaMemsetAsync(Bm, 0, (size_t)n * n * sizeof(double), s), "B zero"));
+        MGX_TRY(matb_product(ctx, mode, a, ((used + 255) / 256) * 256, psi, ld, K, n, Bm, 0, s,
+            sa, work, work_funcs));
+        MGX_TRY(finish(Bm, n, vel, 1, s, sa, sa));
+    }
     return end(ctx, s);
 }
 

@@ -37,8 +37,9 @@ def _time(fn, warmup, reps):
 
 def main(argv=None):
     ap = argparse.ArgumentParser()
-    ap.add_argument("op", choices=["gram", "hmat", "gram_hmat", "mult", "residual", "hpsi",
-                                   "precond", "mgm", "dense", "h2d", "h2d_kernel", "all"])
+    ap.add_argument("op", choices=["gram", "hmat", "gram_hmat", "matb", "gram_hmat_matb", "mult",
+                                   "residual", "hpsi", "precond", "mgm", "dense", "dense_b",
+                                   "normalize", "h2d", "h2d_kernel", "all"])
     ap.add_argument("--streams", type=int, default=1, help="h2d: concurrent copy streams")
     ap.add_argument("--grid", type=int, nargs=3, default=[96, 96, 32])
     ap.add_argument("--h", type=float, default=0.25)
@@ -62,7 +63,8 @@ def main(argv=None):
     V = synth.gaussian_wells_device(n, ll, 16, 11).to(dt)
     hpsi = ctx.hpsi(psi, V)
     torch.cuda.synchronize()
-    ops = ["gram", "hmat", "gram_hmat", "mult", "residual", "hpsi", "precond", "dense", "mgm"] \
+    ops = ["gram", "hmat", "gram_hmat", "matb", "gram_hmat_matb", "mult", "residual", "hpsi",
+           "precond", "dense", "dense_b", "normalize", "mgm"] \
         if args.op == "all" else [args.op]
     out = []
     for op in ops:
@@ -75,6 +77,19 @@ def main(argv=None):
         elif op == "gram_hmat":
             ms = _time(lambda: ctx.gram_hmat(psi, hpsi, mode), args.warmup, args.reps)
             work, unit = N * (N + 1) * npts + 2.0 * N * N * npts, "TFLOP/s"
+        elif op == "matb":
+            wb = torch.empty_like(psi)
+            ms = _time(lambda: ctx.matb(psi, mode, work=wb), args.warmup, args.reps)
+            del wb
+            work, unit = N * (N + 1) * npts, "TFLOP/s"
+        elif op == "gram_hmat_matb":
+            wb = torch.empty_like(psi)
+            ms = _time(lambda: ctx.gram_hmat_matb(psi, hpsi, mode, work=wb), args.warmup, args.reps)
+            del wb
+            work, unit = 2 * N * (N + 1) * npts + 2.0 * N * N * npts, "TFLOP/s"
+        elif op == "normalize":
+            ms = _time(lambda: ctx.normalize(psi), args.warmup, args.reps)
+            work, unit = 3 * N * npts * s, "GB/s"
         elif op in ("mult", "residual"):
             th = (torch.eye(N, dtype=torch.float64, device="cuda")
                   + torch.randn(N, N, dtype=torch.float64, device="cuda") / N)
@@ -110,6 +125,17 @@ def main(argv=None):
                 ctx.theta(Sinv, H)
             ms = _time(dense, args.warmup, args.reps)
             work, unit = (N ** 3 / 3 + 4 * N ** 3 / 3 + 2 * N ** 3), "TFLOP/s"
+        elif op == "dense_b":
+            # the dense algebra of the Mehrstellen step: S^-1, theta = B^-1 H by
+            # substitution, HB = sym(S theta), tr(HB S^-1)
+            S, H, Bm = ctx.gram_hmat_matb(psi, hpsi, mode)
+
+            def dense_b():
+                Sinv = ctx.inverse_from_cholesky(ctx.cholesky(S)).contiguous()
+                th, _ = ctx.theta_from_cholesky(ctx.cholesky(Bm), H)
+                ctx.trace_prod(ctx.update_hb(S, th), Sinv)
+            ms = _time(dense_b, args.warmup, args.reps)
+            work, unit = (2 * N ** 3 / 3 + 4 * N ** 3 / 3 + 2 * N ** 3 + 2 * N ** 3), "TFLOP/s"
         elif op == "h2d":
             # pinned host block -> device block, split over --streams streams
             host = torch.empty(psi.shape, dtype=dt, pin_memory=True)

@@ -1,27 +1,47 @@
 """One orbital sweep of MGmol's hot path, composed from the C-ABI kernels.
 
-A sweep over the N orbitals of a block Psi is one ABPG step
-(ABPG<T>::updateWF / update_states, src/ABPG.cc:37-140):
+A sweep over the N orbitals of a block Psi is one iteration of the
+DFTsolver loop with the ABPG stepper (src/DFTsolver.cc:262-400,
+ABPG<T>::updateWF / update_states, src/ABPG.cc:37-140), for a Mehrstellen
+operator (lap_type 0, ProjectedMatricesMehrstellen, src/MGmol.cc:243-254):
+  0. normalize Psi (LocGridOrbitals::normalize, src/LocGridOrbitals.cc:
+     2230-2311, which the reference runs after every update);
   1. H psi       (Hamiltonian<T>::applyLocal, src/Hamiltonian.cc:85-159);
-  2. S, H        (LocGridOrbitals::computeGram / Hamiltonian::addHlocalij,
-                  src/LocGridOrbitals.cc:1504-1738, src/Hamiltonian.cc:227-239);
-  3. Cholesky of S, S^-1, the energy trace tr(S^-1 H) and theta = S^-1 H in
-     FP64 (GramMatrix::updateLS / computeInverse, src/GramMatrix.cc:75-191,
-     ProjectedMatrices::getEigSum / updateTheta, src/ProjectedMatrices.cc:
-     550-566, src/ProjectedMatrices.h:218-225);
+  2. S, H, B     (LocGridOrbitals::computeGram / Hamiltonian::addHlocalij /
+                  LocGridOrbitals::computeMatB, src/LocGridOrbitals.cc:
+                  1428-1738, src/Hamiltonian.cc:227-239);
+  3. FP64 dense algebra: Cholesky and inverse of S (GramMatrix::updateLS /
+     computeInverse, src/GramMatrix.cc:75-191); Cholesky of B and
+     theta = B^-1 H (ProjectedMatricesMehrstellen::computeInvB /
+     updateTheta); HB = sym(S theta) (updateHB) and the energy
+     tr(HB S^-1) (ProjectedMatrices::getEigSum, src/ProjectedMatrices.cc:
+     550-566).  For the other operators (and, with use_matb=False, for the
+     Mehrstellen operator too) theta = S^-1 H and HB = H
+     (ProjectedMatrices::updateTheta / setHB2H);
   4. the residual res = B(psi) theta - H psi (MGmol::computeResidualUsingHPhi,
      src/MGmol.cc:1227-1290), written over H psi;
   5. one V-cycle preconditioner application on the residual
      (OrbitalsPreconditioning<T>::precond_mg, src/OrbitalsPreconditioning.cc:86-117);
   6. psi += alpha * P(res), alpha = 0.5 * precond_factor (the non-accelerated
      branch of ABPG<T>::update_states).
+
+With the fused update (the default) step 0 costs no pass over the block:
+the step runs on the block as it came out of the previous update, and the
+normalization factors d_i = S(i,i)^-1/2 of that block (the diagonal of its
+own Gram matrix) scale the update instead, psi_i <- d_i (psi_i + alpha
+P(res)_i).  Every quantity of the step is covariant under that column
+scaling (theta -> D^-1 theta D, res -> res D, tr(HB S^-1) unchanged), so the
+result is the reference's normalize-then-step to rounding; the block handed
+back is the reference's block after update_states, before its normalize.
+The unfused schedules call mgx_normalize explicitly first.
+
 Every step runs on the GPU through mgmol_gb300.capi; the only host work is
 the launch sequence and the Cholesky status read-back.
 
 Two precision modes:
   "plain": FP64 orbitals, FP64 stencils, FP64 products, FP64 V-cycle;
-  "mixed": FP32 orbitals and stencils with an FP32 potential, Gram / H and
-           Psi Theta in the requested GEMM mode, FP32 V-cycle; FP64
+  "mixed": FP32 orbitals and stencils with an FP32 potential, Gram / H / B
+           and Psi Theta in the requested GEMM mode, FP32 V-cycle; FP64
            Cholesky / inverse / trace / theta in both.
 """
 import torch
@@ -58,11 +78,11 @@ class OrbitalSweep:
     psi, H psi and two chunk buffers instead of three full blocks, which is
     what lets the FP64 path hold 2048 orbitals on 192^3 in one GPU."""
 
-    PHASES = ("hpsi", "gram", "dense", "residual", "precond", "update")
+    PHASES = ("normalize", "hpsi", "gram", "dense", "residual", "precond", "update")
 
     def __init__(self, ctx, V, nfunc, mode="mixed", gemm=None, lap_type=capi.LAP_MEHR4,
                  maxlevels=2, gamma=None, precond_chunk=0, precond_factor=1.0,
-                 chunk_funcs=0, fuse_update=True, device="cuda"):
+                 chunk_funcs=0, fuse_update=True, use_matb=True, device="cuda"):
         self.ctx = ctx
         self.mode = mode
         self.lap_type = lap_type
@@ -82,6 +102,15 @@ class OrbitalSweep:
             self.work = None
         self.S = torch.empty((nfunc, nfunc), dtype=torch.float64, device=device)
         self.Hm = torch.empty((nfunc, nfunc), dtype=torch.float64, device=device)
+        # Mehrstellen: the residual applies B; with use_matb (the reference's
+        # ProjectedMatricesMehrstellen) theta = B^-1 H with the matrix B of the
+        # generalized eigenproblem, else theta = S^-1 H (ProjectedMatrices)
+        self.mehr = lap_type == capi.LAP_MEHR4
+        self.use_matb = self.mehr and bool(use_matb)
+        self.Bm = torch.empty((nfunc, nfunc), dtype=torch.float64, device=device) \
+            if self.use_matb else None
+        self.dscale = torch.empty(nfunc, dtype=torch.float64, device=device)
+        self.diagS = torch.empty(nfunc, dtype=torch.float64, device=device)
         self.precond_chunk = precond_chunk
         # the update psi += alpha P(res) inside the last fine-level sweep
         # (full-block schedule only; the chunked one defers the update)
@@ -108,27 +137,43 @@ class OrbitalSweep:
 
     def run(self, psi, timed=False, update=True):
         """One sweep; psi is updated in place (unless update is False).
-        Returns the device tensor holding tr(S^-1 H) (Ry)."""
+        Returns the device tensor holding the energy tr(HB S^-1) (Ry)."""
         ctx = self.ctx
-        apply_B = self.lap_type == capi.LAP_MEHR4
+        lazy = self.fuse_update and update
+        if not lazy:
+            self._mark(timed, "normalize")
+            ctx.normalize(psi, diag=self.diagS)
         self._mark(timed, "hpsi")
         ctx.hpsi(psi, self.V, self.lap_type, True, out=self.hpsi)
         self._mark(timed, "gram")
-        ctx.gram_hmat(psi, self.hpsi, self.gemm, S=self.S, H=self.Hm)
+        if self.use_matb:
+            ctx.gram_hmat_matb(psi, self.hpsi, self.gemm, S=self.S, H=self.Hm, B=self.Bm,
+                               work=self.work if self.chunk else self.corr)
+        else:
+            ctx.gram_hmat(psi, self.hpsi, self.gemm, S=self.S, H=self.Hm)
         self._mark(timed, "dense")
-        L = ctx.cholesky(self.S)
-        Sinv = ctx.inverse_from_cholesky(L)
         # Hm holds H column-major; the matrix calls want the row-major view
-        e = ctx.trace_prod(self.Hm.T, Sinv.contiguous())
-        self.theta = ctx.theta(Sinv, self.Hm.T)
+        H = self.Hm.T
+        L = ctx.cholesky(self.S)
+        Sinv = ctx.inverse_from_cholesky(L).contiguous()
+        if self.use_matb:
+            # computeInvB + updateTheta: theta = B^-1 H from the factor of B
+            self.theta, _ = ctx.theta_from_cholesky(ctx.cholesky(self.Bm), H)
+            e = ctx.trace_prod(ctx.update_hb(self.S, self.theta), Sinv)
+        else:
+            e = ctx.trace_prod(H, Sinv)
+            self.theta = ctx.theta(Sinv, H)
+        if lazy:
+            ctx.normalize_scales(self.S, out=self.dscale)
         if not self.chunk:
             self._mark(timed, "residual")
-            ctx.residual(psi, self.hpsi, self.theta, mode=self.gemm, apply_B=apply_B,
+            ctx.residual(psi, self.hpsi, self.theta, mode=self.gemm, apply_B=self.mehr,
                          work=self.corr, out=self.hpsi)
             self._mark(timed, "precond")
-            if self.fuse_update and update:
+            if lazy:
                 ctx.precond_update(self.hpsi, psi, self.alpha, self.lap_type, self.maxlevels,
-                                   self.gamma, chunk=self.precond_chunk, work=self.corr)
+                                   self.gamma, chunk=self.precond_chunk, work=self.corr,
+                                   psi_scale=self.dscale)
                 self._mark(timed, "update")
             else:
                 ctx.precond_mg(self.hpsi, self.lap_type, self.maxlevels, self.gamma,
@@ -144,7 +189,7 @@ class OrbitalSweep:
                 hc = self.hpsi[j0:j1]
                 cb = self.corr[: j1 - j0]
                 self._mark(timed, "residual")
-                ctx.residual_cols(psi, hc, thc[j0:j1], mode=self.gemm, apply_B=apply_B,
+                ctx.residual_cols(psi, hc, thc[j0:j1], mode=self.gemm, apply_B=self.mehr,
                                   work=self.work[: j1 - j0], out=hc)
                 self._mark(timed, "precond")
                 ctx.precond_mg(hc, self.lap_type, self.maxlevels, self.gamma,

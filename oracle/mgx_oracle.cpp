@@ -1684,3 +1684,111 @@ int orc_mgm_f(const int* n, const double* ll, int lap_type, int ng, int cogr,
     return mgm_t(n, ll, lap_type, ng, cogr, max_sweeps, tol, nu1, nu2, vh, rho, out);
 }
 }
+
+/* ------------------------------------------------------------------ */
+/* Mehrstellen projected matrices and the normalization.               */
+/* ------------------------------------------------------------------ */
+
+/* LocGridOrbitals::computeMatB (src/LocGridOrbitals.cc:1428-1487): work_i =
+ * B psi_i (LapOper.rhs, the Mehrstellen right-hand side), ss = psi^T work
+ * (MPgemmTN: float input, FP64 accumulation; src/linear_algebra/
+ * mputils.cc:1035-1054), ss.scal(vel), then the |x| > 1e-14 filter of the
+ * conversion to the distributed matrix (ProjectedMatricesMehrstellen::
+ * initializeMatB -> LocalMatrices2DistMatrix::accumulate).  Both triangles
+ * are formed, as the reference does. */
+template <typename T>
+static int matb_t(const int* n, const double* ll, int nfunc, const T* psi, double* B)
+{
+    const size_t np = (size_t)n[0] * n[1] * n[2];
+    std::vector<T> w(np * nfunc);
+    rhs_mehr_t(n, ll, nfunc, psi, w.data());
+    const double vel = (ll[0] / n[0]) * (ll[1] / n[1]) * (ll[2] / n[2]);
+#pragma omp parallel for schedule(dynamic)
+    for (int j = 0; j < nfunc; j++)
+        for (int i = 0; i < nfunc; i++)
+        {
+            double t = 0.;
+            const T* a = psi + (size_t)i * np;
+            const T* b = w.data() + (size_t)j * np;
+            for (size_t k = 0; k < np; k++)
+                t += (double)a[k] * (double)b[k];
+            double x = t * vel;
+            if (!(std::fabs(x) > 1.e-14)) x = 0.;
+            B[(size_t)j * nfunc + i] = x;
+        }
+    return 0;
+}
+
+/* LocGridOrbitals::normalize (src/LocGridOrbitals.cc:2230-2311, the branch
+ * without short-sighted matrices): diagS_i = vel * BlockVector::dot(i, i)
+ * (MPdot, FP64 accumulation, src/linear_algebra/mputils.cc:145-166), then
+ * BlockVector::scal(1 / sqrt(diagS_i)) (MPscal: (T)(alpha * (double)x),
+ * mputils.cc:53-80).  Returns 1 (psi unchanged) when a diagS_i <= 1e-15,
+ * which the reference asserts against. */
+template <typename T>
+static int normalize_t(const int* n, const double* ll, int nfunc, T* psi, double* diag)
+{
+    const size_t np  = (size_t)n[0] * n[1] * n[2];
+    const double vel = (ll[0] / n[0]) * (ll[1] / n[1]) * (ll[2] / n[2]);
+    for (int i = 0; i < nfunc; i++)
+    {
+        double d = 0.;
+        const T* p = psi + (size_t)i * np;
+        for (size_t k = 0; k < np; k++)
+            d += (double)p[k] * (double)p[k];
+        diag[i] = vel * d;
+        if (!(diag[i] > 1.e-15)) return 1;
+    }
+    for (int i = 0; i < nfunc; i++)
+    {
+        const double alpha = 1. / std::sqrt(diag[i]);
+        T* p = psi + (size_t)i * np;
+        for (size_t k = 0; k < np; k++)
+            p[k] = (T)(alpha * (double)p[k]);
+    }
+    return 0;
+}
+
+extern "C" {
+int orc_matb_d(const int* n, const double* ll, int nfunc, const double* psi, double* B)
+{
+    return matb_t(n, ll, nfunc, psi, B);
+}
+int orc_matb_f(const int* n, const double* ll, int nfunc, const float* psi, double* B)
+{
+    return matb_t(n, ll, nfunc, psi, B);
+}
+int orc_normalize_d(const int* n, const double* ll, int nfunc, double* psi, double* diag)
+{
+    return normalize_t(n, ll, nfunc, psi, diag);
+}
+int orc_normalize_f(const int* n, const double* ll, int nfunc, float* psi, double* diag)
+{
+    return normalize_t(n, ll, nfunc, psi, diag);
+}
+
+/* ProjectedMatricesMehrstellen::updateHB (src/ProjectedMatricesMehrstellen.h:
+ * 55-62): HB = symm('l', 'l', S, theta) (S read from its lower triangle),
+ * then transpose(0.5, copy, 0.5): HB(i, j) = 0.5 HB(i, j) + 0.5 HB(j, i).
+ * Column-major n x n. */
+int orc_update_hb(int n, const double* S, const double* theta, double* HB)
+{
+    std::vector<double> t((size_t)n * n);
+#pragma omp parallel for
+    for (int j = 0; j < n; j++)
+        for (int i = 0; i < n; i++)
+        {
+            double s = 0.;
+            for (int k = 0; k < n; k++)
+            {
+                const double a = (i >= k) ? S[(size_t)k * n + i] : S[(size_t)i * n + k];
+                s += a * theta[(size_t)j * n + k];
+            }
+            t[(size_t)j * n + i] = s;
+        }
+    for (int j = 0; j < n; j++)
+        for (int i = 0; i < n; i++)
+            HB[(size_t)j * n + i] = 0.5 * t[(size_t)j * n + i] + 0.5 * t[(size_t)i * n + j];
+    return 0;
+}
+}

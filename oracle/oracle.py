@@ -328,3 +328,36 @@ def mgm(n, ll, lap_type, vh, rho, ghosts=0, cogr=10, max_sweeps=10, tol=1e-16, n
     if not ref:
         info["levels"] = int(out[5])
     return vh, info
+
+
+def matb(n, ll, psi, ref=False):
+    """B = psi^T (B psi) * vel (LocGridOrbitals::computeMatB), both
+    triangles; row-major numpy (nfunc, nfunc)."""
+    psi = np.ascontiguousarray(psi)
+    nf = psi.shape[0]
+    B = np.zeros((nf, nf))
+    gn, gl = _grid(n, ll)
+    name = f"ref_matb_{_sfx(psi)}" if ref else f"orc_matb_{_sfx(psi)}"
+    _call(ref_lib() if ref else lib(), name, gn, gl, nf, _p(psi), _p(B))
+    return B.T.copy()
+
+
+def normalize(n, ll, psi, ref=False):
+    """LocGridOrbitals::normalize: returns (normalized copy of psi, diagS)."""
+    out = np.array(psi, copy=True, order="C")
+    nf = out.shape[0]
+    d = np.zeros(nf)
+    gn, gl = _grid(n, ll)
+    name = f"ref_normalize_{_sfx(out)}" if ref else f"orc_normalize_{_sfx(out)}"
+    _call(ref_lib() if ref else lib(), name, gn, gl, nf, _p(out), _p(d))
+    return out, d
+
+
+def update_hb(S, th):
+    """HB = sym(S theta) (ProjectedMatricesMehrstellen::updateHB), row-major."""
+    n = S.shape[0]
+    Sc = np.ascontiguousarray(np.asarray(S, dtype=np.float64).T)
+    tc = np.ascontiguousarray(np.asarray(th, dtype=np.float64).T)
+    out = np.zeros((n, n))
+    _call(lib(), "orc_update_hb", n, _p(Sc), _p(tc), _p(out))
+    return out.T.copy()

@@ -398,6 +398,53 @@ int residual(const int* n, const double* ll, int nfunc, const T* psi, const T* h
     return 0;
 }
 
+/* LocGridOrbitals::computeMatB (src/LocGridOrbitals.cc:1428-1487) on one
+ * subdomain: LapOper.rhs per function (pb::Laph4M::rhs), MPgemmTN of psi
+ * and the result, then the scaling by vel and the |x| > 1e-14 filter of the
+ * conversion to the distributed matrix (restated: SquareLocalMatrices::scal
+ * and LocalMatrices2DistMatrix::accumulate are outside this build). */
+template <typename T>
+int matb(const int* n, const double* ll, int nfunc, const T* psi, double* B)
+{
+    pb::Grid g = make_grid(n, ll, 1);
+    const int np = (int)g.size();
+    pb::Laph4M<T> lap(g);
+    std::vector<T> work((size_t)np * nfunc);
+    for (int i = 0; i < nfunc; i++)
+    {
+        pb::GridFunc<T> gf(g, 1, 1, 1);
+        gf.assign(psi + (size_t)i * np, 'd');
+        lap.rhs(gf, work.data() + (size_t)i * np);
+    }
+    MPgemmTN(nfunc, nfunc, np, 1., psi, np, work.data(), np, 0., B, nfunc);
+    const double vel = g.vel();
+    for (size_t k = 0; k < (size_t)nfunc * nfunc; k++)
+    {
+        double x = B[k] * vel;
+        if (!(std::fabs(x) > 1.e-14)) x = 0.;
+        B[k] = x;
+    }
+    return 0;
+}
+
+/* LocGridOrbitals::normalize (src/LocGridOrbitals.cc:2261-2311): diagS_i =
+ * vel * MPdot(psi_i, psi_i), then MPscal(1 / sqrt(diagS_i)) per function --
+ * the reference's own MPdot / MPscal on one subdomain. */
+template <typename T>
+int normalize(const int* n, const double* ll, int nfunc, T* psi, double* diag)
+{
+    pb::Grid g = make_grid(n, ll, 1);
+    const int np = (int)g.size();
+    const double vel = g.vel();
+    for (int i = 0; i < nfunc; i++)
+        diag[i] = vel * LinearAlgebraUtils<MemorySpace::Host>::MPdot(np, psi + (size_t)i * np,
+                            psi + (size_t)i * np);
+    for (int i = 0; i < nfunc; i++)
+        LinearAlgebraUtils<MemorySpace::Host>::MPscal(np, 1. / std::sqrt(diag[i]),
+            psi + (size_t)i * np);
+    return 0;
+}
+
 template <typename T>
 int mgm(const int* n, const double* ll, int lap_type, int ng, int cogr, int max_sweeps,
     double tol, int nu1, int nu2, T* vh, const T* rho, double* out)
@@ -419,6 +466,10 @@ int ref_mult_matrix_d(int np, int nf, const double* p, const double* th, double*
 int ref_mult_matrix_f(int np, int nf, const float* p, const double* th, float* o) { return mult_matrix(np, nf, p, th, o); }
 int ref_residual_d(const int* n, const double* ll, int nf, const double* p, const double* h, const double* th, double* o) { return residual(n, ll, nf, p, h, th, o); }
 int ref_residual_f(const int* n, const double* ll, int nf, const float* p, const float* h, const double* th, float* o) { return residual(n, ll, nf, p, h, th, o); }
+int ref_matb_d(const int* n, const double* ll, int nf, const double* p, double* B) { return matb(n, ll, nf, p, B); }
+int ref_matb_f(const int* n, const double* ll, int nf, const float* p, double* B) { return matb(n, ll, nf, p, B); }
+int ref_normalize_d(const int* n, const double* ll, int nf, double* p, double* d) { return normalize(n, ll, nf, p, d); }
+int ref_normalize_f(const int* n, const double* ll, int nf, float* p, double* d) { return normalize(n, ll, nf, p, d); }
 int ref_mgm_d(const int* n, const double* ll, int t, int ng, int cogr, int ms, double tol, int nu1, int nu2, double* vh, const double* rho, double* out)
 { return mgm(n, ll, t, ng, cogr, ms, tol, nu1, nu2, vh, rho, out); }
 int ref_mgm_f(const int* n, const double* ll, int t, int ng, int cogr, int ms, double tol, int nu1, int nu2, float* vh, const float* rho, double* out)

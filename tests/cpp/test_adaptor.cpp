@@ -286,6 +286,82 @@ static void test_residual_and_mgm()
     std::printf("ok   computeResidualUsingHPhi, multiplyByMatrix, pb::Mgm (%d V-cycles)\n", nb);
 }
 
+/* LocGridOrbitals::normalize, computeMatB and ProjectedMatricesMehrstellen
+ * on three plane waves along x, sin(kx), sin(2kx), cos(kx): the
+ * Mehrstellen right-hand side acts on a wave of wave number q as
+ * 5/6 + cos(q h)/6, so after normalization B is diagonal with those
+ * entries, invB their inverses, theta = invB H for diagonal H, and
+ * HB = theta for S = I. */
+static void test_matb_normalize()
+{
+    const double origin[3] = { 0., 0., 0. }, ll[3] = { 6.4, 4.8, 8.0 };
+    const unsigned n[3] = { 32, 24, 40 };
+    pb::Grid grid(origin, ll, n, 1);
+    const int nf = 3;
+    OrbitalBlock<double> phi(grid, nf);
+    const double kx = 2 * M_PI / ll[0], h = grid.hgrid(0);
+    const double q[nf] = { kx, 2 * kx, kx };
+    std::vector<double> all((size_t)nf * grid.size());
+    for (int f = 0; f < nf; f++)
+        for (unsigned x = 0; x < n[0]; x++)
+            for (unsigned yz = 0; yz < n[1] * n[2]; yz++)
+                all[(size_t)f * grid.size() + (size_t)x * n[1] * n[2] + yz]
+                    = (f + 2.) * (f == 2 ? std::cos(q[f] * x * h) : std::sin(q[f] * x * h));
+    phi.set(all.data());
+    phi.normalize();
+    std::vector<double> u(all.size());
+    phi.get(u.data());
+    for (int f = 0; f < nf; f++)
+    {
+        double s2 = 0.;
+        for (size_t i = 0; i < grid.size(); i++)
+            s2 += u[(size_t)f * grid.size() + i] * u[(size_t)f * grid.size() + i];
+        CHECK(std::fabs(s2 * grid.vel() - 1.) < 1e-12, "normalize: vel |psi|^2 = %.16g", s2 * grid.vel());
+    }
+    DeviceArray<double> B((size_t)nf * nf);
+    phi.computeMatB(B);
+    std::vector<double> hb((size_t)nf * nf);
+    B.download(hb.data(), hb.size());
+    double mu[nf];
+    for (int f = 0; f < nf; f++)
+        mu[f] = 5. / 6. + std::cos(q[f] * h) / 6.;
+    double err = 0.;
+    for (int j = 0; j < nf; j++)
+        for (int i = 0; i < nf; i++)
+            err = std::max(err, std::fabs(hb[(size_t)j * nf + i] - (i == j ? mu[i] : 0.)));
+    CHECK(err < 1e-13, "computeMatB vs 5/6 + cos(qh)/6: %g", err);
+    ProjectedMatricesMehrstellen pm(phi.ctx(), nf);
+    pm.initializeMatB(B);
+    pm.computeInvB();
+    std::vector<double> hd((size_t)nf * nf, 0.), id((size_t)nf * nf, 0.);
+    const double eps[nf] = { -0.5, 0.25, 1.5 };
+    for (int i = 0; i < nf; i++)
+    {
+        hd[(size_t)i * nf + i] = eps[i];
+        id[(size_t)i * nf + i] = 1.;
+    }
+    DeviceArray<double> H(hd.size()), S(id.size()), theta(hd.size()), HB(hd.size());
+    H.upload(hd.data(), hd.size());
+    S.upload(id.data(), id.size());
+    pm.updateTheta(H, theta);
+    pm.updateHB(S, theta, HB);
+    std::vector<double> th(hd.size()), hbm(hd.size()), ib(hd.size());
+    theta.download(th.data(), th.size());
+    HB.download(hbm.data(), hbm.size());
+    pm.getInvB().download(ib.data(), ib.size());
+    err = 0.;
+    for (int j = 0; j < nf; j++)
+        for (int i = 0; i < nf; i++)
+        {
+            const double t = i == j ? eps[i] / mu[i] : 0.;
+            err = std::max(err, std::fabs(th[(size_t)j * nf + i] - t));
+            err = std::max(err, std::fabs(hbm[(size_t)j * nf + i] - t));
+            err = std::max(err, std::fabs(ib[(size_t)j * nf + i] - (i == j ? 1. / mu[i] : 0.)));
+        }
+    CHECK(err < 1e-13, "computeInvB / updateTheta / updateHB: %g", err);
+    std::printf("ok   normalize, computeMatB, ProjectedMatricesMehrstellen\n");
+}
+
 int main()
 {
     try
@@ -296,6 +372,7 @@ int main()
         test_gram_matrix();
         test_hamiltonian_and_precond();
         test_residual_and_mgm();
+        test_matb_normalize();
     }
     catch (const std::exception& e)
     {

@@ -84,6 +84,9 @@ def main():
         out[f"res_hpsi_{tag}"] = hp
         out[f"mm_{tag}"] = O.mult_matrix(p, th, ref=True)
         out[f"res_{tag}"] = O.residual(n, ll, p, hp, th, ref=True)
+        # computeMatB and normalize on the same block
+        out[f"matb_{tag}"] = O.matb(n, ll, p, ref=True)
+        out[f"norm_psi_{tag}"], out[f"norm_diag_{tag}"] = O.normalize(n, ll, p, ref=True)
     # pb::Mgm on one field, every operator (6 V-cycles, nu1 = nu2 = 2)
     n = (16, 12, 20)
     ll = (16 * 0.4, 12 * 0.4, 20 * 0.4)

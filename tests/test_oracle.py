@@ -55,6 +55,30 @@ def test_residual_matches_reference_vectors(G, tag, dt):
     assert np.array_equal(O.residual(n, ll, psi, hp, th), G[f"res_{tag}"])
 
 
+@pytest.mark.parametrize("tag,dt", [("d", np.float64), ("f", np.float32)])
+def test_matb_and_normalize_match_reference_vectors(G, tag, dt):
+    n = tuple(int(x) for x in G["res_n"])
+    ll = tuple(float(x) for x in G["res_ll"])
+    psi = G["res_psi"].astype(dt)
+    assert np.array_equal(O.matb(n, ll, psi), G[f"matb_{tag}"])
+    out, d = O.normalize(n, ll, psi)
+    assert np.array_equal(out, G[f"norm_psi_{tag}"])
+    assert np.array_equal(d, G[f"norm_diag_{tag}"])
+
+
+def test_update_hb_oracle_vs_numpy():
+    rng = np.random.default_rng(5)
+    A = rng.standard_normal((9, 9))
+    S = A @ A.T + 9 * np.eye(9)
+    th = rng.standard_normal((9, 9))
+    # only the lower triangle of S is read
+    S_low = np.tril(S) + np.triu(rng.standard_normal((9, 9)), 1)
+    hb = O.update_hb(S_low, th)
+    ref = 0.5 * (S @ th) + 0.5 * (S @ th).T
+    assert np.array_equal(hb, hb.T)
+    assert np.max(np.abs(hb - ref)) < 1e-12 * np.max(np.abs(ref))
+
+
 @pytest.mark.parametrize("lap", range(5))
 def test_mgm_matches_reference_vectors(G, lap):
     n = tuple(int(x) for x in G["mgm_n"])
