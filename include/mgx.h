@@ -390,6 +390,50 @@ int mgx_residual_cols(mgx_ctx* ctx, int mode, mgx_dtype dtype, const void* psi,
     void* work, void* res, void* stream);
 
 /* ---------------------------------------------------------------- */
+/* Anderson extrapolation of the orbital update (AndersonMix<T>,      */
+/* src/AndersonMix.cc:21-321): the accelerated branch of              */
+/* ABPG<T>::update_states (src/ABPG.cc:118-126).                      */
+/* ---------------------------------------------------------------- */
+
+#define MGX_ANDERSON_MAX_M 8
+
+typedef struct mgx_anderson mgx_anderson;
+
+/* What one update did: the history length used (after the reference's
+ * shortening), how many times it was shortened, and the coefficients. */
+typedef struct mgx_anderson_info
+{
+    int mm;
+    int reductions;
+    double theta[MGX_ANDERSON_MAX_M];
+} mgx_anderson_info;
+
+/* AndersonMix<T>(m, beta, x): history of m (x, f) pairs of nfunc x ld
+ * blocks of dtype, device memory owned by the handle (2 m blocks);
+ * 0 <= m <= MGX_ANDERSON_MAX_M. */
+int mgx_anderson_create(mgx_ctx* ctx, int m, double beta, mgx_dtype dtype, size_t ld,
+    int nfunc, mgx_anderson** mix);
+int mgx_anderson_destroy(mgx_anderson* mix);
+/* AndersonMix<T>::restart: forget the history. */
+int mgx_anderson_restart(mgx_anderson* mix);
+
+/* AndersonMix<T>::update(res, work) after res.scal(fscale) (the ABPG step
+ * passes fscale = 0.5 * precond_factor and res = the preconditioned
+ * residual): x (the orbital block, nfunc x ld, updated in place) moves to
+ * factor x + sum_j theta_j x_j + beta (factor f' + sum_j theta_j f_j),
+ * f' = fscale f, factor = 1 - sum_j theta_j; the coefficients solve the
+ * normal equations of the differences f' - f_j under the diagonal dot
+ * product sum_k vel <a_k, b_k> (S^-1)(k, k) (LocGridOrbitals::
+ * dotProductDiagonal), invS the device S^-1 (n x n; only its diagonal is
+ * read; unused on the first update).  The old x and f' enter the history.
+ * fbar (may be NULL or alias f) receives the mixed residual that the
+ * reference leaves in res.  A history matrix that is not positive definite
+ * returns MGX_NOT_SPD (the reference continues with a failed factor).
+ * Synchronous (the small system is solved on the host). */
+int mgx_anderson_update(mgx_anderson* mix, void* x, const void* f, double fscale,
+    const double* invS, void* fbar, mgx_anderson_info* info, void* stream);
+
+/* ---------------------------------------------------------------- */
 /* Poisson multigrid (pb::Mgm, src/pb/Mgm.h:20-112, with pb::Vcycle,  */
 /* src/pb/Vcycle.h:28-249) on one field of the context grid.          */
 /* ---------------------------------------------------------------- */

@@ -65,6 +65,14 @@ class MgmResult(ctypes.Structure):
                 ("converged", ctypes.c_int), ("levels", ctypes.c_int)]
 
 
+ANDERSON_MAX_M = 8
+
+
+class AndersonInfo(ctypes.Structure):
+    _fields_ = [("mm", ctypes.c_int), ("reductions", ctypes.c_int),
+                ("theta", ctypes.c_double * ANDERSON_MAX_M)]
+
+
 _LIB = None
 _vp = ctypes.c_void_p
 _i = ctypes.c_int
@@ -114,6 +122,10 @@ _SIGS = {
     "mgx_residual": [_vp, _i, _i, _vp, _vp, _sz, _i, _vp, _i, _vp, _vp, _vp],
     "mgx_residual_cols": [_vp, _i, _i, _vp, _vp, _sz, _i, _vp, _i, _i, _vp, _vp, _vp],
     "mgx_mgm": [_vp, ctypes.POINTER(MgmParams), _i, _vp, _vp, ctypes.POINTER(MgmResult), _vp],
+    "mgx_anderson_create": [_vp, _i, _d, _i, _sz, _i, ctypes.POINTER(_vp)],
+    "mgx_anderson_destroy": [_vp],
+    "mgx_anderson_restart": [_vp],
+    "mgx_anderson_update": [_vp, _vp, _vp, _d, _vp, _vp, ctypes.POINTER(AndersonInfo), _vp],
 }
 
 # every entry point declared in include/mgx.h
@@ -500,6 +512,49 @@ class Context:
         _check(load().mgx_residual(self.handle, mode, _dtype(psi), p, ph, ld, nf, _ptr(tc),
                                    1 if apply_B else 0, _ptr(work), _ptr(out), _stream(stream)))
         return out
+
+
+class Anderson:
+    """AndersonMix of an orbital block: m history pairs owned by the library
+    (mgx_anderson_*)."""
+
+    def __init__(self, ctx, m, beta, x):
+        _, ld, nf = _block(x, ctx.npts)
+        self.ctx = ctx
+        self.nfunc = nf
+        self.handle = ctypes.c_void_p()
+        _check(load().mgx_anderson_create(ctx.handle, int(m), float(beta), _dtype(x), ld, nf,
+                                          ctypes.byref(self.handle)))
+
+    def update(self, x, f, fscale=1.0, invS=None, fbar=None, stream=None):
+        """x moves by one Anderson step with the residual fscale * f; invS:
+        the FP64 device S^-1 whose diagonal weights the dot products.
+        Returns {"mm", "reductions", "theta"}."""
+        px, ldx, nf = _block(x, self.ctx.npts)
+        pf, ldf, _ = _block(f, self.ctx.npts)
+        if nf != self.nfunc or ldf != ldx:
+            raise ValueError("x and f must be blocks of the mixer's shape")
+        if invS is not None and (invS.dtype != torch.float64 or not invS.is_contiguous()):
+            raise ValueError("invS must be a contiguous FP64 (n, n) tensor")
+        info = AndersonInfo()
+        _check(load().mgx_anderson_update(self.handle, px, pf, float(fscale), _ptr(invS), _ptr(fbar),
+                                          ctypes.byref(info), _stream(stream)))
+        return {"mm": info.mm, "reductions": info.reductions,
+                "theta": [info.theta[j] for j in range(max(info.mm, 0))]}
+
+    def restart(self):
+        _check(load().mgx_anderson_restart(self.handle))
+
+    def close(self):
+        if self.handle:
+            load().mgx_anderson_destroy(self.handle)
+            self.handle = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class Masks:

@@ -82,7 +82,8 @@ class OrbitalSweep:
 
     def __init__(self, ctx, V, nfunc, mode="mixed", gemm=None, lap_type=capi.LAP_MEHR4,
                  maxlevels=2, gamma=None, precond_chunk=0, precond_factor=1.0,
-                 chunk_funcs=0, fuse_update=True, use_matb=True, device="cuda"):
+                 chunk_funcs=0, fuse_update=True, use_matb=True, anderson_m=0,
+                 anderson_beta=1.0, device="cuda"):
         self.ctx = ctx
         self.mode = mode
         self.lap_type = lap_type
@@ -113,8 +114,12 @@ class OrbitalSweep:
         self.diagS = torch.empty(nfunc, dtype=torch.float64, device=device)
         self.precond_chunk = precond_chunk
         # the update psi += alpha P(res) inside the last fine-level sweep
-        # (full-block schedule only; the chunked one defers the update)
-        self.fuse_update = bool(fuse_update) and not self.chunk
+        # (full-block schedule without Anderson mixing only; the chunked one
+        # defers the update)
+        self.anderson_m = int(anderson_m)
+        self.fuse_update = bool(fuse_update) and not self.chunk and self.anderson_m == 0
+        self.anderson_beta = float(anderson_beta)
+        self.mixer = None
         self.alpha = 0.5 * precond_factor
         self.theta = None
         if gamma is None:
@@ -135,11 +140,20 @@ class OrbitalSweep:
         if phase is not None:
             self.marks.append([phase, e, None])
 
-    def run(self, psi, timed=False, update=True):
+    def run(self, psi, timed=False, update=True, accelerate=None):
         """One sweep; psi is updated in place (unless update is False).
+        With anderson_m > 0 the update is the Anderson extrapolation
+        (accelerate, default on) or the plain step (accelerate False, the
+        history untouched), as ABPG<T>::update_states switches.
         Returns the device tensor holding the energy tr(HB S^-1) (Ry)."""
         ctx = self.ctx
         lazy = self.fuse_update and update
+        if accelerate is None:
+            accelerate = self.anderson_m > 0
+        if accelerate and self.mixer is None:
+            if self.anderson_m <= 0:
+                raise ValueError("acceleration needs anderson_m > 0")
+            self.mixer = capi.Anderson(ctx, self.anderson_m, self.anderson_beta, psi)
         if not lazy:
             self._mark(timed, "normalize")
             ctx.normalize(psi, diag=self.diagS)
@@ -180,7 +194,7 @@ class OrbitalSweep:
                                chunk=self.precond_chunk, out=self.corr)
                 self._mark(timed, "update")
                 if update:
-                    capi.axpy(self.alpha, self.corr, psi)
+                    self._update(psi, self.corr, Sinv, accelerate)
         else:
             # theta.T is the column-major buffer: row j holds column j
             thc = self.theta.T
@@ -197,11 +211,24 @@ class OrbitalSweep:
                 hc.copy_(cb)
             self._mark(timed, "update")
             if update:
-                capi.axpy(self.alpha, self.hpsi, psi)
+                self._update(psi, self.hpsi, Sinv, accelerate)
         self._mark(timed)
         if timed:
             self.timed_runs += 1
         return e
+
+    def _update(self, psi, corr, Sinv, accelerate):
+        """psi += alpha corr, or the Anderson step with the residual alpha corr
+        and the dot-product weights of S^-1 (AndersonMix<T>::update)."""
+        if accelerate:
+            self.last_mix = self.mixer.update(psi, corr, self.alpha, Sinv)
+        else:
+            capi.axpy(self.alpha, corr, psi)
+
+    def restart_mixing(self):
+        """AndersonMix<T>::restart (ABPG's restartMixing)."""
+        if self.mixer is not None:
+            self.mixer.restart()
 
     def correction(self):
         """P(res) of the last run (the block psi was moved along); not kept

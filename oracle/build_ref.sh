@@ -28,8 +28,21 @@ for tu in $TUS; do
 done
 $CXX $FLAGS $INC -c "$HERE/ref_driver.cpp" -o "$OUT/obj/ref_driver.o" &
 pids="$pids $!"
+# AndersonMix<T>::update, TESTING build, one instantiation per storage type
+# over the block type of shim_anderson/Solution.h
+# The include guards of the reference's orbital headers are predefined: the
+# TESTING build instantiates AndersonMix only for the shim's block type and
+# needs none of their (ScaLAPACK / HDF5) dependencies.
+AINC="-DMGMOL_EXTENDEDGRIDORBITALS_H -DLOCALGRIDORBITALS_H -I$HERE/shim_anderson $INC"
+$CXX $FLAGS -DTESTING -DSolution=SolutionF $AINC -c "$SRC/AndersonMix.cc" -o "$OUT/obj/AndersonMix_f.o" &
+pids="$pids $!"
+$CXX $FLAGS -DTESTING -DSolution=SolutionD $AINC -c "$SRC/AndersonMix.cc" -o "$OUT/obj/AndersonMix_d.o" &
+pids="$pids $!"
+$CXX $FLAGS $AINC -c "$HERE/ref_anderson.cpp" -o "$OUT/obj/ref_anderson.o" &
+pids="$pids $!"
 $CXX $FLAGS -c "$HERE/shim/blas_shim.cpp" -o "$OUT/obj/blas_shim.o" &
 pids="$pids $!"
 for p in $pids; do wait $p; done
-$CXX $FLAGS -shared -o "$OUT/libmgref.so" $OBJS "$OUT/obj/ref_driver.o" "$OUT/obj/blas_shim.o"
+$CXX $FLAGS -shared -o "$OUT/libmgref.so" $OBJS "$OUT/obj/ref_driver.o" "$OUT/obj/blas_shim.o" \
+    "$OUT/obj/AndersonMix_f.o" "$OUT/obj/AndersonMix_d.o" "$OUT/obj/ref_anderson.o"
 echo "build_ref: $OUT/libmgref.so"

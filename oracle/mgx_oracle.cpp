@@ -1792,3 +1792,329 @@ int orc_update_hb(int n, const double* S, const double* theta, double* HB)
     return 0;
 }
 }
+
+/* ------------------------------------------------------------------ */
+/* Anderson extrapolation (AndersonMix<T>::update).                     */
+/* ------------------------------------------------------------------ */
+
+/* eigenvalues (ascending) of the symmetric n x n matrix in the lower
+ * triangle of a (column-major, leading dimension lda), cyclic Jacobi: the
+ * DSYEV('N', 'l') of src/AndersonMix.cc:138 */
+static void orc_sym_eig(const double* a, int n, int lda, double* w)
+{
+    std::vector<double> A((size_t)n * n);
+    for (int j = 0; j < n; j++)
+        for (int i = j; i < n; i++)
+            A[i + (size_t)j * n] = A[j + (size_t)i * n] = a[i + (size_t)j * lda];
+    for (int sweep = 0; sweep < 100; sweep++)
+    {
+        double off = 0., tot = 0.;
+        for (size_t t = 0; t < A.size(); t++)
+        {
+            tot += A[t] * A[t];
+            if (t % n != t / n) off += A[t] * A[t];
+        }
+        if (off == 0. || off <= 1e-30 * tot) break;
+        for (int p = 0; p < n - 1; p++)
+            for (int q = p + 1; q < n; q++)
+            {
+                const double apq = A[p + (size_t)q * n];
+                if (apq == 0.) continue;
+                const double tau = (A[q + (size_t)q * n] - A[p + (size_t)p * n]) / (2. * apq);
+                const double t = (tau >= 0. ? 1. : -1.) / (std::fabs(tau) + std::sqrt(1. + tau * tau));
+                const double c = 1. / std::sqrt(1. + t * t), s = t * c;
+                for (int r = 0; r < n; r++)
+                {
+                    const double x = A[r + (size_t)p * n], y = A[r + (size_t)q * n];
+                    A[r + (size_t)p * n] = c * x - s * y;
+                    A[r + (size_t)q * n] = s * x + c * y;
+                }
+                for (int r = 0; r < n; r++)
+                {
+                    const double x = A[p + (size_t)r * n], y = A[q + (size_t)r * n];
+                    A[p + (size_t)r * n] = c * x - s * y;
+                    A[q + (size_t)r * n] = s * x + c * y;
+                }
+            }
+    }
+    for (int i = 0; i < n; i++)
+        w[i] = A[i + (size_t)i * n];
+    std::sort(w, w + n);
+}
+
+/* DPOTRF + DPOTRS with uplo 'l' on the leading n x n block (leading
+ * dimension lda) of a copy of a; b overwritten; returns the DPOTRF info */
+static int orc_chol_solve(const double* a0, int n, int lda, double* b)
+{
+    std::vector<double> a(a0, a0 + (size_t)lda * n);
+    for (int j = 0; j < n; j++)
+    {
+        double d = a[j + (size_t)j * lda];
+        for (int k = 0; k < j; k++)
+            d -= a[j + (size_t)k * lda] * a[j + (size_t)k * lda];
+        if (!(d > 0.)) return j + 1;
+        d = std::sqrt(d);
+        a[j + (size_t)j * lda] = d;
+        for (int i = j + 1; i < n; i++)
+        {
+            double t = a[i + (size_t)j * lda];
+            for (int k = 0; k < j; k++)
+                t -= a[i + (size_t)k * lda] * a[j + (size_t)k * lda];
+            a[i + (size_t)j * lda] = t / d;
+        }
+    }
+    for (int i = 0; i < n; i++)
+    {
+        double t = b[i];
+        for (int k = 0; k < i; k++)
+            t -= a[i + (size_t)k * lda] * b[k];
+        b[i] = t / a[i + (size_t)i * lda];
+    }
+    for (int i = n - 1; i >= 0; i--)
+    {
+        double t = b[i];
+        for (int k = i + 1; k < n; k++)
+            t -= a[k + (size_t)i * lda] * b[k];
+        b[i] = t / a[i + (size_t)i * lda];
+    }
+    return 0;
+}
+
+/* the orbital block arithmetic the update uses (LocGridOrbitals over
+ * BlockVector and mputils): MPscal, MPaxpy, v -= s in the storage type, and
+ * the diagonal dot product sum_k (double)(MPdot_k * vel) * invS(k, k) */
+template <typename T>
+struct OrcBlocks
+{
+    int nfunc;
+    size_t npts;
+    double vel;
+    const double* invs;
+    static void scal(std::vector<T>& u, double a)
+    {
+        if (a == 1.) return;
+        for (auto& v : u)
+            v = (a == 0.) ? (T)0 : (T)(a * (double)v);
+    }
+    static void axpy(std::vector<T>& y, double a, const std::vector<T>& x)
+    {
+        for (size_t i = 0; i < y.size(); i++)
+            y[i] += (T)(a * (double)x[i]);
+    }
+    static void sub(std::vector<T>& v, const std::vector<T>& s)
+    {
+        for (size_t i = 0; i < v.size(); i++)
+            v[i] -= s[i];
+    }
+    double dot(const std::vector<T>& a, const std::vector<T>& b) const
+    {
+        double tr = 0.;
+        std::vector<double> ss(nfunc);
+        for (int k = 0; k < nfunc; k++)
+        {
+            double d = 0.;
+            for (size_t p = 0; p < npts; p++)
+                d += (double)a[k * npts + p] * (double)b[k * npts + p];
+            ss[k] = d * vel;
+        }
+        for (int k = 0; k < nfunc; k++)
+            tr += ss[k] * invs[k];
+        return tr;
+    }
+};
+
+/* AndersonMix<T>::update (src/AndersonMix.cc:63-321) for nsteps residuals
+ * res_s = fscale * f_s: history of m pairs, mm grown by one per call up to
+ * m; mat / rhs from the differences f - f_i; mm shortened while the
+ * matrix rescaled to unit diagonal has a determinant (product of its
+ * eigenvalues) below 0.01 and whenever a coefficient leaves [-3, 0.5] with
+ * mm > 1; a lone coefficient outside is reset; then x and f are mixed and
+ * the old x and f enter the history.  invs: nsteps x nfunc weights
+ * (S^-1)(k, k).  xs_out[s]: x after update s.  Returns 1 where the
+ * reference's factorization fails. */
+template <typename T>
+struct OrcAnderson
+{
+    int m, mm = -1;
+    double beta;
+    std::vector<std::vector<T>> xi, fi;
+    std::vector<double> mat, rhs, theta;
+    OrcAnderson(int m_, double b, size_t nb)
+        : m(m_), beta(b), xi(m_, std::vector<T>(nb)), fi(m_, std::vector<T>(nb)),
+          mat((size_t)m_ * m_), rhs(m_), theta(m_)
+    {
+    }
+
+    /* one update of x with the residual f (already scaled); returns 1 where
+     * the reference's factorization fails */
+    int update(std::vector<T>& x, std::vector<T>& f, const OrcBlocks<T>& B)
+    {
+        const double min_det = 0.01, max_theta = 0.5, min_theta = -3.;
+        if (mm < m) mm++;
+        if (mm > 0)
+        {
+            std::vector<std::vector<T>> u(mm, f);
+            for (int i = 0; i < mm; i++)
+                OrcBlocks<T>::sub(u[i], fi[i]);
+            for (int i = 0; i < mm; i++)
+            {
+                mat[(size_t)i * m + i] = B.dot(u[i], u[i]);
+                rhs[i]                 = B.dot(u[i], f);
+                for (int j = 0; j < i; j++)
+                    mat[(size_t)j * m + i] = B.dot(u[i], u[j]);
+            }
+            bool flag = true;
+            while (flag)
+            {
+                flag = false;
+                for (int i = 0; i < mm; i++)
+                    theta[i] = rhs[i];
+                while (mm > 1)
+                {
+                    std::vector<double> t(mat);
+                    for (int i = 0; i < mm; i++)
+                    {
+                        const double alpha = 1. / std::sqrt(t[(size_t)(m + 1) * i]);
+                        for (int j = 0; j <= i; j++)
+                            t[(size_t)j * m + i] *= alpha;
+                        for (int j = i; j < mm; j++)
+                            t[(size_t)i * m + j] *= alpha;
+                    }
+                    std::vector<double> w(mm);
+                    orc_sym_eig(t.data(), mm, m, w.data());
+                    double det = 1.;
+                    for (int i = 0; i < mm; i++)
+                        det *= w[i];
+                    if (det < min_det)
+                        mm--;
+                    else
+                        break;
+                }
+                if (orc_chol_solve(mat.data(), mm, m, theta.data()) != 0) return 1;
+                for (int j = 0; j < mm; j++)
+                {
+                    if (theta[j] > max_theta)
+                    {
+                        if (mm > 1)
+                        {
+                            mm--;
+                            flag = true;
+                            break;
+                        }
+                        theta[j] = theta[j] > 1. ? -0.5 : 0.;
+                    }
+                    else if (theta[j] < min_theta)
+                    {
+                        if (mm > 1)
+                        {
+                            mm--;
+                            flag = true;
+                            break;
+                        }
+                        theta[j] = min_theta;
+                    }
+                }
+            }
+        }
+        double factor = 1.;
+        for (int j = 0; j < mm; j++)
+            factor -= theta[j];
+        if (m > 0)
+        {
+            std::vector<T> xold(x);
+            if (mm > 0) OrcBlocks<T>::scal(x, factor);
+            for (int j = 0; j < mm; j++)
+                OrcBlocks<T>::axpy(x, theta[j], xi[j]);
+            std::rotate(xi.rbegin(), xi.rbegin() + 1, xi.rend());
+            xi[0] = xold;
+            std::vector<T> fold(f);
+            if (mm > 0) OrcBlocks<T>::scal(f, factor);
+            for (int j = 0; j < mm; j++)
+                OrcBlocks<T>::axpy(f, theta[j], fi[j]);
+            std::rotate(fi.rbegin(), fi.rbegin() + 1, fi.rend());
+            fi[0] = fold;
+        }
+        OrcBlocks<T>::axpy(x, mm > 0 ? beta : 1., f);
+        return 0;
+    }
+};
+
+/* AndersonMix<T>::update (src/AndersonMix.cc:63-321) for nsteps residuals
+ * res_s = fscale * f_s: history of m pairs, mm grown by one per call up to
+ * m; mat / rhs from the differences f - f_i; mm shortened while the
+ * matrix rescaled to unit diagonal has a determinant (product of its
+ * eigenvalues) below 0.01 and whenever a coefficient leaves [-3, 0.5] with
+ * mm > 1; a lone coefficient outside is reset; then x and f are mixed and
+ * the old x and f enter the history.  invs: nsteps x nfunc weights
+ * (S^-1)(k, k).  xs_out[s]: x after update s.  Returns 1 where the
+ * reference's factorization fails. */
+template <typename T>
+static int anderson_t(int npts, int nfunc, int m, double beta, double vel, const double* invs,
+    const T* x0, int nsteps, const T* fseq, double fscale, T* xs_out)
+{
+    const size_t nb = (size_t)nfunc * npts;
+    std::vector<T> x(x0, x0 + nb);
+    OrcAnderson<T> mix(m, beta, nb);
+    OrcBlocks<T> B{ nfunc, (size_t)npts, vel, nullptr };
+    for (int s = 0; s < nsteps; s++)
+    {
+        B.invs = invs + (size_t)s * nfunc;
+        std::vector<T> f(fseq + s * nb, fseq + (s + 1) * nb);
+        OrcBlocks<T>::scal(f, fscale);
+        if (mix.update(x, f, B)) return 1;
+        std::copy(x.begin(), x.end(), xs_out + s * nb);
+    }
+    return 0;
+}
+
+/* a mixer that lives across calls (for checking an iteration whose
+ * residuals depend on x): handle = orc_anderson_new, then one step per
+ * orc_anderson_step (x updated in place), orc_anderson_free */
+template <typename T>
+static void* anderson_new(int m, double beta, long nb)
+{
+    return new OrcAnderson<T>(m, beta, (size_t)nb);
+}
+template <typename T>
+static int anderson_step(void* h, int npts, int nfunc, double vel, const double* invs, T* x,
+    const T* f0, double fscale)
+{
+    auto* mix = static_cast<OrcAnderson<T>*>(h);
+    const size_t nb = (size_t)nfunc * npts;
+    OrcBlocks<T> B{ nfunc, (size_t)npts, vel, invs };
+    std::vector<T> xv(x, x + nb), f(f0, f0 + nb);
+    OrcBlocks<T>::scal(f, fscale);
+    if (mix->update(xv, f, B)) return 1;
+    std::copy(xv.begin(), xv.end(), x);
+    return 0;
+}
+
+extern "C" {
+void* orc_anderson_new_f(int m, double beta, long nb) { return anderson_new<float>(m, beta, nb); }
+void* orc_anderson_new_d(int m, double beta, long nb) { return anderson_new<double>(m, beta, nb); }
+void orc_anderson_free_f(void* h) { delete static_cast<OrcAnderson<float>*>(h); }
+void orc_anderson_free_d(void* h) { delete static_cast<OrcAnderson<double>*>(h); }
+int orc_anderson_step_f(void* h, int npts, int nfunc, double vel, const double* invs, float* x,
+    const float* f, double fscale)
+{
+    return anderson_step(h, npts, nfunc, vel, invs, x, f, fscale);
+}
+int orc_anderson_step_d(void* h, int npts, int nfunc, double vel, const double* invs, double* x,
+    const double* f, double fscale)
+{
+    return anderson_step(h, npts, nfunc, vel, invs, x, f, fscale);
+}
+}
+
+extern "C" {
+int orc_anderson_f(int npts, int nfunc, int m, double beta, double vel, const double* invs,
+    const float* x0, int nsteps, const float* fseq, double fscale, float* xs_out)
+{
+    return anderson_t(npts, nfunc, m, beta, vel, invs, x0, nsteps, fseq, fscale, xs_out);
+}
+int orc_anderson_d(int npts, int nfunc, int m, double beta, double vel, const double* invs,
+    const double* x0, int nsteps, const double* fseq, double fscale, double* xs_out)
+{
+    return anderson_t(npts, nfunc, m, beta, vel, invs, x0, nsteps, fseq, fscale, xs_out);
+}
+}

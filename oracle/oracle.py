@@ -361,3 +361,46 @@ def update_hb(S, th):
     out = np.zeros((n, n))
     _call(lib(), "orc_update_hb", n, _p(Sc), _p(tc), _p(out))
     return out.T.copy()
+
+
+def anderson(x0, fseq, m, beta, vel, invs, fscale=1.0, ref=False):
+    """nsteps AndersonMix updates of x0 (nfunc, npts) with the residuals
+    fscale * fseq[s] (nsteps, nfunc, npts); invs (nsteps, nfunc) the weights
+    (S^-1)(k, k) of each step.  Returns x after every update."""
+    x0 = np.ascontiguousarray(x0)
+    fseq = np.ascontiguousarray(fseq, dtype=x0.dtype)
+    invs = np.ascontiguousarray(invs, dtype=np.float64)
+    ns, nf, npt = fseq.shape
+    out = np.zeros((ns, nf, npt), dtype=x0.dtype)
+    L = ref_lib() if ref else lib()
+    name = f"{'ref' if ref else 'orc'}_anderson_{_sfx(x0)}"
+    _call(L, name, npt, nf, m, ctypes.c_double(beta), ctypes.c_double(vel), _p(invs), _p(x0), ns,
+          _p(fseq), ctypes.c_double(fscale), _p(out))
+    return out
+
+
+class AndersonState:
+    """The oracle's AndersonMix kept across steps (for an iteration whose
+    residuals depend on x)."""
+
+    def __init__(self, m, beta, shape, dtype):
+        self.sfx = "d" if np.dtype(dtype) == np.float64 else "f"
+        L = lib()
+        new = getattr(L, f"orc_anderson_new_{self.sfx}")
+        new.restype = ctypes.c_void_p
+        self.h = ctypes.c_void_p(new(m, ctypes.c_double(beta), ctypes.c_long(int(np.prod(shape)))))
+        self.shape = shape
+
+    def step(self, x, f, vel, invs_diag, fscale):
+        """x (numpy, updated in place) moves by one update with fscale * f."""
+        nf, npt = self.shape
+        invs_diag = np.ascontiguousarray(invs_diag, dtype=np.float64)
+        f = np.ascontiguousarray(f, dtype=x.dtype)
+        _call(lib(), f"orc_anderson_step_{self.sfx}", self.h, npt, nf, ctypes.c_double(vel),
+              _p(invs_diag), _p(x), _p(f), ctypes.c_double(fscale))
+        return x
+
+    def close(self):
+        if self.h:
+            getattr(lib(), f"orc_anderson_free_{self.sfx}")(self.h)
+            self.h = None

@@ -4,9 +4,11 @@
  * (test infrastructure only).  Routines that the hot path never reaches
  * abort if called.
  */
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
+#include <vector>
 
 extern "C" {
 static void oracle_blas_unused(const char* n)
@@ -80,8 +82,119 @@ void oracle_dsymv() { oracle_blas_unused("dsymv"); }
 void oracle_dsymm() { oracle_blas_unused("dsymm"); }
 void oracle_drot() { oracle_blas_unused("drot"); }
 void oracle_srot() { oracle_blas_unused("srot"); }
-void oracle_dpotrf() { oracle_blas_unused("dpotrf"); }
-void oracle_dpotrs() { oracle_blas_unused("dpotrs"); }
 void oracle_dpotri() { oracle_blas_unused("dpotri"); }
-void oracle_dsyev() { oracle_blas_unused("dsyev"); }
+
+/* LAPACK stand-ins for the small Anderson system (AndersonMix.cc calls
+ * DSYEV, DPOTRF, DPOTRS with uplo 'l'; only 'l' is implemented).
+ * DPOTRF: the unblocked left-looking Cholesky of LAPACK's DPOTF2, info = j
+ * (1-based) at the first non-positive pivot. */
+void oracle_dpotrf(const char* uplo, const int* n, double* a, const int* lda, int* info)
+{
+    *info = 0;
+    if (!(*uplo == 'l' || *uplo == 'L')) { oracle_blas_unused("dpotrf upper"); return; }
+    const int N = *n, ld = *lda;
+    for (int j = 0; j < N; j++)
+    {
+        double ajj = a[j + j * ld];
+        for (int k = 0; k < j; k++)
+            ajj -= a[j + k * ld] * a[j + k * ld];
+        if (!(ajj > 0.))
+        {
+            a[j + j * ld] = ajj;
+            *info = j + 1;
+            return;
+        }
+        ajj = std::sqrt(ajj);
+        a[j + j * ld] = ajj;
+        for (int i = j + 1; i < N; i++)
+        {
+            double t = a[i + j * ld];
+            for (int k = 0; k < j; k++)
+                t -= a[i + k * ld] * a[j + k * ld];
+            a[i + j * ld] = t / ajj;
+        }
+    }
+}
+
+/* DPOTRS, lower: L y = b, then L^T x = y, for nrhs columns of b */
+void oracle_dpotrs(const char* uplo, const int* n, const int* nrhs, const double* a,
+    const int* lda, double* b, const int* ldb, int* info)
+{
+    *info = 0;
+    if (!(*uplo == 'l' || *uplo == 'L')) { oracle_blas_unused("dpotrs upper"); return; }
+    const int N = *n, ld = *lda;
+    for (int r = 0; r < *nrhs; r++)
+    {
+        double* x = b + (size_t)r * *ldb;
+        for (int i = 0; i < N; i++)
+        {
+            double t = x[i];
+            for (int k = 0; k < i; k++)
+                t -= a[i + k * ld] * x[k];
+            x[i] = t / a[i + i * ld];
+        }
+        for (int i = N - 1; i >= 0; i--)
+        {
+            double t = x[i];
+            for (int k = i + 1; k < N; k++)
+                t -= a[k + i * ld] * x[k];
+            x[i] = t / a[i + i * ld];
+        }
+    }
+}
+
+/* DSYEV with jobz 'N': eigenvalues (ascending) of the symmetric matrix in
+ * the lower triangle of a, by cyclic Jacobi rotations (LAPACK reduces to
+ * tridiagonal form and iterates; the eigenvalues agree to rounding) */
+void oracle_dsyev(const char* jobz, const char* uplo, const int* n, double* a, const int* lda,
+    double* w, double* work, const int* lwork, int* info)
+{
+    (void)work;
+    (void)lwork;
+    *info = 0;
+    if (!(*jobz == 'n' || *jobz == 'N') || !(*uplo == 'l' || *uplo == 'L'))
+    {
+        oracle_blas_unused("dsyev with vectors or upper");
+        return;
+    }
+    const int N = *n, ld = *lda;
+    std::vector<double> A((size_t)N * N);
+    for (int j = 0; j < N; j++)
+        for (int i = j; i < N; i++)
+            A[i + (size_t)j * N] = A[j + (size_t)i * N] = a[i + j * ld];
+    for (int sweep = 0; sweep < 100; sweep++)
+    {
+        double off = 0., tot = 0.;
+        for (size_t t = 0; t < A.size(); t++)
+        {
+            tot += A[t] * A[t];
+            if (t % N != t / N) off += A[t] * A[t];
+        }
+        if (off == 0. || off <= 1e-30 * tot) break;
+        for (int p = 0; p < N - 1; p++)
+            for (int q = p + 1; q < N; q++)
+            {
+                const double apq = A[p + (size_t)q * N];
+                if (apq == 0.) continue;
+                const double tau = (A[q + (size_t)q * N] - A[p + (size_t)p * N]) / (2. * apq);
+                const double t = (tau >= 0. ? 1. : -1.) / (std::fabs(tau) + std::sqrt(1. + tau * tau));
+                const double c = 1. / std::sqrt(1. + t * t), sn = t * c;
+                for (int r = 0; r < N; r++)
+                {
+                    const double arp = A[r + (size_t)p * N], arq = A[r + (size_t)q * N];
+                    A[r + (size_t)p * N] = c * arp - sn * arq;
+                    A[r + (size_t)q * N] = sn * arp + c * arq;
+                }
+                for (int r = 0; r < N; r++)
+                {
+                    const double apr = A[p + (size_t)r * N], aqr = A[q + (size_t)r * N];
+                    A[p + (size_t)r * N] = c * apr - sn * aqr;
+                    A[q + (size_t)r * N] = sn * apr + c * aqr;
+                }
+            }
+    }
+    for (int i = 0; i < N; i++)
+        w[i] = A[i + (size_t)i * N];
+    std::sort(w, w + N);
+}
 }

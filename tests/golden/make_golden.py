@@ -106,6 +106,29 @@ def main():
     vh, info = O.mgm(n, ll, 0, vh0.astype(np.float32), rho.astype(np.float32), max_sweeps=3,
                      tol=1e-10, ref=True)
     out["mgm0_vh_f"] = vh
+    # AndersonMix<T>::update on residual sequences: a converging one, a
+    # nearly collinear one (the determinant safeguard shortens the history)
+    # and one with repeated residuals (coefficients outside [-3, 0.5])
+    rng = np.random.default_rng(1007)
+    nf, npt, ns = 5, 640, 9
+    x0 = rng.standard_normal((nf, npt))
+    g = rng.standard_normal((nf, npt))
+    seqs = {
+        "conv": np.stack([(0.6 ** s) * rng.standard_normal((nf, npt)) for s in range(ns)]),
+        "collinear": np.stack([(0.7 ** s) * (g + 1e-3 * rng.standard_normal((nf, npt)))
+                               for s in range(ns)]),
+        "repeat": np.stack([(1.0 + 1e-4 * s) * g + 1e-6 * rng.standard_normal((nf, npt))
+                            for s in range(ns)]),
+    }
+    invs = 1.0 + 0.2 * rng.random((ns, nf))
+    out["and_x0"] = x0
+    out["and_invs"] = invs
+    for name, fs in seqs.items():
+        out[f"and_f_{name}"] = fs
+        for tag, dt in (("d", np.float64), ("f", np.float32)):
+            for m in (1, 3):
+                out[f"and_{name}_m{m}_{tag}"] = O.anderson(x0.astype(dt), fs.astype(dt), m, 1.0,
+                                                           0.02, invs, fscale=0.5, ref=True)
     np.savez_compressed(os.path.join(HERE, "ref_vectors.npz"), **out)
     print("wrote", os.path.join(HERE, "ref_vectors.npz"), len(out), "arrays")
 

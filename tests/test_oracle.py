@@ -66,6 +66,15 @@ def test_matb_and_normalize_match_reference_vectors(G, tag, dt):
     assert np.array_equal(d, G[f"norm_diag_{tag}"])
 
 
+@pytest.mark.parametrize("name", ["conv", "collinear", "repeat"])
+@pytest.mark.parametrize("m", [1, 3])
+@pytest.mark.parametrize("tag,dt", [("d", np.float64), ("f", np.float32)])
+def test_anderson_matches_reference_vectors(G, name, m, tag, dt):
+    got = O.anderson(G["and_x0"].astype(dt), G[f"and_f_{name}"].astype(dt), m, 1.0, 0.02,
+                     G["and_invs"], fscale=0.5)
+    assert np.array_equal(got, G[f"and_{name}_m{m}_{tag}"])
+
+
 def test_update_hb_oracle_vs_numpy():
     rng = np.random.default_rng(5)
     A = rng.standard_normal((9, 9))
