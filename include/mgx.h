@@ -328,6 +328,13 @@ int mgx_normalize_scales(mgx_ctx* ctx, int n, const double* S, double* scale,
  * (host) receives 0 or the 1-based index of the first non-positive pivot;
  * the call then returns MGX_NOT_SPD instead of aborting. Synchronous. */
 int mgx_cholesky(mgx_ctx* ctx, int n, double* A, int* info, void* stream);
+/* mgx_cholesky without waiting for the result: *info (DEVICE int)
+ * receives 0 or the pivot index once the factorization has run on
+ * `stream`, and the caller checks it when convenient; the call itself
+ * returns at once, so that factorizations on several streams (each with its
+ * own ctx) overlap.  No counterpart in the reference. */
+int mgx_cholesky_async(mgx_ctx* ctx, int n, double* A, int* info, void* stream);
+
 /* GramMatrix::computeInverse (src/GramMatrix.cc:75-91): Sinv = (L L^T)^-1
  * from the factor L. */
 int mgx_inverse_from_cholesky(mgx_ctx* ctx, int n, const double* L,

@@ -113,6 +113,7 @@ _SIGS = {
     "mgx_normalize": [_vp, _i, _vp, _sz, _i, _vp, _vp],
     "mgx_normalize_scales": [_vp, _i, _vp, _vp, _vp],
     "mgx_cholesky": [_vp, _i, _vp, _ip, _vp],
+    "mgx_cholesky_async": [_vp, _i, _vp, _vp, _vp],
     "mgx_inverse_from_cholesky": [_vp, _i, _vp, _vp, _vp],
     "mgx_trace_prod": [_vp, _i, _vp, _vp, _vp, _vp],
     "mgx_theta": [_vp, _i, _vp, _vp, _vp, _vp],
@@ -407,10 +408,17 @@ class Context:
         _check(load().mgx_normalize_scales(self.handle, n, _ptr(S), _ptr(d), _stream(stream)))
         return d
 
-    def cholesky(self, S, stream=None):
-        """Lower factor L (returned as a row-major tensor) of symmetric S."""
+    def cholesky(self, S, stream=None, info=None):
+        """Lower factor L (returned as a row-major tensor) of symmetric S.
+        With info (a device int32 tensor) nothing waits for the
+        factorization: info receives 0 or the pivot index on the stream."""
         n = S.shape[0]
         A = S.T.contiguous().clone()
+        if info is not None:
+            if info.dtype != torch.int32 or not info.is_cuda:
+                raise ValueError("info must be a device int32 tensor")
+            _check(load().mgx_cholesky_async(self.handle, n, _ptr(A), _ptr(info), _stream(stream)))
+            return A.T
         info = ctypes.c_int(0)
         st = load().mgx_cholesky(self.handle, n, _ptr(A), ctypes.byref(info), _stream(stream))
         if st != MGX_OK:

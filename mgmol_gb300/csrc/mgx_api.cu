@@ -100,7 +100,7 @@ int matb_tcgen05(mgx_ctx*, int, const void*, size_t, size_t, int, double, double
 int update_hb(int, const double*, const double*, double*, cudaStream_t);
 int normalize(mgx_ctx*, int, void*, size_t, size_t, int, double, double*, cudaStream_t);
 int diag_rsqrt(mgx_ctx*, int, const double*, double*, cudaStream_t);
-int cholesky(mgx_ctx*, int, double*, int*, cudaStream_t);
+int cholesky(mgx_ctx*, int, double*, int*, cudaStream_t, int* info_dev = nullptr);
 int inverse_from_cholesky(mgx_ctx*, int, const double*, double*, cudaStream_t);
 int trace_prod(mgx_ctx*, int, const double*, const double*, double*, cudaStream_t);
 
@@ -726,6 +726,13 @@ int mgx_cholesky(mgx_ctx* ctx, int n, double* A, int* info, void* stream)
 {
     if (!ctx) return fail(MGX_BAD_ARG, "ctx is NULL");
     return cholesky(ctx, n, A, info, (cudaStream_t)stream);
+}
+
+int mgx_cholesky_async(mgx_ctx* ctx, int n, double* A, int* info, void* stream)
+{
+    if (!ctx) return fail(MGX_BAD_ARG, "ctx is NULL");
+    if (!info) return fail(MGX_BAD_ARG, "info is NULL");
+    return cholesky(ctx, n, A, nullptr, (cudaStream_t)stream, info);
 }
 
 int mgx_inverse_from_cholesky(mgx_ctx* ctx, int n, const double* L, double* Sinv,

@@ -516,12 +516,17 @@ static int dense_ws(mgx_ctx* ctx, int n, double** winv, double** panel,
     return MGX_OK;
 }
 
-int cholesky(mgx_ctx* ctx, int n, double* A, int* info_host, cudaStream_t s)
+/* info_host set: synchronous, *info_host receives the pivot index; else
+ * info_dev (device) receives it and nothing waits for the factorization */
+int cholesky(mgx_ctx* ctx, int n, double* A, int* info_host, cudaStream_t s,
+    int* info_dev = nullptr)
 {
-    if (n <= 0 || !A || !info_host) return fail(MGX_BAD_ARG, "cholesky: bad arguments");
+    if (n <= 0 || !A || (!info_host && !info_dev))
+        return fail(MGX_BAD_ARG, "cholesky: bad arguments");
     double *winv, *panel, *X;
     int* dinfo;
     MGX_TRY(dense_ws(ctx, n, &winv, &panel, &X, &dinfo));
+    if (info_dev) dinfo = info_dev;
     MGX_TRY(cuda_check(cudaMemsetAsync(dinfo, 0, sizeof(int), s), "info reset"));
     MGX_TRY(cuda_check(cudaFuncSetAttribute(potrf_diag_kernel,
                            cudaFuncAttributeMaxDynamicSharedMemorySize, DIAG_SMEM),
@@ -546,6 +551,7 @@ int cholesky(mgx_ctx* ctx, int n, double* A, int* info_host, cudaStream_t s)
     }
     zero_upper_kernel<<<std::min<size_t>(((size_t)n * n + 255) / 256, 4096), 256, 0, s>>>(A, n);
     MGX_LAUNCH_CHECK("zero_upper_kernel");
+    if (!info_host) return MGX_OK;
     int hinfo = 0;
     MGX_TRY(cuda_check(cudaMemcpyAsync(&hinfo, dinfo, sizeof(int), cudaMemcpyDeviceToHost, s),
         "info download"));

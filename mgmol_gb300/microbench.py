@@ -39,7 +39,7 @@ def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("op", choices=["gram", "hmat", "gram_hmat", "matb", "gram_hmat_matb", "mult",
                                    "residual", "hpsi", "precond", "mgm", "dense", "dense_b",
-                                   "normalize", "h2d", "h2d_kernel", "all"])
+                                   "dense_parts", "normalize", "h2d", "h2d_kernel", "all"])
     ap.add_argument("--streams", type=int, default=1, help="h2d: concurrent copy streams")
     ap.add_argument("--grid", type=int, nargs=3, default=[96, 96, 32])
     ap.add_argument("--h", type=float, default=0.25)
@@ -87,6 +87,27 @@ def main(argv=None):
             ms = _time(lambda: ctx.gram_hmat_matb(psi, hpsi, mode, work=wb), args.warmup, args.reps)
             del wb
             work, unit = 2 * N * (N + 1) * npts + 2.0 * N * N * npts, "TFLOP/s"
+        elif op == "dense_parts":
+            # each FP64 piece of the dense phase on its own (N from --nfunc)
+            S, H, Bm = ctx.gram_hmat_matb(psi, hpsi, mode)
+            L = ctx.cholesky(S)
+            Sinv = ctx.inverse_from_cholesky(L).contiguous()
+            th = ctx.theta(Sinv, H)
+            parts = {
+                "cholesky": (lambda: ctx.cholesky(S), N ** 3 / 3),
+                "inverse_from_cholesky": (lambda: ctx.inverse_from_cholesky(L), N ** 3),
+                "theta_symm": (lambda: ctx.theta(Sinv, H), 2 * N ** 3),
+                "theta_from_cholesky": (lambda: ctx.theta_from_cholesky(L, H), 2 * N ** 3),
+                "update_hb": (lambda: ctx.update_hb(S, th), 2 * N ** 3),
+                "trace_prod": (lambda: ctx.trace_prod(H, Sinv), 2 * N ** 2),
+            }
+            for name, (fn, fl) in parts.items():
+                pms = _time(fn, args.warmup, args.reps)
+                line = {"op": "dense_parts", "part": name, "nfunc": N, "ms": pms,
+                        "achieved": fl / (pms * 1e-3) / 1e12, "unit": "TFLOP/s"}
+                out.append(line)
+                print(json.dumps(line), flush=True)
+            continue
         elif op == "normalize":
             ms = _time(lambda: ctx.normalize(psi), args.warmup, args.reps)
             work, unit = 3 * N * npts * s, "GB/s"

@@ -120,6 +120,13 @@ class OrbitalSweep:
         self.fuse_update = bool(fuse_update) and not self.chunk and self.anderson_m == 0
         self.anderson_beta = float(anderson_beta)
         self.mixer = None
+        # the S side of the dense algebra (Cholesky and inverse of S, HB and
+        # the energy) runs on a second stream with its own context, next to
+        # the critical path theta = B^-1 H -> residual -> V-cycle
+        self.side = torch.cuda.Stream(device=device) if self.use_matb else None
+        self.sctx = capi.Context(ctx.n, ctx.ll) if self.use_matb else None
+        self.info = torch.zeros(2, dtype=torch.int32, device=device)
+        self.Sinv = None
         self.alpha = 0.5 * precond_factor
         self.theta = None
         if gamma is None:
@@ -168,15 +175,25 @@ class OrbitalSweep:
         self._mark(timed, "dense")
         # Hm holds H column-major; the matrix calls want the row-major view
         H = self.Hm.T
-        L = ctx.cholesky(self.S)
-        Sinv = ctx.inverse_from_cholesky(L).contiguous()
         if self.use_matb:
+            main = torch.cuda.current_stream()
+            self.side.wait_stream(main)
             # computeInvB + updateTheta: theta = B^-1 H from the factor of B
-            self.theta, _ = ctx.theta_from_cholesky(ctx.cholesky(self.Bm), H)
-            e = ctx.trace_prod(ctx.update_hb(self.S, self.theta), Sinv)
+            self.theta, _ = ctx.theta_from_cholesky(ctx.cholesky(self.Bm, info=self.info[0:1]), H)
+            theta_done = torch.cuda.Event()
+            theta_done.record(main)
+            with torch.cuda.stream(self.side):
+                # computeGramAndInvS, updateHB and getEigSum beside it
+                L = self.sctx.cholesky(self.S, info=self.info[1:2])
+                self.Sinv = self.sctx.inverse_from_cholesky(L).contiguous()
+                self.side.wait_event(theta_done)
+                e = self.sctx.trace_prod(self.sctx.update_hb(self.S, self.theta), self.Sinv)
         else:
-            e = ctx.trace_prod(H, Sinv)
-            self.theta = ctx.theta(Sinv, H)
+            L = ctx.cholesky(self.S)
+            self.Sinv = ctx.inverse_from_cholesky(L).contiguous()
+            e = ctx.trace_prod(H, self.Sinv)
+            self.theta = ctx.theta(self.Sinv, H)
+        Sinv = self.Sinv
         if lazy:
             ctx.normalize_scales(self.S, out=self.dscale)
         if not self.chunk:
@@ -212,6 +229,12 @@ class OrbitalSweep:
             self._mark(timed, "update")
             if update:
                 self._update(psi, self.hpsi, Sinv, accelerate)
+        if self.use_matb:
+            torch.cuda.current_stream().wait_stream(self.side)
+            if int(self.info.max()) != 0:
+                which = "B" if int(self.info[0]) else "S"
+                raise capi.MgxError(capi.MGX_NOT_SPD, f"Cholesky of {which}: leading minor "
+                                    f"{int(self.info.max())} not positive")
         self._mark(timed)
         if timed:
             self.timed_runs += 1
@@ -221,6 +244,8 @@ class OrbitalSweep:
         """psi += alpha corr, or the Anderson step with the residual alpha corr
         and the dot-product weights of S^-1 (AndersonMix<T>::update)."""
         if accelerate:
+            if self.side is not None:
+                torch.cuda.current_stream().wait_stream(self.side)
             self.last_mix = self.mixer.update(psi, corr, self.alpha, Sinv)
         else:
             capi.axpy(self.alpha, corr, psi)
