@@ -408,23 +408,31 @@ constexpr int DIAG_SMEM = 2 * NB * (NB + 1) * sizeof(double);
 
 /* Factor the diagonal block A[k0:k0+nb, k0:k0+nb] (lower), write L_kk in
  * place (upper part zeroed) and its inverse W (nb x nb, column-major, ld
- * NB) to `winv`.  Sets *info to the 1-based global pivot index on failure. */
+ * NB) to `winv`.  Sets *info to the 1-based global pivot index on failure.
+ * Right-looking by columns, the column scaled by the reciprocal of its
+ * pivot (as LAPACK's dpotf2 scales); the trailing update has a thread per
+ * column of the block and four row groups.  The inverse is formed row by
+ * row, W(i, c) = -W(i, i) sum_{c <= q < i} L(i, q) W(q, c), four threads per
+ * column summing a quarter of each dot product. */
 __global__ void __launch_bounds__(256) potrf_diag_kernel(double* A, int n, int k0,
     int nb, double* winv, int* info)
 {
     extern __shared__ double dsm[];
     double(*L)[NB + 1] = reinterpret_cast<double(*)[NB + 1]>(dsm);
     double(*W)[NB + 1] = reinterpret_cast<double(*)[NB + 1]>(dsm + NB * (NB + 1));
+    __shared__ double rdiag[NB];
     __shared__ int bad;
     if (*info != 0) return;
     const int tid = threadIdx.x;
-    for (int e = tid; e < nb * nb; e += blockDim.x)
+    for (int e = tid; e < NB * NB; e += blockDim.x)
     {
-        const int i = e % nb, j = e / nb;
-        L[i][j]     = (i >= j) ? A[(size_t)(k0 + j) * n + k0 + i] : 0.;
+        const int i = e % NB, j = e / NB;
+        L[i][j]     = (i >= j && i < nb && j < nb) ? A[(size_t)(k0 + j) * n + k0 + i] : 0.;
+        W[i][j]     = 0.;
     }
     if (tid == 0) bad = 0;
     __syncthreads();
+    const int cl = tid & 63, rg = tid >> 6;
     for (int j = 0; j < nb; j++)
     {
         if (tid == 0)
@@ -433,19 +441,25 @@ __global__ void __launch_bounds__(256) potrf_diag_kernel(double* A, int n, int k
             if (!(d > 0.) || !isfinite(d))
                 bad = k0 + j + 1;
             else
-                L[j][j] = sqrt(d);
+            {
+                const double sq = sqrt(d);
+                L[j][j]         = sq;
+                rdiag[j]        = 1. / sq;
+            }
         }
         __syncthreads();
         if (bad) break;
-        const double djj = L[j][j];
+        const double r = rdiag[j];
         for (int i = j + 1 + tid; i < nb; i += blockDim.x)
-            L[i][j] /= djj;
+            L[i][j] *= r;
         __syncthreads();
-        // trailing update of the block (lower part)
-        for (int e = tid; e < nb * nb; e += blockDim.x)
+        // trailing update of the block: column c, rows i >= c
+        const int c = j + 1 + cl;
+        if (c < nb)
         {
-            const int i = e % nb, c = e / nb;
-            if (c > j && i >= c) L[i][c] -= L[i][j] * L[c][j];
+            const double lcj = L[c][j];
+            for (int i = j + 1 + rg; i < nb; i += 4)
+                if (i >= c) L[i][c] -= L[i][j] * lcj;
         }
         __syncthreads();
     }
@@ -454,27 +468,62 @@ __global__ void __launch_bounds__(256) potrf_diag_kernel(double* A, int n, int k
         if (tid == 0) atomicCAS(info, 0, bad);
         return;
     }
-    // inverse of the lower-triangular block, column by column
-    for (int e = tid; e < nb * nb; e += blockDim.x)
-        W[e % nb][e / nb] = 0.;
+    for (int i = tid; i < nb; i += blockDim.x)
+        W[i][i] = rdiag[i];
     __syncthreads();
-    for (int c = tid; c < nb; c += blockDim.x)
     {
-        W[c][c] = 1. / L[c][c];
-        for (int i = c + 1; i < nb; i++)
+        const int c = tid >> 2, part = tid & 3;
+        for (int i = 1; i < nb; i++)
         {
-            double s = 0.;
-            for (int q = c; q < i; q++)
-                s -= L[i][q] * W[q][c];
-            W[i][c] = s / L[i][i];
+            double sum = 0.;
+            if (c < i)
+                for (int q = c + part; q < i; q += 4)
+                    sum += L[i][q] * W[q][c];
+            sum += __shfl_xor_sync(0xffffffffu, sum, 1);
+            sum += __shfl_xor_sync(0xffffffffu, sum, 2);
+            if (c < i && part == 0) W[i][c] = -rdiag[i] * sum;
+            __syncthreads();
         }
     }
-    __syncthreads();
     for (int e = tid; e < nb * nb; e += blockDim.x)
     {
         const int i = e % nb, j = e / nb;
         A[(size_t)(k0 + j) * n + k0 + i] = (i >= j) ? L[i][j] : 0.;
         winv[(size_t)j * NB + i]         = W[i][j];
+    }
+}
+
+/* The panel of a Cholesky step in place: rows [k0 + nb, n) of columns
+ * k0 .. k0+nb of A (column-major, leading dimension n) become
+ * A_panel W^T, W = L_kk^-1 (lower, column-major, leading dimension NB):
+ * the L_ik = A_ik L_kk^-T of the blocked algorithm.  16 rows per CTA. */
+constexpr int PANEL_ROWS = 16;
+
+__global__ void __launch_bounds__(256) panel_trsm_kernel(double* A, int n, int k0, int nb,
+    const double* __restrict__ winv)
+{
+    __shared__ double Ws[NB][NB + 1];
+    __shared__ double As[PANEL_ROWS][NB + 1];
+    const int tid = threadIdx.x;
+    const int r0  = k0 + nb + blockIdx.x * PANEL_ROWS;
+    for (int e = tid; e < NB * NB; e += blockDim.x)
+    {
+        const int i = e % NB, j = e / NB;
+        Ws[i][j]    = (i >= j && i < nb) ? winv[(size_t)j * NB + i] : 0.;
+    }
+    for (int e = tid; e < PANEL_ROWS * NB; e += blockDim.x)
+    {
+        const int rr = e % PANEL_ROWS, q = e / PANEL_ROWS;
+        As[rr][q]    = (q < nb && r0 + rr < n) ? A[(size_t)(k0 + q) * n + r0 + rr] : 0.;
+    }
+    __syncthreads();
+    const int rr = tid % PANEL_ROWS;
+    for (int c = tid / PANEL_ROWS; c < nb; c += blockDim.x / PANEL_ROWS)
+    {
+        double acc = 0.;
+        for (int q = 0; q <= c; q++)
+            acc += As[rr][q] * Ws[c][q];
+        if (r0 + rr < n) A[(size_t)(k0 + c) * n + r0 + rr] = acc;
     }
 }
 
@@ -540,14 +589,13 @@ int cholesky(mgx_ctx* ctx, int n, double* A, int* info_host, cudaStream_t s,
         const int m = n - k0 - nb; // rows below the block
         if (m <= 0) continue;
         double* Ap = A + (size_t)k0 * n + k0 + nb; // panel A[k0+nb:, k0:k0+nb]
-        // panel <- A_panel * W^T   (L_ik = A_ik L_kk^-T)
-        MGX_TRY(dgemm(false, true, m, nb, nb, 1., Ap, n, winv + (size_t)kb * NB * NB,
-            NB, 0., panel, n, 0, s));
-        copy_panel_kernel<<<std::min(1024, (m * nb + 255) / 256), 256, 0, s>>>(panel, n, Ap, n, m, nb);
-        MGX_LAUNCH_CHECK("copy_panel_kernel");
+        // panel <- A_panel * W^T   (L_ik = A_ik L_kk^-T), in place
+        panel_trsm_kernel<<<(m + PANEL_ROWS - 1) / PANEL_ROWS, 256, 0, s>>>(A, n, k0, nb,
+            winv + (size_t)kb * NB * NB);
+        MGX_LAUNCH_CHECK("panel_trsm_kernel");
         // trailing update A22 -= P P^T (lower)
         double* A22 = A + (size_t)(k0 + nb) * n + k0 + nb;
-        MGX_TRY(dgemm(false, true, m, m, nb, -1., panel, n, panel, n, 1., A22, n, 1, s));
+        MGX_TRY(dgemm(false, true, m, m, nb, -1., Ap, n, Ap, n, 1., A22, n, 1, s));
     }
     zero_upper_kernel<<<std::min<size_t>(((size_t)n * n + 255) / 256, 4096), 256, 0, s>>>(A, n);
     MGX_LAUNCH_CHECK("zero_upper_kernel");
@@ -578,18 +626,25 @@ __global__ void __launch_bounds__(256) trinv_diag_kernel(const double* L, int n,
         W[i][j]     = 0.;
     }
     __syncthreads();
-    for (int c = tid; c < nb; c += blockDim.x)
+    // row by row as in potrf_diag_kernel: W(i, c) = -W(i, i) sum_{c <= q < i}
+    // T(i, q) W(q, c), four threads per column
+    for (int i = tid; i < nb; i += blockDim.x)
+        W[i][i] = 1. / T[i][i];
+    __syncthreads();
     {
-        W[c][c] = 1. / T[c][c];
-        for (int i = c + 1; i < nb; i++)
+        const int c = tid >> 2, part = tid & 3;
+        for (int i = 1; i < nb; i++)
         {
-            double s = 0.;
-            for (int q = c; q < i; q++)
-                s -= T[i][q] * W[q][c];
-            W[i][c] = s / T[i][i];
+            double sum = 0.;
+            if (c < i)
+                for (int q = c + part; q < i; q += 4)
+                    sum += T[i][q] * W[q][c];
+            sum += __shfl_xor_sync(0xffffffffu, sum, 1);
+            sum += __shfl_xor_sync(0xffffffffu, sum, 2);
+            if (c < i && part == 0) W[i][c] = -W[i][i] * sum;
+            __syncthreads();
         }
     }
-    __syncthreads();
     for (int e = tid; e < nb * nb; e += blockDim.x)
     {
         const int i = e % nb, j = e / nb;
