@@ -397,6 +397,26 @@ int mgx_residual_cols(mgx_ctx* ctx, int mode, mgx_dtype dtype, const void* psi,
     void* work, void* res, void* stream);
 
 /* ---------------------------------------------------------------- */
+/* Electronic density (Rho<T>, src/Rho.cc).                           */
+/* ---------------------------------------------------------------- */
+
+/* Rho<T>::computeRho for non-orthogonal orbitals (src/Rho.cc:282-320, with
+ * computeRhoSubdomainUsingBlas3, :359-450) and rescaleTotalCharge
+ * (:150-200): rho(p) = sum_j (Psi X)_j(p) psi_j(p), X the density matrix
+ * (nfunc x nfunc FP64, column-major, device), then charge = vel sum_p rho(p)
+ * and, when nel > 0 and the charge is positive, rho *= nel / charge.  A
+ * factor off 1 by more than 0.02 (where the reference aborts) returns
+ * MGX_BAD_ARG with rho unscaled.  rho: npts FP64 values (device); *charge
+ * (host, may be NULL) receives the charge before the rescaling.  mode as for
+ * mgx_mult_matrix; the tensor-core modes reduce the product against Psi in
+ * the product's epilogue, the CUDA-core modes form it in column chunks in
+ * `work` (work_funcs functions of ld values, or NULL for a block of at most
+ * 256 functions owned by ctx).  Synchronous. */
+int mgx_rho(mgx_ctx* ctx, int mode, mgx_dtype dtype, const void* psi, size_t ld, int nfunc,
+    const double* dm, double nel, double* rho, double* charge, void* work, int work_funcs,
+    void* stream);
+
+/* ---------------------------------------------------------------- */
 /* Anderson extrapolation of the orbital update (AndersonMix<T>,      */
 /* src/AndersonMix.cc:21-321): the accelerated branch of              */
 /* ABPG<T>::update_states (src/ABPG.cc:118-126).                      */

@@ -123,6 +123,7 @@ _SIGS = {
     "mgx_residual": [_vp, _i, _i, _vp, _vp, _sz, _i, _vp, _i, _vp, _vp, _vp],
     "mgx_residual_cols": [_vp, _i, _i, _vp, _vp, _sz, _i, _vp, _i, _i, _vp, _vp, _vp],
     "mgx_mgm": [_vp, ctypes.POINTER(MgmParams), _i, _vp, _vp, ctypes.POINTER(MgmResult), _vp],
+    "mgx_rho": [_vp, _i, _i, _vp, _sz, _i, _vp, _d, _vp, _dp, _vp, _i, _vp],
     "mgx_anderson_create": [_vp, _i, _d, _i, _sz, _i, ctypes.POINTER(_vp)],
     "mgx_anderson_destroy": [_vp],
     "mgx_anderson_restart": [_vp],
@@ -454,6 +455,20 @@ class Context:
                                         _ptr(theta_cols), nc, 1 if apply_B else 0, _ptr(work),
                                         _ptr(out), _stream(stream)))
         return out
+
+    # ------------------------------------------------------------ density
+    def rho(self, psi, X, mode=GEMM_FP64, nel=0.0, out=None, work=None, stream=None):
+        """Rho<T>::computeRho: (rho, charge) with rho(p) = sum_j (Psi X)_j(p)
+        psi_j(p) (X a row-major FP64 tensor), rescaled to nel electrons when
+        nel > 0."""
+        p, ld, nf = _block(psi, self.npts)
+        rho = torch.empty(self.npts, dtype=torch.float64, device=psi.device) if out is None else out
+        Xc = self._colmajor(X)
+        q = ctypes.c_double()
+        pw, nw = (None, 0) if work is None else _block(work, self.npts)[0::2]
+        _check(load().mgx_rho(self.handle, mode, _dtype(psi), p, ld, nf, _ptr(Xc), float(nel),
+                              _ptr(rho), ctypes.byref(q), pw, nw, _stream(stream)))
+        return rho, q.value
 
     # ------------------------------------------------------------ Poisson
     def mgm(self, vh, rho, lap_type=LAP_MEHR4, max_levels=10, max_sweeps=10, tol=1e-16, nu1=2,

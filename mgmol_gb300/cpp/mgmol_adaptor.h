@@ -20,6 +20,7 @@
 //   ProjectedMatricesMehrstellen::computeInvB / updateTheta / updateHB
 //                             src/ProjectedMatricesMehrstellen.cc:38-64,
 //                             src/ProjectedMatricesMehrstellen.h:49-62
+//   Rho<T>::computeRho (non-orthogonal orbitals) src/Rho.cc:124-450
 // Where the reference aborts (unsupported operator, failed Cholesky), these
 // classes throw mgx::Error carrying the C-ABI status.  Header only; link
 // against libmgx.so and the CUDA runtime.
@@ -553,6 +554,32 @@ public:
         check(mgx_update_hb(ctx_, n_, S.data(), theta.data(), HB.data(), nullptr),
             "ProjectedMatricesMehrstellen::updateHB");
     }
+};
+
+/* Rho<T>: the electronic density of a block of non-orthogonal orbitals
+ * (device, one FP64 value per grid point) */
+template <typename T>
+class Rho
+{
+    DeviceArray<double> rho_;
+
+public:
+    explicit Rho(const pb::Grid& g) : rho_(g.size()) {}
+    /* computeRho(orbitals, dm) then rescaleTotalCharge to nel electrons
+     * (src/Rho.cc:282-320, 124-200); throws where the reference aborts.
+     * Returns the charge before the rescaling. */
+    double computeRho(const OrbitalBlock<T>& orbitals, const DeviceArray<double>& dm, double nel,
+        int mode = -1)
+    {
+        if (mode < 0) mode = std::is_same<T, double>::value ? MGX_GEMM_FP64 : MGX_GEMM_BF16X3;
+        double q = 0.;
+        check(mgx_rho(orbitals.ctx(), mode, dtype_of<T>(), orbitals.psi(0), orbitals.numpt(),
+                  orbitals.chromatic_number(), dm.data(), nel, rho_.data(), &q, nullptr, 0,
+                  nullptr),
+            "Rho::computeRho");
+        return q;
+    }
+    const DeviceArray<double>& rho() const { return rho_; }
 };
 
 namespace pb

@@ -82,7 +82,7 @@ int gram_cuda_cores(mgx_ctx*, int, const void*, const void*, size_t, size_t,
 int psi_theta_cuda_cores(int, const void*, size_t, size_t, int, const double*, int, int,
     double, const void*, void*, cudaStream_t);
 int psi_theta_tcgen05(mgx_ctx*, int, const float*, size_t, size_t, int,
-    const double*, int, int, float, const float*, float*, cudaStream_t);
+    const double*, int, int, float, const float*, float*, cudaStream_t, double* rho = nullptr);
 int theta_product(int, const double*, const double*, double*, cudaStream_t);
 int theta_from_cholesky(mgx_ctx*, int, const double*, const double*, double*, double*,
     cudaStream_t);

@@ -188,6 +188,11 @@ struct Params
     // epilogue multiplies by sa->down * sb->down
     const ScaleSlot* sa = nullptr;
     const ScaleSlot* sb = nullptr;
+    // density epilogue (store mode): instead of storing the product,
+    // rho[i] += sum_j (float)(acc(i, j) * rpsi[j * ldr + i]) in FP64
+    double* rho       = nullptr;
+    const float* rpsi = nullptr;
+    size_t ldr        = 0;
 };
 
 // KIND 0: tf32 (NPROD 1); KIND 1: bf16 (NPROD 1 plain, 3 for hi/lo split).
@@ -332,6 +337,7 @@ __global__ void __launch_bounds__(THREADS, 1) gram_kernel(
         const int q   = warp & 3; // TMEM lane quarter this warp may access
         const int row = q * 32 + lane;
         const int i   = i0 + row;
+        double racc   = 0.; // density epilogue: this row's share
         if (got && nkb > 0)
         {
 #pragma unroll 1
@@ -348,7 +354,22 @@ __global__ void __launch_bounds__(THREADS, 1) gram_kernel(
                         for (int t = 0; t < 32; t++)
                             v[t] *= ds;
                     }
-                    if (i < p.nrows)
+                    if (p.rho != nullptr)
+                    {
+                        // each load instruction of the warp reads 32
+                        // consecutive points of one function
+                        if (i < p.nrows)
+                        {
+#pragma unroll
+                            for (int t = 0; t < 32; t++)
+                            {
+                                const int j = j0 + c0 + t;
+                                if (j < p.ncols)
+                                    racc += (double)(v[t] * p.rpsi[(size_t)j * p.ldr + i]);
+                            }
+                        }
+                    }
+                    else if (i < p.nrows)
                     {
                         // each store instruction of the warp covers 32
                         // consecutive points of one function: 128 bytes
@@ -378,6 +399,8 @@ __global__ void __launch_bounds__(THREADS, 1) gram_kernel(
         }
         else if (!got && p.err && lane == 0)
             atomicExch(p.err, MGX_TIMEOUT);
+        if (STORE && p.rho != nullptr && got && nkb > 0 && i < p.nrows)
+            atomicAdd(p.rho + i, racc);
     }
     fence_before_sync();
     __syncthreads();
@@ -1251,7 +1274,7 @@ int gram_hmat_tcgen05(mgx_ctx* ctx, int mode, const void* psi, const void* hpsi,
  * workspace; theta is converted once.  One CTA per 128 x BN output tile. */
 int psi_theta_tcgen05(mgx_ctx* ctx, int mode, const float* psi, size_t ld, size_t npts,
     int n, const double* theta, int ldt, int ncols, float beta, const float* cin, float* out,
-    cudaStream_t s)
+    cudaStream_t s, double* rho)
 {
     using namespace tc;
     const bool half       = (mode == MGX_GEMM_FP16X3);
@@ -1360,8 +1383,15 @@ int psi_theta_tcgen05(mgx_ctx* ctx, int mode, const float* psi, size_t ld, size_
         p.symmetric  = 0;
         p.C          = nullptr;
         p.err        = (int*)ctx->tc_err.ptr;
-        p.out        = out + p0;
+        p.out        = out ? out + p0 : nullptr;
         p.cin        = cin ? cin + p0 : nullptr;
+        if (rho)
+        {
+            // the density: the product is reduced against psi itself
+            p.rho  = rho + p0;
+            p.rpsi = psi + p0;
+            p.ldr  = ld;
+        }
         p.ldo        = ld;
         p.beta       = cin ? beta : 0.f;
         p.nrows      = Pc;

@@ -2118,3 +2118,65 @@ int orc_anderson_d(int npts, int nfunc, int m, double beta, double vel, const do
     return anderson_t(npts, nfunc, m, beta, vel, invs, x0, nsteps, fseq, fscale, xs_out);
 }
 }
+
+/* ------------------------------------------------------------------ */
+/* Electronic density.                                                  */
+/* ------------------------------------------------------------------ */
+
+/* Rho<T>::computeRho for non-orthogonal orbitals, one subdomain
+ * (src/Rho.cc:282-320, computeRhoSubdomainUsingBlas3 :359-450):
+ * product = MPgemmNN(psi, X) (FP64 accumulation, stored in the orbital
+ * type), rho(p) += product_j(p) * psi_j(p) (the product of two orbital-type
+ * values, added in FP64, j in order), then rescaleTotalCharge (:124-200):
+ * charge = vel * sum_p rho(p) in order; when charge > 0, t = nel / charge and
+ * rho *= t (MPscal).  Returns 1 where the reference aborts (|t - 1| > 0.02)
+ * and leaves rho unscaled then.  out[0] = charge, out[1] = t. */
+template <typename T>
+static int rho_t(const int* n, const double* ll, int nfunc, const T* psi, const double* X,
+    double nel, double* rho, double* out)
+{
+    const size_t np  = (size_t)n[0] * n[1] * n[2];
+    const double vel = (ll[0] / n[0]) * (ll[1] / n[1]) * (ll[2] / n[2]);
+    std::vector<T> prod(np * nfunc);
+#pragma omp parallel for
+    for (long p = 0; p < (long)np; p++)
+        for (int j = 0; j < nfunc; j++)
+        {
+            double s = 0.;
+            for (int i = 0; i < nfunc; i++)
+                s += (double)psi[(size_t)i * np + p] * X[(size_t)j * nfunc + i];
+            prod[(size_t)j * np + p] = (T)s;
+        }
+    for (size_t p = 0; p < np; p++)
+    {
+        double acc = 0.;
+        for (int j = 0; j < nfunc; j++)
+            acc += (double)(T)(prod[(size_t)j * np + p] * psi[(size_t)j * np + p]);
+        rho[p] = acc;
+    }
+    double q = 0.;
+    for (size_t p = 0; p < np; p++)
+        q += rho[p];
+    q *= vel;
+    out[0]   = q;
+    double t = 1.;
+    if (nel > 0. && q > 0.) t = nel / q;
+    out[1] = t;
+    if (std::fabs(t - 1.) > 0.02) return 1;
+    for (size_t p = 0; p < np; p++)
+        rho[p] *= t;
+    return 0;
+}
+
+extern "C" {
+int orc_rho_d(const int* n, const double* ll, int nfunc, const double* psi, const double* X,
+    double nel, double* rho, double* out)
+{
+    return rho_t(n, ll, nfunc, psi, X, nel, rho, out);
+}
+int orc_rho_f(const int* n, const double* ll, int nfunc, const float* psi, const double* X,
+    double nel, double* rho, double* out)
+{
+    return rho_t(n, ll, nfunc, psi, X, nel, rho, out);
+}
+}

@@ -404,3 +404,23 @@ class AndersonState:
         if self.h:
             getattr(lib(), f"orc_anderson_free_{self.sfx}")(self.h)
             self.h = None
+
+
+def rho(n, ll, psi, X, nel=0.0, ref=False):
+    """Density of the block with density matrix X (row-major numpy, n x n):
+    (rho, charge, factor); the reference arm returns the unscaled density of
+    its own MPgemmNN and loop (charge and factor None)."""
+    psi = np.ascontiguousarray(psi)
+    nf, npt = psi.shape
+    Xc = np.ascontiguousarray(np.asarray(X, dtype=np.float64).T)
+    out = np.zeros(npt)
+    if ref:
+        _call(ref_lib(), f"ref_rho_{_sfx(psi)}", npt, nf, _p(psi), _p(Xc), _p(out))
+        return out, None, None
+    gn, gl = _grid(n, ll)
+    info = np.zeros(2)
+    rc = getattr(lib(), f"orc_rho_{_sfx(psi)}")(gn, gl, nf, _p(psi), _p(Xc), ctypes.c_double(nel),
+                                                 _p(out), _p(info))
+    if rc != 0:
+        raise RuntimeError("density charge off by more than 2%")
+    return out, info[0], info[1]

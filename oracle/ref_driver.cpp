@@ -445,6 +445,24 @@ int normalize(const int* n, const double* ll, int nfunc, T* psi, double* diag)
     return 0;
 }
 
+/* Rho<T>::computeRhoSubdomainUsingBlas3 (src/Rho.cc:359-450) on one
+ * subdomain: the reference's MPgemmNN for the product, then its O(N^2)
+ * loop (product * phi added into the FP64 density; run here in the order j
+ * outer, points inner, which the reference leaves to OpenMP atomics).  No
+ * rescaling. */
+template <typename T>
+int rho_blas3(int np, int nfunc, const T* psi, const double* X, double* rho)
+{
+    std::vector<T> product((size_t)np * nfunc);
+    LinearAlgebraUtils<MemorySpace::Host>::MPgemmNN(np, nfunc, nfunc, 1., psi, np, X, nfunc, 0.,
+        product.data(), np);
+    std::fill(rho, rho + np, 0.);
+    for (int j = 0; j < nfunc; ++j)
+        for (int i = 0; i < np; ++i)
+            rho[i] += product[(size_t)j * np + i] * psi[(size_t)j * np + i];
+    return 0;
+}
+
 template <typename T>
 int mgm(const int* n, const double* ll, int lap_type, int ng, int cogr, int max_sweeps,
     double tol, int nu1, int nu2, T* vh, const T* rho, double* out)
@@ -466,6 +484,8 @@ int ref_mult_matrix_d(int np, int nf, const double* p, const double* th, double*
 int ref_mult_matrix_f(int np, int nf, const float* p, const double* th, float* o) { return mult_matrix(np, nf, p, th, o); }
 int ref_residual_d(const int* n, const double* ll, int nf, const double* p, const double* h, const double* th, double* o) { return residual(n, ll, nf, p, h, th, o); }
 int ref_residual_f(const int* n, const double* ll, int nf, const float* p, const float* h, const double* th, float* o) { return residual(n, ll, nf, p, h, th, o); }
+int ref_rho_d(int np, int nf, const double* p, const double* X, double* r) { return rho_blas3(np, nf, p, X, r); }
+int ref_rho_f(int np, int nf, const float* p, const double* X, double* r) { return rho_blas3(np, nf, p, X, r); }
 int ref_matb_d(const int* n, const double* ll, int nf, const double* p, double* B) { return matb(n, ll, nf, p, B); }
 int ref_matb_f(const int* n, const double* ll, int nf, const float* p, double* B) { return matb(n, ll, nf, p, B); }
 int ref_normalize_d(const int* n, const double* ll, int nf, double* p, double* d) { return normalize(n, ll, nf, p, d); }

@@ -359,7 +359,28 @@ static void test_matb_normalize()
             err = std::max(err, std::fabs(ib[(size_t)j * nf + i] - (i == j ? 1. / mu[i] : 0.)));
         }
     CHECK(err < 1e-13, "computeInvB / updateTheta / updateHB: %g", err);
-    std::printf("ok   normalize, computeMatB, ProjectedMatricesMehrstellen\n");
+    // Rho with the density matrix X = 2 I on the normalized waves: rho =
+    // 2 sum_f psi_f^2, whose charge is 2 nf
+    DeviceArray<double> X(hd.size());
+    std::vector<double> x2((size_t)nf * nf, 0.);
+    for (int i = 0; i < nf; i++)
+        x2[(size_t)i * nf + i] = 2.;
+    X.upload(x2.data(), x2.size());
+    Rho<double> rho(grid);
+    const double charge = rho.computeRho(phi, X, 2. * nf);
+    CHECK(std::fabs(charge - 2. * nf) < 1e-12, "Rho charge %.16g", charge);
+    std::vector<double> r(grid.size());
+    rho.rho().download(r.data(), r.size());
+    err = 0.;
+    for (size_t p = 0; p < grid.size(); p++)
+    {
+        double s2 = 0.;
+        for (int f = 0; f < nf; f++)
+            s2 += 2. * u[(size_t)f * grid.size() + p] * u[(size_t)f * grid.size() + p];
+        err = std::max(err, std::fabs(r[p] - s2));
+    }
+    CHECK(err < 1e-13, "Rho vs 2 sum psi^2: %g", err);
+    std::printf("ok   normalize, computeMatB, ProjectedMatricesMehrstellen, Rho\n");
 }
 
 int main()

@@ -78,6 +78,8 @@ def main():
     out["res_ll"] = np.array(ll)
     out["res_psi"] = psi
     out["res_theta"] = th
+    Xr = rng.standard_normal((7, 7))
+    out["rho_X"] = 2.0 * (Xr @ Xr.T / 7 + np.eye(7))
     for tag, dt in (("d", np.float64), ("f", np.float32)):
         p = psi.astype(dt)
         hp = O.hpsi(n, ll, 0, p, V, ref=True)
@@ -86,6 +88,8 @@ def main():
         out[f"res_{tag}"] = O.residual(n, ll, p, hp, th, ref=True)
         # computeMatB and normalize on the same block
         out[f"matb_{tag}"] = O.matb(n, ll, p, ref=True)
+        # the density of the block with a density matrix (unscaled)
+        out[f"rho_{tag}"] = O.rho(n, ll, p, out["rho_X"], ref=True)[0]
         out[f"norm_psi_{tag}"], out[f"norm_diag_{tag}"] = O.normalize(n, ll, p, ref=True)
     # pb::Mgm on one field, every operator (6 V-cycles, nu1 = nu2 = 2)
     n = (16, 12, 20)

@@ -75,6 +75,21 @@ def test_anderson_matches_reference_vectors(G, name, m, tag, dt):
     assert np.array_equal(got, G[f"and_{name}_m{m}_{tag}"])
 
 
+@pytest.mark.parametrize("tag,dt", [("d", np.float64), ("f", np.float32)])
+def test_rho_matches_reference_vectors(G, tag, dt):
+    n = tuple(int(x) for x in G["res_n"])
+    ll = tuple(float(x) for x in G["res_ll"])
+    rho, charge, t = O.rho(n, ll, G["res_psi"].astype(dt), G["rho_X"])
+    assert np.array_equal(rho, G[f"rho_{tag}"])
+    vel = np.prod([a / b for a, b in zip(ll, n)])
+    assert abs(charge - vel * G[f"rho_{tag}"].sum()) < 1e-12 * abs(charge)
+    # rescaled to a charge within 2 %: the density scales by nel / charge
+    scaled, c2, t2 = O.rho(n, ll, G["res_psi"].astype(dt), G["rho_X"], nel=1.01 * charge)
+    assert abs(t2 - 1.01) < 1e-12 and np.allclose(scaled, 1.01 * rho, rtol=1e-14, atol=0)
+    with pytest.raises(RuntimeError):
+        O.rho(n, ll, G["res_psi"].astype(dt), G["rho_X"], nel=1.1 * charge)
+
+
 def test_update_hb_oracle_vs_numpy():
     rng = np.random.default_rng(5)
     A = rng.standard_normal((9, 9))
