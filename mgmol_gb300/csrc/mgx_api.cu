@@ -143,6 +143,18 @@ static PlaneParams plane(const mgx_grid& g)
     return p;
 }
 
+int rhs_split_block(const mgx_grid& g, const float* u, size_t ldu, int nfunc, void* hi,
+    void* lo, int rows, cudaStream_t s)
+{
+    PlaneParams p = plane(g);
+    p.u          = u;
+    p.ldu        = ldu;
+    p.split_hi   = hi;
+    p.split_lo   = lo;
+    p.split_rows = rows;
+    return stencil_launch(OP_RHS_SPLIT, 0, MGX_F32, MGX_F32, p, make_level(g, 0), 0., nfunc, s);
+}
+
 int rhs_block(const mgx_grid& g, int dtype, const void* u, size_t ldu, void* out,
     size_t ldo, int nfunc, cudaStream_t s)
 {

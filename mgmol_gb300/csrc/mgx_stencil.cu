@@ -13,6 +13,7 @@
 //
 // Coefficients follow src/pb/FDkernels.cc (del2 2nd/4th/6th/8th and
 // Mehrstellen) and src/pb/Laph*.h (diagonals and Jacobi factors).
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -839,6 +840,27 @@ __global__ void __launch_bounds__(256) plane_vec_kernel(PlaneParams p, DevCoef<T
                         VH::set(q, v, uscale * (VH::get(q, v) + ualpha * VH::get(res, v)));
                     *reinterpret_cast<V4*>(updp + xoff + goff[k]) = q;
                 }
+                else if (OP == OP_RHS_SPLIT)
+                {
+                    if constexpr (sizeof(T) == 4 && VEC == 4)
+                    {
+                        // 4 consecutive points, never across a 64-point block
+                        const size_t pt = xoff + goff[k];
+                        const size_t o  = ((pt / 64) * (size_t)p.split_rows + f) * 64 + pt % 64;
+                        __align__(8) __nv_bfloat16 h[4], l[4];
+#pragma unroll
+                        for (int v = 0; v < 4; v++)
+                        {
+                            const float x = VH::get(res, v);
+                            h[v]          = __float2bfloat16_rn(x);
+                            l[v]          = __float2bfloat16_rn(x - __bfloat162float(h[v]));
+                        }
+                        *reinterpret_cast<uint2*>(reinterpret_cast<__nv_bfloat16*>(p.split_hi) + o)
+                            = *reinterpret_cast<const uint2*>(h);
+                        *reinterpret_cast<uint2*>(reinterpret_cast<__nv_bfloat16*>(p.split_lo) + o)
+                            = *reinterpret_cast<const uint2*>(l);
+                    }
+                }
                 else
                     *reinterpret_cast<V4*>(outp + xoff + goff[k]) = res;
                 if (is_jacobi(OP) && wp != nullptr)
@@ -1086,6 +1108,15 @@ int stencil_launch(int op, int lap_type, int dtype, int v_dtype,
                 p, to_dev<double>(sc, jf), nfunc, stream, force_direct);
         return launch_t<float, float, 0, OP_RHS, 1>(
             p, to_dev<float>(sc, jf), nfunc, stream, force_direct);
+    }
+    if (op == OP_RHS_SPLIT)
+    {
+        // float blocks through the vector kernel only
+        if (dtype != MGX_F32 || !vec_ok<float, float, 0, OP_RHS_SPLIT, 1>(p, force_direct)
+            || (L.npts() % 64) != 0)
+            return fail(MGX_UNSUPPORTED, "split right-hand side needs the vector kernel");
+        return launch_vec<float, float, 0, OP_RHS_SPLIT, 1>(p, to_dev<float>(sc, jf), nfunc,
+            stream);
     }
     if (op == OP_RHS_SUB)
     {

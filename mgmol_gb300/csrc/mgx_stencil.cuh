@@ -19,10 +19,14 @@ enum StencilOp
     OP_JACOBI = 3, // w = -Lap u - f ; out = mask(u - jf w) ; w_out = mask(w)
     OP_RHS    = 4, // out = B u
     OP_RHS_SUB = 5, // out = B u - g (g pointwise, passed as f)
-    OP_JACOBI_UPD = 6 // OP_JACOBI whose result r is added into upd: upd += upd_alpha r
+    OP_JACOBI_UPD = 6, // OP_JACOBI whose result r is added into upd: upd += upd_alpha r
+    OP_RHS_SPLIT  = 7  // out = B u stored as bf16 hi / lo planes of a tensor-core operand
 };
 
-__host__ __device__ constexpr bool is_rhs_op(int op) { return op == OP_RHS || op == OP_RHS_SUB; }
+__host__ __device__ constexpr bool is_rhs_op(int op)
+{
+    return op == OP_RHS || op == OP_RHS_SUB || op == OP_RHS_SPLIT;
+}
 __host__ __device__ constexpr bool is_jacobi(int op) { return op == OP_JACOBI || op == OP_JACOBI_UPD; }
 
 /* Localization masks of one level in box form: for function f, values of
@@ -69,6 +73,12 @@ struct PlaneParams
     // OP_JACOBI_UPD only, or NULL: upd = upd_scale[f] * (upd + upd_alpha r),
     // the column normalization of the updated block folded into the store
     const double* upd_scale = nullptr;
+    // OP_RHS_SPLIT only: the result r of point k of function f is stored as
+    // bf16 hi = rn(r), lo = rn(r - hi) at ((k / 64) * split_rows + f) * 64 +
+    // k % 64 of split_hi / split_lo (the K-blocked operand planes)
+    void* split_hi = nullptr;
+    void* split_lo = nullptr;
+    int split_rows = 0;
 };
 
 int stencil_launch(int op, int lap_type, int dtype, int v_dtype,
@@ -79,6 +89,12 @@ int stencil_launch(int op, int lap_type, int dtype, int v_dtype,
  * functions of grid level 0; u and out with leading dimensions ldu, ldo. */
 int rhs_block(const mgx_grid& g, int dtype, const void* u, size_t ldu, void* out,
     size_t ldo, int nfunc, cudaStream_t s);
+/* B u of nfunc FP32 functions written straight into bf16 hi / lo K-blocked
+ * planes of `rows` rows (the tensor-core operand layout).  MGX_UNSUPPORTED
+ * when the vector kernel cannot run the block (alignment, plane size) or
+ * the points are not a multiple of 64; nothing is launched then. */
+int rhs_split_block(const mgx_grid& g, const float* u, size_t ldu, int nfunc, void* hi,
+    void* lo, int rows, cudaStream_t s);
 
 int ghosted_del2(const mgx_grid& g, int ghosts, int lap_type, int dtype,
     const void* v, void* b, size_t nfunc, cudaStream_t s);

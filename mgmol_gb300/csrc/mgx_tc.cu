@@ -1150,6 +1150,46 @@ int matb_product(mgx_ctx* ctx, int mode, const Operand& a, size_t a_used, const 
     size_t ld, size_t K, int n, double* C, int tile_slot, cudaStream_t s,
     const tc::ScaleSlot* sb, void* work, int work_funcs)
 {
+    // BF16X3 on K-blocked planes: the stencil writes the hi / lo planes of
+    // B Psi itself (no FP32 B Psi block, no split pass), CHUNK rows a time
+    if (mode == MGX_GEMM_BF16X3 && blocked_planes() && (K % 64) == 0 && (ld % 4) == 0
+        && ((uintptr_t)psi % 16) == 0)
+    {
+        const size_t kblocks = K / 64;
+        // the B-side workspace holds min(n, CHUNK) rows (operand_bytes)
+        const size_t plane = kblocks * 64 * (size_t)std::min(n, CHUNK) * sizeof(__nv_bfloat16);
+        char* base           = (char*)ctx->tc_split.ptr + a_used;
+        bool fused           = true;
+        for (int j0 = 0; j0 < n && fused; j0 += CHUNK)
+        {
+            const int nc  = std::min(CHUNK, n - j0);
+            const int BN  = tile_n(nc);
+            void* hi      = base;
+            void* lo      = base + plane;
+            const int st  = rhs_split_block(ctx->grid, (const float*)psi + (size_t)j0 * ld, ld, nc,
+                hi, lo, nc, s);
+            if (st == MGX_UNSUPPORTED && j0 == 0)
+            {
+                fused = false; // nothing launched: take the unfused path below
+                break;
+            }
+            MGX_TRY(st);
+            Operand b;
+            b.sw      = bf16_swizzle();
+            b.blocked = true;
+            b.half    = false;
+            b.bf16    = true;
+            b.base0   = hi;
+            b.base1   = lo;
+            b.K       = K;
+            b.ld      = kblocks * 64;
+            b.rows    = nc;
+            MGX_TRY(tc::make_map_blocked(&b.m0, hi, nc, kblocks, BN, b.sw));
+            MGX_TRY(tc::make_map_blocked(&b.m1, lo, nc, kblocks, BN, b.sw));
+            MGX_TRY(run(ctx, mode, a, b, n, nc, 1, C + (size_t)j0 * n, n, K, tile_slot, BN, s, j0));
+        }
+        if (fused) return MGX_OK;
+    }
     const int step = std::min(std::max(work_funcs, 1), CHUNK);
     for (int j0 = 0; j0 < n; j0 += step)
     {

@@ -35,8 +35,11 @@ def _setup(grid, nf, seed):
 
 
 @pytest.mark.parametrize("mode", sorted(TOL))
-@pytest.mark.parametrize("grid,nf", [((16, 16, 16), 24), ((32, 24, 20), 150)])
+@pytest.mark.parametrize("grid,nf", [((16, 16, 16), 24), ((32, 24, 20), 150), ((10, 12, 14), 20)])
 def test_matb_matches_oracle(mode, grid, nf):
+    """(10, 12, 14): points not a multiple of 64 and rows not of whole
+    vectors, so B Psi is formed in FP32 and split afterwards; the others
+    write the BF16 planes from the stencil directly."""
     ll, psi, ctx = _setup(grid, nf, 61)
     dt = np.float64 if mode == capi.GEMM_FP64 else np.float32
     p = psi.astype(dt)
