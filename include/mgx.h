@@ -345,6 +345,16 @@ int mgx_inverse_from_cholesky(mgx_ctx* ctx, int n, const double* L,
 int mgx_trace_prod(mgx_ctx* ctx, int n, const double* H, const double* Sinv,
     double* trace, void* stream);
 
+/* Lets the Psi Theta products of this context (mgx_mult_matrix,
+ * mgx_residual, mgx_residual_cols, mgx_rho) in the BF16X3 mode read the
+ * BF16 conversion of psi that the last mgx_gram / mgx_hmat /
+ * mgx_gram_hmat / mgx_matb / mgx_gram_hmat_matb call on this context made
+ * of the same block (same pointer, leading dimension and size), instead of
+ * converting psi again.  With it on, the caller guarantees that psi has
+ * not changed in between.  Off by default.  No counterpart in the
+ * reference. */
+int mgx_set_reuse_conversion(mgx_ctx* ctx, int on);
+
 /* ---------------------------------------------------------------- */
 /* Residual and orbital update (rows of the ABPG step).              */
 /* ---------------------------------------------------------------- */

@@ -114,6 +114,7 @@ _SIGS = {
     "mgx_normalize_scales": [_vp, _i, _vp, _vp, _vp],
     "mgx_cholesky": [_vp, _i, _vp, _ip, _vp],
     "mgx_cholesky_async": [_vp, _i, _vp, _vp, _vp],
+    "mgx_set_reuse_conversion": [_vp, _i],
     "mgx_inverse_from_cholesky": [_vp, _i, _vp, _vp, _vp],
     "mgx_trace_prod": [_vp, _i, _vp, _vp, _vp, _vp],
     "mgx_theta": [_vp, _i, _vp, _vp, _vp, _vp],
@@ -225,6 +226,11 @@ class Context:
         h = ctypes.c_void_p()
         _check(load().mgx_create(ctypes.byref(self.grid), ctypes.byref(h)))
         self.handle = h
+
+    def set_reuse_conversion(self, on):
+        """mgx_set_reuse_conversion: Psi Theta products may read the last
+        Gram-type product's BF16 conversion of the same (unchanged) block."""
+        _check(load().mgx_set_reuse_conversion(self.handle, 1 if on else 0))
 
     def close(self):
         if getattr(self, "handle", None):

@@ -740,6 +740,13 @@ int mgx_cholesky(mgx_ctx* ctx, int n, double* A, int* info, void* stream)
     return cholesky(ctx, n, A, info, (cudaStream_t)stream);
 }
 
+int mgx_set_reuse_conversion(mgx_ctx* ctx, int on)
+{
+    if (!ctx) return fail(MGX_BAD_ARG, "ctx is NULL");
+    ctx->reuse_conversion = on ? 1 : 0;
+    return MGX_OK;
+}
+
 int mgx_cholesky_async(mgx_ctx* ctx, int n, double* A, int* info, void* stream)
 {
     if (!ctx) return fail(MGX_BAD_ARG, "ctx is NULL");

@@ -99,6 +99,21 @@ struct mgx_ctx
     mgx::DeviceBuffer flag;
     // tensor-core GEMM: bf16 hi/lo planes, tile list, status word
     mgx::DeviceBuffer tc_split, tc_tiles, tc_err;
+    // the BF16 K-blocked hi / lo planes that the last Gram-type product left
+    // at the start of tc_split (its A operand: rows = functions, K =
+    // points), described so that a Psi Theta product on the same block can
+    // read them instead of converting the block again (only when the
+    // caller has allowed it with mgx_set_reuse_conversion)
+    struct Conversion
+    {
+        const void* psi = nullptr;
+        size_t ld = 0, K = 0, used = 0;
+        int n      = 0;
+        bool valid = false;
+        void* hi   = nullptr;
+        void* lo   = nullptr;
+    } conv;
+    int reuse_conversion = 0;
     // residual: Psi Theta when the caller passes no work block
     mgx::DeviceBuffer resid;
     // Poisson multigrid levels

@@ -60,6 +60,21 @@ __device__ __forceinline__ uint64_t desc_sw(uint32_t saddr)
     return d;
 }
 
+// Shared-memory descriptor of an MN-major tile (bf16) under SWIZZLE_128B:
+// rows of 128 bytes hold 64 consecutive MN elements (one K index each),
+// 8-row groups (K) are 1024 bytes apart (stride byte offset) and the next
+// 64 MN elements start lbo bytes further (leading byte offset).
+__device__ __forceinline__ uint64_t desc_mn128(uint32_t saddr, uint32_t lbo)
+{
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);
+    d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+    d |= (uint64_t)(1024 >> 4) << 32;
+    d |= (uint64_t)1 << 46;
+    d |= (uint64_t)2 << 61;
+    return d;
+}
+
 // kind::tf32 (KIND 0, operand format 2), kind::f16 with bf16 operands
 // (KIND 1, format 1) or with fp16 operands (KIND 2, format 0); FP32 D, both
 // operands K-major
@@ -200,7 +215,11 @@ struct Params
 // STORE true: one CTA per output tile over the whole K range, FP32 store.
 // SW: bytes of K per tile row and stage (128: SWIZZLE_128B; 64: SWIZZLE_64B,
 // half the K per stage and twice the stages in the same shared memory).
-template <int KIND, int NPROD, int BN, int STAGES, bool STORE = false, int SW = 128>
+// AMN: the A operand is MN-major (bf16, rows of 64 points per K index, the
+// K-blocked planes of the Gram product read with the roles of points and
+// functions exchanged): A tiles are 2 blocks of 64 MN elements x BK K rows.
+template <int KIND, int NPROD, int BN, int STAGES, bool STORE = false, int SW = 128,
+    bool AMN = false>
 __global__ void __launch_bounds__(THREADS, 1) gram_kernel(
     const __grid_constant__ CUtensorMap mA0, const __grid_constant__ CUtensorMap mA1,
     const __grid_constant__ CUtensorMap mB0, const __grid_constant__ CUtensorMap mB1,
@@ -274,7 +293,17 @@ __global__ void __launch_bounds__(THREADS, 1) gram_kernel(
             unsigned char* st = smem + s * STAGE;
             mbar_arrive_expect_tx(full + s, STAGE);
             const int kc = (kb0 + it) * BK;
-            if (p.blocked)
+            if (AMN)
+            {
+                // A: points i0 .. i0 + 127 (two 64-point blocks) x K rows kc ..
+                tma_load_3d(st, &mA0, 0, kc, i0 / 64, full + s);
+                if (NPROD == 3) tma_load_3d(st + A_BYTES, &mA1, 0, kc, i0 / 64, full + s);
+                const int e0 = kc % 64, kb = kc / 64;
+                tma_load_3d(st + NOP * A_BYTES, &mB0, e0, j0, kb, full + s);
+                if (NPROD == 3)
+                    tma_load_3d(st + NOP * A_BYTES + B_BYTES, &mB1, e0, j0, kb, full + s);
+            }
+            else if (p.blocked)
             {
                 const int e0 = kc % 64, kb = kc / 64;
                 tma_load_3d(st, &mA0, e0, i0, kb, full + s);
@@ -299,7 +328,8 @@ __global__ void __launch_bounds__(THREADS, 1) gram_kernel(
     }
     else if (warp == 1 && lane == 0)
     {
-        constexpr uint32_t idesc = instr_desc<KIND>(BM, BN);
+        // bit 15: A is MN-major
+        constexpr uint32_t idesc = instr_desc<KIND>(BM, BN) | (AMN ? (1u << 15) : 0u);
         int it = 0;
         for (; it < nkb && ok; it++)
         {
@@ -313,13 +343,17 @@ __global__ void __launch_bounds__(THREADS, 1) gram_kernel(
 #pragma unroll
             for (int kk = 0; kk < NK; kk++)
             {
-                const uint64_t ad = desc_sw<SW>(a0 + kk * KSTEP);
+                // MN-major A: 16 K rows of 128 bytes per MMA, the two 64-point
+                // blocks BK rows apart
+                const uint64_t ad = AMN ? desc_mn128(a0 + kk * 16 * 128, BK * 128)
+                                        : desc_sw<SW>(a0 + kk * KSTEP);
                 const uint64_t bd = desc_sw<SW>(b0 + kk * KSTEP);
                 mma<KIND>(tmem, ad, bd, idesc, (it > 0 || kk > 0) ? 1u : 0u);
                 if (NPROD == 3)
                 {
                     const uint64_t bl = desc_sw<SW>(b0 + B_BYTES + kk * KSTEP);
-                    const uint64_t al = desc_sw<SW>(a0 + A_BYTES + kk * KSTEP);
+                    const uint64_t al = AMN ? desc_mn128(a0 + A_BYTES + kk * 16 * 128, BK * 128)
+                                            : desc_sw<SW>(a0 + A_BYTES + kk * KSTEP);
                     mma<KIND>(tmem, ad, bl, idesc, 1u);
                     mma<KIND>(tmem, al, bd, idesc, 1u);
                 }
@@ -769,14 +803,34 @@ static int make_map_blocked(CUtensorMap* m, const void* base, size_t rows, size_
     return MGX_OK;
 }
 
-template <int KIND, int NPROD, int BN, int STAGES, bool STORE = false, int SW = 128>
+/* Map of K-blocked bf16 planes (element (r, k) at ((k / 64) * rows + r) *
+ * 64 + k % 64) read MN-major: boxes of 64 K elements (the MN side of the
+ * consumer, 128 bytes, SWIZZLE_128B) x box_r rows (the consumer's K) x 2
+ * consecutive 64-element blocks. */
+static int make_map_mn(CUtensorMap* m, const void* base, size_t rows, size_t kblocks, int box_r)
+{
+    auto enc = encoder();
+    if (!enc) return fail(MGX_CUDA_ERROR, "cuTensorMapEncodeTiled unavailable");
+    cuuint64_t dims[3]    = { 64, (cuuint64_t)rows, (cuuint64_t)kblocks };
+    cuuint64_t strides[2] = { 128, (cuuint64_t)(rows * 128) };
+    cuuint32_t box[3]     = { 64, (cuuint32_t)box_r, 2 };
+    cuuint32_t estr[3]    = { 1, 1, 1 };
+    CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<void*>(base), dims,
+        strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+        CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return fail(MGX_CUDA_ERROR, "MN-major tensor map (%d)", (int)r);
+    return MGX_OK;
+}
+
+template <int KIND, int NPROD, int BN, int STAGES, bool STORE = false, int SW = 128,
+    bool AMN = false>
 static int launch(const CUtensorMap& a0, const CUtensorMap& a1, const CUtensorMap& b0,
     const CUtensorMap& b1, const Params& p, int ntiles, int ksplit, cudaStream_t s)
 {
     constexpr int NOP   = (NPROD == 3) ? 2 : 1;
     constexpr int STAGE = NOP * (BM * SW + BN * SW);
     const size_t smem   = (size_t)STAGES * STAGE + (2 * STAGES + 1) * 8 + 16 + 1024;
-    auto kern           = gram_kernel<KIND, NPROD, BN, STAGES, STORE, SW>;
+    auto kern           = gram_kernel<KIND, NPROD, BN, STAGES, STORE, SW, AMN>;
     MGX_TRY(cuda_check(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)smem),
         "gram_kernel smem attribute"));
@@ -1124,6 +1178,22 @@ int finish(double* C, int n, double vel, int symmetric, cudaStream_t s,
 // columns of the second operand converted per pass (bounds the workspace)
 constexpr int CHUNK = 512;
 
+/* records the A operand just prepared at the start of tc_split (BF16 K-blocked
+ * planes only) as the context's reusable conversion of psi */
+void record_conversion(mgx_ctx* ctx, int mode, const Operand& a, const void* psi, size_t ld,
+    size_t K, int n, size_t used)
+{
+    auto& c = ctx->conv;
+    c.valid = (mode == MGX_GEMM_BF16X3) && a.blocked && !a.half;
+    c.psi   = psi;
+    c.ld    = ld;
+    c.K     = K;
+    c.n     = n;
+    c.used  = used;
+    c.hi    = const_cast<void*>(a.base0);
+    c.lo    = const_cast<void*>(a.base1);
+}
+
 /* C = A B^T over K with B processed CHUNK rows at a time; A prepared once */
 int product(mgx_ctx* ctx, int mode, const Operand& a, size_t a_used, const void* B,
     size_t ld, size_t K, int n, double* C, int tile_slot, cudaStream_t s,
@@ -1226,7 +1296,9 @@ int matb_tcgen05(mgx_ctx* ctx, int mode, const void* psi, size_t ld, size_t K, i
     }
     Operand a;
     size_t used = 0;
+    ctx->conv.valid = false;
     MGX_TRY(prepare(mode, psi, ld, K, n, tc::BM, (char*)ctx->tc_split.ptr, &used, a, s, sa));
+    record_conversion(ctx, mode, a, psi, ld, K, n, used);
     MGX_TRY(matb_product(ctx, mode, a, ((used + 255) / 256) * 256, psi, ld, K, n, Bm, 0, s, sa,
         work, work_funcs));
     MGX_TRY(finish(Bm, n, vel, 1, s, sa, sa));
@@ -1257,7 +1329,9 @@ int gram_tcgen05(mgx_ctx* ctx, int mode, const void* A, const void* B, size_t ld
     }
     Operand a;
     size_t used = 0;
+    ctx->conv.valid = false;
     MGX_TRY(prepare(mode, A, ld, K, n, tc::BM, (char*)ctx->tc_split.ptr, &used, a, s, sa));
+    record_conversion(ctx, mode, a, A, ld, K, n, used);
     if (same)
         MGX_TRY(run_sym(ctx, mode, a, n, C, K, 0, s));
     else
@@ -1290,7 +1364,9 @@ int gram_hmat_tcgen05(mgx_ctx* ctx, int mode, const void* psi, const void* hpsi,
     }
     Operand a;
     size_t used = 0;
+    ctx->conv.valid = false;
     MGX_TRY(prepare(mode, psi, ld, K, n, tc::BM, (char*)ctx->tc_split.ptr, &used, a, s, sa));
+    record_conversion(ctx, mode, a, psi, ld, K, n, used);
     MGX_TRY(run_sym(ctx, mode, a, n, S, K, 0, s));
     MGX_TRY(product(ctx, mode, a, ((used + 255) / 256) * 256, hpsi, ld, K, n, H, 1, s, sb));
     MGX_TRY(finish(S, n, vel, 1, s, sa, sa));
@@ -1317,6 +1393,78 @@ int psi_theta_tcgen05(mgx_ctx* ctx, int mode, const float* psi, size_t ld, size_
     cudaStream_t s, double* rho)
 {
     using namespace tc;
+    // Psi Theta straight from the Gram's conversion of the same block: its
+    // K-blocked planes (rows = functions, K = points) are the MN-major A
+    // operand here (M = points, K = functions), so psi is not converted again
+    {
+        const auto& cv = ctx->conv;
+        const int sw   = bf16_swizzle();
+        const size_t ldk0     = ((n + 63) / 64) * 64;
+        const size_t bplane   = ((ldk0 * (size_t)ncols * 2 + 1023) / 1024) * 1024;
+        const size_t off      = ((cv.used + 1023) / 1024) * 1024;
+        if (mode == MGX_GEMM_BF16X3 && ctx->reuse_conversion && cv.valid && cv.psi == psi
+            && cv.ld == ld && cv.K == npts && cv.n == n && off + 2 * bplane <= ctx->tc_split.bytes)
+        {
+            MGX_TRY(begin(ctx, s));
+            char* ws       = (char*)ctx->tc_split.ptr + off;
+            void* bhi      = ws;
+            void* blo      = ws + bplane;
+            const int nkbf = (int)(ldk0 / 64);
+            const int nb   = (int)std::min<size_t>((ncols * ldk0 + 255) / 256, 1 << 16);
+            matrix_split_blocked_kernel<__nv_bfloat16><<<nb, 256, 0, s>>>(theta, n, ldt, ncols,
+                nkbf, (__nv_bfloat16*)bhi, (__nv_bfloat16*)blo, nullptr);
+            MGX_LAUNCH_CHECK("matrix_split_kernel");
+            const int BN = (ncols > 128) ? 256 : 128;
+            const int BK = sw / 2;
+            CUtensorMap mb0, mb1, ma0, ma1;
+            MGX_TRY(make_map_blocked(&mb0, bhi, ncols, nkbf, BN, sw));
+            MGX_TRY(make_map_blocked(&mb1, blo, ncols, nkbf, BN, sw));
+            const size_t kbp = (npts + 63) / 64;
+            MGX_TRY(make_map_mn(&ma0, cv.hi, (size_t)n, kbp, BK));
+            MGX_TRY(make_map_mn(&ma1, cv.lo, (size_t)n, kbp, BK));
+            const int ntj = (ncols + BN - 1) / BN;
+            Params p;
+            p.tiles      = nullptr;
+            p.kblocks    = (n + BK - 1) / BK;
+            p.kb_per_cta = p.kblocks;
+            p.n          = 0;
+            p.ncols      = ncols;
+            p.symmetric  = 0;
+            p.C          = nullptr;
+            p.err        = (int*)ctx->tc_err.ptr;
+            p.out        = out;
+            p.cin        = cin;
+            p.ldo        = ld;
+            p.beta       = cin ? beta : 0.f;
+            p.nrows      = (int)npts;
+            p.ntj        = ntj;
+            p.blocked    = 1;
+            if (rho)
+            {
+                p.rho  = rho;
+                p.rpsi = psi;
+                p.ldr  = ld;
+            }
+            const int ntiles = (int)((npts + BM - 1) / BM) * ntj;
+            if (sw == 64)
+            {
+                if (BN == 256)
+                    MGX_TRY((launch<1, 3, 256, 4, true, 64, true>(ma0, ma1, mb0, mb1, p, ntiles, 1, s)));
+                else
+                    MGX_TRY((launch<1, 3, 128, 6, true, 64, true>(ma0, ma1, mb0, mb1, p, ntiles, 1, s)));
+            }
+            else
+            {
+                if (BN == 256)
+                    MGX_TRY((launch<1, 3, 256, 2, true, 128, true>(ma0, ma1, mb0, mb1, p, ntiles, 1, s)));
+                else
+                    MGX_TRY((launch<1, 3, 128, 3, true, 128, true>(ma0, ma1, mb0, mb1, p, ntiles, 1, s)));
+            }
+            return end(ctx, s);
+        }
+    }
+    // the conversion below overwrites the start of the workspace
+    ctx->conv.valid = false;
     const bool half       = (mode == MGX_GEMM_FP16X3);
     const bool bf         = split_mode(mode);
     const size_t esz      = bf ? 2 : 4;

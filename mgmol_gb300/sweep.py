@@ -127,6 +127,9 @@ class OrbitalSweep:
         self.sctx = capi.Context(ctx.n, ctx.ll) if self.use_matb else None
         self.info = torch.zeros(2, dtype=torch.int32, device=device)
         self.Sinv = None
+        # psi does not change between the Gram products and Psi Theta: the
+        # residual reads the Gram's BF16 conversion of psi
+        ctx.set_reuse_conversion(True)
         self.alpha = 0.5 * precond_factor
         self.theta = None
         if gamma is None:

@@ -144,6 +144,39 @@ def test_residual_fp32(mode):
     assert err < (3e-7 if mode == capi.GEMM_FP64 else TOL[mode])
 
 
+@pytest.mark.parametrize("grid,nf", [((16, 16, 16), 40), ((32, 24, 20), 300), ((10, 12, 14), 70)])
+def test_psi_theta_reuses_gram_conversion(grid, nf):
+    """With mgx_set_reuse_conversion on, Psi Theta reads the Gram product's
+    BF16 planes of the same block as an MN-major operand; the result is that
+    of the converting path.  Another block is not taken for the converted
+    one."""
+    ll = tuple(x * 0.35 for x in grid)
+    psi, _, _ = synth.gaussian_orbitals(grid, ll, nf, 29)
+    p32 = psi.astype(np.float32)
+    ctx = capi.Context(grid, ll)
+    d = _dev(p32, np.float32)
+    th = _theta(nf, 30)
+    thd = _dev(th)
+    ref = ctx.mult_matrix(d, thd, capi.GEMM_BF16X3).cpu().numpy()
+    ctx.set_reuse_conversion(True)
+    ctx.gram(d, capi.GEMM_BF16X3)
+    got = ctx.mult_matrix(d, thd, capi.GEMM_BF16X3).cpu().numpy()
+    assert rel_err(got, ref) < 1e-6
+    assert rel_err(got, O.mult_matrix(p32, th)) < TOL[capi.GEMM_BF16X3]
+    # column chunks of the residual read the same planes
+    hp = _dev(O.hpsi(grid, ll, 0, p32, synth.gaussian_wells(grid, ll, 3, 29)), np.float32)
+    full = ctx.residual(d, hp, thd, capi.GEMM_BF16X3).cpu().numpy()
+    thc = torch.from_numpy(np.ascontiguousarray(th.T)).cuda()
+    part = ctx.residual_cols(d, hp[: nf // 2], thc[: nf // 2].contiguous(), capi.GEMM_BF16X3)
+    assert rel_err(part.cpu().numpy(), full[: nf // 2]) < 1e-6
+    ref_res = O.residual(grid, ll, p32, hp.cpu().numpy(), th)
+    assert rel_err(full, ref_res) < TOL[capi.GEMM_BF16X3]
+    # a different block goes through its own conversion
+    d2 = 2 * d
+    got2 = ctx.mult_matrix(d2, thd, capi.GEMM_BF16X3).cpu().numpy()
+    assert rel_err(got2, 2 * ref) < 1e-6
+
+
 def test_residual_rejects_aliases():
     grid, nf = (8, 8, 8), 3
     ctx = capi.Context(grid, (2.8, 2.8, 2.8))
