@@ -6,9 +6,10 @@ scale folded in.
 Error bars (relative to max |reference|) are those of the products:
 FP64 mode 1e-12; FP32 CUDA cores 2e-5; tensor-core modes as in the Gram
 tests (TF32 2e-3, BF16X3 2e-5, FP16X3 5e-6).  The normalization of FP64
-blocks agrees to 1e-14 (the device sums the squares in another order,
-which moves diagS and its inverse square root by ~1e-14); FP32 blocks to
-one FP32 ulp.
+blocks agrees to 1e-12 (the device sums the squares in another order, a
+tree instead of the reference's sequential loop, which moves diagS and its
+inverse square root by up to ~P ulps for P points); FP32 blocks to one FP32
+ulp.
 """
 import numpy as np
 import pytest
@@ -113,18 +114,20 @@ def test_normalize_matches_oracle(dt):
     d = _dev(p, dt)
     diag = ctx.normalize(d).cpu().numpy()
     ref, rdiag = O.normalize(grid, ll, p)
-    assert rel_err(diag, rdiag) < 1e-14
+    # a sequential and a tree sum of P squares differ by up to ~P ulps in the
+    # worst case (the reference's own sum carries that error)
+    assert rel_err(diag, rdiag) < 1e-12
     got = d.cpu().numpy()
     if dt == np.float64:
         # alpha = diagS^-1/2 carries the relative error of the reordered sum
-        assert rel_err(got, ref) < 1e-14
+        assert rel_err(got, ref) < 1e-12
     else:
         # FP32: the same rounding of alpha * x, alpha equal to ~1e-16
         ulp = np.spacing(np.abs(ref).astype(np.float32))
         assert np.all(np.abs(got - ref) <= ulp)
     # normalized: vel |psi_i|^2 = 1
     again = ctx.normalize(d).cpu().numpy()
-    assert np.max(np.abs(again - 1.0)) < (1e-14 if dt == np.float64 else 1e-6)
+    assert np.max(np.abs(again - 1.0)) < (1e-12 if dt == np.float64 else 1e-6)
 
 
 def test_normalize_rejects_zero_function():
@@ -145,7 +148,7 @@ def test_normalize_scales_from_gram():
     S = ctx.gram(p)
     d = ctx.normalize_scales(S).cpu().numpy()
     _, diag = O.normalize(grid, ll, 2.5 * psi)
-    assert rel_err(d, 1.0 / np.sqrt(diag)) < 1e-14
+    assert rel_err(d, 1.0 / np.sqrt(diag)) < 1e-12
 
 
 @pytest.mark.parametrize("dt,tol", [(np.float64, 1e-13), (np.float32, 2e-6)])
