@@ -250,6 +250,10 @@ def run_gpu(args, cfg):
         dist.barrier()
     torch.cuda.synchronize()
     l0 = capi.launches()
+    # CUDA events around every tensor-core product launch, on its stream
+    capi.timing_read(capi.TIMING_TC_SPLITK)
+    capi.timing_read(capi.TIMING_TC_STORE)
+    capi.timing_enable(True)
     start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     start.record()
     for _ in range(args.steps):
@@ -259,6 +263,9 @@ def run_gpu(args, cfg):
     if world > 1:
         dist.barrier()
     launches = capi.launches() - l0
+    capi.timing_enable(False)
+    tk_ms, tk_n = capi.timing_read(capi.TIMING_TC_SPLITK)
+    ts_ms, ts_n = capi.timing_read(capi.TIMING_TC_STORE)
     ms = start.elapsed_time(stop) / args.steps
     clocks.stop()
     phases = sw.phase_ms()
@@ -305,9 +312,36 @@ def run_gpu(args, cfg):
     gram_flops = (2 if sw.use_matb else 1) * N * (N + 1) * npts + 2.0 * N * N * npts
     shares = {k: v / sum(phases.values()) for k, v in phases.items()}
     dominant = max(phases, key=phases.get)
-    if dominant == "gram":
+    # the tensor-core kernels themselves (event-timed launches inside the
+    # timed sweeps): split-BF16x3 issues 3 bf16 MMAs per algorithmic
+    # multiply-add, so "issued" is 3x the algorithmic rate in that mode
+    nprod = 3 if (mode == "mixed" and args.gemm in ("bf16x3", "fp16x3")) else 1
+    psi_theta_flops = 2.0 * N * N * npts
+    kernels = {}
+    if tk_n:
+        k_ms = tk_ms / args.steps
+        kernels["gram_kernel split-K (S, H, B)"] = {
+            "launches_per_sweep": tk_n / args.steps, "ms_per_sweep": k_ms,
+            "algorithmic_tflops": gram_flops / (k_ms * 1e-3) / 1e12,
+            "issued_tflops": nprod * gram_flops / (k_ms * 1e-3) / 1e12}
+    if ts_n:
+        k_ms = ts_ms / args.steps
+        kernels["gram_kernel store (Psi Theta)"] = {
+            "launches_per_sweep": ts_n / args.steps, "ms_per_sweep": k_ms,
+            "algorithmic_tflops": psi_theta_flops / (k_ms * 1e-3) / 1e12,
+            "issued_tflops": nprod * psi_theta_flops / (k_ms * 1e-3) / 1e12}
+    if dominant == "gram" and tk_n:
+        k_ms = tk_ms / tk_n                       # one launch on average
+        per_launch = gram_flops / (tk_n / args.steps)
+        achieved = per_launch / (k_ms * 1e-3) / 1e12
+        roof = {"kernel": "gram_kernel (tcgen05 split-K: S, H, B)", "bound": "tensor",
+                "achieved": achieved, "peak": bf16, "unit": "TFLOP/s", "frac": achieved / bf16,
+                "traffic": None, "issued_frac": nprod * achieved / bf16,
+                "algorithmic": f"{gram_flops:.3e} flop per sweep (S{' and B' if sw.use_matb else ''} "
+                               f"lower incl. diagonal + H) over {tk_n / args.steps:.0f} launches"}
+    elif dominant == "gram":
         achieved = gram_flops / (phases["gram"] * 1e-3) / 1e12
-        roof = {"kernel": "gram+hmat", "bound": "tensor", "achieved": achieved, "peak": bf16,
+        roof = {"kernel": "gram+hmat phase", "bound": "tensor", "achieved": achieved, "peak": bf16,
                 "unit": "TFLOP/s", "frac": achieved / bf16, "traffic": None,
                 "algorithmic": f"{gram_flops:.3e} flop per sweep (S{' and B' if sw.use_matb else ''} "
                                f"lower incl. diagonal + H)"}
@@ -342,7 +376,8 @@ def run_gpu(args, cfg):
                    "schedule": f"column chunks of {sw.chunk}" if sw.chunk else "full blocks",
                    "l2": "inputs larger than L2 (no flush)", "parallelism": f"replicas x{world}"},
         "phases_ms": phases, "phase_share": shares, "energy_trace_ry": energy,
-        "roofline": roof, "gpu_launches": launches, "clocks": clocks.summary(),
+        "roofline": roof, "tensor_kernels": kernels, "gpu_launches": launches,
+        "clocks": clocks.summary(),
     }
     if e2e:
         line["e2e"] = e2e

@@ -94,6 +94,17 @@ typedef struct mgx_masks mgx_masks;
 int mgx_create(const mgx_grid* grid, mgx_ctx** ctx);
 int mgx_destroy(mgx_ctx* ctx);
 const char* mgx_last_error_string(void);
+/* Kernel timing for benchmarks: with timing on, every tensor-core product
+ * launch is bracketed by CUDA events on its stream; mgx_timing_read returns
+ * the summed device time (ms) and the number of launches of one class since
+ * the last read of that class (waiting for the events), and forgets them.
+ * Classes: split-K products (S, H, B), store-epilogue products (Psi Theta,
+ * the density). */
+#define MGX_TIMING_TC_SPLITK 1
+#define MGX_TIMING_TC_STORE 2
+int mgx_timing_enable(int on);
+int mgx_timing_read(int cls, double* total_ms, int* launches);
+
 /* Number of kernels this library launched since process start (all
  * contexts); a counter for benchmarks and tests. */
 unsigned long long mgx_kernel_launch_count(void);

@@ -115,6 +115,8 @@ _SIGS = {
     "mgx_cholesky": [_vp, _i, _vp, _ip, _vp],
     "mgx_cholesky_async": [_vp, _i, _vp, _vp, _vp],
     "mgx_set_reuse_conversion": [_vp, _i],
+    "mgx_timing_enable": [_i],
+    "mgx_timing_read": [_i, _dp, _ip],
     "mgx_inverse_from_cholesky": [_vp, _i, _vp, _vp, _vp],
     "mgx_trace_prod": [_vp, _i, _vp, _vp, _vp, _vp],
     "mgx_theta": [_vp, _i, _vp, _vp, _vp, _vp],
@@ -165,6 +167,22 @@ def _check(status):
 
 def launches():
     return int(load().mgx_kernel_launch_count())
+
+
+TIMING_TC_SPLITK, TIMING_TC_STORE = 1, 2
+
+
+def timing_enable(on):
+    """Brackets every tensor-core product launch with CUDA events."""
+    _check(load().mgx_timing_enable(1 if on else 0))
+
+
+def timing_read(cls):
+    """(total device ms, launches) of one timing class since its last read."""
+    ms = ctypes.c_double()
+    n = ctypes.c_int()
+    _check(load().mgx_timing_read(int(cls), ctypes.byref(ms), ctypes.byref(n)))
+    return ms.value, n.value
 
 
 def _stream(stream=None):

@@ -28,7 +28,9 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstdlib>
+#include <mutex>
 #include <vector>
 
 #include "mgx_internal.cuh"
@@ -822,11 +824,42 @@ static int make_map_mn(CUtensorMap* m, const void* base, size_t rows, size_t kbl
     return MGX_OK;
 }
 
+} // namespace tc
+
+/* ---------------- kernel timing (CUDA events around launches) -------- */
+struct TimedLaunch
+{
+    int cls;
+    cudaEvent_t a, b;
+};
+static std::mutex g_timing_mu;
+static std::vector<TimedLaunch> g_timed;
+static std::atomic<int> g_timing_on{ 0 };
+
+/* records an event pair around the launch issued by fn() when timing is on */
+template <typename F>
+static int timed_launch(int cls, cudaStream_t s, F fn)
+{
+    if (!g_timing_on.load()) return fn();
+    TimedLaunch t{ cls, nullptr, nullptr };
+    if (cudaEventCreate(&t.a) != cudaSuccess || cudaEventCreate(&t.b) != cudaSuccess)
+        return fn();
+    cudaEventRecord(t.a, s);
+    const int st = fn();
+    cudaEventRecord(t.b, s);
+    std::lock_guard<std::mutex> lk(g_timing_mu);
+    g_timed.push_back(t);
+    return st;
+}
+
+namespace tc
+{
 template <int KIND, int NPROD, int BN, int STAGES, bool STORE = false, int SW = 128,
     bool AMN = false>
 static int launch(const CUtensorMap& a0, const CUtensorMap& a1, const CUtensorMap& b0,
     const CUtensorMap& b1, const Params& p, int ntiles, int ksplit, cudaStream_t s)
 {
+    return timed_launch(STORE ? MGX_TIMING_TC_STORE : MGX_TIMING_TC_SPLITK, s, [&]() -> int {
     constexpr int NOP   = (NPROD == 3) ? 2 : 1;
     constexpr int STAGE = NOP * (BM * SW + BN * SW);
     const size_t smem   = (size_t)STAGES * STAGE + (2 * STAGES + 1) * 8 + 16 + 1024;
@@ -838,6 +871,7 @@ static int launch(const CUtensorMap& a0, const CUtensorMap& a1, const CUtensorMa
     kern<<<grid, THREADS, smem, s>>>(a0, a1, b0, b1, p);
     MGX_LAUNCH_CHECK("tc gram_kernel");
     return MGX_OK;
+    });
 }
 
 __global__ void finish_kernel(double* C, int n, double vel, int symmetric,
@@ -1178,6 +1212,16 @@ int finish(double* C, int n, double vel, int symmetric, cudaStream_t s,
 // columns of the second operand converted per pass (bounds the workspace)
 constexpr int CHUNK = 512;
 
+/* room kept after the operands for the BF16 planes of an n x n theta, so
+ * that a Psi Theta product can reuse the conversion of psi without growing
+ * (and so losing) the workspace */
+size_t theta_room(const mgx_ctx* ctx, int n)
+{
+    if (!ctx->reuse_conversion) return 0;
+    const size_t ldk = ((size_t)(n + 63) / 64) * 64;
+    return 2 * (((ldk * (size_t)n * 2) + 1023) / 1024) * 1024 + 2048;
+}
+
 /* records the A operand just prepared at the start of tc_split (BF16 K-blocked
  * planes only) as the context's reusable conversion of psi */
 void record_conversion(mgx_ctx* ctx, int mode, const Operand& a, const void* psi, size_t ld,
@@ -1285,7 +1329,7 @@ int matb_tcgen05(mgx_ctx* ctx, int mode, const void* psi, size_t ld, size_t K, i
 {
     const size_t a_bytes = operand_bytes(mode, K, n);
     const size_t b_bytes = operand_bytes(mode, K, std::min(n, CHUNK));
-    MGX_TRY(ctx->tc_split.ensure(a_bytes + b_bytes + 512));
+    MGX_TRY(ctx->tc_split.ensure(a_bytes + b_bytes + 512 + theta_room(ctx, n)));
     MGX_TRY(begin(ctx, s));
     MGX_TRY(cuda_check(cudaMemsetAsync(Bm, 0, (size_t)n * n * sizeof(double), s), "B zero"));
     tc::ScaleSlot* sa = nullptr;
@@ -1311,7 +1355,7 @@ int gram_tcgen05(mgx_ctx* ctx, int mode, const void* A, const void* B, size_t ld
     const bool same = (A == B) && symmetric;
     const size_t a_bytes = operand_bytes(mode, K, n);
     const size_t b_bytes = same ? 0 : operand_bytes(mode, K, std::min(n, CHUNK));
-    MGX_TRY(ctx->tc_split.ensure(a_bytes + b_bytes + 256));
+    MGX_TRY(ctx->tc_split.ensure(a_bytes + b_bytes + 256 + theta_room(ctx, n)));
     MGX_TRY(begin(ctx, s));
     MGX_TRY(cuda_check(cudaMemsetAsync(C, 0, (size_t)n * n * sizeof(double), s), "C zero"));
     tc::ScaleSlot* sa = nullptr;
@@ -1349,7 +1393,7 @@ int gram_hmat_tcgen05(mgx_ctx* ctx, int mode, const void* psi, const void* hpsi,
 {
     const size_t a_bytes = operand_bytes(mode, K, n);
     const size_t b_bytes = operand_bytes(mode, K, std::min(n, CHUNK));
-    MGX_TRY(ctx->tc_split.ensure(a_bytes + b_bytes + 512));
+    MGX_TRY(ctx->tc_split.ensure(a_bytes + b_bytes + 512 + theta_room(ctx, n)));
     MGX_TRY(begin(ctx, s));
     MGX_TRY(cuda_check(cudaMemsetAsync(S, 0, (size_t)n * n * sizeof(double), s), "S zero"));
     MGX_TRY(cuda_check(cudaMemsetAsync(H, 0, (size_t)n * n * sizeof(double), s), "H zero"));
@@ -1617,3 +1661,43 @@ int psi_theta_tcgen05(mgx_ctx* ctx, int mode, const float* psi, size_t ld, size_
     return end(ctx, s);
 }
 } // namespace mgx
+
+extern "C" {
+
+int mgx_timing_enable(int on)
+{
+    mgx::g_timing_on.store(on ? 1 : 0);
+    return MGX_OK;
+}
+
+int mgx_timing_read(int cls, double* total_ms, int* launches)
+{
+    using namespace mgx;
+    if (!total_ms || !launches) return fail(MGX_BAD_ARG, "NULL output");
+    std::lock_guard<std::mutex> lk(g_timing_mu);
+    double tot = 0.;
+    int n      = 0;
+    std::vector<TimedLaunch> keep;
+    for (auto& t : g_timed)
+    {
+        if (t.cls != cls)
+        {
+            keep.push_back(t);
+            continue;
+        }
+        float ms = 0.f;
+        if (cudaEventSynchronize(t.b) == cudaSuccess && cudaEventElapsedTime(&ms, t.a, t.b) == cudaSuccess)
+        {
+            tot += ms;
+            n++;
+        }
+        cudaEventDestroy(t.a);
+        cudaEventDestroy(t.b);
+    }
+    g_timed.swap(keep);
+    *total_ms = tot;
+    *launches = n;
+    return MGX_OK;
+}
+
+} // extern "C"

@@ -39,7 +39,8 @@ def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("op", choices=["gram", "hmat", "gram_hmat", "matb", "gram_hmat_matb", "mult",
                                    "residual", "hpsi", "precond", "mgm", "dense", "dense_b",
-                                   "dense_parts", "normalize", "h2d", "h2d_kernel", "all"])
+                                   "dense_parts", "normalize", "mult_reuse", "h2d", "h2d_kernel",
+                                   "all"])
     ap.add_argument("--streams", type=int, default=1, help="h2d: concurrent copy streams")
     ap.add_argument("--grid", type=int, nargs=3, default=[96, 96, 32])
     ap.add_argument("--h", type=float, default=0.25)
@@ -111,6 +112,17 @@ def main(argv=None):
         elif op == "normalize":
             ms = _time(lambda: ctx.normalize(psi), args.warmup, args.reps)
             work, unit = 3 * N * npts * s, "GB/s"
+        elif op == "mult_reuse":
+            # Psi Theta reading the Gram product's conversion of psi (MN-major A)
+            th = (torch.eye(N, dtype=torch.float64, device="cuda")
+                  + torch.randn(N, N, dtype=torch.float64, device="cuda") / N)
+            dst = torch.empty_like(psi)
+            ctx.set_reuse_conversion(True)
+            ctx.gram(psi, mode)
+            ms = _time(lambda: ctx.mult_matrix(psi, th, mode, out=dst), args.warmup, args.reps)
+            ctx.set_reuse_conversion(False)
+            del dst
+            work, unit = 2.0 * N * N * npts, "TFLOP/s"
         elif op in ("mult", "residual"):
             th = (torch.eye(N, dtype=torch.float64, device="cuda")
                   + torch.randn(N, N, dtype=torch.float64, device="cuda") / N)

@@ -157,10 +157,15 @@ def test_psi_theta_reuses_gram_conversion(grid, nf):
     d = _dev(p32, np.float32)
     th = _theta(nf, 30)
     thd = _dev(th)
+    l0 = capi.launches()
     ref = ctx.mult_matrix(d, thd, capi.GEMM_BF16X3).cpu().numpy()
+    n_convert = capi.launches() - l0
     ctx.set_reuse_conversion(True)
     ctx.gram(d, capi.GEMM_BF16X3)
+    l0 = capi.launches()
     got = ctx.mult_matrix(d, thd, capi.GEMM_BF16X3).cpu().numpy()
+    # the reusing product launches no conversion of psi
+    assert capi.launches() - l0 < n_convert
     assert rel_err(got, ref) < 1e-6
     assert rel_err(got, O.mult_matrix(p32, th)) < TOL[capi.GEMM_BF16X3]
     # column chunks of the residual read the same planes
