@@ -447,6 +447,307 @@ __global__ void __launch_bounds__(THREADS, 1) gram_kernel(
                      : "memory");
 }
 
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar)
+{
+    asm volatile("mbarrier.arrive.release.cta.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar))
+                 : "memory");
+}
+
+/* The persistent form of gram_kernel: one CTA per SM walks the work items
+ * w = blockIdx.x, blockIdx.x + gridDim.x, ... (split-K: tile w % ntiles of
+ * the list, K slice w / ntiles; store: output tile w), with two TMEM
+ * accumulators of BN columns.  The MMA warp fills accumulator t & 1 for the
+ * CTA's t-th item while the epilogue warps drain the other one, so the
+ * epilogue (FP64 atomics, FP32 stores or the density reduction) overlaps
+ * the next item's MMAs instead of idling the tensor pipe; the TMA ring runs
+ * on across items.  accf[b]: MMAs of accumulator b done (tcgen05.commit);
+ * acce[b]: the four epilogue warps have read it.  Every wait is bounded; a
+ * timeout records MGX_TIMEOUT and stops the other roles at their next
+ * item. */
+template <int KIND, int NPROD, int BN, int STAGES, bool STORE = false, int SW = 128,
+    bool AMN = false>
+__global__ void __launch_bounds__(THREADS, 1) gram_kernel_ps(
+    const __grid_constant__ CUtensorMap mA0, const __grid_constant__ CUtensorMap mA1,
+    const __grid_constant__ CUtensorMap mB0, const __grid_constant__ CUtensorMap mB1,
+    Params p, int nitems, int ntiles)
+{
+    constexpr int NOP     = (NPROD == 3) ? 2 : 1;
+    constexpr int A_BYTES = BM * SW;
+    constexpr int B_BYTES = BN * SW;
+    constexpr int STAGE   = NOP * (A_BYTES + B_BYTES);
+    constexpr int KSTEP   = 32;
+    constexpr int NK      = SW / KSTEP;
+    constexpr int ELEM    = (KIND == 0) ? 4 : 2;
+    constexpr int BK      = SW / ELEM;
+    constexpr uint32_t TMEM_COLS = 2 * BN; // two accumulators
+    static_assert(2 * BN <= 512, "two accumulators must fit in TMEM");
+
+    extern __shared__ unsigned char smem_raw[];
+    unsigned char* smem = reinterpret_cast<unsigned char*>(
+        (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    uint64_t* full  = reinterpret_cast<uint64_t*>(smem + STAGES * STAGE);
+    uint64_t* empty = full + STAGES;
+    uint64_t* accf  = empty + STAGES; // [2]
+    uint64_t* acce  = accf + 2;       // [2]
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(acce + 2);
+    __shared__ volatile int abort_all;
+
+    const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+
+    // the item's output tile and K-block range
+    auto decode = [&](int w, int& i0, int& j0, int& kb0, int& nkb) {
+        if (STORE)
+        {
+            i0  = (w / p.ntj) * BM;
+            j0  = (w % p.ntj) * BN;
+            kb0 = 0;
+            nkb = p.kblocks;
+        }
+        else
+        {
+            const int2 tile = p.tiles[w % ntiles];
+            i0              = tile.x * BM;
+            j0              = tile.y * BN;
+            kb0             = (w / ntiles) * p.kb_per_cta;
+            nkb             = min(p.kblocks, kb0 + p.kb_per_cta) - kb0;
+        }
+    };
+
+    if (threadIdx.x == 0)
+    {
+        for (int s = 0; s < STAGES; s++)
+        {
+            mbar_init(full + s, 1);
+            mbar_init(empty + s, 1);
+        }
+        for (int b = 0; b < 2; b++)
+        {
+            mbar_init(accf + b, 1);
+            mbar_init(acce + b, 4);
+        }
+        abort_all = 0;
+        fence_mbar_init();
+    }
+    if (warp == 1)
+    {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                         smem_u32(tslot)),
+            "r"(TMEM_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    fence_before_sync();
+    __syncthreads();
+    fence_after_sync();
+    const uint32_t tmem = *tslot;
+
+    if (warp == 0 && lane == 0)
+    {
+        prefetch_map(&mA0);
+        prefetch_map(&mB0);
+        if (NPROD == 3)
+        {
+            prefetch_map(&mA1);
+            prefetch_map(&mB1);
+        }
+        int g = 0; // stages issued so far, over all items
+        for (int w = blockIdx.x; w < nitems && !abort_all; w += gridDim.x)
+        {
+            int i0, j0, kb0, nkb;
+            decode(w, i0, j0, kb0, nkb);
+            for (int it = 0; it < nkb; it++, g++)
+            {
+                const int s       = g % STAGES;
+                const uint32_t ph = (uint32_t)((g / STAGES) & 1);
+                if (!mbar_wait(empty + s, ph ^ 1u))
+                {
+                    abort_all = 1;
+                    break;
+                }
+                unsigned char* st = smem + s * STAGE;
+                mbar_arrive_expect_tx(full + s, STAGE);
+                const int kc = (kb0 + it) * BK;
+                if (AMN)
+                {
+                    tma_load_3d(st, &mA0, 0, kc, i0 / 64, full + s);
+                    if (NPROD == 3) tma_load_3d(st + A_BYTES, &mA1, 0, kc, i0 / 64, full + s);
+                    const int e0 = kc % 64, kb = kc / 64;
+                    tma_load_3d(st + NOP * A_BYTES, &mB0, e0, j0, kb, full + s);
+                    if (NPROD == 3)
+                        tma_load_3d(st + NOP * A_BYTES + B_BYTES, &mB1, e0, j0, kb, full + s);
+                }
+                else if (p.blocked)
+                {
+                    const int e0 = kc % 64, kb = kc / 64;
+                    tma_load_3d(st, &mA0, e0, i0, kb, full + s);
+                    tma_load_3d(st + NOP * A_BYTES, &mB0, e0, j0, kb, full + s);
+                    if (NPROD == 3)
+                    {
+                        tma_load_3d(st + A_BYTES, &mA1, e0, i0, kb, full + s);
+                        tma_load_3d(st + NOP * A_BYTES + B_BYTES, &mB1, e0, j0, kb, full + s);
+                    }
+                }
+                else
+                {
+                    tma_load_2d(st, &mA0, kc, i0, full + s);
+                    tma_load_2d(st + NOP * A_BYTES, &mB0, kc, j0, full + s);
+                    if (NPROD == 3)
+                    {
+                        tma_load_2d(st + A_BYTES, &mA1, kc, i0, full + s);
+                        tma_load_2d(st + NOP * A_BYTES + B_BYTES, &mB1, kc, j0, full + s);
+                    }
+                }
+            }
+        }
+    }
+    else if (warp == 1 && lane == 0)
+    {
+        constexpr uint32_t idesc = instr_desc<KIND>(BM, BN) | (AMN ? (1u << 15) : 0u);
+        int g = 0, t = 0;
+        for (int w = blockIdx.x; w < nitems && !abort_all; w += gridDim.x, t++)
+        {
+            int i0, j0, kb0, nkb;
+            decode(w, i0, j0, kb0, nkb);
+            const int b       = t & 1;
+            const uint32_t tb = tmem + (uint32_t)(b * BN);
+            // the epilogue has drained this accumulator's previous item
+            if (!mbar_wait(acce + b, (uint32_t)(((t >> 1) & 1) ^ 1)))
+            {
+                abort_all = 1;
+                break;
+            }
+            fence_after_sync();
+            bool ok = true;
+            for (int it = 0; it < nkb; it++, g++)
+            {
+                const int s       = g % STAGES;
+                const uint32_t ph = (uint32_t)((g / STAGES) & 1);
+                if (!mbar_wait(full + s, ph))
+                {
+                    ok = false;
+                    break;
+                }
+                fence_after_sync();
+                const uint32_t a0 = smem_u32(smem + s * STAGE);
+                const uint32_t b0 = a0 + NOP * A_BYTES;
+#pragma unroll
+                for (int kk = 0; kk < NK; kk++)
+                {
+                    const uint64_t ad = AMN ? desc_mn128(a0 + kk * 16 * 128, BK * 128)
+                                            : desc_sw<SW>(a0 + kk * KSTEP);
+                    const uint64_t bd = desc_sw<SW>(b0 + kk * KSTEP);
+                    mma<KIND>(tb, ad, bd, idesc, (it > 0 || kk > 0) ? 1u : 0u);
+                    if (NPROD == 3)
+                    {
+                        const uint64_t bl = desc_sw<SW>(b0 + B_BYTES + kk * KSTEP);
+                        const uint64_t al = AMN ? desc_mn128(a0 + A_BYTES + kk * 16 * 128, BK * 128)
+                                                : desc_sw<SW>(a0 + A_BYTES + kk * KSTEP);
+                        mma<KIND>(tb, ad, bl, idesc, 1u);
+                        mma<KIND>(tb, al, bd, idesc, 1u);
+                    }
+                }
+                mma_commit(empty + s);
+            }
+            mma_commit(accf + b);
+            if (!ok)
+            {
+                abort_all = 1;
+                break;
+            }
+        }
+    }
+    else if (warp >= 2)
+    {
+        const int q   = warp & 3; // TMEM lane quarter this warp may access
+        const int row = q * 32 + lane;
+        int t         = 0;
+        for (int w = blockIdx.x; w < nitems; w += gridDim.x, t++)
+        {
+            int i0, j0, kb0, nkb;
+            decode(w, i0, j0, kb0, nkb);
+            const int b = t & 1;
+            const bool got = !abort_all && mbar_wait(accf + b, (uint32_t)((t >> 1) & 1));
+            if (!got)
+            {
+                abort_all = 1;
+                break;
+            }
+            fence_after_sync();
+            const int i   = i0 + row;
+            double racc   = 0.;
+            if (nkb > 0)
+            {
+#pragma unroll 1
+                for (int c0 = 0; c0 < BN; c0 += 32)
+                {
+                    float v[32];
+                    tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * BN + c0), v);
+                    if (STORE)
+                    {
+                        if (KIND == 2)
+                        {
+                            const float ds = (float)(p.sa->down * p.sb->down);
+#pragma unroll
+                            for (int u = 0; u < 32; u++)
+                                v[u] *= ds;
+                        }
+                        if (p.rho != nullptr)
+                        {
+                            if (i < p.nrows)
+                            {
+#pragma unroll
+                                for (int u = 0; u < 32; u++)
+                                {
+                                    const int j = j0 + c0 + u;
+                                    if (j < p.ncols)
+                                        racc += (double)(v[u] * p.rpsi[(size_t)j * p.ldr + i]);
+                                }
+                            }
+                        }
+                        else if (i < p.nrows)
+                        {
+#pragma unroll
+                            for (int u = 0; u < 32; u++)
+                            {
+                                const int j = j0 + c0 + u;
+                                if (j < p.ncols)
+                                {
+                                    const size_t o = (size_t)j * p.ldo + i;
+                                    p.out[o] = (p.beta != 0.f) ? v[u] + p.beta * p.cin[o] : v[u];
+                                }
+                            }
+                        }
+                    }
+                    else if (i < p.n)
+                    {
+#pragma unroll
+                        for (int u = 0; u < 32; u++)
+                        {
+                            const int j = j0 + c0 + u;
+                            if (j < p.ncols && (!p.symmetric || i >= j + p.col0))
+                                atomicAdd(p.C + (size_t)j * p.n + i, (double)v[u]);
+                        }
+                    }
+                }
+            }
+            if (STORE && p.rho != nullptr && nkb > 0 && i < p.nrows) atomicAdd(p.rho + i, racc);
+            // every tcgen05.ld of this warp has completed (wait::ld): hand
+            // the accumulator back to the MMA warp
+            fence_before_sync();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(acce + b);
+        }
+    }
+    if (abort_all && threadIdx.x == 0 && p.err) atomicExch(p.err, MGX_TIMEOUT);
+    fence_before_sync();
+    __syncthreads();
+    fence_after_sync();
+    if (warp == 1)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+            "r"(TMEM_COLS)
+                     : "memory");
+}
+
 // fp32 -> bf16 hi + lo planes (x = hi + lo + O(2^-17 |x|)); rows of K
 // values with leading dimension ld (source) and ldo (planes)
 __global__ void split_kernel(const float* __restrict__ x, size_t ld, int rows,
@@ -854,14 +1155,31 @@ static int timed_launch(int cls, cudaStream_t s, F fn)
 
 namespace tc
 {
+/* sms > 0: the persistent kernel on min(items, sms) CTAs (items = ntiles x
+ * ksplit); else one CTA per item */
 template <int KIND, int NPROD, int BN, int STAGES, bool STORE = false, int SW = 128,
     bool AMN = false>
 static int launch(const CUtensorMap& a0, const CUtensorMap& a1, const CUtensorMap& b0,
-    const CUtensorMap& b1, const Params& p, int ntiles, int ksplit, cudaStream_t s)
+    const CUtensorMap& b1, const Params& p, int ntiles, int ksplit, cudaStream_t s,
+    int sms = 0)
 {
     return timed_launch(STORE ? MGX_TIMING_TC_STORE : MGX_TIMING_TC_SPLITK, s, [&]() -> int {
     constexpr int NOP   = (NPROD == 3) ? 2 : 1;
     constexpr int STAGE = NOP * (BM * SW + BN * SW);
+    if (sms > 0)
+    {
+        const size_t smem = (size_t)STAGES * STAGE + (2 * STAGES + 4) * 8 + 16 + 1024;
+        auto kern         = gram_kernel_ps<KIND, NPROD, BN, STAGES, STORE, SW, AMN>;
+        MGX_TRY(cuda_check(cudaFuncSetAttribute(kern,
+                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+            "gram_kernel_ps smem attribute"));
+        const long items = (long)ntiles * ksplit;
+        if (items > (1L << 30)) return fail(MGX_UNSUPPORTED, "too many work items");
+        const int grid = (int)std::min<long>(items, sms);
+        kern<<<grid, THREADS, smem, s>>>(a0, a1, b0, b1, p, (int)items, ntiles);
+        MGX_LAUNCH_CHECK("tc gram_kernel_ps");
+        return MGX_OK;
+    }
     const size_t smem   = (size_t)STAGES * STAGE + (2 * STAGES + 1) * 8 + 16 + 1024;
     auto kern           = gram_kernel<KIND, NPROD, BN, STAGES, STORE, SW, AMN>;
     MGX_TRY(cuda_check(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -932,6 +1250,19 @@ int compute_scale(const void* X, size_t ld, int rows, size_t K, tc::ScaleSlot* s
  * at 128 x 256 tiles; the default, 8 % faster than 128 on the Gram and the
  * Psi Theta product at 2048 orbitals on 192^3) or 128 (SWIZZLE_128B, 2
  * stages); MGX_TC_SWIZZLE (64 or 128) overrides the default for tuning. */
+/* the persistent double-buffered tensor-core kernel (default);
+ * MGX_TC_PERSIST=0 selects one CTA per output tile */
+bool persist_on()
+{
+    static int v = -1;
+    if (v < 0)
+    {
+        const char* e = getenv("MGX_TC_PERSIST");
+        v             = (e && atoi(e) == 0) ? 0 : 1;
+    }
+    return v == 1;
+}
+
 int bf16_swizzle()
 {
     static int sw = 0;
@@ -1096,6 +1427,7 @@ int run(mgx_ctx* ctx, int mode, const Operand& a, const Operand& b, int nrows, i
     int col0 = 0)
 {
     using namespace tc;
+    const int sms = persist_on() ? ctx->sm_count : 0;
     const int nti = (nrows + BM - 1) / BM, ntj = (ncols + BN - 1) / BN;
     std::vector<int2> tiles;
     for (int j = 0; j < ntj; j++)
@@ -1137,22 +1469,22 @@ int run(mgx_ctx* ctx, int mode, const Operand& a, const Operand& b, int nrows, i
     if (mode == MGX_GEMM_FP16X3)
     {
         if (BN == 256)
-            return launch<2, 3, 256, 4, false, 64>(a.m0, a.m1, b.m0, b.m1, p, ntiles, ksplit, s);
-        return launch<2, 3, 128, 6, false, 64>(a.m0, a.m1, b.m0, b.m1, p, ntiles, ksplit, s);
+            return launch<2, 3, 256, 4, false, 64>(a.m0, a.m1, b.m0, b.m1, p, ntiles, ksplit, s, sms);
+        return launch<2, 3, 128, 6, false, 64>(a.m0, a.m1, b.m0, b.m1, p, ntiles, ksplit, s, sms);
     }
     if (BN == 256)
     {
         if (mode == MGX_GEMM_TF32)
-            return launch<0, 1, 256, 4>(a.m0, a.m0, b.m0, b.m0, p, ntiles, ksplit, s);
+            return launch<0, 1, 256, 4>(a.m0, a.m0, b.m0, b.m0, p, ntiles, ksplit, s, sms);
         if (a.sw == 64)
-            return launch<1, 3, 256, 4, false, 64>(a.m0, a.m1, b.m0, b.m1, p, ntiles, ksplit, s);
-        return launch<1, 3, 256, 2>(a.m0, a.m1, b.m0, b.m1, p, ntiles, ksplit, s);
+            return launch<1, 3, 256, 4, false, 64>(a.m0, a.m1, b.m0, b.m1, p, ntiles, ksplit, s, sms);
+        return launch<1, 3, 256, 2>(a.m0, a.m1, b.m0, b.m1, p, ntiles, ksplit, s, sms);
     }
     if (mode == MGX_GEMM_TF32)
-        return launch<0, 1, 128, 6>(a.m0, a.m0, b.m0, b.m0, p, ntiles, ksplit, s);
+        return launch<0, 1, 128, 6>(a.m0, a.m0, b.m0, b.m0, p, ntiles, ksplit, s, sms);
     if (a.sw == 64)
-        return launch<1, 3, 128, 6, false, 64>(a.m0, a.m1, b.m0, b.m1, p, ntiles, ksplit, s);
-    return launch<1, 3, 128, 3>(a.m0, a.m1, b.m0, b.m1, p, ntiles, ksplit, s);
+        return launch<1, 3, 128, 6, false, 64>(a.m0, a.m1, b.m0, b.m1, p, ntiles, ksplit, s, sms);
+    return launch<1, 3, 128, 3>(a.m0, a.m1, b.m0, b.m1, p, ntiles, ksplit, s, sms);
 }
 
 /* output tile width: 256 when the product is wide enough; MGX_TC_TILE_N
@@ -1437,6 +1769,7 @@ int psi_theta_tcgen05(mgx_ctx* ctx, int mode, const float* psi, size_t ld, size_
     cudaStream_t s, double* rho)
 {
     using namespace tc;
+    const int sms = persist_on() ? ctx->sm_count : 0;
     // Psi Theta straight from the Gram's conversion of the same block: its
     // K-blocked planes (rows = functions, K = points) are the MN-major A
     // operand here (M = points, K = functions), so psi is not converted again
@@ -1493,16 +1826,16 @@ int psi_theta_tcgen05(mgx_ctx* ctx, int mode, const float* psi, size_t ld, size_
             if (sw == 64)
             {
                 if (BN == 256)
-                    MGX_TRY((launch<1, 3, 256, 4, true, 64, true>(ma0, ma1, mb0, mb1, p, ntiles, 1, s)));
+                    MGX_TRY((launch<1, 3, 256, 4, true, 64, true>(ma0, ma1, mb0, mb1, p, ntiles, 1, s, sms)));
                 else
-                    MGX_TRY((launch<1, 3, 128, 6, true, 64, true>(ma0, ma1, mb0, mb1, p, ntiles, 1, s)));
+                    MGX_TRY((launch<1, 3, 128, 6, true, 64, true>(ma0, ma1, mb0, mb1, p, ntiles, 1, s, sms)));
             }
             else
             {
                 if (BN == 256)
-                    MGX_TRY((launch<1, 3, 256, 2, true, 128, true>(ma0, ma1, mb0, mb1, p, ntiles, 1, s)));
+                    MGX_TRY((launch<1, 3, 256, 2, true, 128, true>(ma0, ma1, mb0, mb1, p, ntiles, 1, s, sms)));
                 else
-                    MGX_TRY((launch<1, 3, 128, 3, true, 128, true>(ma0, ma1, mb0, mb1, p, ntiles, 1, s)));
+                    MGX_TRY((launch<1, 3, 128, 3, true, 128, true>(ma0, ma1, mb0, mb1, p, ntiles, 1, s, sms)));
             }
             return end(ctx, s);
         }
@@ -1635,27 +1968,27 @@ int psi_theta_tcgen05(mgx_ctx* ctx, int mode, const float* psi, size_t ld, size_
         if (half)
         {
             if (BN == 256)
-                MGX_TRY((launch<2, 3, 256, 4, true, 64>(ma0, ma1, mb0, mb1, p, ntiles, 1, s)));
+                MGX_TRY((launch<2, 3, 256, 4, true, 64>(ma0, ma1, mb0, mb1, p, ntiles, 1, s, sms)));
             else
-                MGX_TRY((launch<2, 3, 128, 6, true, 64>(ma0, ma1, mb0, mb1, p, ntiles, 1, s)));
+                MGX_TRY((launch<2, 3, 128, 6, true, 64>(ma0, ma1, mb0, mb1, p, ntiles, 1, s, sms)));
         }
         else if (BN == 256)
         {
             if (bf && sw == 64)
-                MGX_TRY((launch<1, 3, 256, 4, true, 64>(ma0, ma1, mb0, mb1, p, ntiles, 1, s)));
+                MGX_TRY((launch<1, 3, 256, 4, true, 64>(ma0, ma1, mb0, mb1, p, ntiles, 1, s, sms)));
             else if (bf)
-                MGX_TRY((launch<1, 3, 256, 2, true>(ma0, ma1, mb0, mb1, p, ntiles, 1, s)));
+                MGX_TRY((launch<1, 3, 256, 2, true>(ma0, ma1, mb0, mb1, p, ntiles, 1, s, sms)));
             else
-                MGX_TRY((launch<0, 1, 256, 4, true>(ma0, ma0, mb0, mb0, p, ntiles, 1, s)));
+                MGX_TRY((launch<0, 1, 256, 4, true>(ma0, ma0, mb0, mb0, p, ntiles, 1, s, sms)));
         }
         else
         {
             if (bf && sw == 64)
-                MGX_TRY((launch<1, 3, 128, 6, true, 64>(ma0, ma1, mb0, mb1, p, ntiles, 1, s)));
+                MGX_TRY((launch<1, 3, 128, 6, true, 64>(ma0, ma1, mb0, mb1, p, ntiles, 1, s, sms)));
             else if (bf)
-                MGX_TRY((launch<1, 3, 128, 3, true>(ma0, ma1, mb0, mb1, p, ntiles, 1, s)));
+                MGX_TRY((launch<1, 3, 128, 3, true>(ma0, ma1, mb0, mb1, p, ntiles, 1, s, sms)));
             else
-                MGX_TRY((launch<0, 1, 128, 6, true>(ma0, ma0, mb0, mb0, p, ntiles, 1, s)));
+                MGX_TRY((launch<0, 1, 128, 6, true>(ma0, ma0, mb0, mb0, p, ntiles, 1, s, sms)));
         }
     }
     return end(ctx, s);
