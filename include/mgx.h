@@ -261,6 +261,14 @@ int mgx_masks_create(mgx_ctx* ctx, int nlevels, int nfunc,
     const double* centers, const double* radii, int func, int kind,
     int mesh_ghosts, mgx_dtype dtype, mgx_masks** masks, void* stream);
 int mgx_masks_destroy(mgx_masks* masks);
+/* MasksSet::update (src/MasksSet.cc:208-218): rebuilds the masks of all
+ * levels for new centres (nfunc x 3) and radii (nfunc), HOST arrays, with
+ * the set's levels, functions, profile and kind; the handle stays valid.
+ * The correction masks of LocGridOrbitals::applyCorrMask
+ * (src/LocGridOrbitals.cc:454-480) are a second set of profile 1 (`one`)
+ * applied with mgx_masks_apply. */
+int mgx_masks_update(mgx_ctx* ctx, mgx_masks* masks, const double* centers,
+    const double* radii, void* stream);
 /* Applies level `level` masks to nfunc ghost-free functions in place
  * (GridFuncVector::app_mask, src/pb/GridFuncVector.cc:2427-2438). */
 int mgx_masks_apply(mgx_ctx* ctx, const mgx_masks* masks, int level,

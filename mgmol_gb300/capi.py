@@ -102,6 +102,7 @@ _SIGS = {
     "mgx_precond_gamma": [ctypes.POINTER(Grid), _i, _i, _d, _d, _dp],
     "mgx_masks_create": [_vp, _i, _i, _dp, _dp, _i, _i, _i, _i, ctypes.POINTER(_vp), _vp],
     "mgx_masks_destroy": [_vp],
+    "mgx_masks_update": [_vp, _vp, _dp, _dp, _vp],
     "mgx_masks_apply": [_vp, _vp, _i, _vp, _sz, _i, _vp],
     "mgx_masks_expand": [_vp, _i, _vp, _ip, _vp],
     "mgx_gram": [_vp, _i, _vp, _sz, _i, _vp, _vp],
@@ -622,6 +623,17 @@ class Masks:
                                        F64 if dtype == torch.float64 else F32, ctypes.byref(h),
                                        _stream(stream)))
         self.handle = h
+
+    def update(self, centers, radii, stream=None):
+        """MasksSet::update: the masks rebuilt for moved centres / new radii."""
+        import numpy as np
+        c = np.ascontiguousarray(np.asarray(centers, dtype=np.float64).reshape(-1))
+        r = np.ascontiguousarray(np.asarray(radii, dtype=np.float64).reshape(-1))
+        if r.shape[0] != self.nfunc or c.shape[0] != 3 * self.nfunc:
+            raise ValueError("update needs nfunc centres and radii")
+        _check(load().mgx_masks_update(self.ctx.handle, self.handle, c.ctypes.data_as(_dp),
+                                       r.ctypes.data_as(_dp), _stream(stream)))
+        return self
 
     def apply(self, u, level, stream=None):
         p, ld, nf = _block(u, self.ctx.level_points(level))

@@ -21,6 +21,8 @@
 //                             src/ProjectedMatricesMehrstellen.cc:38-64,
 //                             src/ProjectedMatricesMehrstellen.h:49-62
 //   Rho<T>::computeRho (non-orthogonal orbitals) src/Rho.cc:124-450
+//   MasksSet::setup / update, applyMask / applyCorrMask
+//                             src/MasksSet.cc:136-218, src/LocGridOrbitals.cc:427-480
 // Where the reference aborts (unsupported operator, failed Cholesky), these
 // classes throw mgx::Error carrying the C-ABI status.  Header only; link
 // against libmgx.so and the CUDA runtime.
@@ -554,6 +556,42 @@ public:
         check(mgx_update_hb(ctx_, n_, S.data(), theta.data(), HB.data(), nullptr),
             "ProjectedMatricesMehrstellen::updateHB");
     }
+};
+
+/* MasksSet: the localization masks of nfunc orbitals at every multigrid
+ * level (GridMaskMax, profile gaussianDecay, or GridMaskMult with profile
+ * one for the correction masks), device-resident */
+class MasksSet
+{
+    mgx_ctx* ctx_;
+    mgx_masks* m_ = nullptr;
+
+public:
+    /* MasksSet::setup from centres (nfunc x 3) and radii (host arrays) */
+    MasksSet(mgx_ctx* ctx, int nlevels, int nfunc, const double* centers, const double* radii,
+        int func, int kind, int mesh_ghosts, mgx_dtype type)
+        : ctx_(ctx)
+    {
+        check(mgx_masks_create(ctx, nlevels, nfunc, centers, radii, func, kind, mesh_ghosts, type,
+                  &m_, nullptr),
+            "MasksSet::setup");
+    }
+    ~MasksSet() { mgx_masks_destroy(m_); }
+    MasksSet(const MasksSet&) = delete;
+    /* MasksSet::update (src/MasksSet.cc:208-218): new centres and radii */
+    void update(const double* centers, const double* radii)
+    {
+        check(mgx_masks_update(ctx_, m_, centers, radii, nullptr), "MasksSet::update");
+    }
+    /* LocGridOrbitals::applyMask / applyCorrMask on a block of the level */
+    template <typename T>
+    void apply(OrbitalBlock<T>& block, int level = 0) const
+    {
+        check(mgx_masks_apply(ctx_, m_, level, block.psi(0), block.numpt(), block.chromatic_number(),
+                  nullptr),
+            "MasksSet::apply");
+    }
+    const mgx_masks* get() const { return m_; }
 };
 
 /* Rho<T>: the electronic density of a block of non-orthogonal orbitals

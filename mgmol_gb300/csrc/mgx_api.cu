@@ -76,6 +76,7 @@ int prolong_launch(int, int, const Level&, const void*, size_t, void*, size_t,
 int masks_create(mgx_ctx*, int, int, const double*, const double*, int, int,
     int, int, mgx_masks**, cudaStream_t);
 int masks_apply(mgx_ctx*, const mgx_masks*, int, void*, size_t, int, cudaStream_t);
+int masks_update(mgx_ctx*, mgx_masks*, const double*, const double*, cudaStream_t);
 int masks_expand(const mgx_masks*, int, void*, int*, cudaStream_t);
 int gram_cuda_cores(mgx_ctx*, int, const void*, const void*, size_t, size_t,
     int, double, int, double*, cudaStream_t);
@@ -533,6 +534,13 @@ int mgx_masks_create(mgx_ctx* ctx, int nlevels, int nfunc, const double* centers
     if (mesh_ghosts < 1) return fail(MGX_BAD_ARG, "mesh ghost width < 1");
     return masks_create(ctx, nlevels, nfunc, centers, radii, func, kind, mesh_ghosts,
         dtype, masks, (cudaStream_t)stream);
+}
+
+int mgx_masks_update(mgx_ctx* ctx, mgx_masks* masks, const double* centers,
+    const double* radii, void* stream)
+{
+    if (!ctx) return fail(MGX_BAD_ARG, "ctx is NULL");
+    return masks_update(ctx, masks, centers, radii, (cudaStream_t)stream);
 }
 
 int mgx_masks_destroy(mgx_masks* masks)

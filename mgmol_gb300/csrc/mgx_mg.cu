@@ -20,6 +20,7 @@
 #include <cmath>
 #include <cstring>
 #include <mutex>
+#include <memory>
 #include <vector>
 
 #include "mgx_internal.cuh"
@@ -415,11 +416,13 @@ int masks_create(mgx_ctx* ctx, int nlevels, int nfunc, const double* centers,
     if (func != 0 && func != 1) return fail(MGX_BAD_ARG, "mask func %d", func);
     if (kind != 0 && kind != 1) return fail(MGX_BAD_ARG, "mask kind %d", kind);
     const mgx_grid& g = ctx->grid;
-    mgx_masks* M      = new mgx_masks;
-    M->nlevels = nlevels;
-    M->nfunc   = nfunc;
-    M->kind    = kind;
-    M->dtype   = dtype;
+    std::unique_ptr<mgx_masks> M(new mgx_masks);
+    M->nlevels     = nlevels;
+    M->nfunc       = nfunc;
+    M->kind        = kind;
+    M->dtype       = dtype;
+    M->func        = func;
+    M->mesh_ghosts = mesh_ghosts;
     for (int i = 0; i < 3; i++)
         M->n[i] = g.n[i];
     M->state.resize(nlevels);
@@ -474,11 +477,7 @@ int masks_create(mgx_ctx* ctx, int nlevels, int nfunc, const double* centers,
             const double* c  = centers + 3 * f;
             const double rc  = radii[f];
             const double ovr = rc + delta;
-            if (!(rc > 0.001))
-            {
-                delete M;
-                return fail(MGX_BAD_ARG, "mask radius %g too small", rc);
-            }
+            if (!(rc > 0.001)) return fail(MGX_BAD_ARG, "mask radius %g too small", rc);
             if (!sphere_overlap(c, ovr, g.ll, nl, hs))
             {
                 st[f] = -1;
@@ -607,7 +606,22 @@ int masks_create(mgx_ctx* ctx, int nlevels, int nfunc, const double* centers,
             D.n[i] = nl[i];
         D.kind = kind;
     }
-    *out = M;
+    *out = M.release();
+    return MGX_OK;
+}
+
+/* MasksSet::update (src/MasksSet.cc:208-218): the set rebuilt for moved
+ * centres or new radii, with its levels, functions, profile and kind; the
+ * handle keeps its address, so calls holding it see the new masks */
+int masks_update(mgx_ctx* ctx, mgx_masks* M, const double* centers, const double* radii,
+    cudaStream_t s)
+{
+    if (!M || !centers || !radii) return fail(MGX_BAD_ARG, "masks_update: bad arguments");
+    mgx_masks* T = nullptr;
+    MGX_TRY(masks_create(ctx, M->nlevels, M->nfunc, centers, radii, M->func, M->kind,
+        M->mesh_ghosts, M->dtype, &T, s));
+    std::swap(*M, *T);
+    delete T;
     return MGX_OK;
 }
 

@@ -108,7 +108,7 @@ int ghosted_trade(const mgx_grid& g, int ghosts, int dtype, void* u,
 /* the opaque mask set of the C ABI: per level, device arrays in box form */
 struct mgx_masks
 {
-    int nlevels = 0, nfunc = 0, kind = 0, dtype = 0;
+    int nlevels = 0, nfunc = 0, kind = 0, dtype = 0, func = 0, mesh_ghosts = 1;
     int n[3]    = { 0, 0, 0 };
     std::vector<mgx::DeviceBuffer> state, box, offset, values;
     std::vector<std::vector<int>> h_state, h_box;

@@ -189,3 +189,39 @@ def test_precond_leading_dimension_above_points():
     ref = ctx.precond_mg(_dev(res), 0, 2, 0.3)
     assert torch.equal(out_wide[:, :npts], ref)
     assert torch.all(out_wide[:, npts:] == 7.0)
+
+
+def test_masks_update_after_centres_move():
+    """MasksSet::update: the set rebuilt for moved centres and new radii is
+    bit-identical to a fresh one (and to the oracle), through the same
+    handle; a correction-mask set (profile one, GridMaskMult) applied to a
+    block as LocGridOrbitals::applyCorrMask does matches the oracle."""
+    n = (48, 40, 32)
+    ll = tuple(x * 0.3 for x in n)
+    _, centers, _ = synth.gaussian_orbitals(n, ll, 10, 91)
+    radii = synth.mask_radii(10, 91, 2.0, 6.0)
+    ctx = capi.Context(n, ll)
+    M = capi.Masks(ctx, 3, centers, radii, func=0, kind=0, mesh_ghosts=2)
+    rng = np.random.default_rng(92)
+    moved = (centers + rng.uniform(-1.0, 1.0, centers.shape)) % np.asarray(ll)
+    radii2 = radii * 1.1
+    M.update(moved, radii2)
+    fresh = capi.Masks(ctx, 3, moved, radii2, func=0, kind=0, mesh_ghosts=2)
+    st_ref, vals_ref = O.mask_build(n, ll, 2, 3, moved, radii2, func=0)
+    for l in range(3):
+        st, dense = M.expand(l)
+        st2, dense2 = fresh.expand(l)
+        assert np.array_equal(st, st2) and np.array_equal(st, st_ref[l])
+        assert np.array_equal(dense.cpu().numpy(), dense2.cpu().numpy())
+        d = dense.cpu().numpy()
+        for f in range(10):
+            if st_ref[l][f] == 2:
+                assert np.array_equal(d[f], vals_ref[l][f]), (l, f)
+    # correction masks: profile one, multiplied in
+    C = capi.Masks(ctx, 1, moved, radii2 * 1.5, func=1, kind=1, mesh_ghosts=2)
+    res, _, _ = synth.gaussian_orbitals(n, ll, 10, 93)
+    u = _dev(res)
+    C.apply(u, 0)
+    st1, vals1 = O.mask_build(n, ll, 2, 1, moved, radii2 * 1.5, func=1)
+    ref = O.mask_apply(n, 0, st1, vals1, res, kind=1)
+    assert np.array_equal(u.cpu().numpy(), ref)
