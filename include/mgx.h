@@ -208,6 +208,14 @@ int mgx_precond_mg(mgx_ctx* ctx, const mgx_precond_params* p, mgx_dtype dtype,
     const void* res, size_t ld, void* out, int nfunc, const mgx_masks* masks,
     void* stream);
 
+/* mgx_precond_mg started from the iterate that out holds on entry instead
+ * of gamma * res (gamma is not used): the warm-started V-cycle of the
+ * learned preconditioner.  With out = gamma * res on entry the result is
+ * mgx_precond_mg's. */
+int mgx_precond_mg_warm(mgx_ctx* ctx, const mgx_precond_params* p, mgx_dtype dtype,
+    const void* res, size_t ld, void* out, int nfunc, const mgx_masks* masks,
+    void* stream);
+
 /* One preconditioned ABPG update, ABPG<T>::update_states without
  * acceleration (src/ABPG.cc:72-140): psi += alpha * V-cycle(res), with
  * alpha = 0.5 * precond_factor.  The V-cycle is mgx_precond_mg's; its last
@@ -531,6 +539,78 @@ typedef struct mgx_mgm_result
  * Synchronous (the residual norms are read on the host every cycle). */
 int mgx_mgm(mgx_ctx* ctx, const mgx_mgm_params* params, mgx_dtype dtype,
     void* vh, const void* rho, mgx_mgm_result* result, void* stream);
+
+/* ---------------- learned preconditioner ----------------
+ * A 3-level 3-D convolutional U-Net that maps a residual field to an
+ * approximation of the V-cycle correction (mgx_precond_mg); it has no
+ * counterpart in the reference and is used through
+ * mgx_precond_learned, which keeps the V-cycle as the per-function
+ * fallback.  Level l is the context grid coarsened l times (each
+ * dimension divisible by 4), periodic.  Bias-free layers, so that
+ * net(a x) = a net(x) for a > 0; inputs are scaled by their RMS and the
+ * output scaled back.  Layers (3x3x3 convolutions, channels in -> out,
+ * level): E0 1->16 @0, E1 16->32 @1, E2 32->64 @2, D2 64->32 @2,
+ * D1 32->16 @1, D0 16->1 @0; downsampling by the full-weighting
+ * restriction and upsampling by the trilinear prolongation of
+ * mgx_mg_restrict / mgx_mg_prolong; skip sums with ReLU at levels 1 and 0:
+ *   a0 = relu(E0 x)        a1 = relu(E1 R a0)     a2 = relu(E2 R a1)
+ *   s1 = relu(P D2 a2 + a1) s0 = relu(P D1 s1 + a0) y = D0 s0.
+ * Weights: FP32 master copy, BF16 in the convolutions, FP32
+ * accumulation and activations.  Parameter vector: the six weight
+ * tensors in layer order, each [out][in][3][3][3] (x, y, z offsets -1..1,
+ * z fastest). */
+#define MGX_UNET_PARAMS 139104
+
+typedef struct mgx_unet mgx_unet;
+
+typedef struct mgx_adam_params
+{
+    float lr;
+    float beta1;
+    float beta2;
+    float eps;
+} mgx_adam_params;
+
+int mgx_unet_create(mgx_ctx* ctx, mgx_unet** net);
+int mgx_unet_destroy(mgx_unet* net);
+/* copies MGX_UNET_PARAMS FP32 values (device) into / out of the master
+ * weights; set resets the optimizer state */
+int mgx_unet_set_params(mgx_unet* net, const float* params, void* stream);
+int mgx_unet_get_params(mgx_unet* net, float* params, void* stream);
+/* y_j = net(x_j) for nfunc FP32 fields of the context grid (leading
+ * dimension ld); x and y may not alias */
+int mgx_unet_forward(mgx_unet* net, const float* x, size_t ld, float* y, int nfunc,
+    void* stream);
+/* loss = mean over functions and points of (net(x_j / s_j) - t_j / s_j)^2,
+ * s_j = RMS(x_j); grad (device, MGX_UNET_PARAMS) = d loss / d weights
+ * (the BF16 weights the forward pass used); loss is one device double */
+int mgx_unet_loss_grad(mgx_unet* net, const float* x, const float* target, size_t ld,
+    int nfunc, float* grad, double* loss, void* stream);
+/* one Adam step (bias-corrected) of the master weights with grad */
+int mgx_unet_adam(mgx_unet* net, const float* grad, const mgx_adam_params* p, void* stream);
+/* mgx_unet_loss_grad then mgx_unet_adam, the gradient kept by the net */
+int mgx_unet_train_step(mgx_unet* net, const float* x, const float* target, size_t ld,
+    int nfunc, const mgx_adam_params* p, double* loss, void* stream);
+
+#define MGX_LEARNED_REPLACE 0 /* correction = net(res) */
+#define MGX_LEARNED_WARM 1    /* correction = V-cycle(res) started from net(res) */
+#define MGX_LEARNED_REFRESH 2 /* flag: run the plain V-cycle on every function */
+
+/* The learned correction of nfunc FP32 residuals, with the plain V-cycle
+ * (mgx_precond_mg with p) as the per-function fallback.  The residual
+ * reduction of a correction v of res is |res - A v| / |res|, A the fine
+ * operator of p->lap_type (the operator the V-cycle inverts).  tau (host,
+ * nfunc, in / out) holds the plain V-cycle's reduction for each function
+ * as last measured (<= 0: unknown).  The V-cycle runs on every function
+ * whose tau is unknown, whose learned reduction exceeds tau, or on all of
+ * them with MGX_LEARNED_REFRESH; it measures tau again, and out_j takes
+ * the V-cycle's correction where its reduction is the smaller.
+ * reduction (host, nfunc, or NULL) receives the reduction of each
+ * returned correction, nfallback (or NULL) the number of functions that
+ * took the V-cycle's.  Synchronizes the stream to make the choice. */
+int mgx_precond_learned(mgx_ctx* ctx, mgx_unet* net, const mgx_precond_params* p,
+    const float* res, size_t ld, float* out, int nfunc, int mode, double* tau,
+    double* reduction, int* nfallback, void* stream);
 
 #ifdef __cplusplus
 }

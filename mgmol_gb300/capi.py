@@ -14,6 +14,7 @@ C ABI (use .T to read them row-major; S and S^-1 are symmetric).
 import ctypes
 import os
 
+import numpy as np
 import torch
 
 HERE = os.path.dirname(os.path.abspath(__file__))
@@ -72,6 +73,14 @@ class AndersonInfo(ctypes.Structure):
     _fields_ = [("mm", ctypes.c_int), ("reductions", ctypes.c_int),
                 ("theta", ctypes.c_double * ANDERSON_MAX_M)]
 
+
+class AdamParams(ctypes.Structure):
+    _fields_ = [("lr", ctypes.c_float), ("beta1", ctypes.c_float), ("beta2", ctypes.c_float),
+                ("eps", ctypes.c_float)]
+
+
+UNET_PARAMS = 139104
+LEARNED_REPLACE, LEARNED_WARM, LEARNED_REFRESH = 0, 1, 2
 
 _LIB = None
 _vp = ctypes.c_void_p
@@ -132,6 +141,17 @@ _SIGS = {
     "mgx_anderson_destroy": [_vp],
     "mgx_anderson_restart": [_vp],
     "mgx_anderson_update": [_vp, _vp, _vp, _d, _vp, _vp, ctypes.POINTER(AndersonInfo), _vp],
+    "mgx_precond_mg_warm": [_vp, ctypes.POINTER(PrecondParams), _i, _vp, _sz, _vp, _i, _vp, _vp],
+    "mgx_unet_create": [_vp, ctypes.POINTER(_vp)],
+    "mgx_unet_destroy": [_vp],
+    "mgx_unet_set_params": [_vp, _vp, _vp],
+    "mgx_unet_get_params": [_vp, _vp, _vp],
+    "mgx_unet_forward": [_vp, _vp, _sz, _vp, _i, _vp],
+    "mgx_unet_loss_grad": [_vp, _vp, _vp, _sz, _i, _vp, _vp, _vp],
+    "mgx_unet_adam": [_vp, _vp, ctypes.POINTER(AdamParams), _vp],
+    "mgx_unet_train_step": [_vp, _vp, _vp, _sz, _i, ctypes.POINTER(AdamParams), _vp, _vp],
+    "mgx_precond_learned": [_vp, _vp, ctypes.POINTER(PrecondParams), _vp, _sz, _vp, _i, _i, _dp,
+                            _dp, _ip, _vp],
 }
 
 # every entry point declared in include/mgx.h
@@ -320,6 +340,17 @@ class Context:
         prm = PrecondParams(lap_type, maxlevels, float(gamma), int(chunk))
         _check(load().mgx_precond_mg(self.handle, ctypes.byref(prm), _dtype(res), p, ld, _ptr(out), nf,
                                      masks.handle if masks is not None else None, _stream(stream)))
+        return out
+
+    def precond_mg_warm(self, res, out, lap_type, maxlevels, masks=None, chunk=0, stream=None):
+        """out <- V-cycle(res) started from the iterate out holds."""
+        p, ld, nf = _block(res, self.npts)
+        po, ldo, _ = _block(out, self.npts)
+        assert ldo == ld
+        prm = PrecondParams(lap_type, maxlevels, 0.0, int(chunk))
+        _check(load().mgx_precond_mg_warm(self.handle, ctypes.byref(prm), _dtype(res), p, ld, po, nf,
+                                          masks.handle if masks is not None else None,
+                                          _stream(stream)))
         return out
 
     def precond_update(self, res, psi, alpha, lap_type, maxlevels, gamma, masks=None, chunk=0,
@@ -690,3 +721,86 @@ def mgkernel_extend3d(n, ll, ghosts, coarse, fine, nfunc, stream=None):
     g = Grid.make(n, ll)
     _check(load().mgx_mgkernel_extend3d(ctypes.byref(g), ghosts, _dtype(coarse), _ptr(coarse),
                                         _ptr(fine), nfunc, _stream(stream)))
+
+
+class UNet:
+    """The learned preconditioner's network on a context's grid
+    (mgx_unet_*): FP32 master weights, BF16 in the convolutions."""
+
+    def __init__(self, ctx):
+        self.ctx = ctx
+        self.handle = ctypes.c_void_p()
+        _check(load().mgx_unet_create(ctx.handle, ctypes.byref(self.handle)))
+        self._loss = torch.zeros(1, dtype=torch.float64, device="cuda")
+
+    def __del__(self):
+        if getattr(self, "handle", None) and _LIB is not None:
+            _LIB.mgx_unet_destroy(self.handle)
+            self.handle = None
+
+    def set_params(self, p, stream=None):
+        p = torch.as_tensor(p, dtype=torch.float32).cuda().contiguous()
+        if p.numel() != UNET_PARAMS:
+            raise ValueError(f"{UNET_PARAMS} parameters expected")
+        _check(load().mgx_unet_set_params(self.handle, _ptr(p), _stream(stream)))
+        torch.cuda.current_stream().synchronize() if stream is None else stream.synchronize()
+
+    def get_params(self, stream=None):
+        p = torch.empty(UNET_PARAMS, dtype=torch.float32, device="cuda")
+        _check(load().mgx_unet_get_params(self.handle, _ptr(p), _stream(stream)))
+        return p
+
+    def forward(self, x, out=None, stream=None):
+        px, ld, nf = _block(x, self.ctx.npts)
+        out = torch.empty_like(x) if out is None else out
+        po, ldo, _ = _block(out, self.ctx.npts)
+        assert ldo == ld and x.dtype == torch.float32
+        _check(load().mgx_unet_forward(self.handle, px, ld, po, nf, _stream(stream)))
+        return out
+
+    def loss_grad(self, x, target, grad=None, stream=None):
+        """(loss tensor, grad tensor) of mean((net(x/s) - target/s)^2)."""
+        px, ld, nf = _block(x, self.ctx.npts)
+        pt, ldt, _ = _block(target, self.ctx.npts)
+        assert ldt == ld
+        grad = torch.empty(UNET_PARAMS, dtype=torch.float32, device="cuda") if grad is None else grad
+        loss = torch.empty(1, dtype=torch.float64, device="cuda")
+        _check(load().mgx_unet_loss_grad(self.handle, px, pt, ld, nf, _ptr(grad), _ptr(loss),
+                                         _stream(stream)))
+        return loss, grad
+
+    def adam(self, grad, lr, beta1=0.9, beta2=0.999, eps=1e-8, stream=None):
+        prm = AdamParams(lr, beta1, beta2, eps)
+        _check(load().mgx_unet_adam(self.handle, _ptr(grad), ctypes.byref(prm), _stream(stream)))
+
+    def train_step(self, x, target, lr, beta1=0.9, beta2=0.999, eps=1e-8, stream=None):
+        """One loss / gradient / Adam step; returns the loss as a device tensor."""
+        px, ld, nf = _block(x, self.ctx.npts)
+        pt, ldt, _ = _block(target, self.ctx.npts)
+        assert ldt == ld
+        prm = AdamParams(lr, beta1, beta2, eps)
+        loss = torch.empty(1, dtype=torch.float64, device="cuda")
+        _check(load().mgx_unet_train_step(self.handle, px, pt, ld, nf, ctypes.byref(prm), _ptr(loss),
+                                          _stream(stream)))
+        return loss
+
+
+def precond_learned(ctx, net, res, lap_type, maxlevels, gamma, tau, mode=LEARNED_WARM, chunk=0,
+                    out=None, stream=None):
+    """The learned correction of res with the V-cycle as per-function
+    fallback (mgx_precond_learned).  tau: float64 numpy array (nfunc), the
+    V-cycle's residual reduction per function, updated in place.  Returns
+    (out, reduction per function, number of fallbacks)."""
+    p, ld, nf = _block(res, ctx.npts)
+    out = torch.empty_like(res) if out is None else out
+    po, ldo, _ = _block(out, ctx.npts)
+    assert ldo == ld and res.dtype == torch.float32
+    if tau.dtype != np.float64 or tau.size < nf or not tau.flags["C_CONTIGUOUS"]:
+        raise ValueError("tau must be a contiguous float64 array of nfunc values")
+    red = np.zeros(nf)
+    nfb = ctypes.c_int()
+    prm = PrecondParams(lap_type, maxlevels, float(gamma), int(chunk))
+    _check(load().mgx_precond_learned(ctx.handle, net.handle, ctypes.byref(prm), p, ld, po, nf,
+                                      int(mode), tau.ctypes.data_as(_dp), red.ctypes.data_as(_dp),
+                                      ctypes.byref(nfb), _stream(stream)))
+    return out, red, nfb.value

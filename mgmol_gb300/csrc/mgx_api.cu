@@ -68,7 +68,7 @@ void DeviceBuffer::release()
 // defined in the other translation units
 int precond_mg(mgx_ctx*, const mgx_precond_params*, int, const void*, size_t,
     void*, int, const mgx_masks*, cudaStream_t, void* upd = nullptr, double alpha = 0.,
-    const double* scale = nullptr);
+    const double* scale = nullptr, bool warm = false);
 int restrict_launch(int, const Level&, const void*, size_t, void*, size_t, int,
     const MaskDev&, cudaStream_t);
 int prolong_launch(int, int, const Level&, const void*, size_t, void*, size_t,
@@ -480,6 +480,21 @@ int mgx_precond_mg(mgx_ctx* ctx, const mgx_precond_params* p, mgx_dtype dtype,
     int st = precond_mg(ctx, p, dtype, res, ldv, out, nfunc, masks, (cudaStream_t)stream);
     if (st != MGX_OK) return st;
     return MGX_OK;
+}
+
+int mgx_precond_mg_warm(mgx_ctx* ctx, const mgx_precond_params* p, mgx_dtype dtype,
+    const void* res, size_t ld, void* out, int nfunc, const mgx_masks* masks, void* stream)
+{
+    if (!ctx) return fail(MGX_BAD_ARG, "ctx is NULL");
+    MGX_TRY(check_dtype(dtype));
+    MGX_TRY(check_block(ctx->grid, res, ld, nfunc, "res"));
+    MGX_TRY(check_block(ctx->grid, out, ld, nfunc, "out"));
+    if (masks && masks->dtype != dtype)
+        return fail(MGX_BAD_ARG, "mask value type differs from the orbital type");
+    const size_t np  = (size_t)ctx->grid.n[0] * ctx->grid.n[1] * ctx->grid.n[2];
+    const size_t ldv = nfunc > 1 ? ld : (ld ? ld : np);
+    return precond_mg(ctx, p, dtype, res, ldv, out, nfunc, masks, (cudaStream_t)stream, nullptr,
+        0., nullptr, true);
 }
 
 int mgx_precond_mg_update(mgx_ctx* ctx, const mgx_precond_params* p, mgx_dtype dtype,

@@ -824,13 +824,17 @@ struct VCycle
 /* out = V-cycle(res); or, with upd set, upd += alpha * V-cycle(res)
  * through the last fine-level sweep (upd_j = scale_j (upd_j + alpha
  * V-cycle(res)_j) when scale is given), and out (nfunc x ld, may be NULL)
- * is only scratch for the fine-level iterate */
+ * is only scratch for the fine-level iterate.  warm: the V-cycle starts
+ * from the iterate that out holds on entry instead of gamma * res. */
 int precond_mg(mgx_ctx* ctx, const mgx_precond_params* P, int dtype,
     const void* res, size_t ld, void* out, int nfunc, const mgx_masks* masks,
-    cudaStream_t s, void* upd = nullptr, double alpha = 0., const double* scale = nullptr)
+    cudaStream_t s, void* upd = nullptr, double alpha = 0., const double* scale = nullptr,
+    bool warm = false)
 {
     if (!P || !res || (!out && !upd) || nfunc < 0)
         return fail(MGX_BAD_ARG, "precond_mg: null argument");
+    if (warm && (!out || upd))
+        return fail(MGX_BAD_ARG, "precond_mg: a warm start needs out and no update block");
     if (res == out || res == upd || (upd && upd == out))
         return fail(MGX_BAD_ARG, "precond_mg: res, out and the update block alias");
     if (P->lap_type < 0 || P->lap_type > 4) return fail(MGX_BAD_ARG, "lap_type %d", P->lap_type);
@@ -926,9 +930,10 @@ int precond_mg(mgx_ctx* ctx, const mgx_precond_params* P, int dtype,
             V.f[l] = base;
             base += (size_t)nf * pl * es;
         }
-        // v = gamma * res (src/OrbitalsPreconditioning.cc:102-107)
+        // v = gamma * res (src/OrbitalsPreconditioning.cc:102-107), or, for
+        // a warm start, the iterate the caller left in out
         V.gamma         = P->gamma;
-        V.pending_scale = true;
+        V.pending_scale = !warm;
         const int c = V.mg(0);
         if (c < 0) return -(c + 1);
         if (c != 0) return fail(MGX_UNSUPPORTED, "V-cycle ended in the work buffer");
