@@ -9,10 +9,11 @@ systems that the orbital V-cycle preconditions (Preconditioning<T>::mg,
 src/Preconditioning.cc:155-216, with the fine operator A of lap_type,
 periodic, right-hand sides of zero mean):
 
-    r = f - A x ;  x += P(r)
+    r = f - A x ;  x += omega P(r)
 
 with P the plain V-cycle (mgx_precond_mg, started from gamma r as
-OrbitalsPreconditioning::precond_mg does) or the learned correction.  x and
+OrbitalsPreconditioning::precond_mg does) or the learned correction, and
+omega the step (1; ABPG's 0.5 * precond_factor is 0.5).  x and
 r are FP64, so that |r| can fall to 1e-6 |f|; P works on the FP32 residual
 like the reference's float preconditioner.
 
@@ -58,12 +59,13 @@ def init_params(seed):
 class BlockSolver:
     """The block preconditioned-gradient iteration for A x = f."""
 
-    def __init__(self, ctx, lap_type, maxlevels, gamma, chunk=0):
+    def __init__(self, ctx, lap_type, maxlevels, gamma, chunk=0, omega=1.0):
         self.ctx = ctx
         self.lap = lap_type
         self.maxlevels = maxlevels
         self.gamma = gamma
         self.chunk = chunk
+        self.omega = omega
 
     def vcycle(self, r32, out=None):
         return self.ctx.precond_mg(r32, self.lap, self.maxlevels, self.gamma, chunk=self.chunk,
@@ -92,7 +94,7 @@ class BlockSolver:
             c = precond(r32)
             if on_pair is not None:
                 on_pair(r32, c)
-            x += c.double()
+            x.add_(c.double(), alpha=self.omega)
             self.ctx.fd_apply(x, self.lap, out=r)
             torch.sub(f, r, out=r)
         return its, hist
@@ -172,17 +174,22 @@ def main(argv=None):
     ap.add_argument("--test-funcs", type=int, default=64)
     ap.add_argument("--tol", type=float, default=1e-6)
     ap.add_argument("--maxit", type=int, default=300)
+    ap.add_argument("--omega", type=float, default=1.0)
+    ap.add_argument("--mode", choices=["warm", "replace"], default="warm")
+    ap.add_argument("--refresh", action="store_true",
+                    help="run the V-cycle on every function at every step (exact fallback)")
     ap.add_argument("--seed", type=int, default=1004)
     ap.add_argument("--save", default=None, help="write the trained weights (.npy)")
+    ap.add_argument("--load", default=None, help="start from these weights (.npy)")
     a = ap.parse_args(argv)
 
     n = tuple(a.grid)
     ll = tuple(x * a.h for x in n)
     ctx = capi.Context(n, ll)
     gamma = ctx.gamma(a.lap, a.maxlevels, 0.0, 0.0)
-    solver = BlockSolver(ctx, a.lap, a.maxlevels, gamma)
+    solver = BlockSolver(ctx, a.lap, a.maxlevels, gamma, omega=a.omega)
     net = capi.UNet(ctx)
-    net.set_params(init_params(a.seed))
+    net.set_params(np.load(a.load) if a.load else init_params(a.seed))
 
     # training on the plain iteration's pairs, generated chunk by chunk
     t0 = time.time()
@@ -203,7 +210,9 @@ def main(argv=None):
     # the test block: plain against learned (warm start, fallback)
     f = rhs_block(n, ll, a.test_funcs, a.seed + 200)
     res = {}
-    for name, pc in (("plain", solver.vcycle), ("learned", Learned(solver, net))):
+    mode = capi.LEARNED_WARM if a.mode == "warm" else capi.LEARNED_REPLACE
+    for name, pc in (("plain", solver.vcycle),
+                     ("learned", Learned(solver, net, mode=mode, refresh=a.refresh))):
         torch.cuda.synchronize()
         t1 = time.time()
         its, hist = solver.run(f, pc, tol=a.tol, maxit=a.maxit)
@@ -228,7 +237,8 @@ def main(argv=None):
         e1.record()
         torch.cuda.synchronize()
         res[f"ms_{name}"] = e0.elapsed_time(e1) / 3
-    out = {"grid": list(n), "h": a.h, "lap_type": a.lap, "train_funcs": a.train_funcs,
+    out = {"grid": list(n), "h": a.h, "lap_type": a.lap, "omega": a.omega, "mode": a.mode,
+           "refresh": a.refresh, "train_funcs": a.train_funcs,
            "pairs": pairs, "train_seconds": t_train, "loss_first": losses[0] if losses else None,
            "loss_last": losses[-1] if losses else None, "test_funcs": a.test_funcs, "tol": a.tol,
            **res}
