@@ -612,6 +612,50 @@ int mgx_precond_learned(mgx_ctx* ctx, mgx_unet* net, const mgx_precond_params* p
     const float* res, size_t ld, float* out, int nfunc, int mode, double* tau,
     double* reduction, int* nfallback, void* stream);
 
+/* ---------------- localized orbitals ----------------
+ * Orbital j stored on the level-0 box of its mask in `masks` (origin o_j,
+ * extents e_j; box point b is grid point (o_j + b) mod n, z fastest), the
+ * boxes packed one after another: the localized storage of
+ * LocGridOrbitals, without the zeros outside the localization regions.
+ * masks: FP32, GridMaskMax (kind 0), every orbital with a box of values;
+ * corr: the correction masks (profile one, GridMaskMult) of the same
+ * centres and radii, so the same boxes.  Each box extent must leave room for
+ * a halo of 3 points inside the grid.  Both mask sets must outlive the
+ * handle. */
+typedef struct mgx_local mgx_local;
+
+int mgx_local_create(mgx_ctx* ctx, const mgx_masks* masks, const mgx_masks* corr,
+    mgx_local** loc);
+int mgx_local_destroy(mgx_local* loc);
+/* total packed points; offsets (nfunc + 1 values) and boxes (6 per orbital:
+ * origin, extents), each optional */
+int mgx_local_layout(const mgx_local* loc, size_t* total, size_t* offsets, int* boxes);
+/* whole-grid block (leading dimension ld) -> packed boxes, and back (scatter
+ * writes the box points only) */
+int mgx_local_gather(mgx_local* loc, const float* full, size_t ld, float* packed, void* stream);
+int mgx_local_scatter(mgx_local* loc, const float* packed, float* full, size_t ld, void* stream);
+/* The fused fine-level step on packed FP32 blocks, one persistent kernel
+ * over (orbital, tile) items:
+ *   r  = Mc (B phi - H psi),  H psi = -Delta_M psi + B(V psi)
+ *   u1 = M(gamma r - jf (A gamma r - r)),  A = -Delta_M
+ *   u  = M(u1 - jf (A u1 - r)),  w = M(A u1 - r)
+ * (Hamiltonian::applyLocal, the residual of computeResidualUsingHPhi with
+ * phi = (Psi Theta)_j and the correction mask, and the two masked Jacobi
+ * pre-sweeps of Preconditioning<T>::mg started from gamma r, jf the
+ * Mehrstellen Jacobi factor).  V: FP32, the whole grid.  With the graph
+ * option (the default) the launch is a CUDA graph, captured again when an
+ * argument or the configuration changes. */
+int mgx_local_step(mgx_local* loc, const float* psi, const float* phi, const float* V,
+    double gamma, float* u, float* w, void* stream);
+/* times every column shape (TY x TZ; 0: 8x32, 1: 16x32, 2: 16x16) with 1,
+ * 2, 4 and 8 resident CTAs per SM on these arguments and keeps the fastest; ms
+ * (optional, *ncand entries) receives each candidate's time (-1: not
+ * resident), *ncand the number of candidates */
+int mgx_local_tune(mgx_local* loc, const float* psi, const float* phi, const float* V,
+    double gamma, float* u, float* w, double* ms, int* ncand, void* stream);
+int mgx_local_set_config(mgx_local* loc, int shape, int ctas_per_sm, int use_graph);
+int mgx_local_get_config(const mgx_local* loc, int* shape, int* ctas_per_sm, int* use_graph);
+
 #ifdef __cplusplus
 }
 #endif

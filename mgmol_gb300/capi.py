@@ -150,6 +150,15 @@ _SIGS = {
     "mgx_unet_loss_grad": [_vp, _vp, _vp, _sz, _i, _vp, _vp, _vp],
     "mgx_unet_adam": [_vp, _vp, ctypes.POINTER(AdamParams), _vp],
     "mgx_unet_train_step": [_vp, _vp, _vp, _sz, _i, ctypes.POINTER(AdamParams), _vp, _vp],
+    "mgx_local_create": [_vp, _vp, _vp, ctypes.POINTER(_vp)],
+    "mgx_local_destroy": [_vp],
+    "mgx_local_layout": [_vp, ctypes.POINTER(_sz), ctypes.POINTER(_sz), _ip],
+    "mgx_local_gather": [_vp, _vp, _sz, _vp, _vp],
+    "mgx_local_scatter": [_vp, _vp, _vp, _sz, _vp],
+    "mgx_local_step": [_vp, _vp, _vp, _vp, _d, _vp, _vp, _vp],
+    "mgx_local_tune": [_vp, _vp, _vp, _vp, _d, _vp, _vp, _dp, _ip, _vp],
+    "mgx_local_set_config": [_vp, _i, _i, _i],
+    "mgx_local_get_config": [_vp, _ip, _ip, _ip],
     "mgx_precond_learned": [_vp, _vp, ctypes.POINTER(PrecondParams), _vp, _sz, _vp, _i, _i, _dp,
                             _dp, _ip, _vp],
 }
@@ -804,3 +813,73 @@ def precond_learned(ctx, net, res, lap_type, maxlevels, gamma, tau, mode=LEARNED
                                       int(mode), tau.ctypes.data_as(_dp), red.ctypes.data_as(_dp),
                                       ctypes.byref(nfb), _stream(stream)))
     return out, red, nfb.value
+
+
+class Local:
+    """Localized orbitals on their mask boxes (mgx_local_*): packed box-local
+    FP32 blocks and the fused fine-level step."""
+
+    def __init__(self, ctx, masks, corr):
+        self.ctx = ctx
+        self._keep = (masks, corr)
+        self.handle = ctypes.c_void_p()
+        _check(load().mgx_local_create(ctx.handle, masks.handle, corr.handle,
+                                       ctypes.byref(self.handle)))
+        self.nfunc = masks.nfunc
+        tot = ctypes.c_size_t()
+        self.offsets = np.zeros(self.nfunc + 1, dtype=np.uint64)
+        self.boxes = np.zeros(6 * self.nfunc, dtype=np.int32)
+        _check(load().mgx_local_layout(self.handle, ctypes.byref(tot),
+                                       self.offsets.ctypes.data_as(ctypes.POINTER(_sz)),
+                                       self.boxes.ctypes.data_as(_ip)))
+        self.total = tot.value
+        self.boxes = self.boxes.reshape(self.nfunc, 6)
+
+    def __del__(self):
+        if getattr(self, "handle", None) and _LIB is not None:
+            _LIB.mgx_local_destroy(self.handle)
+            self.handle = None
+
+    def empty(self):
+        return torch.empty(max(self.total, 1), dtype=torch.float32, device="cuda")
+
+    def gather(self, full, out=None, stream=None):
+        p, ld, nf = _block(full, self.ctx.npts)
+        assert nf == self.nfunc and full.dtype == torch.float32
+        out = self.empty() if out is None else out
+        _check(load().mgx_local_gather(self.handle, p, ld, _ptr(out), _stream(stream)))
+        return out
+
+    def scatter(self, packed, out=None, stream=None):
+        out = (torch.zeros((self.nfunc, self.ctx.npts), dtype=torch.float32, device="cuda")
+               if out is None else out)
+        p, ld, nf = _block(out, self.ctx.npts)
+        _check(load().mgx_local_scatter(self.handle, _ptr(packed), p, ld, _stream(stream)))
+        return out
+
+    def step(self, psi, phi, V, gamma, u=None, w=None, stream=None):
+        u = self.empty() if u is None else u
+        w = self.empty() if w is None else w
+        _check(load().mgx_local_step(self.handle, _ptr(psi), _ptr(phi), _ptr(V), float(gamma),
+                                     _ptr(u), _ptr(w), _stream(stream)))
+        return u, w
+
+    def tune(self, psi, phi, V, gamma, u, w, stream=None):
+        """Times the candidates and keeps the fastest; returns (times in ms
+        per candidate, (shape, ctas_per_sm, graph))."""
+        ms = np.zeros(32)
+        n = ctypes.c_int(32)
+        _check(load().mgx_local_tune(self.handle, _ptr(psi), _ptr(phi), _ptr(V), float(gamma),
+                                     _ptr(u), _ptr(w), ms.ctypes.data_as(_dp), ctypes.byref(n),
+                                     _stream(stream)))
+        return ms[:n.value].copy(), self.config()
+
+    def config(self):
+        a, b, c = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        _check(load().mgx_local_get_config(self.handle, ctypes.byref(a), ctypes.byref(b),
+                                           ctypes.byref(c)))
+        return a.value, b.value, c.value
+
+    def set_config(self, shape, ctas_per_sm, graph=True):
+        _check(load().mgx_local_set_config(self.handle, int(shape), int(ctas_per_sm),
+                                           1 if graph else 0))

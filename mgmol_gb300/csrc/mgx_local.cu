@@ -1,0 +1,692 @@
+// Localized orbitals: box-local storage and one persistent fused kernel for
+// the fine-level work of an orbital iteration on uneven mask boxes.
+//
+// Orbital j lives on the level-0 box of its localization mask (origin o_j,
+// extents e_j, the box form of mgx_masks: point b of the box is grid point
+// (o_j + b) mod n, z fastest), packed one box after another.  Outside its
+// box an orbital is zero, which is what the masks make of it on the whole
+// grid: the mask values are zero there (src/GridMask.cc:120-264).
+//
+// The fused step, per orbital (FP32, the reference's operators):
+//   r  = Mc (B(phi - V psi) + Delta_M psi)       = Mc (B phi - H psi)
+//   u0 = gamma r
+//   u1 = M(u0 - jf (A u0 - r))                    first Jacobi sweep
+//   u2 = M(u1 - jf (A u1 - r)),  w = M(A u1 - r)  second sweep
+// with H psi = -Delta_M psi + B(V psi) (Hamiltonian::applyLocal,
+// src/Hamiltonian.cc:106-132), phi the column of Psi Theta (the residual of
+// MGmol::computeResidualUsingHPhi, src/MGmol.cc:1227-1290, with the
+// correction mask Mc of LocGridOrbitals::applyCorrMask), A = -Delta_M and
+// the orbital mask M (GridMaskMax) of the V-cycle's fine-level pre-sweeps
+// (Preconditioning<T>::mg, src/Preconditioning.cc:170-178).  u2 and w are
+// what the V-cycle restricts next.
+//
+// One CTA takes (orbital, column) items from a work list until it is empty
+// (largest boxes first); a column is a TY x TZ window of the box marched
+// along x, each stage keeping three planes in shared memory, so the
+// orbital block is read once (plus the y / z halo) and u2, w written once.
+// The column shape and the CTAs per SM are chosen by timing
+// (mgx_local_tune); the launch can be a CUDA graph.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <memory>
+#include <vector>
+
+#include "mgx_internal.cuh"
+#include "mgx_stencil.cuh"
+
+namespace mgx
+{
+namespace loc
+{
+constexpr int THREADS = 256;
+constexpr int HALO    = 3;
+
+struct StepParams
+{
+    const float* psi;
+    const float* phi;
+    const float* V; // FP32 potential on the whole grid
+    float* u;
+    float* w;
+    const int* box;       // 6 per orbital: origin, extents
+    const size_t* off;    // packed offset of each orbital
+    const float* mvals;   // orbital mask values, box-local
+    const size_t* moff;
+    const float* cvals;   // correction mask values, box-local
+    const size_t* coff;
+    const int4* items;    // (orbital, 0, column origin y, z)
+    int nitems;
+    int* counter;
+    int n[3];
+    float c0, cx, cy, cz, cxy, cyz, cxz; // -Delta_M
+    float gamma, jf;
+};
+
+__device__ __forceinline__ int wrapi(int i, int n)
+{
+    i %= n;
+    return i < 0 ? i + n : i;
+}
+
+__device__ __forceinline__ float clampm(float v, float m)
+{
+    if (v > m) return m;
+    if (v < -m) return -m;
+    return v;
+}
+
+/* -Delta_M at index i of plane C, with the x neighbours in planes M and P
+ * (plane stride sy along y, 1 along z) */
+__device__ __forceinline__ float lap_m(const float* M, const float* C, const float* Pn, int i,
+    int sy, const StepParams& P)
+{
+    const float faces = P.cx * (M[i] + Pn[i]) + P.cy * (C[i - sy] + C[i + sy])
+        + P.cz * (C[i - 1] + C[i + 1]);
+    const float exy = M[i - sy] + M[i + sy] + Pn[i - sy] + Pn[i + sy];
+    const float eyz = C[i - sy - 1] + C[i - sy + 1] + C[i + sy - 1] + C[i + sy + 1];
+    const float exz = M[i - 1] + M[i + 1] + Pn[i - 1] + Pn[i + 1];
+    return P.c0 * C[i] + faces + P.cxy * exy + P.cyz * eyz + P.cxz * exz;
+}
+
+/* B = 1/2 + (1/12) sum of the six faces (FDkernelRHS_4th_Mehr1) */
+__device__ __forceinline__ float rhs_b(const float* M, const float* C, const float* Pn, int i,
+    int sy)
+{
+    const float s = (M[i] + Pn[i]) + (C[i - sy] + C[i + sy]) + (C[i - 1] + C[i + 1]);
+    return 0.5f * C[i] + (1.f / 12.f) * s;
+}
+
+/* one periodic coordinate of a box point: b in [-3, e + 3) with e + 6 <= n */
+__device__ __forceinline__ int wrap1(int g, int n)
+{
+    return g < 0 ? g + n : (g >= n ? g - n : g);
+}
+
+/* A CTA owns a TY x TZ column of an orbital's box and marches along x.
+ * Plane regions shrink by one point per stage in y and z: stage 0 (psi and
+ * phi - V psi) on (TY + 6) x (TZ + 6), stage 1 (r) on (TY + 4) x (TZ + 4),
+ * stage 2 (u1) on (TY + 2) x (TZ + 2), stage 3 (u, w) on TY x TZ.  Each
+ * stage keeps its last three planes in a ring; at march step t the stages
+ * produce planes t - 3, t - 4, t - 5 and t - 6 (box-local x), so every
+ * plane a stage reads was made at an earlier step or earlier in this one. */
+template <int TY, int TZ> struct Cols
+{
+    static constexpr int Y3 = TY + 6, Z3 = TZ + 6, N3 = Y3 * Z3;
+    static constexpr int Y2 = TY + 4, Z2 = TZ + 4, N2 = Y2 * Z2;
+    static constexpr int Y1 = TY + 2, Z1 = TZ + 2, N1 = Y1 * Z1;
+    static constexpr int N0 = TY * TZ;
+    static constexpr size_t SMEM = (size_t)(3 * (2 * N3 + N2 + N1)) * sizeof(float);
+};
+
+template <int TY, int TZ>
+__global__ void __launch_bounds__(THREADS) local_step_kernel(StepParams P)
+{
+    using C = Cols<TY, TZ>;
+    extern __shared__ __align__(16) float sm[];
+    float* s_psi = sm;               // 3 x N3
+    float* s_d   = s_psi + 3 * C::N3; // 3 x N3: phi - V psi
+    float* s_r   = s_d + 3 * C::N3;   // 3 x N2
+    float* s_u   = s_r + 3 * C::N2;   // 3 x N1
+    __shared__ int s_item;
+    const int tid = threadIdx.x;
+    for (;;)
+    {
+        __syncthreads();
+        if (tid == 0) s_item = atomicAdd(P.counter, 1);
+        __syncthreads();
+        const int it = s_item;
+        if (it >= P.nitems) break;
+        const int4 W = P.items[it]; // (orbital, -, y0, z0)
+        const int f  = W.x;
+        const int* b = P.box + 6 * f;
+        const int o0 = b[0], o1 = b[1], o2 = b[2], e0 = b[3], e1 = b[4], e2 = b[5];
+        const int y0 = W.z, z0 = W.w;
+        const size_t ex = (size_t)e1 * e2;
+        const float* psi = P.psi + P.off[f];
+        const float* phi = P.phi + P.off[f];
+        const float* mo  = P.mvals + P.moff[f];
+        const float* mc  = P.cvals + P.coff[f];
+        for (int t = 0; t < e0 + 6; t++)
+        {
+            // stage 0: plane t - 3 of psi and phi - V psi
+            {
+                const int p   = t - 3;
+                float* dp     = s_psi + ((p + 3) % 3) * C::N3;
+                float* dd     = s_d + ((p + 3) % 3) * C::N3;
+                const bool in = (p >= 0 && p < e0);
+                const int gx  = wrap1(o0 + p, P.n[0]);
+                for (int q = tid; q < C::N3; q += THREADS)
+                {
+                    const int qy = q / C::Z3, qz = q - qy * C::Z3;
+                    const int by = y0 + qy - 3, bz = z0 + qz - 3;
+                    float ps = 0.f, d = 0.f;
+                    if (in && by >= 0 && by < e1 && bz >= 0 && bz < e2)
+                    {
+                        const size_t li = (size_t)p * ex + (size_t)by * e2 + bz;
+                        ps              = psi[li];
+                        const int gy = wrap1(o1 + by, P.n[1]), gz = wrap1(o2 + bz, P.n[2]);
+                        const float v = P.V[((size_t)gx * P.n[1] + gy) * P.n[2] + gz];
+                        d             = phi[li] - v * ps;
+                    }
+                    dp[q] = ps;
+                    dd[q] = d;
+                }
+            }
+            __syncthreads();
+            // stage 1: plane t - 4 of r = Mc (B(phi - V psi) + Delta_M psi)
+            if (t >= 2)
+            {
+                const int p    = t - 4;
+                const float* M = s_psi + ((p + 2) % 3) * C::N3; // plane p - 1
+                const float* X = s_psi + ((p + 3) % 3) * C::N3;
+                const float* N = s_psi + ((p + 4) % 3) * C::N3;
+                const float* dM = s_d + ((p + 2) % 3) * C::N3;
+                const float* dX = s_d + ((p + 3) % 3) * C::N3;
+                const float* dN = s_d + ((p + 4) % 3) * C::N3;
+                float* out      = s_r + ((p + 3) % 3) * C::N2;
+                const bool in   = (p >= 0 && p < e0);
+                for (int q = tid; q < C::N2; q += THREADS)
+                {
+                    const int qy = q / C::Z2, qz = q - qy * C::Z2;
+                    const int by = y0 + qy - 2, bz = z0 + qz - 2;
+                    float m      = 0.f;
+                    if (in && by >= 0 && by < e1 && bz >= 0 && bz < e2)
+                        m = mc[(size_t)p * ex + (size_t)by * e2 + bz];
+                    float r = 0.f;
+                    if (m != 0.f)
+                    {
+                        const int i = (qy + 1) * C::Z3 + qz + 1;
+                        r = m * (rhs_b(dM, dX, dN, i, C::Z3) - lap_m(M, X, N, i, C::Z3, P));
+                    }
+                    out[q] = r;
+                }
+            }
+            __syncthreads();
+            // stage 2: plane t - 5 of the first sweep u1, from u0 = gamma r
+            if (t >= 4)
+            {
+                const int p    = t - 5;
+                const float* M = s_r + ((p + 2) % 3) * C::N2;
+                const float* X = s_r + ((p + 3) % 3) * C::N2;
+                const float* N = s_r + ((p + 4) % 3) * C::N2;
+                float* out     = s_u + ((p + 3) % 3) * C::N1;
+                const bool in  = (p >= 0 && p < e0);
+                for (int q = tid; q < C::N1; q += THREADS)
+                {
+                    const int qy = q / C::Z1, qz = q - qy * C::Z1;
+                    const int by = y0 + qy - 1, bz = z0 + qz - 1;
+                    float m      = 0.f;
+                    if (in && by >= 0 && by < e1 && bz >= 0 && bz < e2)
+                        m = mo[(size_t)p * ex + (size_t)by * e2 + bz];
+                    const int i    = (qy + 1) * C::Z2 + qz + 1;
+                    const float r  = X[i];
+                    const float w0 = P.gamma * lap_m(M, X, N, i, C::Z2, P) - r;
+                    out[q]         = clampm(P.gamma * r - P.jf * w0, m);
+                }
+            }
+            __syncthreads();
+            // stage 3: plane t - 6 of the second sweep, stored inside the box
+            if (t >= 6)
+            {
+                const int p    = t - 6;
+                const float* M = s_u + ((p + 2) % 3) * C::N1;
+                const float* X = s_u + ((p + 3) % 3) * C::N1;
+                const float* N = s_u + ((p + 4) % 3) * C::N1;
+                const float* R = s_r + ((p + 3) % 3) * C::N2;
+                for (int q = tid; q < C::N0; q += THREADS)
+                {
+                    const int qy = q / TZ, qz = q - qy * TZ;
+                    const int by = y0 + qy, bz = z0 + qz;
+                    if (by >= e1 || bz >= e2) continue;
+                    const size_t li = (size_t)p * ex + (size_t)by * e2 + bz;
+                    const float m   = mo[li];
+                    const int i     = (qy + 1) * C::Z1 + qz + 1;
+                    const float w1  = lap_m(M, X, N, i, C::Z1, P) - R[(qy + 2) * C::Z2 + qz + 2];
+                    P.u[P.off[f] + li] = clampm(X[i] - P.jf * w1, m);
+                    P.w[P.off[f] + li] = clampm(w1, m);
+                }
+            }
+        }
+    }
+}
+
+/* packed box-local <-> whole-grid copies (blockIdx.y = orbital) */
+__global__ void __launch_bounds__(256) gather_kernel(const float* __restrict__ full, size_t ld,
+    float* __restrict__ packed, const int* __restrict__ box, const size_t* __restrict__ off,
+    int n0, int n1, int n2)
+{
+    const int f  = blockIdx.y;
+    const int* b = box + 6 * f;
+    const size_t vol = (size_t)b[3] * b[4] * b[5];
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < vol;
+         i += (size_t)gridDim.x * blockDim.x)
+    {
+        const int bz = (int)(i % b[5]), by = (int)((i / b[5]) % b[4]), bx = (int)(i / ((size_t)b[5] * b[4]));
+        const int gx = wrapi(b[0] + bx, n0), gy = wrapi(b[1] + by, n1), gz = wrapi(b[2] + bz, n2);
+        packed[off[f] + i] = full[(size_t)f * ld + ((size_t)gx * n1 + gy) * n2 + gz];
+    }
+}
+
+__global__ void __launch_bounds__(256) scatter_kernel(const float* __restrict__ packed,
+    float* __restrict__ full, size_t ld, const int* __restrict__ box,
+    const size_t* __restrict__ off, int n0, int n1, int n2)
+{
+    const int f  = blockIdx.y;
+    const int* b = box + 6 * f;
+    const size_t vol = (size_t)b[3] * b[4] * b[5];
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < vol;
+         i += (size_t)gridDim.x * blockDim.x)
+    {
+        const int bz = (int)(i % b[5]), by = (int)((i / b[5]) % b[4]), bx = (int)(i / ((size_t)b[5] * b[4]));
+        const int gx = wrapi(b[0] + bx, n0), gy = wrapi(b[1] + by, n1), gz = wrapi(b[2] + bz, n2);
+        full[(size_t)f * ld + ((size_t)gx * n1 + gy) * n2 + gz] = packed[off[f] + i];
+    }
+}
+
+/* the column shapes (TY x TZ) the tuner chooses from */
+struct Shape
+{
+    int ty, tz;
+};
+constexpr int NSHAPE           = 3;
+constexpr Shape SHAPES[NSHAPE] = { { 8, 32 }, { 16, 32 }, { 16, 16 } };
+
+template <int TY, int TZ> int set_attr()
+{
+    static bool done = false;
+    if (!done)
+    {
+        MGX_TRY(cuda_check(cudaFuncSetAttribute(local_step_kernel<TY, TZ>,
+                               cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)Cols<TY, TZ>::SMEM),
+            "local smem"));
+        done = true;
+    }
+    return MGX_OK;
+}
+
+template <int TY, int TZ> int occupancy()
+{
+    if (set_attr<TY, TZ>() != MGX_OK) return 1;
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, local_step_kernel<TY, TZ>, THREADS,
+            Cols<TY, TZ>::SMEM)
+        != cudaSuccess)
+    {
+        cudaGetLastError();
+        return 1;
+    }
+    return std::max(n, 1);
+}
+
+/* resident CTAs per SM of shape s (also sets its shared-memory limit) */
+int max_ctas_per_sm(int s)
+{
+    switch (s)
+    {
+        case 0: return occupancy<8, 32>();
+        case 1: return occupancy<16, 32>();
+        default: return occupancy<16, 16>();
+    }
+}
+
+template <int TY, int TZ> int launch_shape(const StepParams& P, int ctas, cudaStream_t s)
+{
+    local_step_kernel<TY, TZ><<<ctas, THREADS, Cols<TY, TZ>::SMEM, s>>>(P);
+    MGX_LAUNCH_CHECK("local_step_kernel");
+    return MGX_OK;
+}
+
+} // namespace loc
+} // namespace mgx
+
+struct mgx_local
+{
+    mgx_ctx* ctx       = nullptr;
+    int nfunc          = 0;
+    size_t total       = 0;
+    std::vector<int> h_box;      // 6 per orbital
+    std::vector<size_t> h_off;   // nfunc + 1
+    mgx::DeviceBuffer box, off, counter;
+    mgx::DeviceBuffer items[mgx::loc::NSHAPE];
+    int nitems[mgx::loc::NSHAPE] = { 0, 0, 0 };
+    const mgx_masks* masks = nullptr;
+    const mgx_masks* corr  = nullptr;
+    // chosen configuration
+    int shape = 1, ctas_per_sm = 2, use_graph = 1;
+    // the captured step, valid for the arguments it was captured with
+    cudaGraphExec_t exec = nullptr;
+    cudaGraph_t graph    = nullptr;
+    const void* key[5]   = { nullptr, nullptr, nullptr, nullptr, nullptr };
+    double key_gamma     = 0.;
+    int key_shape = -1, key_ctas = -1;
+    ~mgx_local()
+    {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+    }
+};
+
+namespace mgx
+{
+namespace loc
+{
+int build_items(mgx_local* L, int s)
+{
+    const Shape S = SHAPES[s];
+    std::vector<int4> it;
+    std::vector<std::pair<size_t, int>> order; // largest box first
+    for (int f = 0; f < L->nfunc; f++)
+        order.push_back({ (size_t)L->h_box[6 * f + 3] * L->h_box[6 * f + 4] * L->h_box[6 * f + 5], f });
+    std::stable_sort(order.begin(), order.end(),
+        [](const std::pair<size_t, int>& a, const std::pair<size_t, int>& b) { return a.first > b.first; });
+    for (const auto& pr : order)
+    {
+        const int f  = pr.second;
+        const int* e = &L->h_box[6 * f + 3];
+        for (int y = 0; y < e[1]; y += S.ty)
+            for (int z = 0; z < e[2]; z += S.tz)
+                it.push_back(make_int4(f, 0, y, z));
+    }
+    L->nitems[s] = (int)it.size();
+    MGX_TRY(L->items[s].ensure(std::max<size_t>(it.size(), 1) * sizeof(int4)));
+    if (!it.empty())
+        MGX_TRY(cuda_check(cudaMemcpy(L->items[s].ptr, it.data(), it.size() * sizeof(int4),
+                               cudaMemcpyHostToDevice),
+            "items upload"));
+    return MGX_OK;
+}
+
+StepParams params(mgx_local* L, int s, const float* psi, const float* phi, const float* V,
+    double gamma, float* u, float* w)
+{
+    StepParams P;
+    P.psi   = psi;
+    P.phi   = phi;
+    P.V     = V;
+    P.u     = u;
+    P.w     = w;
+    P.box   = (const int*)L->box.ptr;
+    P.off   = (const size_t*)L->off.ptr;
+    P.mvals = (const float*)L->masks->values[0].ptr;
+    P.moff  = (const size_t*)L->masks->offset[0].ptr;
+    P.cvals = (const float*)L->corr->values[0].ptr;
+    P.coff  = (const size_t*)L->corr->offset[0].ptr;
+    P.items   = (const int4*)L->items[s].ptr;
+    P.nitems  = L->nitems[s];
+    P.counter = (int*)L->counter.ptr;
+    const mgx_grid& g = L->ctx->grid;
+    for (int i = 0; i < 3; i++)
+        P.n[i] = g.n[i];
+    const Level L0        = make_level(g, 0);
+    const StencilCoeffs c = stencil_coeffs(0, L0.h);
+    P.c0    = (float)c.c0;
+    P.cx    = (float)c.cx[0];
+    P.cy    = (float)c.cy[0];
+    P.cz    = (float)c.cz[0];
+    P.cxy   = (float)c.cxy;
+    P.cyz   = (float)c.cyz;
+    P.cxz   = (float)c.cxz;
+    P.gamma = (float)gamma;
+    P.jf    = (float)jacobi_factor(0, L0.h);
+    return P;
+}
+
+/* persistent grid of shape s: ctas_per_sm per SM, at most what is resident */
+int grid_ctas(mgx_local* L, int s, int ctas_per_sm)
+{
+    return L->ctx->sm_count * std::max(1, std::min(ctas_per_sm, max_ctas_per_sm(s)));
+}
+
+int enqueue(mgx_local* L, int s, int ctas, const StepParams& P, cudaStream_t st)
+{
+    MGX_TRY(cuda_check(cudaMemsetAsync(L->counter.ptr, 0, sizeof(int), st), "counter reset"));
+    switch (s)
+    {
+        case 0: return launch_shape<8, 32>(P, ctas, st);
+        case 1: return launch_shape<16, 32>(P, ctas, st);
+        default: return launch_shape<16, 16>(P, ctas, st);
+    }
+}
+
+int step(mgx_local* L, const float* psi, const float* phi, const float* V, double gamma, float* u,
+    float* w, cudaStream_t st)
+{
+    const int s         = L->shape;
+    const StepParams P  = params(L, s, psi, phi, V, gamma, u, w);
+    const int ctas      = grid_ctas(L, s, L->ctas_per_sm);
+    if (!L->use_graph) return enqueue(L, s, ctas, P, st);
+    const void* key[5] = { psi, phi, V, u, w };
+    bool same = L->exec && L->key_gamma == gamma && L->key_shape == s && L->key_ctas == L->ctas_per_sm;
+    for (int i = 0; i < 5 && same; i++)
+        same = (key[i] == L->key[i]);
+    if (!same)
+    {
+        if (L->exec) cudaGraphExecDestroy(L->exec);
+        if (L->graph) cudaGraphDestroy(L->graph);
+        L->exec  = nullptr;
+        L->graph = nullptr;
+        // capture on a private stream (the caller's may be the legacy stream)
+        cudaStream_t cs = nullptr;
+        MGX_TRY(cuda_check(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking), "capture stream"));
+        // (the kernel's attributes were set by grid_ctas, before the capture)
+        int rc = cuda_check(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal), "begin capture");
+        if (rc == MGX_OK)
+        {
+            const int e1 = enqueue(L, s, ctas, P, cs);
+            cudaGraph_t g  = nullptr;
+            const int e2   = cuda_check(cudaStreamEndCapture(cs, &g), "end capture");
+            rc             = e1 != MGX_OK ? e1 : e2;
+            if (rc == MGX_OK)
+            {
+                rc = cuda_check(cudaGraphInstantiate(&L->exec, g, 0), "graph instantiate");
+                L->graph = g;
+            }
+            else if (g)
+                cudaGraphDestroy(g);
+        }
+        cudaStreamDestroy(cs);
+        MGX_TRY(rc);
+        for (int i = 0; i < 5; i++)
+            L->key[i] = key[i];
+        L->key_gamma = gamma;
+        L->key_shape = s;
+        L->key_ctas  = L->ctas_per_sm;
+    }
+    count_launch();
+    return cuda_check(cudaGraphLaunch(L->exec, st), "graph launch");
+}
+
+} // namespace loc
+} // namespace mgx
+
+using namespace mgx;
+
+extern "C" {
+
+int mgx_local_create(mgx_ctx* ctx, const mgx_masks* masks, const mgx_masks* corr,
+    mgx_local** out)
+{
+    if (!ctx || !masks || !corr || !out) return fail(MGX_BAD_ARG, "NULL argument");
+    if (masks->dtype != MGX_F32 || corr->dtype != MGX_F32)
+        return fail(MGX_BAD_ARG, "localized orbitals need FP32 masks");
+    if (masks->nfunc != corr->nfunc) return fail(MGX_BAD_ARG, "mask sets of different sizes");
+    if (masks->kind != 0 || corr->kind != 1)
+        return fail(MGX_BAD_ARG, "orbital masks must clamp (GridMaskMax), correction masks multiply");
+    const mgx_grid& g = ctx->grid;
+    for (int i = 0; i < 3; i++)
+        if (masks->n[i] != g.n[i] || corr->n[i] != g.n[i])
+            return fail(MGX_BAD_ARG, "masks of another grid");
+    auto L   = std::make_unique<mgx_local>();
+    L->ctx   = ctx;
+    L->nfunc = masks->nfunc;
+    L->masks = masks;
+    L->corr  = corr;
+    L->h_box.resize(6 * (size_t)L->nfunc);
+    L->h_off.resize(L->nfunc + 1);
+    size_t tot = 0;
+    for (int f = 0; f < L->nfunc; f++)
+    {
+        if (masks->h_state[0][f] != 2 || corr->h_state[0][f] != 2)
+            return fail(MGX_UNSUPPORTED, "orbital %d: mask without a box of values", f);
+        for (int k = 0; k < 6; k++)
+        {
+            const int v = masks->h_box[0][6 * f + k];
+            if (corr->h_box[0][6 * f + k] != v)
+                return fail(MGX_UNSUPPORTED, "orbital %d: correction box differs from the mask box", f);
+            L->h_box[6 * f + k] = v;
+        }
+        for (int k = 0; k < 3; k++)
+            if (L->h_box[6 * f + 3 + k] + 2 * loc::HALO > g.n[k])
+                return fail(MGX_UNSUPPORTED, "orbital %d: box wider than the grid less the halo", f);
+        L->h_off[f] = tot;
+        tot += (size_t)L->h_box[6 * f + 3] * L->h_box[6 * f + 4] * L->h_box[6 * f + 5];
+    }
+    L->h_off[L->nfunc] = tot;
+    L->total           = tot;
+    MGX_TRY(L->box.ensure(std::max<size_t>(L->h_box.size(), 1) * sizeof(int)));
+    MGX_TRY(L->off.ensure(L->h_off.size() * sizeof(size_t)));
+    MGX_TRY(L->counter.ensure(256));
+    if (L->nfunc)
+    {
+        MGX_TRY(cuda_check(cudaMemcpy(L->box.ptr, L->h_box.data(), L->h_box.size() * sizeof(int),
+                               cudaMemcpyHostToDevice),
+            "box upload"));
+        MGX_TRY(cuda_check(cudaMemcpy(L->off.ptr, L->h_off.data(), L->h_off.size() * sizeof(size_t),
+                               cudaMemcpyHostToDevice),
+            "offset upload"));
+    }
+    for (int s = 0; s < loc::NSHAPE; s++)
+        MGX_TRY(loc::build_items(L.get(), s));
+    *out = L.release();
+    return MGX_OK;
+}
+
+int mgx_local_destroy(mgx_local* L)
+{
+    delete L;
+    return MGX_OK;
+}
+
+int mgx_local_layout(const mgx_local* L, size_t* total, size_t* offsets, int* boxes)
+{
+    if (!L) return fail(MGX_BAD_ARG, "NULL argument");
+    if (total) *total = L->total;
+    if (offsets) std::memcpy(offsets, L->h_off.data(), L->h_off.size() * sizeof(size_t));
+    if (boxes) std::memcpy(boxes, L->h_box.data(), L->h_box.size() * sizeof(int));
+    return MGX_OK;
+}
+
+int mgx_local_gather(mgx_local* L, const float* full, size_t ld, float* packed, void* stream)
+{
+    if (!L || (L->nfunc && (!full || !packed))) return fail(MGX_BAD_ARG, "NULL argument");
+    const mgx_grid& g = L->ctx->grid;
+    const size_t np   = (size_t)g.n[0] * g.n[1] * g.n[2];
+    if (L->nfunc > 1 && ld < np) return fail(MGX_BAD_ARG, "ld %zu < %zu points", ld, np);
+    if (L->nfunc == 0) return MGX_OK;
+    loc::gather_kernel<<<dim3(64, L->nfunc), 256, 0, (cudaStream_t)stream>>>(full, ld ? ld : np,
+        packed, (const int*)L->box.ptr, (const size_t*)L->off.ptr, g.n[0], g.n[1], g.n[2]);
+    MGX_LAUNCH_CHECK("gather_kernel");
+    return MGX_OK;
+}
+
+int mgx_local_scatter(mgx_local* L, const float* packed, float* full, size_t ld, void* stream)
+{
+    if (!L || (L->nfunc && (!full || !packed))) return fail(MGX_BAD_ARG, "NULL argument");
+    const mgx_grid& g = L->ctx->grid;
+    const size_t np   = (size_t)g.n[0] * g.n[1] * g.n[2];
+    if (L->nfunc > 1 && ld < np) return fail(MGX_BAD_ARG, "ld %zu < %zu points", ld, np);
+    if (L->nfunc == 0) return MGX_OK;
+    loc::scatter_kernel<<<dim3(64, L->nfunc), 256, 0, (cudaStream_t)stream>>>(packed, full,
+        ld ? ld : np, (const int*)L->box.ptr, (const size_t*)L->off.ptr, g.n[0], g.n[1], g.n[2]);
+    MGX_LAUNCH_CHECK("scatter_kernel");
+    return MGX_OK;
+}
+
+int mgx_local_set_config(mgx_local* L, int shape, int ctas_per_sm, int use_graph)
+{
+    if (!L) return fail(MGX_BAD_ARG, "NULL argument");
+    if (shape < 0 || shape >= loc::NSHAPE) return fail(MGX_BAD_ARG, "shape %d", shape);
+    if (ctas_per_sm < 1 || ctas_per_sm > 8) return fail(MGX_BAD_ARG, "ctas_per_sm %d", ctas_per_sm);
+    L->shape       = shape;
+    L->ctas_per_sm = ctas_per_sm;
+    L->use_graph   = use_graph ? 1 : 0;
+    return MGX_OK;
+}
+
+int mgx_local_get_config(const mgx_local* L, int* shape, int* ctas_per_sm, int* use_graph)
+{
+    if (!L) return fail(MGX_BAD_ARG, "NULL argument");
+    if (shape) *shape = L->shape;
+    if (ctas_per_sm) *ctas_per_sm = L->ctas_per_sm;
+    if (use_graph) *use_graph = L->use_graph;
+    return MGX_OK;
+}
+
+int mgx_local_step(mgx_local* L, const float* psi, const float* phi, const float* V,
+    double gamma, float* u, float* w, void* stream)
+{
+    if (!L) return fail(MGX_BAD_ARG, "NULL argument");
+    if (L->total && (!psi || !phi || !V || !u || !w)) return fail(MGX_BAD_ARG, "NULL block");
+    if (u == w || u == psi || u == phi || w == psi || w == phi)
+        return fail(MGX_BAD_ARG, "outputs alias the inputs or each other");
+    if (L->total == 0) return MGX_OK;
+    return loc::step(L, psi, phi, V, gamma, u, w, (cudaStream_t)stream);
+}
+
+int mgx_local_tune(mgx_local* L, const float* psi, const float* phi, const float* V,
+    double gamma, float* u, float* w, double* ms, int* ncand, void* stream)
+{
+    if (!L) return fail(MGX_BAD_ARG, "NULL argument");
+    if (L->total == 0) return MGX_OK;
+    if (!psi || !phi || !V || !u || !w) return fail(MGX_BAD_ARG, "NULL block");
+    const cudaStream_t st = (cudaStream_t)stream;
+    cudaEvent_t e0, e1;
+    MGX_TRY(cuda_check(cudaEventCreate(&e0), "event"));
+    MGX_TRY(cuda_check(cudaEventCreate(&e1), "event"));
+    int best_s = L->shape, best_c = L->ctas_per_sm, k = 0;
+    double best = 1e300;
+    int rc = MGX_OK;
+    for (int s = 0; s < loc::NSHAPE && rc == MGX_OK; s++)
+    {
+        const int cmax = loc::max_ctas_per_sm(s);
+        for (int ci = 0; ci < 4 && rc == MGX_OK; ci++)
+        {
+            const int c = 1 << ci;
+            double t = 1e300;
+            if (c <= cmax)
+            {
+                const loc::StepParams P = loc::params(L, s, psi, phi, V, gamma, u, w);
+                const int ctas          = loc::grid_ctas(L, s, c);
+                rc = loc::enqueue(L, s, ctas, P, st); // warm-up
+                if (rc == MGX_OK) rc = cuda_check(cudaEventRecord(e0, st), "event");
+                for (int r = 0; r < 3 && rc == MGX_OK; r++)
+                    rc = loc::enqueue(L, s, ctas, P, st);
+                if (rc == MGX_OK) rc = cuda_check(cudaEventRecord(e1, st), "event");
+                if (rc == MGX_OK) rc = cuda_check(cudaEventSynchronize(e1), "event");
+                float f = 0.f;
+                if (rc == MGX_OK) rc = cuda_check(cudaEventElapsedTime(&f, e0, e1), "event");
+                t = f / 3.;
+                if (t < best)
+                {
+                    best   = t;
+                    best_s = s;
+                    best_c = c;
+                }
+            }
+            if (ms && ncand && k < *ncand) ms[k] = t < 1e299 ? t : -1.;
+            k++;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    MGX_TRY(rc);
+    if (ncand) *ncand = k;
+    L->shape       = best_s;
+    L->ctas_per_sm = best_c;
+    return MGX_OK;
+}
+
+} // extern "C"
