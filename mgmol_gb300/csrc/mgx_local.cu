@@ -104,31 +104,36 @@ __device__ __forceinline__ int wrap1(int g, int n)
     return g < 0 ? g + n : (g >= n ? g - n : g);
 }
 
-/* A CTA owns a TY x TZ column of an orbital's box and marches along x.
- * Plane regions shrink by one point per stage in y and z: stage 0 (psi and
- * phi - V psi) on (TY + 6) x (TZ + 6), stage 1 (r) on (TY + 4) x (TZ + 4),
- * stage 2 (u1) on (TY + 2) x (TZ + 2), stage 3 (u, w) on TY x TZ.  Each
- * stage keeps its last three planes in a ring; at march step t the stages
- * produce planes t - 3, t - 4, t - 5 and t - 6 (box-local x), so every
- * plane a stage reads was made at an earlier step or earlier in this one. */
-template <int TY, int TZ> struct Cols
+/* A CTA owns a TY x TZ column of an orbital's box and marches along x,
+ * PPS planes per step.  Plane regions shrink by one point per stage in y
+ * and z: stage 0 (psi and phi - V psi) on (TY + 6) x (TZ + 6), stage 1 (r)
+ * on (TY + 4) x (TZ + 4), stage 2 (u1) on (TY + 2) x (TZ + 2), stage 3
+ * (u, w) on TY x TZ.  Stage k makes planes PPS t + j - 3 - k (j < PPS,
+ * box-local x) at step t, within [k - 3, e0 - 1 + 3 - k]; a plane needs
+ * the planes p - 1 .. p + 1 of the stage before, made at this step or the
+ * one before, so each stage keeps a ring of PPS + 2 planes.  Three
+ * barriers per step. */
+template <int TY, int TZ, int PPS> struct Cols
 {
+    static constexpr int RING = PPS + 2;
     static constexpr int Y3 = TY + 6, Z3 = TZ + 6, N3 = Y3 * Z3;
     static constexpr int Y2 = TY + 4, Z2 = TZ + 4, N2 = Y2 * Z2;
     static constexpr int Y1 = TY + 2, Z1 = TZ + 2, N1 = Y1 * Z1;
     static constexpr int N0 = TY * TZ;
-    static constexpr size_t SMEM = (size_t)(3 * (2 * N3 + N2 + N1)) * sizeof(float);
+    static constexpr size_t SMEM = (size_t)(RING * (2 * N3 + N2 + N1)) * sizeof(float);
+    // ring slot of plane p >= -3
+    static __device__ __forceinline__ int slot(int p) { return (p + 3 * RING) % RING; }
 };
 
-template <int TY, int TZ>
+template <int TY, int TZ, int PPS>
 __global__ void __launch_bounds__(THREADS) local_step_kernel(StepParams P)
 {
-    using C = Cols<TY, TZ>;
+    using C = Cols<TY, TZ, PPS>;
     extern __shared__ __align__(16) float sm[];
-    float* s_psi = sm;               // 3 x N3
-    float* s_d   = s_psi + 3 * C::N3; // 3 x N3: phi - V psi
-    float* s_r   = s_d + 3 * C::N3;   // 3 x N2
-    float* s_u   = s_r + 3 * C::N2;   // 3 x N1
+    float* s_psi = sm;                      // RING x N3
+    float* s_d   = s_psi + C::RING * C::N3; // RING x N3: phi - V psi
+    float* s_r   = s_d + C::RING * C::N3;   // RING x N2
+    float* s_u   = s_r + C::RING * C::N2;   // RING x N1
     __shared__ int s_item;
     const int tid = threadIdx.x;
     for (;;)
@@ -148,13 +153,16 @@ __global__ void __launch_bounds__(THREADS) local_step_kernel(StepParams P)
         const float* phi = P.phi + P.off[f];
         const float* mo  = P.mvals + P.moff[f];
         const float* mc  = P.cvals + P.coff[f];
-        for (int t = 0; t < e0 + 6; t++)
+        for (int t = 0; PPS * t - 6 < e0; t++)
         {
-            // stage 0: plane t - 3 of psi and phi - V psi
+            // stage 0: psi and phi - V psi
+#pragma unroll
+            for (int j = 0; j < PPS; j++)
             {
-                const int p   = t - 3;
-                float* dp     = s_psi + ((p + 3) % 3) * C::N3;
-                float* dd     = s_d + ((p + 3) % 3) * C::N3;
+                const int p = PPS * t + j - 3;
+                if (p > e0 + 2) break;
+                float* dp     = s_psi + C::slot(p) * C::N3;
+                float* dd     = s_d + C::slot(p) * C::N3;
                 const bool in = (p >= 0 && p < e0);
                 const int gx  = wrap1(o0 + p, P.n[0]);
                 for (int q = tid; q < C::N3; q += THREADS)
@@ -175,17 +183,19 @@ __global__ void __launch_bounds__(THREADS) local_step_kernel(StepParams P)
                 }
             }
             __syncthreads();
-            // stage 1: plane t - 4 of r = Mc (B(phi - V psi) + Delta_M psi)
-            if (t >= 2)
+            // stage 1: r = Mc (B(phi - V psi) + Delta_M psi)
+#pragma unroll
+            for (int j = 0; j < PPS; j++)
             {
-                const int p    = t - 4;
-                const float* M = s_psi + ((p + 2) % 3) * C::N3; // plane p - 1
-                const float* X = s_psi + ((p + 3) % 3) * C::N3;
-                const float* N = s_psi + ((p + 4) % 3) * C::N3;
-                const float* dM = s_d + ((p + 2) % 3) * C::N3;
-                const float* dX = s_d + ((p + 3) % 3) * C::N3;
-                const float* dN = s_d + ((p + 4) % 3) * C::N3;
-                float* out      = s_r + ((p + 3) % 3) * C::N2;
+                const int p = PPS * t + j - 4;
+                if (p < -2 || p > e0 + 1) continue;
+                const float* M  = s_psi + C::slot(p - 1) * C::N3;
+                const float* X  = s_psi + C::slot(p) * C::N3;
+                const float* N  = s_psi + C::slot(p + 1) * C::N3;
+                const float* dM = s_d + C::slot(p - 1) * C::N3;
+                const float* dX = s_d + C::slot(p) * C::N3;
+                const float* dN = s_d + C::slot(p + 1) * C::N3;
+                float* out      = s_r + C::slot(p) * C::N2;
                 const bool in   = (p >= 0 && p < e0);
                 for (int q = tid; q < C::N2; q += THREADS)
                 {
@@ -204,14 +214,16 @@ __global__ void __launch_bounds__(THREADS) local_step_kernel(StepParams P)
                 }
             }
             __syncthreads();
-            // stage 2: plane t - 5 of the first sweep u1, from u0 = gamma r
-            if (t >= 4)
+            // stage 2: the first sweep u1, from u0 = gamma r
+#pragma unroll
+            for (int j = 0; j < PPS; j++)
             {
-                const int p    = t - 5;
-                const float* M = s_r + ((p + 2) % 3) * C::N2;
-                const float* X = s_r + ((p + 3) % 3) * C::N2;
-                const float* N = s_r + ((p + 4) % 3) * C::N2;
-                float* out     = s_u + ((p + 3) % 3) * C::N1;
+                const int p = PPS * t + j - 5;
+                if (p < -1 || p > e0) continue;
+                const float* M = s_r + C::slot(p - 1) * C::N2;
+                const float* X = s_r + C::slot(p) * C::N2;
+                const float* N = s_r + C::slot(p + 1) * C::N2;
+                float* out     = s_u + C::slot(p) * C::N1;
                 const bool in  = (p >= 0 && p < e0);
                 for (int q = tid; q < C::N1; q += THREADS)
                 {
@@ -227,14 +239,16 @@ __global__ void __launch_bounds__(THREADS) local_step_kernel(StepParams P)
                 }
             }
             __syncthreads();
-            // stage 3: plane t - 6 of the second sweep, stored inside the box
-            if (t >= 6)
+            // stage 3: the second sweep, stored inside the box
+#pragma unroll
+            for (int j = 0; j < PPS; j++)
             {
-                const int p    = t - 6;
-                const float* M = s_u + ((p + 2) % 3) * C::N1;
-                const float* X = s_u + ((p + 3) % 3) * C::N1;
-                const float* N = s_u + ((p + 4) % 3) * C::N1;
-                const float* R = s_r + ((p + 3) % 3) * C::N2;
+                const int p = PPS * t + j - 6;
+                if (p < 0 || p >= e0) continue;
+                const float* M = s_u + C::slot(p - 1) * C::N1;
+                const float* X = s_u + C::slot(p) * C::N1;
+                const float* N = s_u + C::slot(p + 1) * C::N1;
+                const float* R = s_r + C::slot(p) * C::N2;
                 for (int q = tid; q < C::N0; q += THREADS)
                 {
                     const int qy = q / TZ, qz = q - qy * TZ;
@@ -285,34 +299,36 @@ __global__ void __launch_bounds__(256) scatter_kernel(const float* __restrict__ 
     }
 }
 
-/* the column shapes (TY x TZ) the tuner chooses from */
+/* the kernel variants the tuner chooses from: column TY x TZ and planes
+ * per march step */
 struct Shape
 {
-    int ty, tz;
+    int ty, tz, pps;
 };
-constexpr int NSHAPE           = 3;
-constexpr Shape SHAPES[NSHAPE] = { { 8, 32 }, { 16, 32 }, { 16, 16 } };
+constexpr int NSHAPE           = 6;
+constexpr Shape SHAPES[NSHAPE] = { { 8, 32, 1 }, { 16, 32, 1 }, { 16, 16, 1 }, { 8, 32, 2 },
+    { 16, 32, 2 }, { 16, 16, 2 } };
 
-template <int TY, int TZ> int set_attr()
+template <int TY, int TZ, int PPS> int set_attr()
 {
     static bool done = false;
     if (!done)
     {
-        MGX_TRY(cuda_check(cudaFuncSetAttribute(local_step_kernel<TY, TZ>,
+        MGX_TRY(cuda_check(cudaFuncSetAttribute(local_step_kernel<TY, TZ, PPS>,
                                cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               (int)Cols<TY, TZ>::SMEM),
+                               (int)Cols<TY, TZ, PPS>::SMEM),
             "local smem"));
         done = true;
     }
     return MGX_OK;
 }
 
-template <int TY, int TZ> int occupancy()
+template <int TY, int TZ, int PPS> int occupancy()
 {
-    if (set_attr<TY, TZ>() != MGX_OK) return 1;
+    if (set_attr<TY, TZ, PPS>() != MGX_OK) return 1;
     int n = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, local_step_kernel<TY, TZ>, THREADS,
-            Cols<TY, TZ>::SMEM)
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, local_step_kernel<TY, TZ, PPS>,
+            THREADS, Cols<TY, TZ, PPS>::SMEM)
         != cudaSuccess)
     {
         cudaGetLastError();
@@ -321,20 +337,23 @@ template <int TY, int TZ> int occupancy()
     return std::max(n, 1);
 }
 
-/* resident CTAs per SM of shape s (also sets its shared-memory limit) */
+/* resident CTAs per SM of variant s (also sets its shared-memory limit) */
 int max_ctas_per_sm(int s)
 {
     switch (s)
     {
-        case 0: return occupancy<8, 32>();
-        case 1: return occupancy<16, 32>();
-        default: return occupancy<16, 16>();
+        case 0: return occupancy<8, 32, 1>();
+        case 1: return occupancy<16, 32, 1>();
+        case 2: return occupancy<16, 16, 1>();
+        case 3: return occupancy<8, 32, 2>();
+        case 4: return occupancy<16, 32, 2>();
+        default: return occupancy<16, 16, 2>();
     }
 }
 
-template <int TY, int TZ> int launch_shape(const StepParams& P, int ctas, cudaStream_t s)
+template <int TY, int TZ, int PPS> int launch_shape(const StepParams& P, int ctas, cudaStream_t s)
 {
-    local_step_kernel<TY, TZ><<<ctas, THREADS, Cols<TY, TZ>::SMEM, s>>>(P);
+    local_step_kernel<TY, TZ, PPS><<<ctas, THREADS, Cols<TY, TZ, PPS>::SMEM, s>>>(P);
     MGX_LAUNCH_CHECK("local_step_kernel");
     return MGX_OK;
 }
@@ -351,7 +370,7 @@ struct mgx_local
     std::vector<size_t> h_off;   // nfunc + 1
     mgx::DeviceBuffer box, off, counter;
     mgx::DeviceBuffer items[mgx::loc::NSHAPE];
-    int nitems[mgx::loc::NSHAPE] = { 0, 0, 0 };
+    int nitems[mgx::loc::NSHAPE] = {};
     const mgx_masks* masks = nullptr;
     const mgx_masks* corr  = nullptr;
     // chosen configuration
@@ -445,9 +464,12 @@ int enqueue(mgx_local* L, int s, int ctas, const StepParams& P, cudaStream_t st)
     MGX_TRY(cuda_check(cudaMemsetAsync(L->counter.ptr, 0, sizeof(int), st), "counter reset"));
     switch (s)
     {
-        case 0: return launch_shape<8, 32>(P, ctas, st);
-        case 1: return launch_shape<16, 32>(P, ctas, st);
-        default: return launch_shape<16, 16>(P, ctas, st);
+        case 0: return launch_shape<8, 32, 1>(P, ctas, st);
+        case 1: return launch_shape<16, 32, 1>(P, ctas, st);
+        case 2: return launch_shape<16, 16, 1>(P, ctas, st);
+        case 3: return launch_shape<8, 32, 2>(P, ctas, st);
+        case 4: return launch_shape<16, 32, 2>(P, ctas, st);
+        default: return launch_shape<16, 16, 2>(P, ctas, st);
     }
 }
 

@@ -22,6 +22,8 @@ from . import capi, synth
 
 # algorithmic bytes per box point: psi, phi, V, two mask values read; u, w written
 BYTES_PER_POINT = 7 * 4
+# the kernel variants of mgx_local_tune: (column TY x TZ, planes per march step)
+VARIANTS = [("8x32", 1), ("16x32", 1), ("16x16", 1), ("8x32", 2), ("16x32", 2), ("16x16", 2)]
 
 
 def build(n, h, nfunc, seed, rlo=4.0, rhi=8.0, chunk=128):
@@ -72,11 +74,17 @@ def main(argv=None):
     ap.add_argument("--nfunc", type=int, default=1536)
     ap.add_argument("--seed", type=int, default=1003)
     ap.add_argument("--reps", type=int, default=20)
+    ap.add_argument("--config", type=int, nargs=2, default=None, metavar=("VARIANT", "CTAS"),
+                    help="skip the tuner: kernel variant and CTAs per SM")
     a = ap.parse_args(argv)
     n = tuple(a.grid)
     ctx, loc, keep, psi, phi, V, gamma = build(n, a.h, a.nfunc, a.seed)
     u, w = loc.empty(), loc.empty()
-    ms, cfg = loc.tune(psi, phi, V, gamma, u, w)
+    if a.config:
+        loc.set_config(a.config[0], a.config[1], True)
+        ms, cfg = np.zeros(0), loc.config()
+    else:
+        ms, cfg = loc.tune(psi, phi, V, gamma, u, w)
     loc.step(psi, phi, V, gamma, u=u, w=w)
     torch.cuda.synchronize()
     s = torch.cuda.current_stream()
@@ -93,7 +101,8 @@ def main(argv=None):
            "box_points_total": int(loc.total), "box_points_mean": float(vols.mean()),
            "box_points_min": int(vols.min()), "box_points_max": int(vols.max()),
            "ms_per_step": t, "algorithmic_GBps": gbs, "bytes_per_point": BYTES_PER_POINT,
-           "config": {"column": ["8x32", "16x32", "16x16"][cfg[0]], "ctas_per_sm": cfg[1],
+           "config": {"column": VARIANTS[cfg[0]][0], "planes_per_step": VARIANTS[cfg[0]][1],
+                      "ctas_per_sm": cfg[1],
                       "graph": bool(cfg[2])},
            "tune_ms": [round(float(x), 4) for x in ms],
            "whole_grid_points": a.nfunc * ctx.npts}

@@ -80,7 +80,7 @@ def test_every_configuration_gives_the_same_bits():
     f32 = lambda a: torch.from_numpy(np.ascontiguousarray(a, dtype=np.float32)).cuda()
     psi_p, phi_p, Vd = loc.gather(f32(psi)), loc.gather(f32(phi)), f32(V)
     ref = None
-    for shape in range(3):
+    for shape in range(6):
         for ctas in (1, 4):
             for graph in (False, True):
                 loc.set_config(shape, ctas, graph)
@@ -107,7 +107,7 @@ def test_tuner_picks_a_resident_configuration():
     psi_p, phi_p, Vd = loc.gather(f32(psi)), loc.gather(f32(phi)), f32(V)
     u, w = loc.empty(), loc.empty()
     ms, (shape, ctas, graph) = loc.tune(psi_p, phi_p, Vd, 0.01, u, w)
-    assert ms.size == 12 and np.all(ms[ms >= 0] > 0)
+    assert ms.size == 24 and np.all(ms[ms >= 0] > 0)
     assert ms[4 * shape + int(np.log2(ctas))] == ms[ms >= 0].min()
     assert graph == 1
 
