@@ -236,13 +236,42 @@ def run_gpu(args, cfg):
         free, _ = torch.cuda.mem_get_info()
         block = N * ctx.npts * (8 if mode == "plain" else 4)
         lean = 0 if 3.6 * block < free else 128
+    net = None
+    if args.precond == "learned":
+        # the learned preconditioner, trained during the warm-up sweeps on
+        # the (residual, V-cycle correction) pairs they make
+        from mgmol_gb300 import learned as lrn
+        net = capi.UNet(ctx)
+        net.set_params(lrn.init_params(cfg["seed"]))
     sw = OrbitalSweep(ctx, V, N, mode=mode, gemm=gemm, precond_chunk=args.chunk,
-                      chunk_funcs=lean, use_matb=args.theta == "b")
+                      chunk_funcs=lean, use_matb=args.theta == "b", learned=net)
     torch.cuda.synchronize()
 
+    train = {"pairs": 0, "steps": 0, "loss_first": None, "loss_last": None}
+    if net is not None:
+        sw.use_learned = False
+        gen = torch.Generator(device="cpu")
+        gen.manual_seed(cfg["seed"])
+
+        def on_pair(res, corr):
+            rows = torch.randperm(N, generator=gen)[: args.train_pairs].tolist()
+            if not rows:
+                return
+            for b0 in range(0, len(rows), 4):
+                idx = rows[b0:b0 + 4]
+                loss = net.train_step(res[idx].contiguous(), corr[idx].contiguous(), 1e-3)
+                train["steps"] += 1
+                if train["loss_first"] is None:
+                    train["loss_first"] = float(loss)
+            train["loss_last"] = float(loss)
+            train["pairs"] += len(rows)
+        sw.on_pair = on_pair
     for _ in range(args.warmup):
         sw.run(psi)
     torch.cuda.synchronize()
+    if net is not None:
+        sw.on_pair = None
+        sw.use_learned = True
 
     clocks = ClockSampler(local)
     clocks.start()
@@ -263,6 +292,7 @@ def run_gpu(args, cfg):
     if world > 1:
         dist.barrier()
     launches = capi.launches() - l0
+    fallbacks_timed = sw.fallbacks
     capi.timing_enable(False)
     tk_ms, tk_n = capi.timing_read(capi.TIMING_TC_SPLITK)
     ts_ms, ts_n = capi.timing_read(capi.TIMING_TC_STORE)
@@ -370,7 +400,9 @@ def run_gpu(args, cfg):
         "data": "synthetic (seeded Gaussian orbitals and wells generated on the device)",
         "config": {"workload": cfg["workload"], "grid": list(n), "h": cfg["h"], "orbitals": N,
                    "mode": mode, "gemm": args.gemm if mode == "mixed" else "fp64",
-                   "lap_type": "mehrstellen", "precond": "V-cycle 2 coarse levels",
+                   "lap_type": "mehrstellen",
+                   "precond": "V-cycle 2 coarse levels" if net is None else
+                   "learned U-Net, warm-started V-cycle, per-function V-cycle fallback",
                    "theta": "B^-1 H (ProjectedMatricesMehrstellen)" if sw.use_matb
                    else "S^-1 H (ProjectedMatrices)",
                    "schedule": f"column chunks of {sw.chunk}" if sw.chunk else "full blocks",
@@ -379,6 +411,9 @@ def run_gpu(args, cfg):
         "roofline": roof, "tensor_kernels": kernels, "gpu_launches": launches,
         "clocks": clocks.summary(),
     }
+    if net is not None:
+        line["learned"] = {"train": train, "fallbacks_per_sweep": fallbacks_timed / args.steps,
+                           "functions": N}
     if e2e:
         line["e2e"] = e2e
     if not args.no_cpu:
@@ -406,6 +441,11 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=32,
                     help="orbitals of the timed CPU sample of the linear phases")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--precond", default="vcycle", choices=["vcycle", "learned"],
+                    help="learned: the U-Net preconditioner with V-cycle fallback, trained "
+                         "during the warm-up sweeps")
+    ap.add_argument("--train-pairs", type=int, default=256,
+                    help="pairs per warm-up sweep the learned preconditioner trains on")
     ap.add_argument("--no-e2e", dest="e2e", action="store_false")
     args = ap.parse_args()
     cfg = CONFIGS[args.config]

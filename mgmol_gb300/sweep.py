@@ -44,6 +44,7 @@ Two precision modes:
            and Psi Theta in the requested GEMM mode, FP32 V-cycle; FP64
            Cholesky / inverse / trace / theta in both.
 """
+import numpy as np
 import torch
 
 from . import capi
@@ -83,7 +84,8 @@ class OrbitalSweep:
     def __init__(self, ctx, V, nfunc, mode="mixed", gemm=None, lap_type=capi.LAP_MEHR4,
                  maxlevels=2, gamma=None, precond_chunk=0, precond_factor=1.0,
                  chunk_funcs=0, fuse_update=True, use_matb=True, anderson_m=0,
-                 anderson_beta=1.0, device="cuda"):
+                 anderson_beta=1.0, learned=None, learned_mode=capi.LEARNED_WARM,
+                 device="cuda"):
         self.ctx = ctx
         self.mode = mode
         self.lap_type = lap_type
@@ -117,7 +119,18 @@ class OrbitalSweep:
         # (full-block schedule without Anderson mixing only; the chunked one
         # defers the update)
         self.anderson_m = int(anderson_m)
-        self.fuse_update = bool(fuse_update) and not self.chunk and self.anderson_m == 0
+        # the learned preconditioner (a capi.UNet) in place of the V-cycle,
+        # the V-cycle as per-function fallback (mgx_precond_learned); off
+        # while use_learned is False, when on_pair(res, corr), if set, sees
+        # every residual block and its V-cycle correction (training)
+        self.learned = learned
+        self.learned_mode = learned_mode
+        self.use_learned = learned is not None
+        self.on_pair = None
+        self.tau = np.zeros(nfunc)
+        self.fallbacks = 0
+        self.fuse_update = (bool(fuse_update) and not self.chunk and self.anderson_m == 0
+                            and learned is None)
         self.anderson_beta = float(anderson_beta)
         self.mixer = None
         # the S side of the dense algebra (Cholesky and inverse of S, HB and
@@ -209,9 +222,20 @@ class OrbitalSweep:
                                    self.gamma, chunk=self.precond_chunk, work=self.corr,
                                    psi_scale=self.dscale)
                 self._mark(timed, "update")
+            elif self.use_learned:
+                _, _, nfb = capi.precond_learned(ctx, self.learned, self.hpsi, self.lap_type,
+                                                 self.maxlevels, self.gamma, self.tau,
+                                                 mode=self.learned_mode,
+                                                 chunk=self.precond_chunk, out=self.corr)
+                self.fallbacks += nfb
+                self._mark(timed, "update")
+                if update:
+                    self._update(psi, self.corr, Sinv, accelerate)
             else:
                 ctx.precond_mg(self.hpsi, self.lap_type, self.maxlevels, self.gamma,
                                chunk=self.precond_chunk, out=self.corr)
+                if self.on_pair is not None:
+                    self.on_pair(self.hpsi, self.corr)
                 self._mark(timed, "update")
                 if update:
                     self._update(psi, self.corr, Sinv, accelerate)
