@@ -649,7 +649,7 @@ int mgx_local_step(mgx_local* loc, const float* psi, const float* phi, const flo
     double gamma, float* u, float* w, void* stream);
 /* times every kernel variant (column TY x TZ and planes per march step;
  * 0: 8x32, 1: 16x32, 2: 16x16 with one plane, 3..5 the same with two) with
- * 1, 2, 4 and 8 resident CTAs per SM on these arguments and keeps the
+ * 2, 4, 6 and 8 resident CTAs per SM on these arguments and keeps the
  * fastest; ms
  * (optional, *ncand entries) receives each candidate's time (-1: not
  * resident), *ncand the number of candidates */

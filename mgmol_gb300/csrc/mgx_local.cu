@@ -98,6 +98,59 @@ __device__ __forceinline__ float rhs_b(const float* M, const float* C, const flo
     return 0.5f * C[i] + (1.f / 12.f) * s;
 }
 
+/* values at z - 1, z, z + 1, z + 2 of a plane column, i the (odd) index of
+ * z: two 8-byte loads */
+struct Col4
+{
+    float a, b, c, d;
+};
+__device__ __forceinline__ Col4 col4(const float* A, int i)
+{
+    const float2 lo = *reinterpret_cast<const float2*>(A + i - 1);
+    const float2 hi = *reinterpret_cast<const float2*>(A + i + 1);
+    return { lo.x, lo.y, hi.x, hi.y };
+}
+
+/* lap_m at the z pair (i, i + 1), i odd; the same operation order as lap_m */
+__device__ __forceinline__ void lap_m2(const float* M, const float* C, const float* Pn, int i,
+    int sy, const StepParams& P, float& o0, float& o1)
+{
+    const Col4 c = col4(C, i), m = col4(M, i), p = col4(Pn, i);
+    const Col4 ym = col4(C, i - sy), yp = col4(C, i + sy);
+    const Col4 mym = col4(M, i - sy), myp = col4(M, i + sy);
+    const Col4 pym = col4(Pn, i - sy), pyp = col4(Pn, i + sy);
+    {
+        const float faces = P.cx * (m.b + p.b) + P.cy * (ym.b + yp.b) + P.cz * (c.a + c.c);
+        const float exy   = mym.b + myp.b + pym.b + pyp.b;
+        const float eyz   = ym.a + ym.c + yp.a + yp.c;
+        const float exz   = m.a + m.c + p.a + p.c;
+        o0 = P.c0 * c.b + faces + P.cxy * exy + P.cyz * eyz + P.cxz * exz;
+    }
+    {
+        const float faces = P.cx * (m.c + p.c) + P.cy * (ym.c + yp.c) + P.cz * (c.b + c.d);
+        const float exy   = mym.c + myp.c + pym.c + pyp.c;
+        const float eyz   = ym.b + ym.d + yp.b + yp.d;
+        const float exz   = m.b + m.d + p.b + p.d;
+        o1 = P.c0 * c.c + faces + P.cxy * exy + P.cyz * eyz + P.cxz * exz;
+    }
+}
+
+/* rhs_b at the z pair (i, i + 1), i odd; the same operation order */
+__device__ __forceinline__ void rhs_b2(const float* M, const float* C, const float* Pn, int i,
+    int sy, float& o0, float& o1)
+{
+    const Col4 c = col4(C, i);
+    const float2 m  = *reinterpret_cast<const float2*>(M + i - 1);
+    const float2 m2 = *reinterpret_cast<const float2*>(M + i + 1);
+    const float2 p  = *reinterpret_cast<const float2*>(Pn + i - 1);
+    const float2 p2 = *reinterpret_cast<const float2*>(Pn + i + 1);
+    const Col4 ym = col4(C, i - sy), yp = col4(C, i + sy);
+    const float s0 = (m.y + p.y) + (ym.b + yp.b) + (c.a + c.c);
+    const float s1 = (m2.x + p2.x) + (ym.c + yp.c) + (c.b + c.d);
+    o0 = 0.5f * c.b + (1.f / 12.f) * s0;
+    o1 = 0.5f * c.c + (1.f / 12.f) * s1;
+}
+
 /* one periodic coordinate of a box point: b in [-3, e + 3) with e + 6 <= n */
 __device__ __forceinline__ int wrap1(int g, int n)
 {
@@ -183,7 +236,7 @@ __global__ void __launch_bounds__(THREADS) local_step_kernel(StepParams P)
                 }
             }
             __syncthreads();
-            // stage 1: r = Mc (B(phi - V psi) + Delta_M psi)
+            // stage 1: r = Mc (B(phi - V psi) + Delta_M psi), z pairs
 #pragma unroll
             for (int j = 0; j < PPS; j++)
             {
@@ -197,24 +250,32 @@ __global__ void __launch_bounds__(THREADS) local_step_kernel(StepParams P)
                 const float* dN = s_d + C::slot(p + 1) * C::N3;
                 float* out      = s_r + C::slot(p) * C::N2;
                 const bool in   = (p >= 0 && p < e0);
-                for (int q = tid; q < C::N2; q += THREADS)
+                for (int q = tid; q < C::N2 / 2; q += THREADS)
                 {
-                    const int qy = q / C::Z2, qz = q - qy * C::Z2;
+                    const int qy = q / (C::Z2 / 2), qz = 2 * (q - qy * (C::Z2 / 2));
                     const int by = y0 + qy - 2, bz = z0 + qz - 2;
-                    float m      = 0.f;
-                    if (in && by >= 0 && by < e1 && bz >= 0 && bz < e2)
-                        m = mc[(size_t)p * ex + (size_t)by * e2 + bz];
-                    float r = 0.f;
-                    if (m != 0.f)
+                    float m0 = 0.f, m1 = 0.f;
+                    if (in && by >= 0 && by < e1)
+                    {
+                        const float* mrow = mc + (size_t)p * ex + (size_t)by * e2;
+                        if (bz >= 0 && bz < e2) m0 = mrow[bz];
+                        if (bz + 1 >= 0 && bz + 1 < e2) m1 = mrow[bz + 1];
+                    }
+                    float r0 = 0.f, r1 = 0.f;
+                    if (m0 != 0.f || m1 != 0.f)
                     {
                         const int i = (qy + 1) * C::Z3 + qz + 1;
-                        r = m * (rhs_b(dM, dX, dN, i, C::Z3) - lap_m(M, X, N, i, C::Z3, P));
+                        float b0, b1, l0, l1;
+                        rhs_b2(dM, dX, dN, i, C::Z3, b0, b1);
+                        lap_m2(M, X, N, i, C::Z3, P, l0, l1);
+                        r0 = m0 * (b0 - l0);
+                        r1 = m1 * (b1 - l1);
                     }
-                    out[q] = r;
+                    *reinterpret_cast<float2*>(out + qy * C::Z2 + qz) = make_float2(r0, r1);
                 }
             }
             __syncthreads();
-            // stage 2: the first sweep u1, from u0 = gamma r
+            // stage 2: the first sweep u1, from u0 = gamma r, z pairs
 #pragma unroll
             for (int j = 0; j < PPS; j++)
             {
@@ -225,21 +286,30 @@ __global__ void __launch_bounds__(THREADS) local_step_kernel(StepParams P)
                 const float* N = s_r + C::slot(p + 1) * C::N2;
                 float* out     = s_u + C::slot(p) * C::N1;
                 const bool in  = (p >= 0 && p < e0);
-                for (int q = tid; q < C::N1; q += THREADS)
+                for (int q = tid; q < C::N1 / 2; q += THREADS)
                 {
-                    const int qy = q / C::Z1, qz = q - qy * C::Z1;
+                    const int qy = q / (C::Z1 / 2), qz = 2 * (q - qy * (C::Z1 / 2));
                     const int by = y0 + qy - 1, bz = z0 + qz - 1;
-                    float m      = 0.f;
-                    if (in && by >= 0 && by < e1 && bz >= 0 && bz < e2)
-                        m = mo[(size_t)p * ex + (size_t)by * e2 + bz];
-                    const int i    = (qy + 1) * C::Z2 + qz + 1;
-                    const float r  = X[i];
-                    const float w0 = P.gamma * lap_m(M, X, N, i, C::Z2, P) - r;
-                    out[q]         = clampm(P.gamma * r - P.jf * w0, m);
+                    float m0 = 0.f, m1 = 0.f;
+                    if (in && by >= 0 && by < e1)
+                    {
+                        const float* mrow = mo + (size_t)p * ex + (size_t)by * e2;
+                        if (bz >= 0 && bz < e2) m0 = mrow[bz];
+                        if (bz + 1 >= 0 && bz + 1 < e2) m1 = mrow[bz + 1];
+                    }
+                    const int i = (qy + 1) * C::Z2 + qz + 1;
+                    float l0, l1;
+                    lap_m2(M, X, N, i, C::Z2, P, l0, l1);
+                    const float2 r  = make_float2(X[i], X[i + 1]);
+                    const float w0  = P.gamma * l0 - r.x;
+                    const float w1  = P.gamma * l1 - r.y;
+                    *reinterpret_cast<float2*>(out + qy * C::Z1 + qz)
+                        = make_float2(clampm(P.gamma * r.x - P.jf * w0, m0),
+                            clampm(P.gamma * r.y - P.jf * w1, m1));
                 }
             }
             __syncthreads();
-            // stage 3: the second sweep, stored inside the box
+            // stage 3: the second sweep, stored inside the box, z pairs
 #pragma unroll
             for (int j = 0; j < PPS; j++)
             {
@@ -249,17 +319,27 @@ __global__ void __launch_bounds__(THREADS) local_step_kernel(StepParams P)
                 const float* X = s_u + C::slot(p) * C::N1;
                 const float* N = s_u + C::slot(p + 1) * C::N1;
                 const float* R = s_r + C::slot(p) * C::N2;
-                for (int q = tid; q < C::N0; q += THREADS)
+                for (int q = tid; q < C::N0 / 2; q += THREADS)
                 {
-                    const int qy = q / TZ, qz = q - qy * TZ;
+                    const int qy = q / (TZ / 2), qz = 2 * (q - qy * (TZ / 2));
                     const int by = y0 + qy, bz = z0 + qz;
                     if (by >= e1 || bz >= e2) continue;
                     const size_t li = (size_t)p * ex + (size_t)by * e2 + bz;
-                    const float m   = mo[li];
                     const int i     = (qy + 1) * C::Z1 + qz + 1;
-                    const float w1  = lap_m(M, X, N, i, C::Z1, P) - R[(qy + 2) * C::Z2 + qz + 2];
-                    P.u[P.off[f] + li] = clampm(X[i] - P.jf * w1, m);
-                    P.w[P.off[f] + li] = clampm(w1, m);
+                    float l0, l1;
+                    lap_m2(M, X, N, i, C::Z1, P, l0, l1);
+                    const int ir    = (qy + 2) * C::Z2 + qz + 2;
+                    const float w0  = l0 - R[ir];
+                    const float m0  = mo[li];
+                    P.u[P.off[f] + li] = clampm(X[i] - P.jf * w0, m0);
+                    P.w[P.off[f] + li] = clampm(w0, m0);
+                    if (bz + 1 < e2)
+                    {
+                        const float w1 = l1 - R[ir + 1];
+                        const float m1 = mo[li + 1];
+                        P.u[P.off[f] + li + 1] = clampm(X[i + 1] - P.jf * w1, m1);
+                        P.w[P.off[f] + li + 1] = clampm(w1, m1);
+                    }
                 }
             }
         }
@@ -676,7 +756,7 @@ int mgx_local_tune(mgx_local* L, const float* psi, const float* phi, const float
         const int cmax = loc::max_ctas_per_sm(s);
         for (int ci = 0; ci < 4 && rc == MGX_OK; ci++)
         {
-            const int c = 1 << ci;
+            const int c = 2 * (ci + 1); // 2, 4, 6, 8 resident CTAs per SM
             double t = 1e300;
             if (c <= cmax)
             {
