@@ -621,7 +621,8 @@ int mgx_precond_learned(mgx_ctx* ctx, mgx_unet* net, const mgx_precond_params* p
  * corr: the correction masks (profile one, GridMaskMult) of the same
  * centres and radii, so the same boxes.  Each box extent must leave room for
  * a halo of 3 points inside the grid.  Both mask sets must outlive the
- * handle. */
+ * handle, and the boxes are read once: after mgx_masks_update moves the
+ * centres, create the handle again. */
 typedef struct mgx_local mgx_local;
 
 int mgx_local_create(mgx_ctx* ctx, const mgx_masks* masks, const mgx_masks* corr,

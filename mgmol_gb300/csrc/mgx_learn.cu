@@ -560,6 +560,8 @@ struct mgx_unet
     mgx_ctx* ctx = nullptr;
     mgx::Level lev[3];
     mgx::DeviceBuffer master, adam_m, adam_v, grad, wbf, wbft, act, red, scal, work;
+    // the gathered residuals and V-cycle corrections of the fallback
+    mgx::DeviceBuffer fallback;
     int step = 0;
 };
 
@@ -962,10 +964,10 @@ int mgx_precond_learned(mgx_ctx* ctx, mgx_unet* net, const mgx_precond_params* p
         cudaMemGetInfo(&fr, &tot);
         const int m = (int)run.size();
         int chunk   = (int)std::max<size_t>(1, std::min<size_t>(m,
-                                             (size_t)(0.2 * (double)fr) / (2 * n0 * sizeof(float))));
-        DeviceBuffer wb;
-        MGX_TRY(wb.ensure((size_t)2 * chunk * n0 * sizeof(float) + 256));
-        float* wres = (float*)wb.ptr;
+                                             (size_t)(0.2 * (double)(fr + net->fallback.bytes))
+                                                 / (2 * n0 * sizeof(float))));
+        MGX_TRY(net->fallback.ensure((size_t)2 * chunk * n0 * sizeof(float) + 256));
+        float* wres = (float*)net->fallback.ptr;
         float* wout = wres + (size_t)chunk * n0;
         std::vector<double> rv(chunk);
         for (int k0 = 0; k0 < m; k0 += chunk)
