@@ -1263,6 +1263,21 @@ bool persist_on()
     return v == 1;
 }
 
+/* the split-K products (S, H, B) use the persistent kernel only when
+ * MGX_TC_PERSIST_SPLITK=1: their FP64-atomic epilogues gain less from the
+ * overlap than the store epilogue of Psi Theta, and one CTA per (tile,
+ * K range) measured faster at the benchmark shape */
+bool persist_splitk_on()
+{
+    static int v = -1;
+    if (v < 0)
+    {
+        const char* e = getenv("MGX_TC_PERSIST_SPLITK");
+        v             = (e && atoi(e) == 1 && persist_on()) ? 1 : 0;
+    }
+    return v == 1;
+}
+
 int bf16_swizzle()
 {
     static int sw = 0;
@@ -1427,7 +1442,7 @@ int run(mgx_ctx* ctx, int mode, const Operand& a, const Operand& b, int nrows, i
     int col0 = 0)
 {
     using namespace tc;
-    const int sms = persist_on() ? ctx->sm_count : 0;
+    const int sms = persist_splitk_on() ? ctx->sm_count : 0;
     const int nti = (nrows + BM - 1) / BM, ntj = (ncols + BN - 1) / BN;
     std::vector<int2> tiles;
     for (int j = 0; j < ntj; j++)
