@@ -136,7 +136,10 @@ class OrbitalSweep:
         # the S side of the dense algebra (Cholesky and inverse of S, HB and
         # the energy) runs on a second stream with its own context, next to
         # the critical path theta = B^-1 H -> residual -> V-cycle
-        self.side = torch.cuda.Stream(device=device) if self.use_matb else None
+        # (high priority: its blocks are scheduled as soon as SMs free up
+        # beside the residual and the V-cycle, instead of after them)
+        self.side = torch.cuda.Stream(device=device, priority=-1) if self.use_matb else None
+        self.side_after_theta = True
         self.sctx = capi.Context(ctx.n, ctx.ll) if self.use_matb else None
         self.info = torch.zeros(2, dtype=torch.int32, device=device)
         self.Sinv = None
@@ -199,7 +202,12 @@ class OrbitalSweep:
             theta_done = torch.cuda.Event()
             theta_done.record(main)
             with torch.cuda.stream(self.side):
-                # computeGramAndInvS, updateHB and getEigSum beside it
+                # computeGramAndInvS, updateHB and getEigSum beside the
+                # residual and the V-cycle; started after theta, so that the
+                # FP64 work of the critical path does not share the FP64
+                # units with it (side_after_theta False: beside theta too)
+                if self.side_after_theta:
+                    self.side.wait_event(theta_done)
                 L = self.sctx.cholesky(self.S, info=self.info[1:2])
                 self.Sinv = self.sctx.inverse_from_cholesky(L).contiguous()
                 self.side.wait_event(theta_done)
