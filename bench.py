@@ -47,6 +47,14 @@ CONFIGS = {
 METRIC = "orbital sweeps/s (ABPG step: normalize, Hpsi, S/H/B, theta, residual, precond, update)"
 
 
+# DRAM bytes (read + write) per split-K gram_kernel launch at the 2048-orbital
+# 192^3 workload in split-BF16x3, measured once with ncu over the nine
+# launches of one sweep (dram__bytes_read.sum + dram__bytes_write.sum, one
+# pass); the operand planes read once would be 6.12e10 B per launch
+SPLITK_DRAM_BYTES_PER_LAUNCH = 8.095e10
+SPLITK_ALGO_BYTES_PER_LAUNCH = 6.122e10
+
+
 def _env_int(k, d):
     try:
         return int(os.environ.get(k, d))
@@ -366,7 +374,13 @@ def run_gpu(args, cfg):
         achieved = per_launch / (k_ms * 1e-3) / 1e12
         roof = {"kernel": "gram_kernel (tcgen05 split-K: S, H, B)", "bound": "tensor",
                 "achieved": achieved, "peak": bf16, "unit": "TFLOP/s", "frac": achieved / bf16,
-                "traffic": None, "issued_frac": nprod * achieved / bf16,
+                "traffic": (SPLITK_DRAM_BYTES_PER_LAUNCH
+                            if (cfg["workload"] == CONFIGS["c5"]["workload"] and mode == "mixed"
+                                and args.gemm == "bf16x3") else None),
+                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of the nine "
+                                  "split-K launches of one sweep, averaged per launch; algorithmic "
+                                  f"{SPLITK_ALGO_BYTES_PER_LAUNCH:.3e} B per launch",
+                "issued_frac": nprod * achieved / bf16,
                 "algorithmic": f"{gram_flops:.3e} flop per sweep (S{' and B' if sw.use_matb else ''} "
                                f"lower incl. diagonal + H) over {tk_n / args.steps:.0f} launches"}
     elif dominant == "gram":
