@@ -924,6 +924,7 @@ int mgx_unet_adam(mgx_unet* net, const float* grad, const mgx_adam_params* p, vo
 int mgx_unet_train_step(mgx_unet* net, const float* x, const float* target, size_t ld,
     int nfunc, const mgx_adam_params* p, double* loss, void* stream)
 {
+    MGX_TRY(check_net(net));
     MGX_TRY(mgx_unet_loss_grad(net, x, target, ld, nfunc, (float*)net->grad.ptr, loss, stream));
     return mgx_unet_adam(net, (const float*)net->grad.ptr, p, stream);
 }

@@ -63,3 +63,28 @@ def test_bad_arguments_are_reported_not_aborted():
     out = ctypes.c_double()
     assert L.mgx_precond_gamma(ctypes.byref(capi.Grid.make((8, 8, 8), (1, 1, 1))), 9, 1, 0.0, 0.0,
                                ctypes.byref(out)) == capi.MGX_BAD_ARG
+
+
+def test_learned_and_local_entry_points_check_their_arguments():
+    """Entry points of the learned preconditioner and the localized orbitals
+    refuse NULL handles and inconsistent arguments before any device work."""
+    L = capi.load()
+    h = ctypes.c_void_p()
+    assert L.mgx_unet_create(None, ctypes.byref(h)) == capi.MGX_BAD_ARG
+    assert L.mgx_unet_forward(None, None, 0, None, 1, None) == capi.MGX_BAD_ARG
+    assert L.mgx_unet_loss_grad(None, None, None, 0, 1, None, None, None) == capi.MGX_BAD_ARG
+    prm = capi.AdamParams(1e-3, 0.9, 0.999, 1e-8)
+    assert L.mgx_unet_adam(None, None, ctypes.byref(prm), None) == capi.MGX_BAD_ARG
+    assert L.mgx_unet_train_step(None, None, None, 0, 1, ctypes.byref(prm), None, None) \
+        == capi.MGX_BAD_ARG
+    pp = capi.PrecondParams(0, 2, 0.1, 0)
+    assert L.mgx_precond_learned(None, None, ctypes.byref(pp), None, 0, None, 1, 0, None, None,
+                                 None, None) == capi.MGX_BAD_ARG
+    assert L.mgx_precond_mg_warm(None, ctypes.byref(pp), 0, None, 0, None, 1, None, None) \
+        == capi.MGX_BAD_ARG
+    assert L.mgx_local_create(None, None, None, ctypes.byref(h)) == capi.MGX_BAD_ARG
+    assert L.mgx_local_step(None, None, None, None, 0.1, None, None, None) == capi.MGX_BAD_ARG
+    assert L.mgx_local_set_config(None, 0, 2, 1) == capi.MGX_BAD_ARG
+    assert L.mgx_local_layout(None, None, None, None) == capi.MGX_BAD_ARG
+    assert capi.UNET_PARAMS == sum(ci * co * 27 for ci, co in
+                                   ((1, 16), (16, 32), (32, 64), (64, 32), (32, 16), (16, 1)))
