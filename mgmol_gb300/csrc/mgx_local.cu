@@ -179,7 +179,7 @@ template <int TY, int TZ, int PPS> struct Cols
 };
 
 template <int TY, int TZ, int PPS>
-__global__ void __launch_bounds__(THREADS) local_step_kernel(StepParams P)
+__global__ void __launch_bounds__(THREADS, 4) local_step_kernel(StepParams P)
 {
     using C = Cols<TY, TZ, PPS>;
     extern __shared__ __align__(16) float sm[];
@@ -206,34 +206,60 @@ __global__ void __launch_bounds__(THREADS) local_step_kernel(StepParams P)
         const float* phi = P.phi + P.off[f];
         const float* mo  = P.mvals + P.moff[f];
         const float* mc  = P.cvals + P.coff[f];
+        // stage 0 inputs of the next PPS planes, loaded into registers one
+        // march step ahead so that their latency overlaps stages 1 to 3
+        constexpr int NQ = (C::N3 + THREADS - 1) / THREADS;
+        float rps[PPS][NQ], rph[PPS][NQ], rv[PPS][NQ];
+        auto load_plane = [&](int p, int j) {
+            const bool in = (p >= 0 && p < e0);
+            const int gx  = wrap1(o0 + (in ? p : 0), P.n[0]);
+#pragma unroll
+            for (int k = 0; k < NQ; k++)
+            {
+                const int q  = tid + k * THREADS;
+                const int qy = q / C::Z3, qz = q - qy * C::Z3;
+                const int by = y0 + qy - 3, bz = z0 + qz - 3;
+                float ps = 0.f, ph = 0.f, v = 0.f;
+                if (q < C::N3 && in && by >= 0 && by < e1 && bz >= 0 && bz < e2)
+                {
+                    const size_t li = (size_t)p * ex + (size_t)by * e2 + bz;
+                    ps              = psi[li];
+                    ph              = phi[li];
+                    const int gy = wrap1(o1 + by, P.n[1]), gz = wrap1(o2 + bz, P.n[2]);
+                    v = P.V[((size_t)gx * P.n[1] + gy) * P.n[2] + gz];
+                }
+                rps[j][k] = ps;
+                rph[j][k] = ph;
+                rv[j][k]  = v;
+            }
+        };
+#pragma unroll
+        for (int j = 0; j < PPS; j++)
+            load_plane(j - 3, j);
         for (int t = 0; PPS * t - 6 < e0; t++)
         {
-            // stage 0: psi and phi - V psi
+            // stage 0: psi and phi - V psi, from the registers; then the
+            // loads of the planes of the next step
 #pragma unroll
             for (int j = 0; j < PPS; j++)
             {
                 const int p = PPS * t + j - 3;
-                if (p > e0 + 2) break;
-                float* dp     = s_psi + C::slot(p) * C::N3;
-                float* dd     = s_d + C::slot(p) * C::N3;
-                const bool in = (p >= 0 && p < e0);
-                const int gx  = wrap1(o0 + p, P.n[0]);
-                for (int q = tid; q < C::N3; q += THREADS)
+                if (p <= e0 + 2)
                 {
-                    const int qy = q / C::Z3, qz = q - qy * C::Z3;
-                    const int by = y0 + qy - 3, bz = z0 + qz - 3;
-                    float ps = 0.f, d = 0.f;
-                    if (in && by >= 0 && by < e1 && bz >= 0 && bz < e2)
+                    float* dp = s_psi + C::slot(p) * C::N3;
+                    float* dd = s_d + C::slot(p) * C::N3;
+#pragma unroll
+                    for (int k = 0; k < NQ; k++)
                     {
-                        const size_t li = (size_t)p * ex + (size_t)by * e2 + bz;
-                        ps              = psi[li];
-                        const int gy = wrap1(o1 + by, P.n[1]), gz = wrap1(o2 + bz, P.n[2]);
-                        const float v = P.V[((size_t)gx * P.n[1] + gy) * P.n[2] + gz];
-                        d             = phi[li] - v * ps;
+                        const int q = tid + k * THREADS;
+                        if (q < C::N3)
+                        {
+                            dp[q] = rps[j][k];
+                            dd[q] = rph[j][k] - rv[j][k] * rps[j][k];
+                        }
                     }
-                    dp[q] = ps;
-                    dd[q] = d;
                 }
+                load_plane(p + PPS, j);
             }
             __syncthreads();
             // stage 1: r = Mc (B(phi - V psi) + Delta_M psi), z pairs
