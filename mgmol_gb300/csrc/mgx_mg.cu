@@ -67,69 +67,134 @@ __device__ __forceinline__ T mask_point(const MaskDev& m, int f, int x, int y,
 }
 
 /* restriction of nfunc functions; accumulation type A (double for the FP64
- * path, as the reference; float for the FP32 path).  One block per coarse
- * (i, j) line, threads along coarse z; blockIdx.y = function. */
+ * path, as the reference; float for the FP32 path).  One block per pair of
+ * coarse (i, j) lines (i and i + 1), threads along coarse z; blockIdx.y =
+ * function.  A thread loads the 5 x 3 fine rows around its pair once (at
+ * z - 1, z, z + 1; the plane x = 2i + 1 serves both) and forms each coarse
+ * point with the grouping and order of src/pb/MGkernels.cc:249-270. */
 template <typename T, typename A>
 __global__ void restrict_kernel(const T* __restrict__ fine, size_t ldf,
     T* __restrict__ coarse, size_t ldc, int fx, int fy, int fz, MaskDev mask)
 {
-    const int cy = fy >> 1, cz = fz >> 1;
+    const int cx = fx >> 1, cy = fy >> 1, cz = fz >> 1;
     const int f  = blockIdx.y;
-    const int i  = blockIdx.x / cy, j = blockIdx.x - (blockIdx.x / cy) * cy;
+    const int i0 = 2 * (blockIdx.x / cy), j = blockIdx.x - (blockIdx.x / cy) * cy;
     const T* u   = fine + (size_t)f * ldf;
-    const int x = 2 * i, y = 2 * j;
-    const int xm = wrp(x - 1, fx), xp = wrp(x + 1, fx);
-    const int ym = wrp(y - 1, fy), yp = wrp(y + 1, fy);
-    const T* r00 = u + ((size_t)x * fy + y) * fz;
-    const T* rp0 = u + ((size_t)xp * fy + y) * fz;
-    const T* rm0 = u + ((size_t)xm * fy + y) * fz;
-    const T* r0p = u + ((size_t)x * fy + yp) * fz;
-    const T* r0m = u + ((size_t)x * fy + ym) * fz;
-    const T* rpp = u + ((size_t)xp * fy + yp) * fz;
-    const T* rpm = u + ((size_t)xp * fy + ym) * fz;
-    const T* rmp = u + ((size_t)xm * fy + yp) * fz;
-    const T* rmm = u + ((size_t)xm * fy + ym) * fz;
+    // rows[a][b]: fine row x = 2 i0 - 1 + a, y = 2 j - 1 + b
+    const T* rows[5][3];
+#pragma unroll
+    for (int a = 0; a < 5; a++)
+    {
+        const int x = wrp(2 * i0 - 1 + a, fx);
+#pragma unroll
+        for (int b = 0; b < 3; b++)
+            rows[a][b] = u + ((size_t)x * fy + wrp(2 * j - 1 + b, fy)) * fz;
+    }
+    const int npair = (i0 + 1 < cx) ? 2 : 1;
     for (int k = threadIdx.x; k < cz; k += blockDim.x)
     {
         const int z = 2 * k, zm = wrp(z - 1, fz), zp = wrp(z + 1, fz);
-        // grouping and order of src/pb/MGkernels.cc:249-270
-        const A face = (A)rp0[z] + (A)rm0[z] + (A)r0p[z] + (A)r0m[z] + (A)r00[zm] + (A)r00[zp];
-        const A corner = (A)rpp[zm] + (A)rpp[zp] + (A)rpm[zm] + (A)rpm[zp] + (A)rmp[zm]
-                         + (A)rmp[zp] + (A)rmm[zm] + (A)rmm[zp];
-        const A edge = (A)r0p[zm] + (A)r0p[zp] + (A)r0m[zm] + (A)r0m[zp] + (A)rp0[zm]
-                       + (A)rp0[zp] + (A)rm0[zm] + (A)rm0[zp] + (A)rmm[z] + (A)rpm[z]
-                       + (A)rmp[z] + (A)rpp[z];
-        const A r = (A)(1. / 64.) * ((A)8. * (A)r00[z] + (A)4. * face + (A)2. * edge + corner);
-        coarse[(size_t)f * ldc + ((size_t)i * cy + j) * cz + k]
-            = mask_point<T>(mask, f, i, j, k, (T)r);
+        A v[5][3][3];
+#pragma unroll
+        for (int a = 0; a < 5; a++)
+#pragma unroll
+            for (int b = 0; b < 3; b++)
+            {
+                v[a][b][0] = (A)rows[a][b][zm];
+                v[a][b][1] = (A)rows[a][b][z];
+                v[a][b][2] = (A)rows[a][b][zp];
+            }
+#pragma unroll
+        for (int di = 0; di < 2; di++)
+        {
+            if (di >= npair) break;
+            const int i  = i0 + di;
+            const int ca = 2 * di + 1; // centre plane x = 2i
+            const A* r00 = v[ca][1];
+            const A* rp0 = v[ca + 1][1];
+            const A* rm0 = v[ca - 1][1];
+            const A* r0p = v[ca][2];
+            const A* r0m = v[ca][0];
+            const A* rpp = v[ca + 1][2];
+            const A* rpm = v[ca + 1][0];
+            const A* rmp = v[ca - 1][2];
+            const A* rmm = v[ca - 1][0];
+            const A face = rp0[1] + rm0[1] + r0p[1] + r0m[1] + r00[0] + r00[2];
+            const A corner = rpp[0] + rpp[2] + rpm[0] + rpm[2] + rmp[0] + rmp[2] + rmm[0] + rmm[2];
+            const A edge = r0p[0] + r0p[2] + r0m[0] + r0m[2] + rp0[0] + rp0[2] + rm0[0] + rm0[2]
+                           + rmm[1] + rpm[1] + rmp[1] + rpp[1];
+            const A r = (A)(1. / 64.) * ((A)8. * r00[1] + (A)4. * face + (A)2. * edge + corner);
+            coarse[(size_t)f * ldc + ((size_t)i * cy + j) * cz + k]
+                = mask_point<T>(mask, f, i, j, k, (T)r);
+        }
     }
 }
-
-/* trilinear prolongation; MODE 0: out = P e; MODE 1: out -= mask(P e).
- * One block per fine x plane and band of PROLONG_CROWS coarse y rows.  A
- * thread owns coarse point (j, k) of the band and writes the 2 x 2 fine
- * points (2j + b, 2k + c) of its x plane: it loads the coarse values at
- * k and k + 1 of rows j and j + 1 (and of plane i + 1 for odd x) once and
- * forms every output with the operation order of src/pb/MGkernels.cc:84-197.
- * VEC2: the two z neighbours are stored (and, MODE 1, read) as one pair. */
-constexpr int PROLONG_CROWS = 4;
 
 template <typename T> struct Pair;
 template <> struct Pair<float> { using type = float2; };
 template <> struct Pair<double> { using type = double2; };
 
+/* one fine output pair (z, z + 1) of plane x, row y: MODE 0 stores, MODE 1
+ * subtracts mask(P e) */
+template <typename T, int MODE, bool VEC2>
+__device__ __forceinline__ void prolong_store(T* out, size_t ldo, int fy, int fz, int f, int x,
+    int y, int z, T w0, T w1, const MaskDev& mask)
+{
+    using P2 = typename Pair<T>::type;
+    T* o = out + (size_t)f * ldo + ((size_t)x * fy + y) * fz + z;
+    if (MODE == 1)
+    {
+        w0 = mask_point<T>(mask, f, x, y, z, w0);
+        w1 = mask_point<T>(mask, f, x, y, z + 1, w1);
+    }
+    if (VEC2)
+    {
+        P2 q;
+        if (MODE == 1)
+        {
+            q   = *reinterpret_cast<const P2*>(o);
+            q.x = q.x - w0;
+            q.y = q.y - w1;
+        }
+        else
+        {
+            q.x = w0;
+            q.y = w1;
+        }
+        *reinterpret_cast<P2*>(o) = q;
+    }
+    else if (MODE == 1)
+    {
+        o[0] = o[0] - w0;
+        o[1] = o[1] - w1;
+    }
+    else
+    {
+        o[0] = w0;
+        o[1] = w1;
+    }
+}
+
+/* trilinear prolongation; MODE 0: out = P e; MODE 1: out -= mask(P e).
+ * One block per coarse x plane i and band of PROLONG_CROWS coarse y rows.
+ * A thread owns coarse point (j, k) of the band: it loads the coarse values
+ * at k and k + 1 of rows j and j + 1 in planes i and i + 1 once and writes
+ * the 2 x 2 x 2 fine points (2i + a, 2j + b, 2k + c), each formed with the
+ * operation order of src/pb/MGkernels.cc:84-197.  VEC2: the two z
+ * neighbours are stored (and, MODE 1, read) as one pair. */
+constexpr int PROLONG_CROWS = 4;
+
 template <typename T, int MODE, bool VEC2>
 __global__ void __launch_bounds__(256) prolong_kernel(const T* __restrict__ coarse,
     size_t ldc, T* __restrict__ out, size_t ldo, int fx, int fy, int fz, MaskDev mask)
 {
-    using P2 = typename Pair<T>::type;
     const int cx = fx >> 1, cy = fy >> 1, cz = fz >> 1;
     const int f      = blockIdx.y;
     const int bands  = (cy + PROLONG_CROWS - 1) / PROLONG_CROWS;
-    const int x      = blockIdx.x / bands;
-    const int jb     = (blockIdx.x - x * bands) * PROLONG_CROWS;
+    const int i      = blockIdx.x / bands;
+    const int jb     = (blockIdx.x - i * bands) * PROLONG_CROWS;
     const T* e       = coarse + (size_t)f * ldc;
-    const int i = x >> 1, a = x & 1, i1 = wrp(i + 1, cx);
+    const int i1     = wrp(i + 1, cx);
     for (int t = threadIdx.x; t < PROLONG_CROWS * cz; t += blockDim.x)
     {
         const int r = t / cz, k = t - (t / cz) * cz;
@@ -138,62 +203,26 @@ __global__ void __launch_bounds__(256) prolong_kernel(const T* __restrict__ coar
         const int j1 = wrp(j + 1, cy), k1 = wrp(k + 1, cz);
         const T* c00 = e + ((size_t)i * cy + j) * cz;
         const T* c01 = e + ((size_t)i * cy + j1) * cz;
+        const T* c10 = e + ((size_t)i1 * cy + j) * cz;
+        const T* c11 = e + ((size_t)i1 * cy + j1) * cz;
         const T a0 = c00[k], a1 = c00[k1], b0 = c01[k], b1 = c01[k1];
-        T v[2][2]; // [y parity][z parity]
-        if (!a)
+        const T d0 = c10[k], d1 = c10[k1], g0 = c11[k], g1 = c11[k1];
+        // even plane x = 2i
         {
-            v[0][0] = a0;
-            v[0][1] = (T)0.5 * (a0 + a1);
-            v[1][0] = (T)0.5 * (b0 + a0);
-            v[1][1] = (T)0.25 * (b1 + a1 + b0 + a0);
+            const int x = 2 * i;
+            prolong_store<T, MODE, VEC2>(out, ldo, fy, fz, f, x, 2 * j, 2 * k, a0,
+                (T)0.5 * (a0 + a1), mask);
+            prolong_store<T, MODE, VEC2>(out, ldo, fy, fz, f, x, 2 * j + 1, 2 * k,
+                (T)0.5 * (b0 + a0), (T)0.25 * (b1 + a1 + b0 + a0), mask);
         }
-        else
+        // odd plane x = 2i + 1
         {
-            const T* c10 = e + ((size_t)i1 * cy + j) * cz;
-            const T* c11 = e + ((size_t)i1 * cy + j1) * cz;
-            const T d0 = c10[k], d1 = c10[k1], g0 = c11[k], g1 = c11[k1];
-            v[0][0] = (T)0.5 * (d0 + a0);
-            v[0][1] = (T)0.25 * (d1 + d0 + a1 + a0);
-            v[1][0] = (T)0.25 * (g0 + d0 + b0 + a0);
-            v[1][1] = (T)0.125 * (g1 + g0 + d1 + d0 + b1 + b0 + a1 + a0);
-        }
-#pragma unroll
-        for (int b = 0; b < 2; b++)
-        {
-            const int y = 2 * j + b;
-            T* o = out + (size_t)f * ldo + ((size_t)x * fy + y) * fz + 2 * k;
-            T w0 = v[b][0], w1 = v[b][1];
-            if (MODE == 1)
-            {
-                w0 = mask_point<T>(mask, f, x, y, 2 * k, w0);
-                w1 = mask_point<T>(mask, f, x, y, 2 * k + 1, w1);
-            }
-            if (VEC2)
-            {
-                P2 q;
-                if (MODE == 1)
-                {
-                    q = *reinterpret_cast<const P2*>(o);
-                    q.x = q.x - w0;
-                    q.y = q.y - w1;
-                }
-                else
-                {
-                    q.x = w0;
-                    q.y = w1;
-                }
-                *reinterpret_cast<P2*>(o) = q;
-            }
-            else if (MODE == 1)
-            {
-                o[0] = o[0] - w0;
-                o[1] = o[1] - w1;
-            }
-            else
-            {
-                o[0] = w0;
-                o[1] = w1;
-            }
+            const int x = 2 * i + 1;
+            prolong_store<T, MODE, VEC2>(out, ldo, fy, fz, f, x, 2 * j, 2 * k,
+                (T)0.5 * (d0 + a0), (T)0.25 * (d1 + d0 + a1 + a0), mask);
+            prolong_store<T, MODE, VEC2>(out, ldo, fy, fz, f, x, 2 * j + 1, 2 * k,
+                (T)0.25 * (g0 + d0 + b0 + a0),
+                (T)0.125 * (g1 + g0 + d1 + d0 + b1 + b0 + a1 + a0), mask);
         }
     }
 }
@@ -234,7 +263,7 @@ static dim3 grid_for(size_t npts, int nfunc)
 int restrict_launch(int dtype, const Level& fine, const void* f, size_t ldf,
     void* c, size_t ldc, int nfunc, const MaskDev& mask, cudaStream_t s)
 {
-    const dim3 g((fine.n[0] / 2) * (fine.n[1] / 2), nfunc);
+    const dim3 g((((fine.n[0] / 2) + 1) / 2) * (fine.n[1] / 2), nfunc);
     const int nt = std::min(256, std::max(32, ((fine.n[2] / 2 + 31) / 32) * 32));
     if (dtype == MGX_F64)
         restrict_kernel<double, double><<<g, nt, 0, s>>>((const double*)f, ldf,
@@ -251,7 +280,7 @@ int prolong_launch(int dtype, int mode, const Level& fine, const void* c,
     cudaStream_t s)
 {
     const int bands = ((fine.n[1] / 2) + PROLONG_CROWS - 1) / PROLONG_CROWS;
-    const dim3 g(fine.n[0] * bands, nfunc);
+    const dim3 g((fine.n[0] / 2) * bands, nfunc);
     const int nt = 256;
     const size_t es = dtype_size(dtype);
     const bool v2   = ((ldo % 2) == 0) && ((uintptr_t)out % (2 * es) == 0);
