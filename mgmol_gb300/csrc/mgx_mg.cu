@@ -130,71 +130,31 @@ __global__ void restrict_kernel(const T* __restrict__ fine, size_t ldf,
     }
 }
 
+/* trilinear prolongation; MODE 0: out = P e; MODE 1: out -= mask(P e).
+ * One block per fine x plane and band of PROLONG_CROWS coarse y rows.  A
+ * thread owns coarse point (j, k) of the band and writes the 2 x 2 fine
+ * points (2j + b, 2k + c) of its x plane: it loads the coarse values at
+ * k and k + 1 of rows j and j + 1 (and of plane i + 1 for odd x) once and
+ * forms every output with the operation order of src/pb/MGkernels.cc:84-197.
+ * VEC2: the two z neighbours are stored (and, MODE 1, read) as one pair. */
+constexpr int PROLONG_CROWS = 4;
+
 template <typename T> struct Pair;
 template <> struct Pair<float> { using type = float2; };
 template <> struct Pair<double> { using type = double2; };
-
-/* one fine output pair (z, z + 1) of plane x, row y: MODE 0 stores, MODE 1
- * subtracts mask(P e) */
-template <typename T, int MODE, bool VEC2>
-__device__ __forceinline__ void prolong_store(T* out, size_t ldo, int fy, int fz, int f, int x,
-    int y, int z, T w0, T w1, const MaskDev& mask)
-{
-    using P2 = typename Pair<T>::type;
-    T* o = out + (size_t)f * ldo + ((size_t)x * fy + y) * fz + z;
-    if (MODE == 1)
-    {
-        w0 = mask_point<T>(mask, f, x, y, z, w0);
-        w1 = mask_point<T>(mask, f, x, y, z + 1, w1);
-    }
-    if (VEC2)
-    {
-        P2 q;
-        if (MODE == 1)
-        {
-            q   = *reinterpret_cast<const P2*>(o);
-            q.x = q.x - w0;
-            q.y = q.y - w1;
-        }
-        else
-        {
-            q.x = w0;
-            q.y = w1;
-        }
-        *reinterpret_cast<P2*>(o) = q;
-    }
-    else if (MODE == 1)
-    {
-        o[0] = o[0] - w0;
-        o[1] = o[1] - w1;
-    }
-    else
-    {
-        o[0] = w0;
-        o[1] = w1;
-    }
-}
-
-/* trilinear prolongation; MODE 0: out = P e; MODE 1: out -= mask(P e).
- * One block per coarse x plane i and band of PROLONG_CROWS coarse y rows.
- * A thread owns coarse point (j, k) of the band: it loads the coarse values
- * at k and k + 1 of rows j and j + 1 in planes i and i + 1 once and writes
- * the 2 x 2 x 2 fine points (2i + a, 2j + b, 2k + c), each formed with the
- * operation order of src/pb/MGkernels.cc:84-197.  VEC2: the two z
- * neighbours are stored (and, MODE 1, read) as one pair. */
-constexpr int PROLONG_CROWS = 4;
 
 template <typename T, int MODE, bool VEC2>
 __global__ void __launch_bounds__(256) prolong_kernel(const T* __restrict__ coarse,
     size_t ldc, T* __restrict__ out, size_t ldo, int fx, int fy, int fz, MaskDev mask)
 {
+    using P2 = typename Pair<T>::type;
     const int cx = fx >> 1, cy = fy >> 1, cz = fz >> 1;
     const int f      = blockIdx.y;
     const int bands  = (cy + PROLONG_CROWS - 1) / PROLONG_CROWS;
-    const int i      = blockIdx.x / bands;
-    const int jb     = (blockIdx.x - i * bands) * PROLONG_CROWS;
+    const int x      = blockIdx.x / bands;
+    const int jb     = (blockIdx.x - x * bands) * PROLONG_CROWS;
     const T* e       = coarse + (size_t)f * ldc;
-    const int i1     = wrp(i + 1, cx);
+    const int i = x >> 1, a = x & 1, i1 = wrp(i + 1, cx);
     for (int t = threadIdx.x; t < PROLONG_CROWS * cz; t += blockDim.x)
     {
         const int r = t / cz, k = t - (t / cz) * cz;
@@ -203,26 +163,62 @@ __global__ void __launch_bounds__(256) prolong_kernel(const T* __restrict__ coar
         const int j1 = wrp(j + 1, cy), k1 = wrp(k + 1, cz);
         const T* c00 = e + ((size_t)i * cy + j) * cz;
         const T* c01 = e + ((size_t)i * cy + j1) * cz;
-        const T* c10 = e + ((size_t)i1 * cy + j) * cz;
-        const T* c11 = e + ((size_t)i1 * cy + j1) * cz;
         const T a0 = c00[k], a1 = c00[k1], b0 = c01[k], b1 = c01[k1];
-        const T d0 = c10[k], d1 = c10[k1], g0 = c11[k], g1 = c11[k1];
-        // even plane x = 2i
+        T v[2][2]; // [y parity][z parity]
+        if (!a)
         {
-            const int x = 2 * i;
-            prolong_store<T, MODE, VEC2>(out, ldo, fy, fz, f, x, 2 * j, 2 * k, a0,
-                (T)0.5 * (a0 + a1), mask);
-            prolong_store<T, MODE, VEC2>(out, ldo, fy, fz, f, x, 2 * j + 1, 2 * k,
-                (T)0.5 * (b0 + a0), (T)0.25 * (b1 + a1 + b0 + a0), mask);
+            v[0][0] = a0;
+            v[0][1] = (T)0.5 * (a0 + a1);
+            v[1][0] = (T)0.5 * (b0 + a0);
+            v[1][1] = (T)0.25 * (b1 + a1 + b0 + a0);
         }
-        // odd plane x = 2i + 1
+        else
         {
-            const int x = 2 * i + 1;
-            prolong_store<T, MODE, VEC2>(out, ldo, fy, fz, f, x, 2 * j, 2 * k,
-                (T)0.5 * (d0 + a0), (T)0.25 * (d1 + d0 + a1 + a0), mask);
-            prolong_store<T, MODE, VEC2>(out, ldo, fy, fz, f, x, 2 * j + 1, 2 * k,
-                (T)0.25 * (g0 + d0 + b0 + a0),
-                (T)0.125 * (g1 + g0 + d1 + d0 + b1 + b0 + a1 + a0), mask);
+            const T* c10 = e + ((size_t)i1 * cy + j) * cz;
+            const T* c11 = e + ((size_t)i1 * cy + j1) * cz;
+            const T d0 = c10[k], d1 = c10[k1], g0 = c11[k], g1 = c11[k1];
+            v[0][0] = (T)0.5 * (d0 + a0);
+            v[0][1] = (T)0.25 * (d1 + d0 + a1 + a0);
+            v[1][0] = (T)0.25 * (g0 + d0 + b0 + a0);
+            v[1][1] = (T)0.125 * (g1 + g0 + d1 + d0 + b1 + b0 + a1 + a0);
+        }
+#pragma unroll
+        for (int b = 0; b < 2; b++)
+        {
+            const int y = 2 * j + b;
+            T* o = out + (size_t)f * ldo + ((size_t)x * fy + y) * fz + 2 * k;
+            T w0 = v[b][0], w1 = v[b][1];
+            if (MODE == 1)
+            {
+                w0 = mask_point<T>(mask, f, x, y, 2 * k, w0);
+                w1 = mask_point<T>(mask, f, x, y, 2 * k + 1, w1);
+            }
+            if (VEC2)
+            {
+                P2 q;
+                if (MODE == 1)
+                {
+                    q = *reinterpret_cast<const P2*>(o);
+                    q.x = q.x - w0;
+                    q.y = q.y - w1;
+                }
+                else
+                {
+                    q.x = w0;
+                    q.y = w1;
+                }
+                *reinterpret_cast<P2*>(o) = q;
+            }
+            else if (MODE == 1)
+            {
+                o[0] = o[0] - w0;
+                o[1] = o[1] - w1;
+            }
+            else
+            {
+                o[0] = w0;
+                o[1] = w1;
+            }
         }
     }
 }
@@ -280,7 +276,7 @@ int prolong_launch(int dtype, int mode, const Level& fine, const void* c,
     cudaStream_t s)
 {
     const int bands = ((fine.n[1] / 2) + PROLONG_CROWS - 1) / PROLONG_CROWS;
-    const dim3 g((fine.n[0] / 2) * bands, nfunc);
+    const dim3 g(fine.n[0] * bands, nfunc);
     const int nt = 256;
     const size_t es = dtype_size(dtype);
     const bool v2   = ((ldo % 2) == 0) && ((uintptr_t)out % (2 * es) == 0);

@@ -1,8 +1,9 @@
 """The tensor-core product kernels in their other launch forms, each in a
 fresh process (the library reads the choice once): the split-K products
 (S, H, B) on the persistent two-accumulator kernel (MGX_TC_PERSIST_SPLITK=1)
-and every product on one CTA per output tile (MGX_TC_PERSIST=0), against
-the FP64 oracle at the split-BF16x3 error bars."""
+every product on one CTA per output tile (MGX_TC_PERSIST=0), and the
+split-K tiles in column order (MGX_TC_TILE_ORDER=col), against the FP64
+oracle at the split-BF16x3 error bars."""
 import os
 import subprocess
 import sys
@@ -46,7 +47,8 @@ print("variant ok")
 """
 
 
-@pytest.mark.parametrize("env", [{"MGX_TC_PERSIST_SPLITK": "1"}, {"MGX_TC_PERSIST": "0"}])
+@pytest.mark.parametrize("env", [{"MGX_TC_PERSIST_SPLITK": "1"}, {"MGX_TC_PERSIST": "0"},
+                                 {"MGX_TC_TILE_ORDER": "col"}])
 def test_product_kernel_launch_forms(env):
     r = subprocess.run([sys.executable, "-c", SCRIPT.replace("ROOT", repr(ROOT))],
                        env={**os.environ, **env}, capture_output=True, text=True, timeout=600)
