@@ -1,6 +1,6 @@
 """The tensor-core product kernels in their other launch forms, each in a
 fresh process (the library reads the choice once): the split-K products
-(S, H, B) on the persistent two-accumulator kernel (MGX_TC_PERSIST_SPLITK=1)
+(S, H, B) on the persistent two-accumulator kernel (MGX_TC_PERSIST_SPLITK=1),
 every product on one CTA per output tile (MGX_TC_PERSIST=0), and the
 split-K tiles in column order (MGX_TC_TILE_ORDER=col), against the FP64
 oracle at the split-BF16x3 error bars."""
