@@ -48,10 +48,11 @@ METRIC = "orbital sweeps/s (ABPG step: normalize, Hpsi, S/H/B, theta, residual, 
 
 
 # DRAM bytes (read + write) per split-K gram_kernel launch at the 2048-orbital
-# 192^3 workload in split-BF16x3, measured once with ncu over the nine
-# launches of one sweep (dram__bytes_read.sum + dram__bytes_write.sum, one
-# pass); the operand planes read once would be 6.12e10 B per launch
-SPLITK_DRAM_BYTES_PER_LAUNCH = 8.095e10
+# 192^3 workload in split-BF16x3 (row tile order), measured once with ncu
+# over the nine launches of one sweep (dram__bytes_read.sum +
+# dram__bytes_write.sum, one pass); the operand planes read once would be
+# 6.12e10 B per launch
+SPLITK_DRAM_BYTES_PER_LAUNCH = 7.479e10
 SPLITK_ALGO_BYTES_PER_LAUNCH = 6.122e10
 
 
