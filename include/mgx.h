@@ -233,18 +233,22 @@ int mgx_precond_mg_update(mgx_ctx* ctx, const mgx_precond_params* p,
 
 /* mgx_precond_mg without any device allocation.  This entry point has no
  * counterpart in the reference; it serves callers that cannot allocate
- * device memory (code inside a stream capture that must not allocate,
- * hosts whose device memory belongs to a pool they do not control, plug-ins
- * in processes that forbid allocations after start-up).  Same arguments and
- * results as mgx_precond_mg; ctx only supplies the grid (its workspaces are
- * not used).  The V-cycle levels live in a fixed 64 MiB device array that
- * is part of the library and held by every GPU that loads it: functions are
- * processed in chunks that fit it, and a request whose single function
- * needs more than the array holds is rejected with MGX_BAD_ARG.  The first
- * call on a device looks up the array's device address (make it before any
- * stream capture).  All calls share the array, so calls that overlap on the
- * GPU (other streams, other host threads) race; the call returns after its
- * work is complete on `stream`. */
+ * device memory: hosts whose device memory belongs to a pool they do not
+ * control (an application that reserves the GPU's memory up front and hands
+ * out slices of it), and plug-ins in processes that forbid device
+ * allocations after start-up (cudaMalloc may synchronize the device and
+ * stall the process's other streams).  Same arguments and results as
+ * mgx_precond_mg; ctx only supplies the grid (its workspaces are not used).
+ * The V-cycle levels live in a fixed 64 MiB device array that is part of
+ * the library and held by every GPU that loads it: functions are processed
+ * in chunks that fit it, and a request whose single function needs more
+ * than the array holds is rejected with MGX_BAD_ARG.  The first call on a
+ * device looks up the array's device address and keeps it for the life of
+ * the process (make that call before any stream capture; a cudaDeviceReset
+ * afterwards leaves the kept address stale).  All calls share the array,
+ * so calls that overlap on the GPU (other streams, other host threads)
+ * race.  The call reads the V-cycle's status word back and waits for
+ * `stream` before it returns. */
 int mgx_precond_mg_static(mgx_ctx* ctx, const mgx_precond_params* p,
     mgx_dtype dtype, const void* res, size_t ld, void* out, int nfunc,
     const mgx_masks* masks, void* stream);

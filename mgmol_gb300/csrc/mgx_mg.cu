@@ -969,14 +969,15 @@ int precond_mg(mgx_ctx* ctx, const mgx_precond_params* P, int dtype,
 /* ------------------------------------------------------------------ */
 /* Allocation-free V-cycle                                              */
 /* ------------------------------------------------------------------ */
-// For callers that cannot allocate device memory at all: code running
-// inside a CUDA stream capture that must not allocate, host programs whose
-// device memory is owned by a pool they do not control, or plug-ins loaded
-// into a process that forbids allocations after start-up.  The V-cycle's
-// level buffers and status word then live in this file-scope device array
-// instead of the context workspace.  The array is part of the library's
-// device image: every GPU that loads the library holds these 64 MiB until
-// the process exits.
+// For callers that cannot allocate device memory at all: host programs
+// whose device memory is owned by a pool they do not control (an
+// application that reserves the GPU's memory up front and hands out slices
+// of it), or plug-ins loaded into a process that forbids device allocations
+// after start-up (cudaMalloc may synchronize the device and stall every
+// other stream of the process).  The V-cycle's level buffers and status
+// word then live in this file-scope device array instead of the context
+// workspace.  The array is part of the library's device image: every GPU
+// that loads the library holds these 64 MiB until the process exits.
 constexpr size_t STATIC_VCYCLE_SCRATCH_BYTES = size_t(64) << 20;
 constexpr size_t STATIC_VCYCLE_STATUS_BYTES  = 256;
 static __device__ __align__(256) unsigned char g_vcycle_scratch[STATIC_VCYCLE_SCRATCH_BYTES];
@@ -990,8 +991,10 @@ void* g_scratch_address[MAX_DEVICES] = {};
 /* Device address of the static scratch on the current device.  The host
  * symbol g_vcycle_scratch is only a stand-in for the device array; its
  * device address is looked up once per device, with that device current,
- * on the first call that needs it (which must therefore not happen during
- * a stream capture). */
+ * on the first call that needs it (which should therefore come before any
+ * stream capture).  The cached address belongs to the device's primary
+ * context as it was at that first call: it assumes that context lives as
+ * long as the process (no cudaDeviceReset in between). */
 int static_scratch_address(void** ptr)
 {
     int dev = 0;

@@ -1,9 +1,9 @@
 """The allocation-free V-cycle entry point, mgx_precond_mg_static.
 
-Callers that cannot allocate device memory (inside a stream capture that
-must not allocate, under a memory pool they do not own, in a process that
-forbids allocations after start-up) use this entry point; its scratch is a
-fixed 64 MiB device array inside the library.  This file is collected last
+Callers that cannot allocate device memory (under a memory pool they do
+not own, or in a process that forbids device allocations after start-up)
+use this entry point; its scratch is a fixed 64 MiB device array inside the
+library.  This file is collected last
 so that a failure here never hides another test; it passes alone in a fresh
 process as well as after the rest of the suite.
 """
