@@ -3,9 +3,10 @@
 # translation units, compiled unmodified from the read-only source tree,
 # against the single-task shims in oracle/shim/, plus oracle/ref_driver.cpp.
 # Test infrastructure only (pins the oracle restatement; records fixtures).
-# Usage: oracle/build_ref.sh [path-to-mgmol-source]   (default /root/reference)
+# Usage: oracle/build_ref.sh [path-to-mgmol-source]
+#   (default: $MGMOL_SRC, else /root/reference)
 set -e
-REF=${1:-/root/reference}
+REF=${1:-${MGMOL_SRC:-/root/reference}}
 HERE=$(cd "$(dirname "$0")" && pwd)
 SRC=$REF/src
 if [ ! -d "$SRC/pb" ]; then
@@ -28,6 +29,18 @@ for tu in $TUS; do
 done
 $CXX $FLAGS $INC -c "$HERE/ref_driver.cpp" -o "$OUT/obj/ref_driver.o" &
 pids="$pids $!"
+# S and H through the reference's local matrices and LocalMatrices2DistMatrix
+# (its 1e-14 filter), with single-task stand-ins for the ScaLAPACK-backed
+# DistMatrix / SparseDistMatrix headers (oracle/shim_dist/, searched first)
+MINC="-I$HERE/shim_dist $INC"
+for tu in local_matrices/LocalMatrices.cc local_matrices/SquareLocalMatrices.cc LocalMatrices2DistMatrix.cc; do
+    o=$OUT/obj/$(echo "$tu" | tr '/' '_' | sed 's/\.cc$/.o/')
+    $CXX $FLAGS $MINC -c "$SRC/$tu" -o "$o" &
+    pids="$pids $!"
+    OBJS="$OBJS $o"
+done
+$CXX $FLAGS $MINC -c "$HERE/ref_matrices.cpp" -o "$OUT/obj/ref_matrices.o" &
+pids="$pids $!"
 # AndersonMix<T>::update, TESTING build, one instantiation per storage type
 # over the block type of shim_anderson/Solution.h
 # The include guards of the reference's orbital headers are predefined: the
@@ -43,6 +56,6 @@ pids="$pids $!"
 $CXX $FLAGS -c "$HERE/shim/blas_shim.cpp" -o "$OUT/obj/blas_shim.o" &
 pids="$pids $!"
 for p in $pids; do wait $p; done
-$CXX $FLAGS -shared -o "$OUT/libmgref.so" $OBJS "$OUT/obj/ref_driver.o" "$OUT/obj/blas_shim.o" \
+$CXX $FLAGS -shared -o "$OUT/libmgref.so" $OBJS "$OUT/obj/ref_driver.o" "$OUT/obj/ref_matrices.o" "$OUT/obj/blas_shim.o" \
     "$OUT/obj/AndersonMix_f.o" "$OUT/obj/AndersonMix_d.o" "$OUT/obj/ref_anderson.o"
 echo "build_ref: $OUT/libmgref.so"

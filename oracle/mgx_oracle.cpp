@@ -1462,6 +1462,30 @@ int orc_gram_f(const float* psi, long ld, int nfunc, long numpt, double vel,
     return 0;
 }
 
+/* The reference's mixed-precision (USE_MP) build forms S and H of FP32
+ * orbitals in a float local matrix: LocalMatrices<float>::gemm (MPgemm 't',
+ * 'n': each entry the FP64 MPdot rounded to float), copied to double and
+ * scaled by vel (src/LocGridOrbitals.cc:1584-1602), then the 1e-14 filter.
+ * b is psi for S and hpsi for H; out column-major (j * nfunc + i). */
+int orc_product_f_usemp(const float* psi, const float* b, long ld, int nfunc,
+    long numpt, double vel, double* out)
+{
+#pragma omp parallel for schedule(dynamic)
+    for (int j = 0; j < nfunc; j++)
+        for (int i = 0; i < nfunc; i++)
+        {
+            double t = 0.;
+            const float* x = psi + (size_t)i * ld;
+            const float* y = b + (size_t)j * ld;
+            for (long k = 0; k < numpt; k++)
+                t += (double)x[k] * (double)y[k];
+            double v = (double)(float)t * vel;
+            if (!(std::fabs(v) > 1.e-14)) v = 0.;
+            out[(size_t)j * nfunc + i] = v;
+        }
+    return 0;
+}
+
 /* Hamiltonian::addHlocalij -> LocGridOrbitals::computeLocalProduct
  * (src/LocGridOrbitals.cc:1554-1604): reference-BLAS DGEMM('t','n'),
  * H(i,j) = <psi_i, hpsi_j> * vel, same 1e-14 filter on accumulation. */

@@ -226,22 +226,44 @@ def jacobi_factor(n, ll, lap_type):
     return lib().orc_jacobi_factor(gn, gl, lap_type)
 
 
-def gram(psi, vel):
+def gram(psi, vel, ref=False, usemp=False):
+    """S = psi^T psi * vel with the 1e-14 filter (symmetric).  ref=True runs
+    the reference's own LocalMatrices / LocalMatrices2DistMatrix code; for
+    FP32 orbitals that is the USE_MP path, which keeps the product in a
+    float local matrix (src/LocGridOrbitals.cc:1584-1602).  usemp=True
+    restates that path for FP32 orbitals; the default keeps the FP64 sum
+    (the stricter reference for the mixed-precision GPU path)."""
     psi = np.ascontiguousarray(psi)
     nf, npt = psi.shape
     S = np.zeros((nf, nf))
+    if usemp and psi.dtype == np.float32 and not ref:
+        _call(lib(), "orc_product_f_usemp", _p(psi), _p(psi), ctypes.c_long(npt), nf,
+              ctypes.c_long(npt), ctypes.c_double(vel), _p(S))
+        return S.T.copy()
+    if ref:
+        _call(ref_lib(), f"ref_gram_{_sfx(psi)}", npt, nf, _p(psi), npt, ctypes.c_double(vel), _p(S))
+        return S.T.copy()
     _call(lib(), f"orc_gram_{_sfx(psi)}", _p(psi), ctypes.c_long(npt), nf, ctypes.c_long(npt),
           ctypes.c_double(vel), _p(S))
     return S
 
 
-def hmat(psi, hpsi_, vel):
+def hmat(psi, hpsi_, vel, ref=False, usemp=False):
+    """H[i, j] = <psi_i, hpsi_j> * vel with the 1e-14 filter; ref and usemp
+    as in gram."""
     psi = np.ascontiguousarray(psi)
     hpsi_ = np.ascontiguousarray(hpsi_, dtype=psi.dtype)
     nf, npt = psi.shape
     H = np.zeros((nf, nf))
-    _call(lib(), f"orc_hmat_{_sfx(psi)}", _p(psi), _p(hpsi_), ctypes.c_long(npt), nf,
-          ctypes.c_long(npt), ctypes.c_double(vel), _p(H))
+    if usemp and psi.dtype == np.float32 and not ref:
+        _call(lib(), "orc_product_f_usemp", _p(psi), _p(hpsi_), ctypes.c_long(npt), nf,
+              ctypes.c_long(npt), ctypes.c_double(vel), _p(H))
+    elif ref:
+        _call(ref_lib(), f"ref_hmat_{_sfx(psi)}", npt, nf, _p(psi), _p(hpsi_), npt,
+              ctypes.c_double(vel), _p(H))
+    else:
+        _call(lib(), f"orc_hmat_{_sfx(psi)}", _p(psi), _p(hpsi_), ctypes.c_long(npt), nf,
+              ctypes.c_long(npt), ctypes.c_double(vel), _p(H))
     # H is column-major (j*n+i) = H(i,j); return H[i, j]
     return H.T.copy()
 

@@ -480,6 +480,9 @@ int mgm(const int* n, const double* ll, int lap_type, int ng, int cogr, int max_
 } // namespace
 
 extern "C" {
+/* The single-task environment (PEenv, MGmol_MPI::setup), set up once per
+ * process; the S and H driver (ref_matrices.cpp) needs MGmol_MPI too. */
+void ref_env_init() { (void)env(); }
 int ref_mult_matrix_d(int np, int nf, const double* p, const double* th, double* o) { return mult_matrix(np, nf, p, th, o); }
 int ref_mult_matrix_f(int np, int nf, const float* p, const double* th, float* o) { return mult_matrix(np, nf, p, th, o); }
 int ref_residual_d(const int* n, const double* ll, int nf, const double* p, const double* h, const double* th, double* o) { return residual(n, ll, nf, p, h, th, o); }

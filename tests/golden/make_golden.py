@@ -133,6 +133,24 @@ def main():
             for m in (1, 3):
                 out[f"and_{name}_m{m}_{tag}"] = O.anderson(x0.astype(dt), fs.astype(dt), m, 1.0,
                                                            0.02, invs, fscale=0.5, ref=True)
+    # S and H as getLocalOverlap / computeLocalProduct form them, summed by
+    # LocalMatrices2DistMatrix (1e-14 filter): a dense case and narrow,
+    # well separated orbitals whose far pairs the filter drops
+    for case, (n, h, sig, nf, seed) in {"a": ((16, 12, 20), 0.35, (1.0, 2.0), 7, 1004),
+                                        "b": ((24, 24, 24), 0.6, (0.5, 0.6), 6, 1006)}.items():
+        ll = tuple(x * h for x in n)
+        psi, _, _ = synth.gaussian_orbitals(n, ll, nf, seed, sigma=sig)
+        V = synth.gaussian_wells(n, ll, 4, seed)
+        out[f"sh{case}_n"] = np.array(n)
+        out[f"sh{case}_ll"] = np.array(ll)
+        out[f"sh{case}_psi"] = psi
+        out[f"sh{case}_V"] = V
+        for tag, dt in (("d", np.float64), ("f", np.float32)):
+            p = psi.astype(dt)
+            hp = O.hpsi(n, ll, 0, p, V, ref=True).astype(dt)
+            out[f"sh{case}_hpsi_{tag}"] = hp
+            out[f"sh{case}_S_{tag}"] = O.gram(p, h ** 3, ref=True)
+            out[f"sh{case}_H_{tag}"] = O.hmat(p, hp, h ** 3, ref=True)
     np.savez_compressed(os.path.join(HERE, "ref_vectors.npz"), **out)
     print("wrote", os.path.join(HERE, "ref_vectors.npz"), len(out), "arrays")
 

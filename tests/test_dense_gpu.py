@@ -110,3 +110,30 @@ def test_theta_from_cholesky(n):
     t = float(tr.cpu()[0])
     tref = O.trace_prod(H, Sinv)
     assert abs(t - tref) < 1e-12 * max(1.0, abs(tref)) * n
+
+
+@pytest.mark.parametrize("case", ["a", "b"])
+def test_gram_hmat_match_reference_golden(case):
+    """The GPU's FP64 S and H against the reference's own getLocalOverlap /
+    computeLocalProduct and LocalMatrices2DistMatrix (recorded vectors):
+    1e-12 relative and the same entries dropped by the 1e-14 filter; for
+    FP32 orbitals (split-BF16x3 on the tensor cores) the product tolerance,
+    against the reference's USE_MP matrices."""
+    from helpers import golden
+    g = golden()
+    n = tuple(int(x) for x in g[f"sh{case}_n"])
+    ll = tuple(float(x) for x in g[f"sh{case}_ll"])
+    ctx = capi.Context(n, ll)
+    psi = g[f"sh{case}_psi"]
+    S = ctx.gram(_dev(psi)).cpu().numpy()
+    H = ctx.hmat(_dev(psi), _dev(g[f"sh{case}_hpsi_d"])).cpu().numpy()
+    S_ref, H_ref = g[f"sh{case}_S_d"], g[f"sh{case}_H_d"]
+    assert rel_err(S, S_ref) < TOL_F64
+    assert rel_err(H, H_ref) < TOL_F64
+    assert np.array_equal(S == 0, S_ref == 0)
+    assert np.array_equal(H == 0, H_ref == 0)
+    p32 = _dev(psi, np.float32)
+    S32 = ctx.gram(p32, mode=capi.GEMM_BF16X3).cpu().numpy()
+    H32 = ctx.hmat(p32, _dev(g[f"sh{case}_hpsi_f"], np.float32), mode=capi.GEMM_BF16X3).cpu().numpy()
+    assert rel_err(S32, g[f"sh{case}_S_f"]) < 2e-5
+    assert rel_err(H32, g[f"sh{case}_H_f"]) < 2e-5

@@ -242,6 +242,37 @@ def test_gram_matrix_cholesky_and_loewdin():
     assert info2 > 0
 
 
+@pytest.mark.parametrize("case", ["a", "b"])
+@pytest.mark.parametrize("tag,dt", [("d", np.float64), ("f", np.float32)])
+def test_gram_and_hmat_match_reference_golden(case, tag, dt):
+    """S and H bit for bit against the reference's getLocalOverlap /
+    computeLocalProduct through LocalMatrices2DistMatrix (its 1e-14 filter
+    drops the far pairs of case b).  For FP32 orbitals the reference's
+    USE_MP path keeps each product in a float local matrix; the oracle's
+    usemp form restates it, and its default FP64 sum is within that
+    rounding."""
+    g = golden()
+    n = tuple(int(x) for x in g[f"sh{case}_n"])
+    h = float(g[f"sh{case}_ll"][0]) / n[0]
+    vel = h ** 3
+    p = g[f"sh{case}_psi"].astype(dt)
+    hp = g[f"sh{case}_hpsi_{tag}"]
+    S_ref, H_ref = g[f"sh{case}_S_{tag}"], g[f"sh{case}_H_{tag}"]
+    assert np.array_equal(O.gram(p, vel, usemp=True), S_ref)
+    assert np.array_equal(O.hmat(p, hp, vel, usemp=True), H_ref)
+    if case == "b":
+        assert np.count_nonzero(S_ref == 0) > 0
+    if dt == np.float32:
+        # the FP64 sum the mixed-precision GPU path is measured against
+        mask = S_ref != 0
+        S = O.gram(p, vel)
+        assert np.max(np.abs(S - S_ref)[mask] / np.abs(S_ref)[mask]) <= 2.0 ** -24
+        assert np.array_equal(S == 0, S_ref == 0)
+    if O.ref_lib() is not None:
+        assert np.array_equal(O.gram(p, vel, ref=True), S_ref)
+        assert np.array_equal(O.hmat(p, hp, vel, ref=True), H_ref)
+
+
 def test_gram_and_hmat_oracle_vs_numpy():
     n = (8, 8, 8)
     ll = (2.8, 2.8, 2.8)
