@@ -128,13 +128,27 @@ def _peaks():
 
 
 # --------------------------------------------------------------------- CPU leg
-def cpu_sweep_estimate(cfg, sample_funcs=4):
-    """Times the oracle port (all host threads) of one sweep on
-    `sample_funcs` orbitals of the workload grid and extrapolates to N:
-    normalize, H psi, the B psi of computeMatB, the V-cycle and the
-    residual stencil scale with N; S, H, B and Psi Theta with N^2 (B as the
-    reference forms it, full N x N).  The N x N FP64 algebra is not timed
-    (a few GFLOP against the products' tens of TFLOP)."""
+def _omp_threads(n):
+    """Sets the OpenMP thread count of the oracle's parallel regions entered
+    from this thread (the oracle links the process's one OpenMP runtime)."""
+    import ctypes
+    for name in ("libgomp.so.1", "libgomp.so"):
+        try:
+            ctypes.CDLL(name).omp_set_num_threads(int(n))
+            return True
+        except OSError:
+            continue
+    return False
+
+
+def cpu_sweep_estimate(cfg, sample_funcs=4, products=True):
+    """Times the oracle port of one sweep on `sample_funcs` orbitals of the
+    workload grid and extrapolates to N: normalize, H psi, the B psi of
+    computeMatB, the V-cycle and the residual stencil scale with N; S, H, B
+    and Psi Theta with N^2 (B as the reference forms it, full N x N).  The
+    N x N FP64 algebra is not timed (a few GFLOP against the products' tens
+    of TFLOP).  Returns the seconds of the linear and the quadratic part per
+    sweep (the quadratic part only when `products`)."""
     import numpy as np
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
@@ -150,13 +164,14 @@ def cpu_sweep_estimate(cfg, sample_funcs=4):
     O.normalize(n, ll, psi)
     hp = O.hpsi(n, ll, 0, psi, V)
     O.rhs_mehr(n, ll, psi)
-    t1 = time.perf_counter()
     O.precond(n, ll, 0, 2, 0.2, hp)
-    t2 = time.perf_counter()
     # the linear part of the residual (B applied to the product) and the update
     th = np.eye(sample_funcs)
     O.residual(n, ll, psi, hp.astype(np.float32), th, 1)
-    t2b = time.perf_counter()
+    t1 = time.perf_counter()
+    lin = (t1 - t0) * (N / sample_funcs)
+    if not products:
+        return {"linear_s": lin, "quadratic_s": None, "sample_s": t1 - t0}
     # S, H and Psi Theta on a 128-orbital x 2^19-point slab: time per
     # (pair, point) of each product
     ns, ks = 128, min(1 << 19, n[0] * n[1] * n[2])
@@ -172,42 +187,105 @@ def cpu_sweep_estimate(cfg, sample_funcs=4):
     pairs_s = ns * (ns + 1) / 2 + ns * ns
     per_pair_point = (t4 - t3) / (pairs_s * ks)
     per_mm = (t5 - t4) / (ns * ns * ks)
-    lin = (t2b - t0) * (N / sample_funcs)
     quad = per_pair_point * (N * (N + 1) / 2 + 2 * N * N) * P + per_mm * N * N * P
-    per_sweep = lin + quad
-    t4 = t5
+    return {"linear_s": lin, "quadratic_s": quad, "sample_s": (t1 - t0) + (t5 - t3)}
+
+
+def cpu_baseline(cfg, sample_funcs, reps=1, as_written_funcs=4):
+    """The CPU baseline of one sweep: the median of `reps` samples of the
+    oracle port on all host threads (orbital-parallel stencils), and the
+    reference as written, whose Mehrstellen kernels (FDkernelDel2_4th_Mehr,
+    FDkernelRHS_4th_Mehr1, src/pb/FDkernels.cc:447-584) carry no OpenMP:
+    the stencil phases timed on one thread, the products (threaded BLAS in
+    the reference) on all threads."""
+    import statistics
     cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
-    return {
-        "value": 1.0 / per_sweep, "unit": "sweeps/s", "cores": cores, "kind": "port",
+    samples = [cpu_sweep_estimate(cfg, sample_funcs) for _ in range(max(1, reps))]
+    per = statistics.median(s["linear_s"] + s["quadratic_s"] for s in samples)
+    quad = statistics.median(s["quadratic_s"] for s in samples)
+    out = {
+        "value": 1.0 / per, "unit": "sweeps/s", "cores": cores, "kind": "port",
         "sample": (f"oracle port of the reference loops (FP32 data, FP64 accumulation as the "
-                   f"USE_MP build), {cores} threads: normalize, H psi, B psi, V-cycle and the "
-                   f"residual stencil on {sample_funcs} of {N} orbitals ({n[0]}^3), scaled by N; "
-                   f"S, H, B and Psi Theta timed on a {ns}-orbital x {ks}-point slab, scaled by "
-                   f"pairs x points; N x N FP64 algebra not timed; sample took {t4 - t0:.1f} s"),
-        "seconds_per_sweep": per_sweep,
+                   f"USE_MP build), {cores} threads, median of {len(samples)}: normalize, H psi, "
+                   f"B psi, V-cycle and the residual stencil on {sample_funcs} of {cfg['nfunc']} "
+                   f"orbitals ({cfg['n'][0]}^3), scaled by N; S, H, B and Psi Theta timed on a "
+                   f"128-orbital x 524288-point slab, scaled by pairs x points; N x N FP64 "
+                   f"algebra not timed; one sample took {samples[0]['sample_s']:.1f} s"),
+        "seconds_per_sweep": per,
     }
+    if as_written_funcs:
+        aw = as_written(cfg, quad, cores, as_written_funcs)
+        if aw:
+            out["as_written"] = aw
+    return out
+
+
+def as_written(cfg, quad_s, cores, funcs=4):
+    """The reference as written: its stencil phases on one thread (sampled
+    on `funcs` orbitals, scaled by N) plus the products' `quad_s` seconds on
+    all threads; None when the OpenMP runtime cannot be reached."""
+    if not _omp_threads(1):
+        return None
+    try:
+        lin1 = cpu_sweep_estimate(cfg, funcs, products=False)["linear_s"]
+    finally:
+        _omp_threads(cores)
+    return {"value": 1.0 / (lin1 + quad_s), "unit": "sweeps/s", "cores": cores,
+            "sample": (f"stencil phases on 1 thread ({funcs} orbitals, scaled by N), products "
+                       f"on {cores} threads as in the main sample")}
+
+
+def _config(cfg, args, use_matb=None, chunk=0, net=False, world=1):
+    """The config object of the JSON line (the same keys for both arms)."""
+    mode = args.mode
+    return {"workload": cfg["workload"], "grid": list(cfg["n"]), "h": cfg["h"],
+            "orbitals": cfg["nfunc"], "mode": mode,
+            "gemm": args.gemm if mode == "mixed" else "fp64", "lap_type": "mehrstellen",
+            "precond": "learned U-Net, warm-started V-cycle, per-function V-cycle fallback"
+            if net else "V-cycle 2 coarse levels",
+            "theta": "B^-1 H (ProjectedMatricesMehrstellen)"
+            if (args.theta == "b" if use_matb is None else use_matb)
+            else "S^-1 H (ProjectedMatrices)",
+            "schedule": f"column chunks of {chunk}" if chunk else "full blocks",
+            "l2": "inputs larger than L2 (no flush)", "parallelism": f"replicas x{world}"}
 
 
 def run_reference(args, cfg):
     rank = _env_int("RANK", 0)
     if rank != 0:
         return 0
+    import statistics
     os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count() or 1))
-    vals = []
-    for _ in range(max(1, args.warmup and 0) + args.steps):
-        vals.append(cpu_sweep_estimate(cfg, sample_funcs=args.cpu_sample))
-    best = vals[-1]
+    cores = int(os.environ["OMP_NUM_THREADS"])
+    # each step is one bounded sample of the sweep on the host cores
+    per, quad = [], []
+    first = None
+    for _ in range(args.steps):
+        e = cpu_sweep_estimate(cfg, sample_funcs=args.cpu_sample)
+        first = first or e
+        per.append(e["linear_s"] + e["quadratic_s"])
+        quad.append(e["quadratic_s"])
+    sec = statistics.median(per)
+    aw = as_written(cfg, statistics.median(quad), cores) if args.as_written else None
     line = {
-        "impl": "reference", "metric": METRIC, "value": best["value"], "unit": "sweeps/s",
+        "impl": "reference", "metric": METRIC, "value": 1.0 / sec, "unit": "sweeps/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": 1e3 * best["seconds_per_sweep"], "higher_is_better": True,
+        "ms_per_step": 1e3 * sec, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": cfg["workload"], "grid": list(cfg["n"]), "h": cfg["h"],
-                   "orbitals": cfg["nfunc"]},
-        "cpu_baseline": {k: best[k] for k in ("value", "unit", "cores", "kind", "sample")},
-        "e2e": {"value": best["value"], "unit": "sweeps/s", "h2d_bytes_per_step": 0,
+        "config": _config(cfg, args, chunk=0),
+        "cpu_baseline": {
+            "value": 1.0 / sec, "unit": "sweeps/s", "cores": cores, "kind": "port",
+            "sample": (f"oracle port of the reference loops (FP32 data, FP64 accumulation as "
+                       f"the USE_MP build), {cores} threads, median of {len(per)} samples: "
+                       f"stencil phases on {args.cpu_sample} of {cfg['nfunc']} orbitals scaled "
+                       f"by N, products on a 128-orbital x 524288-point slab scaled by pairs x "
+                       f"points; N x N FP64 algebra not timed; one sample took "
+                       f"{first['sample_s']:.1f} s")},
+        "e2e": {"value": 1.0 / sec, "unit": "sweeps/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
+    if aw:
+        line["cpu_baseline"]["as_written"] = aw
     print(json.dumps(line), flush=True)
     return 0
 
@@ -327,7 +405,7 @@ def run_gpu(args, cfg):
         t0 = torch.cuda.Event(enable_timing=True)
         t1 = torch.cuda.Event(enable_timing=True)
         t0.record()
-        ksteps = max(1, min(args.steps, 3))
+        ksteps = args.steps
         for _ in range(ksteps):
             capi.copy(dev, host)   # SM-driven copy of the pinned host block
             ee = sw.run(dev)
@@ -340,6 +418,37 @@ def run_gpu(args, cfg):
                "h2d_bytes_per_step": int(host.numel() * host.element_size()),
                "d2h_bytes_per_step": int(8 + N * N * 8), "steps": ksteps}
 
+    # the energy gate: the accurate energy of the final block against the
+    # sweep's own, at this workload; and both iterations run to convergence
+    # on a small configuration
+    echeck = None
+    use_matb, sched_chunk = sw.use_matb, sw.chunk
+    if args.energy_check and mode == "mixed" and use_matb:
+        from mgmol_gb300 import convergence
+        V64 = V.to(torch.float64) if V.dtype != torch.float64 else V
+        e_sweep = float(sw.run(psi, update=False).cpu()[0])
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e_acc = convergence.energy_accurate(ctx, V64, psi, chunk=64, hp=sw.hpsi, bp=sw.corr)
+        t_acc = time.perf_counter() - t0
+        del V64
+        echeck = {"workload": {"E_sweep_ha": e_sweep, "E_accurate_ha": e_acc,
+                               "sweep_minus_accurate_ha": e_sweep - e_acc,
+                               "accurate_evaluation_s": t_acc}}
+        del sw, psi
+        torch.cuda.empty_cache()
+        g = convergence.run((48, 48, 48), 0.35, 32, 8, 1001, tol_ha=1e-8)
+        echeck["converged"] = {
+            "config": "32 orbitals on 48^3, h=0.35, 8 wells, seed 1001; DFTsolver energy test "
+                      "at 1e-8 Ha on both paths",
+            "plain_sweeps": g["plain"]["sweeps"], "mixed_sweeps": g["mixed"]["sweeps"],
+            "mixed_accurate_evaluations": g["mixed"]["evaluations"],
+            "E_plain_ha": g["plain"]["E_ha"], "E_mixed_ha": g["mixed"]["E_ha"],
+            "abs_dE_ha": g["mixed"]["abs_dE_vs_plain_ha"],
+            "max_abs_dE_same_sweep_ha": g["mixed"]["max_abs_dE_same_sweep_ha"],
+            "plain_s": g["plain"]["seconds"], "mixed_s": g["mixed"]["seconds"],
+            "converged": bool(g["plain"]["converged"] and g["mixed"]["converged"])}
+
     if rank != 0:
         return 0
     hbm, bf16, bf16s, peak_kind = _peaks()
@@ -348,7 +457,7 @@ def run_gpu(args, cfg):
     # algorithmic work per sweep phase
     hpsi_bytes = N * npts * 2 * s + npts * s
     # S and B lower triangles including the diagonal, H full
-    gram_flops = (2 if sw.use_matb else 1) * N * (N + 1) * npts + 2.0 * N * N * npts
+    gram_flops = (2 if use_matb else 1) * N * (N + 1) * npts + 2.0 * N * N * npts
     shares = {k: v / sum(phases.values()) for k, v in phases.items()}
     dominant = max(phases, key=phases.get)
     # the tensor-core kernels themselves (event-timed launches inside the
@@ -373,22 +482,24 @@ def run_gpu(args, cfg):
         k_ms = tk_ms / tk_n                       # one launch on average
         per_launch = gram_flops / (tk_n / args.steps)
         achieved = per_launch / (k_ms * 1e-3) / 1e12
+        # timed inside a seconds-long loop of sweeps: the sustained peak
         roof = {"kernel": "gram_kernel (tcgen05 split-K: S, H, B)", "bound": "tensor",
-                "achieved": achieved, "peak": bf16, "unit": "TFLOP/s", "frac": achieved / bf16,
+                "achieved": achieved, "peak": bf16s, "peak_burst": bf16, "unit": "TFLOP/s",
+                "frac": achieved / bf16s,
                 "traffic": (SPLITK_DRAM_BYTES_PER_LAUNCH
                             if (cfg["workload"] == CONFIGS["c5"]["workload"] and mode == "mixed"
                                 and args.gemm == "bf16x3") else None),
                 "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of the nine "
                                   "split-K launches of one sweep, averaged per launch; algorithmic "
                                   f"{SPLITK_ALGO_BYTES_PER_LAUNCH:.3e} B per launch",
-                "issued_frac": nprod * achieved / bf16,
-                "algorithmic": f"{gram_flops:.3e} flop per sweep (S{' and B' if sw.use_matb else ''} "
+                "issued_frac": nprod * achieved / bf16s,
+                "algorithmic": f"{gram_flops:.3e} flop per sweep (S{' and B' if use_matb else ''} "
                                f"lower incl. diagonal + H) over {tk_n / args.steps:.0f} launches"}
     elif dominant == "gram":
         achieved = gram_flops / (phases["gram"] * 1e-3) / 1e12
         roof = {"kernel": "gram+hmat phase", "bound": "tensor", "achieved": achieved, "peak": bf16,
                 "unit": "TFLOP/s", "frac": achieved / bf16, "traffic": None,
-                "algorithmic": f"{gram_flops:.3e} flop per sweep (S{' and B' if sw.use_matb else ''} "
+                "algorithmic": f"{gram_flops:.3e} flop per sweep (S{' and B' if use_matb else ''} "
                                f"lower incl. diagonal + H)"}
     elif dominant == "residual":
         rflops = 2.0 * N * N * npts
@@ -413,15 +524,8 @@ def run_gpu(args, cfg):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32" if dt == torch.float32 else "f64",
         "data": "synthetic (seeded Gaussian orbitals and wells generated on the device)",
-        "config": {"workload": cfg["workload"], "grid": list(n), "h": cfg["h"], "orbitals": N,
-                   "mode": mode, "gemm": args.gemm if mode == "mixed" else "fp64",
-                   "lap_type": "mehrstellen",
-                   "precond": "V-cycle 2 coarse levels" if net is None else
-                   "learned U-Net, warm-started V-cycle, per-function V-cycle fallback",
-                   "theta": "B^-1 H (ProjectedMatricesMehrstellen)" if sw.use_matb
-                   else "S^-1 H (ProjectedMatrices)",
-                   "schedule": f"column chunks of {sw.chunk}" if sw.chunk else "full blocks",
-                   "l2": "inputs larger than L2 (no flush)", "parallelism": f"replicas x{world}"},
+        "config": _config(cfg, args, use_matb=use_matb, chunk=sched_chunk, net=net is not None,
+                          world=world),
         "phases_ms": phases, "phase_share": shares, "energy_trace_ry": energy,
         "roofline": roof, "tensor_kernels": kernels, "gpu_launches": launches,
         "clocks": clocks.summary(),
@@ -431,11 +535,221 @@ def run_gpu(args, cfg):
                            "functions": N}
     if e2e:
         line["e2e"] = e2e
+    if echeck:
+        line["energy_check"] = echeck
     if not args.no_cpu:
-        line["cpu_baseline"] = {k: v for k, v in cpu_sweep_estimate(cfg, args.cpu_sample).items()
+        line["cpu_baseline"] = {k: v for k, v in cpu_baseline(cfg, args.cpu_sample).items()
                                 if k != "seconds_per_sweep"}
     print(json.dumps(line), flush=True)
     return 0
+
+
+# ----------------------------------------------------------- per-kernel timing
+def _time(fn, warmup, reps):
+    import torch
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(reps):
+        fn()
+    b.record()
+    torch.cuda.synchronize()
+    return a.elapsed_time(b) / reps
+
+
+def micro(argv=None):
+    """Per-kernel timing at a chosen shape (python bench.py --micro OP ...):
+    each operation through the C ABI on device-resident seeded inputs,
+    --warmup untimed and --reps timed calls between CUDA events on the
+    current stream; one JSON line per operation with milliseconds per call
+    and the rate on its algorithmic work (flop for the products, bytes for
+    the stencil passes)."""
+    import torch
+    from mgmol_gb300 import capi, synth
+    from mgmol_gb300.sweep import vcycle_bytes
+    GEMM = {"fp64": capi.GEMM_FP64, "fp32": capi.GEMM_FP32, "tf32": capi.GEMM_TF32,
+            "bf16x3": capi.GEMM_BF16X3, "fp16x3": capi.GEMM_FP16X3}
+    ap = argparse.ArgumentParser(prog="bench.py --micro")
+    ap.add_argument("op", choices=["gram", "hmat", "gram_hmat", "matb", "gram_hmat_matb", "mult",
+                                   "residual", "hpsi", "precond", "mgm", "dense", "dense_b",
+                                   "dense_parts", "normalize", "mult_reuse", "h2d", "h2d_kernel",
+                                   "all"])
+    ap.add_argument("--streams", type=int, default=1, help="h2d: concurrent copy streams")
+    ap.add_argument("--grid", type=int, nargs=3, default=[96, 96, 32])
+    ap.add_argument("--h", type=float, default=0.25)
+    ap.add_argument("--nfunc", type=int, default=2048)
+    ap.add_argument("--gemm", default="bf16x3", choices=sorted(GEMM))
+    ap.add_argument("--fp64", action="store_true", help="FP64 orbitals (GEMM mode fp64)")
+    ap.add_argument("--warmup", type=int, default=2)
+    ap.add_argument("--reps", type=int, default=5)
+    args = ap.parse_args(argv)
+    torch.manual_seed(0)
+
+    n = tuple(args.grid)
+    ll = tuple(x * args.h for x in n)
+    N = args.nfunc
+    dt = torch.float64 if args.fp64 else torch.float32
+    mode = capi.GEMM_FP64 if args.fp64 else GEMM[args.gemm]
+    ctx = capi.Context(n, ll)
+    npts = ctx.npts
+    s = 8 if args.fp64 else 4
+    psi, _, _ = synth.gaussian_orbitals_device(n, ll, N, 11, dt)
+    V = synth.gaussian_wells_device(n, ll, 16, 11).to(dt)
+    hpsi = ctx.hpsi(psi, V)
+    torch.cuda.synchronize()
+    ops = ["gram", "hmat", "gram_hmat", "matb", "gram_hmat_matb", "mult", "residual", "hpsi",
+           "precond", "dense", "dense_b", "normalize", "mgm"] \
+        if args.op == "all" else [args.op]
+    out = []
+    for op in ops:
+        if op == "gram":
+            ms = _time(lambda: ctx.gram(psi, mode), args.warmup, args.reps)
+            work, unit = N * (N + 1) * npts, "TFLOP/s"
+        elif op == "hmat":
+            ms = _time(lambda: ctx.hmat(psi, hpsi, mode), args.warmup, args.reps)
+            work, unit = 2.0 * N * N * npts, "TFLOP/s"
+        elif op == "gram_hmat":
+            ms = _time(lambda: ctx.gram_hmat(psi, hpsi, mode), args.warmup, args.reps)
+            work, unit = N * (N + 1) * npts + 2.0 * N * N * npts, "TFLOP/s"
+        elif op == "matb":
+            wb = torch.empty_like(psi)
+            ms = _time(lambda: ctx.matb(psi, mode, work=wb), args.warmup, args.reps)
+            del wb
+            work, unit = N * (N + 1) * npts, "TFLOP/s"
+        elif op == "gram_hmat_matb":
+            wb = torch.empty_like(psi)
+            ms = _time(lambda: ctx.gram_hmat_matb(psi, hpsi, mode, work=wb), args.warmup, args.reps)
+            del wb
+            work, unit = 2 * N * (N + 1) * npts + 2.0 * N * N * npts, "TFLOP/s"
+        elif op == "dense_parts":
+            # each FP64 piece of the dense phase on its own (N from --nfunc)
+            S, H, Bm = ctx.gram_hmat_matb(psi, hpsi, mode)
+            L = ctx.cholesky(S)
+            Sinv = ctx.inverse_from_cholesky(L).contiguous()
+            th = ctx.theta(Sinv, H)
+            parts = {
+                "cholesky": (lambda: ctx.cholesky(S), N ** 3 / 3),
+                "inverse_from_cholesky": (lambda: ctx.inverse_from_cholesky(L), N ** 3),
+                "theta_symm": (lambda: ctx.theta(Sinv, H), 2 * N ** 3),
+                "theta_from_cholesky": (lambda: ctx.theta_from_cholesky(L, H), 2 * N ** 3),
+                "update_hb": (lambda: ctx.update_hb(S, th), 2 * N ** 3),
+                "trace_prod": (lambda: ctx.trace_prod(H, Sinv), 2 * N ** 2),
+            }
+            for name, (fn, fl) in parts.items():
+                pms = _time(fn, args.warmup, args.reps)
+                line = {"op": "dense_parts", "part": name, "nfunc": N, "ms": pms,
+                        "achieved": fl / (pms * 1e-3) / 1e12, "unit": "TFLOP/s"}
+                out.append(line)
+                print(json.dumps(line), flush=True)
+            continue
+        elif op == "normalize":
+            ms = _time(lambda: ctx.normalize(psi), args.warmup, args.reps)
+            work, unit = 3 * N * npts * s, "GB/s"
+        elif op == "mult_reuse":
+            # Psi Theta reading the Gram product's conversion of psi (MN-major A)
+            th = (torch.eye(N, dtype=torch.float64, device="cuda")
+                  + torch.randn(N, N, dtype=torch.float64, device="cuda") / N)
+            dst = torch.empty_like(psi)
+            ctx.set_reuse_conversion(True)
+            ctx.gram(psi, mode)
+            ms = _time(lambda: ctx.mult_matrix(psi, th, mode, out=dst), args.warmup, args.reps)
+            ctx.set_reuse_conversion(False)
+            del dst
+            work, unit = 2.0 * N * N * npts, "TFLOP/s"
+        elif op in ("mult", "residual"):
+            th = (torch.eye(N, dtype=torch.float64, device="cuda")
+                  + torch.randn(N, N, dtype=torch.float64, device="cuda") / N)
+            dst = torch.empty_like(psi)
+            if op == "mult":
+                ms = _time(lambda: ctx.mult_matrix(psi, th, mode, out=dst), args.warmup, args.reps)
+            else:
+                work_blk = torch.empty_like(psi)
+                ms = _time(lambda: ctx.residual(psi, hpsi, th, mode, True, work=work_blk, out=dst),
+                           args.warmup, args.reps)
+                del work_blk
+            del dst
+            work, unit = 2.0 * N * N * npts, "TFLOP/s"
+        elif op == "hpsi":
+            dst = torch.empty_like(psi)
+            ms = _time(lambda: ctx.hpsi(psi, V, out=dst), args.warmup, args.reps)
+            del dst
+            work, unit = N * npts * 2 * s + npts * s, "GB/s"
+        elif op == "precond":
+            dst = torch.empty_like(psi)
+            gamma = ctx.gamma(capi.LAP_MEHR4, 2, float(V.max()), float(V.min()))
+            ms = _time(lambda: ctx.precond_mg(hpsi, capi.LAP_MEHR4, 2, gamma, out=dst),
+                       args.warmup, args.reps)
+            del dst
+            work, unit = vcycle_bytes(N, npts, s, 2), "GB/s"
+        elif op == "dense":
+            S, H = ctx.gram_hmat(psi, hpsi, mode)
+
+            def dense():
+                L = ctx.cholesky(S)
+                Sinv = ctx.inverse_from_cholesky(L)
+                ctx.trace_prod(H, Sinv.contiguous())
+                ctx.theta(Sinv, H)
+            ms = _time(dense, args.warmup, args.reps)
+            work, unit = (N ** 3 / 3 + 4 * N ** 3 / 3 + 2 * N ** 3), "TFLOP/s"
+        elif op == "dense_b":
+            # the dense algebra of the Mehrstellen step: S^-1, theta = B^-1 H by
+            # substitution, HB = sym(S theta), tr(HB S^-1)
+            S, H, Bm = ctx.gram_hmat_matb(psi, hpsi, mode)
+
+            def dense_b():
+                Sinv = ctx.inverse_from_cholesky(ctx.cholesky(S)).contiguous()
+                th, _ = ctx.theta_from_cholesky(ctx.cholesky(Bm), H)
+                ctx.trace_prod(ctx.update_hb(S, th), Sinv)
+            ms = _time(dense_b, args.warmup, args.reps)
+            work, unit = (2 * N ** 3 / 3 + 4 * N ** 3 / 3 + 2 * N ** 3 + 2 * N ** 3), "TFLOP/s"
+        elif op == "h2d":
+            # pinned host block -> device block, split over --streams streams
+            host = torch.empty(psi.shape, dtype=dt, pin_memory=True)
+            host.copy_(psi)
+            dst = torch.empty_like(psi)
+            streams = [torch.cuda.Stream() for _ in range(args.streams)]
+            parts = list(zip(host.chunk(args.streams), dst.chunk(args.streams)))
+
+            def copy():
+                cur = torch.cuda.current_stream()
+                for st, (h, d) in zip(streams, parts):
+                    st.wait_stream(cur)
+                    with torch.cuda.stream(st):
+                        d.copy_(h, non_blocking=True)
+                for st in streams:
+                    cur.wait_stream(st)
+            ms = _time(copy, 1, args.reps)
+            work, unit = host.numel() * host.element_size(), "GB/s"
+            del host, dst
+        elif op == "h2d_kernel":
+            host = torch.empty(psi.shape, dtype=dt, pin_memory=True)
+            host.copy_(psi)
+            dst = torch.empty_like(psi)
+            ms = _time(lambda: capi.copy(dst, host), 1, args.reps)
+            assert torch.equal(dst, psi)
+            work, unit = host.numel() * host.element_size(), "GB/s"
+            del host, dst
+        elif op == "mgm":
+            rho = V[0:npts].double() - V.double().mean()
+            vh = torch.zeros(npts, dtype=torch.float64, device="cuda")
+
+            def solve():
+                vh.zero_()
+                ctx.mgm(vh, rho, max_sweeps=10, tol=1e-10)
+            ms = _time(solve, 1, max(1, args.reps // 2))
+            work, unit = None, None
+        rate = None
+        if work is not None:
+            scale = 1e12 if unit == "TFLOP/s" else 1e9
+            rate = work / (ms * 1e-3) / scale
+        line = {"op": op, "grid": list(n), "nfunc": N, "dtype": "f64" if args.fp64 else "f32",
+                "gemm": "fp64" if args.fp64 else args.gemm, "ms": ms, "achieved": rate, "unit": unit}
+        out.append(line)
+        print(json.dumps(line), flush=True)
+    return 0
+
 
 
 def main():
@@ -462,6 +776,13 @@ def main():
     ap.add_argument("--train-pairs", type=int, default=256,
                     help="pairs per warm-up sweep the learned preconditioner trains on")
     ap.add_argument("--no-e2e", dest="e2e", action="store_false")
+    ap.add_argument("--no-energy-check", dest="energy_check", action="store_false",
+                    help="skip the accurate energy of the final block and the small "
+                         "converged comparison of the two paths")
+    ap.add_argument("--as-written", action="store_true",
+                    help="reference arm: also time the stencil phases on one thread")
+    if len(sys.argv) > 1 and sys.argv[1] == "--micro":
+        return micro(sys.argv[2:])
     args = ap.parse_args()
     cfg = CONFIGS[args.config]
     if args.impl == "reference":

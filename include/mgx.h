@@ -69,7 +69,9 @@ typedef enum mgx_lap_type
 typedef enum mgx_gemm_mode
 {
     MGX_GEMM_FP64   = 0, /* FP64 data, FP64 FMA (plain path) */
-    MGX_GEMM_FP32   = 1, /* FP32 data, FP32 FMA on CUDA cores */
+    MGX_GEMM_FP32   = 1, /* FP32 data, FP32 FMA on CUDA cores in 8-term
+                          * chains, the chains summed in FP32 over 128
+                          * terms and those sums in double-float (two FP32) */
     MGX_GEMM_TF32   = 2, /* FP32 data, tcgen05 kind::tf32, FP32 accumulate */
     MGX_GEMM_BF16X3 = 3, /* FP32 data split hi+lo bf16, 3 tcgen05 products */
     MGX_GEMM_FP16X3 = 4  /* FP32 data scaled by a power of two and split hi+lo

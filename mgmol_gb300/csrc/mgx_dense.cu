@@ -2,7 +2,9 @@
 // orbital hot path on sm_103a:
 //  - S = Psi^T Psi * vel and H = Psi^T (H Psi) * vel as split-K tall-skinny
 //    products on CUDA cores (FP64 data with FP64 FMA, or FP32 data with FP32
-//    FMA per K-slice), FP64 atomics across slices, then the finishing pass
+//    FMA in a three-level summation ending in double-float within the
+//    K-slice),
+//    FP64 atomics across slices, then the finishing pass
 //    (scale by vel, the |x| > 1e-14 filter of
 //    src/LocalMatrices2DistMatrix.cc:16,60, symmetric fill of S);
 //  - GramMatrix::updateLS / computeInverse (src/GramMatrix.cc:75-191):
@@ -28,6 +30,24 @@ namespace mgx
 /* ------------------------------------------------------------------ */
 constexpr int GT  = 64; // output tile
 constexpr int GKC = 32; // k chunk
+// FP32 data: three-level summation.  FMAs chain over 8 k values; every 8
+// k values that chain's sum is added to a second FP32 sum; every
+// GKC * GRAM_F32_CHAIN = 128 k values the second sum goes into a
+// double-float (hi + lo, two FP32) accumulator by an error-free two-sum.
+// The rounding error then grows like 8 + 16 terms of FP32 rounding instead
+// of the whole K slice's length, for one FP32 add per 8 FMAs and a two-sum
+// per 128.
+constexpr int GRAM_F32_CHAIN = 4;
+constexpr int GRAM_F32_INNER = 8;
+
+/* s + e = a + b exactly (Knuth's two-sum; no reassociation, no multiply to
+ * contract) */
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e)
+{
+    s              = a + b;
+    const float bb = s - a;
+    e              = (a - (s - bb)) + (b - bb);
+}
 
 template <typename T>
 __global__ void __launch_bounds__(256) gram_splitk_kernel(const T* __restrict__ A,
@@ -43,11 +63,19 @@ __global__ void __launch_bounds__(256) gram_splitk_kernel(const T* __restrict__ 
     const int tid   = threadIdx.x;
     const int tx = tid % 16, ty = tid / 16; // 16 x 16 threads, 4x4 outputs each
     T acc[4][4];
+    float mid[4][4];          // FP32 data: the sum of the 8-term chains
+    float hi[4][4], lo[4][4]; // FP32 data: the double-float sum of the chains
 #pragma unroll
     for (int a = 0; a < 4; a++)
 #pragma unroll
         for (int b = 0; b < 4; b++)
+        {
             acc[a][b] = (T)0;
+            mid[a][b] = 0.f;
+            hi[a][b]  = 0.f;
+            lo[a][b]  = 0.f;
+        }
+    int chain = 0;
     for (size_t kc = k0; kc < k1; kc += GKC)
     {
         // 64 rows x 32 k for each operand: 2048 elements, 8 per thread
@@ -83,8 +111,40 @@ __global__ void __launch_bounds__(256) gram_splitk_kernel(const T* __restrict__ 
 #pragma unroll
                 for (int q = 0; q < 4; q++)
                     acc[p][q] += a[p] * b[q];
+            if constexpr (sizeof(T) == 4)
+            {
+                if (kk % GRAM_F32_INNER == GRAM_F32_INNER - 1)
+                {
+#pragma unroll
+                    for (int p = 0; p < 4; p++)
+#pragma unroll
+                        for (int q = 0; q < 4; q++)
+                        {
+                            mid[p][q] += (float)acc[p][q];
+                            acc[p][q] = (T)0;
+                        }
+                }
+            }
         }
         __syncthreads();
+        if constexpr (sizeof(T) == 4)
+        {
+            if (++chain == GRAM_F32_CHAIN || kc + GKC >= k1)
+            {
+                chain = 0;
+#pragma unroll
+                for (int p = 0; p < 4; p++)
+#pragma unroll
+                    for (int q = 0; q < 4; q++)
+                    {
+                        float sum, err;
+                        two_sum(hi[p][q], mid[p][q], sum, err);
+                        hi[p][q] = sum;
+                        lo[p][q] += err;
+                        mid[p][q] = 0.f;
+                    }
+            }
+        }
     }
 #pragma unroll
     for (int p = 0; p < 4; p++)
@@ -92,7 +152,12 @@ __global__ void __launch_bounds__(256) gram_splitk_kernel(const T* __restrict__ 
         for (int q = 0; q < 4; q++)
         {
             const int i = i0 + ty + 16 * p, j = j0 + tx + 16 * q;
-            if (i < n && j < ncols) atomicAdd(&C[(size_t)j * n + i], (double)acc[p][q]);
+            double v;
+            if constexpr (sizeof(T) == 4)
+                v = (double)hi[p][q] + (double)lo[p][q];
+            else
+                v = (double)acc[p][q];
+            if (i < n && j < ncols) atomicAdd(&C[(size_t)j * n + i], v);
         }
 }
 
