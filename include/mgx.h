@@ -665,6 +665,54 @@ int mgx_local_tune(mgx_local* loc, const float* psi, const float* phi, const flo
 int mgx_local_set_config(mgx_local* loc, int shape, int ctas_per_sm, int use_graph);
 int mgx_local_get_config(const mgx_local* loc, int* shape, int* ctas_per_sm, int* use_graph);
 
+/* ---------------------------------------------------------------- */
+/* Snapshots (the restart role of MGmol::dumpRestart / HDFrestart,      */
+/* src/MGmol.cc:1101-1127, src/HDFrestart.cc, without HDF5).            */
+/* ---------------------------------------------------------------- */
+
+/* Element types of snapshot arrays. */
+typedef enum mgx_snap_type
+{
+    MGX_SNAP_F64 = 0,
+    MGX_SNAP_F32 = 1,
+    MGX_SNAP_I32 = 2,
+    MGX_SNAP_U8  = 3
+} mgx_snap_type;
+
+/* One named array of a snapshot: `data` in device or host memory, C order,
+ * ndim <= 4 extents in `shape`. */
+typedef struct mgx_dataset
+{
+    const char* name; /* unique in the file; no quote, backslash or control character */
+    int type;         /* mgx_snap_type */
+    int ndim;
+    size_t shape[4];
+    const void* data;
+} mgx_dataset;
+
+/* Writes the arrays (orbital blocks, potentials, learned weights ...) and
+ * the grid (may be NULL) into one file: a 64-byte fixed header, a JSON
+ * header listing each array's type, shape, offset and CRC-32 with the
+ * caller's `meta_json` (a JSON value, or NULL), and the raw arrays at
+ * 4096-byte aligned offsets.  Device arrays stream through two pinned host
+ * buffers (64 MiB each), the copy of one chunk overlapping the file write
+ * of the previous one, on `stream`; returns once the file is closed.
+ * Counterpart of MGmol::dumpRestart (src/MGmol.cc:1101-1127), whose HDF5
+ * layout (src/HDFrestart.cc) this build cannot produce without HDF5. */
+int mgx_snapshot_write(const char* path, const mgx_grid* grid, const char* meta_json,
+    int ndata, const mgx_dataset* data, void* stream);
+/* The JSON header of a snapshot into json (cap bytes, NUL-terminated);
+ * *len (may be NULL) receives its length.  MGX_BAD_ARG when cap is too
+ * small (json then holds the truncated text). */
+int mgx_snapshot_header(const char* path, char* json, size_t cap, size_t* len);
+/* Reads array `name` into dst (device or host, `bytes` long, which must be
+ * the array's size) on `stream`, checking its CRC-32; returns when the data
+ * are in place.  MGX_BAD_ARG for a missing array, a size mismatch, a short
+ * file or a checksum mismatch.  Counterpart of the restart read of
+ * LocGridOrbitals::read_func_hdf5 (src/LocGridOrbitals.cc:1182). */
+int mgx_snapshot_read(const char* path, const char* name, void* dst, size_t bytes,
+    void* stream);
+
 #ifdef __cplusplus
 }
 #endif

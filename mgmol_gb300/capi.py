@@ -74,6 +74,14 @@ class AndersonInfo(ctypes.Structure):
                 ("theta", ctypes.c_double * ANDERSON_MAX_M)]
 
 
+class Dataset(ctypes.Structure):
+    _fields_ = [("name", ctypes.c_char_p), ("type", ctypes.c_int), ("ndim", ctypes.c_int),
+                ("shape", ctypes.c_size_t * 4), ("data", ctypes.c_void_p)]
+
+
+SNAP_F64, SNAP_F32, SNAP_I32, SNAP_U8 = 0, 1, 2, 3
+
+
 class AdamParams(ctypes.Structure):
     _fields_ = [("lr", ctypes.c_float), ("beta1", ctypes.c_float), ("beta2", ctypes.c_float),
                 ("eps", ctypes.c_float)]
@@ -161,6 +169,10 @@ _SIGS = {
     "mgx_local_get_config": [_vp, _ip, _ip, _ip],
     "mgx_precond_learned": [_vp, _vp, ctypes.POINTER(PrecondParams), _vp, _sz, _vp, _i, _i, _dp,
                             _dp, _ip, _vp],
+    "mgx_snapshot_write": [ctypes.c_char_p, ctypes.POINTER(Grid), ctypes.c_char_p, _i,
+                           ctypes.POINTER(Dataset), _vp],
+    "mgx_snapshot_header": [ctypes.c_char_p, ctypes.c_char_p, _sz, ctypes.POINTER(_sz)],
+    "mgx_snapshot_read": [ctypes.c_char_p, ctypes.c_char_p, _vp, _sz, _vp],
 }
 
 # every entry point declared in include/mgx.h
