@@ -86,8 +86,8 @@ def test_c2_mixed_products_at_the_stated_size():
     # FP32 products on the CUDA cores: 8-term chains, 128-term FP32 sums,
     # double-float totals
     S, H = ctx.gram_hmat(psi32, hp32, capi.GEMM_FP32)
-    assert float((S - S64).abs().max()) / sc < 2e-8
-    assert float((H - H64).abs().max()) / hc < 2e-8
+    assert float((S - S64).abs().max()) / sc < 1e-7
+    assert float((H - H64).abs().max()) / hc < 1e-7
     del S, H
     L = torch.tril(ctx.cholesky(S_all.clone()))
     assert float((L @ L.T - S_all).abs().max()) / sc < 1e-14
