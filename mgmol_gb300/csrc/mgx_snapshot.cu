@@ -308,8 +308,11 @@ extern "C" int mgx_snapshot_write(const char* path, const mgx_grid* grid, const 
         h = header_json(grid, meta_json, ndata, data, off, crc);
         if (fseek(f, (long)SNAP_FIXED, SEEK_SET) != 0 || fwrite(h.data(), 1, h.size(), f) != h.size())
             rc = fail(MGX_BAD_ARG, "snapshot: header rewrite of %s failed", path);
-        // the file ends on the last array's aligned end
-        if (rc == MGX_OK && pos > 0 && (fseek(f, (long)pos - 1, SEEK_SET) != 0 || fputc(0, f) == EOF))
+        // the file ends on the last array's aligned end: a zero byte there
+        // when that end lies past the data (never over the data itself)
+        const size_t data_end = ndata ? off[ndata - 1] + nbytes[ndata - 1] : d0;
+        if (rc == MGX_OK && pos > data_end
+            && (fseek(f, (long)pos - 1, SEEK_SET) != 0 || fputc(0, f) == EOF))
             rc = fail(MGX_BAD_ARG, "snapshot: write of %s failed", path);
     }
     if (fclose(f) != 0 && rc == MGX_OK) rc = fail(MGX_BAD_ARG, "snapshot: close of %s failed", path);

@@ -38,6 +38,17 @@ def test_round_trip_and_header(tmp_path):
     assert np.array_equal(out.numpy(), psi)
 
 
+def test_last_array_filling_its_aligned_block(tmp_path):
+    # an array whose size is a multiple of the 4096-byte alignment, last in
+    # the file: its final byte is data, not padding
+    a = np.arange(1024, dtype=np.float32) + 1.0      # 4096 bytes
+    b = np.arange(512, dtype=np.float64) - 3.5       # 4096 bytes
+    p = tmp_path / "aligned.bin"
+    restart.save(p, a=a, b=b)
+    assert np.array_equal(restart.load(p, "a").numpy(), a)
+    assert np.array_equal(restart.load(p, "b").numpy(), b)
+
+
 def test_refusals(tmp_path):
     p = tmp_path / "snap.bin"
     a = np.arange(1000, dtype=np.float64)
