@@ -132,24 +132,32 @@ def energy_accurate(ctx, V64, psi32, chunk=256, hp=None, bp=None):
     """tr(B^-1 H) of an FP32 block to FP64-class accuracy at FP32 cost.
 
     H psi and B psi come from the FP64 stencils applied to chunks of the
-    block promoted to FP64, rounded back to FP32; H = Psi^T (H Psi) vel and
-    B = Psi^T (B Psi) vel from the CUDA-core FP32 products whose sums end
-    in double-float (MGX_GEMM_FP32); the Cholesky of B,
-    theta = B^-1 H and its trace in FP64.  The sweep's own energy differs:
-    its FP32 stencils and split-K tensor-core products carry an error that
-    grows with the points per orbital and the number of orbitals.  hp, bp:
-    optional FP32 blocks of psi32's shape for H psi and B psi."""
+    block promoted to FP64, each kept as two FP32 blocks, hi = fl32(x) and
+    lo = fl32(x - hi), so that nothing of the FP64 result is lost to the
+    FP32 storage.  H = Psi^T (H Psi) vel and B = Psi^T (B Psi) vel are then
+    the CUDA-core FP32 products of Psi with hi, whose sums end in
+    double-float (MGX_GEMM_FP32), plus the split-BF16x3 tensor-core products
+    of Psi with lo (2^-24 of the total, so their own 1e-5 error does not
+    show); the Cholesky of B, theta = B^-1 H and its trace in FP64.  The
+    sweep's own energy differs: its FP32 stencils and split-K tensor-core
+    products carry an error that grows with the points per orbital and the
+    number of orbitals.  hp, bp: optional FP32 blocks of psi32's shape, the
+    hi and lo halves of one operator's result (H psi, then B psi)."""
     nf = psi32.shape[0]
-    hp = torch.empty_like(psi32) if hp is None else hp
-    bp = torch.empty_like(psi32) if bp is None else bp
-    for f0 in range(0, nf, chunk):
-        f1 = min(nf, f0 + chunk)
-        p = psi32[f0:f1].to(torch.float64)
-        hp[f0:f1] = ctx.hpsi(p, V64, capi.LAP_MEHR4, True).to(torch.float32)
-        bp[f0:f1] = ctx.rhs_mehr(p).to(torch.float32)
-        del p
-    H = ctx.hmat(psi32, hp, capi.GEMM_FP32)
-    B = ctx.hmat(psi32, bp, capi.GEMM_FP32)
+    hi = torch.empty_like(psi32) if hp is None else hp
+    lo = torch.empty_like(psi32) if bp is None else bp
+
+    def product(apply):
+        for f0 in range(0, nf, chunk):
+            f1 = min(nf, f0 + chunk)
+            r = apply(psi32[f0:f1].to(torch.float64))
+            hi[f0:f1] = r.to(torch.float32)
+            lo[f0:f1] = (r - hi[f0:f1].to(torch.float64)).to(torch.float32)
+            del r
+        return ctx.hmat(psi32, hi, capi.GEMM_FP32) + ctx.hmat(psi32, lo, capi.GEMM_BF16X3)
+
+    H = product(lambda p: ctx.hpsi(p, V64, capi.LAP_MEHR4, True))
+    B = product(lambda p: ctx.rhs_mehr(p))
     _, tr = ctx.theta_from_cholesky(ctx.cholesky(B), H)
     return float(tr.cpu()[0])
 
@@ -241,6 +249,48 @@ def run(grid, h, nfunc, wells, seed, tol_ha=1e-8, max_plain=2000, max_mixed=2000
     return out
 
 
+def evaluation_check(grid, h, nfunc, wells, seed, sweeps=20, gemm="bf16x3"):
+    """After `sweeps` mixed sweeps from the seeded orbitals: the sweep's own
+    energy, energy_accurate and a full FP64 evaluation of the same block,
+    with the seconds of the two evaluations (Hartree)."""
+    n = tuple(grid)
+    ll = tuple(x * h for x in n)
+    ctx = capi.Context(n, ll)
+    V64 = synth.gaussian_wells_device(n, ll, wells, seed)
+    psi, _, _ = synth.gaussian_orbitals_device(n, ll, nfunc, seed, torch.float32)
+    gamma = ctx.gamma(capi.LAP_MEHR4, 2, float(V64.max()), float(V64.min()))
+    sw = OrbitalSweep(ctx, V64, nfunc, mode="mixed", gemm=GEMM[gemm], gamma=gamma)
+    for _ in range(sweeps):
+        sw.run(psi)
+    e_sweep = float(sw.run(psi, update=False).cpu()[0])
+    del sw
+    torch.cuda.empty_cache()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    e_acc = energy_accurate(ctx, V64, psi)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    e64 = energy_fp64(ctx, V64, psi, nfunc, gamma)
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    # FP64 products of H psi and B psi rounded to FP32: the share of the
+    # accurate evaluation's error that the rounding of its stencil outputs
+    # makes (the rest is its FP32 products)
+    p64 = psi.to(torch.float64)
+    hp = ctx.hpsi(p64, V64, capi.LAP_MEHR4, True).float().double()
+    H = ctx.hmat(p64, hp, capi.GEMM_FP64)
+    del hp
+    bp = ctx.rhs_mehr(p64).float().double()
+    B = ctx.hmat(p64, bp, capi.GEMM_FP64)
+    del bp, p64
+    _, tr = ctx.theta_from_cholesky(ctx.cholesky(B), H)
+    e_r = float(tr.cpu()[0])
+    return {"grid": list(n), "h": h, "orbitals": nfunc, "sweeps": sweeps, "E_sweep_ha": e_sweep,
+            "E_accurate_ha": e_acc, "E_fp64_ha": e64, "sweep_minus_fp64_ha": e_sweep - e64,
+            "accurate_minus_fp64_ha": e_acc - e64, "rounded_stencils_minus_fp64_ha": e_r - e64,
+            "accurate_s": t1 - t0, "fp64_s": t2 - t1}
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
     ap.add_argument("--grid", type=int, nargs=3, default=[48, 48, 48])
@@ -256,7 +306,14 @@ def main(argv=None):
     ap.add_argument("--gemm", default="bf16x3", choices=sorted(GEMM))
     ap.add_argument("--diagnose", action="store_true",
                     help="energy of the final mixed block under each evaluation precision")
+    ap.add_argument("--eval-only", type=int, default=0, metavar="SWEEPS",
+                    help="no convergence runs: the three evaluations of the block after this "
+                         "many mixed sweeps")
     a = ap.parse_args(argv)
+    if a.eval_only:
+        print(json.dumps(evaluation_check(a.grid, a.h, a.nfunc, a.wells, a.seed, a.eval_only,
+                                          a.gemm)), flush=True)
+        return 0
     res = run(a.grid, a.h, a.nfunc, a.wells, a.seed, a.tol, a.max_plain, a.max_mixed, a.gemm,
               a.every, a.diagnose)
     print(json.dumps(res), flush=True)
