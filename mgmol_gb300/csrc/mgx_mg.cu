@@ -18,6 +18,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <memory>
@@ -731,6 +732,19 @@ int masks_expand(const mgx_masks* M, int level, void* dense, int* host_state,
 /* ------------------------------------------------------------------ */
 /* the V-cycle                                                          */
 /* ------------------------------------------------------------------ */
+/* The second pre-sweep of a level restricts its residual in the same kernel
+ * (OP_JACOBI_RST) unless MGX_FUSED_RESTRICT=0: the residual block is then
+ * neither written nor read again.  The results are the same bits either
+ * way (the restriction keeps restrict_kernel's operation order). */
+static bool fused_restrict()
+{
+    static const bool on = [] {
+        const char* e = getenv("MGX_FUSED_RESTRICT");
+        return !(e && e[0] == '0');
+    }();
+    return on;
+}
+
 struct VCycle
 {
     mgx_ctx* ctx;
@@ -756,7 +770,10 @@ struct VCycle
     double upd_alpha = 0.;
     const double* upd_scale0 = nullptr; // per-function scale of the update (chunk base)
 
-    int jacobi(int l, int cur, bool write_w, bool last = false)
+    // with restricted set, a sweep that writes w may restrict it in the same
+    // kernel into the next level's right-hand side (f[l + 1]) instead of
+    // storing it; *restricted tells the caller that it did
+    int jacobi(int l, int cur, bool write_w, bool last = false, bool* restricted = nullptr)
     {
         PlaneParams p;
         if (last && l == 0 && upd0)
@@ -807,6 +824,20 @@ struct VCycle
             p.n[i] = lev[l].n[i];
         p.mask = mask_slice(masks, l, f0);
         p.err  = err;
+        if (restricted && write_w && !p.upd && masks == nullptr && l < L && fused_restrict())
+        {
+            PlaneParams q = p;
+            q.w           = nullptr;
+            q.coarse      = f[l + 1];
+            q.ldc         = ld[l + 1];
+            const int st  = stencil_launch(OP_JACOBI_RST, l == 0 ? lap_type : 1, dtype, dtype, q,
+                lev[l], jf[l], nf, s);
+            if (st != MGX_UNSUPPORTED)
+            {
+                *restricted = (st == MGX_OK);
+                return st;
+            }
+        }
         return stencil_launch(p.upd ? OP_JACOBI_UPD : OP_JACOBI, l == 0 ? lap_type : 1, dtype,
             dtype, p, lev[l], jf[l], nf, s);
     }
@@ -816,16 +847,20 @@ struct VCycle
     {
         int cur         = 0;
         const int ncycl = (l == L) ? 4 : 2;
+        bool restricted = false;
         for (int it = 0; it < ncycl; it++)
         {
             // without coarse levels the last of these sweeps is the final one
-            const int st = jacobi(l, cur, (it == ncycl - 1) && (l < L), (l == L) && (it == ncycl - 1));
+            const int st = jacobi(l, cur, (it == ncycl - 1) && (l < L), (l == L) && (it == ncycl - 1),
+                &restricted);
             if (st != MGX_OK) return -st - 1;
             cur ^= 1;
         }
         if (l == L) return cur;
-        int st = restrict_launch(dtype, lev[l], w[l], ld[l], f[l + 1], ld[l + 1],
-            nf, mask_slice(masks, l + 1, f0), s);
+        int st = MGX_OK;
+        if (!restricted)
+            st = restrict_launch(dtype, lev[l], w[l], ld[l], f[l + 1], ld[l + 1], nf,
+                mask_slice(masks, l + 1, f0), s);
         if (st != MGX_OK) return -st - 1;
         st = cuda_check(cudaMemsetAsync(v0[l + 1], 0,
                             ld[l + 1] * nf * dtype_size(dtype), s),

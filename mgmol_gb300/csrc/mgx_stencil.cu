@@ -587,37 +587,44 @@ __global__ void __launch_bounds__(256) plane_vec_kernel(PlaneParams p, DevCoef<T
     constexpr int VEC = VH::N;
     constexpr bool EDGES   = (LAP == 0) && !is_rhs_op(OP);
     constexpr bool STAGE_V = (OP == OP_HPSI_B);
+    // OP_JACOBI_RST: the sweep also forms w on the row y0 - 1 and the plane
+    // x0 - 1 (one more staged row and plane), keeps the last three w planes
+    // in a ring and restricts them as each odd plane is done
+    constexpr bool RST = (OP == OP_JACOBI_RST);
+    constexpr int YO   = RST ? 1 : 0;
     extern __shared__ __align__(128) unsigned char smem_raw[];
 
     const int nx = p.n[0], ny = p.n[1], nz = p.n[2];
     const int TY      = p.ty;
-    const int rows    = TY + 2;
+    const int rows    = TY + 2 + YO;
     const int tile_y  = blockIdx.x % p.ntile_y;
     const int tile_x  = blockIdx.x / p.ntile_y;
     const int f       = blockIdx.y;
     const int y0      = tile_y * TY;
     const int x0      = tile_x * p.xc;
     const int xcount  = min(p.xc, nx - x0);
-    const int nplanes = xcount + 2;
+    const int nplanes = xcount + 2 + YO;
     const bool scaled = is_jacobi(OP) && (p.gamma_in != 0.);
     const T gam       = (T)p.gamma_in;
 
     const size_t stage_elems = (size_t)rows * nz;
     T* stages                = reinterpret_cast<T*>(smem_raw);
     T* vstages = reinterpret_cast<T*>(smem_raw + S * stage_elems * sizeof(T));
+    const size_t ring_elems = RST ? (size_t)(TY + 1) * nz : 0;
+    T* wring = reinterpret_cast<T*>(smem_raw + S * stage_elems * sizeof(T) * (STAGE_V ? 2 : 1));
     uint64_t* bars = reinterpret_cast<uint64_t*>(
-        smem_raw + S * stage_elems * sizeof(T) * (STAGE_V ? 2 : 1));
+        smem_raw + S * stage_elems * sizeof(T) * (STAGE_V ? 2 : 1) + 3 * ring_elems * sizeof(T));
 
     const T* ubase = reinterpret_cast<const T*>(scaled ? p.f : p.u)
                      + (size_t)f * (scaled ? p.ldf : p.ldu);
     const T* vbase = reinterpret_cast<const T*>(p.V);
 
-    int ya = y0 - 1, na, nb;
+    int ya = y0 - 1 - YO, na, nb;
     if (ya < 0)
     {
-        na = 1;
+        na = -ya;
         ya += ny;
-        nb = rows - 1;
+        nb = rows - na;
     }
     else if (ya + rows > ny)
     {
@@ -633,7 +640,7 @@ __global__ void __launch_bounds__(256) plane_vec_kernel(PlaneParams p, DevCoef<T
 
     auto issue = [&](int i) {
         const int slot = i % S;
-        const int x    = wrap(x0 - 1 + i, nx);
+        const int x    = wrap(x0 - 1 - YO + i, nx);
         uint64_t* bar  = bars + slot;
         mbar_arrive_expect_tx(bar, bytes);
         T* dst       = stages + slot * stage_elems;
@@ -664,7 +671,7 @@ __global__ void __launch_bounds__(256) plane_vec_kernel(PlaneParams p, DevCoef<T
 
     // group geometry
     const int gpr  = nz / VEC; // groups per row
-    const int ngrp = TY * gpr;
+    const int ngrp = (TY + YO) * gpr;
     int oc[NG], om[NG], op[NG], goff[NG], gy[NG], gz[NG];
     bool val[NG];
 #pragma unroll
@@ -673,13 +680,14 @@ __global__ void __launch_bounds__(256) plane_vec_kernel(PlaneParams p, DevCoef<T
         const int g  = threadIdx.x + k * 256;
         const int y  = g / gpr;
         const int z0 = (g - y * gpr) * VEC;
-        val[k]       = (g < ngrp) && (y0 + y < ny);
+        val[k]       = (g < ngrp) && (y0 - YO + y < ny);
         gy[k]        = y;
         gz[k]        = z0;
         oc[k]        = (y + 1) * nz + z0;
         om[k]        = (y + 1) * nz + (z0 > 0 ? z0 - 1 : nz - 1);
         op[k]        = (y + 1) * nz + (z0 + VEC < nz ? z0 + VEC : 0);
-        goff[k]      = (y0 + y) * nz + z0; // point offset within an x-plane
+        const int yr = y0 - YO + y; // row y0 - 1 of the first tile wraps
+        goff[k]      = (yr < 0 ? yr + ny : yr) * nz + z0; // point offset within an x-plane
     }
     T A1[NG][VEC], B1[NG][VEC], B2[NG][VEC], U1[NG][VEC];
 #pragma unroll
@@ -703,9 +711,9 @@ __global__ void __launch_bounds__(256) plane_vec_kernel(PlaneParams p, DevCoef<T
     int waited = -1;
     for (int i = 0; i < nplanes; i++)
     {
-        const int xe    = x0 + i - 2;
+        const int xe    = x0 + i - 2 - YO;
         const bool emit = (i >= 2);
-        const size_t xoff = (size_t)(emit ? xe : 0) * ny * nz;
+        const size_t xoff = (size_t)(emit ? (xe < 0 ? xe + nx : xe) : 0) * ny * nz;
         V4 pv[NG];
         V4 uv[NG]; // OP_JACOBI_UPD: the block being updated, fetched with pv
         if (POINTWISE && emit && !scaled)
@@ -861,10 +869,55 @@ __global__ void __launch_bounds__(256) plane_vec_kernel(PlaneParams p, DevCoef<T
                             = *reinterpret_cast<const uint2*>(l);
                     }
                 }
-                else
+                else if (!RST || (gy[k] >= YO && xe >= x0))
                     *reinterpret_cast<V4*>(outp + xoff + goff[k]) = res;
-                if (is_jacobi(OP) && wp != nullptr)
+                if (RST)
+                    *reinterpret_cast<V4*>(wring + (size_t)((xe - x0 + 1) % 3) * ring_elems
+                                           + (size_t)gy[k] * nz + gz[k]) = wres;
+                else if (is_jacobi(OP) && wp != nullptr)
                     *reinterpret_cast<V4*>(wp + xoff + goff[k]) = wres;
+            }
+        }
+        if (RST && emit && xe > x0 && ((xe - x0) & 1))
+        {
+            // coarse plane X = (xe - 1) / 2 from the w planes xe - 2 .. xe,
+            // rows y0 - 1 .. y0 + TY - 1 of the ring; the grouping and
+            // order of restrict_kernel (src/pb/MGkernels.cc:249-270)
+            __syncthreads();
+            const int cy = ny >> 1, cz = nz >> 1;
+            const int X  = (xe - 1) >> 1;
+            const int nyc = min(TY, ny - y0) >> 1;
+            const T* Wm   = wring + (size_t)((xe - x0 - 1) % 3) * ring_elems; // plane 2X - 1
+            const T* W0   = wring + (size_t)((xe - x0) % 3) * ring_elems;     // plane 2X
+            const T* Wp   = wring + (size_t)((xe - x0 + 1) % 3) * ring_elems; // plane 2X + 1
+            T* cp         = reinterpret_cast<T*>(p.coarse) + (size_t)f * p.ldc;
+            for (int t = threadIdx.x; t < nyc * cz; t += 256)
+            {
+                const int yl = t / cz, Z = t - (t / cz) * cz;
+                const int z = 2 * Z, zm = z > 0 ? z - 1 : nz - 1, zp = z + 1;
+                const int r = 2 * yl + 1; // ring row of fine y = y0 + 2 yl
+                auto row = [&](const T* P, int dy, T* v3) {
+                    const T* q = P + (size_t)(r + dy) * nz;
+                    v3[0]      = q[zm];
+                    v3[1]      = q[z];
+                    v3[2]      = q[zp];
+                };
+                T r00[3], rp0[3], rm0[3], r0p[3], r0m[3], rpp[3], rpm[3], rmp[3], rmm[3];
+                row(W0, 0, r00);
+                row(Wp, 0, rp0);
+                row(Wm, 0, rm0);
+                row(W0, 1, r0p);
+                row(W0, -1, r0m);
+                row(Wp, 1, rpp);
+                row(Wp, -1, rpm);
+                row(Wm, 1, rmp);
+                row(Wm, -1, rmm);
+                const T face   = rp0[1] + rm0[1] + r0p[1] + r0m[1] + r00[0] + r00[2];
+                const T corner = rpp[0] + rpp[2] + rpm[0] + rpm[2] + rmp[0] + rmp[2] + rmm[0] + rmm[2];
+                const T edge   = r0p[0] + r0p[2] + r0m[0] + r0m[2] + rp0[0] + rp0[2] + rm0[0] + rm0[2]
+                               + rmm[1] + rpm[1] + rmp[1] + rpp[1];
+                cp[((size_t)X * cy + (y0 >> 1) + yl) * cz + Z]
+                    = (T)(1. / 64.) * ((T)8. * r00[1] + (T)4. * face + (T)2. * edge + corner);
             }
         }
         __syncthreads();
@@ -980,10 +1033,21 @@ static int launch_vec(const PlaneParams& p0, const DevCoef<T>& c, int nfunc,
     const int nx = p.n[0], ny = p.n[1], nz = p.n[2];
     const size_t esz = sizeof(T) * (STAGE_V ? 2 : 1);
     const size_t smem_cap = 110 * 1024;
-    int ty = std::min(32, (256 * NG * VEC) / nz);
-    ty     = std::min(ty, ny - 2);
-    for (; ty >= 1; ty--)
-        if ((size_t)S * (ty + 2) * nz * esz + S * 8 <= smem_cap) break;
+    // OP_JACOBI_RST: one more row of groups (y0 - 1), an even tile height,
+    // and three planes of TY + 1 rows of w for the restriction
+    constexpr bool RST = (OP == OP_JACOBI_RST);
+    constexpr int YO   = RST ? 1 : 0;
+    if (RST && ((nx | ny | nz) & 1))
+        return fail(MGX_UNSUPPORTED, "restriction needs even grid dimensions");
+    auto smem_for = [&](int t) {
+        return (size_t)S * (t + 2 + YO) * nz * esz + (RST ? 3 * (size_t)(t + 1) * nz * sizeof(T) : 0)
+               + S * 8;
+    };
+    int ty = std::min(32, (256 * NG * VEC) / nz - YO);
+    ty     = std::min(ty, ny - 2 - YO);
+    if (RST) ty &= ~1;
+    for (; ty >= 1; ty -= RST ? 2 : 1)
+        if (smem_for(ty) <= smem_cap) break;
     if (ty < 1) return fail(MGX_UNSUPPORTED, "plane too large for the vector kernel");
     p.ty      = ty;
     p.ntile_y = (ny + ty - 1) / ty;
@@ -993,7 +1057,7 @@ static int launch_vec(const PlaneParams& p0, const DevCoef<T>& c, int nfunc,
     if (xc > nx) xc = nx;
     p.xc       = xc;
     p.ntile_x  = (nx + xc - 1) / xc;
-    const size_t smem = (size_t)S * (ty + 2) * nz * esz + S * 8;
+    const size_t smem = smem_for(ty);
     auto kern         = plane_vec_kernel<T, LAP == 1 ? 1 : 0, OP, S, NG>;
     cudaError_t e     = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
         (int)smem);
@@ -1008,8 +1072,10 @@ template <typename T, typename TV, int LAP, int OP, int R>
 static int launch_t(const PlaneParams& p0, const DevCoef<T>& c, int nfunc,
     cudaStream_t stream, int force_direct)
 {
-    if (vec_ok<T, TV, LAP, OP, R>(p0, force_direct))
+    if (vec_ok<T, TV, LAP, OP, R>(p0, force_direct) && (OP != OP_JACOBI_RST || !p0.mask.state))
         return launch_vec<T, TV, LAP, OP, R>(p0, c, nfunc, stream);
+    if (OP == OP_JACOBI_RST)
+        return fail(MGX_UNSUPPORTED, "the fused restriction needs the vector kernel, no masks");
     if (p0.gamma_in != 0.)
         return fail(MGX_UNSUPPORTED, "scaled first sweep needs the vector kernel");
     PlaneParams p = p0;
@@ -1137,6 +1203,8 @@ int stencil_launch(int op, int lap_type, int dtype, int v_dtype,
                 return dispatch_lap<double, double, OP_JACOBI>(lap_type, p, c, nfunc, stream, force_direct);
             case OP_JACOBI_UPD:
                 return dispatch_lap<double, double, OP_JACOBI_UPD>(lap_type, p, c, nfunc, stream, force_direct);
+            case OP_JACOBI_RST:
+                return dispatch_lap<double, double, OP_JACOBI_RST>(lap_type, p, c, nfunc, stream, force_direct);
             case OP_HPSI_B:
                 if (v_dtype == MGX_F64)
                     return launch_t<double, double, 0, OP_HPSI_B, 1>(p, c, nfunc, stream, force_direct);
@@ -1158,6 +1226,8 @@ int stencil_launch(int op, int lap_type, int dtype, int v_dtype,
                 return dispatch_lap<float, float, OP_JACOBI>(lap_type, p, c, nfunc, stream, force_direct);
             case OP_JACOBI_UPD:
                 return dispatch_lap<float, float, OP_JACOBI_UPD>(lap_type, p, c, nfunc, stream, force_direct);
+            case OP_JACOBI_RST:
+                return dispatch_lap<float, float, OP_JACOBI_RST>(lap_type, p, c, nfunc, stream, force_direct);
             case OP_HPSI_B:
                 if (v_dtype == MGX_F64)
                     return launch_t<float, double, 0, OP_HPSI_B, 1>(p, c, nfunc, stream, force_direct);

@@ -20,14 +20,19 @@ enum StencilOp
     OP_RHS    = 4, // out = B u
     OP_RHS_SUB = 5, // out = B u - g (g pointwise, passed as f)
     OP_JACOBI_UPD = 6, // OP_JACOBI whose result r is added into upd: upd += upd_alpha r
-    OP_RHS_SPLIT  = 7  // out = B u stored as bf16 hi / lo planes of a tensor-core operand
+    OP_RHS_SPLIT  = 7, // out = B u stored as bf16 hi / lo planes of a tensor-core operand
+    OP_JACOBI_RST = 8  // OP_JACOBI whose residual w is restricted to the next grid in the
+                       // kernel (full weighting into `coarse`) instead of being stored
 };
 
 __host__ __device__ constexpr bool is_rhs_op(int op)
 {
     return op == OP_RHS || op == OP_RHS_SUB || op == OP_RHS_SPLIT;
 }
-__host__ __device__ constexpr bool is_jacobi(int op) { return op == OP_JACOBI || op == OP_JACOBI_UPD; }
+__host__ __device__ constexpr bool is_jacobi(int op)
+{
+    return op == OP_JACOBI || op == OP_JACOBI_UPD || op == OP_JACOBI_RST;
+}
 
 /* Localization masks of one level in box form: for function f, values of
  * the box starting at (box[6f], box[6f+1], box[6f+2]) (periodic) with
@@ -79,6 +84,11 @@ struct PlaneParams
     void* split_hi = nullptr;
     void* split_lo = nullptr;
     int split_rows = 0;
+    // OP_JACOBI_RST only: the restriction of the residual w (the next
+    // level's right-hand side, n/2 points per direction, leading dimension
+    // ldc); no masks
+    void* coarse = nullptr;
+    size_t ldc   = 0;
 };
 
 int stencil_launch(int op, int lap_type, int dtype, int v_dtype,

@@ -1,0 +1,57 @@
+"""The V-cycle with the residual of each level's second pre-sweep
+restricted inside that sweep's kernel (the default) against the V-cycle
+with the residual stored and restricted by its own kernel
+(MGX_FUSED_RESTRICT=0), each in a fresh process (the library reads the
+choice once): the same bits, FP64 and FP32, on grids whose tile rows and
+x chunks end unevenly; and the fused FP64 V-cycle against the oracle."""
+import os
+import subprocess
+import sys
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+SCRIPT = r"""
+import sys
+import numpy as np
+import torch
+sys.path.insert(0, ROOT)
+sys.path.insert(0, ROOT + "/oracle")
+import oracle as O
+from mgmol_gb300 import capi, synth
+
+outs = {}
+for n, nf, maxl in (((32, 28, 36), 5, 2), ((48, 40, 24), 3, 1), ((64, 64, 64), 4, 2)):
+    ll = tuple(x * 0.35 for x in n)
+    res, _, _ = synth.gaussian_orbitals(n, ll, nf, 61)
+    ctx = capi.Context(n, ll)
+    for dt in (torch.float64, torch.float32):
+        for lap in (0, 2):
+            o = ctx.precond_mg(torch.from_numpy(res).to(dtype=dt, device="cuda"), lap, maxl, 0.3)
+            outs[f"{n}_{dt}_{lap}"] = o.cpu().numpy()
+    ref = O.precond(n, ll, 0, maxl, 0.3, res)
+    got = outs[f"{n}_{torch.float64}_0"]
+    assert np.max(np.abs(got - ref)) / np.max(np.abs(ref)) < 1e-12, n
+np.savez(OUT, **outs)
+print("vcycle ok")
+"""
+
+
+def _run(tmp_path, env, tag):
+    out = str(tmp_path / f"{tag}.npz")
+    r = subprocess.run([sys.executable, "-c", SCRIPT.replace("ROOT", repr(ROOT)).replace("OUT", repr(out))],
+                       env={**os.environ, **env}, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0 and "vcycle ok" in r.stdout, r.stdout[-2000:] + r.stderr[-2000:]
+    return np.load(out)
+
+
+def test_fused_restriction_gives_the_same_bits(tmp_path):
+    a = _run(tmp_path, {"MGX_FUSED_RESTRICT": "1"}, "fused")
+    b = _run(tmp_path, {"MGX_FUSED_RESTRICT": "0"}, "separate")
+    assert sorted(a.files) == sorted(b.files)
+    for k in a.files:
+        assert np.array_equal(a[k], b[k]), k
