@@ -181,7 +181,9 @@ def converge_mixed(ctx, V64, sw, psi, tol_ha, every=10, max_steps=2000):
     converged = False
     while k <= max_steps:
         if fine or k % every == 0:
-            e = energy_accurate(ctx, V64, psi)
+            # the sweep's H psi and work blocks are free between sweeps
+            e = energy_accurate(ctx, V64, psi, hp=sw.hpsi, bp=sw.corr) \
+                if sw.corr.shape == psi.shape else energy_accurate(ctx, V64, psi)
             samples.append((k, e))
             if fine:
                 if test.push(e):
@@ -291,6 +293,30 @@ def evaluation_check(grid, h, nfunc, wells, seed, sweeps=20, gemm="bf16x3"):
             "accurate_s": t1 - t0, "fp64_s": t2 - t1}
 
 
+def mixed_only(grid, h, nfunc, wells, seed, tol_ha, max_mixed, gemm="bf16x3", every=10):
+    """The mixed iteration alone, stopped by the energy test on accurate
+    energies or after max_mixed sweeps (for sizes where the plain FP64
+    iteration cannot be run to convergence): the sampled accurate energies,
+    the sweeps, the seconds, and the last mean change per sweep."""
+    n = tuple(grid)
+    ll = tuple(x * h for x in n)
+    ctx = capi.Context(n, ll)
+    V64 = synth.gaussian_wells_device(n, ll, wells, seed)
+    psi, _, _ = synth.gaussian_orbitals_device(n, ll, nfunc, seed, torch.float32)
+    gamma = ctx.gamma(capi.LAP_MEHR4, 2, float(V64.max()), float(V64.min()))
+    sw = OrbitalSweep(ctx, V64, nfunc, mode="mixed", gemm=GEMM[gemm], gamma=gamma)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    m = converge_mixed(ctx, V64, sw, psi, tol_ha, every, max_mixed)
+    torch.cuda.synchronize()
+    m["seconds"] = time.perf_counter() - t0
+    sm = m["samples"]
+    m["last_change_per_sweep_ha"] = (abs(sm[-1][1] - sm[-2][1]) / max(1, sm[-1][0] - sm[-2][0])
+                                     if len(sm) > 1 else None)
+    m.update({"grid": list(n), "h": h, "orbitals": nfunc, "tol_ha": tol_ha})
+    return m
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
     ap.add_argument("--grid", type=int, nargs=3, default=[48, 48, 48])
@@ -306,10 +332,16 @@ def main(argv=None):
     ap.add_argument("--gemm", default="bf16x3", choices=sorted(GEMM))
     ap.add_argument("--diagnose", action="store_true",
                     help="energy of the final mixed block under each evaluation precision")
+    ap.add_argument("--mixed-only", action="store_true",
+                    help="no plain FP64 run: the mixed iteration to --tol or --max-mixed sweeps")
     ap.add_argument("--eval-only", type=int, default=0, metavar="SWEEPS",
                     help="no convergence runs: the three evaluations of the block after this "
                          "many mixed sweeps")
     a = ap.parse_args(argv)
+    if a.mixed_only:
+        print(json.dumps(mixed_only(a.grid, a.h, a.nfunc, a.wells, a.seed, a.tol, a.max_mixed,
+                                    a.gemm, a.every)), flush=True)
+        return 0
     if a.eval_only:
         print(json.dumps(evaluation_check(a.grid, a.h, a.nfunc, a.wells, a.seed, a.eval_only,
                                           a.gemm)), flush=True)
