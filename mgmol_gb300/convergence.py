@@ -128,7 +128,7 @@ def evaluation_errors(ctx, V64, psi32):
     return out
 
 
-def energy_accurate(ctx, V64, psi32, chunk=256, hp=None, bp=None):
+def energy_accurate(ctx, V64, psi32, chunk=64, hp=None, bp=None):
     """tr(B^-1 H) of an FP32 block to FP64-class accuracy at FP32 cost.
 
     H psi and B psi come from the FP64 stencils applied to chunks of the
@@ -154,6 +154,9 @@ def energy_accurate(ctx, V64, psi32, chunk=256, hp=None, bp=None):
             hi[f0:f1] = r.to(torch.float32)
             lo[f0:f1] = (r - hi[f0:f1].to(torch.float64)).to(torch.float32)
             del r
+        # the library's product workspaces come from cudaMalloc, not from
+        # torch's cache: hand back what the FP64 chunks held
+        torch.cuda.empty_cache()
         return ctx.hmat(psi32, hi, capi.GEMM_FP32) + ctx.hmat(psi32, lo, capi.GEMM_BF16X3)
 
     H = product(lambda p: ctx.hpsi(p, V64, capi.LAP_MEHR4, True))

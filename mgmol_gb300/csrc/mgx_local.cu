@@ -324,8 +324,10 @@ __global__ void __launch_bounds__(THREADS, 4) local_step_kernel(StepParams P)
                         if (bz + 1 >= 0 && bz + 1 < e2) m1 = mrow[bz + 1];
                     }
                     const int i = (qy + 1) * C::Z2 + qz + 1;
-                    float l0, l1;
-                    lap_m2(M, X, N, i, C::Z2, P, l0, l1);
+                    // outside the orbital's mask the sweep clamps to zero
+                    // whatever the stencil gives: skip the stencil there
+                    float l0 = 0.f, l1 = 0.f;
+                    if (m0 != 0.f || m1 != 0.f) lap_m2(M, X, N, i, C::Z2, P, l0, l1);
                     const float2 r  = make_float2(X[i], X[i + 1]);
                     const float w0  = P.gamma * l0 - r.x;
                     const float w1  = P.gamma * l1 - r.y;
@@ -352,17 +354,18 @@ __global__ void __launch_bounds__(THREADS, 4) local_step_kernel(StepParams P)
                     if (by >= e1 || bz >= e2) continue;
                     const size_t li = (size_t)p * ex + (size_t)by * e2 + bz;
                     const int i     = (qy + 1) * C::Z1 + qz + 1;
-                    float l0, l1;
-                    lap_m2(M, X, N, i, C::Z1, P, l0, l1);
+                    const float m0  = mo[li];
+                    const float m1  = (bz + 1 < e2) ? mo[li + 1] : 0.f;
+                    // the stencil only where the mask keeps something
+                    float l0 = 0.f, l1 = 0.f;
+                    if (m0 != 0.f || m1 != 0.f) lap_m2(M, X, N, i, C::Z1, P, l0, l1);
                     const int ir    = (qy + 2) * C::Z2 + qz + 2;
                     const float w0  = l0 - R[ir];
-                    const float m0  = mo[li];
                     P.u[P.off[f] + li] = clampm(X[i] - P.jf * w0, m0);
                     P.w[P.off[f] + li] = clampm(w0, m0);
                     if (bz + 1 < e2)
                     {
                         const float w1 = l1 - R[ir + 1];
-                        const float m1 = mo[li + 1];
                         P.u[P.off[f] + li + 1] = clampm(X[i + 1] - P.jf * w1, m1);
                         P.w[P.off[f] + li + 1] = clampm(w1, m1);
                     }
