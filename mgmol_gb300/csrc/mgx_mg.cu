@@ -224,6 +224,89 @@ __global__ void __launch_bounds__(256) prolong_kernel(const T* __restrict__ coar
     }
 }
 
+/* The FP32 prolongation with four fine z points per thread and y parity:
+ * a thread owns coarse points (j, 2m) and (j, 2m + 1) and writes the 2 x 4
+ * fine points (2j + b, 4m + c) of its x plane as two 16-byte stores (MODE
+ * 1: read-modify-write), which keeps twice the bytes in flight of the
+ * pair form.  Every output has the operation order of prolong_kernel.
+ * Needs fz % 4 == 0 and 16-byte aligned fine rows. */
+constexpr int PROLONG4_CROWS = 16;
+
+template <int MODE>
+__global__ void __launch_bounds__(256) prolong4_kernel(const float* __restrict__ coarse,
+    size_t ldc, float* __restrict__ out, size_t ldo, int fx, int fy, int fz, MaskDev mask)
+{
+    const int cx = fx >> 1, cy = fy >> 1, cz = fz >> 1, hz = cz >> 1;
+    const int f      = blockIdx.y;
+    const int bands  = (cy + PROLONG4_CROWS - 1) / PROLONG4_CROWS;
+    const int x      = blockIdx.x / bands;
+    const int jb     = (blockIdx.x - x * bands) * PROLONG4_CROWS;
+    const float* e   = coarse + (size_t)f * ldc;
+    const int i = x >> 1, a = x & 1, i1 = wrp(i + 1, cx);
+    for (int t = threadIdx.x; t < PROLONG4_CROWS * hz; t += blockDim.x)
+    {
+        const int r = t / hz, m = t - r * hz;
+        const int j = jb + r;
+        if (j >= cy) break;
+        const int j1 = wrp(j + 1, cy);
+        const int k = 2 * m, k1 = k + 1, k2 = wrp(k + 2, cz);
+        const float* c00 = e + ((size_t)i * cy + j) * cz;
+        const float* c01 = e + ((size_t)i * cy + j1) * cz;
+        const float a0 = c00[k], a1 = c00[k1], a2 = c00[k2];
+        const float b0 = c01[k], b1 = c01[k1], b2 = c01[k2];
+        float v[2][4]; // [y parity][fine z - 4m]
+        if (!a)
+        {
+            v[0][0] = a0;
+            v[0][1] = 0.5f * (a0 + a1);
+            v[0][2] = a1;
+            v[0][3] = 0.5f * (a1 + a2);
+            v[1][0] = 0.5f * (b0 + a0);
+            v[1][1] = 0.25f * (b1 + a1 + b0 + a0);
+            v[1][2] = 0.5f * (b1 + a1);
+            v[1][3] = 0.25f * (b2 + a2 + b1 + a1);
+        }
+        else
+        {
+            const float* c10 = e + ((size_t)i1 * cy + j) * cz;
+            const float* c11 = e + ((size_t)i1 * cy + j1) * cz;
+            const float d0 = c10[k], d1 = c10[k1], d2 = c10[k2];
+            const float g0 = c11[k], g1 = c11[k1], g2 = c11[k2];
+            v[0][0] = 0.5f * (d0 + a0);
+            v[0][1] = 0.25f * (d1 + d0 + a1 + a0);
+            v[0][2] = 0.5f * (d1 + a1);
+            v[0][3] = 0.25f * (d2 + d1 + a2 + a1);
+            v[1][0] = 0.25f * (g0 + d0 + b0 + a0);
+            v[1][1] = 0.125f * (g1 + g0 + d1 + d0 + b1 + b0 + a1 + a0);
+            v[1][2] = 0.25f * (g1 + d1 + b1 + a1);
+            v[1][3] = 0.125f * (g2 + g1 + d2 + d1 + b2 + b1 + a2 + a1);
+        }
+#pragma unroll
+        for (int b = 0; b < 2; b++)
+        {
+            const int y = 2 * j + b;
+            float4* o = reinterpret_cast<float4*>(out + (size_t)f * ldo + ((size_t)x * fy + y) * fz
+                                                  + 4 * m);
+            float w[4];
+#pragma unroll
+            for (int c = 0; c < 4; c++)
+                w[c] = MODE == 1 ? mask_point<float>(mask, f, x, y, 4 * m + c, v[b][c]) : v[b][c];
+            float4 q;
+            if (MODE == 1)
+            {
+                q = *o;
+                q.x = q.x - w[0];
+                q.y = q.y - w[1];
+                q.z = q.z - w[2];
+                q.w = q.w - w[3];
+            }
+            else
+                q = make_float4(w[0], w[1], w[2], w[3]);
+            *o = q;
+        }
+    }
+}
+
 template <typename T>
 __global__ void scale_kernel(const T* in, size_t ldi, T* out, size_t ldo,
     size_t npts, T alpha)
@@ -272,10 +355,34 @@ int restrict_launch(int dtype, const Level& fine, const void* f, size_t ldf,
     return MGX_OK;
 }
 
+/* MGX_PROLONG4=0 keeps the pair form for FP32 (the same bits) */
+static bool prolong4_on()
+{
+    static const bool on = [] {
+        const char* e = getenv("MGX_PROLONG4");
+        return !(e && e[0] == '0');
+    }();
+    return on;
+}
+
 int prolong_launch(int dtype, int mode, const Level& fine, const void* c,
     size_t ldc, void* out, size_t ldo, int nfunc, const MaskDev& mask,
     cudaStream_t s)
 {
+    if (dtype == MGX_F32 && (fine.n[2] % 4) == 0 && (ldo % 4) == 0
+        && ((uintptr_t)out % 16) == 0 && prolong4_on())
+    {
+        const int bands4 = ((fine.n[1] / 2) + PROLONG4_CROWS - 1) / PROLONG4_CROWS;
+        const dim3 g4(fine.n[0] * bands4, nfunc);
+        if (mode == 0)
+            prolong4_kernel<0><<<g4, 256, 0, s>>>((const float*)c, ldc, (float*)out, ldo,
+                fine.n[0], fine.n[1], fine.n[2], mask);
+        else
+            prolong4_kernel<1><<<g4, 256, 0, s>>>((const float*)c, ldc, (float*)out, ldo,
+                fine.n[0], fine.n[1], fine.n[2], mask);
+        MGX_LAUNCH_CHECK("prolong4_kernel");
+        return MGX_OK;
+    }
     const int bands = ((fine.n[1] / 2) + PROLONG_CROWS - 1) / PROLONG_CROWS;
     const dim3 g(fine.n[0] * bands, nfunc);
     const int nt = 256;

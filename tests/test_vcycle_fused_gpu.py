@@ -1,9 +1,11 @@
 """The V-cycle with the residual of each level's second pre-sweep
 restricted inside that sweep's kernel (the default) against the V-cycle
 with the residual stored and restricted by its own kernel
-(MGX_FUSED_RESTRICT=0), each in a fresh process (the library reads the
-choice once): the same bits, FP64 and FP32, on grids whose tile rows and
-x chunks end unevenly; and the fused FP64 V-cycle against the oracle."""
+(MGX_FUSED_RESTRICT=0), and the FP32 prolongation with four z points per
+thread against the pair form (MGX_PROLONG4=0), each in a fresh process
+(the library reads the choice once): the same bits, FP64 and FP32, on
+grids whose tile rows and x chunks end unevenly; and the fused FP64
+V-cycle against the oracle."""
 import os
 import subprocess
 import sys
@@ -52,6 +54,14 @@ def _run(tmp_path, env, tag):
 def test_fused_restriction_gives_the_same_bits(tmp_path):
     a = _run(tmp_path, {"MGX_FUSED_RESTRICT": "1"}, "fused")
     b = _run(tmp_path, {"MGX_FUSED_RESTRICT": "0"}, "separate")
+    assert sorted(a.files) == sorted(b.files)
+    for k in a.files:
+        assert np.array_equal(a[k], b[k]), k
+
+
+def test_prolongation_four_wide_gives_the_same_bits(tmp_path):
+    a = _run(tmp_path, {"MGX_PROLONG4": "1"}, "four")
+    b = _run(tmp_path, {"MGX_PROLONG4": "0"}, "pair")
     assert sorted(a.files) == sorted(b.files)
     for k in a.files:
         assert np.array_equal(a[k], b[k]), k
