@@ -654,10 +654,10 @@ int mgx_local_scatter(mgx_local* loc, const float* packed, float* full, size_t l
  * argument or the configuration changes. */
 int mgx_local_step(mgx_local* loc, const float* psi, const float* phi, const float* V,
     double gamma, float* u, float* w, void* stream);
-/* times every kernel variant (column TY x TZ and planes per march step;
- * 0: 8x32, 1: 16x32, 2: 16x16 with one plane, 3..5 the same with two) with
- * 2, 4, 6 and 8 resident CTAs per SM on these arguments and keeps the
- * fastest; ms
+/* times every kernel variant (largest column TY x TZ, fitted to each box,
+ * and planes per march step; 0: 24x32, 1: 16x32, 2: 32x32 with one plane,
+ * 3..5 the same with two) with 1, 2, 3 and 4 resident CTAs per SM on these
+ * arguments and keeps the fastest; ms
  * (optional, *ncand entries) receives each candidate's time (-1: not
  * resident), *ncand the number of candidates */
 int mgx_local_tune(mgx_local* loc, const float* psi, const float* phi, const float* V,

@@ -879,8 +879,8 @@ class Local:
     def tune(self, psi, phi, V, gamma, u, w, stream=None):
         """Times the candidates and keeps the fastest; returns (times in ms
         per candidate, (shape, ctas_per_sm, graph))."""
-        ms = np.zeros(32)
-        n = ctypes.c_int(32)
+        ms = np.zeros(64)
+        n = ctypes.c_int(64)
         _check(load().mgx_local_tune(self.handle, _ptr(psi), _ptr(phi), _ptr(V), float(gamma),
                                      _ptr(u), _ptr(w), ms.ctypes.data_as(_dp), ctypes.byref(n),
                                      _stream(stream)))

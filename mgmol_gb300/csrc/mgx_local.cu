@@ -151,17 +151,29 @@ __device__ __forceinline__ void rhs_b2(const float* M, const float* C, const flo
     o1 = 0.5f * c.c + (1.f / 12.f) * s1;
 }
 
+/* q / d for 0 <= q < 4096 and 1 <= d <= 64 with inv = 1/d rounded to FP32:
+ * (q + 1/2) / d lies at least 1/(2d) from an integer, far more than the
+ * 2^-23 relative error of the product, so the truncation is exact */
+__device__ __forceinline__ int divq(int q, float inv)
+{
+    return __float2int_rz(((float)q + 0.5f) * inv);
+}
+
 /* one periodic coordinate of a box point: b in [-3, e + 3) with e + 6 <= n */
 __device__ __forceinline__ int wrap1(int g, int n)
 {
     return g < 0 ? g + n : (g >= n ? g - n : g);
 }
 
-/* A CTA owns a TY x TZ column of an orbital's box and marches along x,
- * PPS planes per step.  Plane regions shrink by one point per stage in y
- * and z: stage 0 (psi and phi - V psi) on (TY + 6) x (TZ + 6), stage 1 (r)
- * on (TY + 4) x (TZ + 4), stage 2 (u1) on (TY + 2) x (TZ + 2), stage 3
- * (u, w) on TY x TZ.  Stage k makes planes PPS t + j - 3 - k (j < PPS,
+/* A CTA owns a ty x tz column of an orbital's box and marches along x,
+ * PPS planes per step.  The column is fitted to the box: the box's y
+ * extent is cut into ceil(e1 / TY) equal columns, its z extent into
+ * ceil(e2 / TZ) (tz rounded up to even), so that a box a little wider than
+ * TY or TZ does not pay for a second, mostly empty column; TY x TZ bounds
+ * the shared-memory planes.  Plane regions shrink by one point per stage
+ * in y and z: stage 0 (psi and phi - V psi) on (ty + 6) x (tz + 6), stage 1
+ * (r) on (ty + 4) x (tz + 4), stage 2 (u1) on (ty + 2) x (tz + 2), stage 3
+ * (u, w) on ty x tz.  Stage k makes planes PPS t + j - 3 - k (j < PPS,
  * box-local x) at step t, within [k - 3, e0 - 1 + 3 - k]; a plane needs
  * the planes p - 1 .. p + 1 of the stage before, made at this step or the
  * one before, so each stage keeps a ring of PPS + 2 planes.  Three
@@ -176,10 +188,15 @@ template <int TY, int TZ, int PPS> struct Cols
     static constexpr size_t SMEM = (size_t)(RING * (2 * N3 + N2 + N1)) * sizeof(float);
     // ring slot of plane p >= -3
     static __device__ __forceinline__ int slot(int p) { return (p + 3 * RING) % RING; }
+    // resident CTAs per SM the shared memory allows (the register cap of
+    // the launch bounds follows it)
+    static constexpr int MINB = (int)(227 * 1024 / (SMEM + 1024)) < 4
+                                    ? (int)(227 * 1024 / (SMEM + 1024))
+                                    : 4;
 };
 
 template <int TY, int TZ, int PPS>
-__global__ void __launch_bounds__(THREADS, 4) local_step_kernel(StepParams P)
+__global__ void __launch_bounds__(THREADS, Cols<TY, TZ, PPS>::MINB) local_step_kernel(StepParams P)
 {
     using C = Cols<TY, TZ, PPS>;
     extern __shared__ __align__(16) float sm[];
@@ -196,8 +213,17 @@ __global__ void __launch_bounds__(THREADS, 4) local_step_kernel(StepParams P)
         __syncthreads();
         const int it = s_item;
         if (it >= P.nitems) break;
-        const int4 W = P.items[it]; // (orbital, -, y0, z0)
+        const int4 W = P.items[it]; // (orbital, ty | tz << 16, y0, z0)
         const int f  = W.x;
+        const int ty = W.y & 0xffff, tz = W.y >> 16;
+        // the column's plane regions of each stage (row pitch z_k, pairs
+        // per row p_k) and the reciprocals of the divisors
+        const int z3 = tz + 6, n3 = (ty + 6) * z3;
+        const int z2 = tz + 4, n2 = (ty + 4) * z2, p2 = z2 / 2;
+        const int z1 = tz + 2, n1 = (ty + 2) * z1, p1 = z1 / 2;
+        const int n0 = ty * tz, p0 = tz / 2;
+        const float i3 = 1.f / (float)z3, ip2 = 1.f / (float)p2, ip1 = 1.f / (float)p1,
+                    ip0 = 1.f / (float)p0;
         const int* b = P.box + 6 * f;
         const int o0 = b[0], o1 = b[1], o2 = b[2], e0 = b[3], e1 = b[4], e2 = b[5];
         const int y0 = W.z, z0 = W.w;
@@ -217,10 +243,10 @@ __global__ void __launch_bounds__(THREADS, 4) local_step_kernel(StepParams P)
             for (int k = 0; k < NQ; k++)
             {
                 const int q  = tid + k * THREADS;
-                const int qy = q / C::Z3, qz = q - qy * C::Z3;
+                const int qy = divq(q, i3), qz = q - qy * z3;
                 const int by = y0 + qy - 3, bz = z0 + qz - 3;
                 float ps = 0.f, ph = 0.f, v = 0.f;
-                if (q < C::N3 && in && by >= 0 && by < e1 && bz >= 0 && bz < e2)
+                if (q < n3 && in && by >= 0 && by < e1 && bz >= 0 && bz < e2)
                 {
                     const size_t li = (size_t)p * ex + (size_t)by * e2 + bz;
                     ps              = psi[li];
@@ -252,7 +278,7 @@ __global__ void __launch_bounds__(THREADS, 4) local_step_kernel(StepParams P)
                     for (int k = 0; k < NQ; k++)
                     {
                         const int q = tid + k * THREADS;
-                        if (q < C::N3)
+                        if (q < n3)
                         {
                             dp[q] = rps[j][k];
                             dd[q] = rph[j][k] - rv[j][k] * rps[j][k];
@@ -276,9 +302,9 @@ __global__ void __launch_bounds__(THREADS, 4) local_step_kernel(StepParams P)
                 const float* dN = s_d + C::slot(p + 1) * C::N3;
                 float* out      = s_r + C::slot(p) * C::N2;
                 const bool in   = (p >= 0 && p < e0);
-                for (int q = tid; q < C::N2 / 2; q += THREADS)
+                for (int q = tid; q < n2 / 2; q += THREADS)
                 {
-                    const int qy = q / (C::Z2 / 2), qz = 2 * (q - qy * (C::Z2 / 2));
+                    const int qy = divq(q, ip2), qz = 2 * (q - qy * p2);
                     const int by = y0 + qy - 2, bz = z0 + qz - 2;
                     float m0 = 0.f, m1 = 0.f;
                     if (in && by >= 0 && by < e1)
@@ -290,14 +316,14 @@ __global__ void __launch_bounds__(THREADS, 4) local_step_kernel(StepParams P)
                     float r0 = 0.f, r1 = 0.f;
                     if (m0 != 0.f || m1 != 0.f)
                     {
-                        const int i = (qy + 1) * C::Z3 + qz + 1;
+                        const int i = (qy + 1) * z3 + qz + 1;
                         float b0, b1, l0, l1;
-                        rhs_b2(dM, dX, dN, i, C::Z3, b0, b1);
-                        lap_m2(M, X, N, i, C::Z3, P, l0, l1);
+                        rhs_b2(dM, dX, dN, i, z3, b0, b1);
+                        lap_m2(M, X, N, i, z3, P, l0, l1);
                         r0 = m0 * (b0 - l0);
                         r1 = m1 * (b1 - l1);
                     }
-                    *reinterpret_cast<float2*>(out + qy * C::Z2 + qz) = make_float2(r0, r1);
+                    *reinterpret_cast<float2*>(out + qy * z2 + qz) = make_float2(r0, r1);
                 }
             }
             __syncthreads();
@@ -312,9 +338,9 @@ __global__ void __launch_bounds__(THREADS, 4) local_step_kernel(StepParams P)
                 const float* N = s_r + C::slot(p + 1) * C::N2;
                 float* out     = s_u + C::slot(p) * C::N1;
                 const bool in  = (p >= 0 && p < e0);
-                for (int q = tid; q < C::N1 / 2; q += THREADS)
+                for (int q = tid; q < n1 / 2; q += THREADS)
                 {
-                    const int qy = q / (C::Z1 / 2), qz = 2 * (q - qy * (C::Z1 / 2));
+                    const int qy = divq(q, ip1), qz = 2 * (q - qy * p1);
                     const int by = y0 + qy - 1, bz = z0 + qz - 1;
                     float m0 = 0.f, m1 = 0.f;
                     if (in && by >= 0 && by < e1)
@@ -323,15 +349,15 @@ __global__ void __launch_bounds__(THREADS, 4) local_step_kernel(StepParams P)
                         if (bz >= 0 && bz < e2) m0 = mrow[bz];
                         if (bz + 1 >= 0 && bz + 1 < e2) m1 = mrow[bz + 1];
                     }
-                    const int i = (qy + 1) * C::Z2 + qz + 1;
+                    const int i = (qy + 1) * z2 + qz + 1;
                     // outside the orbital's mask the sweep clamps to zero
                     // whatever the stencil gives: skip the stencil there
                     float l0 = 0.f, l1 = 0.f;
-                    if (m0 != 0.f || m1 != 0.f) lap_m2(M, X, N, i, C::Z2, P, l0, l1);
+                    if (m0 != 0.f || m1 != 0.f) lap_m2(M, X, N, i, z2, P, l0, l1);
                     const float2 r  = make_float2(X[i], X[i + 1]);
                     const float w0  = P.gamma * l0 - r.x;
                     const float w1  = P.gamma * l1 - r.y;
-                    *reinterpret_cast<float2*>(out + qy * C::Z1 + qz)
+                    *reinterpret_cast<float2*>(out + qy * z1 + qz)
                         = make_float2(clampm(P.gamma * r.x - P.jf * w0, m0),
                             clampm(P.gamma * r.y - P.jf * w1, m1));
                 }
@@ -347,19 +373,19 @@ __global__ void __launch_bounds__(THREADS, 4) local_step_kernel(StepParams P)
                 const float* X = s_u + C::slot(p) * C::N1;
                 const float* N = s_u + C::slot(p + 1) * C::N1;
                 const float* R = s_r + C::slot(p) * C::N2;
-                for (int q = tid; q < C::N0 / 2; q += THREADS)
+                for (int q = tid; q < n0 / 2; q += THREADS)
                 {
-                    const int qy = q / (TZ / 2), qz = 2 * (q - qy * (TZ / 2));
+                    const int qy = divq(q, ip0), qz = 2 * (q - qy * p0);
                     const int by = y0 + qy, bz = z0 + qz;
                     if (by >= e1 || bz >= e2) continue;
                     const size_t li = (size_t)p * ex + (size_t)by * e2 + bz;
-                    const int i     = (qy + 1) * C::Z1 + qz + 1;
+                    const int i     = (qy + 1) * z1 + qz + 1;
                     const float m0  = mo[li];
                     const float m1  = (bz + 1 < e2) ? mo[li + 1] : 0.f;
                     // the stencil only where the mask keeps something
                     float l0 = 0.f, l1 = 0.f;
-                    if (m0 != 0.f || m1 != 0.f) lap_m2(M, X, N, i, C::Z1, P, l0, l1);
-                    const int ir    = (qy + 2) * C::Z2 + qz + 2;
+                    if (m0 != 0.f || m1 != 0.f) lap_m2(M, X, N, i, z1, P, l0, l1);
+                    const int ir    = (qy + 2) * z2 + qz + 2;
                     const float w0  = l0 - R[ir];
                     P.u[P.off[f] + li] = clampm(X[i] - P.jf * w0, m0);
                     P.w[P.off[f] + li] = clampm(w0, m0);
@@ -408,24 +434,31 @@ __global__ void __launch_bounds__(256) scatter_kernel(const float* __restrict__ 
     }
 }
 
-/* the kernel variants the tuner chooses from: column TY x TZ and planes
- * per march step */
+/* the kernel variants the tuner chooses from: largest column TY x TZ and
+ * planes per march step */
 struct Shape
 {
     int ty, tz, pps;
 };
 constexpr int NSHAPE           = 6;
-constexpr Shape SHAPES[NSHAPE] = { { 8, 32, 1 }, { 16, 32, 1 }, { 16, 16, 1 }, { 8, 32, 2 },
-    { 16, 32, 2 }, { 16, 16, 2 } };
+constexpr Shape SHAPES[NSHAPE] = { { 24, 32, 1 }, { 16, 32, 1 }, { 32, 32, 1 }, { 24, 32, 2 },
+    { 16, 32, 2 }, { 32, 32, 2 } };
+
+/* kernel and dynamic shared memory of a variant */
+template <int TY, int TZ, int PPS> struct Variant
+{
+    static constexpr auto kernel() { return &local_step_kernel<TY, TZ, PPS>; }
+    static constexpr size_t smem = Cols<TY, TZ, PPS>::SMEM;
+};
 
 template <int TY, int TZ, int PPS> int set_attr()
 {
     static bool done = false;
     if (!done)
     {
-        MGX_TRY(cuda_check(cudaFuncSetAttribute(local_step_kernel<TY, TZ, PPS>,
+        MGX_TRY(cuda_check(cudaFuncSetAttribute(Variant<TY, TZ, PPS>::kernel(),
                                cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               (int)Cols<TY, TZ, PPS>::SMEM),
+                               (int)Variant<TY, TZ, PPS>::smem),
             "local smem"));
         done = true;
     }
@@ -436,8 +469,8 @@ template <int TY, int TZ, int PPS> int occupancy()
 {
     if (set_attr<TY, TZ, PPS>() != MGX_OK) return 1;
     int n = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, local_step_kernel<TY, TZ, PPS>,
-            THREADS, Cols<TY, TZ, PPS>::SMEM)
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, Variant<TY, TZ, PPS>::kernel(),
+            THREADS, Variant<TY, TZ, PPS>::smem)
         != cudaSuccess)
     {
         cudaGetLastError();
@@ -451,18 +484,18 @@ int max_ctas_per_sm(int s)
 {
     switch (s)
     {
-        case 0: return occupancy<8, 32, 1>();
+        case 0: return occupancy<24, 32, 1>();
         case 1: return occupancy<16, 32, 1>();
-        case 2: return occupancy<16, 16, 1>();
-        case 3: return occupancy<8, 32, 2>();
+        case 2: return occupancy<32, 32, 1>();
+        case 3: return occupancy<24, 32, 2>();
         case 4: return occupancy<16, 32, 2>();
-        default: return occupancy<16, 16, 2>();
+        default: return occupancy<32, 32, 2>();
     }
 }
 
 template <int TY, int TZ, int PPS> int launch_shape(const StepParams& P, int ctas, cudaStream_t s)
 {
-    local_step_kernel<TY, TZ, PPS><<<ctas, THREADS, Cols<TY, TZ, PPS>::SMEM, s>>>(P);
+    Variant<TY, TZ, PPS>::kernel()<<<ctas, THREADS, Variant<TY, TZ, PPS>::smem, s>>>(P);
     MGX_LAUNCH_CHECK("local_step_kernel");
     return MGX_OK;
 }
@@ -514,9 +547,14 @@ int build_items(mgx_local* L, int s)
     {
         const int f  = pr.second;
         const int* e = &L->h_box[6 * f + 3];
-        for (int y = 0; y < e[1]; y += S.ty)
-            for (int z = 0; z < e[2]; z += S.tz)
-                it.push_back(make_int4(f, 0, y, z));
+        // columns fitted to the box: equal cuts of each extent, at most
+        // S.ty x S.tz, tz even (the kernel works on z pairs)
+        const int ny = (e[1] + S.ty - 1) / S.ty, nz = (e[2] + S.tz - 1) / S.tz;
+        const int ty = (e[1] + ny - 1) / ny;
+        const int tz = (((e[2] + nz - 1) / nz) + 1) & ~1;
+        for (int y = 0; y < e[1]; y += ty)
+            for (int z = 0; z < e[2]; z += tz)
+                it.push_back(make_int4(f, ty | (tz << 16), y, z));
     }
     L->nitems[s] = (int)it.size();
     MGX_TRY(L->items[s].ensure(std::max<size_t>(it.size(), 1) * sizeof(int4)));
@@ -573,12 +611,12 @@ int enqueue(mgx_local* L, int s, int ctas, const StepParams& P, cudaStream_t st)
     MGX_TRY(cuda_check(cudaMemsetAsync(L->counter.ptr, 0, sizeof(int), st), "counter reset"));
     switch (s)
     {
-        case 0: return launch_shape<8, 32, 1>(P, ctas, st);
+        case 0: return launch_shape<24, 32, 1>(P, ctas, st);
         case 1: return launch_shape<16, 32, 1>(P, ctas, st);
-        case 2: return launch_shape<16, 16, 1>(P, ctas, st);
-        case 3: return launch_shape<8, 32, 2>(P, ctas, st);
+        case 2: return launch_shape<32, 32, 1>(P, ctas, st);
+        case 3: return launch_shape<24, 32, 2>(P, ctas, st);
         case 4: return launch_shape<16, 32, 2>(P, ctas, st);
-        default: return launch_shape<16, 16, 2>(P, ctas, st);
+        default: return launch_shape<32, 32, 2>(P, ctas, st);
     }
 }
 
@@ -785,7 +823,7 @@ int mgx_local_tune(mgx_local* L, const float* psi, const float* phi, const float
         const int cmax = loc::max_ctas_per_sm(s);
         for (int ci = 0; ci < 4 && rc == MGX_OK; ci++)
         {
-            const int c = 2 * (ci + 1); // 2, 4, 6, 8 resident CTAs per SM
+            const int c = ci + 1; // 1 to 4 resident CTAs per SM
             double t = 1e300;
             if (c <= cmax)
             {

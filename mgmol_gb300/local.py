@@ -22,8 +22,9 @@ from . import capi, synth
 
 # algorithmic bytes per box point: psi, phi, V, two mask values read; u, w written
 BYTES_PER_POINT = 7 * 4
-# the kernel variants of mgx_local_tune: (column TY x TZ, planes per march step)
-VARIANTS = [("8x32", 1), ("16x32", 1), ("16x16", 1), ("8x32", 2), ("16x32", 2), ("16x16", 2)]
+# the kernel variants of mgx_local_tune: (largest column TY x TZ, fitted to each
+# box, planes per march step)
+VARIANTS = [("24x32", 1), ("16x32", 1), ("32x32", 1), ("24x32", 2), ("16x32", 2), ("32x32", 2)]
 
 
 def build(n, h, nfunc, seed, rlo=4.0, rhi=8.0, chunk=128):

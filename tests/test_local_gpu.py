@@ -45,10 +45,12 @@ def test_gather_scatter_round_trip():
         assert np.all(got[mask] == 0)
 
 
+@pytest.mark.parametrize("shape", [1, 2, 5])
 @pytest.mark.parametrize("n,h,nf,r", [((32, 32, 32), 0.35, 6, (1.5, 2.5)),
                                        ((40, 32, 48), 0.3, 9, (1.2, 2.0))])
-def test_local_step_matches_oracle_chain(n, h, nf, r):
+def test_local_step_matches_oracle_chain(n, h, nf, r, shape):
     ll, ctx, loc, centers, radii, psi, phi, V = _setup(n, h, nf, 41, *r)
+    loc.set_config(shape, 2, True)
     f32 = lambda a: torch.from_numpy(np.ascontiguousarray(a, dtype=np.float32)).cuda()
     psi_p = loc.gather(f32(psi))
     phi_p = loc.gather(f32(phi))
@@ -108,7 +110,7 @@ def test_tuner_picks_a_resident_configuration():
     u, w = loc.empty(), loc.empty()
     ms, (shape, ctas, graph) = loc.tune(psi_p, phi_p, Vd, 0.01, u, w)
     assert ms.size == 24 and np.all(ms[ms >= 0] > 0)
-    assert ms[4 * shape + (2, 4, 6, 8).index(ctas)] == ms[ms >= 0].min()
+    assert ms[4 * shape + (1, 2, 3, 4).index(ctas)] == ms[ms >= 0].min()
     assert graph == 1
 
 
