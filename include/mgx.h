@@ -111,6 +111,11 @@ int mgx_timing_read(int cls, double* total_ms, int* launches);
  * contexts); a counter for benchmarks and tests. */
 unsigned long long mgx_kernel_launch_count(void);
 
+/* The compute capability (major * 10 + minor) that the loaded module of
+ * this library's kernels was compiled for, from the CUDA runtime's
+ * function attributes of one of them: 103 for sm_103a.  Needs a device. */
+int mgx_kernel_arch(int* binary_version);
+
 /* ---------------------------------------------------------------- */
 /* Drop-in kernels on ghosted GridFuncVector blocks (ghosts already     */
 /* filled), the MemorySpace::Device overloads of src/pb/FDkernels.h:   */

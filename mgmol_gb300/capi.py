@@ -107,6 +107,7 @@ _SIGS = {
     "mgx_mgkernel_extend3d": [ctypes.POINTER(Grid), _i, _i, _vp, _vp, _sz, _vp],
     "mgx_trade_boundaries": [ctypes.POINTER(Grid), _i, _i, _vp, _sz, _vp],
     "mgx_axpy": [_sz, _d, _i, _vp, _vp, _vp],
+    "mgx_kernel_arch": [ctypes.POINTER(_i)],
     "mgx_fd_apply": [_vp, _i, _i, _vp, _sz, _vp, _i, _vp],
     "mgx_rhs_mehr": [_vp, _i, _vp, _sz, _vp, _i, _vp],
     "mgx_hpsi": [_vp, _i, _i, _vp, _sz, _vp, _i, _vp, _i, _i, _vp],
@@ -209,6 +210,14 @@ def _check(status):
 
 def launches():
     return int(load().mgx_kernel_launch_count())
+
+
+def kernel_arch():
+    """major * 10 + minor of the architecture the library's kernels were
+    compiled for, as the CUDA runtime reports it for the loaded module."""
+    v = _i()
+    _check(load().mgx_kernel_arch(ctypes.byref(v)))
+    return v.value
 
 
 TIMING_TC_SPLITK, TIMING_TC_STORE = 1, 2

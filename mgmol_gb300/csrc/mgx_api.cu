@@ -261,6 +261,15 @@ int mgx_copy(void* dst, const void* src, size_t bytes, void* stream)
     return cuda_check(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDefault, s), "copy");
 }
 
+int mgx_kernel_arch(int* binary_version)
+{
+    if (!binary_version) return fail(MGX_BAD_ARG, "NULL argument");
+    cudaFuncAttributes a;
+    MGX_TRY(cuda_check(cudaFuncGetAttributes(&a, copy16_kernel), "function attributes"));
+    *binary_version = a.binaryVersion;
+    return MGX_OK;
+}
+
 const char* mgx_last_error_string(void) { return g_err; }
 
 unsigned long long mgx_kernel_launch_count(void) { return g_launches.load(); }

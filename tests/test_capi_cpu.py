@@ -32,11 +32,11 @@ def test_library_exports_every_declared_symbol():
     assert declared == set(capi.EXPORTS)
 
 
-def test_library_is_built_for_sm103a():
-    out = subprocess.run(["cuobjdump", "--list-elf", capi.LIB_PATH], capture_output=True, text=True)
-    if out.returncode != 0:
-        pytest.skip("cuobjdump unavailable")
-    assert "sm_103a" in out.stdout
+def test_build_recipe_targets_sm103a_only():
+    """The recipe compiles and links for sm_103a and nothing else; the
+    loaded module's architecture is checked on the GPU (test_build_gpu)."""
+    from mgmol_gb300 import build
+    assert build.ARCH == ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
 def test_precond_gamma_host_logic():
