@@ -891,18 +891,29 @@ __global__ void __launch_bounds__(256) plane_vec_kernel(PlaneParams p, DevCoef<T
             const T* W0   = wring + (size_t)((xe - x0) % 3) * ring_elems;     // plane 2X
             const T* Wp   = wring + (size_t)((xe - x0 + 1) % 3) * ring_elems; // plane 2X + 1
             T* cp         = reinterpret_cast<T*>(p.coarse) + (size_t)f * p.ldc;
-            for (int t = threadIdx.x; t < nyc * cz; t += 256)
+            // a thread forms the coarse pair (Z, Z + 1), Z even: fine z - 1
+            // (one load) and z .. z + 3 (16-byte loads) of each of the nine
+            // rows, z = 2 Z a multiple of 4
+            const int hz = cz >> 1;
+            for (int t = threadIdx.x; t < nyc * hz; t += 256)
             {
-                const int yl = t / cz, Z = t - (t / cz) * cz;
-                const int z = 2 * Z, zm = z > 0 ? z - 1 : nz - 1, zp = z + 1;
+                const int yl = t / hz, Z = 2 * (t - (t / hz) * hz);
+                const int z = 2 * Z, zm = z > 0 ? z - 1 : nz - 1;
                 const int r = 2 * yl + 1; // ring row of fine y = y0 + 2 yl
-                auto row = [&](const T* P, int dy, T* v3) {
+                // v6[0..4]: fine z - 1 .. z + 3 of one row
+                auto row = [&](const T* P, int dy, T* v6) {
                     const T* q = P + (size_t)(r + dy) * nz;
-                    v3[0]      = q[zm];
-                    v3[1]      = q[z];
-                    v3[2]      = q[zp];
+                    v6[0]      = q[zm];
+#pragma unroll
+                    for (int h = 0; h < 4 / VEC; h++)
+                    {
+                        const V4 c = *reinterpret_cast<const V4*>(q + z + h * VEC);
+#pragma unroll
+                        for (int v = 0; v < VEC; v++)
+                            v6[1 + h * VEC + v] = VH::get(c, v);
+                    }
                 };
-                T r00[3], rp0[3], rm0[3], r0p[3], r0m[3], rpp[3], rpm[3], rmp[3], rmm[3];
+                T r00[5], rp0[5], rm0[5], r0p[5], r0m[5], rpp[5], rpm[5], rmp[5], rmm[5];
                 row(W0, 0, r00);
                 row(Wp, 0, rp0);
                 row(Wm, 0, rm0);
@@ -912,12 +923,21 @@ __global__ void __launch_bounds__(256) plane_vec_kernel(PlaneParams p, DevCoef<T
                 row(Wp, -1, rpm);
                 row(Wm, 1, rmp);
                 row(Wm, -1, rmm);
-                const T face   = rp0[1] + rm0[1] + r0p[1] + r0m[1] + r00[0] + r00[2];
-                const T corner = rpp[0] + rpp[2] + rpm[0] + rpm[2] + rmp[0] + rmp[2] + rmm[0] + rmm[2];
-                const T edge   = r0p[0] + r0p[2] + r0m[0] + r0m[2] + rp0[0] + rp0[2] + rm0[0] + rm0[2]
-                               + rmm[1] + rpm[1] + rmp[1] + rpp[1];
-                cp[((size_t)X * cy + (y0 >> 1) + yl) * cz + Z]
-                    = (T)(1. / 64.) * ((T)8. * r00[1] + (T)4. * face + (T)2. * edge + corner);
+#pragma unroll
+                for (int c2 = 0; c2 < 2; c2++)
+                {
+                    // the three fine z of coarse Z + c2 start at index 2 c2
+                    const int o    = 2 * c2;
+                    const T face   = rp0[o + 1] + rm0[o + 1] + r0p[o + 1] + r0m[o + 1] + r00[o]
+                                   + r00[o + 2];
+                    const T corner = rpp[o] + rpp[o + 2] + rpm[o] + rpm[o + 2] + rmp[o] + rmp[o + 2]
+                                     + rmm[o] + rmm[o + 2];
+                    const T edge   = r0p[o] + r0p[o + 2] + r0m[o] + r0m[o + 2] + rp0[o] + rp0[o + 2]
+                                   + rm0[o] + rm0[o + 2] + rmm[o + 1] + rpm[o + 1] + rmp[o + 1]
+                                   + rpp[o + 1];
+                    cp[((size_t)X * cy + (y0 >> 1) + yl) * cz + Z + c2]
+                        = (T)(1. / 64.) * ((T)8. * r00[o + 1] + (T)4. * face + (T)2. * edge + corner);
+                }
             }
         }
         __syncthreads();
@@ -1037,8 +1057,8 @@ static int launch_vec(const PlaneParams& p0, const DevCoef<T>& c, int nfunc,
     // and three planes of TY + 1 rows of w for the restriction
     constexpr bool RST = (OP == OP_JACOBI_RST);
     constexpr int YO   = RST ? 1 : 0;
-    if (RST && ((nx | ny | nz) & 1))
-        return fail(MGX_UNSUPPORTED, "restriction needs even grid dimensions");
+    if (RST && (((nx | ny) & 1) || (nz % 4)))
+        return fail(MGX_UNSUPPORTED, "the fused restriction needs even x, y and z % 4 == 0");
     auto smem_for = [&](int t) {
         return (size_t)S * (t + 2 + YO) * nz * esz + (RST ? 3 * (size_t)(t + 1) * nz * sizeof(T) : 0)
                + S * 8;
