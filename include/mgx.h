@@ -251,8 +251,8 @@ int mgx_precond_mg_update(mgx_ctx* ctx, const mgx_precond_params* p,
  * in chunks that fit it, and a request whose single function needs more
  * than the array holds is rejected with MGX_BAD_ARG.  The first call on a
  * device looks up the array's device address and keeps it for the life of
- * the process (make that call before any stream capture; a cudaDeviceReset
- * afterwards leaves the kept address stale).  All calls share the array,
+ * the process (a cudaDeviceReset afterwards leaves the kept address
+ * stale).  All calls share the array,
  * so calls that overlap on the GPU (other streams, other host threads)
  * race.  The call reads the V-cycle's status word back and waits for
  * `stream` before it returns. */

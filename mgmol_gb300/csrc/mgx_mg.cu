@@ -1133,8 +1133,7 @@ void* g_scratch_address[MAX_DEVICES] = {};
 /* Device address of the static scratch on the current device.  The host
  * symbol g_vcycle_scratch is only a stand-in for the device array; its
  * device address is looked up once per device, with that device current,
- * on the first call that needs it (which should therefore come before any
- * stream capture).  The cached address belongs to the device's primary
+ * on the first call that needs it.  The cached address belongs to the device's primary
  * context as it was at that first call: it assumes that context lives as
  * long as the process (no cudaDeviceReset in between). */
 int static_scratch_address(void** ptr)
