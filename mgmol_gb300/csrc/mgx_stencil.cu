@@ -580,7 +580,7 @@ struct Vec16<double>
 };
 
 template <typename T, int LAP, int OP, int S, int NG>
-__global__ void __launch_bounds__(256) plane_vec_kernel(PlaneParams p, DevCoef<T> c)
+__global__ void __launch_bounds__(256, 2) plane_vec_kernel(PlaneParams p, DevCoef<T> c)
 {
     using V4          = typename Vec16<T>::type;
     using VH          = Vec16<T>;
@@ -588,8 +588,8 @@ __global__ void __launch_bounds__(256) plane_vec_kernel(PlaneParams p, DevCoef<T
     constexpr bool EDGES   = (LAP == 0) && !is_rhs_op(OP);
     constexpr bool STAGE_V = (OP == OP_HPSI_B);
     // OP_JACOBI_RST: the sweep also forms w on the row y0 - 1 and the plane
-    // x0 - 1 (one more staged row and plane), keeps the last three w planes
-    // in a ring and restricts them as each odd plane is done
+    // x0 - 1 (one more staged row and plane), keeps the last four w planes
+    // in a ring and restricts three of them after each odd plane
     constexpr bool RST = (OP == OP_JACOBI_RST);
     constexpr int YO   = RST ? 1 : 0;
     extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -613,7 +613,7 @@ __global__ void __launch_bounds__(256) plane_vec_kernel(PlaneParams p, DevCoef<T
     const size_t ring_elems = RST ? (size_t)(TY + 1) * nz : 0;
     T* wring = reinterpret_cast<T*>(smem_raw + S * stage_elems * sizeof(T) * (STAGE_V ? 2 : 1));
     uint64_t* bars = reinterpret_cast<uint64_t*>(
-        smem_raw + S * stage_elems * sizeof(T) * (STAGE_V ? 2 : 1) + 3 * ring_elems * sizeof(T));
+        smem_raw + S * stage_elems * sizeof(T) * (STAGE_V ? 2 : 1) + 4 * ring_elems * sizeof(T));
 
     const T* ubase = reinterpret_cast<const T*>(scaled ? p.f : p.u)
                      + (size_t)f * (scaled ? p.ldf : p.ldu);
@@ -707,10 +707,79 @@ __global__ void __launch_bounds__(256) plane_vec_kernel(PlaneParams p, DevCoef<T
     constexpr bool POINTWISE = is_jacobi(OP) || (OP == OP_HPSI_V) || (OP == OP_RHS_SUB);
     const T c12 = (T)(1. / 12.), c05 = (T)0.5;
 
+    // OP_JACOBI_RST: coarse plane X = (xe - 1) / 2 from the w planes xe - 2
+    // .. xe, rows y0 - 1 .. y0 + TY - 1 of the ring; the grouping and order
+    // of restrict_kernel (src/pb/MGkernels.cc:249-270).  Run after the
+    // barrier that ends plane xe, beside the next plane's stencil (the ring
+    // holds four planes, so that plane's w stores go to the fourth slot)
+    auto restrict_plane = [&](const int xe) {
+        const int cy = ny >> 1, cz = nz >> 1;
+        const int X  = (xe - 1) >> 1;
+        const int nyc = min(TY, ny - y0) >> 1;
+        const T* Wm   = wring + (size_t)((xe - x0 - 1) & 3) * ring_elems; // plane 2X - 1
+        const T* W0   = wring + (size_t)((xe - x0) & 3) * ring_elems;     // plane 2X
+        const T* Wp   = wring + (size_t)((xe - x0 + 1) & 3) * ring_elems; // plane 2X + 1
+        T* cp         = reinterpret_cast<T*>(p.coarse) + (size_t)f * p.ldc;
+        // a thread forms the coarse pair (Z, Z + 1), Z even: fine z - 1
+        // (one load) and z .. z + 3 (16-byte loads) of each of the nine
+        // rows, z = 2 Z a multiple of 4
+        const int hz = cz >> 1;
+        for (int t = threadIdx.x; t < nyc * hz; t += 256)
+        {
+            const int yl = t / hz, Z = 2 * (t - (t / hz) * hz);
+            const int z = 2 * Z, zm = z > 0 ? z - 1 : nz - 1;
+            const int r = 2 * yl + 1; // ring row of fine y = y0 + 2 yl
+            // v6[0..4]: fine z - 1 .. z + 3 of one row
+            auto row = [&](const T* P, int dy, T* v6) {
+                const T* q = P + (size_t)(r + dy) * nz;
+                v6[0]      = q[zm];
+#pragma unroll
+                for (int h = 0; h < 4 / VEC; h++)
+                {
+                    const V4 c = *reinterpret_cast<const V4*>(q + z + h * VEC);
+#pragma unroll
+                    for (int v = 0; v < VEC; v++)
+                        v6[1 + h * VEC + v] = VH::get(c, v);
+                }
+            };
+            T r00[5], rp0[5], rm0[5], r0p[5], r0m[5], rpp[5], rpm[5], rmp[5], rmm[5];
+            row(W0, 0, r00);
+            row(Wp, 0, rp0);
+            row(Wm, 0, rm0);
+            row(W0, 1, r0p);
+            row(W0, -1, r0m);
+            row(Wp, 1, rpp);
+            row(Wp, -1, rpm);
+            row(Wm, 1, rmp);
+            row(Wm, -1, rmm);
+#pragma unroll
+            for (int c2 = 0; c2 < 2; c2++)
+            {
+                // the three fine z of coarse Z + c2 start at index 2 c2
+                const int o    = 2 * c2;
+                const T face   = rp0[o + 1] + rm0[o + 1] + r0p[o + 1] + r0m[o + 1] + r00[o]
+                               + r00[o + 2];
+                const T corner = rpp[o] + rpp[o + 2] + rpm[o] + rpm[o + 2] + rmp[o] + rmp[o + 2]
+                                 + rmm[o] + rmm[o + 2];
+                const T edge   = r0p[o] + r0p[o + 2] + r0m[o] + r0m[o + 2] + rp0[o] + rp0[o + 2]
+                               + rm0[o] + rm0[o + 2] + rmm[o + 1] + rpm[o + 1] + rmp[o + 1]
+                               + rpp[o + 1];
+                cp[((size_t)X * cy + (y0 >> 1) + yl) * cz + Z + c2]
+                    = (T)(1. / 64.) * ((T)8. * r00[o + 1] + (T)4. * face + (T)2. * edge + corner);
+            }
+        }
+    };
+    int pend = -1; // the plane whose restriction is due
+
     bool ok    = true;
     int waited = -1;
     for (int i = 0; i < nplanes; i++)
     {
+        if (RST && pend >= 0)
+        {
+            restrict_plane(pend);
+            pend = -1;
+        }
         const int xe    = x0 + i - 2 - YO;
         const bool emit = (i >= 2);
         const size_t xoff = (size_t)(emit ? (xe < 0 ? xe + nx : xe) : 0) * ny * nz;
@@ -872,74 +941,13 @@ __global__ void __launch_bounds__(256) plane_vec_kernel(PlaneParams p, DevCoef<T
                 else if (!RST || (gy[k] >= YO && xe >= x0))
                     *reinterpret_cast<V4*>(outp + xoff + goff[k]) = res;
                 if (RST)
-                    *reinterpret_cast<V4*>(wring + (size_t)((xe - x0 + 1) % 3) * ring_elems
+                    *reinterpret_cast<V4*>(wring + (size_t)((xe - x0 + 1) & 3) * ring_elems
                                            + (size_t)gy[k] * nz + gz[k]) = wres;
                 else if (is_jacobi(OP) && wp != nullptr)
                     *reinterpret_cast<V4*>(wp + xoff + goff[k]) = wres;
             }
         }
-        if (RST && emit && xe > x0 && ((xe - x0) & 1))
-        {
-            // coarse plane X = (xe - 1) / 2 from the w planes xe - 2 .. xe,
-            // rows y0 - 1 .. y0 + TY - 1 of the ring; the grouping and
-            // order of restrict_kernel (src/pb/MGkernels.cc:249-270)
-            __syncthreads();
-            const int cy = ny >> 1, cz = nz >> 1;
-            const int X  = (xe - 1) >> 1;
-            const int nyc = min(TY, ny - y0) >> 1;
-            const T* Wm   = wring + (size_t)((xe - x0 - 1) % 3) * ring_elems; // plane 2X - 1
-            const T* W0   = wring + (size_t)((xe - x0) % 3) * ring_elems;     // plane 2X
-            const T* Wp   = wring + (size_t)((xe - x0 + 1) % 3) * ring_elems; // plane 2X + 1
-            T* cp         = reinterpret_cast<T*>(p.coarse) + (size_t)f * p.ldc;
-            // a thread forms the coarse pair (Z, Z + 1), Z even: fine z - 1
-            // (one load) and z .. z + 3 (16-byte loads) of each of the nine
-            // rows, z = 2 Z a multiple of 4
-            const int hz = cz >> 1;
-            for (int t = threadIdx.x; t < nyc * hz; t += 256)
-            {
-                const int yl = t / hz, Z = 2 * (t - (t / hz) * hz);
-                const int z = 2 * Z, zm = z > 0 ? z - 1 : nz - 1;
-                const int r = 2 * yl + 1; // ring row of fine y = y0 + 2 yl
-                // v6[0..4]: fine z - 1 .. z + 3 of one row
-                auto row = [&](const T* P, int dy, T* v6) {
-                    const T* q = P + (size_t)(r + dy) * nz;
-                    v6[0]      = q[zm];
-#pragma unroll
-                    for (int h = 0; h < 4 / VEC; h++)
-                    {
-                        const V4 c = *reinterpret_cast<const V4*>(q + z + h * VEC);
-#pragma unroll
-                        for (int v = 0; v < VEC; v++)
-                            v6[1 + h * VEC + v] = VH::get(c, v);
-                    }
-                };
-                T r00[5], rp0[5], rm0[5], r0p[5], r0m[5], rpp[5], rpm[5], rmp[5], rmm[5];
-                row(W0, 0, r00);
-                row(Wp, 0, rp0);
-                row(Wm, 0, rm0);
-                row(W0, 1, r0p);
-                row(W0, -1, r0m);
-                row(Wp, 1, rpp);
-                row(Wp, -1, rpm);
-                row(Wm, 1, rmp);
-                row(Wm, -1, rmm);
-#pragma unroll
-                for (int c2 = 0; c2 < 2; c2++)
-                {
-                    // the three fine z of coarse Z + c2 start at index 2 c2
-                    const int o    = 2 * c2;
-                    const T face   = rp0[o + 1] + rm0[o + 1] + r0p[o + 1] + r0m[o + 1] + r00[o]
-                                   + r00[o + 2];
-                    const T corner = rpp[o] + rpp[o + 2] + rpm[o] + rpm[o + 2] + rmp[o] + rmp[o + 2]
-                                     + rmm[o] + rmm[o + 2];
-                    const T edge   = r0p[o] + r0p[o + 2] + r0m[o] + r0m[o + 2] + rp0[o] + rp0[o + 2]
-                                   + rm0[o] + rm0[o + 2] + rmm[o + 1] + rpm[o + 1] + rmp[o + 1]
-                                   + rpp[o + 1];
-                    cp[((size_t)X * cy + (y0 >> 1) + yl) * cz + Z + c2]
-                        = (T)(1. / 64.) * ((T)8. * r00[o + 1] + (T)4. * face + (T)2. * edge + corner);
-                }
-            }
-        }
+        if (RST && emit && xe > x0 && ((xe - x0) & 1)) pend = xe;
         __syncthreads();
         const int nxt = i + S;
         if (nxt < nplanes && nxt > issued)
@@ -952,6 +960,7 @@ __global__ void __launch_bounds__(256) plane_vec_kernel(PlaneParams p, DevCoef<T
             issued = nxt;
         }
     }
+    if (RST && pend >= 0) restrict_plane(pend);
     if (!ok && threadIdx.x == 0)
     {
         if (p.err != nullptr) atomicExch(p.err, MGX_TIMEOUT);
@@ -1060,7 +1069,7 @@ static int launch_vec(const PlaneParams& p0, const DevCoef<T>& c, int nfunc,
     if (RST && (((nx | ny) & 1) || (nz % 4)))
         return fail(MGX_UNSUPPORTED, "the fused restriction needs even x, y and z % 4 == 0");
     auto smem_for = [&](int t) {
-        return (size_t)S * (t + 2 + YO) * nz * esz + (RST ? 3 * (size_t)(t + 1) * nz * sizeof(T) : 0)
+        return (size_t)S * (t + 2 + YO) * nz * esz + (RST ? 4 * (size_t)(t + 1) * nz * sizeof(T) : 0)
                + S * 8;
     };
     int ty = std::min(32, (256 * NG * VEC) / nz - YO);
