@@ -671,6 +671,30 @@ int mgx_local_set_config(mgx_local* loc, int shape, int ctas_per_sm, int use_gra
 int mgx_local_get_config(const mgx_local* loc, int* shape, int* ctas_per_sm, int* use_graph);
 
 /* ---------------------------------------------------------------- */
+/* Function packing (FunctionsPacking with one task,                    */
+/* src/FunctionsPacking.cc:40-160): which localized orbitals may share  */
+/* a storage column.  Host code; no device is needed.                   */
+/* ---------------------------------------------------------------- */
+
+/* The domain of `grid` (origin 0) is cut into subdivx equal sub-boxes
+ * along x (Mesh::subdivx).  Orbital j's localization region is the sphere
+ * of radius radii[j] plus the subdomain margin (ghosts x |h| + 1e-8, as
+ * setupSubdomainGeometry with `ghosts` the operator's ghost width) around
+ * centers[3j .. 3j+2], periodic; it is listed in every sub-box it reaches
+ * (LocalizationRegions::computeSubdivOverlapGids,
+ * src/LocalizationRegions.cc:1039-1099).  Two orbitals overlap when a
+ * sub-box lists both (LocalizationRegions::overlap, :1103-1119).  The
+ * overlap graph is coloured by greedy multicolouring in decreasing-degree
+ * order (rlf = 0: greedyColor, src/tools/coloring.cc) or by Recursive
+ * Largest First (rlf = 1: colorRLF), with the reference's orders and tie
+ * rules.  colors[j] receives orbital j's colour (the gid2color_ map of
+ * FunctionsPacking::getColors), *ncolors their number.  With subdivx = 1
+ * every pair overlaps and the colours are all distinct, as in the
+ * reference's single-task runs. */
+int mgx_pack_functions(const mgx_grid* grid, int ghosts, int nfunc, const double* centers,
+    const float* radii, int subdivx, int rlf, int* colors, int* ncolors);
+
+/* ---------------------------------------------------------------- */
 /* Snapshots (the restart role of MGmol::dumpRestart / HDFrestart,      */
 /* src/MGmol.cc:1101-1127, src/HDFrestart.cc, without HDF5).            */
 /* ---------------------------------------------------------------- */

@@ -108,6 +108,8 @@ _SIGS = {
     "mgx_trade_boundaries": [ctypes.POINTER(Grid), _i, _i, _vp, _sz, _vp],
     "mgx_axpy": [_sz, _d, _i, _vp, _vp, _vp],
     "mgx_kernel_arch": [ctypes.POINTER(_i)],
+    "mgx_pack_functions": [ctypes.POINTER(Grid), _i, _i, _dp, ctypes.POINTER(ctypes.c_float), _i,
+                           _i, ctypes.POINTER(_i), ctypes.POINTER(_i)],
     "mgx_fd_apply": [_vp, _i, _i, _vp, _sz, _vp, _i, _vp],
     "mgx_rhs_mehr": [_vp, _i, _vp, _sz, _vp, _i, _vp],
     "mgx_hpsi": [_vp, _i, _i, _vp, _sz, _vp, _i, _vp, _i, _i, _vp],
@@ -210,6 +212,27 @@ def _check(status):
 
 def launches():
     return int(load().mgx_kernel_launch_count())
+
+
+def pack_functions(n, ll, centers, radii, subdivx, rlf=False, ghosts=1):
+    """FunctionsPacking of one task (mgx_pack_functions): the colour of each
+    orbital and the number of colours.  centers (nfunc x 3, bohr) and radii
+    (nfunc, stored as FP32 like the reference's localization regions)."""
+    import numpy as np
+    c = np.ascontiguousarray(centers, dtype=np.float64).reshape(-1, 3)
+    r = np.ascontiguousarray(radii, dtype=np.float32).reshape(-1)
+    if c.shape[0] != r.shape[0]:
+        raise ValueError("one radius per centre")
+    nf = r.shape[0]
+    colors = np.zeros(max(nf, 1), dtype=np.int32)
+    nc = _i()
+    g = Grid.make(n, ll)
+    _check(load().mgx_pack_functions(ctypes.byref(g), int(ghosts), nf, c.ctypes.data_as(_dp),
+                                     r.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
+                                     int(subdivx), 1 if rlf else 0,
+                                     colors.ctypes.data_as(ctypes.POINTER(_i)),
+                                     ctypes.byref(nc)))
+    return colors[:nf].copy(), nc.value
 
 
 def kernel_arch():

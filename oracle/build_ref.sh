@@ -18,7 +18,7 @@ mkdir -p "$OUT/obj"
 CXX=${CXX:-g++}
 FLAGS="-std=c++17 -O2 -fopenmp -ffp-contract=off -fPIC -w"
 INC="-I$HERE/shim -I$SRC -I$SRC/pb -I$SRC/tools -I$SRC/linear_algebra -I$SRC/local_matrices -I$SRC/DistMatrix -I$SRC/sparse_linear_algebra -I$SRC/radial"
-TUS="pb/Laph2.cc pb/Laph4.cc pb/Laph4M.cc pb/Laph6.cc pb/Laph8.cc tools/MPIdata.cc tools/MGmol_MPI.cc tools/mgmol_mpi_tools.cc Mesh.cc pb/FDkernels.cc pb/MGkernels.cc pb/Grid.cc pb/PEenv.cc pb/GridFunc.cc pb/GridFuncVector.cc pb/FDoper.cc pb/Lap.cc tools/Timer.cc tools/Vector3D.cc linear_algebra/mputils.cc GridMask.cc GridMaskMax.cc GridMaskMult.cc Map2Masks.cc SubCell.cc"
+TUS="pb/Laph2.cc pb/Laph4.cc pb/Laph4M.cc pb/Laph6.cc pb/Laph8.cc tools/MPIdata.cc tools/MGmol_MPI.cc tools/mgmol_mpi_tools.cc Mesh.cc pb/FDkernels.cc pb/MGkernels.cc pb/Grid.cc pb/PEenv.cc pb/GridFunc.cc pb/GridFuncVector.cc pb/FDoper.cc pb/Lap.cc tools/Timer.cc tools/Vector3D.cc linear_algebra/mputils.cc GridMask.cc GridMaskMax.cc GridMaskMult.cc Map2Masks.cc SubCell.cc tools/coloring.cc tools/SymmetricMatrix.cc"
 OBJS=""
 pids=""
 for tu in $TUS; do
@@ -28,6 +28,9 @@ for tu in $TUS; do
     OBJS="$OBJS $o"
 done
 $CXX $FLAGS $INC -c "$HERE/ref_driver.cpp" -o "$OUT/obj/ref_driver.o" &
+pids="$pids $!"
+# FunctionsPacking's colourings (tools/coloring.cc, tools/SymmetricMatrix.cc)
+$CXX $FLAGS $INC -c "$HERE/ref_pack.cpp" -o "$OUT/obj/ref_pack.o" &
 pids="$pids $!"
 # S and H through the reference's local matrices and LocalMatrices2DistMatrix
 # (its 1e-14 filter), with single-task stand-ins for the ScaLAPACK-backed
@@ -56,6 +59,6 @@ pids="$pids $!"
 $CXX $FLAGS -c "$HERE/shim/blas_shim.cpp" -o "$OUT/obj/blas_shim.o" &
 pids="$pids $!"
 for p in $pids; do wait $p; done
-$CXX $FLAGS -shared -o "$OUT/libmgref.so" $OBJS "$OUT/obj/ref_driver.o" "$OUT/obj/ref_matrices.o" "$OUT/obj/blas_shim.o" \
+$CXX $FLAGS -shared -o "$OUT/libmgref.so" $OBJS "$OUT/obj/ref_driver.o" "$OUT/obj/ref_pack.o" "$OUT/obj/ref_matrices.o" "$OUT/obj/blas_shim.o" \
     "$OUT/obj/AndersonMix_f.o" "$OUT/obj/AndersonMix_d.o" "$OUT/obj/ref_anderson.o"
 echo "build_ref: $OUT/libmgref.so"

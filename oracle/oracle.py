@@ -446,3 +446,139 @@ def rho(n, ll, psi, X, nel=0.0, ref=False):
     if rc != 0:
         raise RuntimeError("density charge off by more than 2%")
     return out, info[0], info[1]
+
+
+# ------------------------------------------------------------ function packing
+def pack_overlap(n, ll, centers, radii, subdivx, ghosts=1):
+    """The orbital overlap pattern of FunctionsPacking with one task (uint8
+    nfunc x nfunc, diagonal set).  Restates the subdomain geometry of
+    LocalizationRegions::setupSubdomainGeometry (src/LocalizationRegions.cc:
+    935-967: lattice L, margin ghosts (|h| + 1e-8), mesh lattice L - h),
+    computeSubdivOverlapGids (:1039-1099: each region, radius r + margin
+    rounded to float as LRData holds it, listed in every x sub-box whose
+    closest point lies within it) and overlap (:1103-1119: a shared
+    sub-box).  Pure Python loops, small cases."""
+    h = [ll[i] / n[i] for i in range(3)]
+    div = [ll[i] - h[i] for i in range(3)]
+    delta = (np.sqrt(h[0] * h[0] + h[1] * h[1] + h[2] * h[2]) + 1.e-8) * float(ghosts)
+    loc = ll[0] / subdivx
+    nf = len(radii)
+    inbox = np.zeros((nf, subdivx), dtype=bool)
+    for f in range(nf):
+        radius = np.float32(np.float64(np.float32(radii[f])) + delta)
+        r2 = float(radius * radius)  # float product, as the reference's
+        for iloc in range(subdivx):
+            cc = [0.5 * ((2 * iloc + 1) * loc), 0.5 * div[1], 0.5 * div[2]]
+            t = [float(centers[f][i]) for i in range(3)]
+            for i in range(3):
+                while t[i] >= cc[i] + 0.5 * ll[i]:
+                    t[i] -= ll[i]
+                while t[i] < cc[i] - 0.5 * ll[i]:
+                    t[i] += ll[i]
+            p = list(t)
+            if p[0] < iloc * loc:
+                p[0] = iloc * loc
+            if p[1] < 0.:
+                p[1] = 0.
+            if p[2] < 0.:
+                p[2] = 0.
+            if p[0] > (iloc + 1) * loc - h[0]:
+                p[0] = (iloc + 1) * loc - h[0]
+            if p[1] > div[1]:
+                p[1] = div[1]
+            if p[2] > div[2]:
+                p[2] = div[2]
+            d2 = (p[0] - t[0]) * (p[0] - t[0]) + (p[1] - t[1]) * (p[1] - t[1]) \
+                + (p[2] - t[2]) * (p[2] - t[2])
+            inbox[f, iloc] = d2 < r2
+    ov = (inbox.astype(np.int32) @ inbox.T.astype(np.int32)) > 0
+    np.fill_diagonal(ov, True)
+    return ov.astype(np.uint8)
+
+
+def _sort_desc(a, b, lo, hi):
+    """quicksortI_h2l (src/tools/coloring.cc): a descending, b alongside."""
+    i, j = lo, hi
+    x = a[(lo + hi) // 2]
+    while True:
+        while a[i] > x:
+            i += 1
+        while a[j] < x:
+            j -= 1
+        if i <= j:
+            a[i], a[j] = a[j], a[i]
+            b[i], b[j] = b[j], b[i]
+            i += 1
+            j -= 1
+        if not i <= j:
+            break
+    if lo < j:
+        _sort_desc(a, b, lo, j)
+    if i < hi:
+        _sort_desc(a, b, i, hi)
+
+
+def pack_colors(overlap, rlf=False):
+    """The colouring of FunctionsPacking::getColors (src/FunctionsPacking.cc:
+    79-158) on an overlap pattern: greedyColor (degree order of
+    quicksortI_h2l, then greedyMC's smallest free colour) or colorRLF
+    (src/tools/coloring.cc).  Returns (colour per function, colours)."""
+    ov = np.asarray(overlap).astype(bool)
+    nf = ov.shape[0]
+    color = [-1] * nf
+    if not rlf:
+        deg = [int(ov[i].sum()) for i in range(nf)]
+        order = list(range(nf))
+        if nf:
+            _sort_desc(deg, order, 0, nf - 1)
+        ncol = 0
+        for v in order:
+            taken = {color[j] for j in range(nf) if ov[v, j] and color[j] >= 0}
+            top = max(taken) if taken else -1
+            c = 0
+            while c <= top and c in taken:
+                c += 1
+            color[v] = c
+            ncol = max(ncol, c + 1)
+        return np.asarray(color, dtype=np.int32), ncol
+    unc = list(range(nf))
+    ncol = 0
+    while unc:
+        v0, best = -1, -1
+        for j in unc:  # the multimap keeps the last of equal degrees
+            d = sum(1 for i in unc if ov[i, j])
+            if d > 0 and d >= best:
+                v0, best = j, d
+        unc.remove(v0)
+        color[v0] = ncol
+        u = [i for i in unc if ov[i, v0]]
+        v = [i for i in unc if not ov[i, v0]]
+        while v:
+            u0, bu = -1, -1
+            for j in v:
+                d = sum(1 for i in u if ov[i, j])
+                if d >= bu:
+                    u0, bu = j, d
+            color[u0] = ncol
+            unc.remove(u0)
+            u += [i for i in v if ov[i, u0]]
+            v = [i for i in v if not ov[i, u0]]
+        ncol += 1
+    return np.asarray(color, dtype=np.int32), ncol
+
+
+def ref_pack_colors(overlap, rlf=False):
+    """The same colouring by the reference's own coloring.cc (None when the
+    reference was not built here)."""
+    L = ref_lib()
+    if L is None:
+        return None
+    ov = np.ascontiguousarray(overlap, dtype=np.uint8)
+    nf = ov.shape[0]
+    colors = np.zeros(max(nf, 1), dtype=np.int32)
+    nc = ctypes.c_int()
+    rc = L.ref_pack_colors(nf, ov.ctypes.data_as(ctypes.POINTER(ctypes.c_ubyte)),
+                           1 if rlf else 0, colors.ctypes.data_as(_ip), ctypes.byref(nc))
+    if rc != 0:
+        raise RuntimeError("ref_pack_colors failed")
+    return colors[:nf].copy(), nc.value

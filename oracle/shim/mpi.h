@@ -50,6 +50,7 @@ typedef struct { int MPI_SOURCE, MPI_TAG, MPI_ERROR; } MPI_Status;
 #define MPI_LAND 6
 #define MPI_MINLOC 7
 #define MPI_MAXLOC 8
+#define MPI_BOR 9
 
 static inline size_t oracle_mpi_size(MPI_Datatype t)
 {
