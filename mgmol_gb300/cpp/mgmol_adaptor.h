@@ -607,6 +607,29 @@ public:
     const mgx_masks* get() const { return m_; }
 };
 
+/* FunctionsPacking with one task (src/FunctionsPacking.h): the colour of
+ * each gid, from the localization regions' centres (nfunc x 3) and float
+ * radii, the mesh's x sub-boxes and the grid's ghost width; RLF or greedy
+ * colouring as Control::RLFColoring() selects.  Host only. */
+class FunctionsPacking
+{
+    std::vector<int> gid2color_;
+    int num_colors_ = 0;
+
+public:
+    FunctionsPacking(const pb::Grid& g, const double* centers, const float* radii, int nfunc,
+        int subdivx, bool rlf)
+        : gid2color_(nfunc)
+    {
+        check(mgx_pack_functions(&g.raw(), g.ghost_pt(), nfunc, centers, radii, subdivx,
+                  rlf ? 1 : 0, gid2color_.data(), &num_colors_),
+            "FunctionsPacking::setup");
+    }
+    short getNumColors() const { return (short)num_colors_; }
+    int getGlobalSize() const { return (int)gid2color_.size(); }
+    short getColor(int gid) const { return (short)gid2color_.at(gid); }
+};
+
 /* Rho<T>: the electronic density of a block of non-orthogonal orbitals
  * (device, one FP64 value per grid point) */
 template <typename T>

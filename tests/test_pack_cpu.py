@@ -5,6 +5,7 @@ both colourings and of the subdomain geometry, and against the reference
 colouring code itself when it is built here; plus the defining property
 (overlapping orbitals never share a colour).  Host code, no GPU."""
 import os
+import subprocess
 
 import numpy as np
 import pytest
@@ -80,3 +81,28 @@ def test_bad_arguments_are_reported():
         capi.pack_functions((64, 64, 64), (22.4,) * 3, np.zeros((2, 3)), np.ones(2), 65)
     col, nc = capi.pack_functions((64, 64, 64), (22.4,) * 3, np.zeros((0, 3)), np.ones(0), 4)
     assert col.size == 0 and nc == 0
+
+
+def test_adaptor_class_gives_the_library_colours(tmp_path):
+    """FunctionsPacking of mgmol_adaptor.h from a C++ program (host only)."""
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    cuda = os.environ.get("CUDA_HOME", "/usr/local/cuda")
+    libdir = os.path.dirname(capi.LIB_PATH)
+    capi.load()
+    exe = str(tmp_path / "test_pack")
+    cmd = ["g++", "-O2", "-std=c++17", "-I", os.path.join(root, "mgmol_gb300", "cpp"),
+           "-I", os.path.join(cuda, "include"), os.path.join(root, "tests", "cpp", "test_pack.cpp"),
+           "-o", exe, "-L", libdir, "-lmgx", f"-Wl,-rpath,{libdir}", "-L",
+           os.path.join(cuda, "lib64"), "-lcudart", f"-Wl,-rpath,{os.path.join(cuda, 'lib64')}"]
+    subprocess.run(cmd, check=True, capture_output=True)
+    rng = np.random.default_rng(9)
+    n, ll = (64, 48, 40), (22.4, 16.8, 14.0)
+    c = rng.uniform(0.0, 22.0, size=(40, 3))
+    r = rng.uniform(1.0, 3.0, size=40).astype(np.float32)
+    for rlf in (0, 1):
+        text = f"{n[0]} {n[1]} {n[2]} {ll[0]!r} {ll[1]!r} {ll[2]!r} 2 6 {rlf} 40\n" + "".join(
+            f"{a!r} {b!r} {d!r} {float(e)!r}\n" for (a, b, d), e in zip(c.tolist(), r))
+        out = subprocess.run([exe], input=text, capture_output=True, text=True, check=True).stdout
+        vals = [int(x) for x in out.split()]
+        col, nc = capi.pack_functions(n, ll, c, r, 6, rlf, ghosts=2)
+        assert vals[0] == nc and vals[1:] == col.tolist()
