@@ -590,7 +590,7 @@ def micro(argv=None):
     ap.add_argument("op", choices=["gram", "hmat", "gram_hmat", "matb", "gram_hmat_matb", "mult",
                                    "residual", "hpsi", "precond", "mgm", "dense", "dense_b",
                                    "dense_parts", "normalize", "mult_reuse", "h2d", "h2d_kernel",
-                                   "all"])
+                                   "centers", "all"])
     ap.add_argument("--streams", type=int, default=1, help="h2d: concurrent copy streams")
     ap.add_argument("--grid", type=int, nargs=3, default=[96, 96, 32])
     ap.add_argument("--h", type=float, default=0.25)
@@ -719,6 +719,10 @@ def micro(argv=None):
                 ctx.trace_prod(ctx.update_hb(S, th), Sinv)
             ms = _time(dense_b, args.warmup, args.reps)
             work, unit = (2 * N ** 3 / 3 + 4 * N ** 3 / 3 + 2 * N ** 3 + 2 * N ** 3), "TFLOP/s"
+        elif op == "centers":
+            # the position-matrix diagonal of SpreadsAndCenters: the block read once
+            ms = _time(lambda: ctx.sincos_diag(psi), args.warmup, args.reps)
+            work, unit = N * npts * s, "GB/s"
         elif op == "h2d":
             # pinned host block -> device block, split over --streams streams
             host = torch.empty(psi.shape, dtype=dt, pin_memory=True)

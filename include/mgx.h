@@ -671,6 +671,24 @@ int mgx_local_set_config(mgx_local* loc, int shape, int ctas_per_sm, int use_gra
 int mgx_local_get_config(const mgx_local* loc, int* shape, int* ctas_per_sm, int* use_graph);
 
 /* ---------------------------------------------------------------- */
+/* Centres and spreads of the orbitals (SpreadsAndCenters,              */
+/* src/SpreadsAndCenters.cc:26-104, SinCosOps::computeDiag,             */
+/* src/SinCosOps.cc:733-826).                                           */
+/* ---------------------------------------------------------------- */
+
+/* out (device, nfunc x 6 doubles, row f = orbital f): the diagonal
+ * position-matrix elements a = vel sum_p psi_f(p)^2 t(p) with t = (cos x,
+ * sin x, cos y, sin y, cos z, sin z), x = 2 pi i / n per direction, each
+ * scaled by L / (2 pi) (pb::Grid::getSinCosFunctions); divided by the
+ * norm vel sum psi_f^2 unless `normalized`.  The centre along x is
+ * L / (2 pi) atan2(a_1, a_0), taken in [0, L), and the squared spread
+ * (L / (2 pi))^2 - a_0^2 - a_1^2 (SpreadsAndCenters::computeCenter,
+ * computeSpread2).  FP32 or FP64 blocks, FP64 sums in a fixed order.  The
+ * first call on a context uploads the grid's tables (synchronous). */
+int mgx_sincos_diag(mgx_ctx* ctx, mgx_dtype dtype, const void* psi, size_t ld, int nfunc,
+    int normalized, double* out, void* stream);
+
+/* ---------------------------------------------------------------- */
 /* Function packing (FunctionsPacking with one task,                    */
 /* src/FunctionsPacking.cc:40-160): which localized orbitals may share  */
 /* a storage column.  Host code; no device is needed.                   */

@@ -108,6 +108,7 @@ _SIGS = {
     "mgx_trade_boundaries": [ctypes.POINTER(Grid), _i, _i, _vp, _sz, _vp],
     "mgx_axpy": [_sz, _d, _i, _vp, _vp, _vp],
     "mgx_kernel_arch": [ctypes.POINTER(_i)],
+    "mgx_sincos_diag": [_vp, _i, _vp, _sz, _i, _i, _vp, _vp],
     "mgx_pack_functions": [ctypes.POINTER(Grid), _i, _i, _dp, ctypes.POINTER(ctypes.c_float), _i,
                            _i, ctypes.POINTER(_i), ctypes.POINTER(_i)],
     "mgx_fd_apply": [_vp, _i, _i, _vp, _sz, _vp, _i, _vp],
@@ -578,6 +579,31 @@ class Context:
         _check(load().mgx_rho(self.handle, mode, _dtype(psi), p, ld, nf, _ptr(Xc), float(nel),
                               _ptr(rho), ctypes.byref(q), pw, nw, _stream(stream)))
         return rho, q.value
+
+    # ------------------------------------------------------------ centres
+    def sincos_diag(self, psi, normalized=False, out=None, stream=None):
+        """The diagonal position-matrix elements of the block (mgx_sincos_diag):
+        an (nfunc, 6) FP64 device tensor, columns cos x, sin x, cos y, sin y,
+        cos z, sin z (scaled by L / (2 pi))."""
+        p, ld, nf = _block(psi, self.npts)
+        import torch
+        out = torch.empty((nf, 6), dtype=torch.float64, device=psi.device) if out is None else out
+        _check(load().mgx_sincos_diag(self.handle, _dtype(psi), p, ld, nf, 1 if normalized else 0,
+                                      _ptr(out), _stream(stream)))
+        return out
+
+    def centers_spreads(self, psi, normalized=False, stream=None):
+        """Centres (nfunc x 3, in [0, L)) and spreads (nfunc) of the orbitals,
+        SpreadsAndCenters::computeCenter / computeSpread from sincos_diag."""
+        import numpy as np
+        a = self.sincos_diag(psi, normalized, stream=stream).cpu().numpy()
+        ll = np.asarray(self.ll)
+        lby2pi = ll * (0.5 / np.pi)
+        c, s = a[:, 0::2], a[:, 1::2]
+        x = lby2pi[None, :] * np.arctan2(s, c)
+        x = np.where(x < 0., x + ll[None, :], x)
+        spread2 = (lby2pi[None, :] ** 2 - c * c - s * s).sum(axis=1)
+        return x, np.sqrt(spread2)
 
     # ------------------------------------------------------------ Poisson
     def mgm(self, vh, rho, lap_type=LAP_MEHR4, max_levels=10, max_sweeps=10, tol=1e-16, nu1=2,

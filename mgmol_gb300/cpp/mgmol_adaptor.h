@@ -31,6 +31,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <stdexcept>
 #include <type_traits>
@@ -605,6 +606,62 @@ public:
             "MasksSet::apply");
     }
     const mgx_masks* get() const { return m_; }
+};
+
+/* SpreadsAndCenters<T> (src/SpreadsAndCenters.h) for one block: the
+ * diagonal position-matrix elements on the device, read back once, then
+ * the centres and spreads on the host as computeCenter / computeSpread2 do
+ * (src/SpreadsAndCenters.cc:26-104). */
+template <typename T>
+class SpreadsAndCenters
+{
+    double cell_[3];
+    std::vector<double> r_; // nfunc x 6: cos x, sin x, cos y, sin y, cos z, sin z
+
+public:
+    explicit SpreadsAndCenters(const pb::Grid& g)
+    {
+        for (int i = 0; i < 3; i++)
+            cell_[i] = g.raw().ll[i];
+    }
+    /* computePositionMatrix(orbitals) (the functions need not be normalized) */
+    void computePositionMatrix(const OrbitalBlock<T>& orbitals, bool normalized = false)
+    {
+        const int nf = orbitals.chromatic_number();
+        DeviceArray<double> a((size_t)nf * 6);
+        check(mgx_sincos_diag(orbitals.ctx(), dtype_of<T>(), orbitals.psi(0), orbitals.numpt(),
+                  nf, normalized ? 1 : 0, a.data(), nullptr),
+            "SpreadsAndCenters::computePositionMatrix");
+        r_.resize((size_t)nf * 6);
+        cuda(cudaMemcpy(r_.data(), a.data(), r_.size() * sizeof(double), cudaMemcpyDeviceToHost),
+            "SpreadsAndCenters::computePositionMatrix");
+    }
+    int size() const { return (int)(r_.size() / 6); }
+    /* the centre of orbital i, each coordinate in [0, L) */
+    std::array<double, 3> computeCenter(int i) const
+    {
+        std::array<double, 3> x;
+        for (int d = 0; d < 3; d++)
+        {
+            double v = cell_[d] * (0.5 * M_1_PI) * std::atan2(r_.at(6 * i + 2 * d + 1),
+                                                       r_.at(6 * i + 2 * d));
+            if (v < 0.) v += cell_[d];
+            x[d] = v;
+        }
+        return x;
+    }
+    double computeSpread2(int i) const
+    {
+        double s = 0.;
+        for (int d = 0; d < 3; d++)
+        {
+            const double lby2pi = 0.5 * M_1_PI * cell_[d];
+            const double c = r_.at(6 * i + 2 * d), sn = r_.at(6 * i + 2 * d + 1);
+            s += lby2pi * lby2pi - c * c - sn * sn;
+        }
+        return s;
+    }
+    double computeSpread(int i) const { return std::sqrt(computeSpread2(i)); }
 };
 
 /* FunctionsPacking with one task (src/FunctionsPacking.h): the colour of

@@ -120,6 +120,9 @@ struct mgx_ctx
     mgx::DeviceBuffer mgm;
     // partial sums of the reductions
     mgx::DeviceBuffer red;
+    // the grid's sine / cosine tables of the centre computation, filled by
+    // its first call
+    mgx::DeviceBuffer sincos;
 };
 
 /* ---------------- PTX helpers: mbarrier + 1-D bulk copies ---------------- */

@@ -582,3 +582,58 @@ def ref_pack_colors(overlap, rlf=False):
     if rc != 0:
         raise RuntimeError("ref_pack_colors failed")
     return colors[:nf].copy(), nc.value
+
+
+# ------------------------------------------------------------ centres and spreads
+def sincos_tables(n, ll, ref=False):
+    """pb::Grid::getSinCosFunctions (src/pb/Grid.cc:244-282) in FP64, one
+    task: per direction cos(i 2 pi / n) L / (2 pi), then sin; concatenated
+    as cos x, sin x, cos y, sin y, cos z, sin z.  ref: the reference's own
+    Grid (None when it was not built here)."""
+    if ref:
+        L = ref_lib()
+        if L is None:
+            return None
+        out = np.zeros(2 * sum(n))
+        L.ref_sincos_tables((ctypes.c_int * 3)(*n), (ctypes.c_double * 3)(*ll), _p(out))
+        return out
+    import math
+    parts = []
+    for d in range(3):
+        alpha = ll[d] * (0.5 * (1.0 / math.pi))
+        hh = 2. * math.pi / float(n[d])
+        parts.append([math.cos(float(i) * hh) * alpha for i in range(n[d])])
+        parts.append([math.sin(float(i) * hh) * alpha for i in range(n[d])])
+    return np.asarray(sum(parts, []))
+
+
+def sincos_diag(n, ll, psi, normalized=False):
+    """SinCosOps::computeDiag (src/SinCosOps.cc:733-826) with one task and
+    one subdomain: per orbital the six sums vel sum psi^2 t, divided by the
+    norm vel sum psi^2 unless normalized (FP64, (nfunc, 6))."""
+    t = sincos_tables(n, ll)
+    nx, ny, nz = n
+    cx, sx = t[0:nx], t[nx:2 * nx]
+    cy, sy = t[2 * nx:2 * nx + ny], t[2 * nx + ny:2 * nx + 2 * ny]
+    cz, sz = t[2 * nx + 2 * ny:2 * nx + 2 * ny + nz], t[2 * nx + 2 * ny + nz:]
+    vel = (ll[0] / nx) * (ll[1] / ny) * (ll[2] / nz)
+    a = np.asarray(psi, dtype=np.float64).reshape(-1, nx, ny, nz) ** 2
+    out = np.stack([np.einsum("fxyz,x->f", a, cx), np.einsum("fxyz,x->f", a, sx),
+                    np.einsum("fxyz,y->f", a, cy), np.einsum("fxyz,y->f", a, sy),
+                    np.einsum("fxyz,z->f", a, cz), np.einsum("fxyz,z->f", a, sz)], axis=1)
+    if normalized:
+        return vel * out
+    norm = vel * a.reshape(a.shape[0], -1).sum(axis=1)
+    return vel * out / norm[:, None]
+
+
+def centers_spreads(ll, a):
+    """SpreadsAndCenters::computeCenter and computeSpread
+    (src/SpreadsAndCenters.cc:26-104) from the (nfunc, 6) elements."""
+    import math
+    ll = np.asarray(ll, dtype=np.float64)
+    lby2pi = ll * (0.5 * (1.0 / math.pi))
+    c, s = a[:, 0::2], a[:, 1::2]
+    x = lby2pi[None, :] * np.arctan2(s, c)
+    x = np.where(x < 0., x + ll[None, :], x)
+    return x, np.sqrt((lby2pi[None, :] ** 2 - c * c - s * s).sum(axis=1))

@@ -483,6 +483,19 @@ extern "C" {
 /* The single-task environment (PEenv, MGmol_MPI::setup), set up once per
  * process; the S and H driver (ref_matrices.cpp) needs MGmol_MPI too. */
 void ref_env_init() { (void)env(); }
+/* pb::Grid::getSinCosFunctions (src/pb/Grid.cc:244-282) in FP64: out holds
+ * cos x, sin x (n[0] each), cos y, sin y, cos z, sin z */
+int ref_sincos_tables(const int* n, const double* ll, double* out)
+{
+    pb::Grid g = make_grid(n, ll, 1);
+    std::vector<double> sx, sy, sz, cx, cy, cz;
+    g.getSinCosFunctions(sx, sy, sz, cx, cy, cz);
+    size_t o = 0;
+    for (const auto* v : { &cx, &sx, &cy, &sy, &cz, &sz })
+        for (double x : *v)
+            out[o++] = x;
+    return 0;
+}
 int ref_mult_matrix_d(int np, int nf, const double* p, const double* th, double* o) { return mult_matrix(np, nf, p, th, o); }
 int ref_mult_matrix_f(int np, int nf, const float* p, const double* th, float* o) { return mult_matrix(np, nf, p, th, o); }
 int ref_residual_d(const int* n, const double* ll, int nf, const double* p, const double* h, const double* th, double* o) { return residual(n, ll, nf, p, h, th, o); }

@@ -383,6 +383,65 @@ static void test_matb_normalize()
     std::printf("ok   normalize, computeMatB, ProjectedMatricesMehrstellen, Rho\n");
 }
 
+/* SpreadsAndCenters: Gaussian orbitals (periodic images summed) put their
+ * centre where they were placed; the spread is the periodic formula
+ * sum_d (1 - exp(-k_d^2 s2)) / k_d^2 with s2 = sigma^2 / 2 */
+static void test_spreads_and_centers()
+{
+    const double origin[3] = { 0., 0., 0. }, ll[3] = { 12.8, 11.2, 9.6 };
+    const unsigned n[3] = { 40, 36, 32 };
+    pb::Grid grid(origin, ll, n, 1);
+    const int nf = 3;
+    const double c[nf][3] = { { 1.1, 10.9, 4.0 }, { 6.4, 5.6, 9.5 }, { 12.2, 0.3, 0.05 } };
+    const double sig = 1.0;
+    OrbitalBlock<double> phi(grid, nf);
+    std::vector<double> all((size_t)nf * grid.size());
+    const double h[3] = { grid.hgrid(0), grid.hgrid(1), grid.hgrid(2) };
+    for (int f = 0; f < nf; f++)
+        for (unsigned x = 0; x < n[0]; x++)
+            for (unsigned y = 0; y < n[1]; y++)
+                for (unsigned z = 0; z < n[2]; z++)
+                {
+                    double v = 1.;
+                    const unsigned idx[3] = { x, y, z };
+                    for (int d = 0; d < 3; d++)
+                    {
+                        double g = 0.;
+                        for (int img = -2; img <= 2; img++)
+                        {
+                            const double t = idx[d] * h[d] - c[f][d] + img * ll[d];
+                            g += std::exp(-t * t / (2 * sig * sig));
+                        }
+                        v *= g;
+                    }
+                    all[(size_t)f * grid.size() + ((size_t)x * n[1] + y) * n[2] + z] = v;
+                }
+    phi.set(all.data());
+    SpreadsAndCenters<double> sc(grid);
+    sc.computePositionMatrix(phi);
+    double err = 0., serr = 0.;
+    double expect = 0.;
+    for (int d = 0; d < 3; d++)
+    {
+        const double k = 2 * M_PI / ll[d];
+        expect += (1. - std::exp(-k * k * sig * sig / 2)) / (k * k);
+    }
+    for (int f = 0; f < nf; f++)
+    {
+        const auto x = sc.computeCenter(f);
+        for (int d = 0; d < 3; d++)
+        {
+            double dd = x[d] - c[f][d];
+            dd -= ll[d] * std::round(dd / ll[d]);
+            err = std::max(err, std::fabs(dd));
+        }
+        serr = std::max(serr, std::fabs(sc.computeSpread2(f) - expect));
+    }
+    CHECK(err < 1e-6, "SpreadsAndCenters centre error %g", err);
+    CHECK(serr < 1e-5, "SpreadsAndCenters spread^2 error %g", serr);
+    std::printf("ok   SpreadsAndCenters\n");
+}
+
 int main()
 {
     try
@@ -394,6 +453,7 @@ int main()
         test_hamiltonian_and_precond();
         test_residual_and_mgm();
         test_matb_normalize();
+        test_spreads_and_centers();
     }
     catch (const std::exception& e)
     {

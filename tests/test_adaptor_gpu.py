@@ -34,4 +34,4 @@ def test_reference_unit_tests_through_the_adaptor():
     r = subprocess.run([exe], capture_output=True, text=True, timeout=300)
     print(r.stdout)
     assert r.returncode == 0, r.stdout + r.stderr
-    assert r.stdout.count("ok ") == 7
+    assert r.stdout.count("ok ") == 8
