@@ -104,19 +104,19 @@ __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e)
 }
 
 /* The FP32 form of the partial sums, at FP64 accuracy on the FP32 units:
- * psi^2 = ah + al exactly (al by an FMA); each warp keeps, per z index its
- * lanes own, the double-float sum over its rows of psi^2 (the z profile, in
- * shared memory) and forms each row's double-float total with a butterfly
- * of two-sums, which lane 0 turns to FP64 and weights by the row's x and y
- * factors.  The z weights are applied to the z profile at the end.  Needs
- * nz <= MAXZ. */
-constexpr int MAXZ = 768;
+ * psi^2 = ah + al exactly (al by an FMA); each lane keeps, for the z
+ * indices it owns (l + 32 j, j < ZPL), the double-float sum over its rows
+ * of psi^2 (the z profile) in registers, and the warp forms each row's
+ * double-float total with a butterfly of two-sums, which lane 0 turns to
+ * FP64 and weights by the row's x and y factors.  The z weights are
+ * applied to the z profile at the end.  Needs nz <= 32 ZPL. */
+constexpr int ZPL  = 8;
+constexpr int MAXZ = 32 * ZPL;
 
 __global__ void __launch_bounds__(THREADS) sincos_partial_f32_kernel(const float* __restrict__ psi,
     size_t ld, int nx, int ny, int nz, const double* __restrict__ tab,
     double* __restrict__ partial)
 {
-    extern __shared__ float2 zprof[]; // [WPB][nz]: (hi, lo)
     constexpr int WPB = THREADS / 32;
     const int f       = blockIdx.y;
     const int nblk    = gridDim.x;
@@ -124,29 +124,33 @@ __global__ void __launch_bounds__(THREADS) sincos_partial_f32_kernel(const float
     const double *cx = tab, *sx = tab + nx, *cy = tab + 2 * nx, *sy = cy + ny,
                  *cz = tab + 2 * nx + 2 * ny, *sz = cz + nz;
     const int w = threadIdx.x / 32, l = threadIdx.x % 32;
-    float2* zw  = zprof + (size_t)w * nz;
-    for (int iz = l; iz < nz; iz += 32)
-        zw[iz] = make_float2(0.f, 0.f);
+    float zh[ZPL], zl[ZPL];
+#pragma unroll
+    for (int j = 0; j < ZPL; j++)
+        zh[j] = zl[j] = 0.f;
     double acc[5] = { 0., 0., 0., 0., 0. }; // lane 0: cos x, sin x, cos y, sin y, norm
     const int nrows = nx * ny;
     for (int r = blockIdx.x * WPB + w; r < nrows; r += nblk * WPB)
     {
         const float* row = p + (size_t)r * nz;
         float rh = 0.f, rl = 0.f;
-        for (int iz = l; iz < nz; iz += 32)
+#pragma unroll
+        for (int j = 0; j < ZPL; j++)
         {
-            const float v  = row[iz];
-            const float ah = __fmul_rn(v, v);
-            const float al = fmaf(v, v, -ah);
-            float s, e;
-            two_sum(rh, ah, s, e);
-            rh = s;
-            rl += e + al;
-            float2 z = zw[iz];
-            two_sum(z.x, ah, s, e);
-            z.x = s;
-            z.y += e + al;
-            zw[iz] = z;
+            const int iz = l + 32 * j;
+            if (iz < nz)
+            {
+                const float v  = row[iz];
+                const float ah = __fmul_rn(v, v);
+                const float al = fmaf(v, v, -ah);
+                float s, e;
+                two_sum(rh, ah, s, e);
+                rh = s;
+                rl += e + al;
+                two_sum(zh[j], ah, s, e);
+                zh[j] = s;
+                zl[j] += e + al;
+            }
         }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1)
@@ -169,19 +173,18 @@ __global__ void __launch_bounds__(THREADS) sincos_partial_f32_kernel(const float
             acc[4] += t;
         }
     }
-    __syncthreads();
-    // the z weights on the block's z profile
+    // the z weights on this lane's part of the z profile
     double c4 = 0., c5 = 0.;
-    for (int iz = threadIdx.x; iz < nz; iz += THREADS)
+#pragma unroll
+    for (int j = 0; j < ZPL; j++)
     {
-        double zsum = 0.;
-        for (int q = 0; q < WPB; q++)
+        const int iz = l + 32 * j;
+        if (iz < nz)
         {
-            const float2 z = zprof[(size_t)q * nz + iz];
-            zsum += (double)z.x + (double)z.y;
+            const double z = (double)zh[j] + (double)zl[j];
+            c4 += cz[iz] * z;
+            c5 += sz[iz] * z;
         }
-        c4 += cz[iz] * zsum;
-        c5 += sz[iz] * zsum;
     }
     __shared__ double red[WPB][NSUM];
     const double vals[NSUM] = { acc[0], acc[1], acc[2], acc[3], c4, c5, acc[4] };
@@ -271,17 +274,7 @@ int mgx_sincos_diag(mgx_ctx* ctx, mgx_dtype dtype, const void* psi, size_t ld, i
     const dim3 grid(nblk, nfunc);
     if (dtype == MGX_F32 && g.n[2] <= cen::MAXZ)
     {
-        const size_t smem = (size_t)(cen::THREADS / 32) * g.n[2] * sizeof(float2);
-        static bool attr = false;
-        if (!attr)
-        {
-            MGX_TRY(cuda_check(cudaFuncSetAttribute(cen::sincos_partial_f32_kernel,
-                                   cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)((cen::THREADS / 32) * cen::MAXZ * sizeof(float2))),
-                "sincos smem attribute"));
-            attr = true;
-        }
-        cen::sincos_partial_f32_kernel<<<grid, cen::THREADS, smem, s>>>((const float*)psi, ld,
+        cen::sincos_partial_f32_kernel<<<grid, cen::THREADS, 0, s>>>((const float*)psi, ld,
             g.n[0], g.n[1], g.n[2], dtab, part);
         MGX_LAUNCH_CHECK("sincos_partial_f32_kernel");
     }
