@@ -24,7 +24,7 @@ def fro_rel(a, b):
     return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
 
 
-# tolerances: FP64 path vs the FP64 oracle (BASELINE: 1e-12 relative);
+# tolerances: FP64 path vs the FP64 oracle (the stated 1e-12 relative);
 # FP32 path (FP32 arithmetic) vs the FP64 oracle
 TOL_F64 = 1e-12
 TOL_F32 = 2e-5
