@@ -107,28 +107,28 @@ __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e)
  * psi^2 = ah + al exactly (al by an FMA); each lane keeps, for the z
  * indices it owns (l + 32 j, j < ZPL), the double-float sum over its rows
  * of psi^2 (the z profile) in registers, and the warp forms each row's
- * double-float total with a butterfly of two-sums, which lane 0 turns to
- * FP64 and weights by the row's x and y factors.  The z weights are
- * applied to the z profile at the end.  Needs nz <= 32 ZPL. */
+ * double-float total with a butterfly of two-sums, which lane 0 stores as
+ * one FP64 value in rowsum (the x and y weights are applied to those by
+ * sincos_rows_kernel, off this loop).  The z weights are applied to the z
+ * profile at the end; the other sums of this kernel's partials are 0.
+ * Needs nz <= 32 ZPL. */
 constexpr int ZPL  = 8;
 constexpr int MAXZ = 32 * ZPL;
 
 __global__ void __launch_bounds__(THREADS) sincos_partial_f32_kernel(const float* __restrict__ psi,
     size_t ld, int nx, int ny, int nz, const double* __restrict__ tab,
-    double* __restrict__ partial)
+    double* __restrict__ partial, double* __restrict__ rowsum)
 {
     constexpr int WPB = THREADS / 32;
     const int f       = blockIdx.y;
     const int nblk    = gridDim.x;
     const float* p    = psi + (size_t)f * ld;
-    const double *cx = tab, *sx = tab + nx, *cy = tab + 2 * nx, *sy = cy + ny,
-                 *cz = tab + 2 * nx + 2 * ny, *sz = cz + nz;
+    const double *cz = tab + 2 * nx + 2 * ny, *sz = cz + nz;
     const int w = threadIdx.x / 32, l = threadIdx.x % 32;
     float zh[ZPL], zl[ZPL];
 #pragma unroll
     for (int j = 0; j < ZPL; j++)
         zh[j] = zl[j] = 0.f;
-    double acc[5] = { 0., 0., 0., 0., 0. }; // lane 0: cos x, sin x, cos y, sin y, norm
     const int nrows = nx * ny;
     for (int r = blockIdx.x * WPB + w; r < nrows; r += nblk * WPB)
     {
@@ -162,16 +162,7 @@ __global__ void __launch_bounds__(THREADS) sincos_partial_f32_kernel(const float
             rh = s;
             rl += ol + e;
         }
-        if (l == 0)
-        {
-            const int ix = r / ny, iy = r - ix * ny;
-            const double t = (double)rh + (double)rl;
-            acc[0] += cx[ix] * t;
-            acc[1] += sx[ix] * t;
-            acc[2] += cy[iy] * t;
-            acc[3] += sy[iy] * t;
-            acc[4] += t;
-        }
+        if (l == 0) rowsum[(size_t)f * nrows + r] = (double)rh + (double)rl;
     }
     // the z weights on this lane's part of the z profile
     double c4 = 0., c5 = 0.;
@@ -187,7 +178,7 @@ __global__ void __launch_bounds__(THREADS) sincos_partial_f32_kernel(const float
         }
     }
     __shared__ double red[WPB][NSUM];
-    const double vals[NSUM] = { acc[0], acc[1], acc[2], acc[3], c4, c5, acc[4] };
+    const double vals[NSUM] = { 0., 0., 0., 0., c4, c5, 0. };
 #pragma unroll
     for (int k = 0; k < NSUM; k++)
     {
@@ -201,6 +192,47 @@ __global__ void __launch_bounds__(THREADS) sincos_partial_f32_kernel(const float
         for (int q = 0; q < WPB; q++)
             t += red[q][threadIdx.x];
         partial[((size_t)f * nblk + blockIdx.x) * NSUM + threadIdx.x] = t;
+    }
+}
+
+/* the x and y weights on the row totals of sincos_partial_f32_kernel, one
+ * block per function, rows in a fixed order per thread and a fixed-order
+ * block sum; added into block 0's partials of sums 0-3 and 6 */
+__global__ void __launch_bounds__(THREADS) sincos_rows_kernel(const double* __restrict__ rowsum,
+    int nx, int ny, const double* __restrict__ tab, int nblk, double* __restrict__ partial)
+{
+    const int f      = blockIdx.x;
+    const int nrows  = nx * ny;
+    const double* rs = rowsum + (size_t)f * nrows;
+    const double *cx = tab, *sx = tab + nx, *cy = tab + 2 * nx, *sy = cy + ny;
+    double acc[5] = { 0., 0., 0., 0., 0. };
+    for (int r = threadIdx.x; r < nrows; r += THREADS)
+    {
+        const int ix = r / ny, iy = r - ix * ny;
+        const double t = rs[r];
+        acc[0] += cx[ix] * t;
+        acc[1] += sx[ix] * t;
+        acc[2] += cy[iy] * t;
+        acc[3] += sy[iy] * t;
+        acc[4] += t;
+    }
+    constexpr int WPB = THREADS / 32;
+    __shared__ double red[WPB][5];
+    const int w = threadIdx.x / 32, l = threadIdx.x % 32;
+#pragma unroll
+    for (int k = 0; k < 5; k++)
+    {
+        const double v = warp_sum(acc[k]);
+        if (l == 0) red[w][k] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < 5)
+    {
+        double t = 0.;
+        for (int q = 0; q < WPB; q++)
+            t += red[q][threadIdx.x];
+        const int k = threadIdx.x < 4 ? threadIdx.x : 6;
+        partial[(size_t)f * nblk * NSUM + k] += t;
     }
 }
 
@@ -269,14 +301,20 @@ int mgx_sincos_diag(mgx_ctx* ctx, mgx_dtype dtype, const void* psi, size_t ld, i
     const int wpb   = cen::THREADS / 32;
     const int nblk  = std::max(1, std::min((nrows + wpb - 1) / wpb,
                                      (8 * ctx->sm_count + nfunc - 1) / nfunc));
-    MGX_TRY(ctx->red.ensure((size_t)nfunc * nblk * cen::NSUM * sizeof(double)));
-    double* part = (double*)ctx->red.ptr;
+    const size_t part_bytes = (size_t)nfunc * nblk * cen::NSUM * sizeof(double);
+    const bool f32 = (dtype == MGX_F32 && g.n[2] <= cen::MAXZ);
+    MGX_TRY(ctx->red.ensure(part_bytes + (f32 ? (size_t)nfunc * nrows * sizeof(double) : 0)));
+    double* part   = (double*)ctx->red.ptr;
+    double* rowsum = (double*)((char*)ctx->red.ptr + part_bytes);
     const dim3 grid(nblk, nfunc);
-    if (dtype == MGX_F32 && g.n[2] <= cen::MAXZ)
+    if (f32)
     {
         cen::sincos_partial_f32_kernel<<<grid, cen::THREADS, 0, s>>>((const float*)psi, ld,
-            g.n[0], g.n[1], g.n[2], dtab, part);
+            g.n[0], g.n[1], g.n[2], dtab, part, rowsum);
         MGX_LAUNCH_CHECK("sincos_partial_f32_kernel");
+        cen::sincos_rows_kernel<<<nfunc, cen::THREADS, 0, s>>>(rowsum, g.n[0], g.n[1], dtab, nblk,
+            part);
+        MGX_LAUNCH_CHECK("sincos_rows_kernel");
     }
     else
     {
