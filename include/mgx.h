@@ -688,6 +688,19 @@ int mgx_local_get_config(const mgx_local* loc, int* shape, int* ctas_per_sm, int
 int mgx_sincos_diag(mgx_ctx* ctx, mgx_dtype dtype, const void* psi, size_t ld, int nfunc,
     int normalized, double* out, void* stream);
 
+/* Localization regions of one task (LocalizationRegions, host code).
+ * move_to (LocalizationRegions::moveTo, src/LocalizationRegions.cc:405-450):
+ * each centre (nfunc x 3, in place) moves toward its target by the
+ * periodic minimum-image difference (Vector3D::vminimage), shortened to
+ * 1 bohr when longer; *max_displ receives the longest difference.
+ * update_radii (LocalizationRegions::updateRadii, :354-366, getMeanRadius,
+ * :332-352): radii[j] = ratio x spreads[j] as float, *mean_radius the cube
+ * root of the mean cube.  The new centres and radii go to mgx_masks_update. */
+int mgx_regions_move_to(int nfunc, double* centers, const double* targets, const double cell[3],
+    float* max_displ);
+int mgx_regions_update_radii(int nfunc, const double* spreads, float ratio, float* radii,
+    float* mean_radius);
+
 /* ---------------------------------------------------------------- */
 /* Function packing (FunctionsPacking with one task,                    */
 /* src/FunctionsPacking.cc:40-160): which localized orbitals may share  */

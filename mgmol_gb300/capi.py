@@ -108,6 +108,9 @@ _SIGS = {
     "mgx_trade_boundaries": [ctypes.POINTER(Grid), _i, _i, _vp, _sz, _vp],
     "mgx_axpy": [_sz, _d, _i, _vp, _vp, _vp],
     "mgx_kernel_arch": [ctypes.POINTER(_i)],
+    "mgx_regions_move_to": [_i, _dp, _dp, _dp, ctypes.POINTER(ctypes.c_float)],
+    "mgx_regions_update_radii": [_i, _dp, ctypes.c_float, ctypes.POINTER(ctypes.c_float),
+                                 ctypes.POINTER(ctypes.c_float)],
     "mgx_sincos_diag": [_vp, _i, _vp, _sz, _i, _i, _vp, _vp],
     "mgx_pack_functions": [ctypes.POINTER(Grid), _i, _i, _dp, ctypes.POINTER(ctypes.c_float), _i,
                            _i, ctypes.POINTER(_i), ctypes.POINTER(_i)],
@@ -213,6 +216,34 @@ def _check(status):
 
 def launches():
     return int(load().mgx_kernel_launch_count())
+
+
+def regions_move_to(centers, targets, cell):
+    """LocalizationRegions::moveTo (mgx_regions_move_to): new centres
+    (nfunc x 3) and the largest move before the 1-bohr cap."""
+    import numpy as np
+    c = np.array(centers, dtype=np.float64, order="C").reshape(-1, 3)
+    t = np.ascontiguousarray(targets, dtype=np.float64).reshape(-1, 3)
+    if t.shape != c.shape:
+        raise ValueError("one target per centre")
+    cl = np.ascontiguousarray(cell, dtype=np.float64)
+    mx = ctypes.c_float()
+    _check(load().mgx_regions_move_to(c.shape[0], c.ctypes.data_as(_dp), t.ctypes.data_as(_dp),
+                                      cl.ctypes.data_as(_dp), ctypes.byref(mx)))
+    return c, mx.value
+
+
+def regions_update_radii(spreads, ratio):
+    """LocalizationRegions::updateRadii (mgx_regions_update_radii): FP32
+    radii ratio x spread and their mean radius."""
+    import numpy as np
+    sp = np.ascontiguousarray(spreads, dtype=np.float64).reshape(-1)
+    r = np.zeros(sp.size, dtype=np.float32)
+    mean = ctypes.c_float()
+    _check(load().mgx_regions_update_radii(sp.size, sp.ctypes.data_as(_dp), ctypes.c_float(ratio),
+                                           r.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
+                                           ctypes.byref(mean)))
+    return r, mean.value
 
 
 def pack_functions(n, ll, centers, radii, subdivx, rlf=False, ghosts=1):

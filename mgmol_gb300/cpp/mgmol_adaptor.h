@@ -36,6 +36,7 @@
 #include <stdexcept>
 #include <type_traits>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "../../include/mgx.h"
@@ -662,6 +663,66 @@ public:
         return s;
     }
     double computeSpread(int i) const { return std::sqrt(computeSpread2(i)); }
+};
+
+/* LocalizationRegions with one task: centres (nfunc x 3, bohr) and float
+ * radii, moved to the orbitals' centres and resized from their spreads
+ * (moveTo / move, updateRadii, getMeanRadius of
+ * src/LocalizationRegions.cc); centers() and radii() feed MasksSet::update
+ * (as doubles) and FunctionsPacking. */
+class LocalizationRegions
+{
+    double cell_[3];
+    std::vector<double> centers_;
+    std::vector<float> radii_;
+
+public:
+    LocalizationRegions(const pb::Grid& g, std::vector<double> centers, std::vector<float> radii)
+        : centers_(std::move(centers)), radii_(std::move(radii))
+    {
+        for (int i = 0; i < 3; i++)
+            cell_[i] = g.raw().ll[i];
+        if (centers_.size() != 3 * radii_.size())
+            throw Error(MGX_BAD_ARG, "LocalizationRegions: one radius per centre");
+    }
+    int size() const { return (int)radii_.size(); }
+    /* moveTo(target_centers), the largest move before the 1-bohr cap */
+    float moveTo(const std::vector<double>& targets)
+    {
+        if (targets.size() != centers_.size())
+            throw Error(MGX_BAD_ARG, "LocalizationRegions::moveTo: one target per centre");
+        float mx = 0.f;
+        check(mgx_regions_move_to(size(), centers_.data(), targets.data(), cell_, &mx),
+            "LocalizationRegions::moveTo");
+        return mx;
+    }
+    /* move(sc): to the centres of the orbitals */
+    template <typename T>
+    float move(const SpreadsAndCenters<T>& sc)
+    {
+        std::vector<double> t(centers_.size());
+        for (int f = 0; f < size(); f++)
+        {
+            const auto c = sc.computeCenter(f);
+            for (int d = 0; d < 3; d++)
+                t[3 * f + d] = c[d];
+        }
+        return moveTo(t);
+    }
+    /* updateRadii(sc, ratio): the radii from the spreads; getMeanRadius() */
+    template <typename T>
+    float updateRadii(const SpreadsAndCenters<T>& sc, float ratio)
+    {
+        std::vector<double> sp(size());
+        for (int f = 0; f < size(); f++)
+            sp[f] = sc.computeSpread(f);
+        float mean = 0.f;
+        check(mgx_regions_update_radii(size(), sp.data(), ratio, radii_.data(), &mean),
+            "LocalizationRegions::updateRadii");
+        return mean;
+    }
+    const std::vector<double>& centers() const { return centers_; }
+    const std::vector<float>& radii() const { return radii_; }
 };
 
 /* FunctionsPacking with one task (src/FunctionsPacking.h): the colour of

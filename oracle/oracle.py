@@ -637,3 +637,43 @@ def centers_spreads(ll, a):
     x = lby2pi[None, :] * np.arctan2(s, c)
     x = np.where(x < 0., x + ll[None, :], x)
     return x, np.sqrt((lby2pi[None, :] ** 2 - c * c - s * s).sum(axis=1))
+
+
+# ------------------------------------------------------------ localization regions
+def regions_move_to(centers, targets, cell):
+    """LocalizationRegions::moveTo (src/LocalizationRegions.cc:405-450) with
+    Vector3D::vminimage (src/tools/Vector3D.cc:32-63, periodic): (new
+    centres, largest move as float)."""
+    import math
+    c = [list(map(float, x)) for x in np.asarray(centers, dtype=np.float64).reshape(-1, 3)]
+    t = np.asarray(targets, dtype=np.float64).reshape(-1, 3)
+    mx = np.float32(0.)
+    for f in range(len(c)):
+        d = []
+        for i in range(3):
+            r = math.fmod(float(t[f][i]) - c[f][i], float(cell[i]))
+            ax2 = 0.5 * float(cell[i])
+            if r > ax2:
+                r -= float(cell[i])
+            elif r < -ax2:
+                r += float(cell[i])
+            d.append(r)
+        nrm = np.float32(math.sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]))
+        if nrm > mx:
+            mx = nrm
+        if nrm > 1.:
+            d = [x / float(nrm) for x in d]
+        for i in range(3):
+            c[f][i] += d[i]
+    return np.asarray(c), float(mx)
+
+
+def regions_update_radii(spreads, ratio):
+    """LocalizationRegions::updateRadii and getMeanRadius (:332-366): FP32
+    radii ratio x spread and the cube root of their mean cube (FP32)."""
+    r = np.asarray([np.float32(float(np.float32(ratio)) * float(s)) for s in spreads],
+                   dtype=np.float32)
+    rcube = np.float32(0.)
+    for a in r:
+        rcube = np.float32(rcube + np.float32(a * a * a))
+    return r, float(np.cbrt(np.float32(rcube / np.float32(len(r)))))
