@@ -349,7 +349,8 @@ def run_gpu(args, cfg):
         net = capi.UNet(ctx)
         net.set_params(lrn.init_params(cfg["seed"]))
     sw = OrbitalSweep(ctx, V, N, mode=mode, gemm=gemm, precond_chunk=args.chunk,
-                      chunk_funcs=lean, use_matb=args.theta == "b", learned=net)
+                      chunk_funcs=lean, use_matb=args.theta == "b", learned=net,
+                      fuse_hpsi=not args.no_fuse_hpsi)
     torch.cuda.synchronize()
 
     train = {"pairs": 0, "steps": 0, "loss_first": None, "loss_last": None}
@@ -781,6 +782,8 @@ def main():
     ap.add_argument("--mode", default="mixed", choices=["mixed", "plain"])
     ap.add_argument("--gemm", default="bf16x3", choices=["fp32", "tf32", "bf16x3", "fp16x3"])
     ap.add_argument("--chunk", type=int, default=0, help="V-cycle orbital chunk (0 = auto)")
+    ap.add_argument("--no-fuse-hpsi", action="store_true",
+                    help="H psi as its own pass and its conversion for the H product separate")
     ap.add_argument("--theta", default="b", choices=["b", "gram"],
                     help="b: theta = B^-1 H as the reference for a Mehrstellen operator; "
                          "gram: theta = S^-1 H")

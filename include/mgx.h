@@ -335,6 +335,16 @@ int mgx_gram_hmat_matb(mgx_ctx* ctx, int mode, const void* psi, const void* hpsi
     size_t ld, int nfunc, double* S, double* H, double* Bm, void* work, int work_funcs,
     void* stream);
 
+/* H Psi (mgx_hpsi with lap_type 0 and B(V psi), FP32 block and potential)
+ * and then S, H and B (mgx_gram_hmat_matb) in one call.  With split-BF16x3
+ * products the H psi kernel runs inside the H product, 512 functions at a
+ * time, and writes each chunk both to hpsi (FP32, as mgx_hpsi) and as the
+ * product's bf16 hi / lo operand planes, so H Psi is not read back and
+ * converted; other modes make the two calls.  hpsi is an output. */
+int mgx_hpsi_gram_hmat_matb(mgx_ctx* ctx, int mode, const float* psi, const float* V,
+    float* hpsi, size_t ld, int nfunc, double* S, double* H, double* Bm, void* work,
+    int work_funcs, void* stream);
+
 /* ProjectedMatricesMehrstellen::updateHB
  * (src/ProjectedMatricesMehrstellen.h:55-62): HB = S theta, S read as
  * symmetric from its lower triangle (symm 'l', 'l'), then

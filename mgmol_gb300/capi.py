@@ -134,6 +134,7 @@ _SIGS = {
     "mgx_gram_hmat": [_vp, _i, _vp, _vp, _sz, _i, _vp, _vp, _vp],
     "mgx_matb": [_vp, _i, _vp, _sz, _i, _vp, _vp, _i, _vp],
     "mgx_gram_hmat_matb": [_vp, _i, _vp, _vp, _sz, _i, _vp, _vp, _vp, _vp, _i, _vp],
+    "mgx_hpsi_gram_hmat_matb": [_vp, _i, _vp, _vp, _vp, _sz, _i, _vp, _vp, _vp, _vp, _i, _vp],
     "mgx_update_hb": [_vp, _i, _vp, _vp, _vp, _vp],
     "mgx_normalize": [_vp, _i, _vp, _sz, _i, _vp, _vp],
     "mgx_normalize_scales": [_vp, _i, _vp, _vp, _vp],
@@ -522,6 +523,26 @@ class Context:
         pw, nw = self._work(work, ld, psi.dtype)
         _check(load().mgx_gram_hmat_matb(self.handle, mode, p, ph, ld, nf, _ptr(S), _ptr(H), _ptr(B),
                                          pw, nw, _stream(stream)))
+        return S, H.T, B
+
+    def hpsi_gram_hmat_matb(self, psi, V, hpsi, mode=GEMM_BF16X3, S=None, H=None, B=None,
+                            work=None, stream=None):
+        """H psi into hpsi (Mehrstellen with B(V psi), FP32) and (S, H, B) in
+        one call (mgx_hpsi_gram_hmat_matb); H as the row-major view."""
+        if psi.dtype != torch.float32 or V.dtype != torch.float32 or hpsi.dtype != torch.float32:
+            raise ValueError("FP32 block, potential and H psi")
+        p, ld, nf = _block(psi, self.npts)
+        ph, ldh, _ = _block(hpsi, self.npts)
+        assert ldh == ld
+        if V.numel() != self.npts or not V.is_contiguous():
+            raise ValueError("V must be one contiguous field of the grid")
+        mk = lambda: torch.empty((nf, nf), dtype=torch.float64, device=psi.device)  # noqa: E731
+        S = mk() if S is None else S
+        H = mk() if H is None else H
+        B = mk() if B is None else B
+        pw, nw = self._work(work, ld, psi.dtype)
+        _check(load().mgx_hpsi_gram_hmat_matb(self.handle, mode, p, _ptr(V), ph, ld, nf, _ptr(S),
+                                              _ptr(H), _ptr(B), pw, nw, _stream(stream)))
         return S, H.T, B
 
     def update_hb(self, S, theta, stream=None):

@@ -18,7 +18,10 @@
 // suits one GPU:
 //   - S, H and B come from one call (mgx_gram_hmat_matb), so the
 //     tensor-core modes convert psi once; the Psi Theta product of the
-//     residual reads that conversion again (mgx_set_reuse_conversion);
+//     residual reads that conversion again (mgx_set_reuse_conversion); with
+//     FP32 orbitals and split-BF16x3 products H psi is made inside that call
+//     (mgx_hpsi_gram_hmat_matb), its chunks written straight into the H
+//     product's operand planes;
 //   - the critical path is H psi -> S, H, B -> Cholesky of B ->
 //     theta = B^-1 H -> residual -> V-cycle; the S side of the dense algebra
 //     (Cholesky and inverse of S, HB, the energy) is queued, once theta is
@@ -161,15 +164,29 @@ public:
         const bool lazy = o_.fuse_update && update;
         void* s = (void*)stream;
         if (!lazy) check(mgx_normalize(ctx_, dt(), psi, ld, n_, nullptr, s), "normalize");
-        check(mgx_hpsi(ctx_, o_.lap_type, dt(), psi, ld, V_, vtype_, hpsi_.data(), n_, 1, s),
-            "applyLocal");
-        if (matb_)
-            check(mgx_gram_hmat_matb(ctx_, gemm(), psi, hpsi_.data(), ld, n_, S_.data(), H_.data(),
-                      B_.data(), chunk_ ? work_.data() : corr_.data(), chunk_ ? chunk_ : n_, s),
-                "computeGram / addHlocalij / computeMatB");
+        // FP32 Mehrstellen with B and split-BF16x3 products: H psi made
+        // inside the H product, written straight into its operand planes
+        const bool fused = matb_ && std::is_same<T, float>::value && vtype_ == MGX_F32
+                           && gemm() == MGX_GEMM_BF16X3;
+        if (fused)
+            check(mgx_hpsi_gram_hmat_matb(ctx_, gemm(), (const float*)psi, (const float*)V_,
+                      (float*)hpsi_.data(), ld, n_, S_.data(), H_.data(), B_.data(),
+                      chunk_ ? (void*)work_.data() : (void*)corr_.data(), chunk_ ? chunk_ : n_, s),
+                "applyLocal / computeGram / addHlocalij / computeMatB");
         else
-            check(mgx_gram_hmat(ctx_, gemm(), psi, hpsi_.data(), ld, n_, S_.data(), H_.data(), s),
-                "computeGram / addHlocalij");
+        {
+            check(mgx_hpsi(ctx_, o_.lap_type, dt(), psi, ld, V_, vtype_, hpsi_.data(), n_, 1, s),
+                "applyLocal");
+            if (matb_)
+                check(mgx_gram_hmat_matb(ctx_, gemm(), psi, hpsi_.data(), ld, n_, S_.data(),
+                          H_.data(), B_.data(), chunk_ ? work_.data() : corr_.data(),
+                          chunk_ ? chunk_ : n_, s),
+                    "computeGram / addHlocalij / computeMatB");
+            else
+                check(mgx_gram_hmat(ctx_, gemm(), psi, hpsi_.data(), ld, n_, S_.data(), H_.data(),
+                          s),
+                    "computeGram / addHlocalij");
+        }
         if (matb_)
         {
             // computeInvB + updateTheta: theta = B^-1 H from the factor of B

@@ -93,7 +93,7 @@ int gram_tcgen05(mgx_ctx*, int, const void*, const void*, size_t, size_t, int,
     double, int, double*, cudaStream_t);
 int gram_hmat_tcgen05(mgx_ctx*, int, const void*, const void*, size_t, size_t, int,
     double, double*, double*, cudaStream_t, double* Bm = nullptr, void* work = nullptr,
-    int work_funcs = 0);
+    int work_funcs = 0, const float* V = nullptr, int lap_type = 0);
 int matb_cuda_cores(mgx_ctx*, int, const void*, size_t, size_t, int, double, double*,
     void*, int, cudaStream_t);
 int matb_tcgen05(mgx_ctx*, int, const void*, size_t, size_t, int, double, double*, void*, int,
@@ -154,6 +154,21 @@ int rhs_split_block(const mgx_grid& g, const float* u, size_t ldu, int nfunc, vo
     p.split_lo   = lo;
     p.split_rows = rows;
     return stencil_launch(OP_RHS_SPLIT, 0, MGX_F32, MGX_F32, p, make_level(g, 0), 0., nfunc, s);
+}
+
+int hpsi_split_block(const mgx_grid& g, const float* psi, size_t ld, const float* V, float* out,
+    int nfunc, void* hi, void* lo, int rows, cudaStream_t s)
+{
+    PlaneParams p = plane(g);
+    p.u          = psi;
+    p.ldu        = ld;
+    p.V          = V;
+    p.out        = out;
+    p.ldo        = ld;
+    p.split_hi   = hi;
+    p.split_lo   = lo;
+    p.split_rows = rows;
+    return stencil_launch(OP_HPSI_B, 0, MGX_F32, MGX_F32, p, make_level(g, 0), 0., nfunc, s);
 }
 
 int rhs_block(const mgx_grid& g, int dtype, const void* u, size_t ldu, void* out,
@@ -738,6 +753,33 @@ int mgx_gram_hmat_matb(mgx_ctx* ctx, int mode, const void* psi, const void* hpsi
     MGX_TRY(mgx_gram(ctx, mode, psi, ld, nfunc, S, stream));
     MGX_TRY(mgx_hmat(ctx, mode, psi, hpsi, ld, nfunc, H, stream));
     return mgx_matb(ctx, mode, psi, ld, nfunc, Bm, work, work_funcs, stream);
+}
+
+int mgx_hpsi_gram_hmat_matb(mgx_ctx* ctx, int mode, const float* psi, const float* V,
+    float* hpsi, size_t ld, int nfunc, double* S, double* H, double* Bm, void* work,
+    int work_funcs, void* stream)
+{
+    if (!ctx) return fail(MGX_BAD_ARG, "ctx is NULL");
+    MGX_TRY(check_gemm_mode(mode));
+    MGX_TRY(check_block(ctx->grid, psi, ld, nfunc, "psi"));
+    MGX_TRY(check_block(ctx->grid, hpsi, ld, nfunc, "hpsi"));
+    if (nfunc == 0) return MGX_OK;
+    if (!V) return fail(MGX_BAD_ARG, "V is NULL");
+    if (!S || !H || !Bm) return fail(MGX_BAD_ARG, "S, H or B is NULL");
+    if ((const void*)psi == (const void*)hpsi) return fail(MGX_BAD_ARG, "psi and hpsi alias");
+    if (work == psi || work == hpsi) return fail(MGX_BAD_ARG, "work aliases psi or hpsi");
+    if (mode == MGX_GEMM_BF16X3)
+    {
+        const Level L    = make_level(ctx->grid, 0);
+        const double vel = L.h[0] * L.h[1] * L.h[2];
+        const size_t ldv = nfunc > 1 ? ld : L.npts();
+        int wf = work_funcs;
+        MGX_TRY(matb_work(ctx, mode, ldv, nfunc, &work, &wf));
+        return gram_hmat_tcgen05(ctx, mode, psi, hpsi, ldv, L.npts(), nfunc, vel, S, H,
+            (cudaStream_t)stream, Bm, work, wf, V, 0);
+    }
+    MGX_TRY(mgx_hpsi(ctx, 0, MGX_F32, psi, ld, V, MGX_F32, hpsi, nfunc, 1, stream));
+    return mgx_gram_hmat_matb(ctx, mode, psi, hpsi, ld, nfunc, S, H, Bm, work, work_funcs, stream);
 }
 
 int mgx_update_hb(mgx_ctx* ctx, int n, const double* S, const double* theta, double* HB,

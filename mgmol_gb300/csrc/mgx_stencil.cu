@@ -706,6 +706,27 @@ __global__ void __launch_bounds__(256, 2) plane_vec_kernel(PlaneParams p, DevCoe
     const T* __restrict__ fp = p.f ? reinterpret_cast<const T*>(p.f) + (size_t)f * p.ldf : nullptr;
     constexpr bool POINTWISE = is_jacobi(OP) || (OP == OP_HPSI_V) || (OP == OP_RHS_SUB);
     const T c12 = (T)(1. / 12.), c05 = (T)0.5;
+    // the result of 4 consecutive points (never across a 64-point block) as
+    // bf16 hi = rn(r), lo = rn(r - hi) in the K-blocked operand planes, the
+    // split of the tensor-core products
+    auto store_split = [&](const size_t pt, const V4& res) {
+        if constexpr (sizeof(T) == 4 && VEC == 4)
+        {
+            const size_t o = ((pt / 64) * (size_t)p.split_rows + f) * 64 + pt % 64;
+            __align__(8) __nv_bfloat16 h[4], l[4];
+#pragma unroll
+            for (int v = 0; v < 4; v++)
+            {
+                const float x = VH::get(res, v);
+                h[v]          = __float2bfloat16_rn(x);
+                l[v]          = __float2bfloat16_rn(x - __bfloat162float(h[v]));
+            }
+            *reinterpret_cast<uint2*>(reinterpret_cast<__nv_bfloat16*>(p.split_hi) + o)
+                = *reinterpret_cast<const uint2*>(h);
+            *reinterpret_cast<uint2*>(reinterpret_cast<__nv_bfloat16*>(p.split_lo) + o)
+                = *reinterpret_cast<const uint2*>(l);
+        }
+    };
 
     // OP_JACOBI_RST: coarse plane X = (xe - 1) / 2 from the w planes xe - 2
     // .. xe, rows y0 - 1 .. y0 + TY - 1 of the ring; the grouping and order
@@ -918,28 +939,13 @@ __global__ void __launch_bounds__(256, 2) plane_vec_kernel(PlaneParams p, DevCoe
                     *reinterpret_cast<V4*>(updp + xoff + goff[k]) = q;
                 }
                 else if (OP == OP_RHS_SPLIT)
-                {
-                    if constexpr (sizeof(T) == 4 && VEC == 4)
-                    {
-                        // 4 consecutive points, never across a 64-point block
-                        const size_t pt = xoff + goff[k];
-                        const size_t o  = ((pt / 64) * (size_t)p.split_rows + f) * 64 + pt % 64;
-                        __align__(8) __nv_bfloat16 h[4], l[4];
-#pragma unroll
-                        for (int v = 0; v < 4; v++)
-                        {
-                            const float x = VH::get(res, v);
-                            h[v]          = __float2bfloat16_rn(x);
-                            l[v]          = __float2bfloat16_rn(x - __bfloat162float(h[v]));
-                        }
-                        *reinterpret_cast<uint2*>(reinterpret_cast<__nv_bfloat16*>(p.split_hi) + o)
-                            = *reinterpret_cast<const uint2*>(h);
-                        *reinterpret_cast<uint2*>(reinterpret_cast<__nv_bfloat16*>(p.split_lo) + o)
-                            = *reinterpret_cast<const uint2*>(l);
-                    }
-                }
+                    store_split(xoff + goff[k], res);
                 else if (!RST || (gy[k] >= YO && xe >= x0))
+                {
                     *reinterpret_cast<V4*>(outp + xoff + goff[k]) = res;
+                    // H psi also written as the tensor-core operand planes
+                    if (OP == OP_HPSI_B && p.split_hi != nullptr) store_split(xoff + goff[k], res);
+                }
                 if (RST)
                     *reinterpret_cast<V4*>(wring + (size_t)((xe - x0 + 1) & 3) * ring_elems
                                            + (size_t)gy[k] * nz + gz[k]) = wres;
@@ -1235,6 +1241,7 @@ int stencil_launch(int op, int lap_type, int dtype, int v_dtype,
             case OP_JACOBI_RST:
                 return dispatch_lap<double, double, OP_JACOBI_RST>(lap_type, p, c, nfunc, stream, force_direct);
             case OP_HPSI_B:
+                if (p.split_hi != nullptr) return fail(MGX_UNSUPPORTED, "split H psi is FP32 only");
                 if (v_dtype == MGX_F64)
                     return launch_t<double, double, 0, OP_HPSI_B, 1>(p, c, nfunc, stream, force_direct);
                 return launch_t<double, float, 0, OP_HPSI_B, 1>(p, c, nfunc, stream, force_direct);
@@ -1258,6 +1265,14 @@ int stencil_launch(int op, int lap_type, int dtype, int v_dtype,
             case OP_JACOBI_RST:
                 return dispatch_lap<float, float, OP_JACOBI_RST>(lap_type, p, c, nfunc, stream, force_direct);
             case OP_HPSI_B:
+                if (p.split_hi != nullptr)
+                {
+                    // the operand planes are written by the vector kernel only
+                    if (v_dtype != MGX_F32 || !vec_ok<float, float, 0, OP_HPSI_B, 1>(p, force_direct)
+                        || (L.npts() % 64) != 0)
+                        return fail(MGX_UNSUPPORTED, "split H psi needs the vector kernel");
+                    return launch_vec<float, float, 0, OP_HPSI_B, 1>(p, c, nfunc, stream);
+                }
                 if (v_dtype == MGX_F64)
                     return launch_t<float, double, 0, OP_HPSI_B, 1>(p, c, nfunc, stream, force_direct);
                 return launch_t<float, float, 0, OP_HPSI_B, 1>(p, c, nfunc, stream, force_direct);

@@ -78,9 +78,10 @@ struct PlaneParams
     // OP_JACOBI_UPD only, or NULL: upd = upd_scale[f] * (upd + upd_alpha r),
     // the column normalization of the updated block folded into the store
     const double* upd_scale = nullptr;
-    // OP_RHS_SPLIT only: the result r of point k of function f is stored as
-    // bf16 hi = rn(r), lo = rn(r - hi) at ((k / 64) * split_rows + f) * 64 +
-    // k % 64 of split_hi / split_lo (the K-blocked operand planes)
+    // OP_RHS_SPLIT, and OP_HPSI_B (FP32) when split_hi is set: the result r
+    // of point k of function f is stored as bf16 hi = rn(r), lo = rn(r - hi)
+    // at ((k / 64) * split_rows + f) * 64 + k % 64 of split_hi / split_lo
+    // (the K-blocked operand planes); OP_HPSI_B stores out as well
     void* split_hi = nullptr;
     void* split_lo = nullptr;
     int split_rows = 0;
@@ -105,6 +106,13 @@ int rhs_block(const mgx_grid& g, int dtype, const void* u, size_t ldu, void* out
  * the points are not a multiple of 64; nothing is launched then. */
 int rhs_split_block(const mgx_grid& g, const float* u, size_t ldu, int nfunc, void* hi,
     void* lo, int rows, cudaStream_t s);
+/* H psi = -Lap_M psi + B(V psi) of nfunc FP32 functions (FP32 V) written to
+ * out (leading dimension ld) and, as bf16 hi / lo K-blocked planes of
+ * `rows` rows, to hi / lo.  MGX_UNSUPPORTED, with nothing launched, when
+ * the vector kernel cannot run the block or the points are not a multiple
+ * of 64. */
+int hpsi_split_block(const mgx_grid& g, const float* psi, size_t ld, const float* V, float* out,
+    int nfunc, void* hi, void* lo, int rows, cudaStream_t s);
 
 int ghosted_del2(const mgx_grid& g, int ghosts, int lap_type, int dtype,
     const void* v, void* b, size_t nfunc, cudaStream_t s);

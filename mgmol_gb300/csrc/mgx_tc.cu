@@ -1693,6 +1693,51 @@ int matb_product(mgx_ctx* ctx, int mode, const Operand& a, size_t a_used, const 
     }
     return MGX_OK;
 }
+
+/* H = Psi^T (H Psi) with H Psi made here, CHUNK functions at a time: the
+ * H psi kernel writes each chunk both to hpsi (FP32, for the residual) and,
+ * as the bf16 hi / lo K-blocked planes, straight into the B-side
+ * workspace, which the product then reads; H psi is never read back and
+ * converted.  BF16X3 on K-blocked planes only.  *done false (nothing
+ * launched) when the H psi kernel cannot write the planes. */
+int hpsi_product(mgx_ctx* ctx, int mode, const Operand& a, size_t a_used, const float* psi,
+    const float* V, float* hpsi, size_t ld, size_t K, int n, double* C, int tile_slot,
+    cudaStream_t s, bool* done)
+{
+    *done = false;
+    if (!(mode == MGX_GEMM_BF16X3 && blocked_planes() && (K % 64) == 0 && (ld % 4) == 0
+            && ((uintptr_t)psi % 16) == 0 && ((uintptr_t)hpsi % 16) == 0))
+        return MGX_OK;
+    const size_t kblocks = K / 64;
+    const size_t plane   = kblocks * 64 * (size_t)std::min(n, CHUNK) * sizeof(__nv_bfloat16);
+    char* base           = (char*)ctx->tc_split.ptr + a_used;
+    for (int j0 = 0; j0 < n; j0 += CHUNK)
+    {
+        const int nc = std::min(CHUNK, n - j0);
+        const int BN = tile_n(nc);
+        void* hi     = base;
+        void* lo     = base + plane;
+        const int st = hpsi_split_block(ctx->grid, psi + (size_t)j0 * ld, ld, V,
+            hpsi + (size_t)j0 * ld, nc, hi, lo, nc, s);
+        if (st == MGX_UNSUPPORTED && j0 == 0) return MGX_OK; // nothing launched
+        MGX_TRY(st);
+        Operand b;
+        b.sw      = bf16_swizzle();
+        b.blocked = true;
+        b.half    = false;
+        b.bf16    = true;
+        b.base0   = hi;
+        b.base1   = lo;
+        b.K       = K;
+        b.ld      = kblocks * 64;
+        b.rows    = nc;
+        MGX_TRY(tc::make_map_blocked(&b.m0, hi, nc, kblocks, BN, b.sw));
+        MGX_TRY(tc::make_map_blocked(&b.m1, lo, nc, kblocks, BN, b.sw));
+        MGX_TRY(run(ctx, mode, a, b, n, nc, 0, C + (size_t)j0 * n, n, K, tile_slot, BN, s));
+    }
+    *done = true;
+    return MGX_OK;
+}
 } // namespace
 
 /* B = Psi^T (B Psi) * vel, lower triangle mirrored (the |B u| <= max |u|
@@ -1763,7 +1808,7 @@ int gram_tcgen05(mgx_ctx* ctx, int mode, const void* A, const void* B, size_t ld
  * B Psi formed in `work` */
 int gram_hmat_tcgen05(mgx_ctx* ctx, int mode, const void* psi, const void* hpsi,
     size_t ld, size_t K, int n, double vel, double* S, double* H, cudaStream_t s,
-    double* Bm, void* work, int work_funcs)
+    double* Bm, void* work, int work_funcs, const float* V, int lap_type)
 {
     const size_t a_bytes = operand_bytes(mode, K, n);
     const size_t b_bytes = operand_bytes(mode, K, std::min(n, CHUNK));
@@ -1786,7 +1831,29 @@ int gram_hmat_tcgen05(mgx_ctx* ctx, int mode, const void* psi, const void* hpsi,
     MGX_TRY(prepare(mode, psi, ld, K, n, tc::BM, (char*)ctx->tc_split.ptr, &used, a, s, sa));
     record_conversion(ctx, mode, a, psi, ld, K, n, used);
     MGX_TRY(run_sym(ctx, mode, a, n, S, K, 0, s));
-    MGX_TRY(product(ctx, mode, a, ((used + 255) / 256) * 256, hpsi, ld, K, n, H, 1, s, sb));
+    // with V, hpsi is an output: H psi made chunk by chunk into the
+    // product's operand planes (or, when that cannot run, in full first)
+    bool made = false;
+    if (V)
+    {
+        MGX_TRY(hpsi_product(ctx, mode, a, ((used + 255) / 256) * 256, (const float*)psi, V,
+            (float*)hpsi, ld, K, n, H, 1, s, &made));
+        if (!made)
+        {
+            PlaneParams p;
+            for (int i = 0; i < 3; i++)
+                p.n[i] = ctx->grid.n[i];
+            p.u   = psi;
+            p.ldu = ld;
+            p.V   = V;
+            p.out = const_cast<void*>(hpsi);
+            p.ldo = ld;
+            MGX_TRY(stencil_launch(OP_HPSI_B, lap_type, MGX_F32, MGX_F32, p,
+                make_level(ctx->grid, 0), 0., n, s));
+        }
+    }
+    if (!made)
+        MGX_TRY(product(ctx, mode, a, ((used + 255) / 256) * 256, hpsi, ld, K, n, H, 1, s, sb));
     MGX_TRY(finish(S, n, vel, 1, s, sa, sa));
     MGX_TRY(finish(H, n, vel, 0, s, sa, sb));
     if (Bm)

@@ -85,7 +85,7 @@ class OrbitalSweep:
                  maxlevels=2, gamma=None, precond_chunk=0, precond_factor=1.0,
                  chunk_funcs=0, fuse_update=True, use_matb=True, anderson_m=0,
                  anderson_beta=1.0, learned=None, learned_mode=capi.LEARNED_WARM,
-                 device="cuda"):
+                 fuse_hpsi=True, device="cuda"):
         self.ctx = ctx
         self.mode = mode
         self.lap_type = lap_type
@@ -112,6 +112,11 @@ class OrbitalSweep:
         self.use_matb = self.mehr and bool(use_matb)
         self.Bm = torch.empty((nfunc, nfunc), dtype=torch.float64, device=device) \
             if self.use_matb else None
+        # H psi made inside the H product (its chunks written straight into
+        # the product's split-BF16x3 operand planes): FP32 Mehrstellen with
+        # B(V psi) and the B matrix, split-BF16x3 products
+        self.fuse_hpsi = bool(fuse_hpsi) and mode == "mixed" and self.use_matb \
+            and self.gemm == capi.GEMM_BF16X3
         self.dscale = torch.empty(nfunc, dtype=torch.float64, device=device)
         self.diagS = torch.empty(nfunc, dtype=torch.float64, device=device)
         self.precond_chunk = precond_chunk
@@ -183,14 +188,20 @@ class OrbitalSweep:
         if not lazy:
             self._mark(timed, "normalize")
             ctx.normalize(psi, diag=self.diagS)
-        self._mark(timed, "hpsi")
-        ctx.hpsi(psi, self.V, self.lap_type, True, out=self.hpsi)
-        self._mark(timed, "gram")
-        if self.use_matb:
-            ctx.gram_hmat_matb(psi, self.hpsi, self.gemm, S=self.S, H=self.Hm, B=self.Bm,
-                               work=self.work if self.chunk else self.corr)
+        if self.fuse_hpsi:
+            # H psi inside the H product: its time counts in the gram phase
+            self._mark(timed, "gram")
+            ctx.hpsi_gram_hmat_matb(psi, self.V, self.hpsi, self.gemm, S=self.S, H=self.Hm,
+                                    B=self.Bm, work=self.work if self.chunk else self.corr)
         else:
-            ctx.gram_hmat(psi, self.hpsi, self.gemm, S=self.S, H=self.Hm)
+            self._mark(timed, "hpsi")
+            ctx.hpsi(psi, self.V, self.lap_type, True, out=self.hpsi)
+            self._mark(timed, "gram")
+            if self.use_matb:
+                ctx.gram_hmat_matb(psi, self.hpsi, self.gemm, S=self.S, H=self.Hm, B=self.Bm,
+                                   work=self.work if self.chunk else self.corr)
+            else:
+                ctx.gram_hmat(psi, self.hpsi, self.gemm, S=self.S, H=self.Hm)
         self._mark(timed, "dense")
         # Hm holds H column-major; the matrix calls want the row-major view
         H = self.Hm.T
