@@ -852,6 +852,18 @@ static bool fused_restrict()
     return on;
 }
 
+/* Both pre-sweeps of a level in one kernel and both post-sweeps in another
+ * (jacobi2_launch: the first sweep's iterate stays on chip) unless
+ * MGX_TWO_SWEEPS=0.  The results are the same bits either way. */
+static bool two_sweeps()
+{
+    static const bool on = [] {
+        const char* e = getenv("MGX_TWO_SWEEPS");
+        return !(e && e[0] == '0');
+    }();
+    return on;
+}
+
 struct VCycle
 {
     mgx_ctx* ctx;
@@ -949,20 +961,78 @@ struct VCycle
             dtype, p, lev[l], jf[l], nf, s);
     }
 
+    // both sweeps of a level's pre-smoothing (pre: the second one's
+    // residual restricted into f[l + 1]) or post-smoothing (the last one
+    // with the fused update at level 0) in one kernel, from buffer cur into
+    // the other one; dry: only whether the kernel runs the block
+    int jacobi2(int l, int cur, bool pre, bool dry)
+    {
+        PlaneParams p;
+        p.u   = cur ? v1[l] : v0[l];
+        p.ldu = ld[l];
+        p.f   = f[l];
+        p.ldf = ld[l];
+        p.out = cur ? v0[l] : v1[l];
+        p.ldo = ld[l];
+        for (int i = 0; i < 3; i++)
+            p.n[i] = lev[l].n[i];
+        p.err    = err;
+        int mode = JJ_STORE;
+        if (pre)
+        {
+            if (l == 0 && pending_scale)
+            {
+                // first sweep straight from f with u = gamma f
+                p.gamma_in = gamma;
+                p.u        = f[0];
+                p.ldu      = ld[0];
+            }
+            p.coarse = f[l + 1];
+            p.ldc    = ld[l + 1];
+            mode     = JJ_RST;
+        }
+        else if (l == 0 && upd0)
+        {
+            p.upd       = upd0;
+            p.ldupd     = ld[0];
+            p.upd_alpha = upd_alpha;
+            p.upd_scale = upd_scale0;
+            mode        = JJ_UPD;
+        }
+        const int st = jacobi2_launch(mode, l == 0 ? lap_type : 1, dtype, p, lev[l], jf[l], nf, s,
+            dry);
+        if (!dry && pre && st == MGX_OK && l == 0) pending_scale = false;
+        return st;
+    }
+
     // returns the buffer index holding the result at level l
     int mg(int l)
     {
         int cur         = 0;
         const int ncycl = (l == L) ? 4 : 2;
         bool restricted = false;
-        for (int it = 0; it < ncycl; it++)
+        // the paired sweeps move the iterate to the other buffer once per
+        // pair where two single sweeps move it twice, so a level runs both
+        // pairs or neither and ends in the same buffer either way
+        const bool pairs = l < L && two_sweeps() && masks == nullptr && fused_restrict()
+                           && jacobi2(l, cur, true, true) == MGX_OK
+                           && jacobi2(l, cur ^ 1, false, true) == MGX_OK;
+        if (pairs)
         {
-            // without coarse levels the last of these sweeps is the final one
-            const int st = jacobi(l, cur, (it == ncycl - 1) && (l < L), (l == L) && (it == ncycl - 1),
-                &restricted);
+            const int st = jacobi2(l, cur, true, false);
             if (st != MGX_OK) return -st - 1;
             cur ^= 1;
+            restricted = true;
         }
+        else
+            for (int it = 0; it < ncycl; it++)
+            {
+                // without coarse levels the last of these sweeps is the final one
+                const int st = jacobi(l, cur, (it == ncycl - 1) && (l < L),
+                    (l == L) && (it == ncycl - 1), &restricted);
+                if (st != MGX_OK) return -st - 1;
+                cur ^= 1;
+            }
         if (l == L) return cur;
         int st = MGX_OK;
         if (!restricted)
@@ -978,6 +1048,12 @@ struct VCycle
         st = prolong_launch(dtype, 1, lev[l], c1 ? v1[l + 1] : v0[l + 1],
             ld[l + 1], cur ? v1[l] : v0[l], ld[l], nf, mask_slice(masks, l, f0), s);
         if (st != MGX_OK) return -st - 1;
+        if (pairs)
+        {
+            st = jacobi2(l, cur, false, false);
+            if (st != MGX_OK) return -st - 1;
+            return cur ^ 1;
+        }
         for (int it = 0; it < 2; it++)
         {
             st = jacobi(l, cur, false, it == 1);

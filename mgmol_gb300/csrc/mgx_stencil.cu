@@ -155,6 +155,12 @@ DevCoef<T> to_dev(const StencilCoeffs& c, double jf)
     return d;
 }
 
+/* a + b rounded once and never fused with a product that feeds it, so
+ * that the operator's running sums over x planes (A(x - 1) + B(x - 2) +
+ * B(x)) get the same bits in every kernel that forms them */
+__device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
+
 __device__ __forceinline__ int wrap(int i, int n)
 {
     return i < 0 ? i + n : (i >= n ? i - n : i);
@@ -892,7 +898,7 @@ __global__ void __launch_bounds__(256, 2) plane_vec_kernel(PlaneParams p, DevCoe
                 }
                 if (emit)
                 {
-                    T lap = A1[k][v] + B2[k][v] + b;
+                    T lap = add_rn(add_rn(A1[k][v], B2[k][v]), b);
                     T ucen = U1[k][v];
                     T r    = lap;
                     if (OP == OP_HPSI_V) r = lap + ucen * VH::get(pv[k], v);
@@ -967,6 +973,389 @@ __global__ void __launch_bounds__(256, 2) plane_vec_kernel(PlaneParams p, DevCoe
         }
     }
     if (RST && pend >= 0) restrict_plane(pend);
+    if (!ok && threadIdx.x == 0)
+    {
+        if (p.err != nullptr) atomicExch(p.err, MGX_TIMEOUT);
+        for (int i = waited + 1; i <= issued; i++)
+            mbar_wait(bars + (i % S), (uint32_t)((i / S) & 1));
+    }
+}
+
+/* ------------------------------------------------------------------ */
+/* two Jacobi sweeps in one plane march                                 */
+/* ------------------------------------------------------------------ */
+// Two consecutive Jacobi sweeps of one level, u1 = u - jf (A u - f) and
+// u2 = u1 - jf (A u1 - f), in one launch.  The staged input is folded into
+// u1 as in plane_vec_kernel; each plane of u1 goes to a two-plane buffer in
+// shared memory, and a second set of partial sums folds it into u2 one
+// plane behind.  u1 is formed on the tile's rows and planes and one more on
+// each side, so a tile needs no other tile's u1: the input and f cross DRAM
+// once and u1 never does.  Each point keeps the operation order of two
+// plane_vec_kernel sweeps (the first one scaled when gamma_in is set), so
+// the results are the same bits.  The running sums keep A(x - 1) + B(x - 2)
+// as one value, the first addition of plane_vec_kernel's A1 + B2 + b, and
+// both kernels round those additions one by one (add_rn).
+// MODE JJ_STORE stores u2 to out; JJ_UPD adds it into the update block as
+// OP_JACOBI_UPD does; JJ_RST stores it and restricts the second sweep's
+// residual into the next level's right-hand side as OP_JACOBI_RST does
+// (w on one more row and plane, kept in a four-plane ring).
+template <typename T, int LAP, int MODE, int S, int NG1, int NG2>
+__global__ void __launch_bounds__(256, 2) plane_jj_kernel(PlaneParams p, DevCoef<T> c)
+{
+    using V4             = typename Vec16<T>::type;
+    using VH             = Vec16<T>;
+    constexpr int VEC    = VH::N;
+    constexpr bool EDGES = (LAP == 0);
+    constexpr bool RST   = (MODE == JJ_RST);
+    constexpr bool UPD   = (MODE == JJ_UPD);
+    constexpr int YO     = RST ? 1 : 0;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+
+    const int nx = p.n[0], ny = p.n[1], nz = p.n[2];
+    const int TY      = p.ty;
+    const int rows2   = TY + YO;   // second sweep: rows y0 - YO .. y0 + TY - 1
+    const int rows1   = rows2 + 2; // first sweep: one row more on each side
+    const int rows_s  = rows1 + 2; // staged input
+    const int tile_y  = blockIdx.x % p.ntile_y;
+    const int tile_x  = blockIdx.x / p.ntile_y;
+    const int f       = blockIdx.y;
+    const int y0      = tile_y * TY;
+    const int x0      = tile_x * p.xc;
+    const int xcount  = min(p.xc, nx - x0);
+    const int nplanes = xcount + YO + 4; // staged planes x0 - YO - 2 .. x0 + xcount + 1
+    const bool scaled = (p.gamma_in != 0.);
+    const T gam       = (T)p.gamma_in;
+
+    const size_t stage_elems = (size_t)rows_s * nz;
+    const size_t u1_elems    = (size_t)rows1 * nz;
+    const size_t ring_elems  = RST ? (size_t)(TY + 1) * nz : 0;
+    T* stages      = reinterpret_cast<T*>(smem_raw);
+    T* u1buf       = stages + S * stage_elems;
+    T* wring       = u1buf + 2 * u1_elems;
+    uint64_t* bars = reinterpret_cast<uint64_t*>(wring + 4 * ring_elems);
+
+    const T* ubase = reinterpret_cast<const T*>(scaled ? p.f : p.u)
+                     + (size_t)f * (scaled ? p.ldf : p.ldu);
+    // the staged rows y0 - YO - 2 .. y0 + TY + 1 in at most two pieces
+    int ya = y0 - YO - 2, na, nb;
+    if (ya < 0)
+    {
+        na = -ya;
+        ya += ny;
+        nb = rows_s - na;
+    }
+    else if (ya + rows_s > ny)
+    {
+        na = ny - ya;
+        nb = rows_s - na;
+    }
+    else
+    {
+        na = rows_s;
+        nb = 0;
+    }
+    const uint32_t bytes = (uint32_t)(stage_elems * sizeof(T));
+    auto issue = [&](int i) {
+        const int slot = i % S;
+        const int x    = wrap(x0 - YO - 2 + i, nx);
+        uint64_t* bar  = bars + slot;
+        mbar_arrive_expect_tx(bar, bytes);
+        T* dst       = stages + slot * stage_elems;
+        const T* src = ubase + (size_t)x * ny * nz;
+        bulk_g2s(dst, src + (size_t)ya * nz, (uint32_t)(na * nz * sizeof(T)), bar);
+        if (nb > 0) bulk_g2s(dst + (size_t)na * nz, src, (uint32_t)(nb * nz * sizeof(T)), bar);
+    };
+
+    if (threadIdx.x == 0)
+    {
+        for (int s = 0; s < S; s++)
+            mbar_init(bars + s, 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    int issued = min(S, nplanes) - 1;
+    if (threadIdx.x == 0)
+        for (int i = 0; i <= issued; i++)
+            issue(i);
+
+    // groups of VEC points along z: the first sweep's on rows1 rows (centre
+    // in stage row r + 1, u1 row r), the second sweep's on rows2 rows
+    // (centre in u1 row r + 1)
+    const int gpr = nz / VEC;
+    int o1[NG1], m1[NG1], p1[NG1], g1[NG1];
+    bool ok1[NG1];
+#pragma unroll
+    for (int k = 0; k < NG1; k++)
+    {
+        const int g  = threadIdx.x + k * 256;
+        const int r  = g / gpr;
+        const int z0 = (g - r * gpr) * VEC;
+        ok1[k]       = g < rows1 * gpr;
+        o1[k]        = (r + 1) * nz + z0;
+        m1[k]        = (r + 1) * nz + (z0 > 0 ? z0 - 1 : nz - 1);
+        p1[k]        = (r + 1) * nz + (z0 + VEC < nz ? z0 + VEC : 0);
+        const int yr = y0 - YO - 1 + r;
+        g1[k]        = (yr < 0 ? yr + ny : (yr >= ny ? yr - ny : yr)) * nz + z0;
+    }
+    int o2[NG2], m2[NG2], p2[NG2], g2[NG2], r2[NG2];
+    bool ok2[NG2];
+#pragma unroll
+    for (int k = 0; k < NG2; k++)
+    {
+        const int g  = threadIdx.x + k * 256;
+        const int r  = g / gpr;
+        const int z0 = (g - r * gpr) * VEC;
+        ok2[k]       = g < rows2 * gpr;
+        r2[k]        = r;
+        o2[k]        = (r + 1) * nz + z0;
+        m2[k]        = (r + 1) * nz + (z0 > 0 ? z0 - 1 : nz - 1);
+        p2[k]        = (r + 1) * nz + (z0 + VEC < nz ? z0 + VEC : 0);
+        const int yr = y0 - YO + r;
+        g2[k]        = (yr < 0 ? yr + ny : yr) * nz + z0;
+    }
+    // running sums: P = A(x - 1) + B(x - 2), Q = B(x - 1), C = u(x - 1)
+    T P1[NG1][VEC], Q1[NG1][VEC], C1[NG1][VEC];
+    T P2[NG2][VEC], Q2[NG2][VEC], C2[NG2][VEC];
+#pragma unroll
+    for (int k = 0; k < NG1; k++)
+#pragma unroll
+        for (int v = 0; v < VEC; v++)
+            P1[k][v] = Q1[k][v] = C1[k][v] = (T)0;
+#pragma unroll
+    for (int k = 0; k < NG2; k++)
+#pragma unroll
+        for (int v = 0; v < VEC; v++)
+            P2[k][v] = Q2[k][v] = C2[k][v] = (T)0;
+
+    T* __restrict__ outp     = reinterpret_cast<T*>(p.out) + (size_t)f * p.ldo;
+    T* __restrict__ updp     = UPD ? reinterpret_cast<T*>(p.upd) + (size_t)f * p.ldupd : nullptr;
+    const T ualpha           = (T)p.upd_alpha;
+    const T uscale           = (UPD && p.upd_scale) ? (T)p.upd_scale[f] : (T)1;
+    const T* __restrict__ fp = reinterpret_cast<const T*>(p.f) + (size_t)f * p.ldf;
+
+    // in-plane part a and neighbour-plane part b of the operator at the
+    // group's VEC points (plane_vec_kernel's expressions)
+    auto terms = [&](const T* q, int oc, int om, int op, T (&a)[VEC], T (&b)[VEC], T (&u)[VEC]) {
+        const V4 c0v = *reinterpret_cast<const V4*>(q + oc);
+        const V4 cmv = *reinterpret_cast<const V4*>(q + oc - nz);
+        const V4 cpv = *reinterpret_cast<const V4*>(q + oc + nz);
+        const T zl = q[om], zr = q[op];
+        T ml = 0, mr = 0, pl = 0, pr = 0;
+        if (EDGES)
+        {
+            ml = q[om - nz];
+            mr = q[op - nz];
+            pl = q[om + nz];
+            pr = q[op + nz];
+        }
+#pragma unroll
+        for (int v = 0; v < VEC; v++)
+        {
+            const T uc  = VH::get(c0v, v);
+            const T uzm = v == 0 ? zl : VH::get(c0v, v - 1);
+            const T uzp = v == VEC - 1 ? zr : VH::get(c0v, v + 1);
+            const T uym = VH::get(cmv, v);
+            const T uyp = VH::get(cpv, v);
+            const T sz = uzm + uzp, sy = uym + uyp;
+            T aa       = c.c0 * uc + c.cz[0] * sz + c.cy[0] * sy;
+            T bb       = c.cx[0] * uc;
+            if (EDGES)
+            {
+                const T yml = v == 0 ? ml : VH::get(cmv, v - 1);
+                const T ymr = v == VEC - 1 ? mr : VH::get(cmv, v + 1);
+                const T ypl = v == 0 ? pl : VH::get(cpv, v - 1);
+                const T ypr = v == VEC - 1 ? pr : VH::get(cpv, v + 1);
+                aa += c.cyz * (yml + ymr + ypl + ypr);
+                bb += c.cxz * sz + c.cxy * sy;
+            }
+            a[v] = aa;
+            b[v] = bb;
+            u[v] = uc;
+        }
+    };
+
+    // OP_JACOBI_RST's restriction of the fine plane xe (odd from x0) and the
+    // two before it (plane_vec_kernel's restrict_plane)
+    auto restrict_plane = [&](const int xe) {
+        const int cy = ny >> 1, cz = nz >> 1;
+        const int X   = (xe - 1) >> 1;
+        const int nyc = TY >> 1;
+        const T* Wm   = wring + (size_t)((xe - x0 - 1) & 3) * ring_elems; // plane 2X - 1
+        const T* W0   = wring + (size_t)((xe - x0) & 3) * ring_elems;     // plane 2X
+        const T* Wp   = wring + (size_t)((xe - x0 + 1) & 3) * ring_elems; // plane 2X + 1
+        T* cp         = reinterpret_cast<T*>(p.coarse) + (size_t)f * p.ldc;
+        const int hz  = cz >> 1;
+        for (int t = threadIdx.x; t < nyc * hz; t += 256)
+        {
+            const int yl = t / hz, Z = 2 * (t - (t / hz) * hz);
+            const int z = 2 * Z, zm = z > 0 ? z - 1 : nz - 1;
+            const int r = 2 * yl + 1; // ring row of fine y = y0 + 2 yl
+            auto row = [&](const T* P, int dy, T* v6) {
+                const T* q = P + (size_t)(r + dy) * nz;
+                v6[0]      = q[zm];
+#pragma unroll
+                for (int h = 0; h < 4 / VEC; h++)
+                {
+                    const V4 cc = *reinterpret_cast<const V4*>(q + z + h * VEC);
+#pragma unroll
+                    for (int v = 0; v < VEC; v++)
+                        v6[1 + h * VEC + v] = VH::get(cc, v);
+                }
+            };
+            T r00[5], rp0[5], rm0[5], r0p[5], r0m[5], rpp[5], rpm[5], rmp[5], rmm[5];
+            row(W0, 0, r00);
+            row(Wp, 0, rp0);
+            row(Wm, 0, rm0);
+            row(W0, 1, r0p);
+            row(W0, -1, r0m);
+            row(Wp, 1, rpp);
+            row(Wp, -1, rpm);
+            row(Wm, 1, rmp);
+            row(Wm, -1, rmm);
+#pragma unroll
+            for (int c2 = 0; c2 < 2; c2++)
+            {
+                const int o    = 2 * c2;
+                const T face   = rp0[o + 1] + rm0[o + 1] + r0p[o + 1] + r0m[o + 1] + r00[o]
+                               + r00[o + 2];
+                const T corner = rpp[o] + rpp[o + 2] + rpm[o] + rpm[o + 2] + rmp[o] + rmp[o + 2]
+                                 + rmm[o] + rmm[o + 2];
+                const T edge   = r0p[o] + r0p[o + 2] + r0m[o] + r0m[o + 2] + rp0[o] + rp0[o + 2]
+                               + rm0[o] + rm0[o + 2] + rmm[o + 1] + rpm[o + 1] + rmp[o + 1]
+                               + rpp[o + 1];
+                cp[((size_t)X * cy + (y0 >> 1) + yl) * cz + Z + c2]
+                    = (T)(1. / 64.) * ((T)8. * r00[o + 1] + (T)4. * face + (T)2. * edge + corner);
+            }
+        }
+    };
+    int pend = -1; // the w plane whose restriction is due after the next barrier
+
+    bool ok    = true;
+    int waited = -1;
+    for (int i = 0; i < nplanes; i++)
+    {
+        const int xs     = x0 - YO - 2 + i; // staged plane
+        const bool emit1 = (i >= 2);        // u1 of plane xs - 1
+        const bool emit2 = (i >= 4);        // u2 of plane xs - 2
+        const int e2     = xs - 2;
+        const size_t xo1 = (size_t)(emit1 ? wrap(xs - 1, nx) : 0) * ny * nz;
+        const size_t xo2 = (size_t)(emit2 ? wrap(e2, nx) : 0) * ny * nz;
+        V4 fa[NG1], fb[NG2], ub[NG2];
+        if (emit1 && !scaled)
+        {
+#pragma unroll
+            for (int k = 0; k < NG1; k++)
+                if (ok1[k]) fa[k] = *reinterpret_cast<const V4*>(fp + xo1 + g1[k]);
+        }
+        if (emit2)
+        {
+#pragma unroll
+            for (int k = 0; k < NG2; k++)
+                if (ok2[k])
+                {
+                    fb[k] = *reinterpret_cast<const V4*>(fp + xo2 + g2[k]);
+                    if (UPD) ub[k] = *reinterpret_cast<const V4*>(updp + xo2 + g2[k]);
+                }
+        }
+        ok = ok && mbar_wait(bars + (i % S), (uint32_t)((i / S) & 1));
+        if (ok) waited = i;
+        const T* st = stages + (i % S) * stage_elems;
+        T* u1p      = u1buf + (size_t)(i & 1) * u1_elems;
+        // first sweep
+#pragma unroll
+        for (int k = 0; k < NG1; k++)
+        {
+            if (!ok1[k]) continue;
+            T a[VEC], b[VEC], u[VEC];
+            terms(st, o1[k], m1[k], p1[k], a, b, u);
+            V4 res;
+#pragma unroll
+            for (int v = 0; v < VEC; v++)
+            {
+                if (emit1)
+                {
+                    T lap  = add_rn(P1[k][v], b[v]);
+                    T ucen = C1[k][v];
+                    T fv;
+                    if (scaled)
+                    {
+                        fv   = ucen;
+                        lap  = gam * lap;
+                        ucen = gam * ucen;
+                    }
+                    else
+                        fv = VH::get(fa[k], v);
+                    const T w = lap - fv;
+                    VH::set(res, v, ucen - c.jf * w);
+                }
+                P1[k][v] = add_rn(a[v], Q1[k][v]);
+                Q1[k][v] = b[v];
+                C1[k][v] = u[v];
+            }
+            if (emit1) *reinterpret_cast<V4*>(u1p + o1[k] - nz) = res;
+        }
+        __syncthreads();
+        const int nxt = i + S;
+        if (nxt < nplanes && nxt > issued)
+        {
+            if (threadIdx.x == 0)
+            {
+                fence_proxy_async_smem();
+                issue(nxt);
+            }
+            issued = nxt;
+        }
+        if (RST && pend >= 0)
+        {
+            restrict_plane(pend);
+            pend = -1;
+        }
+        if (!emit1) continue;
+        // second sweep, folding the u1 plane xs - 1 written above
+#pragma unroll
+        for (int k = 0; k < NG2; k++)
+        {
+            if (!ok2[k]) continue;
+            T a[VEC], b[VEC], u[VEC];
+            terms(u1p, o2[k], m2[k], p2[k], a, b, u);
+            V4 res, wres;
+#pragma unroll
+            for (int v = 0; v < VEC; v++)
+            {
+                if (emit2)
+                {
+                    const T lap  = add_rn(P2[k][v], b[v]);
+                    const T ucen = C2[k][v];
+                    const T w    = lap - VH::get(fb[k], v);
+                    VH::set(res, v, ucen - c.jf * w);
+                    VH::set(wres, v, w);
+                }
+                P2[k][v] = add_rn(a[v], Q2[k][v]);
+                Q2[k][v] = b[v];
+                C2[k][v] = u[v];
+            }
+            if (!emit2) continue;
+            if (UPD)
+            {
+                V4 q = ub[k];
+#pragma unroll
+                for (int v = 0; v < VEC; v++)
+                    VH::set(q, v, uscale * (VH::get(q, v) + ualpha * VH::get(res, v)));
+                *reinterpret_cast<V4*>(updp + xo2 + g2[k]) = q;
+            }
+            else if (!RST || (r2[k] >= YO && e2 >= x0))
+                *reinterpret_cast<V4*>(outp + xo2 + g2[k]) = res;
+            if (RST)
+                *reinterpret_cast<V4*>(wring + (size_t)((e2 - x0 + 1) & 3) * ring_elems
+                                       + (size_t)(o2[k] - nz)) = wres;
+        }
+        if (RST && emit2 && e2 > x0 && ((e2 - x0) & 1)) pend = e2;
+    }
+    if (RST && pend >= 0)
+    {
+        __syncthreads();
+        restrict_plane(pend);
+    }
     if (!ok && threadIdx.x == 0)
     {
         if (p.err != nullptr) atomicExch(p.err, MGX_TIMEOUT);
@@ -1283,6 +1672,101 @@ int stencil_launch(int op, int lap_type, int dtype, int v_dtype,
         }
     }
     return fail(MGX_BAD_ARG, "stencil op %d invalid", op);
+}
+
+/* ------------------------------------------------------------------ */
+/* two Jacobi sweeps in one launch                                      */
+/* ------------------------------------------------------------------ */
+template <typename T, int LAP, int MODE>
+static int launch_jj(const PlaneParams& p0, const DevCoef<T>& c, int nfunc, cudaStream_t stream,
+    bool dry)
+{
+    constexpr int S   = 4;
+    constexpr int NG1 = 2;
+    constexpr int NG2 = 2;
+    constexpr int VEC = 16 / sizeof(T);
+    constexpr bool RST = (MODE == JJ_RST);
+    constexpr int YO   = RST ? 1 : 0;
+    PlaneParams p = p0;
+    const int nx = p.n[0], ny = p.n[1], nz = p.n[2];
+    if (p.mask.state != nullptr) return fail(MGX_UNSUPPORTED, "two-sweep kernel: masks");
+    const bool scaled = (p.gamma_in != 0.);
+    if (!p.f || (!scaled && !p.u) || (MODE == JJ_UPD ? !p.upd : !p.out) || (RST && !p.coarse))
+        return fail(MGX_BAD_ARG, "two-sweep kernel: null block");
+    if (MODE != JJ_UPD && (p.out == p.u || p.out == p.f))
+        return fail(MGX_BAD_ARG, "two-sweep kernel: out aliases its input");
+    auto al = [](const void* q, size_t ld) {
+        return q == nullptr || (((uintptr_t)q % 16) == 0 && (ld * sizeof(T)) % 16 == 0);
+    };
+    if ((nz * sizeof(T)) % 16 || !al(p.u, p.ldu) || !al(p.f, p.ldf) || !al(p.out, p.ldo)
+        || !al(p.upd, p.ldupd))
+        return fail(MGX_UNSUPPORTED, "two-sweep kernel: unaligned block");
+    if (RST && (((nx | ny) & 1) || (nz % 4)))
+        return fail(MGX_UNSUPPORTED, "the fused restriction needs even x, y and z % 4 == 0");
+    if (nx < 3) return fail(MGX_UNSUPPORTED, "two-sweep kernel: nx < 3");
+    const int gpr = nz / VEC;
+    auto smem_for = [&](int t) {
+        return (size_t)S * (t + YO + 4) * nz * sizeof(T) + 2 * (size_t)(t + YO + 2) * nz * sizeof(T)
+               + (RST ? 4 * (size_t)(t + 1) * nz * sizeof(T) : 0) + S * 8;
+    };
+    // rows per tile: the first sweep's TY + YO + 2 rows and the second's
+    // TY + YO within the threads' groups, TY dividing ny (even with the
+    // restriction), the staged rows within the grid, ~110 KB of shared memory
+    int ty = std::min(NG1 * 256 / gpr - YO - 2, NG2 * 256 / gpr - YO);
+    ty     = std::min(ty, ny - YO - 4);
+    for (; ty >= 1; ty--)
+        if (ny % ty == 0 && (!RST || ty % 2 == 0) && smem_for(ty) <= 110 * 1024) break;
+    if (ty < 1) return fail(MGX_UNSUPPORTED, "two-sweep kernel: no tile height fits");
+    if (dry) return MGX_OK;
+    p.ty      = ty;
+    p.ntile_y = ny / ty;
+    int xc    = 32;
+    while (xc > 4 && (size_t)p.ntile_y * ((nx + xc - 1) / xc) * nfunc < 4 * 152)
+        xc /= 2;
+    if (xc > nx) xc = nx;
+    p.xc      = xc;
+    p.ntile_x = (nx + xc - 1) / xc;
+    const size_t smem = smem_for(ty);
+    auto kern         = plane_jj_kernel<T, LAP, MODE, S, NG1, NG2>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return cuda_check(e, "plane_jj_kernel smem attribute");
+    dim3 grid(p.ntile_y * p.ntile_x, nfunc);
+    kern<<<grid, 256, smem, stream>>>(p, c);
+    MGX_LAUNCH_CHECK("plane_jj_kernel");
+    return MGX_OK;
+}
+
+template <typename T, int LAP>
+static int jj_mode(int mode, const PlaneParams& p, const DevCoef<T>& c, int nfunc, cudaStream_t s,
+    bool dry)
+{
+    switch (mode)
+    {
+        case JJ_STORE: return launch_jj<T, LAP, JJ_STORE>(p, c, nfunc, s, dry);
+        case JJ_UPD: return launch_jj<T, LAP, JJ_UPD>(p, c, nfunc, s, dry);
+        case JJ_RST: return launch_jj<T, LAP, JJ_RST>(p, c, nfunc, s, dry);
+    }
+    return fail(MGX_BAD_ARG, "two-sweep mode %d", mode);
+}
+
+int jacobi2_launch(int mode, int lap_type, int dtype, const PlaneParams& p, const Level& L,
+    double jf, int nfunc, cudaStream_t s, bool dry)
+{
+    if (nfunc <= 0) return MGX_OK;
+    if (nfunc > 65535) return fail(MGX_BAD_ARG, "nfunc %d > 65535 per launch", nfunc);
+    if (lap_type != 0 && lap_type != 1)
+        return fail(MGX_UNSUPPORTED, "two-sweep kernel: radius-1 operators only");
+    const StencilCoeffs sc = stencil_coeffs(lap_type, L.h);
+    if (dtype == MGX_F64)
+    {
+        const DevCoef<double> c = to_dev<double>(sc, jf);
+        return lap_type == 0 ? jj_mode<double, 0>(mode, p, c, nfunc, s, dry)
+                             : jj_mode<double, 1>(mode, p, c, nfunc, s, dry);
+    }
+    if (dtype != MGX_F32) return fail(MGX_BAD_ARG, "two-sweep kernel: dtype %d", dtype);
+    const DevCoef<float> c = to_dev<float>(sc, jf);
+    return lap_type == 0 ? jj_mode<float, 0>(mode, p, c, nfunc, s, dry)
+                         : jj_mode<float, 1>(mode, p, c, nfunc, s, dry);
 }
 
 /* ------------------------------------------------------------------ */

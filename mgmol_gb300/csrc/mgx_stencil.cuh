@@ -96,6 +96,24 @@ int stencil_launch(int op, int lap_type, int dtype, int v_dtype,
     const PlaneParams& p, const Level& L, double jf, int nfunc,
     cudaStream_t stream, int force_direct = 0);
 
+/* Two consecutive Jacobi sweeps of one level in one kernel, the first
+ * sweep's iterate kept on chip.  p as for OP_JACOBI, out not aliasing u
+ * or f; gamma_in set: the first sweep starts from gamma_in f (u unused).
+ * JJ_STORE stores the second iterate to out; JJ_UPD adds it into p.upd as
+ * OP_JACOBI_UPD does (out unused); JJ_RST stores it and restricts the
+ * second sweep's residual into p.coarse as OP_JACOBI_RST does.  Radius-1
+ * operators (lap_type 0 and 1), no masks.  The same bits as two separate
+ * sweeps.  MGX_UNSUPPORTED, with nothing launched, when the kernel cannot
+ * run the block; dry: only that check. */
+enum Jacobi2Mode
+{
+    JJ_STORE = 0,
+    JJ_UPD   = 1,
+    JJ_RST   = 2
+};
+int jacobi2_launch(int mode, int lap_type, int dtype, const PlaneParams& p, const Level& L,
+    double jf, int nfunc, cudaStream_t s, bool dry = false);
+
 /* out = B u (the Mehrstellen right-hand-side operator) for nfunc ghost-free
  * functions of grid level 0; u and out with leading dimensions ldu, ldo. */
 int rhs_block(const mgx_grid& g, int dtype, const void* u, size_t ldu, void* out,

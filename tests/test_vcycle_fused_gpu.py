@@ -1,10 +1,13 @@
 """The V-cycle with the residual of each level's second pre-sweep
 restricted inside that sweep's kernel (the default) against the V-cycle
 with the residual stored and restricted by its own kernel
-(MGX_FUSED_RESTRICT=0), and the FP32 prolongation with four z points per
+(MGX_FUSED_RESTRICT=0), the V-cycle with both pre-sweeps and both
+post-sweeps of a level each in one kernel against single sweeps
+(MGX_TWO_SWEEPS=0), and the FP32 prolongation with four z points per
 thread against the pair form (MGX_PROLONG4=0), each in a fresh process
 (the library reads the choice once): the same bits, FP64 and FP32, on
-grids whose tile rows and x chunks end unevenly; and the fused FP64
+grids whose tile rows and x chunks end unevenly, plain, warm-started, in
+chunks and with the update fused into the last sweep; and the fused FP64
 V-cycle against the oracle."""
 import os
 import subprocess
@@ -32,9 +35,19 @@ for n, nf, maxl in (((32, 28, 36), 5, 2), ((48, 40, 24), 3, 1), ((64, 64, 64), 4
     res, _, _ = synth.gaussian_orbitals(n, ll, nf, 61)
     ctx = capi.Context(n, ll)
     for dt in (torch.float64, torch.float32):
-        for lap in (0, 2):
-            o = ctx.precond_mg(torch.from_numpy(res).to(dtype=dt, device="cuda"), lap, maxl, 0.3)
+        for lap in (0, 1, 2):
+            rin = torch.from_numpy(res).to(dtype=dt, device="cuda")
+            o = ctx.precond_mg(rin, lap, maxl, 0.3)
             outs[f"{n}_{dt}_{lap}"] = o.cpu().numpy()
+            # a warm start (the first sweep from the iterate out holds)
+            outs[f"warm_{n}_{dt}_{lap}"] = ctx.precond_mg_warm(rin, o.clone(), lap, maxl).cpu().numpy()
+            # chunks of two functions
+            outs[f"chunk_{n}_{dt}_{lap}"] = ctx.precond_mg(rin, lap, maxl, 0.3, chunk=2).cpu().numpy()
+            # the update fused into the last sweep, with the column scale
+            psi = torch.flip(rin, (0,)).contiguous()
+            sc = torch.linspace(0.5, 1.5, nf, dtype=torch.float64, device="cuda")
+            ctx.precond_update(rin, psi, -0.3, lap, maxl, 0.3, psi_scale=sc)
+            outs[f"upd_{n}_{dt}_{lap}"] = psi.cpu().numpy()
     ref = O.precond(n, ll, 0, maxl, 0.3, res)
     got = outs[f"{n}_{torch.float64}_0"]
     assert np.max(np.abs(got - ref)) / np.max(np.abs(ref)) < 1e-12, n
@@ -62,6 +75,14 @@ def test_fused_restriction_gives_the_same_bits(tmp_path):
 def test_prolongation_four_wide_gives_the_same_bits(tmp_path):
     a = _run(tmp_path, {"MGX_PROLONG4": "1"}, "four")
     b = _run(tmp_path, {"MGX_PROLONG4": "0"}, "pair")
+    assert sorted(a.files) == sorted(b.files)
+    for k in a.files:
+        assert np.array_equal(a[k], b[k]), k
+
+
+def test_paired_sweeps_give_the_same_bits(tmp_path):
+    a = _run(tmp_path, {"MGX_TWO_SWEEPS": "1"}, "pairs")
+    b = _run(tmp_path, {"MGX_TWO_SWEEPS": "0"}, "single")
     assert sorted(a.files) == sorted(b.files)
     for k in a.files:
         assert np.array_equal(a[k], b[k]), k
