@@ -852,14 +852,45 @@ static bool fused_restrict()
     return on;
 }
 
-/* Both pre-sweeps of a level in one kernel and both post-sweeps in another
- * (jacobi2_launch: the first sweep's iterate stays on chip) unless
- * MGX_TWO_SWEEPS=0.  The results are the same bits either way. */
+/* Both post-sweeps of a level in one kernel, and both pre-sweeps where the
+ * pair pays (jacobi2_launch: the first sweep's iterate stays on chip),
+ * unless MGX_TWO_SWEEPS=0.  The results are the same bits either way. */
 static bool two_sweeps()
 {
     static const bool on = [] {
         const char* e = getenv("MGX_TWO_SWEEPS");
         return !(e && e[0] == '0');
+    }();
+    return on;
+}
+
+/* The pre-sweep pair forms its first sweep on two more rows than the tile
+ * and its second sweep's residual on one more, so it re-does more work the
+ * lower the tile: it runs when the tile holds at least JJ_PAIR_MIN_ROWS
+ * rows (at most a quarter more first-sweep rows).  On 192^3 FP32 a
+ * 256-thread tile holds 6 rows and the pair ran 23.2 ms per 512 orbitals
+ * against 20.7 ms for the two single kernels; a 512-thread tile holds 16
+ * and it ran 19.6 ms.  MGX_PRE_PAIR=1 runs it whenever the kernel can, 0
+ * never. */
+static int pre_pair_policy()
+{
+    static const int v = [] {
+        const char* e = getenv("MGX_PRE_PAIR");
+        return e ? (e[0] == '0' ? 0 : 1) : -1;
+    }();
+    return v;
+}
+
+/* The post-sweep pair starts from u - P e formed on chip (the coarse-grid
+ * correction folded into it, JJ_PRO) when MGX_PAIR_PROLONG=1; by default the
+ * prolongation kernel runs first, since the folded form's coarse loads sit
+ * before every plane's barrier and made the V-cycle 36 % slower.  The same
+ * bits either way. */
+static bool pair_prolong()
+{
+    static const bool on = [] {
+        const char* e = getenv("MGX_PAIR_PROLONG");
+        return e && e[0] == '1';
     }();
     return on;
 }
@@ -963,9 +994,10 @@ struct VCycle
 
     // both sweeps of a level's pre-smoothing (pre: the second one's
     // residual restricted into f[l + 1]) or post-smoothing (the last one
-    // with the fused update at level 0) in one kernel, from buffer cur into
-    // the other one; dry: only whether the kernel runs the block
-    int jacobi2(int l, int cur, bool pre, bool dry)
+    // with the fused update at level 0; pro: from u - P pro, pro the next
+    // level's correction) in one kernel, from buffer cur into the other
+    // one; dry: only whether the kernel runs the block
+    int jacobi2(int l, int cur, bool pre, bool dry, const void* pro = nullptr, int* ty = nullptr)
     {
         PlaneParams p;
         p.u   = cur ? v1[l] : v0[l];
@@ -999,8 +1031,14 @@ struct VCycle
             p.upd_scale = upd_scale0;
             mode        = JJ_UPD;
         }
+        if (!pre && pro)
+        {
+            p.pro   = pro;
+            p.ldpro = ld[l + 1];
+            mode |= JJ_PRO;
+        }
         const int st = jacobi2_launch(mode, l == 0 ? lap_type : 1, dtype, p, lev[l], jf[l], nf, s,
-            dry);
+            dry, ty);
         if (!dry && pre && st == MGX_OK && l == 0) pending_scale = false;
         return st;
     }
@@ -1011,13 +1049,29 @@ struct VCycle
         int cur         = 0;
         const int ncycl = (l == L) ? 4 : 2;
         bool restricted = false;
-        // the paired sweeps move the iterate to the other buffer once per
-        // pair where two single sweeps move it twice, so a level runs both
-        // pairs or neither and ends in the same buffer either way
-        const bool pairs = l < L && two_sweeps() && masks == nullptr && fused_restrict()
-                           && jacobi2(l, cur, true, true) == MGX_OK
-                           && jacobi2(l, cur ^ 1, false, true) == MGX_OK;
-        if (pairs)
+        const bool can  = l < L && two_sweeps() && masks == nullptr;
+        int ty_pre      = 0;
+        bool pre_pair   = can && fused_restrict() && pre_pair_policy() != 0
+                        && jacobi2(l, 0, true, true, nullptr, &ty_pre) == MGX_OK
+                        && (pre_pair_policy() == 1 || ty_pre >= JJ_PAIR_MIN_ROWS);
+        bool post_pair = can && jacobi2(l, 1, false, true) == MGX_OK;
+        // a pair moves the iterate to the other buffer once where two single
+        // sweeps move it twice.  Level 0 must end in buffer 0 (the caller's
+        // block): with an odd count the first sweep, which reads only f when
+        // it starts from gamma f, writes into buffer 0 instead of 1; a warm
+        // start reads buffer 0, so it runs both pairs or neither
+        if (l == 0 && ((pre_pair ? 1 : 2) + (post_pair ? 1 : 2)) % 2)
+        {
+            if (pending_scale)
+                cur = 1;
+            else
+                pre_pair = post_pair = false;
+        }
+        // the correction folded into the post-sweep pair (checked with a
+        // stand-in block: the coarse result's buffer is known only later)
+        const bool pair_pro = post_pair && pair_prolong()
+                              && jacobi2(l, cur ^ 1, false, true, v0[l + 1]) == MGX_OK;
+        if (pre_pair)
         {
             const int st = jacobi2(l, cur, true, false);
             if (st != MGX_OK) return -st - 1;
@@ -1045,10 +1099,16 @@ struct VCycle
         if (st != MGX_OK) return -st - 1;
         const int c1 = mg(l + 1);
         if (c1 < 0) return c1;
+        if (pair_pro)
+        {
+            st = jacobi2(l, cur, false, false, c1 ? v1[l + 1] : v0[l + 1]);
+            if (st != MGX_OK) return -st - 1;
+            return cur ^ 1;
+        }
         st = prolong_launch(dtype, 1, lev[l], c1 ? v1[l + 1] : v0[l + 1],
             ld[l + 1], cur ? v1[l] : v0[l], ld[l], nf, mask_slice(masks, l, f0), s);
         if (st != MGX_OK) return -st - 1;
-        if (pairs)
+        if (post_pair)
         {
             st = jacobi2(l, cur, false, false);
             if (st != MGX_OK) return -st - 1;

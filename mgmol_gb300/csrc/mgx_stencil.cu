@@ -585,6 +585,10 @@ struct Vec16<double>
     }
 };
 
+template <typename T> struct Vec8;
+template <> struct Vec8<float> { using type = float2; };
+template <> struct Vec8<double> { using type = double2; };
+
 template <typename T, int LAP, int OP, int S, int NG>
 __global__ void __launch_bounds__(256, 2) plane_vec_kernel(PlaneParams p, DevCoef<T> c)
 {
@@ -999,15 +1003,17 @@ __global__ void __launch_bounds__(256, 2) plane_vec_kernel(PlaneParams p, DevCoe
 // OP_JACOBI_UPD does; JJ_RST stores it and restricts the second sweep's
 // residual into the next level's right-hand side as OP_JACOBI_RST does
 // (w on one more row and plane, kept in a four-plane ring).
-template <typename T, int LAP, int MODE, int S, int NG1, int NG2>
-__global__ void __launch_bounds__(256, 2) plane_jj_kernel(PlaneParams p, DevCoef<T> c)
+template <typename T, int LAP, int MODE, int S, int NG1, int NG2, int NT>
+__global__ void __launch_bounds__(NT, 512 / NT) plane_jj_kernel(PlaneParams p, DevCoef<T> c)
 {
     using V4             = typename Vec16<T>::type;
     using VH             = Vec16<T>;
+    using T2             = typename Vec8<T>::type;
     constexpr int VEC    = VH::N;
     constexpr bool EDGES = (LAP == 0);
-    constexpr bool RST   = (MODE == JJ_RST);
-    constexpr bool UPD   = (MODE == JJ_UPD);
+    constexpr bool PRO   = (MODE & JJ_PRO) != 0;
+    constexpr bool RST   = ((MODE & 3) == JJ_RST);
+    constexpr bool UPD   = ((MODE & 3) == JJ_UPD);
     constexpr int YO     = RST ? 1 : 0;
     extern __shared__ __align__(128) unsigned char smem_raw[];
 
@@ -1087,7 +1093,7 @@ __global__ void __launch_bounds__(256, 2) plane_jj_kernel(PlaneParams p, DevCoef
 #pragma unroll
     for (int k = 0; k < NG1; k++)
     {
-        const int g  = threadIdx.x + k * 256;
+        const int g  = threadIdx.x + k * NT;
         const int r  = g / gpr;
         const int z0 = (g - r * gpr) * VEC;
         ok1[k]       = g < rows1 * gpr;
@@ -1102,7 +1108,7 @@ __global__ void __launch_bounds__(256, 2) plane_jj_kernel(PlaneParams p, DevCoef
 #pragma unroll
     for (int k = 0; k < NG2; k++)
     {
-        const int g  = threadIdx.x + k * 256;
+        const int g  = threadIdx.x + k * NT;
         const int r  = g / gpr;
         const int z0 = (g - r * gpr) * VEC;
         ok2[k]       = g < rows2 * gpr;
@@ -1113,6 +1119,8 @@ __global__ void __launch_bounds__(256, 2) plane_jj_kernel(PlaneParams p, DevCoef
         const int yr = y0 - YO + r;
         g2[k]        = (yr < 0 ? yr + ny : yr) * nz + z0;
     }
+    bool ok    = true;
+    int waited = -1;
     // running sums: P = A(x - 1) + B(x - 2), Q = B(x - 1), C = u(x - 1)
     T P1[NG1][VEC], Q1[NG1][VEC], C1[NG1][VEC];
     T P2[NG2][VEC], Q2[NG2][VEC], C2[NG2][VEC];
@@ -1132,6 +1140,73 @@ __global__ void __launch_bounds__(256, 2) plane_jj_kernel(PlaneParams p, DevCoef
     const T ualpha           = (T)p.upd_alpha;
     const T uscale           = (UPD && p.upd_scale) ? (T)p.upd_scale[f] : (T)1;
     const T* __restrict__ fp = reinterpret_cast<const T*>(p.f) + (size_t)f * p.ldf;
+
+    // JJ_PRO: the staged plane i becomes u - P e before the first sweep
+    // reads it; each thread takes fine z pairs (2k, 2k + 1) of the staged
+    // rows, with prolong_kernel's arithmetic for every point
+    const T* __restrict__ ep = PRO ? reinterpret_cast<const T*>(p.pro) + (size_t)f * p.ldpro : nullptr;
+    auto correct = [&](int i) {
+        const int cx = nx >> 1, cy = ny >> 1, cz = nz >> 1;
+        const int x  = wrap(x0 - YO - 2 + i, nx);
+        const int ic = x >> 1, a = x & 1, i1 = ic + 1 < cx ? ic + 1 : 0;
+        T* stp       = stages + (size_t)(i % S) * stage_elems;
+        for (int t = threadIdx.x; t < rows_s * cz; t += NT)
+        {
+            const int rs = t / cz, k = t - rs * cz;
+            int y        = y0 - YO - 2 + rs;
+            y            = y < 0 ? y + ny : (y >= ny ? y - ny : y);
+            const int j = y >> 1, b = y & 1, j1 = j + 1 < cy ? j + 1 : 0;
+            const int k1 = k + 1 < cz ? k + 1 : 0;
+            const T* c00 = ep + ((size_t)ic * cy + j) * cz;
+            const T a0 = c00[k], a1 = c00[k1];
+            T v0, v1;
+            if (!a)
+            {
+                if (!b)
+                {
+                    v0 = a0;
+                    v1 = (T)0.5 * (a0 + a1);
+                }
+                else
+                {
+                    const T* c01 = ep + ((size_t)ic * cy + j1) * cz;
+                    const T b0 = c01[k], b1 = c01[k1];
+                    v0 = (T)0.5 * (b0 + a0);
+                    v1 = (T)0.25 * (b1 + a1 + b0 + a0);
+                }
+            }
+            else
+            {
+                const T* c10 = ep + ((size_t)i1 * cy + j) * cz;
+                const T d0 = c10[k], d1 = c10[k1];
+                if (!b)
+                {
+                    v0 = (T)0.5 * (d0 + a0);
+                    v1 = (T)0.25 * (d1 + d0 + a1 + a0);
+                }
+                else
+                {
+                    const T* c01 = ep + ((size_t)ic * cy + j1) * cz;
+                    const T* c11 = ep + ((size_t)i1 * cy + j1) * cz;
+                    const T b0 = c01[k], b1 = c01[k1], g0 = c11[k], g1 = c11[k1];
+                    v0 = (T)0.25 * (g0 + d0 + b0 + a0);
+                    v1 = (T)0.125 * (g1 + g0 + d1 + d0 + b1 + b0 + a1 + a0);
+                }
+            }
+            T2* q = reinterpret_cast<T2*>(stp + (size_t)rs * nz + 2 * k);
+            T2 uu = *q;
+            uu.x  = uu.x - v0;
+            uu.y  = uu.y - v1;
+            *q    = uu;
+        }
+    };
+    if (PRO)
+    {
+        ok = mbar_wait(bars, 0u);
+        if (ok) waited = 0;
+        if (ok) correct(0);
+        __syncthreads();
+    }
 
     // in-plane part a and neighbour-plane part b of the operator at the
     // group's VEC points (plane_vec_kernel's expressions)
@@ -1185,7 +1260,7 @@ __global__ void __launch_bounds__(256, 2) plane_jj_kernel(PlaneParams p, DevCoef
         const T* Wp   = wring + (size_t)((xe - x0 + 1) & 3) * ring_elems; // plane 2X + 1
         T* cp         = reinterpret_cast<T*>(p.coarse) + (size_t)f * p.ldc;
         const int hz  = cz >> 1;
-        for (int t = threadIdx.x; t < nyc * hz; t += 256)
+        for (int t = threadIdx.x; t < nyc * hz; t += NT)
         {
             const int yl = t / hz, Z = 2 * (t - (t / hz) * hz);
             const int z = 2 * Z, zm = z > 0 ? z - 1 : nz - 1;
@@ -1230,8 +1305,6 @@ __global__ void __launch_bounds__(256, 2) plane_jj_kernel(PlaneParams p, DevCoef
     };
     int pend = -1; // the w plane whose restriction is due after the next barrier
 
-    bool ok    = true;
-    int waited = -1;
     for (int i = 0; i < nplanes; i++)
     {
         const int xs     = x0 - YO - 2 + i; // staged plane
@@ -1247,8 +1320,10 @@ __global__ void __launch_bounds__(256, 2) plane_jj_kernel(PlaneParams p, DevCoef
             for (int k = 0; k < NG1; k++)
                 if (ok1[k]) fa[k] = *reinterpret_cast<const V4*>(fp + xo1 + g1[k]);
         }
-        if (emit2)
-        {
+        // the second sweep's f (and update block), fetched here or, with
+        // JJ_PRO, after the correction (fewer values live across it)
+        auto fetch2 = [&]() {
+            if (!emit2) return;
 #pragma unroll
             for (int k = 0; k < NG2; k++)
                 if (ok2[k])
@@ -1256,7 +1331,8 @@ __global__ void __launch_bounds__(256, 2) plane_jj_kernel(PlaneParams p, DevCoef
                     fb[k] = *reinterpret_cast<const V4*>(fp + xo2 + g2[k]);
                     if (UPD) ub[k] = *reinterpret_cast<const V4*>(updp + xo2 + g2[k]);
                 }
-        }
+        };
+        if (!PRO) fetch2();
         ok = ok && mbar_wait(bars + (i % S), (uint32_t)((i / S) & 1));
         if (ok) waited = i;
         const T* st = stages + (i % S) * stage_elems;
@@ -1293,6 +1369,16 @@ __global__ void __launch_bounds__(256, 2) plane_jj_kernel(PlaneParams p, DevCoef
                 C1[k][v] = u[v];
             }
             if (emit1) *reinterpret_cast<V4*>(u1p + o1[k] - nz) = res;
+        }
+        // JJ_PRO: the next staged plane, read after the barrier below
+        if (PRO)
+        {
+            if (i + 1 < nplanes)
+            {
+                ok = ok && mbar_wait(bars + ((i + 1) % S), (uint32_t)(((i + 1) / S) & 1));
+                if (ok) correct(i + 1);
+            }
+            fetch2();
         }
         __syncthreads();
         const int nxt = i + S;
@@ -1677,24 +1763,46 @@ int stencil_launch(int op, int lap_type, int dtype, int v_dtype,
 /* ------------------------------------------------------------------ */
 /* two Jacobi sweeps in one launch                                      */
 /* ------------------------------------------------------------------ */
-template <typename T, int LAP, int MODE>
-static int launch_jj(const PlaneParams& p0, const DevCoef<T>& c, int nfunc, cudaStream_t stream,
-    bool dry)
+/* Threads per block of the two-sweep kernel: 256 (two blocks per SM), or
+ * 512 (one block per SM, tiles twice as high, so less of the first sweep
+ * is re-done on the halo rows) for the pre-sweep pair when 256 threads
+ * cannot hold JJ_PAIR_MIN_ROWS rows.  On 192^3 FP32 that pair ran 19.6 ms
+ * per 512 orbitals with 512 threads (16 rows) against 23.2 ms with 256 (6
+ * rows); the post-sweep pair ran 15.6 against 14.3 ms, so it keeps 256.
+ * MGX_JJ_THREADS=256 or 512 sets every launch. */
+static int jj_threads()
+{
+    static const int v = [] {
+        const char* e = getenv("MGX_JJ_THREADS");
+        const int n   = e ? atoi(e) : 0;
+        return (n == 256 || n == 512) ? n : 0;
+    }();
+    return v;
+}
+
+template <typename T, int LAP, int MODE, int NT>
+static int launch_jj_nt(const PlaneParams& p0, const DevCoef<T>& c, int nfunc, cudaStream_t stream,
+    bool dry, int* tile_rows)
 {
     constexpr int S   = 4;
     constexpr int NG1 = 2;
     constexpr int NG2 = 2;
     constexpr int VEC = 16 / sizeof(T);
-    constexpr bool RST = (MODE == JJ_RST);
+    constexpr bool RST = ((MODE & 3) == JJ_RST);
+    constexpr bool UPD = ((MODE & 3) == JJ_UPD);
+    constexpr bool PRO = (MODE & JJ_PRO) != 0;
     constexpr int YO   = RST ? 1 : 0;
     PlaneParams p = p0;
     const int nx = p.n[0], ny = p.n[1], nz = p.n[2];
     if (p.mask.state != nullptr) return fail(MGX_UNSUPPORTED, "two-sweep kernel: masks");
     const bool scaled = (p.gamma_in != 0.);
-    if (!p.f || (!scaled && !p.u) || (MODE == JJ_UPD ? !p.upd : !p.out) || (RST && !p.coarse))
+    if (!p.f || (!scaled && !p.u) || (UPD ? !p.upd : !p.out) || (RST && !p.coarse)
+        || (PRO && (!p.pro || scaled)))
         return fail(MGX_BAD_ARG, "two-sweep kernel: null block");
-    if (MODE != JJ_UPD && (p.out == p.u || p.out == p.f))
+    if (!UPD && (p.out == p.u || p.out == p.f))
         return fail(MGX_BAD_ARG, "two-sweep kernel: out aliases its input");
+    if (PRO && ((nx | ny | nz) & 1))
+        return fail(MGX_UNSUPPORTED, "the folded prolongation needs even dimensions");
     auto al = [](const void* q, size_t ld) {
         return q == nullptr || (((uintptr_t)q % 16) == 0 && (ld * sizeof(T)) % 16 == 0);
     };
@@ -1711,12 +1819,15 @@ static int launch_jj(const PlaneParams& p0, const DevCoef<T>& c, int nfunc, cuda
     };
     // rows per tile: the first sweep's TY + YO + 2 rows and the second's
     // TY + YO within the threads' groups, TY dividing ny (even with the
-    // restriction), the staged rows within the grid, ~110 KB of shared memory
-    int ty = std::min(NG1 * 256 / gpr - YO - 2, NG2 * 256 / gpr - YO);
+    // restriction), the staged rows within the grid, shared memory within
+    // ~110 KB per block (220 KB for one 512-thread block per SM)
+    const size_t smem_cap = NT == 512 ? 220 * 1024 : 110 * 1024;
+    int ty = std::min(NG1 * NT / gpr - YO - 2, NG2 * NT / gpr - YO);
     ty     = std::min(ty, ny - YO - 4);
     for (; ty >= 1; ty--)
-        if (ny % ty == 0 && (!RST || ty % 2 == 0) && smem_for(ty) <= 110 * 1024) break;
+        if (ny % ty == 0 && (!RST || ty % 2 == 0) && smem_for(ty) <= smem_cap) break;
     if (ty < 1) return fail(MGX_UNSUPPORTED, "two-sweep kernel: no tile height fits");
+    if (tile_rows) *tile_rows = ty;
     if (dry) return MGX_OK;
     p.ty      = ty;
     p.ntile_y = ny / ty;
@@ -1727,30 +1838,50 @@ static int launch_jj(const PlaneParams& p0, const DevCoef<T>& c, int nfunc, cuda
     p.xc      = xc;
     p.ntile_x = (nx + xc - 1) / xc;
     const size_t smem = smem_for(ty);
-    auto kern         = plane_jj_kernel<T, LAP, MODE, S, NG1, NG2>;
+    auto kern         = plane_jj_kernel<T, LAP, MODE, S, NG1, NG2, NT>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return cuda_check(e, "plane_jj_kernel smem attribute");
     dim3 grid(p.ntile_y * p.ntile_x, nfunc);
-    kern<<<grid, 256, smem, stream>>>(p, c);
+    kern<<<grid, NT, smem, stream>>>(p, c);
     MGX_LAUNCH_CHECK("plane_jj_kernel");
     return MGX_OK;
 }
 
+template <typename T, int LAP, int MODE>
+static int launch_jj(const PlaneParams& p, const DevCoef<T>& c, int nfunc, cudaStream_t stream,
+    bool dry, int* tile_rows)
+{
+    int nt = jj_threads();
+    if (nt == 0)
+    {
+        nt = 256;
+        int ty = 0;
+        if ((MODE & 3) == JJ_RST
+            && launch_jj_nt<T, LAP, MODE, 256>(p, c, nfunc, stream, true, &ty) == MGX_OK
+            && ty < JJ_PAIR_MIN_ROWS)
+            nt = 512;
+    }
+    if (nt == 512) return launch_jj_nt<T, LAP, MODE, 512>(p, c, nfunc, stream, dry, tile_rows);
+    return launch_jj_nt<T, LAP, MODE, 256>(p, c, nfunc, stream, dry, tile_rows);
+}
+
 template <typename T, int LAP>
 static int jj_mode(int mode, const PlaneParams& p, const DevCoef<T>& c, int nfunc, cudaStream_t s,
-    bool dry)
+    bool dry, int* ty)
 {
     switch (mode)
     {
-        case JJ_STORE: return launch_jj<T, LAP, JJ_STORE>(p, c, nfunc, s, dry);
-        case JJ_UPD: return launch_jj<T, LAP, JJ_UPD>(p, c, nfunc, s, dry);
-        case JJ_RST: return launch_jj<T, LAP, JJ_RST>(p, c, nfunc, s, dry);
+        case JJ_STORE: return launch_jj<T, LAP, JJ_STORE>(p, c, nfunc, s, dry, ty);
+        case JJ_UPD: return launch_jj<T, LAP, JJ_UPD>(p, c, nfunc, s, dry, ty);
+        case JJ_RST: return launch_jj<T, LAP, JJ_RST>(p, c, nfunc, s, dry, ty);
+        case JJ_STORE | JJ_PRO: return launch_jj<T, LAP, JJ_STORE | JJ_PRO>(p, c, nfunc, s, dry, ty);
+        case JJ_UPD | JJ_PRO: return launch_jj<T, LAP, JJ_UPD | JJ_PRO>(p, c, nfunc, s, dry, ty);
     }
     return fail(MGX_BAD_ARG, "two-sweep mode %d", mode);
 }
 
 int jacobi2_launch(int mode, int lap_type, int dtype, const PlaneParams& p, const Level& L,
-    double jf, int nfunc, cudaStream_t s, bool dry)
+    double jf, int nfunc, cudaStream_t s, bool dry, int* tile_rows)
 {
     if (nfunc <= 0) return MGX_OK;
     if (nfunc > 65535) return fail(MGX_BAD_ARG, "nfunc %d > 65535 per launch", nfunc);
@@ -1760,13 +1891,13 @@ int jacobi2_launch(int mode, int lap_type, int dtype, const PlaneParams& p, cons
     if (dtype == MGX_F64)
     {
         const DevCoef<double> c = to_dev<double>(sc, jf);
-        return lap_type == 0 ? jj_mode<double, 0>(mode, p, c, nfunc, s, dry)
-                             : jj_mode<double, 1>(mode, p, c, nfunc, s, dry);
+        return lap_type == 0 ? jj_mode<double, 0>(mode, p, c, nfunc, s, dry, tile_rows)
+                             : jj_mode<double, 1>(mode, p, c, nfunc, s, dry, tile_rows);
     }
     if (dtype != MGX_F32) return fail(MGX_BAD_ARG, "two-sweep kernel: dtype %d", dtype);
     const DevCoef<float> c = to_dev<float>(sc, jf);
-    return lap_type == 0 ? jj_mode<float, 0>(mode, p, c, nfunc, s, dry)
-                         : jj_mode<float, 1>(mode, p, c, nfunc, s, dry);
+    return lap_type == 0 ? jj_mode<float, 0>(mode, p, c, nfunc, s, dry, tile_rows)
+                         : jj_mode<float, 1>(mode, p, c, nfunc, s, dry, tile_rows);
 }
 
 /* ------------------------------------------------------------------ */

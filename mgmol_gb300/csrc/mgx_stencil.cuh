@@ -90,6 +90,12 @@ struct PlaneParams
     // ldc); no masks
     void* coarse = nullptr;
     size_t ldc   = 0;
+    // jacobi2_launch with JJ_PRO only: the input is u - P e, e the next
+    // level's correction (n/2 points per direction, leading dimension
+    // ldpro) prolonged as prolong_kernel does, formed on chip (the
+    // coarse-grid correction of the V-cycle folded into its post-sweeps)
+    const void* pro = nullptr;
+    size_t ldpro    = 0;
 };
 
 int stencil_launch(int op, int lap_type, int dtype, int v_dtype,
@@ -101,18 +107,27 @@ int stencil_launch(int op, int lap_type, int dtype, int v_dtype,
  * or f; gamma_in set: the first sweep starts from gamma_in f (u unused).
  * JJ_STORE stores the second iterate to out; JJ_UPD adds it into p.upd as
  * OP_JACOBI_UPD does (out unused); JJ_RST stores it and restricts the
- * second sweep's residual into p.coarse as OP_JACOBI_RST does.  Radius-1
- * operators (lap_type 0 and 1), no masks.  The same bits as two separate
- * sweeps.  MGX_UNSUPPORTED, with nothing launched, when the kernel cannot
- * run the block; dry: only that check. */
+ * second sweep's residual into p.coarse as OP_JACOBI_RST does.  JJ_PRO
+ * added to JJ_STORE or JJ_UPD: the sweeps start from u - P p.pro (the
+ * prolongation of prolong_launch, mode 1).  Radius-1 operators (lap_type
+ * 0 and 1), no masks.  The same bits as the separate kernels.
+ * MGX_UNSUPPORTED, with nothing launched, when the kernel cannot run the
+ * block; dry: only that check.  tile_rows, when given, receives the tile
+ * height (output rows per block; the first sweep also forms YO + 2 more,
+ * YO = 1 with the restriction). */
+/* The pre-sweep pair (JJ_RST) pays only on tiles of at least this many
+ * rows: lower tiles re-do too much of the first sweep on their halo rows. */
+constexpr int JJ_PAIR_MIN_ROWS = 12;
+
 enum Jacobi2Mode
 {
     JJ_STORE = 0,
     JJ_UPD   = 1,
-    JJ_RST   = 2
+    JJ_RST   = 2,
+    JJ_PRO   = 4
 };
 int jacobi2_launch(int mode, int lap_type, int dtype, const PlaneParams& p, const Level& L,
-    double jf, int nfunc, cudaStream_t s, bool dry = false);
+    double jf, int nfunc, cudaStream_t s, bool dry = false, int* tile_rows = nullptr);
 
 /* out = B u (the Mehrstellen right-hand-side operator) for nfunc ghost-free
  * functions of grid level 0; u and out with leading dimensions ldu, ldo. */

@@ -3,7 +3,10 @@ restricted inside that sweep's kernel (the default) against the V-cycle
 with the residual stored and restricted by its own kernel
 (MGX_FUSED_RESTRICT=0), the V-cycle with both pre-sweeps and both
 post-sweeps of a level each in one kernel against single sweeps
-(MGX_TWO_SWEEPS=0), and the FP32 prolongation with four z points per
+(MGX_TWO_SWEEPS=0; the pre-sweep pair where it pays, everywhere it runs,
+and nowhere; blocks of 256 and 512 threads), the post-sweep pair starting from the coarse-grid correction
+formed on chip (MGX_PAIR_PROLONG=1) against the prolongation kernel, and
+the FP32 prolongation with four z points per
 thread against the pair form (MGX_PROLONG4=0), each in a fresh process
 (the library reads the choice once): the same bits, FP64 and FP32, on
 grids whose tile rows and x chunks end unevenly, plain, warm-started, in
@@ -80,9 +83,24 @@ def test_prolongation_four_wide_gives_the_same_bits(tmp_path):
         assert np.array_equal(a[k], b[k]), k
 
 
-def test_paired_sweeps_give_the_same_bits(tmp_path):
-    a = _run(tmp_path, {"MGX_TWO_SWEEPS": "1"}, "pairs")
+@pytest.mark.parametrize("pre_pair,threads", [("auto", "auto"), ("1", "256"), ("0", "auto"),
+                                              ("1", "512")])
+def test_paired_sweeps_give_the_same_bits(tmp_path, pre_pair, threads):
+    env = {"MGX_TWO_SWEEPS": "1"}
+    if threads != "auto":
+        env["MGX_JJ_THREADS"] = threads
+    if pre_pair != "auto":
+        env["MGX_PRE_PAIR"] = pre_pair
+    a = _run(tmp_path, env, "pairs")
     b = _run(tmp_path, {"MGX_TWO_SWEEPS": "0"}, "single")
+    assert sorted(a.files) == sorted(b.files)
+    for k in a.files:
+        assert np.array_equal(a[k], b[k]), k
+
+
+def test_folded_prolongation_gives_the_same_bits(tmp_path):
+    a = _run(tmp_path, {"MGX_PAIR_PROLONG": "1"}, "folded")
+    b = _run(tmp_path, {"MGX_PAIR_PROLONG": "0"}, "kernel")
     assert sorted(a.files) == sorted(b.files)
     for k in a.files:
         assert np.array_equal(a[k], b[k]), k
