@@ -883,9 +883,9 @@ static int pre_pair_policy()
 
 /* The post-sweep pair starts from u - P e formed on chip (the coarse-grid
  * correction folded into it, JJ_PRO) when MGX_PAIR_PROLONG=1; by default the
- * prolongation kernel runs first, since the folded form's coarse loads sit
- * before every plane's barrier and made the V-cycle 36 % slower.  The same
- * bits either way. */
+ * prolongation kernel runs first: the folded correction runs between the
+ * planes' barriers and made the V-cycle of 512 orbitals on 192^3 16 %
+ * slower (52.0 against 44.9 ms).  The same bits either way. */
 static bool pair_prolong()
 {
     static const bool on = [] {

@@ -585,6 +585,8 @@ struct Vec16<double>
     }
 };
 
+constexpr int JJ_CS = 4; // coarse-plane slots of the folded prolongation
+
 template <typename T> struct Vec8;
 template <> struct Vec8<float> { using type = float2; };
 template <> struct Vec8<double> { using type = double2; };
@@ -1035,10 +1037,19 @@ __global__ void __launch_bounds__(NT, 512 / NT) plane_jj_kernel(PlaneParams p, D
     const size_t stage_elems = (size_t)rows_s * nz;
     const size_t u1_elems    = (size_t)rows1 * nz;
     const size_t ring_elems  = RST ? (size_t)(TY + 1) * nz : 0;
+    // JJ_PRO: coarse rows jlo .. jlo + CROWS - 1 of the correction e, one
+    // coarse plane per slot of a JJ_CS-slot ring; coarse plane q (from
+    // (x0 - 2) / 2) rides on the mbarrier of fine stage 0 (q = 0) or
+    // 2q - 1, and fine stage i reads planes i / 2 and, odd, i / 2 + 1
+    const int cz         = nz >> 1;
+    const int crows      = PRO ? (TY + 7) / 2 : 0;
+    const int jlo        = (y0 - 2) >> 1;
+    const size_t c_elems = (size_t)crows * cz;
     T* stages      = reinterpret_cast<T*>(smem_raw);
     T* u1buf       = stages + S * stage_elems;
     T* wring       = u1buf + 2 * u1_elems;
-    uint64_t* bars = reinterpret_cast<uint64_t*>(wring + 4 * ring_elems);
+    T* cring       = wring + 4 * ring_elems;
+    uint64_t* bars = reinterpret_cast<uint64_t*>(cring + JJ_CS * c_elems);
 
     const T* ubase = reinterpret_cast<const T*>(scaled ? p.f : p.u)
                      + (size_t)f * (scaled ? p.ldf : p.ldu);
@@ -1061,15 +1072,35 @@ __global__ void __launch_bounds__(NT, 512 / NT) plane_jj_kernel(PlaneParams p, D
         nb = 0;
     }
     const uint32_t bytes = (uint32_t)(stage_elems * sizeof(T));
+    // JJ_PRO: the coarse rows in at most two pieces
+    const int cy = ny >> 1, cx = nx >> 1;
+    int cja = jlo < 0 ? jlo + cy : jlo, cna = crows, cnb = 0;
+    if (PRO && cja + crows > cy)
+    {
+        cna = cy - cja;
+        cnb = crows - cna;
+    }
+    const T* epb = PRO ? reinterpret_cast<const T*>(p.pro) + (size_t)f * p.ldpro : nullptr;
     auto issue = [&](int i) {
         const int slot = i % S;
         const int x    = wrap(x0 - YO - 2 + i, nx);
         uint64_t* bar  = bars + slot;
-        mbar_arrive_expect_tx(bar, bytes);
+        const bool cpl = PRO && (i == 0 || (i & 1));
+        mbar_arrive_expect_tx(bar, bytes + (cpl ? (uint32_t)(c_elems * sizeof(T)) : 0u));
         T* dst       = stages + slot * stage_elems;
         const T* src = ubase + (size_t)x * ny * nz;
         bulk_g2s(dst, src + (size_t)ya * nz, (uint32_t)(na * nz * sizeof(T)), bar);
         if (nb > 0) bulk_g2s(dst + (size_t)na * nz, src, (uint32_t)(nb * nz * sizeof(T)), bar);
+        if (cpl)
+        {
+            const int q  = (i + 1) >> 1;
+            const int xc = wrap(((x0 - 2) >> 1) + q, cx);
+            T* cdst       = cring + (size_t)(q % JJ_CS) * c_elems;
+            const T* csrc = epb + (size_t)xc * cy * cz;
+            bulk_g2s(cdst, csrc + (size_t)cja * cz, (uint32_t)(cna * cz * sizeof(T)), bar);
+            if (cnb > 0)
+                bulk_g2s(cdst + (size_t)cna * cz, csrc, (uint32_t)(cnb * cz * sizeof(T)), bar);
+        }
     };
 
     if (threadIdx.x == 0)
@@ -1144,20 +1175,20 @@ __global__ void __launch_bounds__(NT, 512 / NT) plane_jj_kernel(PlaneParams p, D
     // JJ_PRO: the staged plane i becomes u - P e before the first sweep
     // reads it; each thread takes fine z pairs (2k, 2k + 1) of the staged
     // rows, with prolong_kernel's arithmetic for every point
-    const T* __restrict__ ep = PRO ? reinterpret_cast<const T*>(p.pro) + (size_t)f * p.ldpro : nullptr;
+    // the staged coarse rows of fine stage i: plane i / 2 (and i / 2 + 1);
+    // fine row y0 - 2 + rs reads coarse rows jr and jr + 1 of them
     auto correct = [&](int i) {
-        const int cx = nx >> 1, cy = ny >> 1, cz = nz >> 1;
-        const int x  = wrap(x0 - YO - 2 + i, nx);
-        const int ic = x >> 1, a = x & 1, i1 = ic + 1 < cx ? ic + 1 : 0;
-        T* stp       = stages + (size_t)(i % S) * stage_elems;
+        const int a = i & 1; // parity of the fine plane (x0 is even)
+        const T* ca = cring + (size_t)((i >> 1) % JJ_CS) * c_elems;
+        const T* cb = cring + (size_t)(((i >> 1) + 1) % JJ_CS) * c_elems;
+        T* stp      = stages + (size_t)(i % S) * stage_elems;
         for (int t = threadIdx.x; t < rows_s * cz; t += NT)
         {
             const int rs = t / cz, k = t - rs * cz;
-            int y        = y0 - YO - 2 + rs;
-            y            = y < 0 ? y + ny : (y >= ny ? y - ny : y);
-            const int j = y >> 1, b = y & 1, j1 = j + 1 < cy ? j + 1 : 0;
+            const int yu = y0 - 2 + rs;
+            const int jr = (yu >> 1) - jlo, b = yu & 1;
             const int k1 = k + 1 < cz ? k + 1 : 0;
-            const T* c00 = ep + ((size_t)ic * cy + j) * cz;
+            const T* c00 = ca + (size_t)jr * cz;
             const T a0 = c00[k], a1 = c00[k1];
             T v0, v1;
             if (!a)
@@ -1169,7 +1200,7 @@ __global__ void __launch_bounds__(NT, 512 / NT) plane_jj_kernel(PlaneParams p, D
                 }
                 else
                 {
-                    const T* c01 = ep + ((size_t)ic * cy + j1) * cz;
+                    const T* c01 = c00 + cz;
                     const T b0 = c01[k], b1 = c01[k1];
                     v0 = (T)0.5 * (b0 + a0);
                     v1 = (T)0.25 * (b1 + a1 + b0 + a0);
@@ -1177,7 +1208,7 @@ __global__ void __launch_bounds__(NT, 512 / NT) plane_jj_kernel(PlaneParams p, D
             }
             else
             {
-                const T* c10 = ep + ((size_t)i1 * cy + j) * cz;
+                const T* c10 = cb + (size_t)jr * cz;
                 const T d0 = c10[k], d1 = c10[k1];
                 if (!b)
                 {
@@ -1186,8 +1217,8 @@ __global__ void __launch_bounds__(NT, 512 / NT) plane_jj_kernel(PlaneParams p, D
                 }
                 else
                 {
-                    const T* c01 = ep + ((size_t)ic * cy + j1) * cz;
-                    const T* c11 = ep + ((size_t)i1 * cy + j1) * cz;
+                    const T* c01 = c00 + cz;
+                    const T* c11 = c10 + cz;
                     const T b0 = c01[k], b1 = c01[k1], g0 = c11[k], g1 = c11[k1];
                     v0 = (T)0.25 * (g0 + d0 + b0 + a0);
                     v1 = (T)0.125 * (g1 + g0 + d1 + d0 + b1 + b0 + a1 + a0);
@@ -1252,7 +1283,6 @@ __global__ void __launch_bounds__(NT, 512 / NT) plane_jj_kernel(PlaneParams p, D
     // OP_JACOBI_RST's restriction of the fine plane xe (odd from x0) and the
     // two before it (plane_vec_kernel's restrict_plane)
     auto restrict_plane = [&](const int xe) {
-        const int cy = ny >> 1, cz = nz >> 1;
         const int X   = (xe - 1) >> 1;
         const int nyc = TY >> 1;
         const T* Wm   = wring + (size_t)((xe - x0 - 1) & 3) * ring_elems; // plane 2X - 1
@@ -1260,7 +1290,8 @@ __global__ void __launch_bounds__(NT, 512 / NT) plane_jj_kernel(PlaneParams p, D
         const T* Wp   = wring + (size_t)((xe - x0 + 1) & 3) * ring_elems; // plane 2X + 1
         T* cp         = reinterpret_cast<T*>(p.coarse) + (size_t)f * p.ldc;
         const int hz  = cz >> 1;
-        for (int t = threadIdx.x; t < nyc * hz; t += NT)
+        // from the last threads, which hold one second-sweep group fewer
+        for (int t = NT - 1 - threadIdx.x; t < nyc * hz; t += NT)
         {
             const int yl = t / hz, Z = 2 * (t - (t / hz) * hz);
             const int z = 2 * Z, zm = z > 0 ? z - 1 : nz - 1;
@@ -1813,9 +1844,13 @@ static int launch_jj_nt(const PlaneParams& p0, const DevCoef<T>& c, int nfunc, c
         return fail(MGX_UNSUPPORTED, "the fused restriction needs even x, y and z % 4 == 0");
     if (nx < 3) return fail(MGX_UNSUPPORTED, "two-sweep kernel: nx < 3");
     const int gpr = nz / VEC;
+    if (PRO
+        && (((nz / 2) * sizeof(T)) % 16 || ((uintptr_t)p.pro % 16) || (p.ldpro * sizeof(T)) % 16))
+        return fail(MGX_UNSUPPORTED, "the folded prolongation needs 16-byte coarse rows");
     auto smem_for = [&](int t) {
         return (size_t)S * (t + YO + 4) * nz * sizeof(T) + 2 * (size_t)(t + YO + 2) * nz * sizeof(T)
-               + (RST ? 4 * (size_t)(t + 1) * nz * sizeof(T) : 0) + S * 8;
+               + (RST ? 4 * (size_t)(t + 1) * nz * sizeof(T) : 0)
+               + (PRO ? (size_t)JJ_CS * ((t + 7) / 2) * (nz / 2) * sizeof(T) : 0) + S * 8;
     };
     // rows per tile: the first sweep's TY + YO + 2 rows and the second's
     // TY + YO within the threads' groups, TY dividing ny (even with the
@@ -1825,7 +1860,9 @@ static int launch_jj_nt(const PlaneParams& p0, const DevCoef<T>& c, int nfunc, c
     int ty = std::min(NG1 * NT / gpr - YO - 2, NG2 * NT / gpr - YO);
     ty     = std::min(ty, ny - YO - 4);
     for (; ty >= 1; ty--)
-        if (ny % ty == 0 && (!RST || ty % 2 == 0) && smem_for(ty) <= smem_cap) break;
+        if (ny % ty == 0 && (!RST || ty % 2 == 0) && (!PRO || (ty + 7) / 2 <= ny / 2)
+            && smem_for(ty) <= smem_cap)
+            break;
     if (ty < 1) return fail(MGX_UNSUPPORTED, "two-sweep kernel: no tile height fits");
     if (tile_rows) *tile_rows = ty;
     if (dry) return MGX_OK;
