@@ -155,11 +155,19 @@ DevCoef<T> to_dev(const StencilCoeffs& c, double jf)
     return d;
 }
 
-/* a + b rounded once and never fused with a product that feeds it, so
- * that the operator's running sums over x planes (A(x - 1) + B(x - 2) +
- * B(x)) get the same bits in every kernel that forms them */
+/* Operations rounded once each, that the compiler may neither fuse nor
+ * split: the stencil kernels that must give the same bits as one another
+ * (single and paired sweeps) form every sum and product of a point with
+ * these, since whether a plain a * b + c becomes one FMA depends on the
+ * code around it. */
 __device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }
 __device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ float sub_rn(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ double sub_rn(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float fma_rn(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ double fma_rn(double a, double b, double c) { return __fma_rn(a, b, c); }
 
 __device__ __forceinline__ int wrap(int i, int n)
 {
@@ -587,6 +595,73 @@ struct Vec16<double>
 
 constexpr int JJ_CS = 4; // coarse-plane slots of the folded prolongation
 
+/* In-plane part a and neighbour-plane part b of a radius-1 operator at the
+ * VEC points of a group along z: centre row c0v with its z neighbours zl /
+ * zr, rows y - 1 / y + 1 cmv / cpv and, for the Mehrstellen edges (EDGES),
+ * their z neighbours ml, mr / pl, pr.  The y sum of each z column is formed
+ * once and serves the column's own term and the edge terms of the columns
+ * beside it.  Every stencil kernel that must give the same bits as another
+ * forms a and b here. */
+template <typename T, typename VH, bool EDGES>
+__device__ __forceinline__ void vec_terms(const DevCoef<T>& c, const typename VH::type& c0v,
+    const typename VH::type& cmv, const typename VH::type& cpv, T zl, T zr, T ml, T mr, T pl,
+    T pr, T* a, T* b, T* u)
+{
+    constexpr int VEC = VH::N;
+    T sy[VEC + 2];
+#pragma unroll
+    for (int v = 0; v < VEC; v++)
+        sy[v + 1] = add_rn(VH::get(cmv, v), VH::get(cpv, v));
+    if (EDGES)
+    {
+        sy[0]       = add_rn(ml, pl);
+        sy[VEC + 1] = add_rn(mr, pr);
+    }
+#pragma unroll
+    for (int v = 0; v < VEC; v++)
+    {
+        const T uc  = VH::get(c0v, v);
+        const T uzm = v == 0 ? zl : VH::get(c0v, v - 1);
+        const T uzp = v == VEC - 1 ? zr : VH::get(c0v, v + 1);
+        const T sz  = add_rn(uzm, uzp);
+        T aa        = fma_rn(c.cy[0], sy[v + 1], fma_rn(c.cz[0], sz, mul_rn(c.c0, uc)));
+        T bb;
+        if (EDGES)
+        {
+            aa = fma_rn(c.cyz, add_rn(sy[v], sy[v + 2]), aa);
+            bb = fma_rn(c.cxy, sy[v + 1], fma_rn(c.cxz, sz, mul_rn(c.cx[0], uc)));
+        }
+        else
+            bb = mul_rn(c.cx[0], uc);
+        a[v] = aa;
+        b[v] = bb;
+        u[v] = uc;
+    }
+}
+
+/* One Jacobi point: w = lap - f and the result ucen - jf w; scaled (the
+ * first sweep from gamma f, with the staged f as input): lap and ucen are
+ * gamma times the staged operator and centre, f the staged centre. */
+template <typename T>
+__device__ __forceinline__ T jacobi_point(T lap, T ucen, T fv, T jf, bool scaled, T gam, T& w)
+{
+    if (scaled)
+    {
+        fv   = ucen;
+        lap  = mul_rn(gam, lap);
+        ucen = mul_rn(gam, ucen);
+    }
+    w = sub_rn(lap, fv);
+    return fma_rn(-jf, w, ucen);
+}
+
+/* The ABPG update of one point: scale (q + alpha r). */
+template <typename T>
+__device__ __forceinline__ T update_point(T q, T r, T alpha, T scale)
+{
+    return mul_rn(scale, fma_rn(alpha, r, q));
+}
+
 template <typename T> struct Vec8;
 template <> struct Vec8<float> { using type = float2; };
 template <> struct Vec8<double> { using type = double2; };
@@ -862,6 +937,8 @@ __global__ void __launch_bounds__(256, 2) plane_vec_kernel(PlaneParams p, DevCoe
             }
             V4 res;
             V4 wres;
+            T ta[VEC], tb[VEC], tu[VEC];
+            if (!is_rhs_op(OP)) vec_terms<T, VH, EDGES>(c, c0v, cmv, cpv, zl, zr, ml, mr, pl, pr, ta, tb, tu);
 #pragma unroll
             for (int v = 0; v < VEC; v++)
             {
@@ -878,18 +955,8 @@ __global__ void __launch_bounds__(256, 2) plane_vec_kernel(PlaneParams p, DevCoe
                 }
                 else
                 {
-                    const T sz = uzm + uzp, sy = uym + uyp;
-                    a          = c.c0 * u + c.cz[0] * sz + c.cy[0] * sy;
-                    b          = c.cx[0] * u;
-                    if (EDGES)
-                    {
-                        const T yml = v == 0 ? ml : VH::get(cmv, v - 1);
-                        const T ymr = v == VEC - 1 ? mr : VH::get(cmv, v + 1);
-                        const T ypl = v == 0 ? pl : VH::get(cpv, v - 1);
-                        const T ypr = v == VEC - 1 ? pr : VH::get(cpv, v + 1);
-                        a += c.cyz * (yml + ymr + ypl + ypr);
-                        b += c.cxz * sz + c.cxy * sy;
-                    }
+                    a = ta[v];
+                    b = tb[v];
                     if (STAGE_V)
                     {
                         const T vc  = VH::get(vcv, v);
@@ -911,18 +978,10 @@ __global__ void __launch_bounds__(256, 2) plane_vec_kernel(PlaneParams p, DevCoe
                     if (OP == OP_RHS_SUB) r = lap - VH::get(pv[k], v);
                     if (is_jacobi(OP))
                     {
-                        T fv;
-                        if (scaled)
-                        {
-                            // staged f: u = gamma f, -Lap u = gamma (-Lap f)
-                            fv   = ucen;
-                            lap  = gam * lap;
-                            ucen = gam * ucen;
-                        }
-                        else
-                            fv = VH::get(pv[k], v);
-                        T w = lap - fv;
-                        r   = ucen - c.jf * w;
+                        // scaled: staged f, u = gamma f, -Lap u = gamma (-Lap f)
+                        T w;
+                        r = jacobi_point<T>(lap, ucen, scaled ? (T)0 : VH::get(pv[k], v), c.jf,
+                            scaled, gam, w);
                         if (p.mask.state != nullptr)
                         {
                             const int y = y0 + gy[k], z = gz[k] + v;
@@ -947,7 +1006,7 @@ __global__ void __launch_bounds__(256, 2) plane_vec_kernel(PlaneParams p, DevCoe
                     V4 q = uv[k];
 #pragma unroll
                     for (int v = 0; v < VEC; v++)
-                        VH::set(q, v, uscale * (VH::get(q, v) + ualpha * VH::get(res, v)));
+                        VH::set(q, v, update_point<T>(VH::get(q, v), VH::get(res, v), ualpha, uscale));
                     *reinterpret_cast<V4*>(updp + xoff + goff[k]) = q;
                 }
                 else if (OP == OP_RHS_SPLIT)
@@ -1240,7 +1299,7 @@ __global__ void __launch_bounds__(NT, 512 / NT) plane_jj_kernel(PlaneParams p, D
     }
 
     // in-plane part a and neighbour-plane part b of the operator at the
-    // group's VEC points (plane_vec_kernel's expressions)
+    // group's VEC points (vec_terms, as in plane_vec_kernel)
     auto terms = [&](const T* q, int oc, int om, int op, T (&a)[VEC], T (&b)[VEC], T (&u)[VEC]) {
         const V4 c0v = *reinterpret_cast<const V4*>(q + oc);
         const V4 cmv = *reinterpret_cast<const V4*>(q + oc - nz);
@@ -1254,30 +1313,7 @@ __global__ void __launch_bounds__(NT, 512 / NT) plane_jj_kernel(PlaneParams p, D
             pl = q[om + nz];
             pr = q[op + nz];
         }
-#pragma unroll
-        for (int v = 0; v < VEC; v++)
-        {
-            const T uc  = VH::get(c0v, v);
-            const T uzm = v == 0 ? zl : VH::get(c0v, v - 1);
-            const T uzp = v == VEC - 1 ? zr : VH::get(c0v, v + 1);
-            const T uym = VH::get(cmv, v);
-            const T uyp = VH::get(cpv, v);
-            const T sz = uzm + uzp, sy = uym + uyp;
-            T aa       = c.c0 * uc + c.cz[0] * sz + c.cy[0] * sy;
-            T bb       = c.cx[0] * uc;
-            if (EDGES)
-            {
-                const T yml = v == 0 ? ml : VH::get(cmv, v - 1);
-                const T ymr = v == VEC - 1 ? mr : VH::get(cmv, v + 1);
-                const T ypl = v == 0 ? pl : VH::get(cpv, v - 1);
-                const T ypr = v == VEC - 1 ? pr : VH::get(cpv, v + 1);
-                aa += c.cyz * (yml + ymr + ypl + ypr);
-                bb += c.cxz * sz + c.cxy * sy;
-            }
-            a[v] = aa;
-            b[v] = bb;
-            u[v] = uc;
-        }
+        vec_terms<T, VH, EDGES>(c, c0v, cmv, cpv, zl, zr, ml, mr, pl, pr, a, b, u);
     };
 
     // OP_JACOBI_RST's restriction of the fine plane xe (odd from x0) and the
@@ -1381,19 +1417,9 @@ __global__ void __launch_bounds__(NT, 512 / NT) plane_jj_kernel(PlaneParams p, D
             {
                 if (emit1)
                 {
-                    T lap  = add_rn(P1[k][v], b[v]);
-                    T ucen = C1[k][v];
-                    T fv;
-                    if (scaled)
-                    {
-                        fv   = ucen;
-                        lap  = gam * lap;
-                        ucen = gam * ucen;
-                    }
-                    else
-                        fv = VH::get(fa[k], v);
-                    const T w = lap - fv;
-                    VH::set(res, v, ucen - c.jf * w);
+                    T w;
+                    VH::set(res, v, jacobi_point<T>(add_rn(P1[k][v], b[v]), C1[k][v],
+                                        scaled ? (T)0 : VH::get(fa[k], v), c.jf, scaled, gam, w));
                 }
                 P1[k][v] = add_rn(a[v], Q1[k][v]);
                 Q1[k][v] = b[v];
@@ -1441,10 +1467,9 @@ __global__ void __launch_bounds__(NT, 512 / NT) plane_jj_kernel(PlaneParams p, D
             {
                 if (emit2)
                 {
-                    const T lap  = add_rn(P2[k][v], b[v]);
-                    const T ucen = C2[k][v];
-                    const T w    = lap - VH::get(fb[k], v);
-                    VH::set(res, v, ucen - c.jf * w);
+                    T w;
+                    VH::set(res, v, jacobi_point<T>(add_rn(P2[k][v], b[v]), C2[k][v],
+                                        VH::get(fb[k], v), c.jf, false, (T)0, w));
                     VH::set(wres, v, w);
                 }
                 P2[k][v] = add_rn(a[v], Q2[k][v]);
@@ -1457,7 +1482,7 @@ __global__ void __launch_bounds__(NT, 512 / NT) plane_jj_kernel(PlaneParams p, D
                 V4 q = ub[k];
 #pragma unroll
                 for (int v = 0; v < VEC; v++)
-                    VH::set(q, v, uscale * (VH::get(q, v) + ualpha * VH::get(res, v)));
+                    VH::set(q, v, update_point<T>(VH::get(q, v), VH::get(res, v), ualpha, uscale));
                 *reinterpret_cast<V4*>(updp + xo2 + g2[k]) = q;
             }
             else if (!RST || (r2[k] >= YO && e2 >= x0))
