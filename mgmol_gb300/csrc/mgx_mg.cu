@@ -1049,7 +1049,21 @@ struct VCycle
         int cur         = 0;
         const int ncycl = (l == L) ? 4 : 2;
         bool restricted = false;
-        const bool can  = l < L && two_sweeps() && masks == nullptr;
+        // the coarsest level's four sweeps as two pairs (an even count of
+        // buffer moves either way); level 0 without coarse levels keeps its
+        // single sweeps, whose last one may carry the update
+        if (l == L && l > 0 && two_sweeps() && masks == nullptr
+            && jacobi2(l, 0, false, true) == MGX_OK)
+        {
+            for (int it = 0; it < 2; it++)
+            {
+                const int st = jacobi2(l, cur, false, false);
+                if (st != MGX_OK) return -st - 1;
+                cur ^= 1;
+            }
+            return cur;
+        }
+        const bool can = l < L && two_sweeps() && masks == nullptr;
         int ty_pre      = 0;
         bool pre_pair   = can && fused_restrict() && pre_pair_policy() != 0
                         && jacobi2(l, 0, true, true, nullptr, &ty_pre) == MGX_OK
