@@ -1059,7 +1059,8 @@ __global__ void __launch_bounds__(256, 2) plane_vec_kernel(PlaneParams p, DevCoe
 // plane_vec_kernel sweeps (the first one scaled when gamma_in is set), so
 // the results are the same bits.  The running sums keep A(x - 1) + B(x - 2)
 // as one value, the first addition of plane_vec_kernel's A1 + B2 + b, and
-// both kernels round those additions one by one (add_rn).
+// both kernels form every sum and product of a point with explicitly
+// rounded operations (vec_terms, jacobi_point, update_point, add_rn).
 // MODE JJ_STORE stores u2 to out; JJ_UPD adds it into the update block as
 // OP_JACOBI_UPD does; JJ_RST stores it and restricts the second sweep's
 // residual into the next level's right-hand side as OP_JACOBI_RST does
